@@ -1,0 +1,190 @@
+/*
+ * korg_gb300.h -- C ABI of the GB300 (sm_103a) spectral-synthesis hot path.
+ *
+ * The entry points replace, one for one, the Julia functions of Korg.jl (v1.2.1) on the
+ * synthesis hot path.  Each declaration names the reference function it stands in for.  The
+ * ABI uses plain pointers and sizes only; every call returns a korg_status and never aborts.
+ *
+ * Layout conventions (identical to Korg):
+ *   - wavelengths in cm, increasing;
+ *   - alpha is a layers x wavelengths matrix stored column-major (layer index fastest):
+ *     alpha[j * L + l] for wavelength j and layer l;
+ *   - the line list is sorted by wavelength and given as a structure of arrays.
+ *
+ * Two families of calls:
+ *   - host-pointer calls (korg_line_absorption, korg_synthesize, ...) take ordinary host
+ *     arrays, copy them to the device, run, copy results back and return when done.  These
+ *     are what a Julia `ccall` or Python `ctypes` binding uses as a drop-in for the reference.
+ *   - `_dev` calls take device pointers (including the arrays inside the structs) and a
+ *     CUDA stream, enqueue the work and return without synchronising.
+ *
+ * Precision: KORG_FP64 evaluates everything in FP64 (the plain form).  KORG_MIXED evaluates
+ * line profiles in FP32 with Kahan-compensated accumulation, and keeps FP64 for the
+ * wavelength offsets from line centres (rounded to FP32 afterwards), the per-layer line
+ * strengths (Boltzmann factors, n/U), the optical-depth integration and the formal solution.
+ */
+#ifndef KORG_GB300_H
+#define KORG_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KORG_API __attribute__((visibility("default")))
+
+typedef enum {
+    KORG_OK = 0,
+    KORG_EINVAL = 1,   /* bad argument (sizes, null pointers, unsorted input, bad scheme) */
+    KORG_ECUDA = 2,    /* a CUDA runtime call failed; korg_last_error() has the message */
+    KORG_ENOMEM = 3,   /* device allocation failed */
+    KORG_ENOTABLES = 4 /* hydrogen lines requested before korg_set_stark_tables() */
+} korg_status;
+
+enum { KORG_FP64 = 0, KORG_MIXED = 1 };
+
+/* Line list (Korg.Line, src/linelist.jl:5-14), sorted by wl. */
+typedef struct {
+    int64_t n;
+    const double *wl;          /* cm */
+    const double *log_gf;
+    const double *E_lower;     /* eV */
+    const double *gamma_rad;   /* s^-1 */
+    const double *gamma_stark; /* s^-1, per perturber at 10,000 K */
+    const double *vdW1;        /* gamma_vdW at 10,000 K (vdW2 == -1) or ABO sigma (cm^2) */
+    const double *vdW2;        /* -1 or ABO alpha */
+    const double *mass;        /* g, get_mass(species) */
+    const int32_t *is_mol;     /* ismolecule(species): no Stark / vdW broadening */
+    const int32_t *species;    /* row of n_div_U for this line's species */
+} korg_lines;
+
+/* Per-layer inputs of line_absorption! (src/line_absorption.jl:33-60).  n_div_U[s * L + l] is
+ * n(species s)/U(species s, ln T_l), the host precompute of line_absorption.jl:42-44;
+ * n_eff_vdW is the perturber density of line_absorption.jl:59; xi is in cm/s. */
+typedef struct {
+    int32_t L;
+    int32_t S;
+    const double *T, *ne, *n_eff_vdW, *xi;
+    const double *n_div_U;
+} korg_layers;
+
+/* Continuum-opacity callables alpha_cntm[l](wl) (src/synthesize.jl:226-228): piecewise linear
+ * over nk knots (cm), vals[l * nk + k].  nk == 1 means a constant per layer (the form used
+ * for the reference-wavelength opacity, src/synthesize.jl:266). */
+typedef struct {
+    int64_t nk;
+    const double *knots;
+    const double *vals;
+} korg_cntm;
+
+/* Stehle & Hutcheon hydrogen tables (src/hydrogen_line_absorption.jl:6-37), packed.  For
+ * transition t: temps[t_off[t] + iT], nes[ne_off[t] + iNe], logdnu[d_off[t] + iD] (log of
+ * delta_nu_over_F0, first knot -DBL_MAX), logP[p_off[t] + (iD * nNe + iNe) * nT + iT] (log
+ * profile, -Inf clipped to -700), lambda0[l_off[t] + iNe * nT + iT] (cm). */
+typedef struct {
+    int32_t ntrans;
+    const int32_t *lower, *upper, *nT, *nNe, *nD;
+    const int64_t *t_off, *ne_off, *d_off, *p_off, *l_off;
+    const double *log_gf;
+    const double *temps, *nes, *logdnu, *logP, *lambda0;
+} korg_stark_tables;
+
+/* Everything synthesize() computes on the host before the hot path (src/synthesize.jl:211-262),
+ * for one atmosphere. */
+typedef struct {
+    korg_layers layers;
+    const double *tau_ref;        /* tau at the reference wavelength, per layer */
+    const double *alpha_ref_cntm; /* continuum alpha at the reference wavelength, per layer */
+    const double *nH_I, *nHe_I, *UH_I; /* per layer, for hydrogen lines */
+    double ref_wl;                /* cm */
+    korg_cntm cntm;
+    int32_t hydrogen_lines, use_MHD;
+    double hydrogen_window;       /* cm */
+    double cutoff_threshold;
+} korg_synth_inputs;
+
+typedef struct {
+    int64_t line_evals;        /* line-layer-wavelength Voigt evaluations of the last call */
+    int64_t lines_in_window;   /* lines with a non-empty window */
+    /* device time (ms) of the stages of the last korg_synthesize*, when timing is enabled:
+     * reference-wavelength lines, hydrogen lines, metal-line prologue (per-line constants,
+     * windows, scans), metal-line tile kernel, both transfers, whole call */
+    float ms_ref_lines, ms_hydrogen, ms_line_prep, ms_line_tile, ms_rt, ms_total;
+} korg_stats;
+
+typedef struct korg_ctx korg_ctx;
+
+/* Context: device, stream-ordered scratch arena, uploaded hydrogen tables.  One per host
+ * thread. */
+KORG_API int korg_create(korg_ctx **ctx, int device);
+KORG_API void korg_destroy(korg_ctx *ctx);
+KORG_API const char *korg_last_error(const korg_ctx *ctx);
+KORG_API int korg_get_stats(korg_ctx *ctx, korg_stats *out);
+/* Timing of the stages with CUDA events (adds event records; off by default). */
+KORG_API int korg_set_timing(korg_ctx *ctx, int enabled);
+
+/* Uploads the Stehle & Hutcheon tables once (src/hydrogen_line_absorption.jl:38-39). */
+KORG_API int korg_set_stark_tables(korg_ctx *ctx, const korg_stark_tables *host_tables);
+
+/* line_absorption!(alpha, linelist, wls, temps, ne, n_densities, partition_fns, xi, alpha_cntm;
+ * cutoff_threshold) -- src/line_absorption.jl:33-129.  alpha (host, L x nwl) is accumulated in
+ * place; an empty line list leaves it untouched (line_absorption.jl:35-37).  n_evals may be
+ * NULL. */
+KORG_API int korg_line_absorption(korg_ctx *ctx, double *alpha, const double *wls, int64_t nwl,
+                                  const korg_lines *lines, const korg_layers *layers,
+                                  const korg_cntm *cntm, double cutoff_threshold, int precision,
+                                  int64_t *n_evals);
+KORG_API int korg_line_absorption_dev(korg_ctx *ctx, double *alpha, const double *wls, int64_t nwl,
+                                      const korg_lines *lines, const korg_layers *layers,
+                                      const korg_cntm *cntm, double cutoff_threshold,
+                                      int precision, void *stream);
+
+/* hydrogen_line_absorption!(alphas, wls, T, ne, nH_I, nHe_I, UH_I, xi, window_size; use_MHD)
+ * -- src/hydrogen_line_absorption.jl:75-163, one layer; alphas (host, nwl) accumulated. */
+KORG_API int korg_hydrogen_line_absorption(korg_ctx *ctx, double *alphas, const double *wls,
+                                           int64_t nwl, double T, double ne, double nH_I,
+                                           double nHe_I, double UH_I, double xi,
+                                           double window_size, int use_MHD, int precision);
+/* All layers at once, as synthesize calls it per layer (src/synthesize.jl:293-303);
+ * alpha is the device L x nwl matrix, per-layer arrays are device pointers. */
+KORG_API int korg_hydrogen_lines_dev(korg_ctx *ctx, double *alpha, const double *wls, int64_t nwl,
+                                     int32_t L, const double *T, const double *ne,
+                                     const double *nH_I, const double *nHe_I, const double *UH_I,
+                                     const double *xi, double window_size, int use_MHD,
+                                     int precision, void *stream);
+
+/* RadiativeTransfer.radiative_transfer(atm::PlanarAtmosphere, alpha, S, mu_points; alpha_ref,
+ * tau_scheme="anchored", I_scheme="linear_flux_only") -- RadiativeTransfer.jl:62-139, the
+ * default planar path (anchored tau, exponential-integral flux).  flux[nwl] = F (erg/s/cm^5,
+ * without synthesize's 1e-8). */
+KORG_API int korg_radiative_transfer(korg_ctx *ctx, const double *alpha, const double *S,
+                                     int32_t L, int64_t nwl, const double *tau_ref,
+                                     const double *alpha_ref, double *flux);
+KORG_API int korg_radiative_transfer_dev(korg_ctx *ctx, const double *alpha, const double *S,
+                                         int32_t L, int64_t nwl, const double *tau_ref,
+                                         const double *alpha_ref, double *flux, void *stream);
+
+/* synthesize(atm, linelist, A_X, wavelengths) steps after chemical equilibrium and continuum
+ * (src/synthesize.jl:249-318): alpha_ref lines at the reference wavelength, source function,
+ * continuum-only transfer, hydrogen lines, metal/molecular lines, final transfer.  lines5 is
+ * the reference-wavelength line list (synthesize.jl:197-200).  flux and cntm (nwl, host) in
+ * erg/s/cm^4/A; alpha_out (L x nwl) and alpha_ref_out (L) may be NULL. */
+KORG_API int korg_synthesize(korg_ctx *ctx, const korg_synth_inputs *in, const korg_lines *lines,
+                             const korg_lines *lines5, const double *wls, int64_t nwl,
+                             int precision, double *flux, double *cntm, double *alpha_out,
+                             double *alpha_ref_out);
+KORG_API int korg_synthesize_dev(korg_ctx *ctx, const korg_synth_inputs *in,
+                                 const korg_lines *lines, const korg_lines *lines5,
+                                 const double *wls, int64_t nwl, int precision, double *flux,
+                                 double *cntm, double *alpha_out, void *stream);
+
+/* Not a counterpart of any reference function: measures the device's sustained FP32
+ * (fp64 == 0) or FP64 FMA throughput in TFLOP/s with independent FMA chains, the roofline
+ * denominator for the profile (FP32) and transfer (FP64) kernels. */
+KORG_API int korg_probe_flops(korg_ctx *ctx, int fp64, double *tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

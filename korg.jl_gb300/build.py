@@ -1,0 +1,46 @@
+"""Build libkorg_gb300.so (the CUDA kernels and the C ABI) in-tree for sm_103a.
+
+    python korg.jl_gb300/build.py [--force]
+
+One translation unit, one -gencode, no cmake: about half a minute with nvcc 13.
+"""
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "libkorg_gb300.so")
+SOURCES = [os.path.join(HERE, "csrc", f) for f in
+           ("korg_gb300.cu", "lines.cuh", "hydrogen.cuh", "rt.cuh", "physics.cuh")]
+HEADER = os.path.join(HERE, "..", "include", "korg_gb300.h")
+
+NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
+              "-shared", "-Xcompiler", "-fPIC", "-diag-suppress", "1444"]
+
+
+def nvcc():
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if cand and (os.path.sep not in cand or os.path.exists(cand)):
+            return cand
+    return "nvcc"
+
+
+def up_to_date():
+    if not os.path.exists(LIB):
+        return False
+    t = os.path.getmtime(LIB)
+    return all(os.path.getmtime(s) <= t for s in SOURCES + [HEADER])
+
+
+def build(force=False, verbose=False):
+    if not force and up_to_date():
+        return LIB
+    cmd = [nvcc()] + NVCC_FLAGS + ["-o", LIB, os.path.join(HERE, "csrc", "korg_gb300.cu")]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    subprocess.run(cmd, check=True)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

@@ -1,0 +1,334 @@
+// lines.cuh -- line opacity: per-(line, layer) prologue, window scans and the wavelength-tile
+// accumulation kernel.  Restates line_absorption! (src/line_absorption.jl:33-129).
+//
+// Work decomposition
+//   prep:  one warp per line, lanes over layers.  Computes sigma, gamma, amplitude, the
+//          continuum-cutoff window (line_absorption.jl:86-119) and the packed profile
+//          constants; lb/ub are the 0-based inclusive wavelength-index window.
+//   scan:  running max of ub (prefix) and running min of lb (suffix) over the sorted lines, so
+//          a wavelength tile finds its candidate lines with two binary searches.
+//   tile:  one CTA per tile of TW wavelengths x all layers.  Thread (j, g) owns wavelength j and
+//          layers g, g+G, g+2G, ...; alpha accumulates in registers (FP64, or FP32 with Kahan
+//          compensation), lines are visited in list order, so results are deterministic and
+//          no atomics touch alpha.  Lines overlapping the tile are compacted per chunk and
+//          their per-layer constants staged in shared memory.
+#pragma once
+#include "physics.cuh"
+
+namespace korg {
+
+constexpr int TILE_W_MAX = 128;  // wavelengths per CTA (64 when more than 4 layer groups)
+constexpr int STAGE_LINES = 32;  // lines staged in shared memory per batch (upper bound)
+
+// FP64 profile constants of one (line, layer): {1/(sigma sqrt2), a, scale, unused}
+struct alignas(32) D4 {
+    double x, y, z, w;
+};
+
+struct LinesDev {
+    int64_t n;
+    const double *wl, *log_gf, *E_lower, *gamma_rad, *gamma_stark, *vdW1, *vdW2, *mass;
+    const int32_t *is_mol, *species;
+};
+struct LayersDev {
+    int32_t L, S;
+    const double *T, *ne, *n_eff_vdW, *xi, *n_div_U;
+};
+struct CntmDev {
+    int64_t nk;
+    const double *knots, *vals;
+};
+
+// Per-layer constants shared by all lines (line_absorption.jl:39 and the temperature scalings
+// of :195 and :210), computed once per call.
+struct LayerConst {
+    double beta;    // 1/(k T)
+    double stark6;  // (T/10^4)^(1/6)
+    double vdw3;    // (T/10^4)^0.3
+};
+
+__global__ void layer_const_kernel(LayersDev lay, LayerConst* out) {
+    int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= lay.L) return;
+    double T = lay.T[l];
+    out[l].beta = 1 / (KBOLTZ_EV * T);
+    out[l].stark6 = pow(T / 10000.0, 1.0 / 6.0);
+    out[l].vdw3 = pow(T / 10000.0, 0.3);
+}
+
+struct PrepOut {
+    void* params;            // [n][L] double4 (FP64) or float4 (mixed)
+    int32_t* lb;             // [n]
+    int32_t* ub;             // [n]
+    unsigned long long* evals;   // running totals: evaluations, lines in window
+    unsigned long long* nlines;
+};
+
+template <bool MIXED>
+__global__ void __launch_bounds__(256) line_prep_kernel(LinesDev ln, LayersDev lay, const LayerConst* lc,
+                                                        CntmDev cn, const double* wls, int64_t nwl,
+                                                        double cutoff, PrepOut out) {
+    const int64_t i = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= ln.n) return;
+    const int L = lay.L;
+    const double wl = ln.wl[i], m = ln.mass[i], El = ln.E_lower[i];
+    const bool mol = ln.is_mol[i] != 0;
+    const double v1 = ln.vdW1[i], v2 = ln.vdW2[i], gstark = ln.gamma_stark[i], grad = ln.gamma_rad[i];
+    const int sp = ln.species[i];
+    // per-line factors (line_absorption.jl:101,105)
+    const double E_upper = El + C_CGS * HPLANCK_EV / wl;
+    const double strength = pow(10.0, ln.log_gf[i]) * sigma_line(wl);
+    const double wl2c = (wl * wl) / (C_CGS * (4 * PI));
+    // ABO prefactor (line_absorption.jl:219), per line
+    double abo_pre = 0.0;
+    if (!mol && v2 != -1) abo_pre = 2 * pow(4 / PI, v2 / 2) * tgamma((4 - v2) / 2) * 1e6 * v1;
+    const KnotPos kp = knot_pos(cn.knots, cn.nk, wl);
+
+    double dwin = 0.0, lwin = 0.0;
+    for (int l = lane; l < L; l += 32) {
+        const double T = lay.T[l];
+        const LayerConst c = lc[l];
+        const double sigma = doppler_width(wl, T, m, lay.xi[l]);  // :86
+        double G = grad;                                          // :90-94
+        if (!mol) {
+            G = G + lay.ne[l] * (gstark * c.stark6);
+            double vdw;
+            if (v2 == -1) {
+                vdw = v1 * c.vdw3;
+            } else {
+                const double invmu = 1 / (1.008 * AMU_CGS) + 1 / m;
+                const double vbar = sqrt(8 * KBOLTZ_CGS * T / PI * invmu);
+                vdw = abo_pre * pow(vbar / 1e6, 1 - v2);
+            }
+            G = G + lay.n_eff_vdW[l] * vdw;
+        }
+        const double gamma = G * wl2c;                                             // :99
+        const double levels = exp(-c.beta * El) - exp(-c.beta * E_upper);          // :101-102
+        const double amp = strength * levels * lay.n_div_U[int64_t(sp) * L + l];  // :105-106
+        const double acntm = knot_eval(cn.vals + int64_t(l) * cn.nk, cn.nk, kp);   // :108
+        const double rho = acntm * cutoff / amp;
+        const double dw = inverse_gaussian_density(rho, sigma);                    // :109-112
+        const double lw = inverse_lorentz_density(rho, gamma);
+        dwin = fmax(dwin, dw);
+        lwin = fmax(lwin, lw);
+        const double inv_s = 1 / (sigma * SQRT_2);                                 // :246-248
+        const double a = gamma * inv_s;
+        const double scale = inv_s / SQRT_PI * amp;
+        if (MIXED) {
+            float4 p;
+            p.x = float(inv_s);
+            p.y = float(a);
+            p.z = float(scale);
+            p.w = (p.y <= 0.2f) ? float(a / SQRT_PI * scale) : float(1.0 / (a * a));
+            reinterpret_cast<float4*>(out.params)[i * L + l] = p;
+        } else {
+            reinterpret_cast<D4*>(out.params)[i * L + l] = D4{inv_s, a, scale, 0.0};
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        dwin = fmax(dwin, __shfl_xor_sync(0xffffffffu, dwin, o));
+        lwin = fmax(lwin, __shfl_xor_sync(0xffffffffu, lwin, o));
+    }
+    if (lane == 0) {
+        const double window = sqrt(lwin * lwin + dwin * dwin);  // :113
+        const int64_t lb = search_first(wls, nwl, wl - window);  // :114-115
+        const int64_t ub = search_last(wls, nwl, wl + window);
+        out.lb[i] = int32_t(lb);
+        out.ub[i] = int32_t(ub);
+        if (lb <= ub) {
+            atomicAdd(out.evals, (unsigned long long)((ub - lb + 1) * L));
+            atomicAdd(out.nlines, 1ull);
+        }
+    }
+}
+
+// Running max of ub and running min of lb over lines (empty windows contribute nothing), one
+// CTA of 1024 threads: per-thread sequential chunks, then a block scan of the chunk totals.
+__global__ void __launch_bounds__(1024) window_scan_kernel(const int32_t* lb, const int32_t* ub, int64_t n,
+                                                           int32_t* pmax_ub, int32_t* smin_lb) {
+    __shared__ int32_t s_max[1024], s_min[1024];
+    const int t = threadIdx.x, T = blockDim.x;
+    const int64_t chunk = (n + T - 1) / T;
+    const int64_t b = t * chunk, e = (b + chunk < n) ? b + chunk : n;
+    int32_t mx = -1, mn = INT32_MAX;
+    for (int64_t k = b; k < e; k++) {
+        if (lb[k] <= ub[k]) mx = max(mx, ub[k]);
+    }
+    for (int64_t k = b; k < e; k++) {
+        if (lb[k] <= ub[k]) mn = min(mn, lb[k]);
+    }
+    s_max[t] = mx;
+    s_min[t] = mn;
+    __syncthreads();
+    // inclusive prefix max (forward) and suffix min (backward) over chunk totals
+    for (int o = 1; o < T; o <<= 1) {
+        int32_t a = (t >= o) ? s_max[t - o] : -1;
+        int32_t c = (t + o < T) ? s_min[t + o] : INT32_MAX;
+        __syncthreads();
+        s_max[t] = max(s_max[t], a);
+        s_min[t] = min(s_min[t], c);
+        __syncthreads();
+    }
+    int32_t run = (t > 0) ? s_max[t - 1] : -1;
+    for (int64_t k = b; k < e; k++) {
+        if (lb[k] <= ub[k]) run = max(run, ub[k]);
+        pmax_ub[k] = run;
+    }
+    run = (t + 1 < T) ? s_min[t + 1] : INT32_MAX;
+    for (int64_t k = e - 1; k >= b; k--) {
+        if (lb[k] <= ub[k]) run = min(run, lb[k]);
+        smin_lb[k] = run;
+    }
+}
+
+template <bool MIXED>
+struct ParamT { using type = D4; };
+template <>
+struct ParamT<true> { using type = float4; };
+
+struct TileArgs {
+    double* alpha;        // [nwl][L]
+    const double* wls;
+    int64_t nwl;
+    int32_t L, G, stage;  // G layer groups per CTA, lines per staging batch
+    int64_t n;
+    const double* wl;     // line centres
+    const void* params;
+    const int32_t *lb, *ub, *pmax_ub, *smin_lb;
+};
+
+// first index in [0, n) with a[i] >= v (a non-decreasing)
+__device__ __forceinline__ int64_t lower_bound_i32(const int32_t* a, int64_t n, int32_t v) {
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        int64_t mid = lo + ((hi - lo) >> 1);
+        if (a[mid] < v) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+// first index in [0, n) with a[i] > v (a non-decreasing)
+__device__ __forceinline__ int64_t upper_bound_i32(const int32_t* a, int64_t n, int32_t v) {
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        int64_t mid = lo + ((hi - lo) >> 1);
+        if (a[mid] <= v) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+template <bool MIXED, int KMAX>
+__global__ void __launch_bounds__(512) line_tile_kernel(TileArgs a) {
+    using P = typename ParamT<MIXED>::type;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int L = a.L, G = a.G, B = a.stage;
+    P* s_par = reinterpret_cast<P*>(smem);                                  // [B][L]
+    double* s_wl = reinterpret_cast<double*>(s_par + size_t(B) * L);        // [B]
+    int32_t* s_lb = reinterpret_cast<int32_t*>(s_wl + B);                   // [B]
+    int32_t* s_ub = s_lb + B;                                               // [B]
+    int32_t* s_list = s_ub + B;                                             // [blockDim]
+    __shared__ int32_t s_warp[32];
+    __shared__ int64_t s_range[2];
+
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const int TW = nthr / G;
+    const int jl = tid % TW, g = tid / TW;
+    const int64_t j0 = int64_t(blockIdx.x) * TW;
+    const int64_t jg = j0 + jl;
+    const int64_t jlast = min(j0 + TW, a.nwl) - 1;
+    const bool live = jg < a.nwl;
+    const double wl_j = live ? a.wls[jg] : 0.0;
+
+    if (tid == 0) {
+        s_range[0] = lower_bound_i32(a.pmax_ub, a.n, int32_t(j0));
+        s_range[1] = upper_bound_i32(a.smin_lb, a.n, int32_t(jlast)) - 1;
+    }
+    __syncthreads();
+    const int64_t i_lo = s_range[0], i_hi = s_range[1];
+
+    using Acc = typename std::conditional<MIXED, float, double>::type;
+    Acc acc[KMAX], comp[KMAX];
+#pragma unroll
+    for (int k = 0; k < KMAX; k++) { acc[k] = Acc(0); comp[k] = Acc(0); }
+
+    const int warp = tid >> 5, lane = tid & 31, nwarps = nthr >> 5;
+    for (int64_t base = i_lo; base <= i_hi; base += nthr) {
+        const int64_t i = base + tid;
+        bool take = false;
+        if (i <= i_hi) {
+            const int32_t lbi = a.lb[i], ubi = a.ub[i];
+            take = lbi <= ubi && lbi <= jlast && ubi >= j0;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, take);
+        if (lane == 0) s_warp[warp] = __popc(m);
+        __syncthreads();
+        if (tid == 0) {
+            int run = 0;
+            for (int w = 0; w < nwarps; w++) { int c = s_warp[w]; s_warp[w] = run; run += c; }
+            s_range[0] = run;  // reuse as the count
+        }
+        __syncthreads();
+        if (take) s_list[s_warp[warp] + __popc(m & ((1u << lane) - 1))] = int32_t(i - base);
+        const int cnt = int(s_range[0]);
+        __syncthreads();
+
+        for (int b0 = 0; b0 < cnt; b0 += B) {
+            const int nb = min(B, cnt - b0);
+            for (int b = warp; b < nb; b += nwarps) {
+                const int64_t li = base + s_list[b0 + b];
+                const P* src = reinterpret_cast<const P*>(a.params) + li * L;
+                for (int l = lane; l < L; l += 32) s_par[b * L + l] = src[l];
+                if (lane == 0) { s_wl[b] = a.wl[li]; s_lb[b] = a.lb[li]; s_ub[b] = a.ub[li]; }
+            }
+            __syncthreads();
+            if (live) {
+                for (int b = 0; b < nb; b++) {
+                    if (jg < s_lb[b] || jg > s_ub[b]) continue;
+                    const double dx = fabs(wl_j - s_wl[b]);  // FP64 offset from the line centre
+                    const P* pr = s_par + b * L;
+                    if (MIXED) {
+                        const float x = float(dx);
+#pragma unroll
+                        for (int k = 0; k < KMAX; k++) {
+                            const int l = g + G * k;
+                            if (l < L) {
+                                const float term = profile32(reinterpret_cast<const float4*>(pr)[l], x);
+                                // Kahan-compensated accumulation
+                                const float y = float(term) - float(comp[k]);
+                                const float t = float(acc[k]) + y;
+                                comp[k] = Acc((t - float(acc[k])) - y);
+                                acc[k] = Acc(t);
+                            }
+                        }
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < KMAX; k++) {
+                            const int l = g + G * k;
+                            if (l < L) {
+                                const D4 p = reinterpret_cast<const D4*>(pr)[l];
+                                acc[k] += Acc(voigt64(p.y, dx * p.x) * p.z);
+                            }
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    if (live) {
+#pragma unroll
+        for (int k = 0; k < KMAX; k++) {
+            const int l = g + G * k;
+            if (l < L) {
+                double* dst = a.alpha + jg * L + l;
+                if (MIXED)
+                    *dst = *dst + (double(acc[k]) - double(comp[k]));
+                else
+                    *dst = *dst + double(acc[k]);
+            }
+        }
+    }
+}
+
+}  // namespace korg

@@ -1,0 +1,200 @@
+"""ctypes binding of libkorg_gb300.so (the C ABI declared in include/korg_gb300.h).
+
+The library is built in-tree by ``korg.jl_gb300/build.py``.  Loading fails loudly when it is
+missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG_ROOT, "libkorg_gb300.so")
+
+KORG_FP64, KORG_MIXED = 0, 1
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+_lp = C.POINTER(C.c_int64)
+
+ERRORS = {1: "KORG_EINVAL", 2: "KORG_ECUDA", 3: "KORG_ENOMEM", 4: "KORG_ENOTABLES"}
+
+
+class KorgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Lines(C.Structure):
+    _fields_ = [("n", C.c_int64), ("wl", _dp), ("log_gf", _dp), ("E_lower", _dp), ("gamma_rad", _dp),
+                ("gamma_stark", _dp), ("vdW1", _dp), ("vdW2", _dp), ("mass", _dp), ("is_mol", _ip),
+                ("species", _ip)]
+
+
+class Layers(C.Structure):
+    _fields_ = [("L", C.c_int32), ("S", C.c_int32), ("T", _dp), ("ne", _dp), ("n_eff_vdW", _dp),
+                ("xi", _dp), ("n_div_U", _dp)]
+
+
+class Cntm(C.Structure):
+    _fields_ = [("nk", C.c_int64), ("knots", _dp), ("vals", _dp)]
+
+
+class StarkTables(C.Structure):
+    _fields_ = [("ntrans", C.c_int32), ("lower", _ip), ("upper", _ip), ("nT", _ip), ("nNe", _ip),
+                ("nD", _ip), ("t_off", _lp), ("ne_off", _lp), ("d_off", _lp), ("p_off", _lp),
+                ("l_off", _lp), ("log_gf", _dp), ("temps", _dp), ("nes", _dp), ("logdnu", _dp),
+                ("logP", _dp), ("lambda0", _dp)]
+
+
+class SynthInputs(C.Structure):
+    _fields_ = [("layers", Layers), ("tau_ref", _dp), ("alpha_ref_cntm", _dp), ("nH_I", _dp),
+                ("nHe_I", _dp), ("UH_I", _dp), ("ref_wl", C.c_double), ("cntm", Cntm),
+                ("hydrogen_lines", C.c_int32), ("use_MHD", C.c_int32), ("hydrogen_window", C.c_double),
+                ("cutoff_threshold", C.c_double)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("line_evals", C.c_int64), ("lines_in_window", C.c_int64), ("ms_ref_lines", C.c_float),
+                ("ms_hydrogen", C.c_float), ("ms_line_prep", C.c_float), ("ms_line_tile", C.c_float),
+                ("ms_rt", C.c_float), ("ms_total", C.c_float)]
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def lib():
+    """Load libkorg_gb300.so (raises if it has not been built)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise ImportError(f"{LIB_PATH} is missing: build it with korg.jl_gb300/build.py "
+                                  "(the CUDA library is required; there is no CPU path)")
+            L = C.CDLL(LIB_PATH)
+            vp = C.c_void_p
+            L.korg_create.argtypes = [C.POINTER(vp), C.c_int]
+            L.korg_destroy.argtypes = [vp]
+            L.korg_destroy.restype = None
+            L.korg_last_error.argtypes = [vp]
+            L.korg_last_error.restype = C.c_char_p
+            L.korg_get_stats.argtypes = [vp, C.POINTER(Stats)]
+            L.korg_set_timing.argtypes = [vp, C.c_int]
+            L.korg_set_stark_tables.argtypes = [vp, C.POINTER(StarkTables)]
+            L.korg_line_absorption.argtypes = [vp, _dp, _dp, C.c_int64, C.POINTER(Lines), C.POINTER(Layers),
+                                               C.POINTER(Cntm), C.c_double, C.c_int, _lp]
+            L.korg_line_absorption_dev.argtypes = [vp, vp, vp, C.c_int64, C.POINTER(Lines), C.POINTER(Layers),
+                                                   C.POINTER(Cntm), C.c_double, C.c_int, vp]
+            L.korg_hydrogen_line_absorption.argtypes = [vp, _dp, _dp, C.c_int64] + [C.c_double] * 7 + [C.c_int, C.c_int]
+            L.korg_hydrogen_lines_dev.argtypes = [vp, vp, vp, C.c_int64, C.c_int32] + [vp] * 6 + \
+                [C.c_double, C.c_int, C.c_int, vp]
+            L.korg_radiative_transfer.argtypes = [vp, _dp, _dp, C.c_int32, C.c_int64, _dp, _dp, _dp]
+            L.korg_radiative_transfer_dev.argtypes = [vp, vp, vp, C.c_int32, C.c_int64, vp, vp, vp, vp]
+            L.korg_synthesize.argtypes = [vp, C.POINTER(SynthInputs), C.POINTER(Lines), C.POINTER(Lines), _dp,
+                                          C.c_int64, C.c_int, _dp, _dp, _dp, _dp]
+            L.korg_synthesize_dev.argtypes = [vp, C.POINTER(SynthInputs), C.POINTER(Lines), C.POINTER(Lines), vp,
+                                              C.c_int64, C.c_int, vp, vp, vp, vp]
+            L.korg_probe_flops.argtypes = [vp, C.c_int, _dp]
+            _lib = L
+    return _lib
+
+
+def exported_symbols():
+    """Names declared in include/korg_gb300.h (checked against the library in the tests)."""
+    return ["korg_create", "korg_destroy", "korg_last_error", "korg_get_stats", "korg_set_timing",
+            "korg_set_stark_tables", "korg_line_absorption", "korg_line_absorption_dev",
+            "korg_hydrogen_line_absorption", "korg_hydrogen_lines_dev", "korg_radiative_transfer",
+            "korg_radiative_transfer_dev", "korg_synthesize", "korg_synthesize_dev", "korg_probe_flops"]
+
+
+def _p(a, kind=_dp):
+    return None if a is None else a.ctypes.data_as(kind)
+
+
+class Keep:
+    """Keeps numpy arrays alive while ctypes structs point into them."""
+
+    def __init__(self):
+        self.items = []
+
+    def f64(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        self.items.append(a)
+        return a
+
+    def i32(self, a):
+        a = np.ascontiguousarray(a, dtype=np.int32)
+        self.items.append(a)
+        return a
+
+    def i64(self, a):
+        a = np.ascontiguousarray(a, dtype=np.int64)
+        self.items.append(a)
+        return a
+
+
+def lines_struct(ll, keep: Keep) -> Lines:
+    return Lines(len(ll), _p(keep.f64(ll.wl)), _p(keep.f64(ll.log_gf)), _p(keep.f64(ll.E_lower)),
+                 _p(keep.f64(ll.gamma_rad)), _p(keep.f64(ll.gamma_stark)), _p(keep.f64(ll.vdW1)),
+                 _p(keep.f64(ll.vdW2)), _p(keep.f64(ll.mass)), _p(keep.i32(ll.is_mol), _ip),
+                 _p(keep.i32(ll.species_idx), _ip))
+
+
+def stark_struct(st, keep: Keep) -> StarkTables:
+    return StarkTables(st["ntrans"], *[_p(keep.i32(st[k]), _ip) for k in ["lower", "upper", "nT", "nNe", "nD"]],
+                       *[_p(keep.i64(st[k]), _lp) for k in ["t_off", "ne_off", "d_off", "p_off", "l_off"]],
+                       *[_p(keep.f64(st[k])) for k in ["log_gf", "temps", "nes", "logdnu", "logP", "lambda0"]])
+
+
+class Context:
+    """One korg_ctx (device, scratch arena, Stark tables)."""
+
+    def __init__(self, device=0):
+        self.lib = lib()
+        self.h = C.c_void_p()
+        rc = self.lib.korg_create(C.byref(self.h), device)
+        if rc != 0:
+            raise KorgError(rc, "korg_create failed (no usable CUDA device?)")
+        self.have_stark = False
+
+    def check(self, rc):
+        if rc != 0:
+            raise KorgError(rc, self.lib.korg_last_error(self.h).decode())
+
+    def ensure_stark(self):
+        if not self.have_stark:
+            from .data import stark_profiles
+            keep = Keep()
+            st = stark_struct(stark_profiles(), keep)
+            self.check(self.lib.korg_set_stark_tables(self.h, C.byref(st)))
+            self.have_stark = True
+
+    def stats(self):
+        s = Stats()
+        self.check(self.lib.korg_get_stats(self.h, C.byref(s)))
+        return s
+
+    def close(self):
+        if self.h:
+            self.lib.korg_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx = None
+
+
+def default_context():
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx

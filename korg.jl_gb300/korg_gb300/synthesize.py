@@ -1,0 +1,320 @@
+"""Python mirror of Korg's hot-path API, backed by the CUDA library.
+
+* :func:`line_absorption_`   -- ``line_absorption!`` (src/line_absorption.jl:33-129)
+* :func:`hydrogen_line_absorption_` -- ``hydrogen_line_absorption!``
+  (src/hydrogen_line_absorption.jl:75-163)
+* :func:`radiative_transfer` -- ``RadiativeTransfer.radiative_transfer`` for a planar
+  atmosphere with the default schemes (RadiativeTransfer.jl:62-139)
+* :func:`synthesize`         -- ``synthesize`` (src/synthesize.jl:138-324)
+
+Arrays follow Korg's memory layout: alpha is (layers x wavelengths) column-major, i.e. a numpy
+array of shape (L, nwl) in Fortran order (equivalently (nwl, L) in C order).  ``precision`` is
+``"fp64"`` (the plain form) or ``"mixed"``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from .constants import c_cgs
+from .data import default_partition_funcs
+from .linelist import LineList, alpha_5000_linelist, filter_linelist
+from .species import Species, atomic_masses, parse_species
+from .wavelengths import Wavelengths
+
+_PREC = {"fp64": _lib.KORG_FP64, "mixed": _lib.KORG_MIXED}
+
+# line_absorption.jl:54-58: perturber-density coefficients of He and H2 relative to H
+_a_H, _a_He, _a_H2 = 4.50711, 1.38375, 5.503
+C_HE = (_a_He / _a_H) ** 0.4 * (atomic_masses[1] / atomic_masses[0]) ** -0.3
+C_H2 = (_a_H2 / _a_H) ** 0.4 * 2 ** -0.3
+
+
+def _prec(p):
+    try:
+        return _PREC[p]
+    except KeyError:
+        raise ValueError(f"precision must be 'fp64' or 'mixed', got {p!r}") from None
+
+
+def _alpha_buffer(alpha, L, nwl):
+    """View alpha as a contiguous buffer in Korg's layout; returns (buffer, writeback)."""
+    a = np.asarray(alpha)
+    if a.dtype != np.float64:
+        raise TypeError("alpha must be float64")
+    if a.shape == (L, nwl) and a.flags.f_contiguous:
+        return a.T, None  # (nwl, L) C-contiguous view of the same memory
+    if a.shape == (nwl, L) and a.flags.c_contiguous:
+        return a, None
+    if a.shape == (L, nwl):
+        buf = np.ascontiguousarray(a.T)
+        return buf, lambda: np.copyto(a, buf.T)
+    raise ValueError(f"alpha must have shape (L, nwl) = ({L}, {nwl})")
+
+
+def n_div_U_matrix(species, n_densities, partition_fns, temps):
+    """Rows n(species)/U(species, ln T) per layer (line_absorption.jl:42-44)."""
+    lnT = np.log(np.asarray(temps, np.float64))
+    rows = []
+    for s in species:
+        if s not in n_densities:
+            raise KeyError(f"no number density for {s}")
+        rows.append(np.asarray(n_densities[s], np.float64) / partition_fns[s](lnT))
+    return np.ascontiguousarray(np.array(rows).reshape(len(species), len(lnT)))
+
+
+def n_eff_vdW(n_densities, L):
+    """line_absorption.jl:59-60"""
+    z = np.zeros(L)
+    g = lambda s: np.asarray(n_densities.get(parse_species(s), z), np.float64)
+    return g("H I") + C_HE * g("He I") + C_H2 * g("H2")
+
+
+class ContinuumInterpolant:
+    """The per-layer continuum callables alpha_cntm[l](wl): piecewise linear over ``knots`` (cm)
+    with ``vals`` of shape (L, nk) (src/synthesize.jl:226-228).  A 1-knot interpolant is a
+    constant per layer."""
+
+    def __init__(self, knots, vals):
+        self.knots = np.ascontiguousarray(knots, np.float64)
+        self.vals = np.ascontiguousarray(vals, np.float64)
+
+    @classmethod
+    def constant(cls, values):
+        v = np.asarray(values, np.float64)
+        return cls(np.zeros(1), v.reshape(-1, 1))
+
+
+def line_absorption_(alpha, linelist: LineList, wls, temps, ne, n_densities, partition_fns, xi, alpha_cntm,
+                     cutoff_threshold=3e-4, precision="fp64", ctx=None):
+    """``line_absorption!``: add line opacity to ``alpha`` (L x nwl) in place.  Returns the
+    number of line-layer-wavelength profile evaluations."""
+    wls = Wavelengths(wls) if not isinstance(wls, Wavelengths) else wls
+    temps = np.asarray(temps, np.float64)
+    L, nwl = len(temps), len(wls)
+    if len(linelist) == 0:
+        return 0  # line_absorption.jl:35-37
+    if parse_species("H I") in linelist.species:
+        import warnings
+        warnings.warn("Atomic hydrogen should not be in the linelist. Korg has built-in hydrogen lines.")
+    ctx = ctx or _lib.default_context()
+    keep = _lib.Keep()
+    nU = n_div_U_matrix(linelist.species, n_densities, partition_fns, temps)
+    xi_l = np.broadcast_to(np.asarray(xi, np.float64), (L,))
+    lay = _lib.Layers(L, nU.shape[0], _lib._p(keep.f64(temps)), _lib._p(keep.f64(ne)),
+                      _lib._p(keep.f64(n_eff_vdW(n_densities, L))), _lib._p(keep.f64(xi_l)), _lib._p(keep.f64(nU)))
+    if isinstance(alpha_cntm, ContinuumInterpolant):
+        ci = alpha_cntm
+    else:
+        ci = ContinuumInterpolant.constant(alpha_cntm)
+    cn = _lib.Cntm(len(ci.knots), _lib._p(keep.f64(ci.knots)), _lib._p(keep.f64(ci.vals)))
+    lines = _lib.lines_struct(linelist, keep)
+    buf, wb = _alpha_buffer(alpha, L, nwl)
+    n = C.c_int64(0)
+    ctx.check(ctx.lib.korg_line_absorption(ctx.h, _lib._p(buf), _lib._p(keep.f64(wls.all_wls)), nwl, C.byref(lines),
+                                           C.byref(lay), C.byref(cn), cutoff_threshold, _prec(precision),
+                                           C.byref(n)))
+    if wb:
+        wb()
+    return n.value
+
+
+def hydrogen_line_absorption_(alphas, wls, T, ne, nH_I, nHe_I, UH_I, xi, window_size, use_MHD=True,
+                              precision="fp64", ctx=None):
+    """``hydrogen_line_absorption!`` for one layer: add to ``alphas`` (nwl) in place."""
+    wls = Wavelengths(wls) if not isinstance(wls, Wavelengths) else wls
+    ctx = ctx or _lib.default_context()
+    ctx.ensure_stark()
+    a = np.asarray(alphas)
+    if a.dtype != np.float64 or not a.flags.c_contiguous or a.shape != (len(wls),):
+        raise ValueError("alphas must be a contiguous float64 vector over the wavelengths")
+    w = np.ascontiguousarray(wls.all_wls)
+    ctx.check(ctx.lib.korg_hydrogen_line_absorption(ctx.h, _lib._p(a), _lib._p(w), len(w), float(T), float(ne),
+                                                    float(nH_I), float(nHe_I), float(UH_I), float(xi),
+                                                    float(window_size), int(bool(use_MHD)), _prec(precision)))
+
+
+def radiative_transfer(atm, alpha, S, mu_points, alpha_ref=None, tau_ref=None, tau_scheme="anchored",
+                       I_scheme="linear_flux_only", ctx=None):
+    """``radiative_transfer(atm::PlanarAtmosphere, alpha, S, mu_points; alpha_ref, ...)`` with
+    the default schemes.  Returns (F, I, mu_grid, mu_weights) where I is the surface intensity
+    of the single exponential-integral ray (RadiativeTransfer.jl:81-84, 135-138)."""
+    if tau_scheme not in ("anchored", "bezier"):
+        raise ValueError('tau_scheme must be one of "anchored" or "bezier"')
+    if I_scheme not in ("linear", "linear_flux_only", "bezier"):
+        raise ValueError('I_scheme must be one of "linear", "bezier", or "linear_flux_only"')
+    if not (tau_scheme == "anchored" and I_scheme == "linear_flux_only"):
+        raise NotImplementedError("the GPU path implements the default planar scheme "
+                                  "(anchored tau, linear_flux_only -> exponential-integral flux)")
+    tau_ref = atm.tau_ref if tau_ref is None else tau_ref
+    L = len(tau_ref)
+    a = np.asarray(alpha)
+    nwl = a.size // L
+    abuf, _ = _alpha_buffer(a, L, nwl)
+    sbuf, _ = _alpha_buffer(np.asarray(S), L, nwl)
+    ctx = ctx or _lib.default_context()
+    keep = _lib.Keep()
+    F = np.empty(nwl)
+    ctx.check(ctx.lib.korg_radiative_transfer(ctx.h, _lib._p(abuf), _lib._p(sbuf), L, nwl, _lib._p(keep.f64(tau_ref)),
+                                              _lib._p(keep.f64(alpha_ref)), _lib._p(F)))
+    I = F / (2 * np.pi)
+    return F, I.reshape(1, nwl), np.array([1.0]), np.array([1.0])
+
+
+# ---------------------------------------------------------------------------------- synthesize
+
+
+@dataclass
+class SynthesisInputs:
+    """Everything synthesize() computes on the host before the hot path
+    (src/synthesize.jl:159-262), for one atmosphere."""
+
+    wls: Wavelengths
+    linelist: LineList
+    linelist5: LineList
+    T: np.ndarray
+    ne: np.ndarray
+    tau_ref: np.ndarray
+    xi: np.ndarray
+    n_eff_vdW: np.ndarray
+    n_div_U: np.ndarray          # (S, L), rows follow linelist.species (shared with linelist5)
+    nH_I: np.ndarray
+    nHe_I: np.ndarray
+    UH_I: np.ndarray
+    alpha_ref_cntm: np.ndarray
+    cntm_knots: np.ndarray
+    cntm_vals: np.ndarray        # (L, nk)
+    ref_wl: float = 5e-5
+    hydrogen_lines: bool = True
+    use_MHD: bool = True
+    hydrogen_window: float = 150e-8
+    cutoff_threshold: float = 3e-4
+    number_densities: dict = field(default_factory=dict)
+
+    def struct(self, keep):
+        L = len(self.T)
+        lay = _lib.Layers(L, self.n_div_U.shape[0], _lib._p(keep.f64(self.T)), _lib._p(keep.f64(self.ne)),
+                          _lib._p(keep.f64(self.n_eff_vdW)), _lib._p(keep.f64(self.xi)),
+                          _lib._p(keep.f64(self.n_div_U)))
+        return _lib.SynthInputs(lay, _lib._p(keep.f64(self.tau_ref)), _lib._p(keep.f64(self.alpha_ref_cntm)),
+                                _lib._p(keep.f64(self.nH_I)), _lib._p(keep.f64(self.nHe_I)),
+                                _lib._p(keep.f64(self.UH_I)), self.ref_wl,
+                                _lib.Cntm(len(self.cntm_knots), _lib._p(keep.f64(self.cntm_knots)),
+                                          _lib._p(keep.f64(self.cntm_vals))),
+                                int(self.hydrogen_lines), int(self.use_MHD), self.hydrogen_window,
+                                self.cutoff_threshold)
+
+
+@dataclass
+class SynthesisResult:
+    """src/synthesize.jl:30-41 (alpha only when requested)."""
+
+    flux: np.ndarray
+    cntm: np.ndarray
+    alpha: np.ndarray | None
+    alpha_ref: np.ndarray | None
+    wavelengths: np.ndarray
+    subspectra: list
+    line_evals: int = 0
+
+
+def _merge_windows(wins):
+    wins = sorted(wins)
+    out = [list(wins[0])]
+    for a, b in wins[1:]:
+        if a <= out[-1][1]:
+            out[-1][1] = max(out[-1][1], b)
+        else:
+            out.append([a, b])
+    return [tuple(w) for w in out]
+
+
+def prepare_synthesis(atm, linelist: LineList, A_X, wavelengths, vmic=1.0, line_buffer=10.0, cntm_step=1.0,
+                      hydrogen_lines=True, use_MHD_for_hydrogen_lines=None, hydrogen_line_window_size=150,
+                      line_cutoff_threshold=3e-4, use_internal_reference_linelist=True,
+                      chemical_equilibrium=None, continuum_opacity=None):
+    """The host part of synthesize (src/synthesize.jl:159-262).  Chemical equilibrium and the
+    continuum come from ``chemical_equilibrium(T, n_tot, A_X) -> (ne, {Species: n})`` and
+    ``continuum_opacity(wls_cm, T, ne, n_HI, n_HII) -> alpha``; by default the stand-ins of
+    :mod:`korg_gb300.standin`."""
+    from . import standin
+    chem = chemical_equilibrium or standin.chemical_equilibrium
+    cont = continuum_opacity or standin.continuum_opacity
+    wls = wavelengths if isinstance(wavelengths, Wavelengths) else Wavelengths(wavelengths)
+    use_MHD = (wls.all_wls[-1] < 13_000e-8) if use_MHD_for_hydrogen_lines is None else use_MHD_for_hydrogen_lines
+    if wls.all_wls[0] < 1300e-8:  # :170-177
+        raise ValueError("Requested wavelength range extends blue-ward of 1300 A, the lowest allowed wavelength.")
+    cstep, lbuf = cntm_step * 1e-8, line_buffer * 1e-8
+    wins = _merge_windows([(a - lbuf - cstep, b + lbuf + cstep) for a, b in wls.eachwindow()])
+    cntm_wls = Wavelengths([(a, b, cstep) for a, b in wins])
+    if not linelist.is_sorted():  # :191-194
+        linelist = linelist.sorted()
+    if atm.reference_wavelength == 5e-5 and use_internal_reference_linelist:
+        ll5 = alpha_5000_linelist()
+    else:
+        raise NotImplementedError("only the built-in 5000 A reference line list is supported")
+    linelist = filter_linelist(linelist, wls, lbuf)
+    # one species table for both lists
+    ll = linelist.concat(ll5.subset(np.zeros(0, dtype=np.int64)))
+    species = list(ll.species)
+    remap = []
+    for s in ll5.species:
+        if s not in species:
+            species.append(s)
+        remap.append(species.index(s))
+    ll = LineList(ll.wl, ll.log_gf, ll.species_idx, species, ll.E_lower, ll.gamma_rad, ll.gamma_stark, ll.vdW1,
+                  ll.vdW2)
+    remap = np.asarray(remap, np.int32)
+    ll5 = LineList(ll5.wl, ll5.log_gf, remap[ll5.species_idx], species, ll5.E_lower, ll5.gamma_rad,
+                   ll5.gamma_stark, ll5.vdW1, ll5.vdW2)
+    T = np.asarray(atm.T, np.float64)
+    L = len(T)
+    ne, nd = chem(T, atm.n_tot, A_X)
+    pf = default_partition_funcs()
+    for s in species:  # species the stand-in does not form get zero density
+        nd.setdefault(s, np.zeros(L))
+    H1, H2, He1 = parse_species("H I"), parse_species("H II"), parse_species("He I")
+    vals = np.empty((L, len(cntm_wls)))
+    aref = np.empty(L)
+    for l in range(L):
+        vals[l] = cont(cntm_wls.all_wls, T[l], ne[l], nd[H1][l], nd[H2][l])
+        aref[l] = cont(np.array([atm.reference_wavelength]), T[l], ne[l], nd[H1][l], nd[H2][l])[0]
+    xi = np.broadcast_to(np.asarray(vmic, np.float64) * 1e5, (L,)).copy()
+    return SynthesisInputs(
+        wls=wls, linelist=ll, linelist5=ll5, T=T, ne=np.asarray(ne, np.float64),
+        tau_ref=np.asarray(atm.tau_ref, np.float64), xi=xi, n_eff_vdW=n_eff_vdW(nd, L),
+        n_div_U=n_div_U_matrix(species, nd, pf, T), nH_I=nd[H1], nHe_I=nd[He1],
+        UH_I=pf[H1](np.log(T)), alpha_ref_cntm=aref, cntm_knots=cntm_wls.all_wls, cntm_vals=vals,
+        ref_wl=atm.reference_wavelength, hydrogen_lines=hydrogen_lines, use_MHD=bool(use_MHD),
+        hydrogen_window=hydrogen_line_window_size * 1e-8, cutoff_threshold=line_cutoff_threshold,
+        number_densities=nd)
+
+
+def synthesize_prepared(inp: SynthesisInputs, precision="mixed", return_alpha=False, ctx=None) -> SynthesisResult:
+    """Run the hot path (src/synthesize.jl:249-318) on prepared inputs through korg_synthesize."""
+    ctx = ctx or _lib.default_context()
+    if inp.hydrogen_lines:
+        ctx.ensure_stark()
+    keep = _lib.Keep()
+    s = inp.struct(keep)
+    lines = _lib.lines_struct(inp.linelist, keep)
+    lines5 = _lib.lines_struct(inp.linelist5, keep)
+    nwl, L = len(inp.wls), len(inp.T)
+    flux, cntm = np.empty(nwl), np.empty(nwl)
+    alpha = np.empty((nwl, L)) if return_alpha else None
+    aref = np.empty(L)
+    w = keep.f64(inp.wls.all_wls)
+    ctx.check(ctx.lib.korg_synthesize(ctx.h, C.byref(s), C.byref(lines), C.byref(lines5), _lib._p(w), nwl,
+                                      _prec(precision), _lib._p(flux), _lib._p(cntm), _lib._p(alpha), _lib._p(aref)))
+    return SynthesisResult(flux=flux, cntm=cntm, alpha=None if alpha is None else alpha.T, alpha_ref=aref,
+                           wavelengths=inp.wls.all_wls * 1e8, subspectra=inp.wls.subspectrum_indices(),
+                           line_evals=ctx.stats().line_evals)
+
+
+def synthesize(atm, linelist, A_X, wavelengths, precision="mixed", return_alpha=False, ctx=None, **kwargs):
+    """``synthesize(atm, linelist, A_X, wavelengths; kwargs...)`` (src/synthesize.jl:138-324)."""
+    inp = prepare_synthesis(atm, linelist, A_X, wavelengths, **kwargs)
+    return synthesize_prepared(inp, precision=precision, return_alpha=return_alpha, ctx=ctx)

@@ -1,0 +1,277 @@
+"""CUDA path vs the FP64 oracle, through the C ABI (needs a GB300).
+
+Tolerances: the plain FP64 path must match the oracle to 1e-9 relative; the mixed form to
+1e-4 maximum relative flux error (the spec budget), with the alpha-level error reported.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+NT = os.cpu_count() or 1
+
+
+@pytest.fixture(scope="module")
+def ctx(gpu_lib):
+    c = gpu_lib.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def cfg0():
+    from korg_gb300 import synthetic
+    return synthetic.prepare(synthetic.config0())
+
+
+def _cont_alpha(inp):
+    """alpha initialised from the continuum interpolants (src/synthesize.jl:249-252)."""
+    w = inp.wls.all_wls
+    return np.ascontiguousarray(np.stack([np.interp(w, inp.cntm_knots, v) for v in inp.cntm_vals], axis=1))
+
+
+def _gpu_line_absorption(ctx, inp, alpha, precision, linelist=None, wls=None, cntm=None):
+    from korg_gb300 import _lib
+    ll = inp.linelist if linelist is None else linelist
+    wls = inp.wls.all_wls if wls is None else wls
+    keep = _lib.Keep()
+    L = len(inp.T)
+    lay = _lib.Layers(L, inp.n_div_U.shape[0], _lib._p(keep.f64(inp.T)), _lib._p(keep.f64(inp.ne)),
+                      _lib._p(keep.f64(inp.n_eff_vdW)), _lib._p(keep.f64(inp.xi)), _lib._p(keep.f64(inp.n_div_U)))
+    knots, vals = (inp.cntm_knots, inp.cntm_vals) if cntm is None else cntm
+    cn = _lib.Cntm(len(knots), _lib._p(keep.f64(knots)), _lib._p(keep.f64(vals)))
+    lines = _lib.lines_struct(ll, keep)
+    n = C.c_int64(0)
+    w = keep.f64(wls)
+    rc = ctx.lib.korg_line_absorption(ctx.h, _lib._p(alpha), _lib._p(w), len(w), C.byref(lines), C.byref(lay),
+                                      C.byref(cn), inp.cutoff_threshold, precision, C.byref(n))
+    return rc, n.value
+
+
+def _oracle_line_absorption(oracle_lib, inp, alpha, linelist=None, wls=None):
+    ll = inp.linelist if linelist is None else linelist
+    wls = inp.wls.all_wls if wls is None else wls
+    return oracle_lib.line_absorption(alpha, ll, wls, inp.T, inp.ne, inp.n_eff_vdW, inp.xi, inp.n_div_U,
+                                      inp.cntm_knots, inp.cntm_vals, cutoff=inp.cutoff_threshold, nthreads=NT)
+
+
+def test_line_absorption_fp64_parity(ctx, cfg0, oracle_lib):
+    a0 = _cont_alpha(cfg0)
+    ref = a0.copy()
+    ev_ref = _oracle_line_absorption(oracle_lib, cfg0, ref)
+    got = a0.copy()
+    rc, ev = _gpu_line_absorption(ctx, cfg0, got, 0)
+    assert rc == 0, ctx.lib.korg_last_error(ctx.h)
+    assert ev == ev_ref  # identical windows: line-layer-wavelength evaluation counts match
+    rel = np.abs(got - ref) / np.abs(ref)
+    assert rel.max() <= 1e-9, rel.max()
+    line = ref - a0  # line part alone, where it is significant
+    sig = line > 1e-6 * ref
+    assert np.max(np.abs((got - a0)[sig] - line[sig]) / line[sig]) <= 1e-9
+
+
+def test_line_absorption_mixed(ctx, cfg0, oracle_lib):
+    a0 = _cont_alpha(cfg0)
+    ref = a0.copy()
+    _oracle_line_absorption(oracle_lib, cfg0, ref)
+    got = a0.copy()
+    rc, _ = _gpu_line_absorption(ctx, cfg0, got, 1)
+    assert rc == 0, ctx.lib.korg_last_error(ctx.h)
+    rel = np.abs(got - ref) / np.abs(ref)
+    print(f"mixed alpha: max rel {rel.max():.3e}, 99.9th pct {np.percentile(rel, 99.9):.3e}")
+    assert np.percentile(rel, 99.9) <= 1e-5
+    assert rel.max() <= 1e-2  # isolated elements at the Hjerting branch seams
+
+
+def test_line_absorption_edge_cases(ctx, cfg0, oracle_lib):
+    from korg_gb300.linelist import LineList
+    a0 = _cont_alpha(cfg0)
+    # empty list leaves alpha untouched (line_absorption.jl:35-37)
+    empty = cfg0.linelist.subset(np.zeros(0, dtype=np.int64))
+    got = a0.copy()
+    rc, ev = _gpu_line_absorption(ctx, cfg0, got, 0, linelist=empty)
+    assert rc == 0 and ev == 0 and np.array_equal(got, a0)
+    # lines entirely outside the grid
+    far = cfg0.linelist.subset(np.arange(5))
+    far = LineList(far.wl + 1e-5, far.log_gf, far.species_idx, far.species, far.E_lower, far.gamma_rad,
+                   far.gamma_stark, far.vdW1, far.vdW2)
+    got = a0.copy()
+    rc, ev = _gpu_line_absorption(ctx, cfg0, got, 0, linelist=far)
+    assert rc == 0 and np.array_equal(got, a0)
+    # ragged grid sizes: one point, and not a multiple of the tile width
+    for sl in (slice(5000, 5001), slice(4000, 4131), slice(0, 257)):
+        w = cfg0.wls.all_wls[sl]
+        ref = a0[sl].copy()
+        ev_ref = _oracle_line_absorption(oracle_lib, cfg0, ref, wls=w)
+        got = a0[sl].copy()
+        rc, ev = _gpu_line_absorption(ctx, cfg0, got, 0, wls=w)
+        assert rc == 0 and ev == ev_ref
+        np.testing.assert_allclose(got, ref, rtol=1e-9, atol=0)
+
+
+def test_line_absorption_errors(ctx, cfg0):
+    from korg_gb300.linelist import LineList
+    a0 = _cont_alpha(cfg0)
+    rc, _ = _gpu_line_absorption(ctx, cfg0, a0.copy(), 0, wls=cfg0.wls.all_wls[::-1].copy())
+    assert rc == 1  # unsorted wavelengths: KORG_EINVAL
+    ll = cfg0.linelist.subset(np.arange(3))
+    bad = LineList(ll.wl, ll.log_gf, np.array([0, 99, 0], np.int32), ll.species, ll.E_lower, ll.gamma_rad,
+                   ll.gamma_stark, ll.vdW1, ll.vdW2)
+    rc, _ = _gpu_line_absorption(ctx, cfg0, a0.copy(), 0, linelist=bad)
+    assert rc == 1 and b"species" in ctx.lib.korg_last_error(ctx.h)
+
+
+def test_line_absorption_80_layers(ctx, oracle_lib):
+    """Five layer groups per CTA (tile width 64) on a cool giant."""
+    from korg_gb300 import synthetic
+    w = synthetic.config4(n_lines=3000)
+    w.wavelengths = (5000, 5050)
+    inp = synthetic.prepare(w)
+    assert len(inp.T) == 80
+    a0 = _cont_alpha(inp)
+    ref = a0.copy()
+    ev_ref = _oracle_line_absorption(oracle_lib, inp, ref)
+    for prec, tol in ((0, 1e-9), (1, 1e-2)):
+        got = a0.copy()
+        rc, ev = _gpu_line_absorption(ctx, inp, got, prec)
+        assert rc == 0 and ev == ev_ref
+        assert np.max(np.abs(got - ref) / ref) <= tol
+
+
+def test_rt_parity(ctx, cfg0, oracle_lib):
+    from korg_gb300 import _lib
+    alpha = _cont_alpha(cfg0)
+    _oracle_line_absorption(oracle_lib, cfg0, alpha)
+    S = np.array([[oracle_lib.blackbody(T, w) for T in cfg0.T] for w in cfg0.wls.all_wls[::10]])
+    alpha = np.ascontiguousarray(alpha[::10])
+    ref = oracle_lib.rt_flux_expint(alpha, S, cfg0.tau_ref, cfg0.alpha_ref_cntm, nthreads=NT)
+    got = np.empty_like(ref)
+    keep = _lib.Keep()
+    rc = ctx.lib.korg_radiative_transfer(ctx.h, _lib._p(alpha), _lib._p(S), len(cfg0.T), len(ref),
+                                         _lib._p(keep.f64(cfg0.tau_ref)), _lib._p(keep.f64(cfg0.alpha_ref_cntm)),
+                                         _lib._p(got))
+    assert rc == 0
+    np.testing.assert_allclose(got, ref, rtol=1e-12, atol=0)
+
+
+def _h_layers(inp, idx):
+    return [(inp.T[l], inp.ne[l], inp.nH_I[l], inp.nHe_I[l], inp.UH_I[l], inp.xi[l]) for l in idx]
+
+
+@pytest.mark.parametrize("rng_A,use_MHD", [((3800, 4200), True), ((6400, 6700), True), ((15000, 17000, 0.01), False)])
+def test_hydrogen_fp64_parity(ctx, oracle_lib, rng_A, use_MHD):
+    from korg_gb300 import _lib, synthetic
+    from korg_gb300.data import stark_profiles
+    from korg_gb300.wavelengths import Wavelengths
+    inp = synthetic.prepare(synthetic.config1(n_lines=10, wl=(5000, 5001)))
+    ctx.ensure_stark()
+    w = Wavelengths(rng_A).all_wls
+    for T, ne, nH, nHe, UH, xi in _h_layers(inp, [5, 30, 45, 55]):
+        ref = np.full(len(w), 1e-7)
+        oracle_lib.hydrogen_line_absorption(ref, w, T, ne, nH, nHe, UH, xi, 150e-8, use_MHD, stark_profiles())
+        got = np.full(len(w), 1e-7)
+        rc = ctx.lib.korg_hydrogen_line_absorption(ctx.h, _lib._p(got), _lib._p(w), len(w), T, ne, nH, nHe, UH, xi,
+                                                   150e-8, int(use_MHD), 0)
+        assert rc == 0, ctx.lib.korg_last_error(ctx.h)
+        np.testing.assert_allclose(got, ref, rtol=1e-9, atol=0)
+        got32 = np.full(len(w), 1e-7)
+        rc = ctx.lib.korg_hydrogen_line_absorption(ctx.h, _lib._p(got32), _lib._p(w), len(w), T, ne, nH, nHe, UH, xi,
+                                                   150e-8, int(use_MHD), 1)
+        assert rc == 0
+        np.testing.assert_allclose(got32, ref, rtol=1e-4, atol=0)
+
+
+def test_lyman_golden_gpu(ctx):
+    """The reference's hydrogen golden vector through the CUDA path (atol 5e-9)."""
+    from korg_gb300 import _lib
+    from korg_gb300.wavelengths import Wavelengths
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "lyman_absorption.npz"))
+    w = Wavelengths([(float(g["start_wl"]), float(g["stop_wl"]), float(g["wl_step"]))]).all_wls
+    ctx.ensure_stark()
+    got = np.zeros(len(w))
+    rc = ctx.lib.korg_hydrogen_line_absorption(ctx.h, _lib._p(got), _lib._p(w), len(w), 9000.0, float(g["ne"]),
+                                               float(g["nH_I"]), 0.0, float(g["UH_I_9000"]), 0.0, 15e-7, 0, 0)
+    assert rc == 0
+    np.testing.assert_allclose(got, g["profile"], rtol=0, atol=5e-9)
+
+
+def test_synthesize_fp64_parity(ctx, cfg0, oracle_lib):
+    from korg_gb300.data import stark_profiles
+    from korg_gb300.synthesize import synthesize_prepared
+    flux, cntm, alpha, aref, ev = oracle_lib.synthesize(cfg0, cfg0.linelist, cfg0.linelist5, stark_profiles(),
+                                                        cfg0.wls.all_wls, nthreads=NT)
+    res = synthesize_prepared(cfg0, precision="fp64", return_alpha=True, ctx=ctx)
+    np.testing.assert_allclose(res.alpha_ref, aref, rtol=1e-9)
+    np.testing.assert_allclose(res.alpha.T, alpha, rtol=1e-9)
+    np.testing.assert_allclose(res.cntm, cntm, rtol=1e-9)
+    np.testing.assert_allclose(res.flux, flux, rtol=1e-9)
+    assert res.line_evals == ev - 0  # lines + reference-wavelength lines
+
+
+def test_synthesize_mixed_error_budget(ctx, cfg0, oracle_lib):
+    from korg_gb300.data import stark_profiles
+    from korg_gb300.synthesize import synthesize_prepared
+    flux, cntm, _, _, _ = oracle_lib.synthesize(cfg0, cfg0.linelist, cfg0.linelist5, stark_profiles(),
+                                                cfg0.wls.all_wls, nthreads=NT)
+    res = synthesize_prepared(cfg0, precision="mixed", ctx=ctx)
+    err = np.max(np.abs(res.flux / flux - 1))
+    rms = np.sqrt(np.mean((res.flux / res.cntm - flux / cntm) ** 2))
+    print(f"mixed: max rel flux err {err:.3e}, rectified RMS {rms:.3e}")
+    assert err <= 1e-4
+    np.testing.assert_allclose(res.cntm, cntm, rtol=1e-9)  # continuum transfer stays FP64
+
+
+def test_synthesize_multi_range_and_determinism(ctx, oracle_lib):
+    from korg_gb300 import synthetic
+    from korg_gb300.data import stark_profiles
+    from korg_gb300.synthesize import synthesize_prepared
+    w = synthetic.config0(n_lines=400)
+    w.wavelengths = [(5000, 5020), (5050, 5070)]
+    inp = synthetic.prepare(w)
+    flux, cntm, _, _, _ = oracle_lib.synthesize(inp, inp.linelist, inp.linelist5, stark_profiles(),
+                                                inp.wls.all_wls, nthreads=NT)
+    r1 = synthesize_prepared(inp, precision="fp64", ctx=ctx)
+    np.testing.assert_allclose(r1.flux, flux, rtol=1e-9)
+    a = synthesize_prepared(inp, precision="mixed", ctx=ctx)
+    b = synthesize_prepared(inp, precision="mixed", ctx=ctx)
+    assert np.array_equal(a.flux, b.flux)  # no atomics on alpha: bitwise reproducible
+
+
+def test_synthesize_device_pointers_match_host(ctx, cfg0):
+    """korg_synthesize_dev on torch-allocated device buffers gives the host call's answer."""
+    torch = pytest.importorskip("torch")
+    from korg_gb300 import _lib
+    from korg_gb300.synthesize import synthesize_prepared
+    host = synthesize_prepared(cfg0, precision="mixed", ctx=ctx)
+    dev = torch.device("cuda:0")
+    keep = []
+
+    def d(a, dt=torch.float64):
+        t = torch.as_tensor(np.ascontiguousarray(a)).to(dt).to(dev)
+        keep.append(t)
+        return C.cast(t.data_ptr(), C.POINTER(C.c_double)) if dt == torch.float64 else \
+            C.cast(t.data_ptr(), C.POINTER(C.c_int32))
+
+    def lines(ll):
+        return _lib.Lines(len(ll), d(ll.wl), d(ll.log_gf), d(ll.E_lower), d(ll.gamma_rad), d(ll.gamma_stark),
+                          d(ll.vdW1), d(ll.vdW2), d(ll.mass), d(ll.is_mol, torch.int32), d(ll.species_idx, torch.int32))
+
+    L = len(cfg0.T)
+    lay = _lib.Layers(L, cfg0.n_div_U.shape[0], d(cfg0.T), d(cfg0.ne), d(cfg0.n_eff_vdW), d(cfg0.xi), d(cfg0.n_div_U))
+    s = _lib.SynthInputs(lay, d(cfg0.tau_ref), d(cfg0.alpha_ref_cntm), d(cfg0.nH_I), d(cfg0.nHe_I), d(cfg0.UH_I),
+                         cfg0.ref_wl, _lib.Cntm(len(cfg0.cntm_knots), d(cfg0.cntm_knots), d(cfg0.cntm_vals)),
+                         1, int(cfg0.use_MHD), cfg0.hydrogen_window, cfg0.cutoff_threshold)
+    l1, l5 = lines(cfg0.linelist), lines(cfg0.linelist5)
+    w = torch.as_tensor(cfg0.wls.all_wls).to(dev)
+    flux = torch.empty(len(cfg0.wls), dtype=torch.float64, device=dev)
+    cntm = torch.empty_like(flux)
+    stream = torch.cuda.current_stream().cuda_stream
+    rc = ctx.lib.korg_synthesize_dev(ctx.h, C.byref(s), C.byref(l1), C.byref(l5), w.data_ptr(), len(w), 1,
+                                     flux.data_ptr(), cntm.data_ptr(), None, stream)
+    assert rc == 0, ctx.lib.korg_last_error(ctx.h)
+    torch.cuda.synchronize()
+    assert np.array_equal(flux.cpu().numpy(), host.flux)
+    assert np.array_equal(cntm.cpu().numpy(), host.cntm)

@@ -1,0 +1,111 @@
+"""Host-side pieces on CPU: wavelength grids, splines, HDF5 reader, line conversion rules, the
+C ABI's exported symbols."""
+import os
+import re
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_wavelengths_correctly_rounded():
+    from korg_gb300.wavelengths import Wavelengths
+    w = Wavelengths((5000, 5100))
+    assert len(w) == 10001
+    c = Fraction(1e-8)
+    for k in range(0, 10001, 97):
+        assert float(Fraction(500000 + k, 100) * c) == w[k]
+    w2 = Wavelengths([(3000, 3001), (4000, 4001, 0.5)])
+    assert len(w2) == 101 + 3
+    assert w2.searchsortedfirst(3000.5) == 50
+    assert w2.searchsortedlast(3500) == 100  # in the gap: last point of the first range
+    assert w2.searchsortedfirst(3500) == 101
+    with pytest.raises(ValueError):
+        Wavelengths([(5000, 5100), (4000, 4100)])
+
+
+def test_cubic_spline_natural():
+    from korg_gb300.cubic_spline import CubicSpline
+    x = np.linspace(0, 3, 13)
+    s = CubicSpline(x, np.sin(x))
+    xs = np.linspace(0, 3, 101)
+    assert np.max(np.abs(s(xs) - np.sin(xs))) < 2e-3
+    assert s(x[5]) == pytest.approx(np.sin(x[5]), abs=1e-15)
+    with pytest.raises(ValueError):
+        s(3.5)
+    assert CubicSpline(x, np.sin(x), extrapolate=True)(3.5) == pytest.approx(np.sin(3.0))
+
+
+def test_hdf5_reader_golden_attributes():
+    from korg_gb300 import hdf5lite
+    path = "/root/reference/test/data/lyman_absorption.h5"
+    if not os.path.exists(path):
+        pytest.skip("reference data not present")
+    f = hdf5lite.File(path)
+    g = np.load(os.path.join(ROOT, "tests", "golden", "lyman_absorption.npz"))
+    np.testing.assert_array_equal(f.read("profile"), g["profile"])
+    assert f["profile"].attrs["T"] == 9000.0
+
+
+def test_line_conversion_rules():
+    """Korg's Line constructor rules (src/linelist.jl:56-100)."""
+    from korg_gb300.linelist import make_line, approximate_radiative_gamma
+    l = make_line(5000.0, -1.0, "Fe I", 2.0, 1e8, 1e-6, -7.5)
+    assert l[0] == 5000.0 * 1e-8 and l[6] == pytest.approx(10 ** -7.5) and l[7] == -1
+    l = make_line(5000.0, -1.0, "Fe I", 2.0, 1e8, 1e-6, 0.0)
+    assert l[6] == 0.0 and l[7] == -1
+    l = make_line(5000.0, -1.0, "Fe I", 2.0, 1e8, 1e-6, 300.25)  # packed ABO
+    assert l[6] == pytest.approx(300 * 5.29177210903e-9 ** 2) and l[7] == pytest.approx(0.25)
+    l = make_line(5e-5, -1.0, "Fe I", 2.0, None, 1e-6, (1e-14, 0.3))
+    assert l[4] == pytest.approx(approximate_radiative_gamma(5e-5, -1.0))
+    l = make_line(5e-5, -1.0, "CO", 1.0, 1e8)  # molecules: no Stark / vdW
+    assert l[5] == 0.0 and l[6] == 0.0
+
+
+def test_alpha5000_linelist():
+    from korg_gb300.linelist import alpha_5000_linelist
+    ll = alpha_5000_linelist()
+    assert len(ll) == 409 and ll.is_sorted()
+    assert np.all(ll.wl > 4.97e-5) and np.all(ll.wl < 5.03e-5)
+
+
+def test_filter_linelist():
+    """src/synthesize.jl:331-350 against a naive filter (test/synthesize.jl:89-110)."""
+    from korg_gb300 import synthetic
+    from korg_gb300.linelist import filter_linelist
+    from korg_gb300.wavelengths import Wavelengths
+    ll = synthetic.synthetic_linelist(5000, 4000, 7000, seed=3)
+    w = Wavelengths([(4500, 4600), (5000, 5050), (6000, 6100)])
+    f = filter_linelist(ll, w, 10e-8)
+    naive = np.zeros(len(ll), bool)
+    for a, b in w.eachwindow():
+        naive |= (ll.wl >= a - 10e-8) & (ll.wl <= b + 10e-8)
+    np.testing.assert_array_equal(f.wl, ll.wl[naive])
+
+
+def test_header_symbols_exported():
+    """Every KORG_API function declared in include/korg_gb300.h is exported by the library."""
+    import subprocess
+    from korg_gb300 import _lib
+    import build as korg_build
+    hdr = open(os.path.join(ROOT, "include", "korg_gb300.h")).read()
+    declared = set(re.findall(r"KORG_API\s+[\w\s\*]+?\b(korg_\w+)\s*\(", hdr))
+    assert declared == set(_lib.exported_symbols())
+    korg_build.build()
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True, text=True, check=True)
+    exported = set(re.findall(r"\bT\s+(korg_\w+)", out.stdout))
+    assert declared <= exported, declared - exported
+    import ctypes
+    ctypes.CDLL(_lib.LIB_PATH)  # loads without a GPU
+
+
+def test_no_oracle_in_product():
+    """The product package never imports or links the oracle."""
+    pkg = os.path.join(ROOT, "korg.jl_gb300")
+    for dirpath, _, files in os.walk(pkg):
+        for fn in files:
+            if fn.endswith((".py", ".cu", ".cuh", ".h", ".jl")):
+                src = open(os.path.join(dirpath, fn)).read()
+                assert "korg_oracle" not in src and "import oracle" not in src, fn
