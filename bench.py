@@ -25,7 +25,9 @@ sys.path.insert(0, os.path.join(ROOT, "korg.jl_gb300"))
 
 METRIC = "spectra/s & line-layer-lambda evals/s, mixed vs plain FP64 at 1e-4 flux err"
 FLOP_PER_EVAL = 24  # FP32 flop per Voigt evaluation (Harris branch, FMA = 2)
-CPU_SAMPLE = (4000.0, 4350.0)  # A: bounded sample of the workload for the CPU baseline
+# bounded sample of the workload for the CPU baseline: 20 windows of 70 A spread evenly over
+# 3000-10000 A (20% of the grid)
+CPU_SAMPLE = [(3140.0 + 350.0 * k, 3210.0 + 350.0 * k) for k in range(20)]
 
 
 def parse():
@@ -35,6 +37,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="korg", choices=["korg", "reference"])
     ap.add_argument("--lines", type=int, default=300_000)
+    ap.add_argument("--wl", type=float, nargs=2, default=[3000.0, 10000.0],
+                    help="wavelength range in A (the full workload is 3000-10000)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     return ap.parse_args()
@@ -42,28 +46,35 @@ def parse():
 
 def workload(n_lines, wl=(3000, 10000)):
     from korg_gb300 import synthetic
-    return synthetic.config1(n_lines=n_lines, wl=wl)
+    return synthetic.config1(n_lines=n_lines, wl=tuple(wl))
 
 
-def cpu_sample(n_lines, threads):
-    """Time the oracle on the CPU sample; returns (spectra/s extrapolated, seconds, evals, info)."""
+def cpu_sample(n_lines, threads, _cache={}):
+    """Time the oracle on the CPU sample; returns (spectra/s extrapolated, seconds, evals, info).
+
+    The sample is the full workload (all lines, the same continuum and atmosphere) evaluated on
+    20% of the grid points: 20 windows of 70 A spread evenly over 3000-10000 A."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     from korg_gb300 import synthetic
     from korg_gb300.data import stark_profiles
+    from korg_gb300.wavelengths import Wavelengths
     oracle.build()
-    w = workload(n_lines)
-    full_points = 700_001
-    w.wavelengths = CPU_SAMPLE
-    inp = synthetic.prepare(w)
+    key = n_lines
+    if key not in _cache:
+        inp = synthetic.prepare(workload(n_lines))
+        full_points = len(inp.wls)
+        inp.wls = Wavelengths(CPU_SAMPLE)
+        _cache[key] = (inp, full_points)
+    inp, full_points = _cache[key]
     frac = len(inp.wls) / full_points
     t0 = time.perf_counter()
     _, _, _, _, ev = oracle.synthesize(inp, inp.linelist, inp.linelist5, stark_profiles(), inp.wls.all_wls,
                                        nthreads=threads)
     dt = time.perf_counter() - t0
-    return frac / dt, dt, ev, (f"{CPU_SAMPLE[0]:.0f}-{CPU_SAMPLE[1]:.0f} A of the workload "
-                               f"({len(inp.wls)} points, {len(inp.linelist)} lines + H lines, fraction "
-                               f"{frac:.4f} of the grid); spectra/s = fraction / seconds")
+    return frac / dt, dt, ev, (f"the full workload ({len(inp.linelist)} lines, H lines) evaluated on 20 windows "
+                               f"of 70 A spread over 3000-10000 A ({len(inp.wls)} of {full_points} points, "
+                               f"fraction {frac:.4f}); spectra/s = fraction / seconds")
 
 
 class Clocks:
@@ -199,7 +210,7 @@ def run_korg(args):
     korg_build.build()
 
     t0 = time.perf_counter()
-    work = workload(args.lines)
+    work = workload(args.lines, args.wl)
     inp = synthetic.prepare(work)
     host_prep_s = time.perf_counter() - t0
 
@@ -321,8 +332,8 @@ def run_korg(args):
         "dtype": "f32 profiles + f64 tau/flux (mixed)",
         "data": "synthetic (seeded line list and stand-in atmosphere)",
         "config": {"workload": "full optical synthesis: 56 layers (Teff 5800, logg 4.4, [M/H] 0), "
-                               f"{args.lines} atomic lines + hydrogen lines, 3000-10000 A @ 0.01 A "
-                               f"({nwl} points)",
+                               f"{args.lines} atomic lines + hydrogen lines, {args.wl[0]:.0f}-{args.wl[1]:.0f} A "
+                               f"@ 0.01 A ({nwl} points)",
                    "precision": "mixed", "l2": "flushed (256 MiB write) between steps; alpha (314 MB) > L2",
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
                    "host_prep_s": host_prep_s},

@@ -31,6 +31,9 @@ enum { HK_OFF = 0, HK_STARK = 1, HK_STARK_ABO = 2, HK_BRACKETT = 3 };
 struct HRec {
     double nu0, amp, invF0, F0;
     double wl0, inv_s, a, scale;   // ABO Voigt (kind 2) or Brackett grid start/step (kind 3)
+    float nu0_hi, nu0_lo;          // mixed precision: line centre frequency as an FP32 pair
+    float invF0_f, amp_f;
+    float4 abo32;                  // ABO constants packed for profile32x
     int32_t lb, ub, kind, nD;
 };
 
@@ -60,7 +63,7 @@ __global__ void hline_prep_kernel(StarkDev st, HLayers hl, const double* wls, in
     const int L = hl.L;
     if (idx >= st.ntrans * L) return;
     const int t = idx / L, l = idx % L;
-    HRec r;
+    HRec r = {};
     r.kind = HK_OFF;
     r.lb = 0;
     r.ub = -1;
@@ -75,8 +78,14 @@ __global__ void hline_prep_kernel(StarkDev st, HLayers hl, const double* wls, in
         const double wt = (T - kT[i]) / (kT[i + 1] - kT[i]);
         const double wn = (ne - kN[j]) / (kN[j + 1] - kN[j]);
         const double* L0 = st.lambda0 + st.l_off[t];
-        double wl0 = (1 - wt) * (1 - wn) * L0[j * nT + i] + wt * (1 - wn) * L0[j * nT + i + 1] +
-                     (1 - wt) * wn * L0[(j + 1) * nT + i] + wt * wn * L0[(j + 1) * nT + i + 1];  // :104
+        // :104 bilinear line centre, every operation rounded separately (no FMA contraction):
+        // table centres sit on 0.01 A multiples, so centre +- window often lands exactly on a
+        // grid point and the window edge is decided by the last bit
+        const double ut = __dsub_rn(1.0, wt), un = __dsub_rn(1.0, wn);
+        double wl0 = __dmul_rn(__dmul_rn(ut, un), L0[j * nT + i]);
+        wl0 = __dadd_rn(wl0, __dmul_rn(__dmul_rn(wt, un), L0[j * nT + i + 1]));
+        wl0 = __dadd_rn(wl0, __dmul_rn(__dmul_rn(ut, wn), L0[(j + 1) * nT + i]));
+        wl0 = __dadd_rn(wl0, __dmul_rn(__dmul_rn(wt, wn), L0[(j + 1) * nT + i + 1]));
         const int lo = st.lower[t], up = st.upper[t];
         const double beta = 1 / (KBOLTZ_EV * T);
         const double w = use_MHD ? hummer_mihalas_w(double(up), hl.nH[l], hl.nHe[l], ne) : 1.0;
@@ -108,6 +117,16 @@ __global__ void hline_prep_kernel(StarkDev st, HLayers hl, const double* wls, in
         r.nu0 = C_CGS / (wl0);  // :140 (the ABO centre replaces the interpolated one)
         r.F0 = 1.25e-9 * pow(ne, 2.0 / 3.0);
         r.invF0 = 1 / r.F0;
+        r.nu0_hi = float(r.nu0);
+        r.nu0_lo = float(r.nu0 - double(r.nu0_hi));
+        r.invF0_f = float(r.invF0);
+        r.amp_f = float(amp);
+        if (r.kind == HK_STARK_ABO) {
+            const double sig = 1 / (r.inv_s * SQRT_2), gam = r.a / r.inv_s;
+            const float af = float(r.a);
+            r.abo32 = make_float4(float(2 * sig * sig), af,
+                                  af <= 0.2f ? float(r.a / SQRT_PI * r.scale) : float(1 / (gam * gam)), float(r.scale));
+        }
         // profile table at (T, ne) along the delta-nu knots
         const double* P = st.logP + st.p_off[t];
         double* Q = Qbase + (int64_t(t) * L + l) * HND_MAX;
@@ -210,7 +229,7 @@ __global__ void __launch_bounds__(256) brackett_prep_kernel(HLayers hl, int ntra
     const double window = 5 * fmax(sdop, stark_width);
     const double wlmin = wls[0], wlmax = wls[nwl - 1];
     const double wstart = fmax(wlmin, wl0 - window), wend = fmin(wl0 + window, wlmax);
-    HRec r;
+    HRec r = {};
     r.kind = HK_OFF;
     r.lb = 0;
     r.ub = -1;
@@ -311,6 +330,7 @@ __global__ void __launch_bounds__(256) brackett_prep_kernel(HLayers hl, int ntra
         r.kind = lb <= ub ? HK_BRACKETT : HK_OFF;
         r.wl0 = wstart;  // grid start
         r.inv_s = step;  // grid step
+        r.a = 1 / step;
         out.rec[int64_t(slot) * L + l] = r;
         if (lb <= ub) {
             atomicMin(out.ulb + slot, r.lb);
@@ -345,6 +365,7 @@ __global__ void __launch_bounds__(512) hline_tile_kernel(HTileArgs a) {
     const double wl = live ? a.wls[jg] : 1.0;
     const double nu = C_CGS / wl;                // :78
     const double dnudl = C_CGS / (wl * wl);      // :79
+    const float nu_hi = float(nu), nu_lo = float(nu - double(nu_hi)), dnudl_f = float(dnudl);
     double acc[KMAX];
 #pragma unroll
     for (int k = 0; k < KMAX; k++) acc[k] = 0.0;
@@ -362,7 +383,7 @@ __global__ void __launch_bounds__(512) hline_tile_kernel(HTileArgs a) {
             if (r.kind == HK_OFF || jg < r.lb || jg > r.ub) continue;
             if (r.kind == HK_BRACKETT) {
                 // linear_interpolation over the 201-point range grid (:249, :160)
-                const double u = (wl - r.wl0) / r.inv_s;
+                const double u = MIXED ? (wl - r.wl0) * r.a : (wl - r.wl0) / r.inv_s;
                 int i = int(floor(u));
                 i = i < 0 ? 0 : (i > BR_NP - 2 ? BR_NP - 2 : i);
                 const double d = u - i;
@@ -370,23 +391,16 @@ __global__ void __launch_bounds__(512) hline_tile_kernel(HTileArgs a) {
                 acc[k] += (q[i] * (1 - d) + q[i + 1] * d) * r.amp;
                 continue;
             }
-            if (r.kind == HK_STARK_ABO) {  // :136
-                if (MIXED) {
-                    float4 p;
-                    p.x = float(r.inv_s);
-                    p.y = float(r.a);
-                    p.z = float(r.scale);
-                    p.w = p.y <= 0.2f ? float(r.a / SQRT_PI * r.scale) : float(1.0 / (r.a * r.a));
-                    acc[k] += double(profile32(p, float(fabs(wl - r.wl0))));
-                } else {
-                    acc[k] += voigt64(r.a, fabs(wl - r.wl0) * r.inv_s) * r.scale;
-                }
-            }
-            // :140-143 Stehle-Hutcheon Stark profile
             const int nDt = r.nD;
             if (MIXED) {
-                const float sd = float(fabs(nu - r.nu0)) * float(r.invF0);
-                const float x = __logf(sd);
+                float v32 = 0.f;
+                if (r.kind == HK_STARK_ABO) {  // :136
+                    const float x = float(fabs(wl - r.wl0));
+                    v32 = profile32x(r.abo32, x, __fdividef(1.f, x * x));
+                }
+                // :140-143, frequency offset from FP32 pairs (exact difference of the high parts)
+                const float dnu = fabsf((nu_hi - r.nu0_hi) + (nu_lo - r.nu0_lo));
+                const float x = __logf(dnu * r.invF0_f);
                 const float* Q = a.Q32 + (int64_t(t) * L + l) * HND_MAX;
                 float v;
                 if (!(x > kd32[1])) {
@@ -402,15 +416,16 @@ __global__ void __launch_bounds__(512) hline_tile_kernel(HTileArgs a) {
                     const float w = (x - kd32[lo]) / (kd32[lo + 1] - kd32[lo]);
                     v = (1.f - w) * Q[lo] + w * Q[lo + 1];
                 }
-                acc[k] += double(__expf(v) * float(dnudl) * float(r.amp));
+                acc[k] += double(v32 + __expf(v) * dnudl_f * r.amp_f);
             } else {
-                double sd = fabs(nu - r.nu0) / r.F0;
+                if (r.kind == HK_STARK_ABO) acc[k] += voigt64(r.a, fabs(wl - r.wl0) * r.inv_s) * r.scale;  // :136
+                double sd = fabs(nu - r.nu0) / r.F0;  // :141
                 sd = sd + (sd == 0) * 2.2250738585072014e-308;  // _zero2epsilon
                 const double x = log(sd);
                 const double* Q = a.Q + (int64_t(t) * L + l) * HND_MAX;
                 double v;
                 if (!(x > kd[1])) {
-                    v = Q[1];  // first interval: weight of the -floatmax knot rounds to 0
+                    v = Q[1];  // first interval: the weight of the -floatmax knot rounds to 0
                 } else if (x >= kd[nDt - 1]) {
                     v = Q[nDt - 1];  // flat extrapolation
                 } else {
@@ -422,7 +437,7 @@ __global__ void __launch_bounds__(512) hline_tile_kernel(HTileArgs a) {
                     const double w = (x - kd[lo]) / (kd[lo + 1] - kd[lo]);
                     v = (1 - w) * Q[lo] + w * Q[lo + 1];
                 }
-                acc[k] += exp(v) * dnudl * r.amp;
+                acc[k] += exp(v) * dnudl * r.amp;  // :142-143
             }
         }
     }

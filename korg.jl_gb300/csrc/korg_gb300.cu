@@ -137,7 +137,7 @@ int launch_tile(korg_ctx* ctx, TileArgs ta, int G, cudaStream_t s) {
     ta.G = G;
     const int TW = G <= 4 ? 128 : 64;
     const int threads = TW * G;
-    const size_t smem = size_t(B) * L * sizeof(P) + size_t(B) * (sizeof(double) + 2 * sizeof(int32_t)) +
+    const size_t smem = size_t(B) * L * sizeof(P) + size_t(B) * (sizeof(double) + sizeof(float2) + 2 * sizeof(int32_t)) +
                         size_t(threads) * sizeof(int32_t);
     KCUDA(cudaFuncSetAttribute(line_tile_kernel<MIXED, KMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                int(smem)));
@@ -169,9 +169,9 @@ int run_line_absorption(korg_ctx* ctx, double* alpha, const double* wls, int64_t
     const int64_t pthreads = ln.n * 32;
     const unsigned pblocks = unsigned((pthreads + 255) / 256);
     if (mixed)
-        line_prep_kernel<true><<<pblocks, 256, 0, s>>>(ln, lay, static_cast<LayerConst*>(ctx->lc.p), cn, wls, nwl, cutoff, po);
+        line_prep_mixed_kernel<<<pblocks, 256, 0, s>>>(ln, lay, static_cast<LayerConst*>(ctx->lc.p), cn, wls, nwl, cutoff, po);
     else
-        line_prep_kernel<false><<<pblocks, 256, 0, s>>>(ln, lay, static_cast<LayerConst*>(ctx->lc.p), cn, wls, nwl, cutoff, po);
+        line_prep64_kernel<<<pblocks, 256, 0, s>>>(ln, lay, static_cast<LayerConst*>(ctx->lc.p), cn, wls, nwl, cutoff, po);
     KCUDA(cudaGetLastError());
     window_scan_kernel<<<1, 1024, 0, s>>>(po.lb, po.ub, ln.n, static_cast<int32_t*>(ctx->pmax.p),
                                          static_cast<int32_t*>(ctx->smin.p));

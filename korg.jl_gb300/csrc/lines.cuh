@@ -64,84 +64,186 @@ struct PrepOut {
     unsigned long long* nlines;
 };
 
-template <bool MIXED>
-__global__ void __launch_bounds__(256) line_prep_kernel(LinesDev ln, LayersDev lay, const LayerConst* lc,
-                                                        CntmDev cn, const double* wls, int64_t nwl,
-                                                        double cutoff, PrepOut out) {
+// Per-line quantities shared by every layer (line_absorption.jl:83,101,105,219).
+struct LineConst {
+    double wl, m, El, E_upper, strength, wl2c, abo_pre, v1, v2, gstark, grad;
+    bool mol;
+    int sp;
+};
+
+__device__ __forceinline__ LineConst line_const(const LinesDev& ln, int64_t i) {
+    LineConst q;
+    q.wl = ln.wl[i];
+    q.m = ln.mass[i];
+    q.El = ln.E_lower[i];
+    q.mol = ln.is_mol[i] != 0;
+    q.v1 = ln.vdW1[i];
+    q.v2 = ln.vdW2[i];
+    q.gstark = ln.gamma_stark[i];
+    q.grad = ln.gamma_rad[i];
+    q.sp = ln.species[i];
+    q.E_upper = q.El + C_CGS * HPLANCK_EV / q.wl;
+    q.strength = pow(10.0, ln.log_gf[i]) * sigma_line(q.wl);
+    q.wl2c = (q.wl * q.wl) / (C_CGS * (4 * PI));
+    q.abo_pre = (!q.mol && q.v2 != -1) ? 2 * pow(4 / PI, q.v2 / 2) * tgamma((4 - q.v2) / 2) * 1e6 * q.v1 : 0.0;
+    return q;
+}
+
+// One (line, layer) in FP64 exactly as line_absorption.jl:86-112 computes it.
+struct LineLayer64 {
+    double sigma, gamma, amp, dw, lw;
+};
+
+__device__ __forceinline__ LineLayer64 line_layer64(const LineConst& q, const LayersDev& lay, const LayerConst& c,
+                                                    const CntmDev& cn, const KnotPos& kp, double cutoff, int l) {
+    LineLayer64 r;
+    const double T = lay.T[l];
+    r.sigma = doppler_width(q.wl, T, q.m, lay.xi[l]);  // :86
+    double G = q.grad;                                 // :90-94
+    if (!q.mol) {
+        G = G + lay.ne[l] * (q.gstark * c.stark6);
+        double vdw;
+        if (q.v2 == -1) {
+            vdw = q.v1 * c.vdw3;
+        } else {
+            const double invmu = 1 / (1.008 * AMU_CGS) + 1 / q.m;
+            const double vbar = sqrt(8 * KBOLTZ_CGS * T / PI * invmu);
+            vdw = q.abo_pre * pow(vbar / 1e6, 1 - q.v2);
+        }
+        G = G + lay.n_eff_vdW[l] * vdw;
+    }
+    r.gamma = G * q.wl2c;                                                       // :99
+    const double levels = exp(-c.beta * q.El) - exp(-c.beta * q.E_upper);       // :101-102
+    r.amp = q.strength * levels * lay.n_div_U[int64_t(q.sp) * lay.L + l];      // :105-106
+    const double acntm = knot_eval(cn.vals + int64_t(l) * cn.nk, cn.nk, kp);    // :108
+    const double rho = acntm * cutoff / r.amp;
+    r.dw = inverse_gaussian_density(rho, r.sigma);                              // :109-112
+    r.lw = inverse_lorentz_density(rho, r.gamma);
+    return r;
+}
+
+__device__ __forceinline__ void store_window(const PrepOut& out, int64_t i, double lwin, double dwin, double wl,
+                                             const double* wls, int64_t nwl, int L) {
+    const double window = sqrt(lwin * lwin + dwin * dwin);   // :113
+    const int64_t lb = search_first(wls, nwl, wl - window);  // :114-115
+    const int64_t ub = search_last(wls, nwl, wl + window);
+    out.lb[i] = int32_t(lb);
+    out.ub[i] = int32_t(ub);
+    if (lb <= ub) {
+        atomicAdd(out.evals, (unsigned long long)((ub - lb + 1) * L));
+        atomicAdd(out.nlines, 1ull);
+    }
+}
+
+// FP64 prologue: one warp per line, lanes over layers.
+__global__ void __launch_bounds__(256) line_prep64_kernel(LinesDev ln, LayersDev lay, const LayerConst* lc, CntmDev cn,
+                                                          const double* wls, int64_t nwl, double cutoff, PrepOut out) {
     const int64_t i = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= ln.n) return;
     const int L = lay.L;
-    const double wl = ln.wl[i], m = ln.mass[i], El = ln.E_lower[i];
-    const bool mol = ln.is_mol[i] != 0;
-    const double v1 = ln.vdW1[i], v2 = ln.vdW2[i], gstark = ln.gamma_stark[i], grad = ln.gamma_rad[i];
-    const int sp = ln.species[i];
-    // per-line factors (line_absorption.jl:101,105)
-    const double E_upper = El + C_CGS * HPLANCK_EV / wl;
-    const double strength = pow(10.0, ln.log_gf[i]) * sigma_line(wl);
-    const double wl2c = (wl * wl) / (C_CGS * (4 * PI));
-    // ABO prefactor (line_absorption.jl:219), per line
-    double abo_pre = 0.0;
-    if (!mol && v2 != -1) abo_pre = 2 * pow(4 / PI, v2 / 2) * tgamma((4 - v2) / 2) * 1e6 * v1;
-    const KnotPos kp = knot_pos(cn.knots, cn.nk, wl);
-
+    const LineConst q = line_const(ln, i);
+    const KnotPos kp = knot_pos(cn.knots, cn.nk, q.wl);
     double dwin = 0.0, lwin = 0.0;
     for (int l = lane; l < L; l += 32) {
-        const double T = lay.T[l];
-        const LayerConst c = lc[l];
-        const double sigma = doppler_width(wl, T, m, lay.xi[l]);  // :86
-        double G = grad;                                          // :90-94
-        if (!mol) {
-            G = G + lay.ne[l] * (gstark * c.stark6);
-            double vdw;
-            if (v2 == -1) {
-                vdw = v1 * c.vdw3;
-            } else {
-                const double invmu = 1 / (1.008 * AMU_CGS) + 1 / m;
-                const double vbar = sqrt(8 * KBOLTZ_CGS * T / PI * invmu);
-                vdw = abo_pre * pow(vbar / 1e6, 1 - v2);
-            }
-            G = G + lay.n_eff_vdW[l] * vdw;
-        }
-        const double gamma = G * wl2c;                                             // :99
-        const double levels = exp(-c.beta * El) - exp(-c.beta * E_upper);          // :101-102
-        const double amp = strength * levels * lay.n_div_U[int64_t(sp) * L + l];  // :105-106
-        const double acntm = knot_eval(cn.vals + int64_t(l) * cn.nk, cn.nk, kp);   // :108
-        const double rho = acntm * cutoff / amp;
-        const double dw = inverse_gaussian_density(rho, sigma);                    // :109-112
-        const double lw = inverse_lorentz_density(rho, gamma);
-        dwin = fmax(dwin, dw);
-        lwin = fmax(lwin, lw);
-        const double inv_s = 1 / (sigma * SQRT_2);                                 // :246-248
-        const double a = gamma * inv_s;
-        const double scale = inv_s / SQRT_PI * amp;
-        if (MIXED) {
-            float4 p;
-            p.x = float(inv_s);
-            p.y = float(a);
-            p.z = float(scale);
-            p.w = (p.y <= 0.2f) ? float(a / SQRT_PI * scale) : float(1.0 / (a * a));
-            reinterpret_cast<float4*>(out.params)[i * L + l] = p;
-        } else {
-            reinterpret_cast<D4*>(out.params)[i * L + l] = D4{inv_s, a, scale, 0.0};
-        }
+        const LineLayer64 r = line_layer64(q, lay, lc[l], cn, kp, cutoff, l);
+        dwin = fmax(dwin, r.dw);
+        lwin = fmax(lwin, r.lw);
+        const double inv_s = 1 / (r.sigma * SQRT_2);  // :246-248
+        reinterpret_cast<D4*>(out.params)[i * L + l] = D4{inv_s, r.gamma * inv_s, inv_s / SQRT_PI * r.amp, 0.0};
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         dwin = fmax(dwin, __shfl_xor_sync(0xffffffffu, dwin, o));
         lwin = fmax(lwin, __shfl_xor_sync(0xffffffffu, lwin, o));
     }
-    if (lane == 0) {
-        const double window = sqrt(lwin * lwin + dwin * dwin);  // :113
-        const int64_t lb = search_first(wls, nwl, wl - window);  // :114-115
-        const int64_t ub = search_last(wls, nwl, wl + window);
-        out.lb[i] = int32_t(lb);
-        out.ub[i] = int32_t(ub);
-        if (lb <= ub) {
-            atomicAdd(out.evals, (unsigned long long)((ub - lb + 1) * L));
-            atomicAdd(out.nlines, 1ull);
-        }
+    if (lane == 0) store_window(out, i, lwin, dwin, q.wl, wls, nwl, L);
+}
+
+// FP32 forms of line_absorption.jl:140-161 (used to locate the widest layers)
+__device__ __forceinline__ float inverse_gaussian32(float rho, float sigma) {
+    if (rho > 1.f / (2.5066282746f * sigma)) return 0.f;
+    return sigma * sqrtf(-2.f * __logf(2.5066282746f * sigma * rho));
+}
+__device__ __forceinline__ float inverse_lorentz32(float rho, float gamma) {
+    if (rho > 1.f / (3.14159265f * gamma)) return 0.f;
+    return sqrtf(fmaxf(gamma / (3.14159265f * rho) - gamma * gamma, 0.f));
+}
+
+__device__ __forceinline__ void argmax_reduce(float& v, int& idx) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, v, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, idx, o);
+        if (ov > v || (ov == v && oi < idx)) { v = ov; idx = oi; }
     }
+}
+
+// Mixed-precision prologue.  sigma, gamma and the profile constants are FP32; the line
+// strength (Boltzmann factor, 10^loggf sigma_line, n/U) is FP64 (line_absorption.jl:101-106).
+// The window is the FP64 window of the reference rule: FP32 locates the layers with the widest
+// Gaussian and Lorentzian windows, and those two layers are re-evaluated in FP64.
+// Packed constants: {c = 1/v-scale^2 = 2 sigma^2, a, w, scale} with scale = amp/(sigma sqrt(2 pi))
+// and w = a/sqrt(pi)*scale (a <= 0.2, asymptotic wing) or 1/gamma^2 (a > 0.2, far Lorentz).
+__global__ void __launch_bounds__(256) line_prep_mixed_kernel(LinesDev ln, LayersDev lay, const LayerConst* lc,
+                                                              CntmDev cn, const double* wls, int64_t nwl,
+                                                              double cutoff, PrepOut out) {
+    const int64_t i = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= ln.n) return;
+    const int L = lay.L;
+    const LineConst q = line_const(ln, i);
+    const KnotPos kp = knot_pos(cn.knots, cn.nk, q.wl);
+    const float wlc = float(q.wl / C_CGS), m32 = float(q.m), wl2c = float(q.wl2c);
+    const float k_m = float(KBOLTZ_CGS / q.m);
+    float dmax = -1.f, lmax = -1.f;
+    int dl = 0, ll = 0;
+    for (int l = lane; l < L; l += 32) {
+        const LayerConst c = lc[l];
+        const float T = float(lay.T[l]);
+        const float xi = float(lay.xi[l]);
+        const float sigma = wlc * sqrtf(k_m * T + 0.5f * xi * xi);
+        float G = float(q.grad);
+        if (!q.mol) {
+            float vdw;
+            if (q.v2 == -1) {
+                vdw = float(q.v1) * float(c.vdw3);
+            } else {
+                const float invmu = float(1 / (1.008 * AMU_CGS)) + 1.f / m32;
+                const float vbar = sqrtf(float(8 * KBOLTZ_CGS / PI) * T * invmu);
+                vdw = float(q.abo_pre) * powf(vbar * 1e-6f, float(1 - q.v2));
+            }
+            G = G + float(lay.ne[l]) * (float(q.gstark) * float(c.stark6)) + float(lay.n_eff_vdW[l]) * vdw;
+        }
+        const float gamma = G * wl2c;
+        const double levels = exp(-c.beta * q.El) - exp(-c.beta * q.E_upper);   // FP64 line strength
+        const float amp = float(q.strength * levels * lay.n_div_U[int64_t(q.sp) * L + l]);
+        const float acntm = float(knot_eval(cn.vals + int64_t(l) * cn.nk, cn.nk, kp));
+        const float rho = acntm * float(cutoff) / amp;
+        const float dw = inverse_gaussian32(rho, sigma), lw = inverse_lorentz32(rho, gamma);
+        if (dw > dmax) { dmax = dw; dl = l; }
+        if (lw > lmax) { lmax = lw; ll = l; }
+        const float s = 1.f / (sigma * 1.41421356f);
+        const float a = gamma * s;
+        const float scale = s * 0.56418958f * amp;  // 1/sqrt(pi)
+        float4 p;
+        p.x = 2.f * sigma * sigma;
+        p.y = a;
+        p.z = (a <= 0.2f) ? a * 0.56418958f * scale : 1.f / (gamma * gamma);
+        p.w = scale;
+        reinterpret_cast<float4*>(out.params)[i * L + l] = p;
+    }
+    argmax_reduce(dmax, dl);
+    argmax_reduce(lmax, ll);
+    // exact FP64 window at the two widest layers (lanes 0 and 1 in parallel)
+    double w = 0.0;
+    if (lane < 2) {
+        const int l = lane == 0 ? dl : ll;
+        const LineLayer64 r = line_layer64(q, lay, lc[l], cn, kp, cutoff, l);
+        w = lane == 0 ? r.dw : r.lw;
+    }
+    const double lwin = __shfl_sync(0xffffffffu, w, 1);
+    if (lane == 0) store_window(out, i, lwin, w, q.wl, wls, nwl, L);
 }
 
 // Running max of ub and running min of lb over lines (empty windows contribute nothing), one
@@ -225,7 +327,8 @@ __global__ void __launch_bounds__(512) line_tile_kernel(TileArgs a) {
     const int L = a.L, G = a.G, B = a.stage;
     P* s_par = reinterpret_cast<P*>(smem);                                  // [B][L]
     double* s_wl = reinterpret_cast<double*>(s_par + size_t(B) * L);        // [B]
-    int32_t* s_lb = reinterpret_cast<int32_t*>(s_wl + B);                   // [B]
+    float2* s_d = reinterpret_cast<float2*>(s_wl + B);                      // [B] (centre - ref) hi, lo
+    int32_t* s_lb = reinterpret_cast<int32_t*>(s_d + B);                    // [B]
     int32_t* s_ub = s_lb + B;                                               // [B]
     int32_t* s_list = s_ub + B;                                             // [blockDim]
     __shared__ int32_t s_warp[32];
@@ -239,6 +342,11 @@ __global__ void __launch_bounds__(512) line_tile_kernel(TileArgs a) {
     const int64_t jlast = min(j0 + TW, a.nwl) - 1;
     const bool live = jg < a.nwl;
     const double wl_j = live ? a.wls[jg] : 0.0;
+    // mixed precision: wavelength offsets from the tile's first point, formed in FP64 and kept
+    // as FP32 hi + lo pairs, so |wl_j - wl0| is recovered in FP32 to about one rounding
+    const double wl_ref = a.wls[j0];
+    const float xj_hi = float(wl_j - wl_ref);
+    const float xj_lo = float((wl_j - wl_ref) - double(xj_hi));
 
     if (tid == 0) {
         s_range[0] = lower_bound_i32(a.pmax_ub, a.n, int32_t(j0));
@@ -279,34 +387,51 @@ __global__ void __launch_bounds__(512) line_tile_kernel(TileArgs a) {
                 const int64_t li = base + s_list[b0 + b];
                 const P* src = reinterpret_cast<const P*>(a.params) + li * L;
                 for (int l = lane; l < L; l += 32) s_par[b * L + l] = src[l];
-                if (lane == 0) { s_wl[b] = a.wl[li]; s_lb[b] = a.lb[li]; s_ub[b] = a.ub[li]; }
+                if (lane == 0) {
+                    const double wl0 = a.wl[li], d = wl0 - wl_ref;
+                    const float dh = float(d);
+                    s_wl[b] = wl0;
+                    s_d[b] = make_float2(dh, float(d - double(dh)));
+                    s_lb[b] = a.lb[li];
+                    s_ub[b] = a.ub[li];
+                }
             }
             __syncthreads();
             if (live) {
-                for (int b = 0; b < nb; b++) {
-                    if (jg < s_lb[b] || jg > s_ub[b]) continue;
-                    const double dx = fabs(wl_j - s_wl[b]);  // FP64 offset from the line centre
-                    const P* pr = s_par + b * L;
-                    if (MIXED) {
-                        const float x = float(dx);
+                if (MIXED) {
+                    float part[KMAX];
+#pragma unroll
+                    for (int k = 0; k < KMAX; k++) part[k] = 0.f;
+                    for (int b = 0; b < nb; b++) {
+                        if (jg < s_lb[b] || jg > s_ub[b]) continue;
+                        const float2 d = s_d[b];
+                        const float x = fabsf((xj_hi - d.x) + (xj_lo - d.y));
+                        const float t = __fdividef(1.f, x * x);
+                        const float4* pr = reinterpret_cast<const float4*>(s_par) + b * L;
 #pragma unroll
                         for (int k = 0; k < KMAX; k++) {
                             const int l = g + G * k;
-                            if (l < L) {
-                                const float term = profile32(reinterpret_cast<const float4*>(pr)[l], x);
-                                // Kahan-compensated accumulation
-                                const float y = float(term) - float(comp[k]);
-                                const float t = float(acc[k]) + y;
-                                comp[k] = Acc((t - float(acc[k])) - y);
-                                acc[k] = Acc(t);
-                            }
+                            if (l < L) part[k] += profile32x(pr[l], x, t);
                         }
-                    } else {
+                    }
+                    // batch partial sums enter the accumulators with Kahan compensation
+#pragma unroll
+                    for (int k = 0; k < KMAX; k++) {
+                        const float y = part[k] - float(comp[k]);
+                        const float tt = float(acc[k]) + y;
+                        comp[k] = Acc((tt - float(acc[k])) - y);
+                        acc[k] = Acc(tt);
+                    }
+                } else {
+                    for (int b = 0; b < nb; b++) {
+                        if (jg < s_lb[b] || jg > s_ub[b]) continue;
+                        const double dx = fabs(wl_j - s_wl[b]);
+                        const D4* pr = reinterpret_cast<const D4*>(s_par) + b * L;
 #pragma unroll
                         for (int k = 0; k < KMAX; k++) {
                             const int l = g + G * k;
                             if (l < L) {
-                                const D4 p = reinterpret_cast<const D4*>(pr)[l];
+                                const D4 p = pr[l];
                                 acc[k] += Acc(voigt64(p.y, dx * p.x) * p.z);
                             }
                         }

@@ -78,55 +78,47 @@ __device__ __forceinline__ double line_profile64(double wl0, double sigma, doubl
 }
 
 // ---------------------------------------------------------------- FP32 Voigt-Hjerting
-// Mixed-precision form of the same branches.  The per-(line, layer) constants are packed as
-// p = {1/(sigma*sqrt2), a = gamma/(sigma*sqrt2), scale = amp/(sigma*sqrt(2 pi)), w} with
-// w = a/sqrt(pi)*scale when a <= 0.2 (asymptotic wing) and w = 1/a^2 otherwise.
-// x = |lambda - lambda0| formed in FP64 and rounded.  Returns H(a, v) * scale.
-__device__ __forceinline__ float profile32(float4 p, float x) {
-    const float v = x * p.x;
+// Mixed-precision H(a, v) * scale for the wavelength-tile kernels.  Per (line, layer):
+// p = {c = 2 sigma^2 (so v^2 = x^2 / c), a, w, scale} with w = a/sqrt(pi)*scale when a <= 0.2
+// and w = 1/gamma^2 otherwise.  Per (line, wavelength), shared by all layers: x = |wl - wl0|
+// and t = 1/x^2.  In the asymptotic wing (a <= 0.2, v >= 5), which holds most evaluations of a
+// wide window, 1/v^2 = t*c and the profile costs one multiply and a short polynomial.
+__device__ __forceinline__ float harris_mod32(float a, float v, bool modified) {
     const float v2 = v * v;
+    const float H0 = __expf(-v2);
+    float H1;
+    if (v < 1.3f)
+        H1 = -1.12470432f + (-0.15516677f + (3.288675912f + (-2.34357915f + 0.42139162f * v) * v) * v) * v;
+    else if (v < 2.4f)
+        H1 = -4.48480194f + (9.39456063f + (-6.61487486f + (1.98919585f - 0.22041650f * v) * v) * v) * v;
+    else
+        H1 = __fdividef(0.554153432f + (0.278711796f + (-0.1883256872f + (0.042991293f - 0.003278278f * v) * v) * v) * v,
+                        v2 - 1.5f);
+    const float H2 = (1.f - 2.f * v2) * H0;
+    if (!modified) return H0 + (H1 + H2 * a) * a;
+    const float c2 = 1.1283791670955126f, c23 = 0.37612638903183754f;  // 2/sqrt(pi), 2/(3 sqrt(pi))
+    const float M0 = H0;
+    const float M1 = H1 + c2 * M0;
+    const float M2 = H2 - M0 + c2 * M1;
+    const float M3 = c23 * (1.f - H2) - 0.6666666666666666f * v2 * M1 + c2 * M2;
+    const float M4 = 0.6666666666666666f * v2 * v2 * M0 - c23 * M1 + c2 * M3;
+    const float psi = 0.979895023f + (-0.962846325f + (0.532770573f - 0.122727278f * a) * a) * a;
+    return psi * (M0 + (M1 + (M2 + (M3 + M4 * a) * a) * a) * a);
+}
+
+__device__ __forceinline__ float profile32x(float4 p, float x, float t) {
     const float a = p.y;
     if (a <= 0.2f) {
-        if (v >= 5.f) {
-            const float i = __fdividef(1.f, v2);
-            return p.w * i * (1.f + 1.5f * i + 3.75f * (i * i));
-        }
-        const float H0 = __expf(-v2);
-        float H1;
-        if (v < 1.3f)
-            H1 = -1.12470432f + (-0.15516677f + (3.288675912f + (-2.34357915f + 0.42139162f * v) * v) * v) * v;
-        else if (v < 2.4f)
-            H1 = -4.48480194f + (9.39456063f + (-6.61487486f + (1.98919585f - 0.22041650f * v) * v) * v) * v;
-        else
-            H1 = __fdividef(0.554153432f + (0.278711796f + (-0.1883256872f + (0.042991293f - 0.003278278f * v) * v) * v) * v,
-                            v2 - 1.5f);
-        const float H2 = (1.f - 2.f * v2) * H0;
-        return (H0 + (H1 + H2 * a) * a) * p.z;
+        const float i = t * p.x;  // 1/v^2
+        if (i <= 0.04f) return (p.z * i) * fmaf(fmaf(3.75f, i, 1.5f), i, 1.f);  // v >= 5
+        return harris_mod32(a, x * rsqrtf(p.x), false) * p.w;
     }
-    if (a <= 1.4f && a + v < 3.2f) {
-        const float H0 = __expf(-v2);
-        float H1;
-        if (v < 1.3f)
-            H1 = -1.12470432f + (-0.15516677f + (3.288675912f + (-2.34357915f + 0.42139162f * v) * v) * v) * v;
-        else if (v < 2.4f)
-            H1 = -4.48480194f + (9.39456063f + (-6.61487486f + (1.98919585f - 0.22041650f * v) * v) * v) * v;
-        else
-            H1 = __fdividef(0.554153432f + (0.278711796f + (-0.1883256872f + (0.042991293f - 0.003278278f * v) * v) * v) * v,
-                            v2 - 1.5f);
-        const float H2 = (1.f - 2.f * v2) * H0;
-        const float c2 = 1.1283791670955126f, c23 = 0.37612638903183754f;  // 2/sqrt(pi), 2/(3 sqrt(pi))
-        const float M0 = H0;
-        const float M1 = H1 + c2 * M0;
-        const float M2 = H2 - M0 + c2 * M1;
-        const float M3 = c23 * (1.f - H2) - 0.6666666666666666f * v2 * M1 + c2 * M2;
-        const float M4 = 0.6666666666666666f * v2 * v2 * M0 - c23 * M1 + c2 * M3;
-        const float psi = 0.979895023f + (-0.962846325f + (0.532770573f - 0.122727278f * a) * a) * a;
-        return psi * (M0 + (M1 + (M2 + (M3 + M4 * a) * a) * a) * a) * p.z;
-    }
-    const float r2 = v2 * p.w;
+    const float v = x * rsqrtf(p.x);
+    if (a <= 1.4f && a + v < 3.2f) return harris_mod32(a, v, true) * p.w;
+    const float r2 = (x * x) * p.z;  // v^2 / a^2 = x^2 / gamma^2
     const float au = __fdividef(0.70710678118654752f, (r2 + 1.f) * a);
     const float au2 = au * au;
-    return 0.7978845608028654f * au * (1.f + (3.f * r2 - 1.f + ((r2 - 2.f) * 15.f * r2 + 2.f) * au2) * au2) * p.z;
+    return 0.7978845608028654f * au * (1.f + (3.f * r2 - 1.f + ((r2 - 2.f) * 15.f * r2 + 2.f) * au2) * au2) * p.w;
 }
 
 // ---------------------------------------------------------------- line-parameter helpers
@@ -230,6 +222,16 @@ __device__ __forceinline__ double expint2_64(double x) {
     }
     const double invx = 1 / x;
     return exp(-x) * (1 + (-2 + (6 + (-24 + 120 * invx) * invx) * invx) * invx) * invx;
+}
+
+// E2 with exp(-x) supplied by the caller (the x >= 9 branch reuses it; same value as computing
+// it inside, RadiativeTransfer.jl:440-443)
+__device__ __forceinline__ double expint2_ex(double x, double ex) {
+    if (x >= 9) {
+        const double invx = 1 / x;
+        return ex * (1 + (-2 + (6 + (-24 + 120 * invx) * invx) * invx) * invx) * invx;
+    }
+    return expint2_64(x);
 }
 
 // RadiativeTransfer.jl:398-400 with E2(tau) and exp(-tau) supplied by the caller (they are

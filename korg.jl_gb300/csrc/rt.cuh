@@ -34,6 +34,30 @@ __device__ __forceinline__ double planck(double pre, double hc_over_wl, double T
     return pre * 1 / expm1(hc_over_wl / KBOLTZ_CGS / T);
 }
 
+// Once tau at a layer exceeds TAU_STOP, every deeper segment of that column contributes less
+// than S_max * exp(-TAU_STOP) (~1e-44 relative): the recursion stops there.
+constexpr double TAU_STOP = 100.0;
+
+// One pass of the column recursion; the continuum-only and full passes share the loop.
+struct RtPass {
+    double ib_prev, tau_prev, e2_prev, ex_prev, I;
+    bool live;
+    __device__ __forceinline__ void step(double alpha, double fac, double dlt, double S, double S_prev) {
+        const double ib = alpha * fac;
+        const double tau = tau_prev + 0.5 * (ib + ib_prev) * dlt;  // RadiativeTransfer.jl:250-251
+        const double m = (S - S_prev) / (tau - tau_prev);          // :382
+        const double b = S_prev - m * tau_prev;                    // :383
+        const double ex = exp(-tau);
+        const double e2 = expint2_ex(tau, ex);
+        I += (expint_core(tau, e2, ex, m, b) - expint_core(tau_prev, e2_prev, ex_prev, m, b));  // :384-385
+        ib_prev = ib;
+        tau_prev = tau;
+        e2_prev = e2;
+        ex_prev = ex;
+        live = tau <= TAU_STOP;
+    }
+};
+
 __global__ void __launch_bounds__(128) rt_kernel(RtArgs a) {
     extern __shared__ double s_rt[];
     const int L = a.L;
@@ -60,43 +84,19 @@ __global__ void __launch_bounds__(128) rt_kernel(RtArgs a) {
     const double* al = a.alpha + j * L;
     const double* Sc = a.S ? a.S + j * L : nullptr;
 
-    // layer 0 (tau = 0, E2(0) = 1, exp(0) = 1)
+    // layer 0: tau = 0, E2(0) = 1, exp(0) = 1
     double S_prev = Sc ? Sc[0] : planck(pre, hcw, s_T[0]);
-    double ib_prev = al[0] * s_fac[0];
-    double tau_prev = 0.0, e2_prev = 1.0, ex_prev = 1.0, I = 0;
-    double cib_prev = 0, ctau_prev = 0.0, ce2_prev = 1.0, cex_prev = 1.0, cI = 0;
-    if (two) cib_prev = knot_eval(a.cn.vals, a.cn.nk, kp) * s_fac[0];
-    for (int l = 1; l < L; l++) {
+    RtPass full{al[0] * s_fac[0], 0.0, 1.0, 1.0, 0.0, true};
+    RtPass cont{two ? knot_eval(a.cn.vals, a.cn.nk, kp) * s_fac[0] : 0.0, 0.0, 1.0, 1.0, 0.0, two};
+    for (int l = 1; l < L && (full.live || cont.live); l++) {
         const double S = Sc ? Sc[l] : planck(pre, hcw, s_T[l]);
         const double dlt = s_ltr[l] - s_ltr[l - 1];
-        {
-            const double ib = al[l] * s_fac[l];
-            const double tau = tau_prev + 0.5 * (ib + ib_prev) * dlt;  // :250-251
-            const double m = (S - S_prev) / (tau - tau_prev);          // :382
-            const double b = S_prev - m * tau_prev;                    // :383
-            const double e2 = expint2_64(tau), ex = exp(-tau);
-            I += (expint_core(tau, e2, ex, m, b) - expint_core(tau_prev, e2_prev, ex_prev, m, b));  // :384-385
-            ib_prev = ib;
-            tau_prev = tau;
-            e2_prev = e2;
-            ex_prev = ex;
-        }
-        if (two) {
-            const double ib = knot_eval(a.cn.vals + int64_t(l) * a.cn.nk, a.cn.nk, kp) * s_fac[l];
-            const double tau = ctau_prev + 0.5 * (ib + cib_prev) * dlt;
-            const double m = (S - S_prev) / (tau - ctau_prev);
-            const double b = S_prev - m * ctau_prev;
-            const double e2 = expint2_64(tau), ex = exp(-tau);
-            cI += (expint_core(tau, e2, ex, m, b) - expint_core(ctau_prev, ce2_prev, cex_prev, m, b));
-            cib_prev = ib;
-            ctau_prev = tau;
-            ce2_prev = e2;
-            cex_prev = ex;
-        }
+        if (full.live) full.step(al[l], s_fac[l], dlt, S, S_prev);
+        if (cont.live) cont.step(knot_eval(a.cn.vals + int64_t(l) * a.cn.nk, a.cn.nk, kp), s_fac[l], dlt, S, S_prev);
         S_prev = S;
     }
-    a.flux[j] = 2 * PI * (I * 1.0) * a.unit;  // :136
-    if (two) a.cntm[j] = 2 * PI * (cI * 1.0) * a.unit;
+    a.flux[j] = 2 * PI * (full.I * 1.0) * a.unit;  // :136
+    if (two) a.cntm[j] = 2 * PI * (cont.I * 1.0) * a.unit;
 }
 
 // alpha[j][l] = continuum interpolant of layer l at wl_j (src/synthesize.jl:226-252)

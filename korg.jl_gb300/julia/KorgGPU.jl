@@ -1,0 +1,178 @@
+"""
+    KorgGPU
+
+Julia binding of libkorg_gb300.so: drop-in GPU replacements for Korg.jl's hot-path functions,
+calling the C ABI declared in include/korg_gb300.h through `ccall`.
+
+    using Korg, KorgGPU
+    KorgGPU.line_absorption!(α, linelist, λs, temps, nₑ, n_densities, partition_fns, ξ, α_cntm;
+                             cutoff_threshold=3e-4, precision=:mixed)
+
+The host-side work that Korg does before each call (n/U(T) per species with Korg's own
+splines, the effective vdW perturber density, the continuum interpolants' knots and values)
+is done here in Julia exactly as Korg does it; the kernels receive plain arrays.  The library
+path comes from `ENV["KORG_GB300_LIB"]` or the in-tree build location.
+"""
+module KorgGPU
+
+using Korg
+
+const LIB = get(ENV, "KORG_GB300_LIB",
+                joinpath(@__DIR__, "..", "libkorg_gb300.so"))
+
+const KORG_FP64 = Cint(0)
+const KORG_MIXED = Cint(1)
+
+# C structs of include/korg_gb300.h (field order and types must match)
+struct CLines
+    n::Int64
+    wl::Ptr{Float64}
+    log_gf::Ptr{Float64}
+    E_lower::Ptr{Float64}
+    gamma_rad::Ptr{Float64}
+    gamma_stark::Ptr{Float64}
+    vdW1::Ptr{Float64}
+    vdW2::Ptr{Float64}
+    mass::Ptr{Float64}
+    is_mol::Ptr{Int32}
+    species::Ptr{Int32}
+end
+
+struct CLayers
+    L::Int32
+    S::Int32
+    T::Ptr{Float64}
+    ne::Ptr{Float64}
+    n_eff_vdW::Ptr{Float64}
+    xi::Ptr{Float64}
+    n_div_U::Ptr{Float64}
+end
+
+struct CCntm
+    nk::Int64
+    knots::Ptr{Float64}
+    vals::Ptr{Float64}
+end
+
+mutable struct Context
+    ptr::Ptr{Cvoid}
+end
+
+function Context(device::Integer=0)
+    out = Ref{Ptr{Cvoid}}(C_NULL)
+    rc = ccall((:korg_create, LIB), Cint, (Ptr{Ptr{Cvoid}}, Cint), out, device)
+    rc == 0 || error("korg_create failed ($rc)")
+    ctx = Context(out[])
+    finalizer(c -> ccall((:korg_destroy, LIB), Cvoid, (Ptr{Cvoid},), c.ptr), ctx)
+    ctx
+end
+
+const _ctx = Ref{Union{Nothing,Context}}(nothing)
+default_context() = (_ctx[] === nothing && (_ctx[] = Context(0)); _ctx[])
+
+function check(ctx::Context, rc)
+    if rc != 0
+        msg = unsafe_string(ccall((:korg_last_error, LIB), Cstring, (Ptr{Cvoid},), ctx.ptr))
+        rc == 1 && throw(ArgumentError(msg))
+        error("korg_gb300 error $rc: $msg")
+    end
+end
+
+_prec(p::Symbol) = p === :fp64 ? KORG_FP64 : p === :mixed ? KORG_MIXED :
+                   throw(ArgumentError("precision must be :fp64 or :mixed"))
+
+# SoA packing of a Vector{Korg.Line} (src/linelist.jl:5-14); species rows follow `species`.
+function _pack_lines(linelist, species)
+    row = Dict(s => Int32(i - 1) for (i, s) in enumerate(species))
+    wl = Float64[l.wl for l in linelist]
+    loggf = Float64[l.log_gf for l in linelist]
+    El = Float64[l.E_lower for l in linelist]
+    grad = Float64[l.gamma_rad for l in linelist]
+    gst = Float64[l.gamma_stark for l in linelist]
+    v1 = Float64[l.vdW[1] for l in linelist]
+    v2 = Float64[l.vdW[2] for l in linelist]
+    mass = Float64[Korg.get_mass(l.species) for l in linelist]
+    ismol = Int32[Korg.ismolecule(l.species) for l in linelist]
+    spec = Int32[row[l.species] for l in linelist]
+    (wl, loggf, El, grad, gst, v1, v2, mass, ismol, spec)
+end
+
+_clines(a) = CLines(length(a[1]), pointer.(a)...)
+
+# the continuum callables Korg builds in synthesize are Interpolations.jl linear interpolants
+# over the continuum grid; a constant function per layer (synthesize.jl:266) maps to nk = 1.
+function _pack_cntm(α_cntm, L, wl_probe)
+    if all(f -> f isa Function && !hasproperty(f, :itp), α_cntm)
+        return [0.0], reshape(Float64[f(wl_probe) for f in α_cntm], 1, L)
+    end
+    knots = collect(Float64, first(α_cntm).itp.knots[1])
+    vals = Matrix{Float64}(undef, length(knots), L)   # column l = layer l (vals[l * nk + k])
+    for (l, f) in enumerate(α_cntm)
+        vals[:, l] .= f.(knots)
+    end
+    knots, vals
+end
+
+"""
+    line_absorption!(α, linelist, λs, temps, nₑ, n_densities, partition_fns, ξ, α_cntm;
+                     cutoff_threshold=3e-4, precision=:fp64, ctx=default_context())
+
+GPU drop-in for `Korg.line_absorption!` (src/line_absorption.jl:33-129).
+"""
+function line_absorption!(α::Matrix{Float64}, linelist, λs::Korg.Wavelengths, temps, nₑ, n_densities,
+                          partition_fns, ξ, α_cntm; cutoff_threshold=3e-4, precision=:fp64,
+                          ctx=default_context())
+    length(linelist) == 0 && return zeros(length(λs))
+    L = length(temps)
+    species = unique([l.species for l in linelist])
+    n_div_U = Matrix{Float64}(undef, L, length(species))   # n_div_U[s * L + l]
+    for (i, s) in enumerate(species)
+        n_div_U[:, i] .= n_densities[s] ./ partition_fns[s].(log.(temps))
+    end
+    c_He = (1.38375 / 4.50711)^0.4 * (Korg.atomic_masses[2] / Korg.atomic_masses[1])^-0.3
+    c_H2 = (5.503 / 4.50711)^0.4 * 2^-0.3
+    n_eff = @. n_densities[Korg.species"H_I"] + c_He * n_densities[Korg.species"He_I"] +
+               c_H2 * n_densities[Korg.species"H2"]
+    xi = ξ isa Number ? fill(Float64(ξ), L) : collect(Float64, ξ)
+    packed = _pack_lines(linelist, species)
+    knots, vals = _pack_cntm(α_cntm, L, first(linelist).wl)
+    T = collect(Float64, temps)
+    ne = collect(Float64, nₑ)
+    wls = collect(Float64, λs.all_wls)
+    nevals = Ref{Int64}(0)
+    GC.@preserve packed n_div_U n_eff xi knots vals T ne wls begin
+        lines = Ref(_clines(packed))
+        lay = Ref(CLayers(L, length(species), pointer(T), pointer(ne), pointer(n_eff), pointer(xi),
+                          pointer(n_div_U)))
+        cn = Ref(CCntm(length(knots), pointer(knots), pointer(vals)))
+        rc = ccall((:korg_line_absorption, LIB), Cint,
+                   (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Int64, Ref{CLines}, Ref{CLayers}, Ref{CCntm},
+                    Float64, Cint, Ref{Int64}),
+                   ctx.ptr, α, wls, length(wls), lines, lay, cn, cutoff_threshold, _prec(precision), nevals)
+        check(ctx, rc)
+    end
+    nothing
+end
+
+"""
+    radiative_transfer(atm::Korg.PlanarAtmosphere, α, S, μ_points; α_ref, ctx=default_context())
+
+GPU drop-in for the default planar path of `Korg.RadiativeTransfer.radiative_transfer`
+(RadiativeTransfer.jl:62-139): anchored τ and the exponential-integral flux.
+"""
+function radiative_transfer(atm::Korg.PlanarAtmosphere, α::Matrix{Float64}, S::Matrix{Float64}, μ_points;
+                            α_ref, τ_scheme="anchored", I_scheme="linear_flux_only", ctx=default_context())
+    (τ_scheme == "anchored" && I_scheme == "linear_flux_only") ||
+        throw(ArgumentError("the GPU path implements the default planar scheme"))
+    L, nwl = size(α)
+    τ_ref = Float64[l.tau_ref for l in atm.layers]
+    aref = collect(Float64, α_ref)
+    F = Vector{Float64}(undef, nwl)
+    rc = ccall((:korg_radiative_transfer, LIB), Cint,
+               (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Int32, Int64, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+               ctx.ptr, α, S, L, nwl, τ_ref, aref, F)
+    check(ctx, rc)
+    F, reshape(F ./ 2π, 1, nwl), [1.0], [1.0]
+end
+
+end # module
