@@ -11,6 +11,8 @@
 //                 each thread owns one wavelength and a set of layers and accumulates in
 //                 registers, then adds to alpha once.
 #pragma once
+#include <type_traits>
+
 #include "physics.cuh"
 
 namespace korg {
@@ -366,9 +368,11 @@ __global__ void __launch_bounds__(512) hline_tile_kernel(HTileArgs a) {
     const double nu = C_CGS / wl;                // :78
     const double dnudl = C_CGS / (wl * wl);      // :79
     const float nu_hi = float(nu), nu_lo = float(nu - double(nu_hi)), dnudl_f = float(dnudl);
-    double acc[KMAX];
+    // FP64 accumulators (plain) or FP32 with Kahan compensation (mixed)
+    using Acc = typename std::conditional<MIXED, float, double>::type;
+    Acc acc[KMAX], comp[KMAX];
 #pragma unroll
-    for (int k = 0; k < KMAX; k++) acc[k] = 0.0;
+    for (int k = 0; k < KMAX; k++) { acc[k] = Acc(0); comp[k] = Acc(0); }
     const int64_t brQ = int64_t(a.ntrans) * L * HND_MAX;
     for (int t = 0; t < a.ntot; t++) {
         if (a.uub[t] < j0 || a.ulb[t] > jlast) continue;  // uniform across the CTA
@@ -388,7 +392,14 @@ __global__ void __launch_bounds__(512) hline_tile_kernel(HTileArgs a) {
                 i = i < 0 ? 0 : (i > BR_NP - 2 ? BR_NP - 2 : i);
                 const double d = u - i;
                 const double* q = a.Q + brQ + (int64_t(t - a.ntrans) * L + l) * BR_NP;
-                acc[k] += (q[i] * (1 - d) + q[i + 1] * d) * r.amp;
+                const double term = (q[i] * (1 - d) + q[i + 1] * d) * r.amp;
+                if (MIXED) {
+                    const float y = float(term) - float(comp[k]), tt = float(acc[k]) + y;
+                    comp[k] = Acc((tt - float(acc[k])) - y);
+                    acc[k] = Acc(tt);
+                } else {
+                    acc[k] += Acc(term);
+                }
                 continue;
             }
             const int nDt = r.nD;
@@ -416,9 +427,12 @@ __global__ void __launch_bounds__(512) hline_tile_kernel(HTileArgs a) {
                     const float w = (x - kd32[lo]) / (kd32[lo + 1] - kd32[lo]);
                     v = (1.f - w) * Q[lo] + w * Q[lo + 1];
                 }
-                acc[k] += double(v32 + __expf(v) * dnudl_f * r.amp_f);
+                const float term = v32 + __expf(v) * dnudl_f * r.amp_f;
+                const float y = term - float(comp[k]), tt = float(acc[k]) + y;
+                comp[k] = Acc((tt - float(acc[k])) - y);
+                acc[k] = Acc(tt);
             } else {
-                if (r.kind == HK_STARK_ABO) acc[k] += voigt64(r.a, fabs(wl - r.wl0) * r.inv_s) * r.scale;  // :136
+                if (r.kind == HK_STARK_ABO) acc[k] += Acc(voigt64(r.a, fabs(wl - r.wl0) * r.inv_s) * r.scale);  // :136
                 double sd = fabs(nu - r.nu0) / r.F0;  // :141
                 sd = sd + (sd == 0) * 2.2250738585072014e-308;  // _zero2epsilon
                 const double x = log(sd);
@@ -437,7 +451,7 @@ __global__ void __launch_bounds__(512) hline_tile_kernel(HTileArgs a) {
                     const double w = (x - kd[lo]) / (kd[lo + 1] - kd[lo]);
                     v = (1 - w) * Q[lo] + w * Q[lo + 1];
                 }
-                acc[k] += exp(v) * dnudl * r.amp;  // :142-143
+                acc[k] += Acc(exp(v) * dnudl * r.amp);  // :142-143
             }
         }
     }
@@ -447,7 +461,7 @@ __global__ void __launch_bounds__(512) hline_tile_kernel(HTileArgs a) {
             const int l = g + G * k;
             if (l < L) {
                 double* dst = a.alpha + jg * L + l;
-                *dst = *dst + acc[k];
+                *dst = *dst + (MIXED ? double(acc[k]) - double(comp[k]) : double(acc[k]));
             }
         }
     }

@@ -34,7 +34,7 @@ struct korg_ctx {
     cudaStream_t stream = nullptr;  // used by the host-pointer calls
     std::string err;
     // scratch arena: grown on demand, never shrunk, freed by korg_destroy
-    DevBuf lc, params, lb, ub, pmax, smin, counters;
+    DevBuf lc, params, xcore, lb, ub, pmax, smin, scanblk, counters;
     DevBuf hrec, hQ, hQ32, hulb, huub;
     DevBuf stage_dev, aref, alpha, flux, cntm;
     void* stage_host = nullptr;
@@ -109,7 +109,10 @@ void record(korg_ctx* ctx, int i, cudaStream_t s) {
     if (ctx->timing) cudaEventRecord(ctx->ev[i], s);
 }
 
+// Layers per thread (K) and layer groups per CTA (G = ceil(L/K) <= 8); layers are padded to
+// G*K.  56-layer (MARCS) atmospheres split exactly into 4 x 14.
 int layer_groups(int L, int* kmax) {
+    if (L % 14 == 0 && L / 14 <= 8) { *kmax = 14; return L / 14; }
     int G = (L + 15) / 16;
     if (G <= 8) { *kmax = 16; return G; }
     G = (L + 31) / 32;
@@ -126,19 +129,20 @@ LayersDev layers_dev(const korg_layers* y) {
 }
 
 // ------------------------------------------------------------------ line opacity
+constexpr int TILE_TW = 64;  // wavelengths per CTA of the line tile kernel
+
 template <bool MIXED, int KMAX>
 int launch_tile(korg_ctx* ctx, TileArgs ta, int G, cudaStream_t s) {
     using P = typename ParamT<MIXED>::type;
-    const int L = ta.L;
-    const size_t budget = 96 * 1024;
-    int B = int(std::min<size_t>(STAGE_LINES, budget / (size_t(L) * sizeof(P))));
-    if (B < 1) B = 1;
+    const int Lp = ta.Lp;
+    int B = MIXED ? STAGE_LINES : STAGE_LINES / 2;
     ta.stage = B;
     ta.G = G;
-    const int TW = G <= 4 ? 128 : 64;
+    const int TW = TILE_TW;
     const int threads = TW * G;
-    const size_t smem = size_t(B) * L * sizeof(P) + size_t(B) * (sizeof(double) + sizeof(float2) + 2 * sizeof(int32_t)) +
-                        size_t(threads) * sizeof(int32_t);
+    const size_t region = (std::max(size_t(B) * Lp * sizeof(P), size_t(TW) * (Lp + 1) * sizeof(double)) + 15) & ~size_t(15);
+    ta.region = int(region);
+    const size_t smem = region + size_t(B) * sizeof(LineStage) + size_t(threads) * sizeof(int32_t);
     KCUDA(cudaFuncSetAttribute(line_tile_kernel<MIXED, KMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                int(smem)));
     const int64_t tiles = (ta.nwl + TW - 1) / TW;
@@ -156,16 +160,20 @@ int run_line_absorption(korg_ctx* ctx, double* alpha, const double* wls, int64_t
     const int G = layer_groups(L, &kmax);
     if (G < 0) return set_err(ctx, KORG_EINVAL, "at most 256 layers are supported (got %d)", L);
     if (ln.n > INT32_MAX || nwl > INT32_MAX - 1) return set_err(ctx, KORG_EINVAL, "sizes exceed int32 indexing");
-    const size_t psz = mixed ? sizeof(float4) : sizeof(D4);
+    const int Lp = G * kmax;
+    const size_t psz = mixed ? sizeof(float4) : sizeof(P64);
     KCHECK(ensure(ctx, ctx->lc, sizeof(LayerConst) * L));
-    KCHECK(ensure(ctx, ctx->params, psz * size_t(ln.n) * L));
+    KCHECK(ensure(ctx, ctx->params, psz * size_t(ln.n) * Lp));
+    KCHECK(ensure(ctx, ctx->xcore, sizeof(float) * ln.n));
     KCHECK(ensure(ctx, ctx->lb, sizeof(int32_t) * ln.n));
     KCHECK(ensure(ctx, ctx->ub, sizeof(int32_t) * ln.n));
     KCHECK(ensure(ctx, ctx->pmax, sizeof(int32_t) * ln.n));
     KCHECK(ensure(ctx, ctx->smin, sizeof(int32_t) * ln.n));
+    KCHECK(ensure(ctx, ctx->scanblk, sizeof(int32_t) * 2 * ((ln.n + SCAN_CHUNK - 1) / SCAN_CHUNK)));
     auto* ctr = static_cast<unsigned long long*>(ctx->counters.p);
     layer_const_kernel<<<(L + 127) / 128, 128, 0, s>>>(lay, static_cast<LayerConst*>(ctx->lc.p));
-    PrepOut po{ctx->params.p, static_cast<int32_t*>(ctx->lb.p), static_cast<int32_t*>(ctx->ub.p), ctr, ctr + 1};
+    PrepOut po{ctx->params.p, static_cast<int32_t*>(ctx->lb.p), static_cast<int32_t*>(ctx->ub.p),
+               static_cast<float*>(ctx->xcore.p), Lp, ctr, ctr + 1};
     const int64_t pthreads = ln.n * 32;
     const unsigned pblocks = unsigned((pthreads + 255) / 256);
     if (mixed)
@@ -173,8 +181,11 @@ int run_line_absorption(korg_ctx* ctx, double* alpha, const double* wls, int64_t
     else
         line_prep64_kernel<<<pblocks, 256, 0, s>>>(ln, lay, static_cast<LayerConst*>(ctx->lc.p), cn, wls, nwl, cutoff, po);
     KCUDA(cudaGetLastError());
-    window_scan_kernel<<<1, 1024, 0, s>>>(po.lb, po.ub, ln.n, static_cast<int32_t*>(ctx->pmax.p),
-                                         static_cast<int32_t*>(ctx->smin.p));
+    const int nblk = int((ln.n + SCAN_CHUNK - 1) / SCAN_CHUNK);
+    int32_t* bmax = static_cast<int32_t*>(ctx->scanblk.p);
+    window_block_kernel<<<nblk, SCAN_THREADS, 0, s>>>(po.lb, po.ub, ln.n, bmax, bmax + nblk);
+    window_scan_kernel<<<nblk, SCAN_THREADS, 0, s>>>(po.lb, po.ub, ln.n, bmax, bmax + nblk, nblk,
+                                                    static_cast<int32_t*>(ctx->pmax.p), static_cast<int32_t*>(ctx->smin.p));
     KCUDA(cudaGetLastError());
     record(ctx, 2, s);
     TileArgs ta{};
@@ -182,6 +193,8 @@ int run_line_absorption(korg_ctx* ctx, double* alpha, const double* wls, int64_t
     ta.wls = wls;
     ta.nwl = nwl;
     ta.L = L;
+    ta.Lp = Lp;
+    ta.xcore = po.xcore;
     ta.n = ln.n;
     ta.wl = ln.wl;
     ta.params = ctx->params.p;
@@ -191,9 +204,11 @@ int run_line_absorption(korg_ctx* ctx, double* alpha, const double* wls, int64_t
     ta.smin_lb = static_cast<int32_t*>(ctx->smin.p);
     int rc;
     if (mixed)
-        rc = kmax == 16 ? launch_tile<true, 16>(ctx, ta, G, s) : launch_tile<true, 32>(ctx, ta, G, s);
+        rc = kmax == 14 ? launch_tile<true, 14>(ctx, ta, G, s)
+                        : (kmax == 16 ? launch_tile<true, 16>(ctx, ta, G, s) : launch_tile<true, 32>(ctx, ta, G, s));
     else
-        rc = kmax == 16 ? launch_tile<false, 16>(ctx, ta, G, s) : launch_tile<false, 32>(ctx, ta, G, s);
+        rc = kmax == 14 ? launch_tile<false, 14>(ctx, ta, G, s)
+                        : (kmax == 16 ? launch_tile<false, 16>(ctx, ta, G, s) : launch_tile<false, 32>(ctx, ta, G, s));
     ctx->stats_pending = true;
     return rc;
 }
@@ -203,9 +218,10 @@ int run_hydrogen(korg_ctx* ctx, double* alpha, const double* wls, int64_t nwl, c
                  int use_MHD, bool mixed, cudaStream_t s) {
     if (!ctx->have_stark) return set_err(ctx, KORG_ENOTABLES, "korg_set_stark_tables() has not been called");
     const int L = hl.L;
-    int kmax = 0;
-    const int G = layer_groups(L, &kmax);
-    if (G < 0) return set_err(ctx, KORG_EINVAL, "at most 256 layers are supported (got %d)", L);
+    // the hydrogen tile kernel interleaves layers: thread group g owns layers g, g+G, ...
+    int kmax = 16, G = (L + 15) / 16;
+    if (G > 8) { kmax = 32; G = (L + 31) / 32; }
+    if (G > 8) return set_err(ctx, KORG_EINVAL, "at most 256 layers are supported (got %d)", L);
     const int ntrans = ctx->stark.ntrans;
     const int nbr = std::max(0, ctx->n_max - 4);
     const int ntot = ntrans + nbr;
@@ -411,7 +427,7 @@ KORG_API void korg_destroy(korg_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    DevBuf* bufs[] = {&ctx->lc, &ctx->params, &ctx->lb, &ctx->ub, &ctx->pmax, &ctx->smin, &ctx->counters,
+    DevBuf* bufs[] = {&ctx->lc, &ctx->params, &ctx->xcore, &ctx->lb, &ctx->ub, &ctx->pmax, &ctx->smin, &ctx->scanblk, &ctx->counters,
                       &ctx->hrec, &ctx->hQ, &ctx->hQ32, &ctx->hulb, &ctx->huub, &ctx->stage_dev, &ctx->aref,
                       &ctx->alpha, &ctx->flux, &ctx->cntm};
     for (DevBuf* b : bufs)

@@ -20,9 +20,10 @@ namespace korg {
 constexpr int TILE_W_MAX = 128;  // wavelengths per CTA (64 when more than 4 layer groups)
 constexpr int STAGE_LINES = 32;  // lines staged in shared memory per batch (upper bound)
 
-// FP64 profile constants of one (line, layer): {1/(sigma sqrt2), a, scale, unused}
-struct alignas(32) D4 {
-    double x, y, z, w;
+// FP64 profile constants of one (line, layer): c = 2 sigma^2 (so 1/v^2 = c / x^2), w as in the
+// mixed form, inv_s = 1/(sigma sqrt2), a = gamma inv_s, scale = amp inv_s / sqrt(pi)
+struct alignas(16) P64 {
+    double c, w, inv_s, a, scale, pad;
 };
 
 struct LinesDev {
@@ -57,9 +58,12 @@ __global__ void layer_const_kernel(LayersDev lay, LayerConst* out) {
 }
 
 struct PrepOut {
-    void* params;            // [n][L] double4 (FP64) or float4 (mixed)
+    void* params;            // [n][Lp] P64 (FP64) or float4 (mixed); layers L..Lp-1 are zero padding
     int32_t* lb;             // [n]
     int32_t* ub;             // [n]
+    float* xcore;            // [n] |wl - wl0| beyond which every layer is in the asymptotic wing
+                             //     (v >= 5 with a <= 0.2); -1 when some layer has a > 0.2
+    int32_t Lp;
     unsigned long long* evals;   // running totals: evaluations, lines in window
     unsigned long long* nlines;
 };
@@ -144,20 +148,34 @@ __global__ void __launch_bounds__(256) line_prep64_kernel(LinesDev ln, LayersDev
     const int L = lay.L;
     const LineConst q = line_const(ln, i);
     const KnotPos kp = knot_pos(cn.knots, cn.nk, q.wl);
-    double dwin = 0.0, lwin = 0.0;
-    for (int l = lane; l < L; l += 32) {
+    double dwin = 0.0, lwin = 0.0, xc = 0.0;
+    const int Lp = out.Lp;
+    P64* dst = reinterpret_cast<P64*>(out.params) + i * Lp;
+    for (int l = lane; l < Lp; l += 32) {
+        if (l >= L) {
+            dst[l] = P64{1.0, 0.0, 1.0, 0.0, 0.0, 0.0};
+            continue;
+        }
         const LineLayer64 r = line_layer64(q, lay, lc[l], cn, kp, cutoff, l);
         dwin = fmax(dwin, r.dw);
         lwin = fmax(lwin, r.lw);
         const double inv_s = 1 / (r.sigma * SQRT_2);  // :246-248
-        reinterpret_cast<D4*>(out.params)[i * L + l] = D4{inv_s, r.gamma * inv_s, inv_s / SQRT_PI * r.amp, 0.0};
+        const double a = r.gamma * inv_s, scale = inv_s / SQRT_PI * r.amp;
+        const double c = 1 / (inv_s * inv_s);
+        dst[l] = P64{c, a <= 0.2 ? a / SQRT_PI * scale : 0.0, inv_s, a, scale, 0.0};
+        xc = (a <= 0.2 && xc >= 0) ? fmax(xc, 5.000005 / inv_s) : -1.0;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         dwin = fmax(dwin, __shfl_xor_sync(0xffffffffu, dwin, o));
         lwin = fmax(lwin, __shfl_xor_sync(0xffffffffu, lwin, o));
+        const double ox = __shfl_xor_sync(0xffffffffu, xc, o);
+        xc = (xc < 0 || ox < 0) ? -1.0 : fmax(xc, ox);
     }
-    if (lane == 0) store_window(out, i, lwin, dwin, q.wl, wls, nwl, L);
+    if (lane == 0) {
+        store_window(out, i, lwin, dwin, q.wl, wls, nwl, L);
+        out.xcore[i] = float(xc);
+    }
 }
 
 // FP32 forms of line_absorption.jl:140-161 (used to locate the widest layers)
@@ -196,9 +214,15 @@ __global__ void __launch_bounds__(256) line_prep_mixed_kernel(LinesDev ln, Layer
     const KnotPos kp = knot_pos(cn.knots, cn.nk, q.wl);
     const float wlc = float(q.wl / C_CGS), m32 = float(q.m), wl2c = float(q.wl2c);
     const float k_m = float(KBOLTZ_CGS / q.m);
-    float dmax = -1.f, lmax = -1.f;
+    float dmax = -1.f, lmax = -1.f, xc = 0.f;
     int dl = 0, ll = 0;
-    for (int l = lane; l < L; l += 32) {
+    const int Lp = out.Lp;
+    float4* dst = reinterpret_cast<float4*>(out.params) + i * Lp;
+    for (int l = lane; l < Lp; l += 32) {
+        if (l >= L) {
+            dst[l] = make_float4(1.f, 0.f, 0.f, 0.f);
+            continue;
+        }
         const LayerConst c = lc[l];
         const float T = float(lay.T[l]);
         const float xi = float(lay.xi[l]);
@@ -231,10 +255,18 @@ __global__ void __launch_bounds__(256) line_prep_mixed_kernel(LinesDev ln, Layer
         p.y = a;
         p.z = (a <= 0.2f) ? a * 0.56418958f * scale : 1.f / (gamma * gamma);
         p.w = scale;
-        reinterpret_cast<float4*>(out.params)[i * L + l] = p;
+        dst[l] = p;
+        // the wing test of the tile kernel uses 1/v^2 = c t <= 0.04, i.e. x >= 5 sqrt(c)
+        xc = (a <= 0.2f && xc >= 0.f) ? fmaxf(xc, 5.0001f * sqrtf(p.x)) : -1.f;
     }
     argmax_reduce(dmax, dl);
     argmax_reduce(lmax, ll);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float ox = __shfl_xor_sync(0xffffffffu, xc, o);
+        xc = (xc < 0.f || ox < 0.f) ? -1.f : fmaxf(xc, ox);
+    }
+    if (lane == 0) out.xcore[i] = xc;
     // exact FP64 window at the two widest layers (lanes 0 and 1 in parallel)
     double w = 0.0;
     if (lane < 2) {
@@ -246,47 +278,91 @@ __global__ void __launch_bounds__(256) line_prep_mixed_kernel(LinesDev ln, Layer
     if (lane == 0) store_window(out, i, lwin, w, q.wl, wls, nwl, L);
 }
 
-// Running max of ub and running min of lb over lines (empty windows contribute nothing), one
-// CTA of 1024 threads: per-thread sequential chunks, then a block scan of the chunk totals.
-__global__ void __launch_bounds__(1024) window_scan_kernel(const int32_t* lb, const int32_t* ub, int64_t n,
-                                                           int32_t* pmax_ub, int32_t* smin_lb) {
-    __shared__ int32_t s_max[1024], s_min[1024];
-    const int t = threadIdx.x, T = blockDim.x;
-    const int64_t chunk = (n + T - 1) / T;
-    const int64_t b = t * chunk, e = (b + chunk < n) ? b + chunk : n;
+// Running max of ub (prefix) and running min of lb (suffix) over the line list, in two
+// launches: per-block totals, then each block scans its chunk starting from the totals of the
+// blocks before (prefix) / after (suffix) it.  Lines with an empty window contribute nothing.
+constexpr int SCAN_THREADS = 256, SCAN_ITEMS = 8, SCAN_CHUNK = SCAN_THREADS * SCAN_ITEMS;
+
+__global__ void __launch_bounds__(SCAN_THREADS) window_block_kernel(const int32_t* lb, const int32_t* ub, int64_t n,
+                                                                    int32_t* bmax, int32_t* bmin) {
+    __shared__ int32_t s_mx[SCAN_THREADS / 32], s_mn[SCAN_THREADS / 32];
+    const int64_t base = int64_t(blockIdx.x) * SCAN_CHUNK;
     int32_t mx = -1, mn = INT32_MAX;
-    for (int64_t k = b; k < e; k++) {
-        if (lb[k] <= ub[k]) mx = max(mx, ub[k]);
+    for (int k = threadIdx.x; k < SCAN_CHUNK; k += SCAN_THREADS) {
+        const int64_t i = base + k;
+        if (i < n && lb[i] <= ub[i]) { mx = max(mx, ub[i]); mn = min(mn, lb[i]); }
     }
-    for (int64_t k = b; k < e; k++) {
-        if (lb[k] <= ub[k]) mn = min(mn, lb[k]);
+    for (int o = 16; o > 0; o >>= 1) {
+        mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
     }
-    s_max[t] = mx;
-    s_min[t] = mn;
+    if ((threadIdx.x & 31) == 0) { s_mx[threadIdx.x >> 5] = mx; s_mn[threadIdx.x >> 5] = mn; }
     __syncthreads();
-    // inclusive prefix max (forward) and suffix min (backward) over chunk totals
-    for (int o = 1; o < T; o <<= 1) {
-        int32_t a = (t >= o) ? s_max[t - o] : -1;
-        int32_t c = (t + o < T) ? s_min[t + o] : INT32_MAX;
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < SCAN_THREADS / 32; w++) { mx = max(mx, s_mx[w]); mn = min(mn, s_mn[w]); }
+        bmax[blockIdx.x] = mx;
+        bmin[blockIdx.x] = mn;
+    }
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) window_scan_kernel(const int32_t* lb, const int32_t* ub, int64_t n,
+                                                                   const int32_t* bmax, const int32_t* bmin, int nblocks,
+                                                                   int32_t* pmax_ub, int32_t* smin_lb) {
+    __shared__ int32_t s_a[SCAN_THREADS], s_b[SCAN_THREADS];
+    __shared__ int32_t s_pre, s_suf;
+    const int t = threadIdx.x, blk = blockIdx.x;
+    // totals of the blocks before / after this one
+    int32_t pre = -1, suf = INT32_MAX;
+    for (int b = t; b < blk; b += SCAN_THREADS) pre = max(pre, bmax[b]);
+    for (int b = blk + 1 + t; b < nblocks; b += SCAN_THREADS) suf = min(suf, bmin[b]);
+    for (int o = 16; o > 0; o >>= 1) {
+        pre = max(pre, __shfl_xor_sync(0xffffffffu, pre, o));
+        suf = min(suf, __shfl_xor_sync(0xffffffffu, suf, o));
+    }
+    if ((t & 31) == 0) { s_a[t >> 5] = pre; s_b[t >> 5] = suf; }
+    __syncthreads();
+    if (t == 0) {
+        for (int w = 1; w < SCAN_THREADS / 32; w++) { pre = max(pre, s_a[w]); suf = min(suf, s_b[w]); }
+        s_pre = pre;
+        s_suf = suf;
+    }
+    __syncthreads();
+    // each thread owns SCAN_ITEMS consecutive lines
+    const int64_t i0 = int64_t(blk) * SCAN_CHUNK + int64_t(t) * SCAN_ITEMS;
+    int32_t mx = -1, mn = INT32_MAX;
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        const int64_t i = i0 + k;
+        if (i < n && lb[i] <= ub[i]) { mx = max(mx, ub[i]); mn = min(mn, lb[i]); }
+    }
+    s_a[t] = mx;
+    s_b[t] = mn;
+    __syncthreads();
+    for (int o = 1; o < SCAN_THREADS; o <<= 1) {  // inclusive prefix max / suffix min over threads
+        const int32_t a = t >= o ? s_a[t - o] : -1;
+        const int32_t c = t + o < SCAN_THREADS ? s_b[t + o] : INT32_MAX;
         __syncthreads();
-        s_max[t] = max(s_max[t], a);
-        s_min[t] = min(s_min[t], c);
+        s_a[t] = max(s_a[t], a);
+        s_b[t] = min(s_b[t], c);
         __syncthreads();
     }
-    int32_t run = (t > 0) ? s_max[t - 1] : -1;
-    for (int64_t k = b; k < e; k++) {
-        if (lb[k] <= ub[k]) run = max(run, ub[k]);
-        pmax_ub[k] = run;
+    int32_t run = max(s_pre, t > 0 ? s_a[t - 1] : -1);
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        const int64_t i = i0 + k;
+        if (i >= n) break;
+        if (lb[i] <= ub[i]) run = max(run, ub[i]);
+        pmax_ub[i] = run;
     }
-    run = (t + 1 < T) ? s_min[t + 1] : INT32_MAX;
-    for (int64_t k = e - 1; k >= b; k--) {
-        if (lb[k] <= ub[k]) run = min(run, lb[k]);
-        smin_lb[k] = run;
+    run = min(s_suf, t + 1 < SCAN_THREADS ? s_b[t + 1] : INT32_MAX);
+    for (int k = SCAN_ITEMS - 1; k >= 0; k--) {
+        const int64_t i = i0 + k;
+        if (i >= n) continue;
+        if (lb[i] <= ub[i]) run = min(run, lb[i]);
+        smin_lb[i] = run;
     }
 }
 
 template <bool MIXED>
-struct ParamT { using type = D4; };
+struct ParamT { using type = P64; };
 template <>
 struct ParamT<true> { using type = float4; };
 
@@ -294,10 +370,12 @@ struct TileArgs {
     double* alpha;        // [nwl][L]
     const double* wls;
     int64_t nwl;
-    int32_t L, G, stage;  // G layer groups per CTA, lines per staging batch
+    int32_t L, Lp, G, stage;  // layers, padded layers (G * K), layer groups, lines per batch
+    int32_t region;           // bytes of the shared region for constants / the alpha tile
     int64_t n;
     const double* wl;     // line centres
     const void* params;
+    const float* xcore;
     const int32_t *lb, *ub, *pmax_ub, *smin_lb;
 };
 
@@ -320,17 +398,26 @@ __device__ __forceinline__ int64_t upper_bound_i32(const int32_t* a, int64_t n, 
     return lo;
 }
 
-template <bool MIXED, int KMAX>
+// a line staged for the current batch
+struct LineStage {
+    double wl;        // centre (FP64 path)
+    float dhi, dlo;   // centre - first wavelength of the tile, as an FP32 pair (mixed path)
+    int32_t lb, ub;
+    int32_t fast;     // the whole tile lies in the asymptotic wing of every layer
+    int32_t pad;
+};
+
+// One CTA per tile of TW = blockDim.x / G wavelengths x all layers.  Thread (j, g) owns
+// wavelength j and the K consecutive (padded) layers g*K .. g*K+K-1.
+template <bool MIXED, int K>
 __global__ void __launch_bounds__(512) line_tile_kernel(TileArgs a) {
     using P = typename ParamT<MIXED>::type;
     extern __shared__ __align__(16) unsigned char smem[];
-    const int L = a.L, G = a.G, B = a.stage;
-    P* s_par = reinterpret_cast<P*>(smem);                                  // [B][L]
-    double* s_wl = reinterpret_cast<double*>(s_par + size_t(B) * L);        // [B]
-    float2* s_d = reinterpret_cast<float2*>(s_wl + B);                      // [B] (centre - ref) hi, lo
-    int32_t* s_lb = reinterpret_cast<int32_t*>(s_d + B);                    // [B]
-    int32_t* s_ub = s_lb + B;                                               // [B]
-    int32_t* s_list = s_ub + B;                                             // [blockDim]
+    const int L = a.L, Lp = a.Lp, G = a.G, B = a.stage;
+    P* s_par = reinterpret_cast<P*>(smem);                                   // [B][Lp]
+    double* s_alpha = reinterpret_cast<double*>(smem);                       // [TW][Lp+1], at the end
+    LineStage* s_ln = reinterpret_cast<LineStage*>(smem + a.region);         // [B]
+    int32_t* s_list = reinterpret_cast<int32_t*>(s_ln + B);                  // [blockDim]
     __shared__ int32_t s_warp[32];
     __shared__ int64_t s_range[2];
 
@@ -342,9 +429,9 @@ __global__ void __launch_bounds__(512) line_tile_kernel(TileArgs a) {
     const int64_t jlast = min(j0 + TW, a.nwl) - 1;
     const bool live = jg < a.nwl;
     const double wl_j = live ? a.wls[jg] : 0.0;
-    // mixed precision: wavelength offsets from the tile's first point, formed in FP64 and kept
-    // as FP32 hi + lo pairs, so |wl_j - wl0| is recovered in FP32 to about one rounding
-    const double wl_ref = a.wls[j0];
+    const double wl_ref = a.wls[j0], wl_last = a.wls[jlast];
+    // mixed precision: offsets from the tile's first wavelength formed in FP64 and kept as
+    // FP32 hi + lo pairs, so |wl_j - wl0| is recovered in FP32 to about one rounding
     const float xj_hi = float(wl_j - wl_ref);
     const float xj_lo = float((wl_j - wl_ref) - double(xj_hi));
 
@@ -356,9 +443,9 @@ __global__ void __launch_bounds__(512) line_tile_kernel(TileArgs a) {
     const int64_t i_lo = s_range[0], i_hi = s_range[1];
 
     using Acc = typename std::conditional<MIXED, float, double>::type;
-    Acc acc[KMAX], comp[KMAX];
+    Acc acc[K], comp[K];
 #pragma unroll
-    for (int k = 0; k < KMAX; k++) { acc[k] = Acc(0); comp[k] = Acc(0); }
+    for (int k = 0; k < K; k++) { acc[k] = Acc(0); comp[k] = Acc(0); }
 
     const int warp = tid >> 5, lane = tid & 31, nwarps = nthr >> 5;
     for (int64_t base = i_lo; base <= i_hi; base += nthr) {
@@ -374,7 +461,7 @@ __global__ void __launch_bounds__(512) line_tile_kernel(TileArgs a) {
         if (tid == 0) {
             int run = 0;
             for (int w = 0; w < nwarps; w++) { int c = s_warp[w]; s_warp[w] = run; run += c; }
-            s_range[0] = run;  // reuse as the count
+            s_range[0] = run;  // reused as the count
         }
         __syncthreads();
         if (take) s_list[s_warp[warp] + __popc(m & ((1u << lane) - 1))] = int32_t(i - base);
@@ -385,38 +472,52 @@ __global__ void __launch_bounds__(512) line_tile_kernel(TileArgs a) {
             const int nb = min(B, cnt - b0);
             for (int b = warp; b < nb; b += nwarps) {
                 const int64_t li = base + s_list[b0 + b];
-                const P* src = reinterpret_cast<const P*>(a.params) + li * L;
-                for (int l = lane; l < L; l += 32) s_par[b * L + l] = src[l];
+                const P* src = reinterpret_cast<const P*>(a.params) + li * Lp;
+                for (int l = lane; l < Lp; l += 32) s_par[b * Lp + l] = src[l];
                 if (lane == 0) {
                     const double wl0 = a.wl[li], d = wl0 - wl_ref;
                     const float dh = float(d);
-                    s_wl[b] = wl0;
-                    s_d[b] = make_float2(dh, float(d - double(dh)));
-                    s_lb[b] = a.lb[li];
-                    s_ub[b] = a.ub[li];
+                    const double dist = wl0 < wl_ref ? wl_ref - wl0 : (wl0 > wl_last ? wl0 - wl_last : 0.0);
+                    const float xc = a.xcore[li];
+                    LineStage st;
+                    st.wl = wl0;
+                    st.dhi = dh;
+                    st.dlo = float(d - double(dh));
+                    st.lb = a.lb[li];
+                    st.ub = a.ub[li];
+                    st.fast = xc >= 0.f && dist > double(xc) * 1.000001;
+                    st.pad = 0;
+                    s_ln[b] = st;
                 }
             }
             __syncthreads();
             if (live) {
                 if (MIXED) {
-                    float part[KMAX];
+                    float part[K];
 #pragma unroll
-                    for (int k = 0; k < KMAX; k++) part[k] = 0.f;
+                    for (int k = 0; k < K; k++) part[k] = 0.f;
                     for (int b = 0; b < nb; b++) {
-                        if (jg < s_lb[b] || jg > s_ub[b]) continue;
-                        const float2 d = s_d[b];
-                        const float x = fabsf((xj_hi - d.x) + (xj_lo - d.y));
+                        const LineStage st = s_ln[b];
+                        if (jg < st.lb || jg > st.ub) continue;
+                        const float x = fabsf((xj_hi - st.dhi) + (xj_lo - st.dlo));
                         const float t = __fdividef(1.f, x * x);
-                        const float4* pr = reinterpret_cast<const float4*>(s_par) + b * L;
+                        const float4* pr = reinterpret_cast<const float4*>(s_par) + b * Lp + g * K;
+                        if (st.fast) {
+                            // asymptotic wing of every layer: w/v^2 (1 + 1.5/v^2 + 3.75/v^4), 1/v^2 = c t
 #pragma unroll
-                        for (int k = 0; k < KMAX; k++) {
-                            const int l = g + G * k;
-                            if (l < L) part[k] += profile32x(pr[l], x, t);
+                            for (int k = 0; k < K; k++) {
+                                const float4 p = pr[k];
+                                const float iv = t * p.x;
+                                part[k] = fmaf(p.z * iv, fmaf(fmaf(3.75f, iv, 1.5f), iv, 1.f), part[k]);
+                            }
+                        } else {
+#pragma unroll
+                            for (int k = 0; k < K; k++) part[k] += profile32x(pr[k], x, t);
                         }
                     }
                     // batch partial sums enter the accumulators with Kahan compensation
 #pragma unroll
-                    for (int k = 0; k < KMAX; k++) {
+                    for (int k = 0; k < K; k++) {
                         const float y = part[k] - float(comp[k]);
                         const float tt = float(acc[k]) + y;
                         comp[k] = Acc((tt - float(acc[k])) - y);
@@ -424,16 +525,20 @@ __global__ void __launch_bounds__(512) line_tile_kernel(TileArgs a) {
                     }
                 } else {
                     for (int b = 0; b < nb; b++) {
-                        if (jg < s_lb[b] || jg > s_ub[b]) continue;
-                        const double dx = fabs(wl_j - s_wl[b]);
-                        const D4* pr = reinterpret_cast<const D4*>(s_par) + b * L;
+                        const LineStage st = s_ln[b];
+                        if (jg < st.lb || jg > st.ub) continue;
+                        const double x = fabs(wl_j - st.wl);
+                        const P64* pr = reinterpret_cast<const P64*>(s_par) + b * Lp + g * K;
+                        if (st.fast) {
+                            const double t = 1 / (x * x);
 #pragma unroll
-                        for (int k = 0; k < KMAX; k++) {
-                            const int l = g + G * k;
-                            if (l < L) {
-                                const D4 p = pr[l];
-                                acc[k] += Acc(voigt64(p.y, dx * p.x) * p.z);
+                            for (int k = 0; k < K; k++) {
+                                const double iv = t * pr[k].c;
+                                acc[k] += Acc((pr[k].w * iv) * (1 + iv * (1.5 + 3.75 * iv)));
                             }
+                        } else {
+#pragma unroll
+                            for (int k = 0; k < K; k++) acc[k] += Acc(voigt64(pr[k].a, x * pr[k].inv_s) * pr[k].scale);
                         }
                     }
                 }
@@ -441,18 +546,17 @@ __global__ void __launch_bounds__(512) line_tile_kernel(TileArgs a) {
             __syncthreads();
         }
     }
-    if (live) {
+    // alpha += accumulated lines, staged through shared memory for coalesced updates
+    const int stride = Lp + 1;
 #pragma unroll
-        for (int k = 0; k < KMAX; k++) {
-            const int l = g + G * k;
-            if (l < L) {
-                double* dst = a.alpha + jg * L + l;
-                if (MIXED)
-                    *dst = *dst + (double(acc[k]) - double(comp[k]));
-                else
-                    *dst = *dst + double(acc[k]);
-            }
-        }
+    for (int k = 0; k < K; k++)
+        s_alpha[jl * stride + g * K + k] = MIXED ? double(acc[k]) - double(comp[k]) : double(acc[k]);
+    __syncthreads();
+    const int64_t nj = jlast - j0 + 1;
+    double* dst = a.alpha + j0 * L;
+    for (int64_t e = tid; e < nj * L; e += nthr) {
+        const int j = int(e / L), l = int(e - int64_t(j) * L);
+        dst[e] = dst[e] + s_alpha[j * stride + l];
     }
 }
 
