@@ -184,6 +184,11 @@ KORG_API int korg_synthesize_dev(korg_ctx *ctx, const korg_synth_inputs *in,
  * denominator for the profile (FP32) and transfer (FP64) kernels. */
 KORG_API int korg_probe_flops(korg_ctx *ctx, int fp64, double *tflops);
 
+/* Not a counterpart of any reference function: compares the table-driven FP64 exp and log
+ * used by the prologue and transfer kernels with the CUDA exp and log on n points; returns the
+ * largest exp error in ulps and the largest absolute log error. */
+KORG_API int korg_math_selftest(korg_ctx *ctx, int64_t n, double *max_ulp_exp, double *max_abs_log);
+
 #ifdef __cplusplus
 }
 #endif

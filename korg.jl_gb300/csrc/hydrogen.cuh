@@ -356,7 +356,7 @@ struct HTileArgs {
 };
 
 template <bool MIXED, int KMAX>
-__global__ void __launch_bounds__(512) hline_tile_kernel(HTileArgs a) {
+__global__ void __launch_bounds__(512, 1) hline_tile_kernel(HTileArgs a) {
     const int tid = threadIdx.x;
     const int L = a.L, G = a.G;
     const int TW = blockDim.x / G;

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -34,9 +35,9 @@ struct korg_ctx {
     cudaStream_t stream = nullptr;  // used by the host-pointer calls
     std::string err;
     // scratch arena: grown on demand, never shrunk, freed by korg_destroy
-    DevBuf lc, params, xcore, lb, ub, pmax, smin, scanblk, counters;
+    DevBuf lc, params, xfar, amask, lb, ub, pmax, smin, scanblk, counters;
     DevBuf hrec, hQ, hQ32, hulb, huub;
-    DevBuf stage_dev, aref, alpha, flux, cntm;
+    DevBuf stage_dev, aref, alpha, flux, cntm, math;
     void* stage_host = nullptr;
     size_t stage_host_cap = 0;
     // Stehle tables
@@ -111,6 +112,17 @@ void record(korg_ctx* ctx, int i, cudaStream_t s) {
 
 // Layers per thread (K) and layer groups per CTA (G = ceil(L/K) <= 8); layers are padded to
 // G*K.  56-layer (MARCS) atmospheres split exactly into 4 x 14.
+// Tables of the table-driven FP64 exp / log (physics.cuh), in extended precision on the host.
+void fill_math_tables(MathTables& t) {
+    for (int j = 0; j < 64; j++) {
+        t.exp2j[j] = double(exp2l((long double)j / 64.0L));
+        const long double c = 1.0L + ((long double)j + 0.5L) / 64.0L;
+        const double ic = double(1.0L / c);
+        t.inv_c[j] = ic;
+        t.log_c[j] = double(-logl((long double)ic));
+    }
+}
+
 int layer_groups(int L, int* kmax) {
     if (L % 14 == 0 && L / 14 <= 8) { *kmax = 14; return L / 14; }
     int G = (L + 15) / 16;
@@ -131,24 +143,34 @@ LayersDev layers_dev(const korg_layers* y) {
 // ------------------------------------------------------------------ line opacity
 constexpr int TILE_TW = 64;  // wavelengths per CTA of the line tile kernel
 
-template <bool MIXED, int KMAX>
+template <bool MIXED, int KMAX, int MAXT, int MINB>
 int launch_tile(korg_ctx* ctx, TileArgs ta, int G, cudaStream_t s) {
     using P = typename ParamT<MIXED>::type;
     const int Lp = ta.Lp;
-    int B = MIXED ? STAGE_LINES : STAGE_LINES / 2;
+    const int B = MIXED ? STAGE_LINES : STAGE_LINES / 2;
     ta.stage = B;
     ta.G = G;
     const int TW = TILE_TW;
     const int threads = TW * G;
-    const size_t region = (std::max(size_t(B) * Lp * sizeof(P), size_t(TW) * (Lp + 1) * sizeof(double)) + 15) & ~size_t(15);
+    size_t region = size_t(B) * Lp * sizeof(P);
+    region = std::max(region, (size_t(TW) * (Lp + 1) * sizeof(double) + 1) / 2);
+    region = (region + 15) & ~size_t(15);
     ta.region = int(region);
-    const size_t smem = region + size_t(B) * sizeof(LineStage) + size_t(threads) * sizeof(int32_t);
-    KCUDA(cudaFuncSetAttribute(line_tile_kernel<MIXED, KMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               int(smem)));
+    const size_t smem = 2 * region + size_t(threads) * sizeof(LineStage);
+    auto kern = line_tile_kernel<MIXED, KMAX, MAXT, MINB>;
+    KCUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     const int64_t tiles = (ta.nwl + TW - 1) / TW;
-    line_tile_kernel<MIXED, KMAX><<<dim3(unsigned(tiles)), threads, smem, s>>>(ta);
+    kern<<<dim3(unsigned(tiles)), threads, smem, s>>>(ta);
     KCUDA(cudaGetLastError());
     return KORG_OK;
+}
+
+template <bool MIXED>
+int dispatch_tile(korg_ctx* ctx, const TileArgs& ta, int G, int kmax, cudaStream_t s) {
+    if (kmax == 14 && G <= 4) return launch_tile<MIXED, 14, 256, MIXED ? 3 : 2>(ctx, ta, G, s);
+    if (kmax == 14) return launch_tile<MIXED, 14, 512, 1>(ctx, ta, G, s);
+    if (kmax == 16) return launch_tile<MIXED, 16, 512, 1>(ctx, ta, G, s);
+    return launch_tile<MIXED, 32, 512, 1>(ctx, ta, G, s);
 }
 
 int run_line_absorption(korg_ctx* ctx, double* alpha, const double* wls, int64_t nwl, const LinesDev& ln,
@@ -164,7 +186,8 @@ int run_line_absorption(korg_ctx* ctx, double* alpha, const double* wls, int64_t
     const size_t psz = mixed ? sizeof(float4) : sizeof(P64);
     KCHECK(ensure(ctx, ctx->lc, sizeof(LayerConst) * L));
     KCHECK(ensure(ctx, ctx->params, psz * size_t(ln.n) * Lp));
-    KCHECK(ensure(ctx, ctx->xcore, sizeof(float) * ln.n));
+    KCHECK(ensure(ctx, ctx->xfar, sizeof(float) * size_t(ln.n) * G));
+    KCHECK(ensure(ctx, ctx->amask, sizeof(uint32_t) * ln.n));
     KCHECK(ensure(ctx, ctx->lb, sizeof(int32_t) * ln.n));
     KCHECK(ensure(ctx, ctx->ub, sizeof(int32_t) * ln.n));
     KCHECK(ensure(ctx, ctx->pmax, sizeof(int32_t) * ln.n));
@@ -173,13 +196,16 @@ int run_line_absorption(korg_ctx* ctx, double* alpha, const double* wls, int64_t
     auto* ctr = static_cast<unsigned long long*>(ctx->counters.p);
     layer_const_kernel<<<(L + 127) / 128, 128, 0, s>>>(lay, static_cast<LayerConst*>(ctx->lc.p));
     PrepOut po{ctx->params.p, static_cast<int32_t*>(ctx->lb.p), static_cast<int32_t*>(ctx->ub.p),
-               static_cast<float*>(ctx->xcore.p), Lp, ctr, ctr + 1};
+               static_cast<float*>(ctx->xfar.p), static_cast<uint32_t*>(ctx->amask.p), Lp, kmax, G, ctr, ctr + 1};
+    const size_t prep_smem = size_t(256 / 32) * Lp * (sizeof(float) + sizeof(int));
     const int64_t pthreads = ln.n * 32;
     const unsigned pblocks = unsigned((pthreads + 255) / 256);
     if (mixed)
-        line_prep_mixed_kernel<<<pblocks, 256, 0, s>>>(ln, lay, static_cast<LayerConst*>(ctx->lc.p), cn, wls, nwl, cutoff, po);
+        line_prep_mixed_kernel<<<pblocks, 256, prep_smem, s>>>(ln, lay, static_cast<LayerConst*>(ctx->lc.p), cn, wls, nwl, cutoff, po,
+                                                       static_cast<MathTables*>(ctx->math.p));
     else
-        line_prep64_kernel<<<pblocks, 256, 0, s>>>(ln, lay, static_cast<LayerConst*>(ctx->lc.p), cn, wls, nwl, cutoff, po);
+        line_prep64_kernel<<<pblocks, 256, prep_smem, s>>>(ln, lay, static_cast<LayerConst*>(ctx->lc.p), cn, wls, nwl, cutoff, po,
+                                                   static_cast<MathTables*>(ctx->math.p));
     KCUDA(cudaGetLastError());
     const int nblk = int((ln.n + SCAN_CHUNK - 1) / SCAN_CHUNK);
     int32_t* bmax = static_cast<int32_t*>(ctx->scanblk.p);
@@ -194,7 +220,8 @@ int run_line_absorption(korg_ctx* ctx, double* alpha, const double* wls, int64_t
     ta.nwl = nwl;
     ta.L = L;
     ta.Lp = Lp;
-    ta.xcore = po.xcore;
+    ta.xfar = po.xfar;
+    ta.amask = po.amask;
     ta.n = ln.n;
     ta.wl = ln.wl;
     ta.params = ctx->params.p;
@@ -204,11 +231,9 @@ int run_line_absorption(korg_ctx* ctx, double* alpha, const double* wls, int64_t
     ta.smin_lb = static_cast<int32_t*>(ctx->smin.p);
     int rc;
     if (mixed)
-        rc = kmax == 14 ? launch_tile<true, 14>(ctx, ta, G, s)
-                        : (kmax == 16 ? launch_tile<true, 16>(ctx, ta, G, s) : launch_tile<true, 32>(ctx, ta, G, s));
+        rc = dispatch_tile<true>(ctx, ta, G, kmax, s);
     else
-        rc = kmax == 14 ? launch_tile<false, 14>(ctx, ta, G, s)
-                        : (kmax == 16 ? launch_tile<false, 16>(ctx, ta, G, s) : launch_tile<false, 32>(ctx, ta, G, s));
+        rc = dispatch_tile<false>(ctx, ta, G, kmax, s);
     ctx->stats_pending = true;
     return rc;
 }
@@ -282,7 +307,7 @@ int run_hydrogen(korg_ctx* ctx, double* alpha, const double* wls, int64_t nwl, c
 int run_rt(korg_ctx* ctx, const double* alpha, const double* S, const double* T, const double* wls, int64_t nwl,
            int L, const double* tau_ref, const double* alpha_ref, CntmDev cn, double* flux, double* cntm,
            double unit, cudaStream_t s) {
-    RtArgs ra{alpha, S, T, wls, nwl, L, tau_ref, alpha_ref, cn, flux, cntm, unit};
+    RtArgs ra{alpha, S, T, wls, nwl, L, tau_ref, alpha_ref, static_cast<MathTables*>(ctx->math.p), cn, flux, cntm, unit};
     const unsigned blocks = unsigned((nwl + 127) / 128);
     rt_kernel<<<blocks, 128, sizeof(double) * 3 * L, s>>>(ra);
     KCUDA(cudaGetLastError());
@@ -415,8 +440,17 @@ KORG_API int korg_create(korg_ctx** out, int device) {
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     for (int i = 0; e == cudaSuccess && i < NEV; i++) e = cudaEventCreate(&ctx->ev[i]);
+    if (e == cudaSuccess) {
+        MathTables t;
+        fill_math_tables(t);
+        e = cudaMalloc(&ctx->math.p, sizeof(MathTables));
+        if (e == cudaSuccess) {
+            ctx->math.cap = sizeof(MathTables);
+            e = cudaMemcpy(ctx->math.p, &t, sizeof t, cudaMemcpyHostToDevice);
+        }
+    }
     if (e != cudaSuccess) {
-        delete ctx;
+        korg_destroy(ctx);
         return KORG_ECUDA;
     }
     *out = ctx;
@@ -427,9 +461,9 @@ KORG_API void korg_destroy(korg_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    DevBuf* bufs[] = {&ctx->lc, &ctx->params, &ctx->xcore, &ctx->lb, &ctx->ub, &ctx->pmax, &ctx->smin, &ctx->scanblk, &ctx->counters,
+    DevBuf* bufs[] = {&ctx->lc, &ctx->params, &ctx->xfar, &ctx->amask, &ctx->lb, &ctx->ub, &ctx->pmax, &ctx->smin, &ctx->scanblk, &ctx->counters,
                       &ctx->hrec, &ctx->hQ, &ctx->hQ32, &ctx->hulb, &ctx->huub, &ctx->stage_dev, &ctx->aref,
-                      &ctx->alpha, &ctx->flux, &ctx->cntm};
+                      &ctx->alpha, &ctx->flux, &ctx->cntm, &ctx->math};
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
     for (void* p : ctx->stark_allocs) cudaFree(p);
@@ -732,6 +766,49 @@ KORG_API int korg_synthesize(korg_ctx* ctx, const korg_synth_inputs* in, const k
 }
 
 }  // extern "C"
+
+// ====================================================================== math self-test
+namespace {
+__device__ __forceinline__ void atomic_max_pos(unsigned long long* a, double v) {
+    atomicMax(a, (unsigned long long)__double_as_longlong(v));  // non-negative doubles order as integers
+}
+// fexp64 against exp over [-700, 700] (error in ulps of the CUDA result) and flog64 against
+// log over [1e-300, 1e300] (absolute error).
+__global__ void math_selftest_kernel(const MathTables* tab, int64_t n, unsigned long long* out) {
+    __shared__ MathTables t;
+    load_math_tables(t, tab);
+    __syncthreads();
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        const double u = (double(i) + 0.5) / double(n);
+        const double x = -700.0 + 1400.0 * u;
+        const double a = fexp64(x, t), b = exp(x);
+        const int eb = int((__double_as_longlong(b) >> 52) & 0x7ff);
+        const double ulp = __longlong_as_double((long long)(eb > 52 ? eb - 52 : 1) << 52);
+        atomic_max_pos(out, fabs(a - b) / ulp);
+        const double y = exp10(-300.0 + 600.0 * u);
+        atomic_max_pos(out + 1, fabs(flog64(y, t) - log(y)));
+    }
+}
+}  // namespace
+
+// Not a counterpart of any reference function: checks the table-driven FP64 exp / log used by
+// the prologue and transfer kernels against the CUDA functions on n points.
+extern "C" KORG_API int korg_math_selftest(korg_ctx* ctx, int64_t n, double* max_ulp_exp, double* max_abs_log) {
+    if (!ctx || n < 1 || !max_ulp_exp || !max_abs_log) return KORG_EINVAL;
+    KCUDA(cudaSetDevice(ctx->device));
+    KCHECK(ensure(ctx, ctx->counters, 4 * sizeof(unsigned long long)));
+    unsigned long long* c = static_cast<unsigned long long*>(ctx->counters.p);
+    KCUDA(cudaMemsetAsync(c, 0, 2 * sizeof(unsigned long long), ctx->stream));
+    math_selftest_kernel<<<608, 256, 0, ctx->stream>>>(static_cast<MathTables*>(ctx->math.p), n, c);
+    KCUDA(cudaGetLastError());
+    unsigned long long h[2];
+    KCUDA(cudaMemcpyAsync(h, c, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+    KCUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->stats_pending = false;
+    memcpy(max_ulp_exp, &h[0], 8);
+    memcpy(max_abs_log, &h[1], 8);
+    return KORG_OK;
+}
 
 // ====================================================================== pipe-throughput probe
 namespace {

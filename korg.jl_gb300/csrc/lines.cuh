@@ -3,22 +3,23 @@
 //
 // Work decomposition
 //   prep:  one warp per line, lanes over layers.  Computes sigma, gamma, amplitude, the
-//          continuum-cutoff window (line_absorption.jl:86-119) and the packed profile
-//          constants; lb/ub are the 0-based inclusive wavelength-index window.
+//          continuum-cutoff window (line_absorption.jl:86-119), the packed profile constants and,
+//          per group of K layers, the distance from the line centre beyond which every layer of
+//          the group is in a closed-form wing branch of the Hjerting approximation.
 //   scan:  running max of ub (prefix) and running min of lb (suffix) over the sorted lines, so
 //          a wavelength tile finds its candidate lines with two binary searches.
 //   tile:  one CTA per tile of TW wavelengths x all layers.  Thread (j, g) owns wavelength j and
-//          layers g, g+G, g+2G, ...; alpha accumulates in registers (FP64, or FP32 with Kahan
-//          compensation), lines are visited in list order, so results are deterministic and
-//          no atomics touch alpha.  Lines overlapping the tile are compacted per chunk and
-//          their per-layer constants staged in shared memory.
+//          the K consecutive layers of group g; alpha accumulates in registers (FP64, or FP32 with
+//          Kahan compensation).  Lines are visited in list order (deterministic, no atomics on
+//          alpha); each chunk of candidates is compacted with warp ballots, and the constants of
+//          32-line batches are copied to shared memory with cp.async, double buffered.
 #pragma once
 #include "physics.cuh"
 
 namespace korg {
 
-constexpr int TILE_W_MAX = 128;  // wavelengths per CTA (64 when more than 4 layer groups)
-constexpr int STAGE_LINES = 32;  // lines staged in shared memory per batch (upper bound)
+constexpr int STAGE_LINES = 32;  // lines staged in shared memory per batch
+constexpr int MAX_GROUPS = 8;    // layer groups per CTA
 
 // FP64 profile constants of one (line, layer): c = 2 sigma^2 (so 1/v^2 = c / x^2), w as in the
 // mixed form, inv_s = 1/(sigma sqrt2), a = gamma inv_s, scale = amp inv_s / sqrt(pi)
@@ -61,9 +62,10 @@ struct PrepOut {
     void* params;            // [n][Lp] P64 (FP64) or float4 (mixed); layers L..Lp-1 are zero padding
     int32_t* lb;             // [n]
     int32_t* ub;             // [n]
-    float* xcore;            // [n] |wl - wl0| beyond which every layer is in the asymptotic wing
-                             //     (v >= 5 with a <= 0.2); -1 when some layer has a > 0.2
-    int32_t Lp;
+    float* xfar;             // [n][G] |wl - wl0| beyond which every layer of group g is in a wing
+                             //        branch: v >= 5 (a <= 0.2) or a + v >= 3.2 / a > 1.4 (a > 0.2)
+    uint32_t* amask;         // [n] bit g: every layer of group g has a <= 0.2
+    int32_t Lp, K, G;
     unsigned long long* evals;   // running totals: evaluations, lines in window
     unsigned long long* nlines;
 };
@@ -99,7 +101,8 @@ struct LineLayer64 {
 };
 
 __device__ __forceinline__ LineLayer64 line_layer64(const LineConst& q, const LayersDev& lay, const LayerConst& c,
-                                                    const CntmDev& cn, const KnotPos& kp, double cutoff, int l) {
+                                                    const CntmDev& cn, const KnotPos& kp, double cutoff, int l,
+                                                    const MathTables& mt) {
     LineLayer64 r;
     const double T = lay.T[l];
     r.sigma = doppler_width(q.wl, T, q.m, lay.xi[l]);  // :86
@@ -117,11 +120,12 @@ __device__ __forceinline__ LineLayer64 line_layer64(const LineConst& q, const La
         G = G + lay.n_eff_vdW[l] * vdw;
     }
     r.gamma = G * q.wl2c;                                                       // :99
-    const double levels = exp(-c.beta * q.El) - exp(-c.beta * q.E_upper);       // :101-102
-    r.amp = q.strength * levels * lay.n_div_U[int64_t(q.sp) * lay.L + l];      // :105-106
+    const double levels = fexp64(-c.beta * q.El, mt) - fexp64(-c.beta * q.E_upper, mt);  // :101-102
+    r.amp = q.strength * levels * lay.n_div_U[int64_t(q.sp) * lay.L + l];                // :105-106
     const double acntm = knot_eval(cn.vals + int64_t(l) * cn.nk, cn.nk, kp);    // :108
     const double rho = acntm * cutoff / r.amp;
-    r.dw = inverse_gaussian_density(rho, r.sigma);                              // :109-112
+    r.dw = (rho > 1 / (SQRT_2PI * r.sigma)) ? 0.0                              // :109-112 (:140-145)
+                                            : r.sigma * sqrt(-2 * flog64(SQRT_2PI * r.sigma * rho, mt));
     r.lw = inverse_lorentz_density(rho, r.gamma);
     return r;
 }
@@ -139,43 +143,69 @@ __device__ __forceinline__ void store_window(const PrepOut& out, int64_t i, doub
     }
 }
 
+// Per-(line, group) wing boundaries from per-layer ones held in shared memory: lanes g < G
+// reduce their group and write xfar / amask.
+__device__ __forceinline__ void group_bounds(const PrepOut& out, int64_t i, const float* s_bnd, const int* s_cls,
+                                             int lane) {
+    unsigned bits = 0;
+    float mx = 0.f;
+    int allA = 1;
+    if (lane < out.G) {
+        for (int k = 0; k < out.K; k++) {
+            mx = fmaxf(mx, s_bnd[lane * out.K + k]);
+            allA &= s_cls[lane * out.K + k];
+        }
+        out.xfar[i * out.G + lane] = mx;
+    }
+    bits = __ballot_sync(0xffffffffu, lane < out.G && allA);
+    if (lane == 0) out.amask[i] = bits;
+}
+
 // FP64 prologue: one warp per line, lanes over layers.
 __global__ void __launch_bounds__(256) line_prep64_kernel(LinesDev ln, LayersDev lay, const LayerConst* lc, CntmDev cn,
-                                                          const double* wls, int64_t nwl, double cutoff, PrepOut out) {
+                                                          const double* wls, int64_t nwl, double cutoff, PrepOut out,
+                                                          const MathTables* math) {
+    __shared__ MathTables s_math;
+    extern __shared__ float s_dyn[];  // [warps][Lp] boundaries, then [warps][Lp] class flags
+    load_math_tables(s_math, math);
+    __syncthreads();
     const int64_t i = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     if (i >= ln.n) return;
-    const int L = lay.L;
+    const int L = lay.L, Lp = out.Lp;
+    float* s_bnd = s_dyn + wib * Lp;
+    int* s_cls = reinterpret_cast<int*>(s_dyn + (blockDim.x >> 5) * Lp) + wib * Lp;
     const LineConst q = line_const(ln, i);
     const KnotPos kp = knot_pos(cn.knots, cn.nk, q.wl);
-    double dwin = 0.0, lwin = 0.0, xc = 0.0;
-    const int Lp = out.Lp;
+    double dwin = 0.0, lwin = 0.0;
     P64* dst = reinterpret_cast<P64*>(out.params) + i * Lp;
     for (int l = lane; l < Lp; l += 32) {
         if (l >= L) {
             dst[l] = P64{1.0, 0.0, 1.0, 0.0, 0.0, 0.0};
+            s_bnd[l] = 0.f;
+            s_cls[l] = 1;
             continue;
         }
-        const LineLayer64 r = line_layer64(q, lay, lc[l], cn, kp, cutoff, l);
+        const LineLayer64 r = line_layer64(q, lay, lc[l], cn, kp, cutoff, l, s_math);
         dwin = fmax(dwin, r.dw);
         lwin = fmax(lwin, r.lw);
         const double inv_s = 1 / (r.sigma * SQRT_2);  // :246-248
         const double a = r.gamma * inv_s, scale = inv_s / SQRT_PI * r.amp;
         const double c = 1 / (inv_s * inv_s);
-        dst[l] = P64{c, a <= 0.2 ? a / SQRT_PI * scale : 0.0, inv_s, a, scale, 0.0};
-        xc = (a <= 0.2 && xc >= 0) ? fmax(xc, 5.000005 / inv_s) : -1.0;
+        const bool A = a <= 0.2;
+        dst[l] = P64{c, A ? a / SQRT_PI * scale : 1 / (r.gamma * r.gamma), inv_s, a, scale, 0.0};
+        // v >= 5 (a <= 0.2) or a + v >= 3.2 (0.2 < a <= 1.4) or any v (a > 1.4), v = x inv_s
+        s_bnd[l] = float((A ? 5.0 : (a <= 1.4 ? 3.2 - a : 0.0)) / inv_s * 1.0001);
+        s_cls[l] = A;
     }
+    __syncwarp();
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         dwin = fmax(dwin, __shfl_xor_sync(0xffffffffu, dwin, o));
         lwin = fmax(lwin, __shfl_xor_sync(0xffffffffu, lwin, o));
-        const double ox = __shfl_xor_sync(0xffffffffu, xc, o);
-        xc = (xc < 0 || ox < 0) ? -1.0 : fmax(xc, ox);
     }
-    if (lane == 0) {
-        store_window(out, i, lwin, dwin, q.wl, wls, nwl, L);
-        out.xcore[i] = float(xc);
-    }
+    group_bounds(out, i, s_bnd, s_cls, lane);
+    if (lane == 0) store_window(out, i, lwin, dwin, q.wl, wls, nwl, L);
 }
 
 // FP32 forms of line_absorption.jl:140-161 (used to locate the widest layers)
@@ -205,22 +235,29 @@ __device__ __forceinline__ void argmax_reduce(float& v, int& idx) {
 // and w = a/sqrt(pi)*scale (a <= 0.2, asymptotic wing) or 1/gamma^2 (a > 0.2, far Lorentz).
 __global__ void __launch_bounds__(256) line_prep_mixed_kernel(LinesDev ln, LayersDev lay, const LayerConst* lc,
                                                               CntmDev cn, const double* wls, int64_t nwl,
-                                                              double cutoff, PrepOut out) {
+                                                              double cutoff, PrepOut out, const MathTables* math) {
+    __shared__ MathTables s_math;
+    extern __shared__ float s_dyn[];
+    load_math_tables(s_math, math);
+    __syncthreads();
     const int64_t i = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     if (i >= ln.n) return;
-    const int L = lay.L;
+    const int L = lay.L, Lp = out.Lp;
+    float* s_bnd = s_dyn + wib * Lp;
+    int* s_cls = reinterpret_cast<int*>(s_dyn + (blockDim.x >> 5) * Lp) + wib * Lp;
     const LineConst q = line_const(ln, i);
     const KnotPos kp = knot_pos(cn.knots, cn.nk, q.wl);
     const float wlc = float(q.wl / C_CGS), m32 = float(q.m), wl2c = float(q.wl2c);
     const float k_m = float(KBOLTZ_CGS / q.m);
-    float dmax = -1.f, lmax = -1.f, xc = 0.f;
+    float dmax = -1.f, lmax = -1.f;
     int dl = 0, ll = 0;
-    const int Lp = out.Lp;
     float4* dst = reinterpret_cast<float4*>(out.params) + i * Lp;
     for (int l = lane; l < Lp; l += 32) {
         if (l >= L) {
             dst[l] = make_float4(1.f, 0.f, 0.f, 0.f);
+            s_bnd[l] = 0.f;
+            s_cls[l] = 1;
             continue;
         }
         const LayerConst c = lc[l];
@@ -240,7 +277,7 @@ __global__ void __launch_bounds__(256) line_prep_mixed_kernel(LinesDev ln, Layer
             G = G + float(lay.ne[l]) * (float(q.gstark) * float(c.stark6)) + float(lay.n_eff_vdW[l]) * vdw;
         }
         const float gamma = G * wl2c;
-        const double levels = exp(-c.beta * q.El) - exp(-c.beta * q.E_upper);   // FP64 line strength
+        const double levels = fexp64(-c.beta * q.El, s_math) - fexp64(-c.beta * q.E_upper, s_math);  // FP64
         const float amp = float(q.strength * levels * lay.n_div_U[int64_t(q.sp) * L + l]);
         const float acntm = float(knot_eval(cn.vals + int64_t(l) * cn.nk, cn.nk, kp));
         const float rho = acntm * float(cutoff) / amp;
@@ -250,28 +287,26 @@ __global__ void __launch_bounds__(256) line_prep_mixed_kernel(LinesDev ln, Layer
         const float s = 1.f / (sigma * 1.41421356f);
         const float a = gamma * s;
         const float scale = s * 0.56418958f * amp;  // 1/sqrt(pi)
+        const bool A = a <= 0.2f;
         float4 p;
         p.x = 2.f * sigma * sigma;
         p.y = a;
-        p.z = (a <= 0.2f) ? a * 0.56418958f * scale : 1.f / (gamma * gamma);
+        p.z = A ? a * 0.56418958f * scale : 1.f / (gamma * gamma);
         p.w = scale;
         dst[l] = p;
-        // the wing test of the tile kernel uses 1/v^2 = c t <= 0.04, i.e. x >= 5 sqrt(c)
-        xc = (a <= 0.2f && xc >= 0.f) ? fmaxf(xc, 5.0001f * sqrtf(p.x)) : -1.f;
+        // v >= 5 (a <= 0.2) or a + v >= 3.2 (0.2 < a <= 1.4) or any v (a > 1.4), v = x / sqrt(c)
+        s_bnd[l] = (A ? 5.f : (a <= 1.4f ? 3.2f - a : 0.f)) * sqrtf(p.x) * 1.0001f;
+        s_cls[l] = A;
     }
+    __syncwarp();
     argmax_reduce(dmax, dl);
     argmax_reduce(lmax, ll);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const float ox = __shfl_xor_sync(0xffffffffu, xc, o);
-        xc = (xc < 0.f || ox < 0.f) ? -1.f : fmaxf(xc, ox);
-    }
-    if (lane == 0) out.xcore[i] = xc;
+    group_bounds(out, i, s_bnd, s_cls, lane);
     // exact FP64 window at the two widest layers (lanes 0 and 1 in parallel)
     double w = 0.0;
     if (lane < 2) {
         const int l = lane == 0 ? dl : ll;
-        const LineLayer64 r = line_layer64(q, lay, lc[l], cn, kp, cutoff, l);
+        const LineLayer64 r = line_layer64(q, lay, lc[l], cn, kp, cutoff, l, s_math);
         w = lane == 0 ? r.dw : r.lw;
     }
     const double lwin = __shfl_sync(0xffffffffu, w, 1);
@@ -371,11 +406,12 @@ struct TileArgs {
     const double* wls;
     int64_t nwl;
     int32_t L, Lp, G, stage;  // layers, padded layers (G * K), layer groups, lines per batch
-    int32_t region;           // bytes of the shared region for constants / the alpha tile
+    int32_t region;           // bytes of one shared buffer of line constants (x2, double buffered)
     int64_t n;
     const double* wl;     // line centres
     const void* params;
-    const float* xcore;
+    const float* xfar;
+    const uint32_t* amask;
     const int32_t *lb, *ub, *pmax_ub, *smin_lb;
 };
 
@@ -398,26 +434,45 @@ __device__ __forceinline__ int64_t upper_bound_i32(const int32_t* a, int64_t n, 
     return lo;
 }
 
-// a line staged for the current batch
+// A candidate line of the current chunk, as the tile sees it.
 struct LineStage {
     double wl;        // centre (FP64 path)
     float dhi, dlo;   // centre - first wavelength of the tile, as an FP32 pair (mixed path)
     int32_t lb, ub;
-    int32_t fast;     // the whole tile lies in the asymptotic wing of every layer
-    int32_t pad;
+    uint32_t cls;     // 2 bits per layer group: 1 = pure asymptotic wing, 2 = wing branches, 0 = general
+    int32_t li;       // line index
 };
+
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+    const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+// Far-Lorentz branch of voigt_hjerting (line_absorption.jl:305-308) with r^2 = x^2/gamma^2.
+__device__ __forceinline__ float far_lorentz32(float4 p, float x2) {
+    const float r2 = x2 * p.z;
+    const float au = __fdividef(0.70710678118654752f, (r2 + 1.f) * p.y);
+    const float au2 = au * au;
+    return 0.7978845608028654f * au * (1.f + (3.f * r2 - 1.f + ((r2 - 2.f) * 15.f * r2 + 2.f) * au2) * au2) * p.w;
+}
+__device__ __forceinline__ double far_lorentz64(const P64& p, double x2) {
+    const double r2 = x2 * p.w;
+    const double au = 1 / SQRT_2 / ((r2 + 1) * p.a);
+    const double au2 = au * au;
+    return 0.7978845608028654 * au * (1 + (3 * r2 - 1 + ((r2 - 2) * 15 * r2 + 2) * au2) * au2) * p.scale;
+}
 
 // One CTA per tile of TW = blockDim.x / G wavelengths x all layers.  Thread (j, g) owns
 // wavelength j and the K consecutive (padded) layers g*K .. g*K+K-1.
-template <bool MIXED, int K>
-__global__ void __launch_bounds__(512) line_tile_kernel(TileArgs a) {
+template <bool MIXED, int K, int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB) line_tile_kernel(TileArgs a) {
     using P = typename ParamT<MIXED>::type;
     extern __shared__ __align__(16) unsigned char smem[];
     const int L = a.L, Lp = a.Lp, G = a.G, B = a.stage;
-    P* s_par = reinterpret_cast<P*>(smem);                                   // [B][Lp]
-    double* s_alpha = reinterpret_cast<double*>(smem);                       // [TW][Lp+1], at the end
-    LineStage* s_ln = reinterpret_cast<LineStage*>(smem + a.region);         // [B]
-    int32_t* s_list = reinterpret_cast<int32_t*>(s_ln + B);                  // [blockDim]
+    double* s_alpha = reinterpret_cast<double*>(smem);                          // [TW][Lp+1], at the end
+    LineStage* s_ln = reinterpret_cast<LineStage*>(smem + 2 * size_t(a.region));  // [blockDim]
     __shared__ int32_t s_warp[32];
     __shared__ int64_t s_range[2];
 
@@ -448,11 +503,14 @@ __global__ void __launch_bounds__(512) line_tile_kernel(TileArgs a) {
     for (int k = 0; k < K; k++) { acc[k] = Acc(0); comp[k] = Acc(0); }
 
     const int warp = tid >> 5, lane = tid & 31, nwarps = nthr >> 5;
+    const int chunks16 = Lp * int(sizeof(P) / 16);  // 16-byte pieces of one line's constants
     for (int64_t base = i_lo; base <= i_hi; base += nthr) {
         const int64_t i = base + tid;
         bool take = false;
+        int32_t lbi = 0, ubi = -1;
         if (i <= i_hi) {
-            const int32_t lbi = a.lb[i], ubi = a.ub[i];
+            lbi = a.lb[i];
+            ubi = a.ub[i];
             take = lbi <= ubi && lbi <= jlast && ubi >= j0;
         }
         const unsigned m = __ballot_sync(0xffffffffu, take);
@@ -464,51 +522,83 @@ __global__ void __launch_bounds__(512) line_tile_kernel(TileArgs a) {
             s_range[0] = run;  // reused as the count
         }
         __syncthreads();
-        if (take) s_list[s_warp[warp] + __popc(m & ((1u << lane) - 1))] = int32_t(i - base);
+        if (take) {  // the thread that found the line describes it for the whole CTA
+            LineStage st;
+            const double wl0 = a.wl[i], d = wl0 - wl_ref;
+            const float dh = float(d);
+            const double dist = wl0 < wl_ref ? wl_ref - wl0 : (wl0 > wl_last ? wl0 - wl_last : 0.0);
+            const uint32_t am = a.amask[i];
+            uint32_t cls = 0;
+            for (int gg = 0; gg < G; gg++) {
+                const float xf = a.xfar[i * G + gg];
+                if (dist > double(xf)) cls |= (((am >> gg) & 1u) ? 1u : 2u) << (2 * gg);
+            }
+            st.wl = wl0;
+            st.dhi = dh;
+            st.dlo = float(d - double(dh));
+            st.lb = lbi;
+            st.ub = ubi;
+            st.cls = cls;
+            st.li = int32_t(i - base);
+            s_ln[s_warp[warp] + __popc(m & ((1u << lane) - 1))] = st;
+        }
         const int cnt = int(s_range[0]);
         __syncthreads();
 
-        for (int b0 = 0; b0 < cnt; b0 += B) {
-            const int nb = min(B, cnt - b0);
-            for (int b = warp; b < nb; b += nwarps) {
-                const int64_t li = base + s_list[b0 + b];
-                const P* src = reinterpret_cast<const P*>(a.params) + li * Lp;
-                for (int l = lane; l < Lp; l += 32) s_par[b * Lp + l] = src[l];
-                if (lane == 0) {
-                    const double wl0 = a.wl[li], d = wl0 - wl_ref;
-                    const float dh = float(d);
-                    const double dist = wl0 < wl_ref ? wl_ref - wl0 : (wl0 > wl_last ? wl0 - wl_last : 0.0);
-                    const float xc = a.xcore[li];
-                    LineStage st;
-                    st.wl = wl0;
-                    st.dhi = dh;
-                    st.dlo = float(d - double(dh));
-                    st.lb = a.lb[li];
-                    st.ub = a.ub[li];
-                    st.fast = xc >= 0.f && dist > double(xc) * 1.000001;
-                    st.pad = 0;
-                    s_ln[b] = st;
+        // batches of B lines: constants copied with cp.async into two alternating buffers
+        const int nq = (cnt + B - 1) / B;
+        auto issue = [&](int q) {
+            if (q < nq) {
+                const int b0 = q * B, nb = min(B, cnt - b0);
+                unsigned char* buf = smem + size_t(q & 1) * a.region;
+                for (int e = tid; e < nb * chunks16; e += nthr) {
+                    const int b = e / chunks16, r = e - b * chunks16;
+                    const int64_t li = base + s_ln[b0 + b].li;
+                    cp_async16(buf + (size_t(b) * chunks16 + r) * 16,
+                               reinterpret_cast<const unsigned char*>(a.params) + (li * chunks16 + r) * 16);
                 }
             }
-            __syncthreads();
+            cp_async_commit();
+        };
+        issue(0);
+        for (int q = 0; q < nq; q++) {
+            issue(q + 1);
+            cp_async_wait_1();  // batch q has landed (this thread's copies) ...
+            __syncthreads();    // ... and everybody else's
+            const int b0 = q * B, nb = min(B, cnt - b0);
+            const P* s_par = reinterpret_cast<const P*>(smem + size_t(q & 1) * a.region);
             if (live) {
                 if (MIXED) {
                     float part[K];
 #pragma unroll
                     for (int k = 0; k < K; k++) part[k] = 0.f;
                     for (int b = 0; b < nb; b++) {
-                        const LineStage st = s_ln[b];
+                        const LineStage& st = s_ln[b0 + b];
                         if (jg < st.lb || jg > st.ub) continue;
                         const float x = fabsf((xj_hi - st.dhi) + (xj_lo - st.dlo));
-                        const float t = __fdividef(1.f, x * x);
+                        const float x2 = x * x;
+                        const float t = __fdividef(1.f, x2);
                         const float4* pr = reinterpret_cast<const float4*>(s_par) + b * Lp + g * K;
-                        if (st.fast) {
-                            // asymptotic wing of every layer: w/v^2 (1 + 1.5/v^2 + 3.75/v^4), 1/v^2 = c t
+                        const uint32_t cls = (st.cls >> (2 * g)) & 3u;
+                        if (cls == 1u) {
+                            // every layer in the asymptotic wing: w/v^2 (1 + 1.5/v^2 + 3.75/v^4), 1/v^2 = c t
 #pragma unroll
                             for (int k = 0; k < K; k++) {
                                 const float4 p = pr[k];
                                 const float iv = t * p.x;
                                 part[k] = fmaf(p.z * iv, fmaf(fmaf(3.75f, iv, 1.5f), iv, 1.f), part[k]);
+                            }
+                        } else if (cls == 2u) {
+                            // every layer in a wing branch, chosen per layer (uniform across the warp)
+#pragma unroll
+                            for (int k = 0; k < K; k++) {
+                                const float4 p = pr[k];
+                                if (p.y <= 0.2f) {
+                                    const float iv = t * p.x;
+                                    part[k] = fmaf(p.z * iv, fmaf(fmaf(3.75f, iv, 1.5f), iv, 1.f), part[k]);
+                                } else {
+                                    part[k] += far_lorentz32(p, x2);
+                                }
                             }
                         } else {
 #pragma unroll
@@ -525,16 +615,21 @@ __global__ void __launch_bounds__(512) line_tile_kernel(TileArgs a) {
                     }
                 } else {
                     for (int b = 0; b < nb; b++) {
-                        const LineStage st = s_ln[b];
+                        const LineStage& st = s_ln[b0 + b];
                         if (jg < st.lb || jg > st.ub) continue;
                         const double x = fabs(wl_j - st.wl);
                         const P64* pr = reinterpret_cast<const P64*>(s_par) + b * Lp + g * K;
-                        if (st.fast) {
-                            const double t = 1 / (x * x);
+                        const uint32_t cls = (st.cls >> (2 * g)) & 3u;
+                        if (cls != 0u) {
+                            const double x2 = x * x, t = 1 / x2;
 #pragma unroll
                             for (int k = 0; k < K; k++) {
-                                const double iv = t * pr[k].c;
-                                acc[k] += Acc((pr[k].w * iv) * (1 + iv * (1.5 + 3.75 * iv)));
+                                if (pr[k].a <= 0.2) {
+                                    const double iv = t * pr[k].c;
+                                    acc[k] += Acc((pr[k].w * iv) * (1 + iv * (1.5 + 3.75 * iv)));
+                                } else {
+                                    acc[k] += Acc(far_lorentz64(pr[k], x2));
+                                }
                             }
                         } else {
 #pragma unroll
@@ -543,7 +638,7 @@ __global__ void __launch_bounds__(512) line_tile_kernel(TileArgs a) {
                     }
                 }
             }
-            __syncthreads();
+            __syncthreads();  // buffer (q & 1) is refilled by issue(q + 2)
         }
     }
     // alpha += accumulated lines, staged through shared memory for coalesced updates

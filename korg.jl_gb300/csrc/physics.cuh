@@ -25,6 +25,70 @@ constexpr double SQRT_PI = 1.7724538509055159;   // sqrt(pi)
 constexpr double SQRT_2 = 1.4142135623730951;
 constexpr double SQRT_2PI = 2.5066282746310002;  // sqrt(2*pi)
 
+// ---------------------------------------------------------------- table-driven FP64 exp / log
+// Tang's table-driven method (P. T. P. Tang, ACM TOMS 15 (1989) 144 and 16 (1990) 378),
+// implemented from the mathematics: exp(x) = 2^m 2^(j/64) e^r with |r| <= ln2/128 and a
+// degree-6 Taylor polynomial; log(x) = e ln2 + log(c_j) + log(1 + r), c_j = 1 + (j + 1/2)/64,
+// r = m/c_j - 1 (|r| <= 1/129) and a degree-8 series.  About half the FP64 operations of the
+// general-purpose functions, which matters on GB300 where the FP64 pipe is 1/64 of FP32.
+// Tables (computed on the host in extended precision at context creation):
+//   exp2j[j] = 2^(j/64), inv_c[j] = 1/c_j rounded to double, log_c[j] = -log(inv_c[j]).
+// Accuracy: exp within 1 ulp for |x| <= 700 (outside that range the CUDA function is used);
+// log within 2e-15 absolute (0.5 ulp for |log x| >~ 4) for normal x.
+struct MathTables {
+    double exp2j[64];
+    double inv_c[64];
+    double log_c[64];
+};
+
+__device__ __forceinline__ double fexp64(double x, const MathTables& t) {
+    if (!(fabs(x) <= 700.0)) return exp(x);
+    const double INV_L = 92.33248261689366;            // 64 / ln 2
+    const double L_HI = 0.010830424696905538;          // ln2 / 64 to 33 bits (k * L_HI exact)
+    const double L_LO = -6.563929801064195e-13;        // ln2 / 64 - L_HI
+    const double MAGIC = 6755399441055744.0;           // 1.5 * 2^52: round to integer
+    double kd = fma(x, INV_L, MAGIC);
+    const int k = __double2loint(kd);
+    kd -= MAGIC;
+    double r = fma(-kd, L_HI, x);
+    r = fma(-kd, L_LO, r);
+    double p = fma(r, 1.0 / 720.0, 1.0 / 120.0);
+    p = fma(p, r, 1.0 / 24.0);
+    p = fma(p, r, 1.0 / 6.0);
+    p = fma(p, r, 0.5);
+    p = fma(p, r, 1.0);
+    p *= r;
+    const double tj = t.exp2j[k & 63];
+    const double res = fma(tj, p, tj);
+    return __longlong_as_double(__double_as_longlong(res) + ((long long)(k >> 6) << 52));
+}
+
+__device__ __forceinline__ double flog64(double x, const MathTables& t) {
+    if (!(x >= 2.2250738585072014e-308 && x <= 1.7976931348623157e308)) return log(x);
+    const long long b = __double_as_longlong(x);
+    const int e = int((b >> 52) & 0x7ff) - 1023;
+    const double m = __longlong_as_double((b & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
+    const int j = int((b >> 46) & 63);
+    const double r = fma(m, t.inv_c[j], -1.0);
+    double p = fma(-0.125, r, 1.0 / 7.0);
+    p = fma(p, r, -1.0 / 6.0);
+    p = fma(p, r, 0.2);
+    p = fma(p, r, -0.25);
+    p = fma(p, r, 1.0 / 3.0);
+    p = fma(p, r, -0.5);
+    p = fma(p, r, 1.0);
+    p *= r;
+    const double LN2_HI = 0.6931471805599453, LN2_LO = 2.3190468138462996e-17;
+    return fma(double(e), LN2_HI, t.log_c[j] + fma(double(e), LN2_LO, p));
+}
+
+// copy the tables into shared memory (call from every thread, then __syncthreads())
+__device__ __forceinline__ void load_math_tables(MathTables& dst, const MathTables* src) {
+    const double* s = reinterpret_cast<const double*>(src);
+    double* d = reinterpret_cast<double*>(&dst);
+    for (int i = threadIdx.x; i < 192; i += blockDim.x) d[i] = s[i];
+}
+
 // ---------------------------------------------------------------- FP64 Voigt-Hjerting
 // src/line_absorption.jl:251-265
 __device__ __forceinline__ void harris64(double v, double& H0, double& H1, double& H2) {
@@ -224,12 +288,17 @@ __device__ __forceinline__ double expint2_64(double x) {
     return exp(-x) * (1 + (-2 + (6 + (-24 + 120 * invx) * invx) * invx) * invx) * invx;
 }
 
-// E2 with exp(-x) supplied by the caller (the x >= 9 branch reuses it; same value as computing
-// it inside, RadiativeTransfer.jl:440-443)
-__device__ __forceinline__ double expint2_ex(double x, double ex) {
+// E2 with exp(-x) supplied by the caller (the x >= 9 branch reuses it, RadiativeTransfer.jl:440-443)
+// and the table-driven log for the small-argument series (:432-439)
+__device__ __forceinline__ double expint2_ex(double x, double ex, const MathTables& t) {
     if (x >= 9) {
         const double invx = 1 / x;
         return ex * (1 + (-2 + (6 + (-24 + 120 * invx) * invx) * invx) * invx) * invx;
+    }
+    if (x < 1.1 && x != 0) {
+        const double EM = 0.57721566490153286060651209008240243104215933593992;
+        return 1 + ((flog64(x, t) + EM - 1) +
+                    (-0.5 + (0.08333333333333333 + (-0.013888888888888888 + 0.0020833333333333333 * x) * x) * x) * x) * x;
     }
     return expint2_64(x);
 }

@@ -23,6 +23,7 @@ struct RtArgs {
     int32_t L;
     const double* tau_ref;   // [L]
     const double* alpha_ref; // [L]
+    const MathTables* math;
     CntmDev cn;              // nk > 0: also run the continuum-only transfer into cntm
     double* flux;
     double* cntm;
@@ -42,13 +43,14 @@ constexpr double TAU_STOP = 100.0;
 struct RtPass {
     double ib_prev, tau_prev, e2_prev, ex_prev, I;
     bool live;
-    __device__ __forceinline__ void step(double alpha, double fac, double dlt, double S, double S_prev) {
+    __device__ __forceinline__ void step(double alpha, double fac, double dlt, double S, double S_prev,
+                                         const MathTables& mt) {
         const double ib = alpha * fac;
         const double tau = tau_prev + 0.5 * (ib + ib_prev) * dlt;  // RadiativeTransfer.jl:250-251
         const double m = (S - S_prev) / (tau - tau_prev);          // :382
         const double b = S_prev - m * tau_prev;                    // :383
-        const double ex = exp(-tau);
-        const double e2 = expint2_ex(tau, ex);
+        const double ex = fexp64(-tau, mt);
+        const double e2 = expint2_ex(tau, ex, mt);
         I += (expint_core(tau, e2, ex, m, b) - expint_core(tau_prev, e2_prev, ex_prev, m, b));  // :384-385
         ib_prev = ib;
         tau_prev = tau;
@@ -60,6 +62,8 @@ struct RtPass {
 
 __global__ void __launch_bounds__(128) rt_kernel(RtArgs a) {
     extern __shared__ double s_rt[];
+    __shared__ MathTables s_math;
+    load_math_tables(s_math, a.math);
     const int L = a.L;
     double* s_fac = s_rt;          // tau_ref/alpha_ref * ds/dz (= 1)
     double* s_ltr = s_rt + L;      // log(tau_ref)
@@ -91,8 +95,9 @@ __global__ void __launch_bounds__(128) rt_kernel(RtArgs a) {
     for (int l = 1; l < L && (full.live || cont.live); l++) {
         const double S = Sc ? Sc[l] : planck(pre, hcw, s_T[l]);
         const double dlt = s_ltr[l] - s_ltr[l - 1];
-        if (full.live) full.step(al[l], s_fac[l], dlt, S, S_prev);
-        if (cont.live) cont.step(knot_eval(a.cn.vals + int64_t(l) * a.cn.nk, a.cn.nk, kp), s_fac[l], dlt, S, S_prev);
+        if (full.live) full.step(al[l], s_fac[l], dlt, S, S_prev, s_math);
+        if (cont.live)
+            cont.step(knot_eval(a.cn.vals + int64_t(l) * a.cn.nk, a.cn.nk, kp), s_fac[l], dlt, S, S_prev, s_math);
         S_prev = S;
     }
     a.flux[j] = 2 * PI * (full.I * 1.0) * a.unit;  // :136

@@ -99,6 +99,7 @@ def lib():
             L.korg_synthesize_dev.argtypes = [vp, C.POINTER(SynthInputs), C.POINTER(Lines), C.POINTER(Lines), vp,
                                               C.c_int64, C.c_int, vp, vp, vp, vp]
             L.korg_probe_flops.argtypes = [vp, C.c_int, _dp]
+            L.korg_math_selftest.argtypes = [vp, C.c_int64, _dp, _dp]
             _lib = L
     return _lib
 
@@ -108,7 +109,8 @@ def exported_symbols():
     return ["korg_create", "korg_destroy", "korg_last_error", "korg_get_stats", "korg_set_timing",
             "korg_set_stark_tables", "korg_line_absorption", "korg_line_absorption_dev",
             "korg_hydrogen_line_absorption", "korg_hydrogen_lines_dev", "korg_radiative_transfer",
-            "korg_radiative_transfer_dev", "korg_synthesize", "korg_synthesize_dev", "korg_probe_flops"]
+            "korg_radiative_transfer_dev", "korg_synthesize", "korg_synthesize_dev", "korg_probe_flops",
+            "korg_math_selftest"]
 
 
 def _p(a, kind=_dp):

@@ -140,6 +140,15 @@ def test_line_absorption_80_layers(ctx, oracle_lib):
         assert np.max(np.abs(got - ref) / ref) <= tol
 
 
+def test_table_driven_math(ctx):
+    """The table-driven FP64 exp / log of the prologue and transfer kernels against CUDA's."""
+    e, l = C.c_double(), C.c_double()
+    assert ctx.lib.korg_math_selftest(ctx.h, 1 << 22, C.byref(e), C.byref(l)) == 0
+    print(f"fexp64 max {e.value:.2f} ulp, flog64 max abs err {l.value:.2e}")
+    assert e.value <= 2.0
+    assert l.value <= 4e-15
+
+
 def test_rt_parity(ctx, cfg0, oracle_lib):
     from korg_gb300 import _lib
     alpha = _cont_alpha(cfg0)
