@@ -186,7 +186,7 @@ KORG_API int korg_probe_flops(korg_ctx *ctx, int fp64, double *tflops);
 
 /* Not a counterpart of any reference function: compares the table-driven FP64 exp and log
  * used by the prologue and transfer kernels with the CUDA exp and log on n points; returns the
- * largest exp error in ulps and the largest absolute log error. */
+ * largest exp error in ulps and the largest log error relative to max(1, |log x|). */
 KORG_API int korg_math_selftest(korg_ctx *ctx, int64_t n, double *max_ulp_exp, double *max_abs_log);
 
 #ifdef __cplusplus

@@ -773,7 +773,7 @@ __device__ __forceinline__ void atomic_max_pos(unsigned long long* a, double v) 
     atomicMax(a, (unsigned long long)__double_as_longlong(v));  // non-negative doubles order as integers
 }
 // fexp64 against exp over [-700, 700] (error in ulps of the CUDA result) and flog64 against
-// log over [1e-300, 1e300] (absolute error).
+// log over [1e-300, 1e300] (error relative to max(1, |log x|)).
 __global__ void math_selftest_kernel(const MathTables* tab, int64_t n, unsigned long long* out) {
     __shared__ MathTables t;
     load_math_tables(t, tab);
@@ -786,7 +786,8 @@ __global__ void math_selftest_kernel(const MathTables* tab, int64_t n, unsigned 
         const double ulp = __longlong_as_double((long long)(eb > 52 ? eb - 52 : 1) << 52);
         atomic_max_pos(out, fabs(a - b) / ulp);
         const double y = exp10(-300.0 + 600.0 * u);
-        atomic_max_pos(out + 1, fabs(flog64(y, t) - log(y)));
+        const double ly = log(y);
+        atomic_max_pos(out + 1, fabs(flog64(y, t) - ly) / fmax(1.0, fabs(ly)));
     }
 }
 }  // namespace

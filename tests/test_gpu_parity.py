@@ -144,9 +144,9 @@ def test_table_driven_math(ctx):
     """The table-driven FP64 exp / log of the prologue and transfer kernels against CUDA's."""
     e, l = C.c_double(), C.c_double()
     assert ctx.lib.korg_math_selftest(ctx.h, 1 << 22, C.byref(e), C.byref(l)) == 0
-    print(f"fexp64 max {e.value:.2f} ulp, flog64 max abs err {l.value:.2e}")
+    print(f"fexp64 max {e.value:.2f} ulp, flog64 max err {l.value:.2e} of max(1, |log x|)")
     assert e.value <= 2.0
-    assert l.value <= 4e-15
+    assert l.value <= 5e-16
 
 
 def test_rt_parity(ctx, cfg0, oracle_lib):
