@@ -35,7 +35,7 @@ struct korg_ctx {
     cudaStream_t stream = nullptr;  // used by the host-pointer calls
     std::string err;
     // scratch arena: grown on demand, never shrunk, freed by korg_destroy
-    DevBuf lc, params, xfar, amask, lb, ub, pmax, smin, scanblk, counters;
+    DevBuf lc, params, xfar, amask, lb, ub, ci, tier_idx, tier_ci, tier_meta, counters;
     DevBuf hrec, hQ, hQ32, hulb, huub;
     DevBuf stage_dev, aref, alpha, flux, cntm, math;
     void* stage_host = nullptr;
@@ -190,13 +190,15 @@ int run_line_absorption(korg_ctx* ctx, double* alpha, const double* wls, int64_t
     KCHECK(ensure(ctx, ctx->amask, sizeof(uint32_t) * ln.n));
     KCHECK(ensure(ctx, ctx->lb, sizeof(int32_t) * ln.n));
     KCHECK(ensure(ctx, ctx->ub, sizeof(int32_t) * ln.n));
-    KCHECK(ensure(ctx, ctx->pmax, sizeof(int32_t) * ln.n));
-    KCHECK(ensure(ctx, ctx->smin, sizeof(int32_t) * ln.n));
-    KCHECK(ensure(ctx, ctx->scanblk, sizeof(int32_t) * 2 * ((ln.n + SCAN_CHUNK - 1) / SCAN_CHUNK)));
+    KCHECK(ensure(ctx, ctx->ci, sizeof(int32_t) * ln.n));
+    KCHECK(ensure(ctx, ctx->tier_idx, sizeof(int32_t) * ln.n));
+    KCHECK(ensure(ctx, ctx->tier_ci, sizeof(int32_t) * ln.n));
+    const int nblk = int((ln.n + PART_CHUNK - 1) / PART_CHUNK);
+    KCHECK(ensure(ctx, ctx->tier_meta, sizeof(int32_t) * (NTIER * size_t(nblk) + NTIER + 2)));
     auto* ctr = static_cast<unsigned long long*>(ctx->counters.p);
     layer_const_kernel<<<(L + 127) / 128, 128, 0, s>>>(lay, static_cast<LayerConst*>(ctx->lc.p));
     PrepOut po{ctx->params.p, static_cast<int32_t*>(ctx->lb.p), static_cast<int32_t*>(ctx->ub.p),
-               static_cast<float*>(ctx->xfar.p), static_cast<uint32_t*>(ctx->amask.p), Lp, kmax, G, ctr, ctr + 1};
+               static_cast<int32_t*>(ctx->ci.p), static_cast<float*>(ctx->xfar.p), static_cast<uint32_t*>(ctx->amask.p), Lp, kmax, G, ctr, ctr + 1};
     const size_t prep_smem = size_t(256 / 32) * Lp * (sizeof(float) + sizeof(int));
     const int64_t pthreads = ln.n * 32;
     const unsigned pblocks = unsigned((pthreads + 255) / 256);
@@ -207,11 +209,12 @@ int run_line_absorption(korg_ctx* ctx, double* alpha, const double* wls, int64_t
         line_prep64_kernel<<<pblocks, 256, prep_smem, s>>>(ln, lay, static_cast<LayerConst*>(ctx->lc.p), cn, wls, nwl, cutoff, po,
                                                    static_cast<MathTables*>(ctx->math.p));
     KCUDA(cudaGetLastError());
-    const int nblk = int((ln.n + SCAN_CHUNK - 1) / SCAN_CHUNK);
-    int32_t* bmax = static_cast<int32_t*>(ctx->scanblk.p);
-    window_block_kernel<<<nblk, SCAN_THREADS, 0, s>>>(po.lb, po.ub, ln.n, bmax, bmax + nblk);
-    window_scan_kernel<<<nblk, SCAN_THREADS, 0, s>>>(po.lb, po.ub, ln.n, bmax, bmax + nblk, nblk,
-                                                    static_cast<int32_t*>(ctx->pmax.p), static_cast<int32_t*>(ctx->smin.p));
+    int32_t* meta = static_cast<int32_t*>(ctx->tier_meta.p);  // [start: NTIER+1][unsorted][block counts]
+    TierLists tl{static_cast<int32_t*>(ctx->tier_idx.p), static_cast<int32_t*>(ctx->tier_ci.p), meta, meta + NTIER + 1};
+    int32_t* bcnt = meta + NTIER + 2;
+    KCUDA(cudaMemsetAsync(tl.unsorted, 0, sizeof(int32_t), s));
+    tier_count_kernel<<<nblk, PART_THREADS, 0, s>>>(po.lb, po.ub, po.ci, ln.n, bcnt, tl.unsorted);
+    tier_scatter_kernel<<<nblk, PART_THREADS, 0, s>>>(po.lb, po.ub, po.ci, ln.n, bcnt, nblk, tl);
     KCUDA(cudaGetLastError());
     record(ctx, 2, s);
     TileArgs ta{};
@@ -227,8 +230,10 @@ int run_line_absorption(korg_ctx* ctx, double* alpha, const double* wls, int64_t
     ta.params = ctx->params.p;
     ta.lb = po.lb;
     ta.ub = po.ub;
-    ta.pmax_ub = static_cast<int32_t*>(ctx->pmax.p);
-    ta.smin_lb = static_cast<int32_t*>(ctx->smin.p);
+    ta.tier_idx = tl.idx;
+    ta.tier_ci = tl.ci;
+    ta.tier_start = tl.start;
+    ta.unsorted = tl.unsorted;
     int rc;
     if (mixed)
         rc = dispatch_tile<true>(ctx, ta, G, kmax, s);
@@ -461,7 +466,7 @@ KORG_API void korg_destroy(korg_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    DevBuf* bufs[] = {&ctx->lc, &ctx->params, &ctx->xfar, &ctx->amask, &ctx->lb, &ctx->ub, &ctx->pmax, &ctx->smin, &ctx->scanblk, &ctx->counters,
+    DevBuf* bufs[] = {&ctx->lc, &ctx->params, &ctx->xfar, &ctx->amask, &ctx->lb, &ctx->ub, &ctx->ci, &ctx->tier_idx, &ctx->tier_ci, &ctx->tier_meta, &ctx->counters,
                       &ctx->hrec, &ctx->hQ, &ctx->hQ32, &ctx->hulb, &ctx->huub, &ctx->stage_dev, &ctx->aref,
                       &ctx->alpha, &ctx->flux, &ctx->cntm, &ctx->math};
     for (DevBuf* b : bufs)

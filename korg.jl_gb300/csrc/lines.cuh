@@ -62,6 +62,7 @@ struct PrepOut {
     void* params;            // [n][Lp] P64 (FP64) or float4 (mixed); layers L..Lp-1 are zero padding
     int32_t* lb;             // [n]
     int32_t* ub;             // [n]
+    int32_t* ci;             // [n] index of the first wavelength >= the line centre
     float* xfar;             // [n][G] |wl - wl0| beyond which every layer of group g is in a wing
                              //        branch: v >= 5 (a <= 0.2) or a + v >= 3.2 / a > 1.4 (a > 0.2)
     uint32_t* amask;         // [n] bit g: every layer of group g has a <= 0.2
@@ -137,6 +138,7 @@ __device__ __forceinline__ void store_window(const PrepOut& out, int64_t i, doub
     const int64_t ub = search_last(wls, nwl, wl + window);
     out.lb[i] = int32_t(lb);
     out.ub[i] = int32_t(ub);
+    out.ci[i] = int32_t(search_first(wls, nwl, wl));
     if (lb <= ub) {
         atomicAdd(out.evals, (unsigned long long)((ub - lb + 1) * L));
         atomicAdd(out.nlines, 1ull);
@@ -313,86 +315,101 @@ __global__ void __launch_bounds__(256) line_prep_mixed_kernel(LinesDev ln, Layer
     if (lane == 0) store_window(out, i, lwin, w, q.wl, wls, nwl, L);
 }
 
-// Running max of ub (prefix) and running min of lb (suffix) over the line list, in two
-// launches: per-block totals, then each block scans its chunk starting from the totals of the
-// blocks before (prefix) / after (suffix) it.  Lines with an empty window contribute nothing.
-constexpr int SCAN_THREADS = 256, SCAN_ITEMS = 8, SCAN_CHUNK = SCAN_THREADS * SCAN_ITEMS;
+// Candidate lists.  Lines are split by window half-width into tiers (at most 256, 4096, 65536
+// wavelength points, and wider).  Within a tier the lines keep list order, so their centre
+// indices are non-decreasing, and the lines that can overlap a tile [j0, j1] are the contiguous
+// run with centre index in [j0 - W - 1, j1 + W + 1]: two binary searches per tier.  A single
+// list with running max/min window bounds degenerates when a few lines have very wide windows
+// (one synthetic line can span the whole grid); the tiers bound the over-scan per tier.
+constexpr int NTIER = 4;
+__device__ __constant__ int32_t c_tier_w[NTIER] = {256, 4096, 65536, 0x3fffffff};
+constexpr int PART_THREADS = 256, PART_ITEMS = 8, PART_CHUNK = PART_THREADS * PART_ITEMS;
 
-__global__ void __launch_bounds__(SCAN_THREADS) window_block_kernel(const int32_t* lb, const int32_t* ub, int64_t n,
-                                                                    int32_t* bmax, int32_t* bmin) {
-    __shared__ int32_t s_mx[SCAN_THREADS / 32], s_mn[SCAN_THREADS / 32];
-    const int64_t base = int64_t(blockIdx.x) * SCAN_CHUNK;
-    int32_t mx = -1, mn = INT32_MAX;
-    for (int k = threadIdx.x; k < SCAN_CHUNK; k += SCAN_THREADS) {
-        const int64_t i = base + k;
-        if (i < n && lb[i] <= ub[i]) { mx = max(mx, ub[i]); mn = min(mn, lb[i]); }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-    }
-    if ((threadIdx.x & 31) == 0) { s_mx[threadIdx.x >> 5] = mx; s_mn[threadIdx.x >> 5] = mn; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int w = 1; w < SCAN_THREADS / 32; w++) { mx = max(mx, s_mx[w]); mn = min(mn, s_mn[w]); }
-        bmax[blockIdx.x] = mx;
-        bmin[blockIdx.x] = mn;
-    }
+__device__ __forceinline__ int line_tier(int32_t lb, int32_t ub, int32_t ci) {
+    if (lb > ub) return -1;  // empty window: never a candidate
+    const int32_t h = max(ci - lb, ub - ci);
+    int k = 0;
+    while (k < NTIER - 1 && h > c_tier_w[k]) k++;
+    return k;
 }
 
-__global__ void __launch_bounds__(SCAN_THREADS) window_scan_kernel(const int32_t* lb, const int32_t* ub, int64_t n,
-                                                                   const int32_t* bmax, const int32_t* bmin, int nblocks,
-                                                                   int32_t* pmax_ub, int32_t* smin_lb) {
-    __shared__ int32_t s_a[SCAN_THREADS], s_b[SCAN_THREADS];
-    __shared__ int32_t s_pre, s_suf;
-    const int t = threadIdx.x, blk = blockIdx.x;
-    // totals of the blocks before / after this one
-    int32_t pre = -1, suf = INT32_MAX;
-    for (int b = t; b < blk; b += SCAN_THREADS) pre = max(pre, bmax[b]);
-    for (int b = blk + 1 + t; b < nblocks; b += SCAN_THREADS) suf = min(suf, bmin[b]);
-    for (int o = 16; o > 0; o >>= 1) {
-        pre = max(pre, __shfl_xor_sync(0xffffffffu, pre, o));
-        suf = min(suf, __shfl_xor_sync(0xffffffffu, suf, o));
-    }
-    if ((t & 31) == 0) { s_a[t >> 5] = pre; s_b[t >> 5] = suf; }
+struct TierLists {
+    int32_t* idx;       // [n] line indices, tier by tier
+    int32_t* ci;        // [n] their centre indices
+    int32_t* start;     // [NTIER + 1] tier offsets into idx / ci
+    int32_t* unsorted;  // set when centre indices decrease along the list (full scans then)
+};
+
+// per-block tier counts, and the sortedness check
+__global__ void __launch_bounds__(PART_THREADS) tier_count_kernel(const int32_t* lb, const int32_t* ub,
+                                                                  const int32_t* ci, int64_t n, int32_t* bcnt,
+                                                                  int32_t* unsorted) {
+    __shared__ int32_t s_cnt[NTIER];
+    if (threadIdx.x < NTIER) s_cnt[threadIdx.x] = 0;
     __syncthreads();
-    if (t == 0) {
-        for (int w = 1; w < SCAN_THREADS / 32; w++) { pre = max(pre, s_a[w]); suf = min(suf, s_b[w]); }
-        s_pre = pre;
-        s_suf = suf;
-    }
-    __syncthreads();
-    // each thread owns SCAN_ITEMS consecutive lines
-    const int64_t i0 = int64_t(blk) * SCAN_CHUNK + int64_t(t) * SCAN_ITEMS;
-    int32_t mx = -1, mn = INT32_MAX;
-    for (int k = 0; k < SCAN_ITEMS; k++) {
-        const int64_t i = i0 + k;
-        if (i < n && lb[i] <= ub[i]) { mx = max(mx, ub[i]); mn = min(mn, lb[i]); }
-    }
-    s_a[t] = mx;
-    s_b[t] = mn;
-    __syncthreads();
-    for (int o = 1; o < SCAN_THREADS; o <<= 1) {  // inclusive prefix max / suffix min over threads
-        const int32_t a = t >= o ? s_a[t - o] : -1;
-        const int32_t c = t + o < SCAN_THREADS ? s_b[t + o] : INT32_MAX;
-        __syncthreads();
-        s_a[t] = max(s_a[t], a);
-        s_b[t] = min(s_b[t], c);
-        __syncthreads();
-    }
-    int32_t run = max(s_pre, t > 0 ? s_a[t - 1] : -1);
-    for (int k = 0; k < SCAN_ITEMS; k++) {
-        const int64_t i = i0 + k;
+    const int64_t base = int64_t(blockIdx.x) * PART_CHUNK;
+    int c[NTIER] = {0, 0, 0, 0};
+    bool bad = false;
+    for (int k = threadIdx.x; k < PART_CHUNK; k += PART_THREADS) {
+        const int64_t i = base + k;
         if (i >= n) break;
-        if (lb[i] <= ub[i]) run = max(run, ub[i]);
-        pmax_ub[i] = run;
+        const int t = line_tier(lb[i], ub[i], ci[i]);
+        if (t >= 0) c[t]++;
+        if (i > 0 && ci[i] < ci[i - 1]) bad = true;
     }
-    run = min(s_suf, t + 1 < SCAN_THREADS ? s_b[t + 1] : INT32_MAX);
-    for (int k = SCAN_ITEMS - 1; k >= 0; k--) {
+    for (int t = 0; t < NTIER; t++)
+        if (c[t]) atomicAdd(&s_cnt[t], c[t]);
+    if (bad) atomicOr(unsorted, 1);
+    __syncthreads();
+    if (threadIdx.x < NTIER) bcnt[blockIdx.x * NTIER + threadIdx.x] = s_cnt[threadIdx.x];
+}
+
+// stable scatter: position = tier base + lines of the tier in earlier blocks + rank in the block
+__global__ void __launch_bounds__(PART_THREADS) tier_scatter_kernel(const int32_t* lb, const int32_t* ub,
+                                                                    const int32_t* ci, int64_t n,
+                                                                    const int32_t* bcnt, int nblocks, TierLists out) {
+    __shared__ int32_t s_base[NTIER];
+    __shared__ int32_t s_scan[NTIER][PART_THREADS];
+    const int t0 = threadIdx.x;
+    if (t0 < NTIER) {
+        int32_t before = 0, total[NTIER] = {0, 0, 0, 0};
+        for (int b = 0; b < nblocks; b++) {
+            for (int k = 0; k < NTIER; k++) total[k] += bcnt[b * NTIER + k];
+            if (b < int(blockIdx.x)) before += bcnt[b * NTIER + t0];
+        }
+        int32_t tb = 0;
+        for (int k = 0; k < t0; k++) tb += total[k];
+        s_base[t0] = tb + before;
+        if (blockIdx.x == 0) {
+            out.start[t0] = tb;
+            if (t0 == NTIER - 1) out.start[NTIER] = tb + total[NTIER - 1];
+        }
+    }
+    // each thread owns PART_ITEMS consecutive lines
+    const int64_t i0 = int64_t(blockIdx.x) * PART_CHUNK + int64_t(t0) * PART_ITEMS;
+    int tier[PART_ITEMS];
+    int c[NTIER] = {0, 0, 0, 0};
+    for (int k = 0; k < PART_ITEMS; k++) {
         const int64_t i = i0 + k;
-        if (i >= n) continue;
-        if (lb[i] <= ub[i]) run = min(run, lb[i]);
-        smin_lb[i] = run;
+        tier[k] = i < n ? line_tier(lb[i], ub[i], ci[i]) : -1;
+        if (tier[k] >= 0) c[tier[k]]++;
+    }
+    for (int k = 0; k < NTIER; k++) s_scan[k][t0] = c[k];
+    __syncthreads();
+    for (int o = 1; o < PART_THREADS; o <<= 1) {  // inclusive scans of the per-thread counts
+        int32_t v[NTIER];
+        for (int k = 0; k < NTIER; k++) v[k] = t0 >= o ? s_scan[k][t0 - o] : 0;
+        __syncthreads();
+        for (int k = 0; k < NTIER; k++) s_scan[k][t0] += v[k];
+        __syncthreads();
+    }
+    int32_t pos[NTIER];
+    for (int k = 0; k < NTIER; k++) pos[k] = s_base[k] + s_scan[k][t0] - c[k];
+    for (int k = 0; k < PART_ITEMS; k++) {
+        if (tier[k] < 0) continue;
+        const int32_t p = pos[tier[k]]++;
+        out.idx[p] = int32_t(i0 + k);
+        out.ci[p] = ci[i0 + k];
     }
 }
 
@@ -412,21 +429,20 @@ struct TileArgs {
     const void* params;
     const float* xfar;
     const uint32_t* amask;
-    const int32_t *lb, *ub, *pmax_ub, *smin_lb;
+    const int32_t *lb, *ub;
+    const int32_t *tier_idx, *tier_ci, *tier_start, *unsorted;
 };
 
-// first index in [0, n) with a[i] >= v (a non-decreasing)
-__device__ __forceinline__ int64_t lower_bound_i32(const int32_t* a, int64_t n, int32_t v) {
-    int64_t lo = 0, hi = n;
+// first index in [lo, hi) with a[i] >= v (a non-decreasing)
+__device__ __forceinline__ int64_t lower_bound_i32(const int32_t* a, int64_t lo, int64_t hi, int32_t v) {
     while (lo < hi) {
         int64_t mid = lo + ((hi - lo) >> 1);
         if (a[mid] < v) lo = mid + 1; else hi = mid;
     }
     return lo;
 }
-// first index in [0, n) with a[i] > v (a non-decreasing)
-__device__ __forceinline__ int64_t upper_bound_i32(const int32_t* a, int64_t n, int32_t v) {
-    int64_t lo = 0, hi = n;
+// first index in [lo, hi) with a[i] > v (a non-decreasing)
+__device__ __forceinline__ int64_t upper_bound_i32(const int32_t* a, int64_t lo, int64_t hi, int32_t v) {
     while (lo < hi) {
         int64_t mid = lo + ((hi - lo) >> 1);
         if (a[mid] <= v) lo = mid + 1; else hi = mid;
@@ -474,7 +490,7 @@ __global__ void __launch_bounds__(MAXT, MINB) line_tile_kernel(TileArgs a) {
     double* s_alpha = reinterpret_cast<double*>(smem);                          // [TW][Lp+1], at the end
     LineStage* s_ln = reinterpret_cast<LineStage*>(smem + 2 * size_t(a.region));  // [blockDim]
     __shared__ int32_t s_warp[32];
-    __shared__ int64_t s_range[2];
+    __shared__ int32_t s_count;
 
     const int tid = threadIdx.x, nthr = blockDim.x;
     const int TW = nthr / G;
@@ -490,12 +506,22 @@ __global__ void __launch_bounds__(MAXT, MINB) line_tile_kernel(TileArgs a) {
     const float xj_hi = float(wl_j - wl_ref);
     const float xj_lo = float((wl_j - wl_ref) - double(xj_hi));
 
-    if (tid == 0) {
-        s_range[0] = lower_bound_i32(a.pmax_ub, a.n, int32_t(j0));
-        s_range[1] = upper_bound_i32(a.smin_lb, a.n, int32_t(jlast)) - 1;
+    // candidate runs of the width tiers (threads 0..NTIER-1 search one tier each)
+    __shared__ int64_t s_tier[NTIER][2];
+    if (tid < NTIER) {
+        const int64_t t0 = a.tier_start[tid], t1 = a.tier_start[tid + 1];
+        if (*a.unsorted) {
+            s_tier[tid][0] = t0;
+            s_tier[tid][1] = t1;
+        } else {
+            const int32_t w = c_tier_w[tid] + 1;
+            const int32_t lo = int32_t(max(int64_t(j0) - w, int64_t(INT32_MIN / 2)));
+            const int32_t hi = int32_t(min(int64_t(jlast) + w, int64_t(INT32_MAX / 2)));
+            s_tier[tid][0] = lower_bound_i32(a.tier_ci, t0, t1, lo);
+            s_tier[tid][1] = upper_bound_i32(a.tier_ci, t0, t1, hi);
+        }
     }
     __syncthreads();
-    const int64_t i_lo = s_range[0], i_hi = s_range[1];
 
     using Acc = typename std::conditional<MIXED, float, double>::type;
     Acc acc[K], comp[K];
@@ -504,14 +530,17 @@ __global__ void __launch_bounds__(MAXT, MINB) line_tile_kernel(TileArgs a) {
 
     const int warp = tid >> 5, lane = tid & 31, nwarps = nthr >> 5;
     const int chunks16 = Lp * int(sizeof(P) / 16);  // 16-byte pieces of one line's constants
-    for (int64_t base = i_lo; base <= i_hi; base += nthr) {
-        const int64_t i = base + tid;
+    for (int tier = 0; tier < NTIER; tier++)
+    for (int64_t base = s_tier[tier][0]; base < s_tier[tier][1]; base += nthr) {
+        const int64_t pidx = base + tid;
+        int64_t i = 0;
         bool take = false;
         int32_t lbi = 0, ubi = -1;
-        if (i <= i_hi) {
+        if (pidx < s_tier[tier][1]) {
+            i = a.tier_idx[pidx];
             lbi = a.lb[i];
             ubi = a.ub[i];
-            take = lbi <= ubi && lbi <= jlast && ubi >= j0;
+            take = lbi <= jlast && ubi >= j0;
         }
         const unsigned m = __ballot_sync(0xffffffffu, take);
         if (lane == 0) s_warp[warp] = __popc(m);
@@ -519,7 +548,7 @@ __global__ void __launch_bounds__(MAXT, MINB) line_tile_kernel(TileArgs a) {
         if (tid == 0) {
             int run = 0;
             for (int w = 0; w < nwarps; w++) { int c = s_warp[w]; s_warp[w] = run; run += c; }
-            s_range[0] = run;  // reused as the count
+            s_count = run;
         }
         __syncthreads();
         if (take) {  // the thread that found the line describes it for the whole CTA
@@ -539,10 +568,10 @@ __global__ void __launch_bounds__(MAXT, MINB) line_tile_kernel(TileArgs a) {
             st.lb = lbi;
             st.ub = ubi;
             st.cls = cls;
-            st.li = int32_t(i - base);
+            st.li = int32_t(i);
             s_ln[s_warp[warp] + __popc(m & ((1u << lane) - 1))] = st;
         }
-        const int cnt = int(s_range[0]);
+        const int cnt = s_count;
         __syncthreads();
 
         // batches of B lines: constants copied with cp.async into two alternating buffers
@@ -553,7 +582,7 @@ __global__ void __launch_bounds__(MAXT, MINB) line_tile_kernel(TileArgs a) {
                 unsigned char* buf = smem + size_t(q & 1) * a.region;
                 for (int e = tid; e < nb * chunks16; e += nthr) {
                     const int b = e / chunks16, r = e - b * chunks16;
-                    const int64_t li = base + s_ln[b0 + b].li;
+                    const int64_t li = s_ln[b0 + b].li;
                     cp_async16(buf + (size_t(b) * chunks16 + r) * 16,
                                reinterpret_cast<const unsigned char*>(a.params) + (li * chunks16 + r) * 16);
                 }
