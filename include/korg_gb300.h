@@ -39,7 +39,8 @@ typedef enum {
     KORG_EINVAL = 1,   /* bad argument (sizes, null pointers, unsorted input, bad scheme) */
     KORG_ECUDA = 2,    /* a CUDA runtime call failed; korg_last_error() has the message */
     KORG_ENOMEM = 3,   /* device allocation failed */
-    KORG_ENOTABLES = 4 /* hydrogen lines requested before korg_set_stark_tables() */
+    KORG_ENOTABLES = 4, /* hydrogen lines requested before korg_set_stark_tables() */
+    KORG_ETOOBIG = 5    /* the problem needs more scratch than KORG_NOALLOC_SCRATCH_BYTES */
 } korg_status;
 
 enum { KORG_FP64 = 0, KORG_MIXED = 1 };
@@ -188,6 +189,26 @@ KORG_API int korg_probe_flops(korg_ctx *ctx, int fp64, double *tflops);
  * used by the prologue and transfer kernels with the CUDA exp and log on n points; returns the
  * largest exp error in ulps and the largest log error relative to max(1, |log x|). */
 KORG_API int korg_math_selftest(korg_ctx *ctx, int64_t n, double *max_ulp_exp, double *max_abs_log);
+
+/* No counterpart in the reference: line_absorption! for callers that cannot allocate device
+ * memory -- code running inside a memory pool or arena it does not own, a process whose
+ * allocator is locked after start-up, or a caller in the middle of stream capture.  Same
+ * arguments and results as korg_line_absorption_dev (device pointers, alpha accumulated in
+ * place on `stream`), but no context and no cudaMalloc / cudaFree / allocating library call:
+ * all scratch lives in one file-scope device array of KORG_NOALLOC_SCRATCH_BYTES (64 MiB) that
+ * every GPU loading the library holds until exit.  That is enough for about 70,000 lines of a
+ * 56-layer atmosphere in KORG_MIXED (constants take layers x 16 bytes per line, 48 in
+ * KORG_FP64); larger problems return KORG_ETOOBIG without launching anything.
+ * The first call on a device looks up the array's address and writes lookup tables into it
+ * with a synchronous copy: make that first call before any stream capture.  Every call shares
+ * the one array (its counters are cleared at the start of each call, the rest is overwritten),
+ * so calls whose work overlaps on the GPU -- different streams, or threads without ordering --
+ * race; serialise them on one stream. */
+#define KORG_NOALLOC_SCRATCH_BYTES (64u << 20)
+KORG_API int korg_line_absorption_noalloc(double *alpha, const double *wls, int64_t nwl,
+                                          const korg_lines *lines, const korg_layers *layers,
+                                          const korg_cntm *cntm, double cutoff_threshold,
+                                          int precision, void *stream);
 
 #ifdef __cplusplus
 }

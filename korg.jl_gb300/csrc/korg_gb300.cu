@@ -7,6 +7,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -862,4 +863,149 @@ extern "C" KORG_API int korg_probe_flops(korg_ctx* ctx, int fp64, double* tflops
     const double flops = 2.0 * 8.0 * double(iters) * blocks * threads;
     *tflops = flops / (best * 1e-3) / 1e12;
     return KORG_OK;
+}
+
+// ====================================================================== allocation-free entry point
+// Some callers cannot allocate device memory: code running inside a memory pool or arena that
+// the caller owns, a process whose allocator is locked down after start-up, or a caller in the
+// middle of stream capture.  korg_line_absorption_noalloc serves them: it runs the same
+// line-opacity kernels as korg_line_absorption_dev but keeps all of its scratch (line constants,
+// windows, candidate lists, counters, math tables) in one file-scope device array of fixed
+// size, so it never calls cudaMalloc, cudaFree or any allocating library routine.
+namespace {
+
+constexpr size_t NOALLOC_SCRATCH_BYTES = size_t(64) << 20;  // KORG_NOALLOC_SCRATCH_BYTES in the header
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mutex;
+unsigned char* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};  // device address of the array, per device
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Device address of the scratch array for the current device; the first call on a device looks
+// it up and writes the math tables into it (a synchronous copy, hence before any capture).
+int noalloc_setup(int dev, unsigned char** out) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return KORG_EINVAL;
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return KORG_ECUDA;
+        MathTables t;
+        fill_math_tables(t);
+        if (cudaMemcpy(p, &t, sizeof t, cudaMemcpyHostToDevice) != cudaSuccess) return KORG_ECUDA;
+        g_noalloc_ptr[dev] = static_cast<unsigned char*>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return KORG_OK;
+}
+
+template <bool MIXED, int KMAX, int MAXT, int MINB>
+int noalloc_launch_tile(TileArgs ta, int G, cudaStream_t s) {
+    using P = typename ParamT<MIXED>::type;
+    const int Lp = ta.Lp;
+    const int B = MIXED ? STAGE_LINES : STAGE_LINES / 2;
+    ta.stage = B;
+    ta.G = G;
+    const int TW = TILE_TW, threads = TW * G;
+    size_t region = size_t(B) * Lp * sizeof(P);
+    region = std::max(region, (size_t(TW) * (Lp + 1) * sizeof(double) + 1) / 2);
+    region = (region + 15) & ~size_t(15);
+    ta.region = int(region);
+    const size_t smem = 2 * region + size_t(threads) * sizeof(LineStage);
+    auto kern = line_tile_kernel<MIXED, KMAX, MAXT, MINB>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess)
+        return KORG_ECUDA;
+    kern<<<dim3(unsigned((ta.nwl + TW - 1) / TW)), threads, smem, s>>>(ta);
+    return cudaGetLastError() == cudaSuccess ? KORG_OK : KORG_ECUDA;
+}
+
+template <bool MIXED>
+int noalloc_dispatch_tile(const TileArgs& ta, int G, int kmax, cudaStream_t s) {
+    if (kmax == 14 && G <= 4) return noalloc_launch_tile<MIXED, 14, 256, MIXED ? 3 : 2>(ta, G, s);
+    if (kmax == 14) return noalloc_launch_tile<MIXED, 14, 512, 1>(ta, G, s);
+    if (kmax == 16) return noalloc_launch_tile<MIXED, 16, 512, 1>(ta, G, s);
+    return noalloc_launch_tile<MIXED, 32, 512, 1>(ta, G, s);
+}
+
+}  // namespace
+
+extern "C" KORG_API int korg_line_absorption_noalloc(double* alpha, const double* wls, int64_t nwl,
+                                                    const korg_lines* lines, const korg_layers* layers,
+                                                    const korg_cntm* cntm, double cutoff, int precision,
+                                                    void* stream) {
+    if (!alpha || !wls || nwl < 1 || !lines || !layers || !cntm || cntm->nk < 1 || lines->n < 0) return KORG_EINVAL;
+    if (lines->n == 0) return KORG_OK;  // src/line_absorption.jl:35-37: alpha untouched
+    const bool mixed = precision == KORG_MIXED;
+    const int L = layers->L;
+    int kmax = 0;
+    const int G = layer_groups(L, &kmax);
+    if (L < 1 || G < 0 || lines->n > INT32_MAX || nwl > INT32_MAX - 1) return KORG_EINVAL;
+    const int64_t n = lines->n;
+    const int Lp = G * kmax;
+    const int nblk = int((n + PART_CHUNK - 1) / PART_CHUNK);
+    // scratch layout (every piece 256-byte aligned)
+    size_t off = 0;
+    const size_t o_math = off; off += align256(sizeof(MathTables));
+    const size_t o_ctr = off; off += align256(4 * sizeof(unsigned long long));
+    const size_t o_lc = off; off += align256(sizeof(LayerConst) * L);
+    const size_t o_par = off; off += align256((mixed ? sizeof(float4) : sizeof(P64)) * size_t(n) * Lp);
+    const size_t o_xfar = off; off += align256(sizeof(float) * size_t(n) * G);
+    const size_t o_am = off; off += align256(sizeof(uint32_t) * size_t(n));
+    const size_t o_lb = off; off += align256(sizeof(int32_t) * size_t(n));
+    const size_t o_ub = off; off += align256(sizeof(int32_t) * size_t(n));
+    const size_t o_ci = off; off += align256(sizeof(int32_t) * size_t(n));
+    const size_t o_ti = off; off += align256(sizeof(int32_t) * size_t(n));
+    const size_t o_tc = off; off += align256(sizeof(int32_t) * size_t(n));
+    const size_t o_meta = off; off += align256(sizeof(int32_t) * (NTIER * size_t(nblk) + NTIER + 2));
+    if (off > NOALLOC_SCRATCH_BYTES) return KORG_ETOOBIG;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return KORG_ECUDA;
+    unsigned char* sp = nullptr;
+    int rc = noalloc_setup(dev, &sp);
+    if (rc != KORG_OK) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    auto* ctr = reinterpret_cast<unsigned long long*>(sp + o_ctr);
+    int32_t* meta = reinterpret_cast<int32_t*>(sp + o_meta);  // [start: NTIER+1][unsorted][block counts]
+    // the array keeps the previous call's contents: zero the counters and the sortedness flag
+    if (cudaMemsetAsync(ctr, 0, 4 * sizeof(unsigned long long), s) != cudaSuccess) return KORG_ECUDA;
+    if (cudaMemsetAsync(meta + NTIER + 1, 0, sizeof(int32_t), s) != cudaSuccess) return KORG_ECUDA;
+    const LinesDev ln = lines_dev(lines);
+    const LayersDev lay = layers_dev(layers);
+    const CntmDev cn{cntm->nk, cntm->knots, cntm->vals};
+    auto* lc = reinterpret_cast<LayerConst*>(sp + o_lc);
+    auto* math = reinterpret_cast<MathTables*>(sp + o_math);
+    layer_const_kernel<<<(L + 127) / 128, 128, 0, s>>>(lay, lc);
+    PrepOut po{sp + o_par, reinterpret_cast<int32_t*>(sp + o_lb), reinterpret_cast<int32_t*>(sp + o_ub),
+               reinterpret_cast<int32_t*>(sp + o_ci), reinterpret_cast<float*>(sp + o_xfar),
+               reinterpret_cast<uint32_t*>(sp + o_am), Lp, kmax, G, ctr, ctr + 1};
+    const size_t prep_smem = size_t(256 / 32) * Lp * (sizeof(float) + sizeof(int));
+    const unsigned pblocks = unsigned((n * 32 + 255) / 256);
+    if (mixed)
+        line_prep_mixed_kernel<<<pblocks, 256, prep_smem, s>>>(ln, lay, lc, cn, wls, nwl, cutoff, po, math);
+    else
+        line_prep64_kernel<<<pblocks, 256, prep_smem, s>>>(ln, lay, lc, cn, wls, nwl, cutoff, po, math);
+    TierLists tl{reinterpret_cast<int32_t*>(sp + o_ti), reinterpret_cast<int32_t*>(sp + o_tc), meta, meta + NTIER + 1};
+    int32_t* bcnt = meta + NTIER + 2;
+    tier_count_kernel<<<nblk, PART_THREADS, 0, s>>>(po.lb, po.ub, po.ci, n, bcnt, tl.unsorted);
+    tier_scatter_kernel<<<nblk, PART_THREADS, 0, s>>>(po.lb, po.ub, po.ci, n, bcnt, nblk, tl);
+    if (cudaGetLastError() != cudaSuccess) return KORG_ECUDA;
+    TileArgs ta{};
+    ta.alpha = alpha;
+    ta.wls = wls;
+    ta.nwl = nwl;
+    ta.L = L;
+    ta.Lp = Lp;
+    ta.xfar = po.xfar;
+    ta.amask = po.amask;
+    ta.n = n;
+    ta.wl = ln.wl;
+    ta.params = po.params;
+    ta.lb = po.lb;
+    ta.ub = po.ub;
+    ta.tier_idx = tl.idx;
+    ta.tier_ci = tl.ci;
+    ta.tier_start = tl.start;
+    ta.unsorted = tl.unsorted;
+    return mixed ? noalloc_dispatch_tile<true>(ta, G, kmax, s) : noalloc_dispatch_tile<false>(ta, G, kmax, s);
 }

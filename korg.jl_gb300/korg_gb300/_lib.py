@@ -19,7 +19,7 @@ _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
 _lp = C.POINTER(C.c_int64)
 
-ERRORS = {1: "KORG_EINVAL", 2: "KORG_ECUDA", 3: "KORG_ENOMEM", 4: "KORG_ENOTABLES"}
+ERRORS = {1: "KORG_EINVAL", 2: "KORG_ECUDA", 3: "KORG_ENOMEM", 4: "KORG_ENOTABLES", 5: "KORG_ETOOBIG"}
 
 
 class KorgError(RuntimeError):
@@ -100,6 +100,8 @@ def lib():
                                               C.c_int64, C.c_int, vp, vp, vp, vp]
             L.korg_probe_flops.argtypes = [vp, C.c_int, _dp]
             L.korg_math_selftest.argtypes = [vp, C.c_int64, _dp, _dp]
+            L.korg_line_absorption_noalloc.argtypes = [vp, vp, C.c_int64, C.POINTER(Lines), C.POINTER(Layers),
+                                                       C.POINTER(Cntm), C.c_double, C.c_int, vp]
             _lib = L
     return _lib
 
@@ -110,7 +112,7 @@ def exported_symbols():
             "korg_set_stark_tables", "korg_line_absorption", "korg_line_absorption_dev",
             "korg_hydrogen_line_absorption", "korg_hydrogen_lines_dev", "korg_radiative_transfer",
             "korg_radiative_transfer_dev", "korg_synthesize", "korg_synthesize_dev", "korg_probe_flops",
-            "korg_math_selftest"]
+            "korg_math_selftest", "korg_line_absorption_noalloc"]
 
 
 def _p(a, kind=_dp):
