@@ -33,7 +33,7 @@ CPU_SAMPLE = [(3140.0 + 350.0 * k, 3210.0 + 350.0 * k) for k in range(20)]
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="korg", choices=["korg", "reference"])
     ap.add_argument("--lines", type=int, default=300_000)
@@ -334,7 +334,8 @@ def run_korg(args):
         "config": {"workload": "full optical synthesis: 56 layers (Teff 5800, logg 4.4, [M/H] 0), "
                                f"{args.lines} atomic lines + hydrogen lines, {args.wl[0]:.0f}-{args.wl[1]:.0f} A "
                                f"@ 0.01 A ({nwl} points)",
-                   "precision": "mixed", "l2": "flushed (256 MiB write) between steps; alpha (314 MB) > L2",
+                   "precision": "mixed",
+                   "l2": f"flushed (256 MiB write) between steps; alpha {8 * L * nwl / 1e6:.0f} MB",
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
                    "host_prep_s": host_prep_s},
         "evals_per_step": evals,
