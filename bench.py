@@ -9,6 +9,13 @@ grid (3000-10000 A at 0.01 A), mixed precision, inputs resident in HBM.  Prints 
 
 --impl reference times the FP64 CPU restatement of the reference (the oracle, all host cores)
 on a bounded sample of the same workload.
+
+    python bench.py --workload batch [--spectra 256]
+
+times the batched form instead: 256 atmospheres (Teff 3500-7000 K, logg 1-5, [M/H] -2.5..0.5),
+each with its own random 20k-200k-line subset of a 500k-line atomic + molecular list, on the
+400,001-point 15000-17000 A grid; one step = the whole batch through korg_synthesize_batch_dev
+(CUDA-graph replay, autotuned tile shape).
 """
 import argparse
 import ctypes as C
@@ -33,7 +40,7 @@ CPU_SAMPLE = [(3140.0 + 350.0 * k, 3210.0 + 350.0 * k) for k in range(20)]
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=None, help="timed steps (20; 3 for --workload batch)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="korg", choices=["korg", "reference"])
     ap.add_argument("--lines", type=int, default=300_000)
@@ -41,6 +48,8 @@ def parse():
                     help="wavelength range in A (the full workload is 3000-10000)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--workload", default="synth", choices=["synth", "batch"])
+    ap.add_argument("--spectra", type=int, default=256, help="batch workload: number of spectra")
     return ap.parse_args()
 
 
@@ -317,7 +326,8 @@ def run_korg(args):
         cpu = {"value": v, "unit": "spectra/s", "cores": threads, "kind": "port", "sample": info,
                "evals_per_s": ev_cpu / dt, "seconds": dt}
 
-    launches_per_step = 1 + 4 + (3 if inp.hydrogen_lines else 0) + 4 + 1
+    # alpha init, reference-wavelength lines (5), hydrogen (3), metal lines (5), transfer
+    launches_per_step = 1 + 5 + (3 if inp.hydrogen_lines else 0) + 5 + 1
     out = {
         "metric": METRIC,
         "value": world * 1000.0 / ms,
@@ -364,9 +374,174 @@ def run_korg(args):
         tdist.destroy_process_group()
 
 
+def _prep_batch_one(w):
+    sys.path.insert(0, os.path.join(ROOT, "korg.jl_gb300"))
+    from korg_gb300 import synthetic
+    return synthetic.prepare(w)
+
+
+def batch_inputs(n_spectra):
+    """Host precompute of the batch workload in a spawn pool (before any CUDA call)."""
+    import multiprocessing as mp
+    from korg_gb300 import synthetic
+    works = synthetic.config3(n_spectra=n_spectra)
+    with mp.get_context("spawn").Pool(min(len(works), os.cpu_count() or 1)) as pool:
+        return pool.map(_prep_batch_one, works, chunksize=1)
+
+
+def cpu_sample_batch(inp, threads):
+    """Oracle on spectrum 0 of the batch over 10 windows of 20 A (10% of its grid)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import copy
+    import oracle
+    from korg_gb300.data import stark_profiles
+    from korg_gb300.wavelengths import Wavelengths
+    oracle.build()
+    s = copy.copy(inp)
+    s.wls = Wavelengths([(15090.0 + 200.0 * k, 15110.0 + 200.0 * k, 0.005) for k in range(10)])
+    frac = len(s.wls) / len(inp.wls)
+    t0 = time.perf_counter()
+    _, _, _, _, ev = oracle.synthesize(s, s.linelist, s.linelist5, stark_profiles(), s.wls.all_wls, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return frac / dt, dt, ev, (f"spectrum 0 of the batch ({len(inp.linelist)} lines) on 10 windows of 20 A "
+                               f"({len(s.wls)} of {len(inp.wls)} points, fraction {frac:.4f}); "
+                               "spectra/s = fraction / seconds")
+
+
+def _progress(msg, t0=time.perf_counter()):
+    print(f"[bench {time.perf_counter() - t0:8.1f} s] {msg}", file=sys.stderr, flush=True)
+
+
+def run_batch(args):
+    import numpy as np
+    t0 = time.perf_counter()
+    _progress(f"host precompute of {args.spectra} spectra")
+    inps = batch_inputs(args.spectra)
+    host_prep_s = time.perf_counter() - t0
+    _progress(f"host precompute done ({host_prep_s:.1f} s, {sum(len(i.linelist) for i in inps)} lines)")
+    import torch
+    import build as korg_build
+    from korg_gb300 import _lib
+    from korg_gb300.batch import BatchSynthesis
+    korg_build.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    nwl, L, n = len(inps[0].wls), len(inps[0].T), len(inps)
+    # one chunk: every spectrum's alpha and line scratch resident at once
+    b = BatchSynthesis(inps, precision="mixed", use_graph=True, autotune=True, max_scratch_bytes=160 << 30)
+    stream = torch.cuda.current_stream(dev)
+    _progress("inputs resident on the device")
+    for w in range(max(args.warmup, 3)):  # eager + autotune, capture, replay
+        b.run(stream)
+        torch.cuda.synchronize()
+        _progress(f"warm-up {w} done")
+    clk = Clocks(0)
+    times = []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.run(stream)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    ms = statistics.mean(times)
+    _progress(f"timed steps done: {ms:.1f} ms per batch")
+    flux_mixed, cntm_mixed = b.results()
+    stats = b.ctx.stats()
+    evals = stats.line_evals
+    cfg = b.tile_config()
+    # end to end: one pinned host->device copy of every input, the batch, flux back to the host
+    out_host = torch.empty((n, nwl), dtype=torch.float64, pin_memory=True)
+    e2e_t = []
+    for _ in range(max(2, min(args.steps, 5))):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        b.upload()
+        f, _ = b.run(stream)
+        out_host.copy_(f, non_blocking=True)
+        torch.cuda.synchronize()
+        e2e_t.append(time.perf_counter() - t1)
+    e2e_s = statistics.mean(e2e_t)
+    assert np.array_equal(out_host.numpy(), flux_mixed)
+    # stage times of one eager run (timing events are not part of the graph)
+    b.ctx.check(b.ctx.lib.korg_set_batch_options(b.ctx.h, 0, 1, 160 << 30))
+    b.ctx.check(b.ctx.lib.korg_set_timing(b.ctx.h, 1))
+    b.run(stream)
+    st = b.ctx.stats()
+    b.ctx.check(b.ctx.lib.korg_set_timing(b.ctx.h, 0))
+    peak = C.c_double(0)
+    b.ctx.check(b.ctx.lib.korg_probe_flops(b.ctx.h, 0, C.byref(peak)))
+    achieved = evals * FLOP_PER_EVAL / (st.ms_line_tile * 1e-3) / 1e12
+    _progress("e2e and stage timing done")
+    # plain FP64 and mixed on the first 8 spectra: speed-up and error of the mixed form
+    sub = inps[:8]
+    res = {}
+    for prec in ("mixed", "fp64"):
+        bs = BatchSynthesis(sub, precision=prec, use_graph=False, autotune=False, max_scratch_bytes=160 << 30)
+        bs.run(stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        bs.run(stream)
+        e1.record(stream)
+        e1.synchronize()
+        res[prec] = (e0.elapsed_time(e1), *bs.results())
+        bs.ctx.close()
+    fm, cm = res["mixed"][1], res["mixed"][2]
+    f64, c64 = res["fp64"][1], res["fp64"][2]
+    fp64 = {"spectra": len(sub), "spectra_per_s": 1000.0 * len(sub) / res["fp64"][0],
+            "mixed_spectra_per_s": 1000.0 * len(sub) / res["mixed"][0],
+            "mixed_speedup": res["fp64"][0] / res["mixed"][0],
+            "mixed_max_rel_flux_err": float(np.max(np.abs(fm / f64 - 1))),
+            "mixed_max_rectified_err": float(np.max(np.abs(fm / cm - f64 / c64))),
+            "mixed_rectified_rms": float(np.sqrt(np.mean((fm / cm - f64 / c64) ** 2)))}
+    _progress("FP64 comparison done")
+    cpu = None
+    if not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v, dt, ev_cpu, info = cpu_sample_batch(inps[0], threads)
+        _progress("CPU sample done")
+        cpu = {"value": v, "unit": "spectra/s", "cores": threads, "kind": "port", "sample": info,
+               "evals_per_s": ev_cpu / dt, "seconds": dt}
+    nchunk = 1
+    out = {
+        "metric": METRIC, "value": 1000.0 * n / ms, "unit": "spectra/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 profiles + f64 tau/flux (mixed)",
+        "data": "synthetic (seeded line list and stand-in atmospheres)",
+        "config": {"workload": f"batch of {n} spectra: 56 layers, Teff 3500-7000 K, logg 1-5, [M/H] -2.5..0.5, "
+                               f"seeded random 20k-200k-line subsets of a 500k-line atomic + molecular list, "
+                               f"15000-17000 A @ 0.005 A ({nwl} points); one step = the whole batch",
+                   "precision": "mixed", "lines_per_spectrum": [len(i.linelist) for i in inps][:8] + ["..."],
+                   "l2": f"batch alpha {8 * L * nwl * n / 1e9:.1f} GB >> L2", "graph": True, "tile": cfg,
+                   "host_prep_s": host_prep_s},
+        "evals_per_step": evals, "evals_per_s": evals / (ms * 1e-3),
+        "stages_ms": {"total_eager": st.ms_total, "line_tile_queue": st.ms_line_tile, "rt_all": st.ms_rt},
+        "fp64": fp64,
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
+                     "frac": achieved / peak.value, "traffic": None,
+                     "kernel": "line_tile_queue_kernel<mixed> (one persistent launch over the batch)",
+                     "algorithmic": f"{FLOP_PER_EVAL} FP32 flop x {evals} line-layer-lambda evals per launch",
+                     "peak_source": "measured in-process (korg_probe_flops: FP32 FMA chains)"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": n / e2e_s, "unit": "spectra/s", "h2d_bytes_per_step": b.h2d_bytes,
+                "d2h_bytes_per_step": 8 * nwl * n},
+        "gpu_launches": args.steps * (n * 14 + nchunk),
+        "clocks": clocks,
+    }
+    print(json.dumps(out), flush=True)
+    b.ctx.close()
+
+
 if __name__ == "__main__":
     a = parse()
+    if a.steps is None:
+        a.steps = 3 if a.workload == "batch" else 20
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload == "batch":
+        run_batch(a)
     else:
         run_korg(a)

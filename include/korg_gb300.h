@@ -166,6 +166,22 @@ KORG_API int korg_radiative_transfer_dev(korg_ctx *ctx, const double *alpha, con
                                          int32_t L, int64_t nwl, const double *tau_ref,
                                          const double *alpha_ref, double *flux, void *stream);
 
+/* RadiativeTransfer.radiative_transfer(alpha, S, spatial_coord, mu_points, spherical;
+ * include_inward_rays, alpha_ref, tau_ref, I_scheme, tau_scheme) -- RadiativeTransfer.jl:77-139
+ * with any scheme: spatial = heights (planar) or radii (spherical), the surface mu grid and its
+ * weights (generate_mu_grid, :13-30, is the caller's), tau_scheme 0 = "anchored", 1 = "bezier";
+ * I_scheme 0 = "linear", 1 = "linear_flux_only", 2 = "bezier", 3 = the exponential-integral
+ * flux (planar, anchored).  flux[nwl] = 2 pi sum_mu w mu I(mu, surface); I_surface
+ * (n_mu x nwl, may be NULL) gets the outward surface intensities.  The ShellAtmosphere
+ * photosphere correction (:73) is the caller's.  Host pointers. */
+KORG_API int korg_radiative_transfer_general(korg_ctx *ctx, const double *alpha, const double *S,
+                                             int32_t L, int64_t nwl, const double *spatial,
+                                             int spherical, const double *tau_ref,
+                                             const double *alpha_ref, const double *mu,
+                                             const double *mu_weights, int32_t n_mu,
+                                             int include_inward_rays, int tau_scheme,
+                                             int I_scheme, double *flux, double *I_surface);
+
 /* synthesize(atm, linelist, A_X, wavelengths) steps after chemical equilibrium and continuum
  * (src/synthesize.jl:249-318): alpha_ref lines at the reference wavelength, source function,
  * continuum-only transfer, hydrogen lines, metal/molecular lines, final transfer.  lines5 is
@@ -179,6 +195,71 @@ KORG_API int korg_synthesize_dev(korg_ctx *ctx, const korg_synth_inputs *in,
                                  const korg_lines *lines, const korg_lines *lines5,
                                  const double *wls, int64_t nwl, int precision, double *flux,
                                  double *cntm, double *alpha_out, void *stream);
+
+/* Reverse mode of korg_synthesize (the vector-Jacobian product of the hot path), for
+ * gradient-based fitting (src/Fit/fit_via_synthesis.jl:304-390, where the reference uses
+ * ForwardDiff through synthesize).  Given cotangents dflux and dcntm (nwl each; either may be
+ * NULL) of synthesize's flux and continuum flux, fills the gradients the caller asks for
+ * (NULL pointers are skipped; the others are overwritten):
+ *   T, ne, n_eff_vdW, xi, nH_I, nHe_I, UH_I      [L]   layer inputs of korg_synth_inputs
+ *   n_div_U                                      [S*L] n(species)/U(species, T) rows
+ *   log_gf                                       [lines->n] per line of `lines`
+ *   cntm_vals                                    [L*nk] continuum interpolant knots
+ *   alpha_ref_cntm                               [L]   continuum opacity at the reference wl
+ * The inputs are independent variables here: the chain rule through the host's chemical
+ * equilibrium, partition functions and continuum (T -> n, U, alpha_cntm) is the caller's.
+ * alpha is recomputed (not stored by the forward call); the line windows carry no derivative,
+ * as under ForwardDiff.  With KORG_VJP_HYDROGEN the hydrogen-line opacity contributes too,
+ * through central differences of the FP64 hydrogen kernel (its Jacobian is layer diagonal);
+ * without it, hydrogen lines are held fixed. */
+typedef struct {
+    double *T, *ne, *n_eff_vdW, *xi;
+    double *n_div_U;
+    double *nH_I, *nHe_I, *UH_I;
+    double *log_gf;
+    double *cntm_vals;
+    double *alpha_ref_cntm;
+} korg_synth_grads;
+enum { KORG_VJP_HYDROGEN = 1 };
+KORG_API int korg_synthesize_vjp(korg_ctx *ctx, const korg_synth_inputs *in, const korg_lines *lines,
+                                 const korg_lines *lines5, const double *wls, int64_t nwl,
+                                 int precision, const double *dflux, const double *dcntm,
+                                 const korg_synth_grads *grads, int flags);
+KORG_API int korg_synthesize_vjp_dev(korg_ctx *ctx, const korg_synth_inputs *in,
+                                     const korg_lines *lines, const korg_lines *lines5,
+                                     const double *wls, int64_t nwl, int precision,
+                                     const double *dflux, const double *dcntm,
+                                     const korg_synth_grads *grads, int flags, void *stream);
+
+/* Batched synthesis: many spectra on one wavelength grid, as the Fit module's repeated-synthesis
+ * loop (src/Fit/fit_via_synthesis.jl:304-390) and grid building call synthesize.  Each item is
+ * one synthesize call of korg_synthesize_dev (device pointers inside; flux and cntm are device
+ * arrays of nwl); all items need the same layer count.  The per-spectrum prologues run first,
+ * then one persistent launch of the line tile kernel works through a queue of
+ * (spectrum, wavelength-tile) items, then the transfers; spectra are processed in chunks whose
+ * scratch fits the budget of korg_set_batch_options.  Results equal korg_synthesize_dev's
+ * for the same tile shape.  korg_stats for a batch: line_evals and lines_in_window are
+ * totals, ms_total covers the batch, ms_line_tile and ms_rt the last chunk. */
+typedef struct {
+    korg_synth_inputs in;
+    korg_lines lines;   /* this spectrum's (pruned) line list */
+    korg_lines lines5;  /* reference-wavelength line list */
+    double *flux, *cntm;
+} korg_batch_item;
+KORG_API int korg_synthesize_batch_dev(korg_ctx *ctx, int32_t nspec, const korg_batch_item *items,
+                                       const double *wls, int64_t nwl, int precision, void *stream);
+/* Batch options (no counterpart in the reference).  use_graph: a batch submitted twice in a row
+ * with identical items (same pointers and sizes; the contents may change) is captured into a
+ * CUDA graph on the second submission and replayed from then on.  autotune: the first large
+ * line-opacity launch for a (layer count, precision) times every candidate tile shape on its
+ * real inputs and keeps the fastest for the context.  max_scratch_bytes: chunk budget for the
+ * batch's alpha and line scratch (0 keeps the current value, 32 GiB by default). */
+KORG_API int korg_set_batch_options(korg_ctx *ctx, int use_graph, int autotune,
+                                    int64_t max_scratch_bytes);
+/* The tile shape the context uses for (L, precision): wavelengths per CTA, lines per shared
+ * memory batch, and whether it came from the autotuner. */
+KORG_API int korg_get_tile_config(korg_ctx *ctx, int32_t L, int precision, int32_t *tw,
+                                  int32_t *stage, int32_t *tuned);
 
 /* Not a counterpart of any reference function: measures the device's sustained FP32
  * (fp64 == 0) or FP64 FMA throughput in TFLOP/s with independent FMA chains, the roofline

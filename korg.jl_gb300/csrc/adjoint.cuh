@@ -1,0 +1,590 @@
+// adjoint.cuh -- reverse-mode (vector-Jacobian) kernels of the synthesis hot path.
+//
+// Given cotangents dL/dF(lambda) and dL/dC(lambda) of the flux and continuum flux, they give
+// dL/d(layer temperatures, n_e, n_eff_vdW, microturbulence, n/U per species, per-line log gf,
+// continuum opacity knots, reference-wavelength continuum opacity):
+//
+//   rt_adjoint_kernel    one warp per wavelength column: tau by a warp-shuffle prefix scan,
+//                        E2 / exp per layer in parallel, the segment partial derivatives of the
+//                        exponential-integral formal solution, and the reverse (suffix) scan of
+//                        the tau recursion.  Outputs dL/dalpha[l, j] (the opacity cotangent G),
+//                        and per-layer sums through the Planck source function and alpha_ref.
+//   line_adj_kernel      (line, window chunk) items, one thread per layer, a sequential walk
+//                        over the chunk's wavelengths: sums of G * dphi/d(amplitude, sigma,
+//                        gamma) with dH/da, dH/dv of every Hjerting branch from forward-mode
+//                        dual numbers (the derivative of the approximation itself, as
+//                        ForwardDiff differentiates line_absorption.jl:286-310).
+//   line_adj_prologue    one warp per line, lanes over layers: the chain rule of
+//                        line_absorption.jl:86-106 from (amplitude, sigma, gamma) to the layer
+//                        inputs and log gf, in FP64.
+//
+// The windows [lb, ub] are integer functions of the inputs and carry no derivative, as in the
+// reference under ForwardDiff.  alpha itself is recomputed by the forward kernels before the
+// reverse pass; nothing of the forward synthesis is stored between the two.
+#pragma once
+#include "lines.cuh"
+#include "physics.cuh"
+#include "rt.cuh"
+
+namespace korg {
+
+// ---------------------------------------------------------------- dual numbers in (a, v)
+template <class R>
+struct Dual {
+    R x, da, dv;
+};
+template <class R>
+__device__ __forceinline__ Dual<R> operator+(Dual<R> p, Dual<R> q) { return {p.x + q.x, p.da + q.da, p.dv + q.dv}; }
+template <class R>
+__device__ __forceinline__ Dual<R> operator-(Dual<R> p, Dual<R> q) { return {p.x - q.x, p.da - q.da, p.dv - q.dv}; }
+template <class R>
+__device__ __forceinline__ Dual<R> operator*(Dual<R> p, Dual<R> q) {
+    return {p.x * q.x, p.da * q.x + p.x * q.da, p.dv * q.x + p.x * q.dv};
+}
+template <class R>
+__device__ __forceinline__ Dual<R> operator/(Dual<R> p, Dual<R> q) {
+    const R inv = R(1) / q.x, r = p.x * inv;
+    return {r, (p.da - r * q.da) * inv, (p.dv - r * q.dv) * inv};
+}
+template <class R>
+__device__ __forceinline__ Dual<R> operator+(Dual<R> p, R c) { return {p.x + c, p.da, p.dv}; }
+template <class R>
+__device__ __forceinline__ Dual<R> operator+(R c, Dual<R> p) { return {p.x + c, p.da, p.dv}; }
+template <class R>
+__device__ __forceinline__ Dual<R> operator-(R c, Dual<R> p) { return {c - p.x, -p.da, -p.dv}; }
+template <class R>
+__device__ __forceinline__ Dual<R> operator-(Dual<R> p, R c) { return {p.x - c, p.da, p.dv}; }
+template <class R>
+__device__ __forceinline__ Dual<R> operator*(R c, Dual<R> p) { return {c * p.x, c * p.da, c * p.dv}; }
+template <class R>
+__device__ __forceinline__ Dual<R> operator*(Dual<R> p, R c) { return {c * p.x, c * p.da, c * p.dv}; }
+template <class R>
+__device__ __forceinline__ Dual<R> operator/(R c, Dual<R> q) {
+    const R r = c / q.x;
+    return {r, -r / q.x * q.da, -r / q.x * q.dv};
+}
+__device__ __forceinline__ double dexp(double x) { return exp(x); }
+__device__ __forceinline__ float dexp(float x) { return __expf(x); }
+template <class R>
+__device__ __forceinline__ Dual<R> dual_exp(Dual<R> p) {
+    const R e = dexp(p.x);
+    return {e, e * p.da, e * p.dv};
+}
+
+// harris_series (line_absorption.jl:251-265) on duals
+template <class R>
+__device__ __forceinline__ void harris_dual(Dual<R> v, Dual<R>& H0, Dual<R>& H1, Dual<R>& H2) {
+    const Dual<R> v2 = v * v;
+    H0 = dual_exp(R(0) - v2);
+    if (v.x < R(1.3))
+        H1 = R(-1.12470432) + (R(-0.15516677) + (R(3.288675912) + (R(-2.34357915) + R(0.42139162) * v) * v) * v) * v;
+    else if (v.x < R(2.4))
+        H1 = R(-4.48480194) + (R(9.39456063) + (R(-6.61487486) + (R(1.98919585) - R(0.22041650) * v) * v) * v) * v;
+    else
+        H1 = (R(0.554153432) + (R(0.278711796) + (R(-0.1883256872) + (R(0.042991293) - R(0.003278278) * v) * v) * v) * v) /
+             (v2 - R(1.5));
+    H2 = (R(1) - R(2) * v2) * H0;
+}
+
+// voigt_hjerting (line_absorption.jl:286-310) with its partial derivatives: returns
+// {H, dH/da, dH/dv} of the branch the value (a, v) selects.
+template <class R>
+__device__ __forceinline__ Dual<R> voigt_dual(R a_, R v_) {
+    const Dual<R> a{a_, R(1), R(0)}, v{v_, R(0), R(1)};
+    const Dual<R> v2 = v * v;
+    const R SQPI = R(1.7724538509055159);
+    if (a_ <= R(0.2) && v_ >= R(5)) {
+        const Dual<R> iv2 = R(1) / v2;
+        return (a * (R(1) / SQPI) * iv2) * (R(1) + R(1.5) * iv2 + R(3.75) * (iv2 * iv2));
+    }
+    Dual<R> H0, H1, H2;
+    if (a_ <= R(0.2)) {
+        harris_dual(v, H0, H1, H2);
+        return H0 + (H1 + H2 * a) * a;
+    }
+    if (a_ <= R(1.4) && a_ + v_ < R(3.2)) {
+        harris_dual(v, H0, H1, H2);
+        const R c2 = R(2) / SQPI, c23 = R(2) / (R(3) * SQPI);
+        const Dual<R> M0 = H0;
+        const Dual<R> M1 = H1 + c2 * M0;
+        const Dual<R> M2 = H2 - M0 + c2 * M1;
+        const Dual<R> M3 = c23 * (R(1) - H2) - (R(2) / R(3)) * v2 * M1 + c2 * M2;
+        const Dual<R> M4 = (R(2) / R(3)) * v2 * v2 * M0 - c23 * M1 + c2 * M3;
+        const Dual<R> psi = R(0.979895023) + (R(-0.962846325) + (R(0.532770573) - R(0.122727278) * a) * a) * a;
+        return psi * (M0 + (M1 + (M2 + (M3 + M4 * a) * a) * a) * a);
+    }
+    const Dual<R> r2 = v2 / (a * a);
+    const Dual<R> au = (R(1) / R(1.4142135623730951)) / ((r2 + R(1)) * a);
+    const Dual<R> au2 = au * au;
+    return R(0.7978845608028654) * au * (R(1) + (R(3) * r2 - R(1) + ((r2 - R(2)) * R(15) * r2 + R(2)) * au2) * au2);
+}
+
+// ---------------------------------------------------------------- transfer adjoint
+struct RtAdjArgs {
+    const double* alpha;      // [nwl][L] full opacity
+    const double* T;          // [L]
+    const double* wls;        // [nwl]
+    int64_t nwl;
+    int32_t L;
+    const double* tau_ref;    // [L]
+    const double* alpha_ref;  // [L]
+    const MathTables* math;
+    CntmDev cn;               // continuum interpolant (continuum-only pass and d/d knots)
+    const double* dflux;      // [nwl] or null
+    const double* dcntm;      // [nwl] or null
+    double unit;              // flux = 2 pi I unit
+    void* G;                  // out [nwl][L]: dL/dalpha (float when g32)
+    int32_t g32;
+    double* dT;               // out [L] (+=): through the source function
+    double* daref;            // out [L] (+=): through alpha_ref
+    double* dvals;            // out [L][nk] (+=) or null: continuum knots
+};
+
+constexpr int RTA_WARPS = 4;
+constexpr int RTA_LMAX = 128;
+constexpr int RTA_ARRAYS = 14;  // per-warp column arrays of the kernel's dynamic shared memory
+
+// Per-warp scratch of one column (each array L + 1 doubles of dynamic shared memory).
+struct RtaCol {
+    double *S, *tau, *e2, *d2, *ex, *ib, *ta, *tb, *sa, *sb, *Sbar, *col, *g, *gc;
+};
+
+// Taylor coefficients of the piecewise E2 (RadiativeTransfer.jl:441-490) around x0 = 2..8
+__device__ __constant__ double c_e2poly[7][6] = {
+    {0.037534261820486914, -0.04890051070806112, 0.033833820809153176, -0.016916910404576574,
+     0.007048712668573576, -0.0026785108140579598},
+    {0.010641925085272673, -0.013048381094197039, 0.008297844727977323, -0.003687930990212144,
+     0.0013061422257001345, -0.0003995258572729822},
+    {0.0031982292493385146, -0.0037793524098489054, 0.0022894548610917728, -0.0009539395254549051,
+     0.00031003034577284415, -8.466213288412284e-5},
+    {0.000996469042708825, -0.0011482955912753257, 0.0006737946999085467, -0.00026951787996341863,
+     8.310134632205409e-5, -2.1202073223788938e-5},
+    {0.0003182574636904001, -0.0003600824521626587, 0.00020656268138886323, -8.032993165122457e-5,
+     2.390771775334065e-5, -5.8334831318151185e-6},
+    {0.00010350984428214624, -0.00011548173161033826, 6.513442611103688e-5, -2.4813114708966427e-5,
+     7.200234178941151e-6, -1.7027366981408086e-6},
+    {3.413764515111217e-5, -3.76656228439249e-5, 2.096641424390699e-5, -7.862405341465122e-6,
+     2.2386015208338193e-6, -5.173353514609864e-7}};
+
+// d/dx of that piecewise approximation of E2, branch by branch (the derivative ForwardDiff
+// takes), given e2 = E2(x) and ex = exp(-x) of the same branch.
+__device__ __forceinline__ double expint2_deriv(double x, double e2, double ex, const MathTables& t) {
+    if (x < 1.1) {  // E2 = 1 + x (ln x + EM - 1) + x Q(x)
+        const double EM = 0.57721566490153286060651209008240243104215933593992;
+        const double c2 = 0.08333333333333333, c3 = -0.013888888888888888, c4 = 0.0020833333333333333;
+        const double Q = (-0.5 + (c2 + (c3 + c4 * x) * x) * x) * x;
+        const double dQ = -0.5 + (2 * c2 + (3 * c3 + 4 * c4 * x) * x) * x;
+        return flog64(x, t) + EM + Q + x * dQ;
+    }
+    if (x < 9) {
+        const int k = x < 2.5 ? 0 : (x < 3.5 ? 1 : (x < 4.5 ? 2 : (x < 5.5 ? 3 : (x < 6.5 ? 4 : (x < 7.5 ? 5 : 6)))));
+        const double y = x - (2 + k);
+        const double* a = c_e2poly[k];
+        return a[1] + y * (2 * a[2] + y * (3 * a[3] + y * (4 * a[4] + y * 5 * a[5])));
+    }
+    // E2 = e^-x u R(u), u = 1/x
+    const double u = 1 / x;
+    const double R = 1 + (-2 + (6 + (-24 + 120 * u) * u) * u) * u;
+    const double dR = -2 + (12 + (-72 + 480 * u) * u) * u;
+    return -e2 - ex * u * u * (R + u * dR);
+}
+
+// One transfer pass over the column `al` (global or shared) with cotangent w of 2 pi I unit:
+// writes dL/dalpha of the pass into gout[l], adds dL/dS into c.Sbar and dL/dalpha_ref into
+// s_daref (shared, atomically).
+__device__ __forceinline__ void rt_adj_pass(const RtaCol& c, const double* al, double w, const double* s_fac,
+                                            const double* s_dlt, const double* s_aref, int L, const MathTables& mt,
+                                            double* gout, double* s_daref, int lane) {
+    // optical depth (RadiativeTransfer.jl:244-253): ib, trapezoid increments, warp scans
+    for (int l = lane; l < L; l += 32) c.ib[l] = al[l] * s_fac[l];
+    __syncwarp();
+    double carry = 0.0;
+    for (int base = 0; base < L; base += 32) {
+        const int l = base + lane;
+        double inc = (l >= 1 && l < L) ? 0.5 * (c.ib[l] + c.ib[l - 1]) * s_dlt[l] : 0.0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        if (l < L) c.tau[l] = carry + inc;
+        carry += __shfl_sync(0xffffffffu, inc, 31);
+    }
+    __syncwarp();
+    // the forward recursion stops after the first layer whose tau exceeds TAU_STOP
+    int lc = L - 1;
+    for (int base = 0; base < L; base += 32) {
+        const int l = base + lane;
+        const unsigned m = __ballot_sync(0xffffffffu, l >= 1 && l < L && c.tau[l] > TAU_STOP);
+        if (m) { lc = min(lc, base + __ffs(m) - 1); break; }
+    }
+    for (int l = lane; l <= L; l += 32) {
+        if (l < L) {
+            const double t = c.tau[l];
+            const double ex = l == 0 ? 1.0 : fexp64(-t, mt);
+            const double e2 = l == 0 ? 1.0 : expint2_ex(t, ex, mt);
+            c.ex[l] = ex;
+            c.e2[l] = e2;
+            c.d2[l] = l == 0 ? 0.0 : expint2_deriv(t, e2, ex, mt);  // tau_0 = 0 is not a variable
+            c.tb[l] = 0.0;
+            c.sb[l] = 0.0;
+        }
+        c.ta[l] = 0.0;
+        c.sa[l] = 0.0;
+    }
+    __syncwarp();
+    // segment l joins layers l-1 and l (RadiativeTransfer.jl:379-388); the partial derivatives
+    // of C(tau_b) - C(tau_a), C(tau) = (tau E2 (3b + 2m tau) - e^-tau (3b + 2m (tau + 1))) / 6,
+    // m = (S_b - S_a)/(tau_b - tau_a), b = S_a - m tau_a, differentiating the E2 approximation
+    // itself (for the exact E2, dC/dtau would be (m tau + b) E2).
+    auto dC = [&](double t, double e2, double d2, double ex, double m, double bb) {
+        return (1.0 / 6.0) * ((e2 + t * d2) * (3 * bb + 2 * m * t) + 2 * m * t * e2 +
+                              ex * (3 * bb + 2 * m * (t + 1)) - 2 * m * ex);
+    };
+    for (int l = 1 + lane; l <= lc; l += 32) {
+        const double ta_ = c.tau[l - 1], tb_ = c.tau[l];
+        const double Sa = c.S[l - 1], Sb = c.S[l];
+        const double D = tb_ - ta_;
+        const double m = (Sb - Sa) / D;
+        const double bb = Sa - m * ta_;
+        const double Pb = 0.5 * ((tb_ * c.e2[l] - c.ex[l]) - (ta_ * c.e2[l - 1] - c.ex[l - 1]));
+        const double Pm = (1.0 / 3.0) * ((tb_ * tb_ * c.e2[l] - c.ex[l] * (tb_ + 1)) -
+                                         (ta_ * ta_ * c.e2[l - 1] - c.ex[l - 1] * (ta_ + 1)));
+        const double Q = Pm - ta_ * Pb;  // total derivative through m (b depends on m)
+        const double Ctb = dC(tb_, c.e2[l], c.d2[l], c.ex[l], m, bb);
+        const double Cta = l == 1 ? 0.0 : dC(ta_, c.e2[l - 1], c.d2[l - 1], c.ex[l - 1], m, bb);
+        c.tb[l] = w * (Ctb - Q * m / D);
+        c.ta[l - 1] = w * (-Cta - Pb * m + Q * m / D);
+        c.sb[l] = w * (Q / D);
+        c.sa[l - 1] = w * (Pb - Q / D);
+    }
+    __syncwarp();
+    // tau_bar[l] = sum over k >= l of the direct cotangents (tau_k = tau_{k-1} + increment):
+    // a reverse warp scan; tau[] is free now and receives tau_bar
+    double carry2 = 0.0;
+    for (int top = ((L - 1) / 32) * 32; top >= 0; top -= 32) {
+        const int l = top + (31 - lane);  // lane 0 holds the deepest layer of the chunk
+        double d = (l >= 1 && l < L) ? c.tb[l] + c.ta[l] : 0.0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double y = __shfl_up_sync(0xffffffffu, d, o);
+            if (lane >= o) d += y;
+        }
+        if (l < L) c.tau[l] = carry2 + d;
+        carry2 += __shfl_sync(0xffffffffu, d, 31);
+    }
+    __syncwarp();
+    for (int l = lane; l < L; l += 32) {
+        // ib_l enters the increments of tau_l and tau_{l+1} (RadiativeTransfer.jl:250-251)
+        double ibar = 0.0;
+        if (l >= 1) ibar += 0.5 * s_dlt[l] * c.tau[l];
+        if (l + 1 < L) ibar += 0.5 * s_dlt[l + 1] * c.tau[l + 1];
+        gout[l] = ibar * s_fac[l];
+        if (ibar != 0.0) atomicAdd(s_daref + l, -ibar * c.ib[l] / s_aref[l]);  // fac = tau_ref/alpha_ref
+        c.Sbar[l] += c.sb[l] + c.sa[l];
+    }
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(32 * RTA_WARPS) rt_adjoint_kernel(RtAdjArgs a) {
+    __shared__ MathTables s_math;
+    __shared__ double s_fac[RTA_LMAX], s_dlt[RTA_LMAX], s_aref[RTA_LMAX], s_T[RTA_LMAX];
+    __shared__ double s_dT[RTA_LMAX], s_dar[RTA_LMAX];
+    extern __shared__ double s_cols[];  // [warps][RTA_ARRAYS][L + 1]
+    load_math_tables(s_math, a.math);
+    const int L = a.L;
+    for (int l = threadIdx.x; l < L; l += blockDim.x) {
+        s_fac[l] = a.tau_ref[l] / a.alpha_ref[l];
+        s_dlt[l] = l == 0 ? 0.0 : log(a.tau_ref[l]) - log(a.tau_ref[l - 1]);
+        s_aref[l] = a.alpha_ref[l];
+        s_T[l] = a.T[l];
+        s_dT[l] = 0.0;
+        s_dar[l] = 0.0;
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double* base = s_cols + size_t(warp) * RTA_ARRAYS * (L + 1);
+    RtaCol c;
+    double** f[RTA_ARRAYS] = {&c.S, &c.tau, &c.e2, &c.d2, &c.ex, &c.ib, &c.ta, &c.tb, &c.sa, &c.sb, &c.Sbar, &c.col,
+                              &c.g, &c.gc};
+    for (int k = 0; k < RTA_ARRAYS; k++) *f[k] = base + k * (L + 1);
+    const bool two = a.cn.nk > 0;
+    const int64_t stride = int64_t(gridDim.x) * RTA_WARPS;
+    for (int64_t j = int64_t(blockIdx.x) * RTA_WARPS + warp; j < a.nwl; j += stride) {
+        const double wl = a.wls[j];
+        const double wf = a.dflux ? a.dflux[j] * 2 * PI * a.unit : 0.0;
+        const double wc = (two && a.dcntm) ? a.dcntm[j] * 2 * PI * a.unit : 0.0;
+        const double pre = 2 * HPLANCK_CGS * (C_CGS * C_CGS) / (wl * wl * wl * wl * wl);
+        const double hcw = HPLANCK_CGS * C_CGS / wl;
+        for (int l = lane; l < L; l += 32) {
+            c.S[l] = planck(pre, hcw, s_T[l]);
+            c.Sbar[l] = 0.0;
+        }
+        __syncwarp();
+        rt_adj_pass(c, a.alpha + j * L, wf, s_fac, s_dlt, s_aref, L, s_math, c.g, s_dar, lane);
+        if (two) {
+            // continuum-only column (src/synthesize.jl:287-291), as the forward interpolates it
+            const KnotPos kp = knot_pos(a.cn.knots, a.cn.nk, wl);
+            for (int l = lane; l < L; l += 32) c.col[l] = knot_eval(a.cn.vals + int64_t(l) * a.cn.nk, a.cn.nk, kp);
+            __syncwarp();
+            rt_adj_pass(c, c.col, wc, s_fac, s_dlt, s_aref, L, s_math, c.gc, s_dar, lane);
+            // the knots feed both passes' opacity (alpha = continuum + hydrogen + lines)
+            if (a.dvals) {
+                for (int l = lane; l < L; l += 32) {
+                    const double gsum = c.g[l] + c.gc[l];
+                    if (gsum == 0.0) continue;
+                    double* row = a.dvals + int64_t(l) * a.cn.nk;
+                    if (a.cn.nk == 1) {
+                        atomicAdd(row, gsum);
+                    } else {
+                        atomicAdd(row + kp.i, gsum * (1.0 - kp.t));
+                        atomicAdd(row + kp.i + 1, gsum * kp.t);
+                    }
+                }
+            }
+        }
+        // Planck source function (src/synthesize.jl:412-418): dB/dT = B x/T (1 + B/pre)
+        for (int l = lane; l < L; l += 32) {
+            const double B = c.S[l];
+            const double x = hcw / KBOLTZ_CGS / s_T[l];
+            const double d = c.Sbar[l] * B * (x / s_T[l]) * (1.0 + B / pre);
+            if (d != 0.0) atomicAdd(s_dT + l, d);
+            if (a.g32)
+                static_cast<float*>(a.G)[j * L + l] = float(c.g[l]);
+            else
+                static_cast<double*>(a.G)[j * L + l] = c.g[l];
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    for (int l = threadIdx.x; l < L; l += blockDim.x) {
+        if (s_dT[l] != 0.0) atomicAdd(a.dT + l, s_dT[l]);
+        if (s_dar[l] != 0.0) atomicAdd(a.daref + l, s_dar[l]);
+    }
+}
+
+// ---------------------------------------------------------------- line adjoint
+struct LineAdjArgs {
+    const void* G;            // [nwl][L] opacity cotangent (float when g32)
+    int32_t g32;
+    const double* wls;
+    int64_t nwl;
+    int32_t L, Lp;
+    const double* wl;         // line centres
+    const void* params;       // forward constants [n][Lp]: float4 {2 sigma^2, a, w, scale} or P64
+    const int32_t *lb, *ub;
+    const int32_t *tier_idx, *tier_start;  // lines with non-empty windows, by width tier
+    double* dpar;             // out [n][Lp][3] (+=): window sums of G H, G (a H_a + v H_v), G H_a
+    unsigned long long* next; // item counter (zero before the launch)
+};
+
+constexpr int ADJ_CHUNK = 4096;  // wavelengths per item
+
+// Items: tier 3 lines x ceil(nwl / CHUNK) chunks first, then tier 2 x 33, tier 1 x 3, tier 0 x 1
+// (window half-widths of at most 65536, 4096 and 256 points bound the chunks per line).
+__device__ __forceinline__ int64_t adj_chunks(int tier, int64_t nwl) {
+    return tier == 3 ? (nwl + ADJ_CHUNK - 1) / ADJ_CHUNK : (tier == 2 ? 33 : (tier == 1 ? 3 : 1));
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(128) line_adj_kernel(LineAdjArgs a) {
+    using R = typename std::conditional<MIXED, float, double>::type;
+    __shared__ long long s_item;
+    __shared__ int64_t s_cnt[NTIER + 1];
+    __shared__ R s_x[ADJ_CHUNK];  // |wl_j - wl0| of the item's wavelengths
+    const int L = a.L, Lp = a.Lp;
+    const int l = threadIdx.x;  // one layer per thread (blockDim.x >= L)
+    if (threadIdx.x == 0) {
+        int64_t acc = 0;
+        for (int t = NTIER - 1; t >= 0; t--) {
+            s_cnt[NTIER - 1 - t] = acc;
+            acc += int64_t(a.tier_start[t + 1] - a.tier_start[t]) * adj_chunks(t, a.nwl);
+        }
+        s_cnt[NTIER] = acc;
+    }
+    __syncthreads();
+    const int64_t total = s_cnt[NTIER];
+    for (;;) {
+        if (threadIdx.x == 0) s_item = (long long)atomicAdd(a.next, 1ull);
+        __syncthreads();
+        const int64_t it = s_item;
+        if (it >= total) break;
+        int q = 0;
+        while (it >= s_cnt[q + 1]) q++;
+        const int tier = NTIER - 1 - q;
+        const int64_t nch = adj_chunks(tier, a.nwl);
+        const int64_t rel = it - s_cnt[q];
+        const int64_t i = a.tier_idx[a.tier_start[tier] + rel / nch];
+        const int64_t j0 = int64_t(a.lb[i]) + (rel % nch) * ADJ_CHUNK;
+        const int64_t j1 = min(int64_t(a.ub[i]), j0 + ADJ_CHUNK - 1);
+        const double wl0 = a.wl[i];
+        for (int64_t j = j0 + threadIdx.x; j <= j1; j += blockDim.x) s_x[j - j0] = R(fabs(a.wls[j] - wl0));
+        __syncthreads();  // s_x filled; s_item read by everyone
+        if (j0 <= j1 && l < L) {
+            R s, av;  // 1/(sigma sqrt 2) and a of this (line, layer)
+            if (MIXED) {
+                const float4 p = reinterpret_cast<const float4*>(a.params)[i * Lp + l];
+                s = R(rsqrtf(p.x));
+                av = R(p.y);
+            } else {
+                const P64 p = reinterpret_cast<const P64*>(a.params)[i * Lp + l];
+                s = R(p.inv_s);
+                av = R(p.a);
+            }
+            // sums over the chunk of G * {H, a H_a + v H_v, H_a}
+            R sH = 0, sX = 0, sA = 0, cH = 0, cX = 0, cA = 0;
+            const int64_t nj = j1 - j0 + 1;
+            for (int64_t jj = 0; jj < nj; jj++) {
+                const int64_t e = (j0 + jj) * L + l;
+                const R g = a.g32 ? R(static_cast<const float*>(a.G)[e]) : R(static_cast<const double*>(a.G)[e]);
+                const R v = s_x[jj] * s;
+                R H, X, A;
+                if (av <= R(0.2) && v >= R(5)) {
+                    // asymptotic wing: H = a/sqrt(pi) u (1 + 1.5u + 3.75u^2), u = 1/v^2
+                    const R u = R(1) / (v * v);
+                    const R k = av * R(0.5641895835477563);
+                    H = k * u * (R(1) + u * (R(1.5) + R(3.75) * u));
+                    A = R(0.5641895835477563) * u * (R(1) + u * (R(1.5) + R(3.75) * u));  // H / a
+                    X = H - R(2) * u * k * (R(1) + u * (R(3) + R(11.25) * u));
+                } else {
+                    const Dual<R> d = voigt_dual<R>(av, v);
+                    H = d.x;
+                    A = d.da;
+                    X = av * d.da + v * d.dv;
+                }
+                if (MIXED) {  // compensated sums
+                    R y = g * H - cH, t = sH + y;
+                    cH = (t - sH) - y;
+                    sH = t;
+                    y = g * X - cX;
+                    t = sX + y;
+                    cX = (t - sX) - y;
+                    sX = t;
+                    y = g * A - cA;
+                    t = sA + y;
+                    cA = (t - sA) - y;
+                    sA = t;
+                } else {
+                    sH += g * H;
+                    sX += g * X;
+                    sA += g * A;
+                }
+            }
+            double* dp = a.dpar + (i * Lp + l) * 3;
+            atomicAdd(dp + 0, double(sH));
+            atomicAdd(dp + 1, double(sX));
+            atomicAdd(dp + 2, double(sA));
+        }
+        __syncthreads();  // s_x and s_item are rewritten for the next item
+    }
+}
+
+// Chain rule of the per-(line, layer) prologue (line_absorption.jl:86-106), FP64, one warp per
+// line.  dpar holds the window sums {sum G H, sum G (a H_a + v H_v), sum G H_a}; with
+// phi = amp s / sqrt(pi) H(gamma s, |dl| s) and s = 1/(sigma sqrt 2):
+//   dL/damp = s/sqrt(pi) sum G H,  dL/ds = amp/sqrt(pi) (sum G H + sum G (a H_a + v H_v)),
+//   dL/dgamma = amp s^2/sqrt(pi) sum G H_a,  dL/dsigma = -s/sigma dL/ds.
+struct LineAdjOut {
+    double *dT, *dne, *dnv, *dxi, *dnU;  // [L], [L], [L], [L], [S][L] (+=); any may be null
+    double* dloggf;                       // [n] (written) or null
+};
+
+__global__ void __launch_bounds__(256) line_adj_prologue_kernel(LinesDev ln, LayersDev lay, const LayerConst* lc,
+                                                                const double* dpar, int32_t Lp, LineAdjOut out,
+                                                                const MathTables* math) {
+    __shared__ MathTables s_math;
+    extern __shared__ double s_acc[];  // [4][L] per-layer sums of the block, then [S][L]
+    load_math_tables(s_math, math);
+    const int L = lay.L, S = lay.S;
+    for (int e = threadIdx.x; e < (4 + S) * L; e += blockDim.x) s_acc[e] = 0.0;
+    __syncthreads();
+    const int64_t i = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    double glog = 0.0;
+    if (i < ln.n) {
+        const LineConst q = line_const(ln, i);
+        for (int l = lane; l < L; l += 32) {
+            const double* d = dpar + (i * Lp + l) * 3;
+            if (d[0] == 0.0 && d[1] == 0.0 && d[2] == 0.0) continue;  // outside every window
+            const double T = lay.T[l], xi = lay.xi[l];
+            const LayerConst c = lc[l];
+            // sigma (:86, line_absorption.jl:190)
+            const double var = KBOLTZ_CGS * T / q.m + (xi * xi) / 2;
+            const double sigma = q.wl * sqrt(var) / C_CGS;
+            const double dsig_dT = sigma * (KBOLTZ_CGS / q.m) / (2 * var);
+            const double dsig_dxi = sigma * xi / (2 * var);
+            // gamma (:90-99)
+            double dG_dT = 0.0, dG_dne = 0.0, dG_dnv = 0.0;
+            if (!q.mol) {
+                const double st = q.gstark * c.stark6;
+                double vdw, ex;
+                if (q.v2 == -1) {
+                    vdw = q.v1 * c.vdw3;
+                    ex = 0.3;
+                } else {
+                    const double invmu = 1 / (1.008 * AMU_CGS) + 1 / q.m;
+                    const double vbar = sqrt(8 * KBOLTZ_CGS * T / PI * invmu);
+                    vdw = q.abo_pre * pow(vbar / 1e6, 1 - q.v2);
+                    ex = (1 - q.v2) / 2;
+                }
+                dG_dne = st;
+                dG_dnv = vdw;
+                dG_dT = lay.ne[l] * st / (6 * T) + lay.n_eff_vdW[l] * vdw * ex / T;
+            }
+            // amplitude (:101-106)
+            const double e1 = fexp64(-c.beta * q.El, s_math), e2 = fexp64(-c.beta * q.E_upper, s_math);
+            const double levels = e1 - e2;
+            const double nU = lay.n_div_U[int64_t(q.sp) * L + l];
+            const double amp = q.strength * levels * nU;
+            const double dlev_dT = c.beta / T * (q.El * e1 - q.E_upper * e2);
+            // cotangents of (amp, sigma, gamma)
+            const double s = 1 / (sigma * SQRT_2);
+            const double g_amp = s / SQRT_PI * d[0];
+            const double g_s = amp / SQRT_PI * (d[0] + d[1]);
+            const double g_gam = amp * s * s / SQRT_PI * d[2];
+            const double g_sig = -s / sigma * g_s;
+            atomicAdd(s_acc + 0 * L + l, g_amp * q.strength * nU * dlev_dT + g_sig * dsig_dT + g_gam * q.wl2c * dG_dT);
+            atomicAdd(s_acc + 1 * L + l, g_gam * q.wl2c * dG_dne);
+            atomicAdd(s_acc + 2 * L + l, g_gam * q.wl2c * dG_dnv);
+            atomicAdd(s_acc + 3 * L + l, g_sig * dsig_dxi);
+            atomicAdd(s_acc + (4 + q.sp) * L + l, g_amp * q.strength * levels);
+            glog += g_amp * amp * 2.302585092994046;  // d amp / d log gf = amp ln 10
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) glog += __shfl_xor_sync(0xffffffffu, glog, o);
+        if (lane == 0 && out.dloggf) out.dloggf[i] = glog;
+    }
+    __syncthreads();
+    double* dst[4] = {out.dT, out.dne, out.dnv, out.dxi};
+    for (int e = threadIdx.x; e < (4 + S) * L; e += blockDim.x) {
+        const double v = s_acc[e];
+        if (v == 0.0) continue;
+        const int r = e / L, l = e - r * L;
+        double* p = r < 4 ? dst[r] : out.dnU;
+        if (p) atomicAdd(p + (r < 4 ? l : int64_t(r - 4) * L + l), v);
+    }
+}
+
+// Hydrogen-line opacity is layer-local (each layer's row depends on that layer's T, n_e,
+// n(H I), n(He I), U(H I), xi only), so its Jacobian is block diagonal: per layer and input,
+// d alpha_H[l, :]/dp_l is a central difference of two FP64 evaluations with every layer
+// perturbed at once, and the cotangent is its contraction with G.
+__global__ void hydro_fd_contract_kernel(const void* G, int32_t g32, const double* ap, const double* am,
+                                         const double* h, int64_t nwl, int32_t L, double* out) {
+    __shared__ double s_acc[RTA_LMAX];
+    for (int l = threadIdx.x; l < L; l += blockDim.x) s_acc[l] = 0.0;
+    __syncthreads();
+    const int64_t n = nwl * L;
+    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < n; e += int64_t(gridDim.x) * blockDim.x) {
+        const double d = ap[e] - am[e];
+        if (d == 0.0) continue;
+        const int l = int(e % L);
+        const double g = g32 ? double(static_cast<const float*>(G)[e]) : static_cast<const double*>(G)[e];
+        atomicAdd(s_acc + l, g * d);
+    }
+    __syncthreads();
+    for (int l = threadIdx.x; l < L; l += blockDim.x)
+        if (s_acc[l] != 0.0) atomicAdd(out + l, s_acc[l] / (2 * h[l]));
+}
+
+}  // namespace korg

@@ -7,12 +7,14 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <type_traits>
 #include <vector>
 
 #include "../../include/korg_gb300.h"
+#include "adjoint.cuh"
 #include "hydrogen.cuh"
 #include "lines.cuh"
 #include "physics.cuh"
@@ -29,18 +31,45 @@ struct DevBuf {
 
 constexpr int NEV = 8;
 
+// Tile shape of the line tile kernel: wavelengths per CTA and lines per shared-memory batch
+// (0: the default for the precision).
+struct TileCfg {
+    int tw, stage;
+};
+struct TuneRecord {
+    int L, mixed, tw, stage;
+    float ms;
+};
+
 }  // namespace
 
 struct korg_ctx {
     int device = 0;
-    cudaStream_t stream = nullptr;  // used by the host-pointer calls
+    int sms = 0;
+    cudaStream_t stream = nullptr;  // used by the host-pointer calls and for graph capture
     std::string err;
     // scratch arena: grown on demand, never shrunk, freed by korg_destroy
-    DevBuf lc, params, xfar, amask, lb, ub, ci, tier_idx, tier_ci, tier_meta, counters;
+    DevBuf lines_scratch, counters, tune_alpha;
     DevBuf hrec, hQ, hQ32, hulb, huub;
     DevBuf stage_dev, aref, alpha, flux, cntm, math;
+    DevBuf vjp_g, vjp_dpar, vjp_small, vjp_hfd;  // reverse mode
     void* stage_host = nullptr;
     size_t stage_host_cap = 0;
+    // batched synthesis: chunk alpha, per-spectrum line scratch, tile arguments + reference
+    // wavelengths + queue counters (device), their host staging (pinned, batch-only)
+    DevBuf b_alpha, b_lines, b_meta;
+    void* b_host = nullptr;
+    size_t b_host_cap = 0;
+    cudaEvent_t b_host_ev = nullptr;  // after the last copy out of b_host
+    int64_t batch_budget = int64_t(32) << 30;
+    // CUDA graph of the last batch: replayed while the same batch is submitted again
+    bool use_graph = false, capturing = false;
+    cudaGraphExec_t gexec = nullptr;
+    std::vector<unsigned char> gkey, pending_key;
+    // autotuned tile shapes per (layers, precision)
+    bool autotune = false;
+    std::map<std::pair<int, int>, TileCfg> tuned;
+    std::vector<TuneRecord> tune_log;
     // Stehle tables
     bool have_stark = false;
     StarkDev stark{};
@@ -79,10 +108,19 @@ int set_err(korg_ctx* c, int code, const char* fmt, ...) {
         if (r_ != KORG_OK) return r_; \
     } while (0)
 
+void drop_graph(korg_ctx* ctx) {
+    if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+    ctx->gexec = nullptr;
+    ctx->gkey.clear();
+    ctx->pending_key.clear();
+}
+
 int ensure(korg_ctx* ctx, DevBuf& b, size_t bytes) {
     if (bytes == 0) bytes = 16;
     if (b.cap >= bytes) return KORG_OK;
+    if (ctx->capturing) return set_err(ctx, KORG_EINVAL, "scratch would grow during graph capture");
     if (b.p) {
+        drop_graph(ctx);  // a captured graph holds the old address
         KCUDA(cudaStreamSynchronize(ctx->stream));
         KCUDA(cudaDeviceSynchronize());
         cudaFree(b.p);
@@ -108,7 +146,7 @@ int reset_counters(korg_ctx* ctx, cudaStream_t s) {
 }
 
 void record(korg_ctx* ctx, int i, cudaStream_t s) {
-    if (ctx->timing) cudaEventRecord(ctx->ev[i], s);
+    if (ctx->timing && !ctx->capturing) cudaEventRecord(ctx->ev[i], s);
 }
 
 // Layers per thread (K) and layer groups per CTA (G = ceil(L/K) <= 8); layers are padded to
@@ -142,37 +180,195 @@ LayersDev layers_dev(const korg_layers* y) {
 }
 
 // ------------------------------------------------------------------ line opacity
-constexpr int TILE_TW = 64;  // wavelengths per CTA of the line tile kernel
+constexpr int TILE_TW = 64;  // default wavelengths per CTA of the line tile kernel
+
+// Pieces of the per-spectrum scratch of the line prologue and candidate lists.
+struct LineScratch {
+    LayerConst* lc = nullptr;
+    void* params = nullptr;
+    float* xfar = nullptr;
+    uint32_t* amask = nullptr;
+    int32_t *lb = nullptr, *ub = nullptr, *ci = nullptr, *tier_idx = nullptr, *tier_ci = nullptr, *tier_meta = nullptr;
+};
+
+size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
+int part_blocks(int64_t n) { return int((n + PART_CHUNK - 1) / PART_CHUNK); }
+
+// Bytes of one LineScratch for n lines (every piece 256-byte aligned); with base != null, the
+// pieces are carved out of base.
+size_t line_scratch(unsigned char* base, int64_t n, int L, int Lp, int G, bool mixed, LineScratch* out) {
+    const size_t nn = size_t(std::max<int64_t>(n, 1));
+    const size_t sz[10] = {sizeof(LayerConst) * L, (mixed ? sizeof(float4) : sizeof(P64)) * nn * Lp,
+                           sizeof(float) * nn * G, sizeof(uint32_t) * nn, 4 * nn, 4 * nn, 4 * nn, 4 * nn, 4 * nn,
+                           sizeof(int32_t) * (NTIER * size_t(part_blocks(n)) + NTIER + 2)};
+    size_t off[10], tot = 0;
+    for (int i = 0; i < 10; i++) { off[i] = tot; tot += a256(sz[i]); }
+    if (base && out) {
+        out->lc = reinterpret_cast<LayerConst*>(base + off[0]);
+        out->params = base + off[1];
+        out->xfar = reinterpret_cast<float*>(base + off[2]);
+        out->amask = reinterpret_cast<uint32_t*>(base + off[3]);
+        out->lb = reinterpret_cast<int32_t*>(base + off[4]);
+        out->ub = reinterpret_cast<int32_t*>(base + off[5]);
+        out->ci = reinterpret_cast<int32_t*>(base + off[6]);
+        out->tier_idx = reinterpret_cast<int32_t*>(base + off[7]);
+        out->tier_ci = reinterpret_cast<int32_t*>(base + off[8]);
+        out->tier_meta = reinterpret_cast<int32_t*>(base + off[9]);
+    }
+    return tot;
+}
+
+// Tile-kernel arguments that follow from the scratch and the inputs (launch geometry aside).
+TileArgs make_tile_args(const LineScratch& sc, double* alpha, const double* wls, int64_t nwl, const LinesDev& ln,
+                        int L, int Lp, int G) {
+    TileArgs ta{};
+    ta.alpha = alpha;
+    ta.wls = wls;
+    ta.nwl = nwl;
+    ta.L = L;
+    ta.Lp = Lp;
+    ta.G = G;
+    ta.xfar = sc.xfar;
+    ta.amask = sc.amask;
+    ta.n = ln.n;
+    ta.wl = ln.wl;
+    ta.params = sc.params;
+    ta.lb = sc.lb;
+    ta.ub = sc.ub;
+    ta.tier_idx = sc.tier_idx;
+    ta.tier_ci = sc.tier_ci;
+    ta.tier_start = sc.tier_meta;                 // [start: NTIER+1][unsorted][block counts]
+    ta.unsorted = sc.tier_meta + NTIER + 1;
+    return ta;
+}
+
+// Per-line prologue (constants, windows, classes) and the width-tier candidate lists.
+int prep_lines(korg_ctx* ctx, const LineScratch& sc, const double* wls, int64_t nwl, const LinesDev& ln,
+               const LayersDev& lay, const CntmDev& cn, double cutoff, bool mixed, int kmax, int G,
+               cudaStream_t s) {
+    const int L = lay.L, Lp = G * kmax;
+    auto* ctr = static_cast<unsigned long long*>(ctx->counters.p);
+    layer_const_kernel<<<(L + 127) / 128, 128, 0, s>>>(lay, sc.lc);
+    PrepOut po{sc.params, sc.lb, sc.ub, sc.ci, sc.xfar, sc.amask, Lp, kmax, G, ctr, ctr + 1};
+    const size_t prep_smem = size_t(256 / 32) * Lp * (sizeof(float) + sizeof(int));
+    const unsigned pblocks = unsigned((ln.n * 32 + 255) / 256);
+    auto* math = static_cast<MathTables*>(ctx->math.p);
+    if (mixed)
+        line_prep_mixed_kernel<<<prep_mixed_blocks(ln.n), 32 * PREP_WARPS, prep_mixed_smem(Lp), s>>>(
+            ln, lay, sc.lc, cn, wls, nwl, cutoff, po, math);
+    else
+        line_prep64_kernel<<<pblocks, 256, prep_smem, s>>>(ln, lay, sc.lc, cn, wls, nwl, cutoff, po, math);
+    KCUDA(cudaGetLastError());
+    const int nblk = part_blocks(ln.n);
+    TierLists tl{sc.tier_idx, sc.tier_ci, sc.tier_meta, sc.tier_meta + NTIER + 1};
+    int32_t* bcnt = sc.tier_meta + NTIER + 2;
+    KCUDA(cudaMemsetAsync(tl.unsorted, 0, sizeof(int32_t), s));
+    tier_count_kernel<<<nblk, PART_THREADS, 0, s>>>(sc.lb, sc.ub, sc.ci, ln.n, bcnt, tl.unsorted);
+    tier_scatter_kernel<<<nblk, PART_THREADS, 0, s>>>(sc.lb, sc.ub, sc.ci, ln.n, bcnt, nblk, tl);
+    KCUDA(cudaGetLastError());
+    return KORG_OK;
+}
+
+// Launch shape of the tile kernel: TW wavelengths x G layer groups per CTA, `stage` lines per
+// shared-memory batch.
+struct TileGeom {
+    int tw, threads, stage, region;
+    size_t smem;
+};
+
+bool tile_geom(bool mixed, int Lp, int G, TileCfg c, TileGeom* g) {
+    const size_t psz = mixed ? sizeof(float4) : sizeof(P64);
+    const int B = c.stage > 0 ? c.stage : (mixed ? STAGE_LINES : STAGE_LINES / 2);
+    if (c.tw < 32 || c.tw % 32 != 0 || c.tw * G > 512 || B < 1) return false;
+    size_t region = size_t(B) * Lp * psz;
+    region = std::max(region, (size_t(c.tw) * (Lp + 1) * sizeof(double) + 1) / 2);
+    region = (region + 15) & ~size_t(15);
+    g->tw = c.tw;
+    g->threads = c.tw * G;
+    g->stage = B;
+    g->region = int(region);
+    g->smem = 2 * region + size_t(g->threads) * sizeof(LineStage);
+    return g->smem <= 227 * 1024;
+}
 
 template <bool MIXED, int KMAX, int MAXT, int MINB>
-int launch_tile(korg_ctx* ctx, TileArgs ta, int G, cudaStream_t s) {
-    using P = typename ParamT<MIXED>::type;
-    const int Lp = ta.Lp;
-    const int B = MIXED ? STAGE_LINES : STAGE_LINES / 2;
-    ta.stage = B;
-    ta.G = G;
-    const int TW = TILE_TW;
-    const int threads = TW * G;
-    size_t region = size_t(B) * Lp * sizeof(P);
-    region = std::max(region, (size_t(TW) * (Lp + 1) * sizeof(double) + 1) / 2);
-    region = (region + 15) & ~size_t(15);
-    ta.region = int(region);
-    const size_t smem = 2 * region + size_t(threads) * sizeof(LineStage);
-    auto kern = line_tile_kernel<MIXED, KMAX, MAXT, MINB>;
-    KCUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    const int64_t tiles = (ta.nwl + TW - 1) / TW;
-    kern<<<dim3(unsigned(tiles)), threads, smem, s>>>(ta);
+int launch_tile(korg_ctx* ctx, TileArgs ta, const TileGeom& g, const TileQueue* q, cudaStream_t s) {
+    ta.stage = g.stage;
+    ta.region = g.region;
+    if (q) {
+        auto kern = line_tile_queue_kernel<MIXED, KMAX, MAXT, MINB>;
+        KCUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g.smem)));
+        int per_sm = 0;
+        KCUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, g.threads, g.smem));
+        const int64_t grid = std::min<int64_t>(q->nitems, int64_t(ctx->sms) * std::max(per_sm, 1));
+        if (grid > 0) kern<<<unsigned(grid), g.threads, g.smem, s>>>(*q);
+    } else {
+        auto kern = line_tile_kernel<MIXED, KMAX, MAXT, MINB>;
+        KCUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g.smem)));
+        const int64_t tiles = (ta.nwl + g.tw - 1) / g.tw;
+        kern<<<dim3(unsigned(tiles)), g.threads, g.smem, s>>>(ta);
+    }
     KCUDA(cudaGetLastError());
     return KORG_OK;
 }
 
 template <bool MIXED>
-int dispatch_tile(korg_ctx* ctx, const TileArgs& ta, int G, int kmax, cudaStream_t s) {
-    if (kmax == 14 && G <= 4) return launch_tile<MIXED, 14, 256, MIXED ? 3 : 2>(ctx, ta, G, s);
-    if (kmax == 14) return launch_tile<MIXED, 14, 512, 1>(ctx, ta, G, s);
-    if (kmax == 16) return launch_tile<MIXED, 16, 512, 1>(ctx, ta, G, s);
-    return launch_tile<MIXED, 32, 512, 1>(ctx, ta, G, s);
+int dispatch_tile(korg_ctx* ctx, const TileArgs& ta, int kmax, const TileGeom& g, const TileQueue* q,
+                  cudaStream_t s) {
+    if (kmax == 14 && g.threads <= 256) return launch_tile<MIXED, 14, 256, MIXED ? 3 : 2>(ctx, ta, g, q, s);
+    if (kmax == 14) return launch_tile<MIXED, 14, 512, 1>(ctx, ta, g, q, s);
+    if (kmax == 16) return launch_tile<MIXED, 16, 512, 1>(ctx, ta, g, q, s);
+    return launch_tile<MIXED, 32, 512, 1>(ctx, ta, g, q, s);
 }
+
+int run_tiles(korg_ctx* ctx, const TileArgs& ta, int kmax, const TileGeom& g, const TileQueue* q, bool mixed,
+              cudaStream_t s) {
+    return mixed ? dispatch_tile<true>(ctx, ta, kmax, g, q, s) : dispatch_tile<false>(ctx, ta, kmax, g, q, s);
+}
+
+// The tile shape for (L, precision): the autotuned one when there is one, else the default.
+TileCfg tile_cfg(const korg_ctx* ctx, int L, bool mixed) {
+    auto it = ctx->tuned.find(std::make_pair(L, int(mixed)));
+    return it != ctx->tuned.end() ? it->second : TileCfg{TILE_TW, 0};
+}
+
+// Autotuner: times every candidate shape (TW in {32, 64, 128} x stage in {B/2, B}) on the real
+// candidate lists of one spectrum, writing into a scratch alpha, and keeps the fastest for
+// (L, precision).  Runs once per (L, precision) per context, outside any stream capture.
+int autotune_tiles(korg_ctx* ctx, const TileArgs& ta0, int kmax, bool mixed, cudaStream_t s) {
+    const int L = ta0.L, Lp = ta0.Lp, G = ta0.G;
+    const auto key = std::make_pair(L, int(mixed));
+    if (ctx->tuned.count(key)) return KORG_OK;
+    KCHECK(ensure(ctx, ctx->tune_alpha, sizeof(double) * size_t(L) * ta0.nwl));
+    KCUDA(cudaMemsetAsync(ctx->tune_alpha.p, 0, sizeof(double) * size_t(L) * ta0.nwl, s));
+    TileArgs ta = ta0;
+    ta.alpha = static_cast<double*>(ctx->tune_alpha.p);
+    const int B0 = mixed ? STAGE_LINES : STAGE_LINES / 2;
+    TileCfg best{TILE_TW, 0};
+    float best_ms = 1e30f;
+    for (int tw : {64, 32, 128})
+        for (int B : {B0, B0 / 2}) {
+            TileGeom g;
+            if (!tile_geom(mixed, Lp, G, TileCfg{tw, B}, &g)) continue;
+            float t = 1e30f;
+            for (int rep = 0; rep < 3; rep++) {
+                KCUDA(cudaEventRecord(ctx->ev[6], s));
+                KCHECK(run_tiles(ctx, ta, kmax, g, nullptr, mixed, s));
+                KCUDA(cudaEventRecord(ctx->ev[7], s));
+                KCUDA(cudaEventSynchronize(ctx->ev[7]));
+                float ms = 0;
+                KCUDA(cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]));
+                if (rep > 0) t = std::min(t, ms);
+            }
+            ctx->tune_log.push_back({L, int(mixed), tw, B, t});
+            if (t < best_ms) { best_ms = t; best = TileCfg{tw, B}; }
+        }
+    ctx->tuned[key] = best;
+    return KORG_OK;
+}
+
+// Candidate lists big enough to be worth tuning on (a few thousand tiles).
+bool worth_tuning(int64_t nwl, int64_t nlines) { return nwl >= 100000 && nlines >= 10000; }
 
 int run_line_absorption(korg_ctx* ctx, double* alpha, const double* wls, int64_t nwl, const LinesDev& ln,
                         const LayersDev& lay, const CntmDev& cn, double cutoff, bool mixed,
@@ -184,64 +380,17 @@ int run_line_absorption(korg_ctx* ctx, double* alpha, const double* wls, int64_t
     if (G < 0) return set_err(ctx, KORG_EINVAL, "at most 256 layers are supported (got %d)", L);
     if (ln.n > INT32_MAX || nwl > INT32_MAX - 1) return set_err(ctx, KORG_EINVAL, "sizes exceed int32 indexing");
     const int Lp = G * kmax;
-    const size_t psz = mixed ? sizeof(float4) : sizeof(P64);
-    KCHECK(ensure(ctx, ctx->lc, sizeof(LayerConst) * L));
-    KCHECK(ensure(ctx, ctx->params, psz * size_t(ln.n) * Lp));
-    KCHECK(ensure(ctx, ctx->xfar, sizeof(float) * size_t(ln.n) * G));
-    KCHECK(ensure(ctx, ctx->amask, sizeof(uint32_t) * ln.n));
-    KCHECK(ensure(ctx, ctx->lb, sizeof(int32_t) * ln.n));
-    KCHECK(ensure(ctx, ctx->ub, sizeof(int32_t) * ln.n));
-    KCHECK(ensure(ctx, ctx->ci, sizeof(int32_t) * ln.n));
-    KCHECK(ensure(ctx, ctx->tier_idx, sizeof(int32_t) * ln.n));
-    KCHECK(ensure(ctx, ctx->tier_ci, sizeof(int32_t) * ln.n));
-    const int nblk = int((ln.n + PART_CHUNK - 1) / PART_CHUNK);
-    KCHECK(ensure(ctx, ctx->tier_meta, sizeof(int32_t) * (NTIER * size_t(nblk) + NTIER + 2)));
-    auto* ctr = static_cast<unsigned long long*>(ctx->counters.p);
-    layer_const_kernel<<<(L + 127) / 128, 128, 0, s>>>(lay, static_cast<LayerConst*>(ctx->lc.p));
-    PrepOut po{ctx->params.p, static_cast<int32_t*>(ctx->lb.p), static_cast<int32_t*>(ctx->ub.p),
-               static_cast<int32_t*>(ctx->ci.p), static_cast<float*>(ctx->xfar.p), static_cast<uint32_t*>(ctx->amask.p), Lp, kmax, G, ctr, ctr + 1};
-    const size_t prep_smem = size_t(256 / 32) * Lp * (sizeof(float) + sizeof(int));
-    const int64_t pthreads = ln.n * 32;
-    const unsigned pblocks = unsigned((pthreads + 255) / 256);
-    if (mixed)
-        line_prep_mixed_kernel<<<pblocks, 256, prep_smem, s>>>(ln, lay, static_cast<LayerConst*>(ctx->lc.p), cn, wls, nwl, cutoff, po,
-                                                       static_cast<MathTables*>(ctx->math.p));
-    else
-        line_prep64_kernel<<<pblocks, 256, prep_smem, s>>>(ln, lay, static_cast<LayerConst*>(ctx->lc.p), cn, wls, nwl, cutoff, po,
-                                                   static_cast<MathTables*>(ctx->math.p));
-    KCUDA(cudaGetLastError());
-    int32_t* meta = static_cast<int32_t*>(ctx->tier_meta.p);  // [start: NTIER+1][unsorted][block counts]
-    TierLists tl{static_cast<int32_t*>(ctx->tier_idx.p), static_cast<int32_t*>(ctx->tier_ci.p), meta, meta + NTIER + 1};
-    int32_t* bcnt = meta + NTIER + 2;
-    KCUDA(cudaMemsetAsync(tl.unsorted, 0, sizeof(int32_t), s));
-    tier_count_kernel<<<nblk, PART_THREADS, 0, s>>>(po.lb, po.ub, po.ci, ln.n, bcnt, tl.unsorted);
-    tier_scatter_kernel<<<nblk, PART_THREADS, 0, s>>>(po.lb, po.ub, po.ci, ln.n, bcnt, nblk, tl);
-    KCUDA(cudaGetLastError());
+    KCHECK(ensure(ctx, ctx->lines_scratch, line_scratch(nullptr, ln.n, L, Lp, G, mixed, nullptr)));
+    LineScratch sc;
+    line_scratch(static_cast<unsigned char*>(ctx->lines_scratch.p), ln.n, L, Lp, G, mixed, &sc);
+    KCHECK(prep_lines(ctx, sc, wls, nwl, ln, lay, cn, cutoff, mixed, kmax, G, s));
     record(ctx, 2, s);
-    TileArgs ta{};
-    ta.alpha = alpha;
-    ta.wls = wls;
-    ta.nwl = nwl;
-    ta.L = L;
-    ta.Lp = Lp;
-    ta.xfar = po.xfar;
-    ta.amask = po.amask;
-    ta.n = ln.n;
-    ta.wl = ln.wl;
-    ta.params = ctx->params.p;
-    ta.lb = po.lb;
-    ta.ub = po.ub;
-    ta.tier_idx = tl.idx;
-    ta.tier_ci = tl.ci;
-    ta.tier_start = tl.start;
-    ta.unsorted = tl.unsorted;
-    int rc;
-    if (mixed)
-        rc = dispatch_tile<true>(ctx, ta, G, kmax, s);
-    else
-        rc = dispatch_tile<false>(ctx, ta, G, kmax, s);
+    const TileArgs ta = make_tile_args(sc, alpha, wls, nwl, ln, L, Lp, G);
+    if (ctx->autotune && !ctx->capturing && worth_tuning(nwl, ln.n)) KCHECK(autotune_tiles(ctx, ta, kmax, mixed, s));
+    TileGeom g;
+    if (!tile_geom(mixed, Lp, G, tile_cfg(ctx, L, mixed), &g)) return set_err(ctx, KORG_EINVAL, "bad tile shape");
     ctx->stats_pending = true;
-    return rc;
+    return run_tiles(ctx, ta, kmax, g, nullptr, mixed, s);
 }
 
 // ------------------------------------------------------------------ hydrogen lines
@@ -352,6 +501,336 @@ int run_synthesize(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& l
     return KORG_OK;
 }
 
+// ------------------------------------------------------------------ batched synthesis
+// Many spectra on one wavelength grid, each with its own atmosphere and (pruned) line list:
+// the per-spectrum prologues run first, then ONE persistent tile launch per chunk works
+// through the (spectrum, tile) queue, then the transfers.  Spectra are grouped into chunks
+// whose alpha and line scratch fit the context's batch budget.
+struct BatchPlan {
+    int L, Lp, G, kmax;
+    bool mixed;
+    TileGeom geom;
+    std::vector<int> chunk_first;        // first spectrum of each chunk, plus nspec at the end
+    std::vector<size_t> line_off;        // offset of each spectrum's line scratch in b_lines
+    size_t alpha_bytes, lines_bytes, meta_bytes, host_bytes;
+    size_t o_targs, o_refwl, o_aref, o_ctr, o_zero;  // pieces of b_meta (b_host holds the first two)
+};
+
+int plan_batch(korg_ctx* ctx, int nspec, const korg_batch_item* it, int64_t nwl, bool mixed, BatchPlan* p) {
+    const int L = it[0].in.layers.L;
+    for (int i = 0; i < nspec; i++) {
+        const korg_batch_item& b = it[i];
+        if (b.in.layers.L != L) return set_err(ctx, KORG_EINVAL, "all spectra of a batch need the same layer count");
+        if (!b.flux || !b.cntm || b.in.cntm.nk < 2 || !b.in.tau_ref || !b.in.alpha_ref_cntm || b.lines.n < 0 ||
+            b.lines5.n < 0 || b.lines.n > INT32_MAX)
+            return set_err(ctx, KORG_EINVAL, "bad batch item %d", i);
+        if (b.in.hydrogen_lines && !ctx->have_stark)
+            return set_err(ctx, KORG_ENOTABLES, "korg_set_stark_tables() has not been called");
+    }
+    p->L = L;
+    p->mixed = mixed;
+    p->G = layer_groups(L, &p->kmax);
+    if (p->G < 0) return set_err(ctx, KORG_EINVAL, "at most 256 layers are supported (got %d)", L);
+    p->Lp = p->G * p->kmax;
+    if (!tile_geom(mixed, p->Lp, p->G, tile_cfg(ctx, L, mixed), &p->geom))
+        return set_err(ctx, KORG_EINVAL, "bad tile shape");
+    const size_t per_alpha = a256(sizeof(double) * size_t(L) * nwl);
+    p->chunk_first.assign(1, 0);
+    p->line_off.assign(nspec, 0);
+    size_t cur_a = 0, cur_l = 0;
+    p->alpha_bytes = p->lines_bytes = 0;
+    for (int i = 0; i < nspec; i++) {
+        const size_t lb = line_scratch(nullptr, it[i].lines.n, L, p->Lp, p->G, mixed, nullptr);
+        if (i > p->chunk_first.back() && int64_t(cur_a + cur_l + per_alpha + lb) > ctx->batch_budget) {
+            p->chunk_first.push_back(i);
+            cur_a = cur_l = 0;
+        }
+        p->line_off[i] = cur_l;
+        cur_a += per_alpha;
+        cur_l += lb;
+        p->alpha_bytes = std::max(p->alpha_bytes, cur_a);
+        p->lines_bytes = std::max(p->lines_bytes, cur_l);
+    }
+    p->chunk_first.push_back(nspec);
+    const int nchunk = int(p->chunk_first.size()) - 1;
+    p->o_targs = 0;
+    p->o_refwl = a256(sizeof(TileArgs) * nspec);
+    p->host_bytes = p->o_refwl + a256(sizeof(double) * nspec);
+    p->o_aref = p->host_bytes;
+    p->o_ctr = p->o_aref + a256(sizeof(double) * size_t(L) * nspec);
+    p->o_zero = p->o_ctr + a256(sizeof(unsigned long long) * nchunk);
+    p->meta_bytes = p->o_zero + a256(sizeof(int32_t) * (NTIER + 2));
+    return KORG_OK;
+}
+
+// Enqueues the whole batch on stream s (also what a graph capture records).
+int enqueue_batch(korg_ctx* ctx, const BatchPlan& p, int nspec, const korg_batch_item* it, const double* wls,
+                  int64_t nwl, cudaStream_t s) {
+    const int L = p.L;
+    const bool mixed = p.mixed;
+    unsigned char* meta = static_cast<unsigned char*>(ctx->b_meta.p);
+    auto* d_targs = reinterpret_cast<TileArgs*>(meta + p.o_targs);
+    auto* d_refwl = reinterpret_cast<double*>(meta + p.o_refwl);
+    auto* d_aref = reinterpret_cast<double*>(meta + p.o_aref);
+    auto* d_ctr = reinterpret_cast<unsigned long long*>(meta + p.o_ctr);
+    const int nchunk = int(p.chunk_first.size()) - 1;
+    record(ctx, 0, s);
+    KCHECK(reset_counters(ctx, s));
+    // tile arguments and reference wavelengths, prepared on the host (pinned, batch-only buffer)
+    KCUDA(cudaMemcpyAsync(meta, ctx->b_host, p.host_bytes, cudaMemcpyHostToDevice, s));
+    // queue counters, and the empty tier table of spectra without lines
+    KCUDA(cudaMemsetAsync(d_ctr, 0, p.meta_bytes - p.o_ctr, s));
+    const int64_t ntiles = (nwl + p.geom.tw - 1) / p.geom.tw;
+    for (int c = 0; c < nchunk; c++) {
+        const int s0 = p.chunk_first[c], s1 = p.chunk_first[c + 1];
+        for (int i = s0; i < s1; i++) {
+            const korg_synth_inputs& in = it[i].in;
+            const LayersDev lay = layers_dev(&in.layers);
+            const CntmDev cn{in.cntm.nk, in.cntm.knots, in.cntm.vals};
+            double* alpha = static_cast<double*>(ctx->b_alpha.p) + size_t(i - s0) * a256(8 * size_t(L) * nwl) / 8;
+            double* aref = d_aref + size_t(i) * L;
+            // src/synthesize.jl:249-252, 265-283, 293-303 as in the single-spectrum path
+            alpha_init_kernel<<<unsigned((nwl + 63) / 64), 256, 0, s>>>(alpha, wls, nwl, L, cn);
+            KCUDA(cudaGetLastError());
+            KCUDA(cudaMemcpyAsync(aref, in.alpha_ref_cntm, sizeof(double) * L, cudaMemcpyDeviceToDevice, s));
+            const CntmDev cref{1, nullptr, in.alpha_ref_cntm};
+            KCHECK(run_line_absorption(ctx, aref, d_refwl + i, 1, lines_dev(&it[i].lines5), lay, cref,
+                                       in.cutoff_threshold, mixed, s));
+            if (in.hydrogen_lines) {
+                const HLayers hl{L, lay.T, lay.ne, in.nH_I, in.nHe_I, in.UH_I, lay.xi};
+                KCHECK(run_hydrogen(ctx, alpha, wls, nwl, hl, in.hydrogen_window, in.use_MHD, mixed, s));
+            }
+            if (it[i].lines.n > 0) {
+                LineScratch sc;
+                line_scratch(static_cast<unsigned char*>(ctx->b_lines.p) + p.line_off[i], it[i].lines.n, L, p.Lp,
+                             p.G, mixed, &sc);
+                KCHECK(prep_lines(ctx, sc, wls, nwl, lines_dev(&it[i].lines), lay, cn, in.cutoff_threshold, mixed,
+                                  p.kmax, p.G, s));
+            }
+        }
+        record(ctx, 2, s);
+        const TileQueue q{d_targs + s0, s1 - s0, int64_t(s1 - s0) * ntiles, d_ctr + c};
+        KCHECK(run_tiles(ctx, TileArgs{}, p.kmax, p.geom, &q, mixed, s));
+        record(ctx, 5, s);
+        for (int i = s0; i < s1; i++) {
+            const korg_synth_inputs& in = it[i].in;
+            const CntmDev cn{in.cntm.nk, in.cntm.knots, in.cntm.vals};
+            double* alpha = static_cast<double*>(ctx->b_alpha.p) + size_t(i - s0) * a256(8 * size_t(L) * nwl) / 8;
+            KCHECK(run_rt(ctx, alpha, nullptr, in.layers.T, wls, nwl, L, in.tau_ref, d_aref + size_t(i) * L, cn,
+                          it[i].flux, it[i].cntm, 1e-8, s));
+        }
+    }
+    record(ctx, 6, s);
+    ctx->stats_pending = true;
+    return KORG_OK;
+}
+
+// Device address of spectrum i's alpha in the chunk buffer.
+double* batch_alpha(korg_ctx* ctx, const BatchPlan& p, int i, int64_t nwl) {
+    int c = 0;
+    while (p.chunk_first[c + 1] <= i) c++;
+    return static_cast<double*>(ctx->b_alpha.p) + size_t(i - p.chunk_first[c]) * (a256(8 * size_t(p.L) * nwl) / 8);
+}
+
+// Host copies of the tile arguments (one per spectrum) and of the reference wavelengths.
+void fill_batch_host(korg_ctx* ctx, const BatchPlan& p, int nspec, const korg_batch_item* it, const double* wls,
+                     int64_t nwl) {
+    unsigned char* h = static_cast<unsigned char*>(ctx->b_host);
+    auto* targs = reinterpret_cast<TileArgs*>(h + p.o_targs);
+    auto* refwl = reinterpret_cast<double*>(h + p.o_refwl);
+    unsigned char* meta = static_cast<unsigned char*>(ctx->b_meta.p);
+    auto* zero = reinterpret_cast<int32_t*>(meta + p.o_zero);
+    for (int i = 0; i < nspec; i++) {
+        LineScratch sc;
+        line_scratch(static_cast<unsigned char*>(ctx->b_lines.p) + p.line_off[i], it[i].lines.n, p.L, p.Lp, p.G,
+                     p.mixed, &sc);
+        if (it[i].lines.n == 0) {
+            sc.tier_meta = zero;  // all tier runs empty
+        }
+        TileArgs ta = make_tile_args(sc, batch_alpha(ctx, p, i, nwl), wls, nwl, lines_dev(&it[i].lines), p.L, p.Lp, p.G);
+        ta.stage = p.geom.stage;
+        ta.region = p.geom.region;
+        targs[i] = ta;
+        refwl[i] = it[i].in.ref_wl;
+    }
+}
+
+// Identity of a batch submission: everything the enqueued work depends on.
+std::vector<unsigned char> batch_key(korg_ctx* ctx, int nspec, const korg_batch_item* it, const double* wls,
+                                     int64_t nwl, int precision) {
+    std::vector<unsigned char> k;
+    auto put = [&](const void* p, size_t n) {
+        const unsigned char* c = static_cast<const unsigned char*>(p);
+        k.insert(k.end(), c, c + n);
+    };
+    const int L = it[0].in.layers.L;
+    const TileCfg cfg = tile_cfg(ctx, L, precision == KORG_MIXED);
+    put(&nspec, sizeof nspec);
+    put(it, sizeof(korg_batch_item) * size_t(nspec));
+    put(&wls, sizeof wls);
+    put(&nwl, sizeof nwl);
+    put(&precision, sizeof precision);
+    put(&ctx->batch_budget, sizeof ctx->batch_budget);
+    put(&cfg, sizeof cfg);
+    return k;
+}
+
+// ------------------------------------------------------------------ reverse mode (VJP)
+// Perturbed copies of the per-layer hydrogen-line inputs: field `which` of {T, ne, nH_I, nHe_I,
+// UH_I, xi} scaled by (1 + sign * rel) in every layer; h[l] = rel * |value|.
+__global__ void hfd_perturb_kernel(HLayers src, int which, double rel, double sign, double* dst, double* h) {
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    const int L = src.L;
+    if (l >= L) return;
+    const double* f[6] = {src.T, src.ne, src.nH, src.nHe, src.UH, src.xi};
+    for (int k = 0; k < 6; k++) {
+        double v = f[k][l];
+        if (k == which) {
+            const double d = rel * fabs(v);
+            if (sign > 0) h[l] = d;
+            v += sign * d;
+        }
+        dst[k * L + l] = v;
+    }
+}
+
+int run_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& ln, const LinesDev& ln5, const double* wls,
+            int64_t nwl, bool mixed, const double* dflux, const double* dcntm, const korg_synth_grads& gr, int flags,
+            const double* ref_wl_dev, cudaStream_t s) {
+    const LayersDev lay = layers_dev(&in->layers);
+    const int L = lay.L, S = lay.S;
+    if (L > RTA_LMAX) return set_err(ctx, KORG_EINVAL, "the adjoint supports at most %d layers", RTA_LMAX);
+    int kmax = 0;
+    const int G = layer_groups(L, &kmax);
+    if (G < 0) return set_err(ctx, KORG_EINVAL, "at most 256 layers are supported (got %d)", L);
+    const int Lp = G * kmax;
+    const CntmDev cn{in->cntm.nk, in->cntm.knots, in->cntm.vals};
+    const size_t nLw = size_t(L) * nwl;
+    const int64_t nmax = std::max<int64_t>(std::max<int64_t>(ln.n, ln5.n), 1);
+    KCHECK(ensure(ctx, ctx->alpha, sizeof(double) * nLw));
+    KCHECK(ensure(ctx, ctx->aref, sizeof(double) * (L + 1)));
+    KCHECK(ensure(ctx, ctx->vjp_g, (mixed ? sizeof(float) : sizeof(double)) * nLw));
+    KCHECK(ensure(ctx, ctx->vjp_dpar, sizeof(double) * 3 * size_t(nmax) * Lp));
+    // small pieces: daref [L], a scratch dT [L], hydrogen FD inputs [2][6][L], steps [L], counter
+    const size_t o_dar = 0, o_dT = a256(8 * L), o_hin = o_dT + a256(8 * L), o_h = o_hin + a256(8 * 12 * L),
+                 o_ctr = o_h + a256(8 * L), small = o_ctr + 256;
+    KCHECK(ensure(ctx, ctx->vjp_small, small));
+    unsigned char* sm = static_cast<unsigned char*>(ctx->vjp_small.p);
+    double* daref = reinterpret_cast<double*>(sm + o_dar);
+    double* dT = gr.T ? gr.T : reinterpret_cast<double*>(sm + o_dT);
+    auto* ctr = reinterpret_cast<unsigned long long*>(sm + o_ctr);
+    // outputs start at zero (every kernel below accumulates)
+    auto zero = [&](double* p, size_t n) -> int {
+        if (p) KCUDA(cudaMemsetAsync(p, 0, 8 * n, s));
+        return KORG_OK;
+    };
+    KCHECK(zero(dT, L));
+    KCHECK(zero(gr.ne, L));
+    KCHECK(zero(gr.n_eff_vdW, L));
+    KCHECK(zero(gr.xi, L));
+    KCHECK(zero(gr.n_div_U, size_t(S) * L));
+    KCHECK(zero(gr.nH_I, L));
+    KCHECK(zero(gr.nHe_I, L));
+    KCHECK(zero(gr.UH_I, L));
+    KCHECK(zero(gr.log_gf, size_t(ln.n)));
+    KCHECK(zero(gr.cntm_vals, size_t(L) * in->cntm.nk));
+    KCHECK(zero(daref, L));
+    KCHECK(reset_counters(ctx, s));
+
+    // 1. opacity, recomputed (src/synthesize.jl:249-306 as in the forward)
+    double* alpha = static_cast<double*>(ctx->alpha.p);
+    double* aref = static_cast<double*>(ctx->aref.p);
+    alpha_init_kernel<<<unsigned((nwl + 63) / 64), 256, 0, s>>>(alpha, wls, nwl, L, cn);
+    KCUDA(cudaGetLastError());
+    KCUDA(cudaMemcpyAsync(aref, in->alpha_ref_cntm, sizeof(double) * L, cudaMemcpyDeviceToDevice, s));
+    const CntmDev cref{1, nullptr, in->alpha_ref_cntm};
+    KCHECK(run_line_absorption(ctx, aref, ref_wl_dev, 1, ln5, lay, cref, in->cutoff_threshold, mixed, s));
+    const HLayers hl{L, lay.T, lay.ne, in->nH_I, in->nHe_I, in->UH_I, lay.xi};
+    if (in->hydrogen_lines) KCHECK(run_hydrogen(ctx, alpha, wls, nwl, hl, in->hydrogen_window, in->use_MHD, mixed, s));
+    KCHECK(run_line_absorption(ctx, alpha, wls, nwl, ln, lay, cn, in->cutoff_threshold, mixed, s));
+
+    // 2. transfer adjoint: opacity cotangent G, dL/dT through the source function, dL/dalpha_ref
+    RtAdjArgs ra{alpha, lay.T, wls, nwl, L, in->tau_ref, aref, static_cast<MathTables*>(ctx->math.p), cn, dflux,
+                 dcntm, 1e-8, ctx->vjp_g.p, int32_t(mixed), dT, daref, gr.cntm_vals};
+    {
+        const size_t smem = size_t(RTA_WARPS) * RTA_ARRAYS * (L + 1) * sizeof(double);
+        KCUDA(cudaFuncSetAttribute(rt_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        const int64_t blocks = std::min<int64_t>((nwl + RTA_WARPS - 1) / RTA_WARPS, int64_t(ctx->sms) * 8);
+        rt_adjoint_kernel<<<unsigned(blocks), 32 * RTA_WARPS, smem, s>>>(ra);
+        KCUDA(cudaGetLastError());
+    }
+
+    // 3. hydrogen lines: layer-diagonal Jacobian by central differences of the FP64 kernel
+    if (in->hydrogen_lines && (flags & KORG_VJP_HYDROGEN)) {
+        KCHECK(ensure(ctx, ctx->vjp_hfd, sizeof(double) * 2 * nLw));
+        double* ap = static_cast<double*>(ctx->vjp_hfd.p);
+        double* am = ap + nLw;
+        double* hin = reinterpret_cast<double*>(sm + o_hin);
+        double* h = reinterpret_cast<double*>(sm + o_h);
+        double* outs[6] = {dT, gr.ne, gr.nH_I, gr.nHe_I, gr.UH_I, gr.xi};
+        for (int k = 0; k < 6; k++) {
+            if (!outs[k]) continue;
+            const double rel = 1e-5;
+            hfd_perturb_kernel<<<(L + 127) / 128, 128, 0, s>>>(hl, k, rel, +1.0, hin, h);
+            hfd_perturb_kernel<<<(L + 127) / 128, 128, 0, s>>>(hl, k, rel, -1.0, hin + 6 * L, h);
+            KCUDA(cudaGetLastError());
+            KCUDA(cudaMemsetAsync(ap, 0, sizeof(double) * 2 * nLw, s));
+            const HLayers hp{L, hin, hin + L, hin + 2 * L, hin + 3 * L, hin + 4 * L, hin + 5 * L};
+            const double* hm0 = hin + 6 * L;
+            const HLayers hm{L, hm0, hm0 + L, hm0 + 2 * L, hm0 + 3 * L, hm0 + 4 * L, hm0 + 5 * L};
+            KCHECK(run_hydrogen(ctx, ap, wls, nwl, hp, in->hydrogen_window, in->use_MHD, false, s));
+            KCHECK(run_hydrogen(ctx, am, wls, nwl, hm, in->hydrogen_window, in->use_MHD, false, s));
+            hydro_fd_contract_kernel<<<ctx->sms * 4, 256, 0, s>>>(ctx->vjp_g.p, int32_t(mixed), ap, am, h, nwl, L,
+                                                                 outs[k]);
+            KCUDA(cudaGetLastError());
+        }
+    }
+
+    // 4. metal and molecular lines: window sums per (line, layer), then the prologue chain rule
+    const LineAdjOut lo{dT, gr.ne, gr.n_eff_vdW, gr.xi, gr.n_div_U, gr.log_gf};
+    auto line_adjoint = [&](const LinesDev& lns, const void* Gp, int g32, const double* w, int64_t nw,
+                            const LineAdjOut& out) -> int {
+        if (lns.n == 0) return KORG_OK;
+        LineScratch sc;
+        line_scratch(static_cast<unsigned char*>(ctx->lines_scratch.p), lns.n, L, Lp, G, mixed, &sc);
+        double* dpar = static_cast<double*>(ctx->vjp_dpar.p);
+        KCUDA(cudaMemsetAsync(dpar, 0, sizeof(double) * 3 * size_t(lns.n) * Lp, s));
+        KCUDA(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), s));
+        LineAdjArgs la{Gp, g32, w, nw, L, Lp, lns.wl, sc.params, sc.lb, sc.ub, sc.tier_idx, sc.tier_meta, dpar, ctr};
+        const int threads = ((L + 31) / 32) * 32;
+        int per_sm = 0;
+        if (mixed) {
+            KCUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, line_adj_kernel<true>, threads, 0));
+            line_adj_kernel<true><<<ctx->sms * std::max(per_sm, 1), threads, 0, s>>>(la);
+        } else {
+            KCUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, line_adj_kernel<false>, threads, 0));
+            line_adj_kernel<false><<<ctx->sms * std::max(per_sm, 1), threads, 0, s>>>(la);
+        }
+        KCUDA(cudaGetLastError());
+        const size_t psmem = sizeof(double) * size_t(4 + S) * L;
+        KCUDA(cudaFuncSetAttribute(line_adj_prologue_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(psmem)));
+        line_adj_prologue_kernel<<<unsigned((lns.n * 32 + 255) / 256), 256, psmem, s>>>(
+            lns, lay, sc.lc, dpar, Lp, out, static_cast<MathTables*>(ctx->math.p));
+        KCUDA(cudaGetLastError());
+        return KORG_OK;
+    };
+    // the metal-line prologue of step 1 is still in the line scratch
+    KCHECK(line_adjoint(ln, ctx->vjp_g.p, int(mixed), wls, nwl, lo));
+    // 5. reference-wavelength lines: alpha_ref = continuum + lines at ref_wl, cotangent daref
+    if (ln5.n > 0) {
+        LineScratch sc;
+        KCHECK(ensure(ctx, ctx->lines_scratch, line_scratch(nullptr, ln5.n, L, Lp, G, mixed, nullptr)));
+        line_scratch(static_cast<unsigned char*>(ctx->lines_scratch.p), ln5.n, L, Lp, G, mixed, &sc);
+        KCHECK(prep_lines(ctx, sc, ref_wl_dev, 1, ln5, lay, cref, in->cutoff_threshold, mixed, kmax, G, s));
+        const LineAdjOut lo5{dT, gr.ne, gr.n_eff_vdW, gr.xi, gr.n_div_U, nullptr};
+        KCHECK(line_adjoint(ln5, daref, 0, ref_wl_dev, 1, lo5));
+    }
+    if (gr.alpha_ref_cntm)
+        KCUDA(cudaMemcpyAsync(gr.alpha_ref_cntm, daref, sizeof(double) * L, cudaMemcpyDeviceToDevice, s));
+    ctx->stats_pending = true;
+    return KORG_OK;
+}
+
 // ------------------------------------------------------------------ host staging
 struct Stager {
     std::vector<std::pair<const void*, size_t>> items;
@@ -444,8 +923,10 @@ KORG_API int korg_create(korg_ctx** out, int device) {
     korg_ctx* ctx = new korg_ctx();
     ctx->device = device;
     cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     for (int i = 0; e == cudaSuccess && i < NEV; i++) e = cudaEventCreate(&ctx->ev[i]);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->b_host_ev, cudaEventDisableTiming);
     if (e == cudaSuccess) {
         MathTables t;
         fill_math_tables(t);
@@ -467,15 +948,19 @@ KORG_API void korg_destroy(korg_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    DevBuf* bufs[] = {&ctx->lc, &ctx->params, &ctx->xfar, &ctx->amask, &ctx->lb, &ctx->ub, &ctx->ci, &ctx->tier_idx, &ctx->tier_ci, &ctx->tier_meta, &ctx->counters,
-                      &ctx->hrec, &ctx->hQ, &ctx->hQ32, &ctx->hulb, &ctx->huub, &ctx->stage_dev, &ctx->aref,
-                      &ctx->alpha, &ctx->flux, &ctx->cntm, &ctx->math};
+    drop_graph(ctx);
+    DevBuf* bufs[] = {&ctx->lines_scratch, &ctx->counters, &ctx->tune_alpha, &ctx->hrec, &ctx->hQ, &ctx->hQ32,
+                      &ctx->hulb, &ctx->huub, &ctx->stage_dev, &ctx->aref, &ctx->alpha, &ctx->flux, &ctx->cntm,
+                      &ctx->math, &ctx->b_alpha, &ctx->b_lines, &ctx->b_meta, &ctx->vjp_g, &ctx->vjp_dpar,
+                      &ctx->vjp_small, &ctx->vjp_hfd};
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
     for (void* p : ctx->stark_allocs) cudaFree(p);
     if (ctx->stage_host) cudaFreeHost(ctx->stage_host);
+    if (ctx->b_host) cudaFreeHost(ctx->b_host);
     for (int i = 0; i < NEV; i++)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+    if (ctx->b_host_ev) cudaEventDestroy(ctx->b_host_ev);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -519,6 +1004,8 @@ KORG_API int korg_get_stats(korg_ctx* ctx, korg_stats* out) {
 KORG_API int korg_set_stark_tables(korg_ctx* ctx, const korg_stark_tables* t) {
     if (!ctx || !t || t->ntrans < 1) return KORG_EINVAL;
     KCUDA(cudaSetDevice(ctx->device));
+    drop_graph(ctx);  // a captured batch holds the old table addresses
+    KCUDA(cudaDeviceSynchronize());
     for (void* p : ctx->stark_allocs) cudaFree(p);
     ctx->stark_allocs.clear();
     ctx->have_stark = false;
@@ -689,6 +1176,97 @@ KORG_API int korg_radiative_transfer(korg_ctx* ctx, const double* alpha, const d
     return KORG_OK;
 }
 
+KORG_API int korg_radiative_transfer_general(korg_ctx* ctx, const double* alpha, const double* S, int32_t L,
+                                             int64_t nwl, const double* spatial, int spherical,
+                                             const double* tau_ref, const double* alpha_ref, const double* mu,
+                                             const double* mu_weights, int32_t n_mu, int include_inward_rays,
+                                             int tau_scheme, int I_scheme, double* flux, double* I_surface) {
+    if (!ctx) return KORG_EINVAL;
+    if (!alpha || !S || L < 1 || nwl < 1 || !spatial || !tau_ref || !alpha_ref || !mu || !mu_weights || n_mu < 1 ||
+        !flux)
+        return set_err(ctx, KORG_EINVAL, "bad arguments");
+    if (tau_scheme < 0 || tau_scheme > 1)
+        return set_err(ctx, KORG_EINVAL, "tau_scheme must be one of \"anchored\" or \"bezier\"");
+    if (I_scheme < 0 || I_scheme > 3)
+        return set_err(ctx, KORG_EINVAL, "I_scheme must be one of \"linear\", \"bezier\", or \"linear_flux_only\"");
+    if (I_scheme == 3 && (spherical || tau_scheme != 0))
+        return set_err(ctx, KORG_EINVAL, "the exponential-integral flux needs a planar atmosphere and anchored tau");
+    if (L > RTG_LMAX) return set_err(ctx, KORG_EINVAL, "at most %d layers", RTG_LMAX);
+    // rays (RadiativeTransfer.jl:218-242): path length s and ds/dz per surface mu
+    std::vector<int32_t> nlay(n_mu);
+    std::vector<double> s(size_t(n_mu) * L), dsdz(size_t(n_mu) * L);
+    for (int u = 0; u < n_mu; u++) {
+        if (spherical) {
+            const double b = spatial[0] * std::sqrt(1 - mu[u] * mu[u]);
+            int low;
+            if (b < spatial[L - 1]) {
+                low = L;
+            } else {
+                int am = 0;
+                for (int k = 1; k < L; k++)
+                    if (std::fabs(spatial[k] - b) < std::fabs(spatial[am] - b)) am = k;
+                if (spatial[am] < b) am -= 1;
+                low = am + 1;
+            }
+            nlay[u] = low;
+            for (int k = 0; k < low; k++) {
+                s[size_t(u) * L + k] = std::sqrt(spatial[k] * spatial[k] - b * b);
+                dsdz[size_t(u) * L + k] = spatial[k] / s[size_t(u) * L + k];
+            }
+        } else {
+            nlay[u] = L;
+            for (int k = 0; k < L; k++) {
+                s[size_t(u) * L + k] = spatial[k] / mu[u];
+                dsdz[size_t(u) * L + k] = 1.0 / mu[u];
+            }
+        }
+    }
+    // inward rays: all, or those that do not reach the bottom (:94-98)
+    std::vector<int> in_idx;
+    for (int u = 0; u < n_mu; u++)
+        if (include_inward_rays || nlay[u] < L) in_idx.push_back(u);
+    const int n_in = int(in_idx.size()), nrays = n_in + n_mu;
+    if (nrays > RTG_RMAX) return set_err(ctx, KORG_EINVAL, "at most %d rays (inward + outward)", RTG_RMAX);
+    std::vector<int32_t> rn(nrays);
+    std::vector<double> rfac(size_t(nrays) * L, 0.0), rlt(size_t(nrays) * L, 0.0), rpath(size_t(nrays) * L, 0.0);
+    for (int r = 0; r < nrays; r++) {
+        const bool inward = r < n_in;
+        const int u = inward ? in_idx[r] : r - n_in;
+        const int n = nlay[u];
+        rn[r] = n;
+        for (int k = 0; k < n; k++) {
+            const int lk = inward ? n - 1 - k : k;
+            rpath[size_t(r) * L + k] = inward ? -s[size_t(u) * L + lk] : s[size_t(u) * L + lk];
+            rfac[size_t(r) * L + k] = tau_ref[lk] / alpha_ref[lk] * dsdz[size_t(u) * L + lk];
+            rlt[size_t(r) * L + k] = inward ? -std::log(tau_ref[lk]) : std::log(tau_ref[lk]);
+        }
+    }
+    std::vector<double> wmu(n_mu);
+    for (int u = 0; u < n_mu; u++) wmu[u] = mu_weights[u] * mu[u];
+    KCUDA(cudaSetDevice(ctx->device));
+    Stager st;
+    const size_t n = size_t(L) * nwl;
+    const size_t o_a = st.add(alpha, 8 * n), o_s = st.add(S, 8 * n);
+    const size_t o_rn = st.add(rn.data(), 4 * rn.size()), o_rf = st.add(rfac.data(), 8 * rfac.size());
+    const size_t o_rl = st.add(rlt.data(), 8 * rlt.size()), o_rp = st.add(rpath.data(), 8 * rpath.size());
+    const size_t o_w = st.add(wmu.data(), 8 * wmu.size());
+    const size_t o_f = st.add(nullptr, 8 * size_t(nwl));
+    const size_t o_i = I_surface ? st.add(nullptr, 8 * size_t(nwl) * n_mu) : 0;
+    char* b = nullptr;
+    KCHECK(upload(ctx, st, &b));
+    RtGenArgs ra{(double*)(b + o_a), (double*)(b + o_s), L, nwl, nrays, n_in, n_mu, (int32_t*)(b + o_rn),
+                 (double*)(b + o_rf), (double*)(b + o_rl), (double*)(b + o_rp), (double*)(b + o_w), tau_scheme,
+                 I_scheme, static_cast<MathTables*>(ctx->math.p), (double*)(b + o_f),
+                 I_surface ? (double*)(b + o_i) : nullptr};
+    rt_general_kernel<<<unsigned((nwl + 127) / 128), 128, 0, ctx->stream>>>(ra);
+    KCUDA(cudaGetLastError());
+    KCUDA(cudaMemcpyAsync(flux, b + o_f, 8 * size_t(nwl), cudaMemcpyDeviceToHost, ctx->stream));
+    if (I_surface)
+        KCUDA(cudaMemcpyAsync(I_surface, b + o_i, 8 * size_t(nwl) * n_mu, cudaMemcpyDeviceToHost, ctx->stream));
+    KCUDA(cudaStreamSynchronize(ctx->stream));
+    return KORG_OK;
+}
+
 KORG_API int korg_synthesize_dev(korg_ctx* ctx, const korg_synth_inputs* in, const korg_lines* lines,
                                  const korg_lines* lines5, const double* wls, int64_t nwl, int precision,
                                  double* flux, double* cntm, double* alpha_out, void* stream) {
@@ -768,6 +1346,197 @@ KORG_API int korg_synthesize(korg_ctx* ctx, const korg_synth_inputs* in, const k
         KCUDA(cudaMemcpyAsync(alpha_out, d_alpha, 8 * size_t(L) * nwl, cudaMemcpyDeviceToHost, ctx->stream));
     if (alpha_ref_out) KCUDA(cudaMemcpyAsync(alpha_ref_out, aref, 8 * size_t(L), cudaMemcpyDeviceToHost, ctx->stream));
     KCUDA(cudaStreamSynchronize(ctx->stream));
+    return KORG_OK;
+}
+
+
+KORG_API int korg_synthesize_vjp_dev(korg_ctx* ctx, const korg_synth_inputs* in, const korg_lines* lines,
+                                     const korg_lines* lines5, const double* wls, int64_t nwl, int precision,
+                                     const double* dflux, const double* dcntm, const korg_synth_grads* grads,
+                                     int flags, void* stream) {
+    if (!ctx) return KORG_EINVAL;
+    if (!in || !lines || !lines5 || !wls || nwl < 1 || !grads || (!dflux && !dcntm))
+        return set_err(ctx, KORG_EINVAL, "bad arguments");
+    if (in->cntm.nk < 2 || in->layers.L < 1)
+        return set_err(ctx, KORG_EINVAL, "synthesize needs a continuum grid of at least 2 knots");
+    if (in->hydrogen_lines && !ctx->have_stark)
+        return set_err(ctx, KORG_ENOTABLES, "korg_set_stark_tables() has not been called");
+    KCUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int L = in->layers.L;
+    KCHECK(ensure(ctx, ctx->aref, sizeof(double) * (L + 1)));
+    double* aref = static_cast<double*>(ctx->aref.p);
+    KCUDA(cudaMemcpyAsync(aref + L, &in->ref_wl, sizeof(double), cudaMemcpyHostToDevice, s));
+    return run_vjp(ctx, in, lines_dev(lines), lines_dev(lines5), wls, nwl, precision == KORG_MIXED, dflux, dcntm,
+                   *grads, flags, aref + L, s);
+}
+
+KORG_API int korg_synthesize_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const korg_lines* lines,
+                                 const korg_lines* lines5, const double* wls, int64_t nwl, int precision,
+                                 const double* dflux, const double* dcntm, const korg_synth_grads* grads, int flags) {
+    if (!ctx) return KORG_EINVAL;
+    if (!in || !grads || (!dflux && !dcntm)) return set_err(ctx, KORG_EINVAL, "bad arguments");
+    KCHECK(check_wls(ctx, wls, nwl));
+    KCHECK(check_layers(ctx, &in->layers));
+    KCHECK(check_lines(ctx, lines, in->layers.S));
+    KCHECK(check_lines(ctx, lines5, in->layers.S));
+    if (in->cntm.nk < 2 || !in->cntm.knots || !in->cntm.vals || !in->tau_ref || !in->alpha_ref_cntm)
+        return set_err(ctx, KORG_EINVAL, "bad continuum / reference inputs");
+    if (in->hydrogen_lines && (!in->nH_I || !in->nHe_I || !in->UH_I))
+        return set_err(ctx, KORG_EINVAL, "hydrogen lines need nH_I, nHe_I and UH_I");
+    KCUDA(cudaSetDevice(ctx->device));
+    const int L = in->layers.L, S = in->layers.S;
+    const int64_t nk = in->cntm.nk;
+    Stager st;
+    const size_t o_w = st.add(wls, 8 * size_t(nwl));
+    LinesStage ls = stage_lines(st, lines), ls5 = stage_lines(st, lines5);
+    const korg_layers& y = in->layers;
+    const size_t o_T = st.add(y.T, 8 * L), o_ne = st.add(y.ne, 8 * L), o_nv = st.add(y.n_eff_vdW, 8 * L),
+                 o_xi = st.add(y.xi, 8 * L), o_nu = st.add(y.n_div_U, 8 * size_t(L) * S);
+    const size_t o_tr = st.add(in->tau_ref, 8 * L), o_ar = st.add(in->alpha_ref_cntm, 8 * L);
+    const size_t o_h1 = in->hydrogen_lines ? st.add(in->nH_I, 8 * L) : 0;
+    const size_t o_h2 = in->hydrogen_lines ? st.add(in->nHe_I, 8 * L) : 0;
+    const size_t o_h3 = in->hydrogen_lines ? st.add(in->UH_I, 8 * L) : 0;
+    const size_t o_ck = st.add(in->cntm.knots, 8 * nk);
+    const size_t o_cv = st.add(in->cntm.vals, 8 * size_t(L) * nk);
+    const size_t o_df = dflux ? st.add(dflux, 8 * size_t(nwl)) : 0;
+    const size_t o_dc = dcntm ? st.add(dcntm, 8 * size_t(nwl)) : 0;
+    // device outputs: one slot per gradient the caller asked for
+    const size_t sizes[11] = {size_t(L), size_t(L), size_t(L), size_t(L), size_t(S) * L, size_t(L), size_t(L),
+                              size_t(L), size_t(lines->n), size_t(L) * nk, size_t(L)};
+    double* const host_out[11] = {grads->T, grads->ne, grads->n_eff_vdW, grads->xi, grads->n_div_U, grads->nH_I,
+                                  grads->nHe_I, grads->UH_I, grads->log_gf, grads->cntm_vals, grads->alpha_ref_cntm};
+    size_t o_out[11];
+    for (int k = 0; k < 11; k++) o_out[k] = host_out[k] ? st.add(nullptr, 8 * std::max<size_t>(sizes[k], 1)) : 0;
+    char* b = nullptr;
+    KCHECK(upload(ctx, st, &b));
+    korg_synth_inputs d = *in;
+    d.layers = korg_layers{L, S, (double*)(b + o_T), (double*)(b + o_ne), (double*)(b + o_nv), (double*)(b + o_xi),
+                           (double*)(b + o_nu)};
+    d.tau_ref = (double*)(b + o_tr);
+    d.alpha_ref_cntm = (double*)(b + o_ar);
+    d.nH_I = in->hydrogen_lines ? (double*)(b + o_h1) : nullptr;
+    d.nHe_I = in->hydrogen_lines ? (double*)(b + o_h2) : nullptr;
+    d.UH_I = in->hydrogen_lines ? (double*)(b + o_h3) : nullptr;
+    d.cntm = korg_cntm{nk, (double*)(b + o_ck), (double*)(b + o_cv)};
+    double* dev_out[11];
+    for (int k = 0; k < 11; k++) dev_out[k] = host_out[k] ? (double*)(b + o_out[k]) : nullptr;
+    const korg_synth_grads dg{dev_out[0], dev_out[1], dev_out[2], dev_out[3], dev_out[4], dev_out[5],
+                              dev_out[6], dev_out[7], dev_out[8], dev_out[9], dev_out[10]};
+    KCHECK(ensure(ctx, ctx->aref, sizeof(double) * (L + 1)));
+    double* aref = static_cast<double*>(ctx->aref.p);
+    KCUDA(cudaMemcpyAsync(aref + L, &in->ref_wl, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    KCHECK(run_vjp(ctx, &d, lines_from_stage(ls, b, lines->n), lines_from_stage(ls5, b, lines5->n),
+                   (double*)(b + o_w), nwl, precision == KORG_MIXED, dflux ? (double*)(b + o_df) : nullptr,
+                   dcntm ? (double*)(b + o_dc) : nullptr, dg, flags, aref + L, ctx->stream));
+    for (int k = 0; k < 11; k++)
+        if (host_out[k] && sizes[k])
+            KCUDA(cudaMemcpyAsync(host_out[k], dev_out[k], 8 * sizes[k], cudaMemcpyDeviceToHost, ctx->stream));
+    KCUDA(cudaStreamSynchronize(ctx->stream));
+    return KORG_OK;
+}
+
+KORG_API int korg_set_batch_options(korg_ctx* ctx, int use_graph, int autotune, int64_t max_scratch_bytes) {
+    if (!ctx) return KORG_EINVAL;
+    if (max_scratch_bytes < 0) return set_err(ctx, KORG_EINVAL, "negative scratch budget");
+    drop_graph(ctx);
+    ctx->use_graph = use_graph != 0;
+    ctx->autotune = autotune != 0;
+    if (max_scratch_bytes > 0) ctx->batch_budget = max_scratch_bytes;
+    return KORG_OK;
+}
+
+KORG_API int korg_get_tile_config(korg_ctx* ctx, int32_t L, int precision, int32_t* tw, int32_t* stage,
+                                  int32_t* tuned) {
+    if (!ctx || !tw || !stage) return KORG_EINVAL;
+    const bool mixed = precision == KORG_MIXED;
+    const TileCfg c = tile_cfg(ctx, L, mixed);
+    *tw = c.tw;
+    *stage = c.stage > 0 ? c.stage : (mixed ? STAGE_LINES : STAGE_LINES / 2);
+    if (tuned) *tuned = ctx->tuned.count(std::make_pair(int(L), int(mixed))) ? 1 : 0;
+    return KORG_OK;
+}
+
+KORG_API int korg_synthesize_batch_dev(korg_ctx* ctx, int32_t nspec, const korg_batch_item* items,
+                                       const double* wls, int64_t nwl, int precision, void* stream) {
+    if (!ctx) return KORG_EINVAL;
+    if (nspec < 1 || !items || !wls || nwl < 1 || nwl > INT32_MAX - 1)
+        return set_err(ctx, KORG_EINVAL, "bad batch arguments");
+    KCUDA(cudaSetDevice(ctx->device));
+    cudaStream_t us = static_cast<cudaStream_t>(stream);
+    const bool mixed = precision == KORG_MIXED;
+    std::vector<unsigned char> key = batch_key(ctx, nspec, items, wls, nwl, precision);
+    if (ctx->use_graph && ctx->gexec && key == ctx->gkey) {  // same batch again: replay
+        KCUDA(cudaGraphLaunch(ctx->gexec, us));
+        KCUDA(cudaEventRecord(ctx->b_host_ev, us));
+        ctx->stats_pending = true;
+        return KORG_OK;
+    }
+    BatchPlan p;
+    KCHECK(plan_batch(ctx, nspec, items, nwl, mixed, &p));
+    if (ctx->autotune && !ctx->tuned.count(std::make_pair(p.L, int(mixed)))) {
+        int first = -1;  // the spectrum with most lines stands for the batch
+        for (int i = 0; i < nspec; i++)
+            if (first < 0 || items[i].lines.n > items[first].lines.n) first = i;
+        if (worth_tuning(nwl, items[first].lines.n)) {
+            const korg_batch_item& b = items[first];
+            const LinesDev ln = lines_dev(&b.lines);
+            KCHECK(ensure(ctx, ctx->lines_scratch, line_scratch(nullptr, ln.n, p.L, p.Lp, p.G, mixed, nullptr)));
+            LineScratch sc;
+            line_scratch(static_cast<unsigned char*>(ctx->lines_scratch.p), ln.n, p.L, p.Lp, p.G, mixed, &sc);
+            KCHECK(reset_counters(ctx, us));
+            KCHECK(prep_lines(ctx, sc, wls, nwl, ln, layers_dev(&b.in.layers),
+                              CntmDev{b.in.cntm.nk, b.in.cntm.knots, b.in.cntm.vals}, b.in.cutoff_threshold, mixed,
+                              p.kmax, p.G, us));
+            KCHECK(autotune_tiles(ctx, make_tile_args(sc, nullptr, wls, nwl, ln, p.L, p.Lp, p.G), p.kmax, mixed, us));
+            KCHECK(plan_batch(ctx, nspec, items, nwl, mixed, &p));
+            key = batch_key(ctx, nspec, items, wls, nwl, precision);
+        }
+    }
+    KCHECK(ensure(ctx, ctx->b_alpha, p.alpha_bytes));
+    KCHECK(ensure(ctx, ctx->b_lines, p.lines_bytes));
+    KCHECK(ensure(ctx, ctx->b_meta, p.meta_bytes));
+    // the previous batch's copy out of the host buffer (eager or replayed) must have run
+    KCUDA(cudaEventSynchronize(ctx->b_host_ev));
+    if (ctx->b_host_cap < p.host_bytes) {
+        drop_graph(ctx);
+        if (ctx->b_host) cudaFreeHost(ctx->b_host);
+        ctx->b_host = nullptr;
+        ctx->b_host_cap = 0;
+        KCUDA(cudaHostAlloc(&ctx->b_host, p.host_bytes + p.host_bytes / 4, cudaHostAllocDefault));
+        ctx->b_host_cap = p.host_bytes + p.host_bytes / 4;
+    }
+    fill_batch_host(ctx, p, nspec, items, wls, nwl);
+    if (ctx->use_graph && !ctx->pending_key.empty() && key == ctx->pending_key) {
+        // second submission of the same batch: capture it on the context's stream, then replay
+        if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+        ctx->gexec = nullptr;
+        ctx->gkey.clear();
+        KCUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed));
+        ctx->capturing = true;
+        const int rc = enqueue_batch(ctx, p, nspec, items, wls, nwl, ctx->stream);
+        ctx->capturing = false;
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+        if (rc != KORG_OK) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) return set_err(ctx, KORG_ECUDA, "graph capture: %s", cudaGetErrorString(e));
+        const cudaError_t e2 = cudaGraphInstantiate(&ctx->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (e2 != cudaSuccess) {
+            ctx->gexec = nullptr;
+            return set_err(ctx, KORG_ECUDA, "graph instantiation: %s", cudaGetErrorString(e2));
+        }
+        ctx->gkey = key;
+        ctx->pending_key.clear();
+        KCUDA(cudaGraphLaunch(ctx->gexec, us));
+    } else {
+        KCHECK(enqueue_batch(ctx, p, nspec, items, wls, nwl, us));
+        if (ctx->use_graph) ctx->pending_key = key;
+    }
+    KCUDA(cudaEventRecord(ctx->b_host_ev, us));
     return KORG_OK;
 }
 
@@ -982,7 +1751,8 @@ extern "C" KORG_API int korg_line_absorption_noalloc(double* alpha, const double
     const size_t prep_smem = size_t(256 / 32) * Lp * (sizeof(float) + sizeof(int));
     const unsigned pblocks = unsigned((n * 32 + 255) / 256);
     if (mixed)
-        line_prep_mixed_kernel<<<pblocks, 256, prep_smem, s>>>(ln, lay, lc, cn, wls, nwl, cutoff, po, math);
+        line_prep_mixed_kernel<<<prep_mixed_blocks(n), 32 * PREP_WARPS, prep_mixed_smem(Lp), s>>>(
+            ln, lay, lc, cn, wls, nwl, cutoff, po, math);
     else
         line_prep64_kernel<<<pblocks, 256, prep_smem, s>>>(ln, lay, lc, cn, wls, nwl, cutoff, po, math);
     TierLists tl{reinterpret_cast<int32_t*>(sp + o_ti), reinterpret_cast<int32_t*>(sp + o_tc), meta, meta + NTIER + 1};

@@ -47,15 +47,25 @@ struct LayerConst {
     double beta;    // 1/(k T)
     double stark6;  // (T/10^4)^(1/6)
     double vdw3;    // (T/10^4)^0.3
+    // FP32 copies for the mixed-precision prologue: T, xi, n_e, n_eff_vdW, stark6, vdw3
+    float T32, xi32, ne32, nv32, stark6_32, vdw3_32;
 };
 
 __global__ void layer_const_kernel(LayersDev lay, LayerConst* out) {
     int l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l >= lay.L) return;
     double T = lay.T[l];
-    out[l].beta = 1 / (KBOLTZ_EV * T);
-    out[l].stark6 = pow(T / 10000.0, 1.0 / 6.0);
-    out[l].vdw3 = pow(T / 10000.0, 0.3);
+    LayerConst c;
+    c.beta = 1 / (KBOLTZ_EV * T);
+    c.stark6 = pow(T / 10000.0, 1.0 / 6.0);
+    c.vdw3 = pow(T / 10000.0, 0.3);
+    c.T32 = float(T);
+    c.xi32 = float(lay.xi[l]);
+    c.ne32 = float(lay.ne[l]);
+    c.nv32 = float(lay.n_eff_vdW[l]);
+    c.stark6_32 = float(c.stark6);
+    c.vdw3_32 = float(c.vdw3);
+    out[l] = c;
 }
 
 struct PrepOut {
@@ -235,85 +245,134 @@ __device__ __forceinline__ void argmax_reduce(float& v, int& idx) {
 // Gaussian and Lorentzian windows, and those two layers are re-evaluated in FP64.
 // Packed constants: {c = 1/v-scale^2 = 2 sigma^2, a, w, scale} with scale = amp/(sigma sqrt(2 pi))
 // and w = a/sqrt(pi)*scale (a <= 0.2, asymptotic wing) or 1/gamma^2 (a > 0.2, far Lorentz).
-__global__ void __launch_bounds__(256) line_prep_mixed_kernel(LinesDev ln, LayersDev lay, const LayerConst* lc,
-                                                              CntmDev cn, const double* wls, int64_t nwl,
-                                                              double cutoff, PrepOut out, const MathTables* math) {
+//
+// Each warp handles 32 lines.  The per-line FP64 work (10^loggf, the continuum knot search,
+// the exact window at two layers) runs with one lane per line; the per-(line, layer) work runs
+// line by line with lanes over layers.  FP64 is 1/64 of the FP32 rate here, so keeping the
+// per-line FP64 work lane-parallel is what bounds this kernel.
+struct LinePrep32 {
+    double El, Eu, strength;   // FP64 line-strength inputs
+    float wlc, k_m, wl2c, grad, gstark, v1, abo_pre, vexp, invmu, t32;
+    int32_t flags, sp, ki;     // flags: 1 molecule, 2 ABO broadening; ki: continuum knot interval
+};
+constexpr int PREP_WARPS = 8;
+
+__global__ void __launch_bounds__(32 * PREP_WARPS) line_prep_mixed_kernel(LinesDev ln, LayersDev lay,
+                                                                          const LayerConst* lc, CntmDev cn,
+                                                                          const double* wls, int64_t nwl,
+                                                                          double cutoff, PrepOut out,
+                                                                          const MathTables* math) {
     __shared__ MathTables s_math;
-    extern __shared__ float s_dyn[];
+    __shared__ LinePrep32 s_line[PREP_WARPS][32];
+    extern __shared__ float s_dyn[];  // [warps][Lp] boundaries, then [warps][Lp] class flags
     load_math_tables(s_math, math);
     __syncthreads();
-    const int64_t i = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    if (i >= ln.n) return;
+    const int64_t base = (int64_t(blockIdx.x) * PREP_WARPS + wib) * 32;
+    if (base >= ln.n) return;
+    const int nl = int(min(int64_t(32), ln.n - base));
     const int L = lay.L, Lp = out.Lp;
     float* s_bnd = s_dyn + wib * Lp;
-    int* s_cls = reinterpret_cast<int*>(s_dyn + (blockDim.x >> 5) * Lp) + wib * Lp;
-    const LineConst q = line_const(ln, i);
-    const KnotPos kp = knot_pos(cn.knots, cn.nk, q.wl);
-    const float wlc = float(q.wl / C_CGS), m32 = float(q.m), wl2c = float(q.wl2c);
-    const float k_m = float(KBOLTZ_CGS / q.m);
-    float dmax = -1.f, lmax = -1.f;
-    int dl = 0, ll = 0;
-    float4* dst = reinterpret_cast<float4*>(out.params) + i * Lp;
-    for (int l = lane; l < Lp; l += 32) {
-        if (l >= L) {
-            dst[l] = make_float4(1.f, 0.f, 0.f, 0.f);
-            s_bnd[l] = 0.f;
-            s_cls[l] = 1;
-            continue;
-        }
-        const LayerConst c = lc[l];
-        const float T = float(lay.T[l]);
-        const float xi = float(lay.xi[l]);
-        const float sigma = wlc * sqrtf(k_m * T + 0.5f * xi * xi);
-        float G = float(q.grad);
-        if (!q.mol) {
-            float vdw;
-            if (q.v2 == -1) {
-                vdw = float(q.v1) * float(c.vdw3);
-            } else {
-                const float invmu = float(1 / (1.008 * AMU_CGS)) + 1.f / m32;
-                const float vbar = sqrtf(float(8 * KBOLTZ_CGS / PI) * T * invmu);
-                vdw = float(q.abo_pre) * powf(vbar * 1e-6f, float(1 - q.v2));
-            }
-            G = G + float(lay.ne[l]) * (float(q.gstark) * float(c.stark6)) + float(lay.n_eff_vdW[l]) * vdw;
-        }
-        const float gamma = G * wl2c;
-        const double levels = fexp64(-c.beta * q.El, s_math) - fexp64(-c.beta * q.E_upper, s_math);  // FP64
-        const float amp = float(q.strength * levels * lay.n_div_U[int64_t(q.sp) * L + l]);
-        const float acntm = float(knot_eval(cn.vals + int64_t(l) * cn.nk, cn.nk, kp));
-        const float rho = acntm * float(cutoff) / amp;
-        const float dw = inverse_gaussian32(rho, sigma), lw = inverse_lorentz32(rho, gamma);
-        if (dw > dmax) { dmax = dw; dl = l; }
-        if (lw > lmax) { lmax = lw; ll = l; }
-        const float s = 1.f / (sigma * 1.41421356f);
-        const float a = gamma * s;
-        const float scale = s * 0.56418958f * amp;  // 1/sqrt(pi)
-        const bool A = a <= 0.2f;
-        float4 p;
-        p.x = 2.f * sigma * sigma;
-        p.y = a;
-        p.z = A ? a * 0.56418958f * scale : 1.f / (gamma * gamma);
-        p.w = scale;
-        dst[l] = p;
-        // v >= 5 (a <= 0.2) or a + v >= 3.2 (0.2 < a <= 1.4) or any v (a > 1.4), v = x / sqrt(c)
-        s_bnd[l] = (A ? 5.f : (a <= 1.4f ? 3.2f - a : 0.f)) * sqrtf(p.x) * 1.0001f;
-        s_cls[l] = A;
+    int* s_cls = reinterpret_cast<int*>(s_dyn + PREP_WARPS * Lp) + wib * Lp;
+    // phase A: one lane per line
+    KnotPos kp_mine{0, 0.0};
+    if (lane < nl) {
+        const int64_t i = base + lane;
+        const LineConst q = line_const(ln, i);
+        kp_mine = knot_pos(cn.knots, cn.nk, q.wl);
+        LinePrep32 p;
+        p.El = q.El;
+        p.Eu = q.E_upper;
+        p.strength = q.strength;
+        p.wlc = float(q.wl / C_CGS);
+        p.k_m = float(KBOLTZ_CGS / q.m);
+        p.wl2c = float(q.wl2c);
+        p.grad = float(q.grad);
+        p.gstark = float(q.gstark);
+        p.v1 = float(q.v1);
+        p.abo_pre = float(q.abo_pre);
+        p.vexp = float(1 - q.v2);
+        p.invmu = float(1 / (1.008 * AMU_CGS)) + 1.f / float(q.m);
+        p.t32 = float(kp_mine.t);
+        p.flags = (q.mol ? 1 : 0) | ((!q.mol && q.v2 != -1) ? 2 : 0);
+        p.sp = q.sp;
+        p.ki = int32_t(kp_mine.i);
+        s_line[wib][lane] = p;
     }
     __syncwarp();
-    argmax_reduce(dmax, dl);
-    argmax_reduce(lmax, ll);
-    group_bounds(out, i, s_bnd, s_cls, lane);
-    // exact FP64 window at the two widest layers (lanes 0 and 1 in parallel)
-    double w = 0.0;
-    if (lane < 2) {
-        const int l = lane == 0 ? dl : ll;
-        const LineLayer64 r = line_layer64(q, lay, lc[l], cn, kp, cutoff, l, s_math);
-        w = lane == 0 ? r.dw : r.lw;
+    // phase B: line by line, lanes over layers
+    int my_dl = 0, my_ll = 0;
+    for (int t = 0; t < nl; t++) {
+        const int64_t i = base + t;
+        const LinePrep32& q = s_line[wib][t];
+        const bool mol = q.flags & 1, abo = q.flags & 2;
+        float dmax = -1.f, lmax = -1.f;
+        int dl = 0, ll = 0;
+        float4* dst = reinterpret_cast<float4*>(out.params) + i * Lp;
+        for (int l = lane; l < Lp; l += 32) {
+            if (l >= L) {
+                dst[l] = make_float4(1.f, 0.f, 0.f, 0.f);
+                s_bnd[l] = 0.f;
+                s_cls[l] = 1;
+                continue;
+            }
+            const LayerConst c = lc[l];
+            const float sigma = q.wlc * sqrtf(q.k_m * c.T32 + 0.5f * c.xi32 * c.xi32);
+            float G = q.grad;
+            if (!mol) {
+                float vdw;
+                if (!abo) {
+                    vdw = q.v1 * c.vdw3_32;
+                } else {
+                    const float vbar = sqrtf(float(8 * KBOLTZ_CGS / PI) * c.T32 * q.invmu);
+                    vdw = q.abo_pre * powf(vbar * 1e-6f, q.vexp);
+                }
+                G = G + c.ne32 * (q.gstark * c.stark6_32) + c.nv32 * vdw;
+            }
+            const float gamma = G * q.wl2c;
+            const double levels = fexp64(-c.beta * q.El, s_math) - fexp64(-c.beta * q.Eu, s_math);  // FP64
+            const float amp = float(q.strength * levels * lay.n_div_U[int64_t(q.sp) * L + l]);
+            const double* row = cn.vals + int64_t(l) * cn.nk;
+            const float acntm = cn.nk == 1 ? float(row[0])
+                                           : float(row[q.ki]) * (1.f - q.t32) + float(row[q.ki + 1]) * q.t32;
+            const float rho = acntm * float(cutoff) / amp;
+            const float dw = inverse_gaussian32(rho, sigma), lw = inverse_lorentz32(rho, gamma);
+            if (dw > dmax) { dmax = dw; dl = l; }
+            if (lw > lmax) { lmax = lw; ll = l; }
+            const float s = 1.f / (sigma * 1.41421356f);
+            const float a = gamma * s;
+            const float scale = s * 0.56418958f * amp;  // 1/sqrt(pi)
+            const bool A = a <= 0.2f;
+            float4 p;
+            p.x = 2.f * sigma * sigma;
+            p.y = a;
+            p.z = A ? a * 0.56418958f * scale : 1.f / (gamma * gamma);
+            p.w = scale;
+            dst[l] = p;
+            // v >= 5 (a <= 0.2) or a + v >= 3.2 (0.2 < a <= 1.4) or any v (a > 1.4), v = x / sqrt(c)
+            s_bnd[l] = (A ? 5.f : (a <= 1.4f ? 3.2f - a : 0.f)) * sqrtf(p.x) * 1.0001f;
+            s_cls[l] = A;
+        }
+        __syncwarp();
+        argmax_reduce(dmax, dl);
+        argmax_reduce(lmax, ll);
+        group_bounds(out, i, s_bnd, s_cls, lane);
+        __syncwarp();  // s_bnd / s_cls are rewritten by the next line
+        if (lane == t) { my_dl = dl; my_ll = ll; }
     }
-    const double lwin = __shfl_sync(0xffffffffu, w, 1);
-    if (lane == 0) store_window(out, i, lwin, w, q.wl, wls, nwl, L);
+    // phase C: the exact FP64 window of each line at its two widest layers, one lane per line
+    if (lane < nl) {
+        const int64_t i = base + lane;
+        const LineConst q = line_const(ln, i);
+        const LineLayer64 rd = line_layer64(q, lay, lc[my_dl], cn, kp_mine, cutoff, my_dl, s_math);
+        const LineLayer64 rl = line_layer64(q, lay, lc[my_ll], cn, kp_mine, cutoff, my_ll, s_math);
+        store_window(out, i, rl.lw, rd.dw, q.wl, wls, nwl, L);
+    }
 }
+
+// Launch geometry of line_prep_mixed_kernel for n lines.
+inline unsigned prep_mixed_blocks(int64_t n) { return unsigned((n + 32 * PREP_WARPS - 1) / (32 * PREP_WARPS)); }
+inline size_t prep_mixed_smem(int Lp) { return size_t(PREP_WARPS) * Lp * (sizeof(float) + sizeof(int)); }
 
 // Candidate lists.  Lines are split by window half-width into tiers (at most 256, 4096, 65536
 // wavelength points, and wider).  Within a tier the lines keep list order, so their centre
@@ -480,12 +539,12 @@ __device__ __forceinline__ double far_lorentz64(const P64& p, double x2) {
     return 0.7978845608028654 * au * (1 + (3 * r2 - 1 + ((r2 - 2) * 15 * r2 + 2) * au2) * au2) * p.scale;
 }
 
-// One CTA per tile of TW = blockDim.x / G wavelengths x all layers.  Thread (j, g) owns
-// wavelength j and the K consecutive (padded) layers g*K .. g*K+K-1.
-template <bool MIXED, int K, int MAXT, int MINB>
-__global__ void __launch_bounds__(MAXT, MINB) line_tile_kernel(TileArgs a) {
+// One tile of TW = blockDim.x / G wavelengths x all layers, computed by one CTA.  Thread (j, g)
+// owns wavelength j and the K consecutive (padded) layers g*K .. g*K+K-1.  `smem` is the
+// dynamic shared memory of the launch (two line-constant buffers, then the LineStage array).
+template <bool MIXED, int K>
+__device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, unsigned char* smem) {
     using P = typename ParamT<MIXED>::type;
-    extern __shared__ __align__(16) unsigned char smem[];
     const int L = a.L, Lp = a.Lp, G = a.G, B = a.stage;
     double* s_alpha = reinterpret_cast<double*>(smem);                          // [TW][Lp+1], at the end
     LineStage* s_ln = reinterpret_cast<LineStage*>(smem + 2 * size_t(a.region));  // [blockDim]
@@ -495,7 +554,7 @@ __global__ void __launch_bounds__(MAXT, MINB) line_tile_kernel(TileArgs a) {
     const int tid = threadIdx.x, nthr = blockDim.x;
     const int TW = nthr / G;
     const int jl = tid % TW, g = tid / TW;
-    const int64_t j0 = int64_t(blockIdx.x) * TW;
+    const int64_t j0 = tile * TW;
     const int64_t jg = j0 + jl;
     const int64_t jlast = min(j0 + TW, a.nwl) - 1;
     const bool live = jg < a.nwl;
@@ -681,6 +740,44 @@ __global__ void __launch_bounds__(MAXT, MINB) line_tile_kernel(TileArgs a) {
     for (int64_t e = tid; e < nj * L; e += nthr) {
         const int j = int(e / L), l = int(e - int64_t(j) * L);
         dst[e] = dst[e] + s_alpha[j * stride + l];
+    }
+}
+
+// One CTA per tile of one spectrum.
+template <bool MIXED, int K, int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB) line_tile_kernel(TileArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    line_tile_body<MIXED, K>(a, blockIdx.x, smem);
+}
+
+// Work queue of (spectrum, tile) items for a batch of spectra on one wavelength grid.  Item k
+// is tile k / nspec of spectrum k % nspec: the queue walks the grid once, visiting every
+// spectrum's tile before moving on, so spectra with few and many lines are interleaved.
+struct TileQueue {
+    const TileArgs* spec;        // [nspec], device
+    int32_t nspec;
+    int64_t nitems;              // nspec * tiles
+    unsigned long long* next;    // item counter, zero before the launch
+};
+
+// Persistent form: a grid sized to the resident CTAs of the GPU takes items from the queue
+// until it is empty.
+template <bool MIXED, int K, int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB) line_tile_queue_kernel(TileQueue q) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ TileArgs s_a;
+    __shared__ long long s_item;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const long long it = (long long)atomicAdd(q.next, 1ull);
+            s_item = it;
+            if (it < q.nitems) s_a = q.spec[it % q.nspec];
+        }
+        __syncthreads();
+        const long long it = s_item;
+        if (it >= q.nitems) break;
+        line_tile_body<MIXED, K>(s_a, it / q.nspec, smem);
+        __syncthreads();  // s_a and s_item are rewritten for the next item
     }
 }
 

@@ -125,4 +125,142 @@ __global__ void __launch_bounds__(256) alpha_init_kernel(double* alpha, const do
     }
 }
 
+// ---------------------------------------------------------------- secondary schemes
+// RadiativeTransfer.jl:77-139 and :147-371 for any atmosphere geometry and scheme: rays along
+// the surface mu grid (planar or spherical), inward rays seeding the outward ones at the bottom,
+// tau by the anchored or the Bezier scheme, intensity by the linear, linear-flux-only or Bezier
+// formal solution, or the exponential-integral flux.  One thread per wavelength walks every ray;
+// the ray geometry (path, ds/dz, layers reached) is computed once on the host.
+constexpr int RTG_LMAX = 128;  // layers per ray
+constexpr int RTG_RMAX = 64;   // rays (inward + outward)
+
+struct RtGenArgs {
+    const double* alpha;     // [nwl][L]
+    const double* S;         // [nwl][L]
+    int32_t L;
+    int64_t nwl;
+    int32_t nrays, n_in, n_mu;
+    const int32_t* ray_n;    // [nrays] layers on the ray
+    const double* ray_fac;   // [nrays][L] tau_ref/alpha_ref * ds/dz, in ray order
+    const double* ray_lt;    // [nrays][L] +-log tau_ref, in ray order
+    const double* ray_path;  // [nrays][L] +-s, in ray order
+    const double* wmu;       // [n_mu] mu weight * mu of the outward rays
+    int32_t tau_scheme;      // 0 anchored, 1 bezier
+    int32_t I_scheme;        // 0 linear, 1 linear_flux_only, 2 bezier, 3 linear_flux_only_expint
+    const MathTables* math;
+    double* flux;            // [nwl] 2 pi sum_mu w mu I_surface
+    double* Isurf;           // [n_mu][nwl] surface intensity of the outward rays, or null
+};
+
+// fritsch_butland_C (RadiativeTransfer.jl:361-371) evaluated for one interval k of n points
+__device__ __forceinline__ double fb_control(const double* x, const double* y, int n, int k) {
+    if (n < 3) return 0.5 * (y[0] + y[1]);  // two points: the reference has no interior slope
+    auto yp = [&](int q) {  // interior slope estimate at point q + 1
+        const double h0 = x[q + 1] - x[q], h1 = x[q + 2] - x[q + 1];
+        const double d0 = (y[q + 1] - y[q]) / h0, d1 = (y[q + 2] - y[q + 1]) / h1;
+        const double al = 1.0 / 3.0 * (1 + h1 / (h1 + h0));
+        return (d0 * d1) / (al * d1 + (1 - al) * d0);
+    };
+    const double A = k < n - 2 ? y[k + 1] + (x[k + 1] - x[k]) * yp(k) / 2
+                               : y[n - 2] - (x[n - 1] - x[n - 2]) * yp(n - 3) / 2;
+    const double B = k == 0 ? y[1] + (x[1] - x[0]) * yp(0) / 2 : y[k] - (x[k + 1] - x[k]) * yp(k - 1) / 2;
+    return (A + B) / 2;
+}
+
+__global__ void __launch_bounds__(128) rt_general_kernel(RtGenArgs a) {
+    const int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= a.nwl) return;
+    const int L = a.L;
+    double tau[RTG_LMAX], col[RTG_LMAX], Sc[RTG_LMAX], I[RTG_LMAX];
+    double seed[RTG_RMAX];  // per ray: bottom intensity (linear) or start value (flux only)
+    for (int r = 0; r < a.nrays; r++) seed[r] = 0.0;
+    double F = 0.0;
+    for (int r = 0; r < a.nrays; r++) {
+        const bool inward = r < a.n_in;
+        const int n = a.ray_n[r];
+        double Iout = 0.0;
+        const double* fac = a.ray_fac + int64_t(r) * L;
+        const double* lt = a.ray_lt + int64_t(r) * L;
+        const double* path = a.ray_path + int64_t(r) * L;
+        if (!(n == 1 && (a.I_scheme == 2 || a.tau_scheme == 1))) {  // :150-154
+            for (int k = 0; k < n; k++) {
+                const int lk = inward ? n - 1 - k : k;  // reversed path for inward rays (:118-121)
+                col[k] = a.alpha[j * L + lk];
+                Sc[k] = a.S[j * L + lk];
+            }
+            if (a.tau_scheme == 0) {  // :244-253
+                double prev = col[0] * fac[0];
+                tau[0] = 0.0;
+                for (int k = 1; k < n; k++) {
+                    const double ib = col[k] * fac[k];
+                    tau[k] = tau[k - 1] + 0.5 * (ib + prev) * (lt[k] - lt[k - 1]);
+                    prev = ib;
+                }
+            } else {  // :263-273
+                double amin = col[0], amax = col[0];
+                for (int k = 1; k < n; k++) { amin = fmin(amin, col[k]); amax = fmax(amax, col[k]); }
+                tau[0] = 1e-5;
+                for (int i = 1; i < n; i++) {
+                    const double C = fmin(fmax(fb_control(path, col, n, i - 1), 0.5 * amin), 2 * amax);
+                    tau[i] = tau[i - 1] + (path[i - 1] - path[i]) / 3 * (col[i] + col[i - 1] + C);
+                }
+            }
+            if (a.I_scheme == 0) {  // :286-298
+                I[n - 1] = seed[r];
+                for (int k = n - 2; k >= 0; k--) {
+                    const double d = tau[k + 1] - tau[k];
+                    const double m = (Sc[k + 1] - Sc[k]) / d;
+                    I[k] = (I[k + 1] - Sc[k] - m * (d + 1)) * exp(-d) + m + Sc[k];
+                }
+                Iout = I[0];
+                if (inward && r + a.n_in < a.nrays) seed[r + a.n_in] = I[0];  // :196-198
+            } else if (a.I_scheme == 2) {  // :333-350 (the bottom value is not used)
+                I[n - 1] = 0.0;
+                for (int k = n - 2; k >= 0; k--) {
+                    const double d = tau[k + 1] - tau[k], e = exp(-d), d2 = d * d;
+                    const double al = (2 + d2 - 2 * d - 2 * e) / d2;
+                    const double be = (2 - (2 + 2 * d + d2) * e) / d2;
+                    const double ga = (2 * d - 4 + (2 * d + 4) * e) / d2;
+                    I[k] = I[k + 1] * e + al * Sc[k] + be * Sc[k + 1] + ga * fb_control(tau, Sc, n, k);
+                }
+                I[0] *= exp(-tau[0]);
+                Iout = I[0];
+                if (inward && r + a.n_in < a.nrays) seed[r + a.n_in] = I[0];
+            } else {
+                double add = 0.0;
+                if (a.I_scheme == 1) {  // :307-324
+                    double next = exp(-tau[0]);
+                    for (int i = 0; i + 1 < n; i++) {
+                        double dt = tau[i + 1] - tau[i];
+                        dt += (dt == 0);
+                        const double m = (Sc[i + 1] - Sc[i]) / dt;
+                        const double cur = next;
+                        next = exp(-tau[i + 1]);
+                        add += (-next * (Sc[i + 1] + m) + cur * (Sc[i] + m));
+                    }
+                } else {  // :379-388
+                    double e2p = 1.0, exp_ = 1.0;
+                    for (int i = 0; i + 1 < n; i++) {
+                        const double m = (Sc[i + 1] - Sc[i]) / (tau[i + 1] - tau[i]);
+                        const double b = Sc[i] - m * tau[i];
+                        const double ex = exp(-tau[i + 1]);
+                        const double e2 = expint2_64(tau[i + 1]);
+                        add += expint_core(tau[i + 1], e2, ex, m, b) - expint_core(tau[i], e2p, exp_, m, b);
+                        e2p = e2;
+                        exp_ = ex;
+                    }
+                }
+                Iout = seed[r] + add;  // += onto a seeded value (:177-180)
+                if (inward && r + a.n_in < a.nrays) seed[r + a.n_in] = Iout * exp(-tau[n - 1]);
+            }
+        }
+        if (!inward) {
+            const int u = r - a.n_in;
+            F += Iout * a.wmu[u];
+            if (a.Isurf) a.Isurf[int64_t(u) * a.nwl + j] = Iout;
+        }
+    }
+    a.flux[j] = 2 * PI * F;
+}
+
 }  // namespace korg

@@ -175,4 +175,105 @@ function radiative_transfer(atm::Korg.PlanarAtmosphere, α::Matrix{Float64}, S::
     F, reshape(F ./ 2π, 1, nwl), [1.0], [1.0]
 end
 
+# ---------------------------------------------------------------------------- differentiable path
+# korg_synth_inputs / korg_synth_grads of include/korg_gb300.h
+struct CSynthInputs
+    layers::CLayers
+    tau_ref::Ptr{Float64}
+    alpha_ref_cntm::Ptr{Float64}
+    nH_I::Ptr{Float64}
+    nHe_I::Ptr{Float64}
+    UH_I::Ptr{Float64}
+    ref_wl::Float64
+    cntm::CCntm
+    hydrogen_lines::Int32
+    use_MHD::Int32
+    hydrogen_window::Float64
+    cutoff_threshold::Float64
+end
+
+struct CSynthGrads
+    T::Ptr{Float64}; ne::Ptr{Float64}; n_eff_vdW::Ptr{Float64}; xi::Ptr{Float64}; n_div_U::Ptr{Float64}
+    nH_I::Ptr{Float64}; nHe_I::Ptr{Float64}; UH_I::Ptr{Float64}; log_gf::Ptr{Float64}
+    cntm_vals::Ptr{Float64}; alpha_ref_cntm::Ptr{Float64}
+end
+
+"""
+    HotPath(fixed inputs of one synthesize call)
+
+Everything `synthesize` computes on the host before the hot path (src/synthesize.jl:159-262)
+that is held fixed while fitting: the wavelengths, both line lists (packed), τ_ref, the
+hydrogen-line layer inputs and the continuum knots.  `hotpath_flux(hp, T, nₑ, n_eff, ξ,
+n_div_U, log_gf, cntm_vals, α_ref_cntm)` is differentiable through `ChainRulesCore.rrule`.
+"""
+struct HotPath
+    wls::Vector{Float64}
+    lines::Tuple
+    lines5::Tuple
+    tau_ref::Vector{Float64}
+    nH_I::Vector{Float64}
+    nHe_I::Vector{Float64}
+    UH_I::Vector{Float64}
+    knots::Vector{Float64}
+    ref_wl::Float64
+    hydrogen_lines::Bool
+    use_MHD::Bool
+    hydrogen_window::Float64
+    cutoff_threshold::Float64
+    precision::Symbol
+end
+
+function _with_inputs(f, hp::HotPath, T, ne, n_eff, xi, n_div_U, log_gf, cntm_vals, aref)
+    L = length(T)
+    lines = (hp.lines[1], collect(Float64, log_gf), hp.lines[3:end]...)
+    GC.@preserve hp lines T ne n_eff xi n_div_U cntm_vals aref begin
+        lay = CLayers(L, size(n_div_U, 2), pointer(T), pointer(ne), pointer(n_eff), pointer(xi), pointer(n_div_U))
+        inp = Ref(CSynthInputs(lay, pointer(hp.tau_ref), pointer(aref), pointer(hp.nH_I), pointer(hp.nHe_I),
+                               pointer(hp.UH_I), hp.ref_wl, CCntm(length(hp.knots), pointer(hp.knots),
+                                                                  pointer(cntm_vals)),
+                               hp.hydrogen_lines, hp.use_MHD, hp.hydrogen_window, hp.cutoff_threshold))
+        f(inp, Ref(_clines(lines)), Ref(_clines(hp.lines5)), lines)
+    end
+end
+
+function hotpath_flux(hp::HotPath, T, ne, n_eff, xi, n_div_U, log_gf, cntm_vals, aref; ctx=default_context())
+    nwl = length(hp.wls)
+    flux = Vector{Float64}(undef, nwl)
+    cntm = Vector{Float64}(undef, nwl)
+    _with_inputs(hp, T, ne, n_eff, xi, n_div_U, log_gf, cntm_vals, aref) do inp, l1, l5, _
+        rc = ccall((:korg_synthesize, LIB), Cint,
+                   (Ptr{Cvoid}, Ref{CSynthInputs}, Ref{CLines}, Ref{CLines}, Ptr{Float64}, Int64, Cint,
+                    Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+                   ctx.ptr, inp, l1, l5, hp.wls, nwl, _prec(hp.precision), flux, cntm, C_NULL, C_NULL)
+        check(ctx, rc)
+    end
+    flux, cntm
+end
+
+using ChainRulesCore
+
+function ChainRulesCore.rrule(::typeof(hotpath_flux), hp::HotPath, T, ne, n_eff, xi, n_div_U, log_gf,
+                              cntm_vals, aref; ctx=default_context())
+    y = hotpath_flux(hp, T, ne, n_eff, xi, n_div_U, log_gf, cntm_vals, aref; ctx=ctx)
+    function hotpath_pullback(ȳ)
+        dF = collect(Float64, unthunk(ȳ[1]) isa AbstractZero ? zeros(length(hp.wls)) : unthunk(ȳ[1]))
+        dC = collect(Float64, unthunk(ȳ[2]) isa AbstractZero ? zeros(length(hp.wls)) : unthunk(ȳ[2]))
+        g = map(similar ∘ (x -> collect(Float64, x)), (T, ne, n_eff, xi, n_div_U, log_gf, cntm_vals, aref))
+        _with_inputs(hp, T, ne, n_eff, xi, n_div_U, log_gf, cntm_vals, aref) do inp, l1, l5, _
+            GC.@preserve g dF dC begin
+                grads = Ref(CSynthGrads(pointer(g[1]), pointer(g[2]), pointer(g[3]), pointer(g[4]), pointer(g[5]),
+                                        C_NULL, C_NULL, C_NULL, pointer(g[6]), pointer(g[7]), pointer(g[8])))
+                rc = ccall((:korg_synthesize_vjp, LIB), Cint,
+                           (Ptr{Cvoid}, Ref{CSynthInputs}, Ref{CLines}, Ref{CLines}, Ptr{Float64}, Int64, Cint,
+                            Ptr{Float64}, Ptr{Float64}, Ref{CSynthGrads}, Cint),
+                           ctx.ptr, inp, l1, l5, hp.wls, length(hp.wls), _prec(hp.precision), dF, dC, grads,
+                           Cint(1))
+                check(ctx, rc)
+            end
+        end
+        (NoTangent(), NoTangent(), g...)
+    end
+    y, hotpath_pullback
+end
+
 end # module

@@ -16,9 +16,12 @@ __all__ = ["Wavelengths", "LineList", "make_line", "filter_linelist", "alpha_500
 
 
 def __getattr__(name):
+    # the API module is imported on first use (it loads the CUDA library binding); importing it
+    # binds the package attribute `synthesize` to the module, whose synthesize() is the function
     if name in ("line_absorption_", "hydrogen_line_absorption_", "radiative_transfer", "synthesize",
                 "prepare_synthesis", "synthesize_prepared", "SynthesisInputs", "SynthesisResult",
-                "ContinuumInterpolant"):
-        from . import synthesize as _s
-        return getattr(_s, name)
+                "ContinuumInterpolant", "synthesize_vjp", "loss_and_gradient", "physical_gradient"):
+        import importlib
+        _s = importlib.import_module(".synthesize", __name__)
+        return _s if name == "synthesize" else getattr(_s, name)
     raise AttributeError(name)

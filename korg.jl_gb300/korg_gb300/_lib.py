@@ -57,6 +57,18 @@ class SynthInputs(C.Structure):
                 ("cutoff_threshold", C.c_double)]
 
 
+class SynthGrads(C.Structure):
+    _fields_ = [("T", _dp), ("ne", _dp), ("n_eff_vdW", _dp), ("xi", _dp), ("n_div_U", _dp), ("nH_I", _dp),
+                ("nHe_I", _dp), ("UH_I", _dp), ("log_gf", _dp), ("cntm_vals", _dp), ("alpha_ref_cntm", _dp)]
+
+
+KORG_VJP_HYDROGEN = 1
+
+
+class BatchItem(C.Structure):
+    _fields_ = [("inp", SynthInputs), ("lines", Lines), ("lines5", Lines), ("flux", _dp), ("cntm", _dp)]
+
+
 class Stats(C.Structure):
     _fields_ = [("line_evals", C.c_int64), ("lines_in_window", C.c_int64), ("ms_ref_lines", C.c_float),
                 ("ms_hydrogen", C.c_float), ("ms_line_prep", C.c_float), ("ms_line_tile", C.c_float),
@@ -102,6 +114,15 @@ def lib():
             L.korg_math_selftest.argtypes = [vp, C.c_int64, _dp, _dp]
             L.korg_line_absorption_noalloc.argtypes = [vp, vp, C.c_int64, C.POINTER(Lines), C.POINTER(Layers),
                                                        C.POINTER(Cntm), C.c_double, C.c_int, vp]
+            L.korg_radiative_transfer_general.argtypes = [vp, _dp, _dp, C.c_int32, C.c_int64, _dp, C.c_int, _dp, _dp,
+                                                          _dp, _dp, C.c_int32, C.c_int, C.c_int, C.c_int, _dp, _dp]
+            L.korg_synthesize_vjp.argtypes = [vp, C.POINTER(SynthInputs), C.POINTER(Lines), C.POINTER(Lines), _dp,
+                                              C.c_int64, C.c_int, _dp, _dp, C.POINTER(SynthGrads), C.c_int]
+            L.korg_synthesize_vjp_dev.argtypes = [vp, C.POINTER(SynthInputs), C.POINTER(Lines), C.POINTER(Lines), vp,
+                                                  C.c_int64, C.c_int, vp, vp, C.POINTER(SynthGrads), C.c_int, vp]
+            L.korg_synthesize_batch_dev.argtypes = [vp, C.c_int32, C.POINTER(BatchItem), vp, C.c_int64, C.c_int, vp]
+            L.korg_set_batch_options.argtypes = [vp, C.c_int, C.c_int, C.c_int64]
+            L.korg_get_tile_config.argtypes = [vp, C.c_int32, C.c_int, _ip, _ip, _ip]
             _lib = L
     return _lib
 
@@ -112,7 +133,9 @@ def exported_symbols():
             "korg_set_stark_tables", "korg_line_absorption", "korg_line_absorption_dev",
             "korg_hydrogen_line_absorption", "korg_hydrogen_lines_dev", "korg_radiative_transfer",
             "korg_radiative_transfer_dev", "korg_synthesize", "korg_synthesize_dev", "korg_probe_flops",
-            "korg_math_selftest", "korg_line_absorption_noalloc"]
+            "korg_math_selftest", "korg_line_absorption_noalloc", "korg_synthesize_batch_dev",
+            "korg_set_batch_options", "korg_get_tile_config", "korg_synthesize_vjp", "korg_synthesize_vjp_dev",
+            "korg_radiative_transfer_general"]
 
 
 def _p(a, kind=_dp):

@@ -44,6 +44,18 @@ class CubicSpline:
         return float(out[0]) if scalar else out
 
 
+    def derivative(self, x):
+        """d/dx of the spline (zero outside the knots, where the value is clamped)."""
+        x = np.atleast_1d(np.asarray(x, dtype=np.float64))
+        t, u, h, z = self.t, self.u, self.h, self.z
+        xc = np.clip(x, t[0], t[-1])
+        i = np.clip(np.searchsorted(t, xc, side="right") - 1, 0, len(t) - 2)
+        h1 = h[i + 1]
+        d = (-z[i] * (t[i + 1] - xc) ** 2 / (2 * h1) + z[i + 1] * (xc - t[i]) ** 2 / (2 * h1)
+             + (u[i + 1] / h1 - z[i + 1] * h1 / 6) - (u[i] / h1 - z[i] * h1 / 6))
+        return np.where((x < t[0]) | (x > t[-1]), 0.0, d)
+
+
 def _solve_tridiagonal(dl, d, du, rhs):
     """Thomas algorithm for the (n+1)x(n+1) system of CubicSplines.jl:58-61."""
     n = len(d)

@@ -40,6 +40,9 @@ class Species(tuple):
     def __new__(cls, atoms, charge=0):
         return super().__new__(cls, (tuple(sorted(atoms)), int(charge)))
 
+    def __reduce__(self):  # pickles as Species(atoms, charge)
+        return (Species, (self[0], self[1]))
+
     @property
     def atoms(self):
         return self[0]

@@ -60,68 +60,75 @@ def _transU(m, T):
 
 def chemical_equilibrium(T, n_tot, A_X, n_iter=200):
     """Stand-in chemical equilibrium for arrays of layer temperatures and total particle
-    densities.  Returns (n_e, {Species: array of number densities})."""
+    densities.  Returns (n_e, {Species: array of number densities}).
+
+    Saha ionisation (neutral, singly and doubly ionised) of every element with ionisation
+    energies, plus the diatomic dissociation equilibria of DIATOMICS, solved by fixed-point
+    iteration on n_e (outer) and the neutral atom densities (inner), all elements and layers
+    at once."""
     T = np.asarray(T, dtype=np.float64)
     n_tot = np.asarray(n_tot, dtype=np.float64)
     pf = default_partition_funcs()
     chi = ionization_energies()
     lnT = np.log(T)
     Zs = [z for z in range(1, 93) if z in chi]
+    zi = {z: k for k, z in enumerate(Zs)}
     abund = 10.0 ** (np.asarray(A_X) - 12)
     abund = abund / abund.sum()
-    U = {}
-    for z in Zs:
-        for q in range(3):
-            s = Species([z], q)
-            if s in pf:
-                U[s] = pf[s](np.clip(lnT, pf[s].t[0], pf[s].t[-1]))
-            else:
-                U[s] = np.ones_like(T)
+
+    def U(z, q):
+        s = Species([z], q)
+        return pf[s](np.clip(lnT, pf[s].t[0], pf[s].t[-1])) if s in pf else np.ones_like(T)
+
+    U0 = np.array([U(z, 0) for z in Zs])
+    U1 = np.array([U(z, 1) for z in Zs])
+    U2 = np.array([U(z, 2) for z in Zs])
+    chi1 = np.array([chi[z][0] for z in Zs])[:, None]
+    chi2 = np.array([chi[z][1] for z in Zs])[:, None]
+    third = np.array([z != 1 and chi[z][1] >= 0 for z in Zs])[:, None]
+    A = np.array([abund[z - 1] for z in Zs])[:, None]
     tU = _transU(electron_mass_cgs, T)
     kT = kboltz_eV * T
-    mols = []
+    mols, ia, ib, Ks = [], [], [], []
     for name, D0 in DIATOMICS:
         sp = parse_species(name)
         a, b = sp.atoms
         mu = atomic_masses[a - 1] * atomic_masses[b - 1] / (atomic_masses[a - 1] + atomic_masses[b - 1])
         Umol = pf[sp](lnT) if sp in pf else np.ones_like(T)
-        Ua, Ub = U[Species([a], 0)], U[Species([b], 0)]
-        K = _transU(mu, T) * Ua * Ub / Umol * np.exp(-D0 / kT)  # n_a n_b / n_ab
-        mols.append((sp, a, b, K))
+        K = _transU(mu, T) * U0[zi[a]] * U0[zi[b]] / Umol * np.exp(-D0 / kT)  # n_a n_b / n_ab
+        mols.append(sp)
+        ia.append(zi[a])
+        ib.append(zi[b])
+        Ks.append(K)
+    ia, ib, Ks = np.array(ia), np.array(ib), np.array(Ks)
+    homo = ia == ib
+    saha1 = (U1 / U0) * tU * np.exp(-chi1 / kT)
+    saha2 = np.where(third, (U2 / np.where(third, U1, 1.0)) * tU * np.exp(-np.where(third, chi2, 0.0) / kT), 0.0)
     ne = 1e-4 * n_tot * np.clip(T / 5000.0, 0.5, 3) ** 4
     for it in range(n_iter):
-        wII = {z: 2.0 / ne * (U[Species([z], 1)] / U[Species([z], 0)]) * tU * np.exp(-chi[z][0] / kT) for z in Zs}
-        wIII = {}
-        for z in Zs:
-            if z == 1 or chi[z][1] < 0:
-                wIII[z] = np.zeros_like(T)
-            else:
-                wIII[z] = wII[z] * 2.0 / ne * (U[Species([z], 2)] / U[Species([z], 1)]) * tU * np.exp(-chi[z][1] / kT)
-        n_nuc = n_tot - ne
-        N = {z: abund[z - 1] * n_nuc for z in Zs}
-        n0 = {z: N[z] / (1 + wII[z] + wIII[z]) for z in Zs}
+        wII = 2.0 / ne * saha1
+        wIII = wII * 2.0 / ne * saha2
+        N = A * (n_tot - ne)
+        base = 1 + wII + wIII
+        n0 = N / base
         for _ in range(30):
-            denom = {z: 1 + wII[z] + wIII[z] for z in Zs}
-            for sp, a, b, K in mols:
-                if a == b:
-                    denom[a] = denom[a] + 2 * n0[a] / K
-                else:
-                    denom[a] = denom[a] + n0[b] / K
-                    denom[b] = denom[b] + n0[a] / K
-            new = {z: N[z] / denom[z] for z in Zs}
-            n0 = {z: np.sqrt(n0[z] * new[z]) for z in Zs}
-        ne_new = sum(n0[z] * (wII[z] + 2 * wIII[z]) for z in Zs)
-        ne_new = np.maximum(ne_new, 1e-10 * n_tot)
+            denom = base.copy()
+            np.add.at(denom, ia[homo], 2 * n0[ia[homo]] / Ks[homo])
+            np.add.at(denom, ia[~homo], n0[ib[~homo]] / Ks[~homo])
+            np.add.at(denom, ib[~homo], n0[ia[~homo]] / Ks[~homo])
+            n0 = np.sqrt(n0 * (N / denom))
+        ne_new = np.maximum(np.sum(n0 * (wII + 2 * wIII), axis=0), 1e-10 * n_tot)
         if np.max(np.abs(ne_new / ne - 1)) < 1e-10:
             ne = ne_new
             break
         ne = np.sqrt(ne * ne_new)
     nd = {}
     for z in Zs:
-        nd[Species([z], 0)] = n0[z]
-        nd[Species([z], 1)] = n0[z] * wII[z]
-        nd[Species([z], 2)] = n0[z] * wIII[z]
-    for sp, a, b, K in mols:
+        k = zi[z]
+        nd[Species([z], 0)] = n0[k]
+        nd[Species([z], 1)] = n0[k] * wII[k]
+        nd[Species([z], 2)] = n0[k] * wIII[k]
+    for sp, a, b, K in zip(mols, ia, ib, Ks):
         nd[sp] = n0[a] * n0[b] / K
     return ne, nd
 

@@ -137,19 +137,43 @@ def hydrogen_line_absorption_(alphas, wls, T, ne, nH_I, nHe_I, UH_I, xi, window_
                                                     float(window_size), int(bool(use_MHD)), _prec(precision)))
 
 
+def generate_mu_grid(mu_points):
+    """RadiativeTransfer.jl:13-30: Gauss-Legendre on [0, 1] for an integer, trapezoid weights for
+    an explicit sorted grid in [0, 1]."""
+    if np.ndim(mu_points) == 0:
+        mu, w = np.polynomial.legendre.leggauss(int(mu_points))
+        return mu / 2 + 0.5, w / 2
+    mu = np.asarray(mu_points, np.float64)
+    if len(mu) == 1:
+        return mu, np.array([1.0])
+    if np.any(np.diff(mu) < 0) or mu[0] < 0 or mu[-1] > 1:
+        raise ValueError("mu_grid must be sorted and bounded between 0 and 1")
+    d = np.diff(mu)
+    return mu, 0.5 * np.concatenate([[d[0]], d[:-1] + d[1:], [d[-1]]])
+
+
+_TAU = {"anchored": 0, "bezier": 1}
+_ISCHEME = {"linear": 0, "linear_flux_only": 1, "bezier": 2}
+
+
 def radiative_transfer(atm, alpha, S, mu_points, alpha_ref=None, tau_ref=None, tau_scheme="anchored",
-                       I_scheme="linear_flux_only", ctx=None):
-    """``radiative_transfer(atm::PlanarAtmosphere, alpha, S, mu_points; alpha_ref, ...)`` with
-    the default schemes.  Returns (F, I, mu_grid, mu_weights) where I is the surface intensity
-    of the single exponential-integral ray (RadiativeTransfer.jl:81-84, 135-138)."""
-    if tau_scheme not in ("anchored", "bezier"):
+                       I_scheme=None, include_inward_rays=False, spherical=None, spatial_coord=None, R=None,
+                       ctx=None):
+    """``RadiativeTransfer.radiative_transfer(atm, alpha, S, mu_points; alpha_ref, tau_ref,
+    tau_scheme, I_scheme)`` (RadiativeTransfer.jl:62-139).  ``atm`` supplies tau_ref and the
+    heights (``atm.z``); ``spherical=True`` with radius ``R`` makes it a shell atmosphere
+    (radii R + z, default I_scheme "linear" and the photosphere correction of :73).  Returns
+    (F, I_surface (n_mu x nwl), mu_grid, mu_weights).  The planar default (anchored tau,
+    linear_flux_only) is the exponential-integral flux on one ray (:81-84); every other
+    combination runs korg_radiative_transfer_general."""
+    if tau_scheme not in _TAU:
         raise ValueError('tau_scheme must be one of "anchored" or "bezier"')
-    if I_scheme not in ("linear", "linear_flux_only", "bezier"):
+    spherical = bool(R is not None) if spherical is None else spherical
+    I_scheme = I_scheme or ("linear" if spherical else "linear_flux_only")
+    if I_scheme not in _ISCHEME:
         raise ValueError('I_scheme must be one of "linear", "bezier", or "linear_flux_only"')
-    if not (tau_scheme == "anchored" and I_scheme == "linear_flux_only"):
-        raise NotImplementedError("the GPU path implements the default planar scheme "
-                                  "(anchored tau, linear_flux_only -> exponential-integral flux)")
     tau_ref = atm.tau_ref if tau_ref is None else tau_ref
+    tau_ref = np.asarray(tau_ref, np.float64)
     L = len(tau_ref)
     a = np.asarray(alpha)
     nwl = a.size // L
@@ -158,10 +182,25 @@ def radiative_transfer(atm, alpha, S, mu_points, alpha_ref=None, tau_ref=None, t
     ctx = ctx or _lib.default_context()
     keep = _lib.Keep()
     F = np.empty(nwl)
-    ctx.check(ctx.lib.korg_radiative_transfer(ctx.h, _lib._p(abuf), _lib._p(sbuf), L, nwl, _lib._p(keep.f64(tau_ref)),
-                                              _lib._p(keep.f64(alpha_ref)), _lib._p(F)))
-    I = F / (2 * np.pi)
-    return F, I.reshape(1, nwl), np.array([1.0]), np.array([1.0])
+    if I_scheme == "linear_flux_only" and tau_scheme == "anchored" and not spherical:
+        ctx.check(ctx.lib.korg_radiative_transfer(ctx.h, _lib._p(abuf), _lib._p(sbuf), L, nwl,
+                                                  _lib._p(keep.f64(tau_ref)), _lib._p(keep.f64(alpha_ref)),
+                                                  _lib._p(F)))
+        return F, (F / (2 * np.pi)).reshape(1, nwl), np.array([1.0]), np.array([1.0])
+    mu, w = generate_mu_grid(mu_points)
+    if spatial_coord is None:
+        z = np.asarray(atm.z, np.float64)
+        spatial_coord = (R + z) if spherical else z
+    spatial_coord = keep.f64(spatial_coord)
+    Isurf = np.empty((len(mu), nwl))
+    ctx.check(ctx.lib.korg_radiative_transfer_general(
+        ctx.h, _lib._p(abuf), _lib._p(sbuf), L, nwl, _lib._p(spatial_coord), int(spherical),
+        _lib._p(keep.f64(tau_ref)), _lib._p(keep.f64(alpha_ref)), _lib._p(keep.f64(mu)), _lib._p(keep.f64(w)),
+        len(mu), int(bool(include_inward_rays)), _TAU[tau_scheme], _ISCHEME[I_scheme], _lib._p(F),
+        _lib._p(Isurf)))
+    if spherical and R is not None:
+        F = F * (spatial_coord[0] ** 2 / R ** 2)  # photosphere correction (:73)
+    return F, Isurf, mu, w
 
 
 # ---------------------------------------------------------------------------------- synthesize
@@ -318,3 +357,75 @@ def synthesize(atm, linelist, A_X, wavelengths, precision="mixed", return_alpha=
     """``synthesize(atm, linelist, A_X, wavelengths; kwargs...)`` (src/synthesize.jl:138-324)."""
     inp = prepare_synthesis(atm, linelist, A_X, wavelengths, **kwargs)
     return synthesize_prepared(inp, precision=precision, return_alpha=return_alpha, ctx=ctx)
+
+
+# ---------------------------------------------------------------------------------- reverse mode
+
+GRAD_FIELDS = ("T", "ne", "n_eff_vdW", "xi", "n_div_U", "nH_I", "nHe_I", "UH_I", "log_gf", "cntm_vals",
+               "alpha_ref_cntm")
+
+
+def synthesize_vjp(inp: SynthesisInputs, dflux, dcntm=None, precision="fp64", hydrogen=True, wanted=GRAD_FIELDS,
+                   ctx=None):
+    """Vector-Jacobian product of :func:`synthesize_prepared` (korg_synthesize_vjp): the
+    gradient of sum(dflux * flux + dcntm * cntm) with respect to the hot-path inputs, as a dict
+    keyed by GRAD_FIELDS (shapes: [L], n_div_U [S, L], log_gf [n lines], cntm_vals [L, nk])."""
+    ctx = ctx or _lib.default_context()
+    if inp.hydrogen_lines:
+        ctx.ensure_stark()
+    keep = _lib.Keep()
+    s = inp.struct(keep)
+    lines = _lib.lines_struct(inp.linelist, keep)
+    lines5 = _lib.lines_struct(inp.linelist5, keep)
+    L, nwl = len(inp.T), len(inp.wls)
+    shapes = {"n_div_U": inp.n_div_U.shape, "log_gf": (len(inp.linelist),), "cntm_vals": inp.cntm_vals.shape}
+    out = {k: np.zeros(shapes.get(k, (L,))) for k in wanted}
+    g = _lib.SynthGrads(*[_lib._p(out[k]) if k in out else None for k in GRAD_FIELDS])
+    df = None if dflux is None else keep.f64(dflux)
+    dc = None if dcntm is None else keep.f64(dcntm)
+    w = keep.f64(inp.wls.all_wls)
+    ctx.check(ctx.lib.korg_synthesize_vjp(ctx.h, C.byref(s), C.byref(lines), C.byref(lines5), _lib._p(w), nwl,
+                                          _prec(precision), _lib._p(df), _lib._p(dc), C.byref(g),
+                                          _lib.KORG_VJP_HYDROGEN if hydrogen else 0))
+    return out
+
+
+def rectified_loss(flux, cntm, obs):
+    """loss = sum((flux/cntm - obs)^2) and its cotangents (dL/dflux, dL/dcntm)."""
+    r = flux / cntm - obs
+    return float(np.sum(r * r)), 2 * r / cntm, -2 * r * flux / cntm ** 2
+
+
+def loss_and_gradient(inp: SynthesisInputs, obs, precision="fp64", hydrogen=True, ctx=None):
+    """Rectified-flux least squares against ``obs`` and its gradient with respect to the
+    hot-path inputs (a forward synthesis, then the reverse mode)."""
+    res = synthesize_prepared(inp, precision=precision, ctx=ctx)
+    loss, dF, dC = rectified_loss(res.flux, res.cntm, obs)
+    return loss, synthesize_vjp(inp, dF, dC, precision=precision, hydrogen=hydrogen, ctx=ctx)
+
+
+def physical_gradient(inp: SynthesisInputs, g, vmic_scalar=True):
+    """Chain rule from the hot-path inputs to the quantities a fit varies, holding the continuum
+    opacity fixed: layer temperatures (through n/U(T) and U_HI(T) as well), electron density,
+    number densities per species (through n/U, n_eff_vdW and the hydrogen-line inputs),
+    microturbulence (km/s) and log gf per line."""
+    pf = default_partition_funcs()
+    T = inp.T
+    lnT = np.log(T)
+    dT = g["T"].copy()
+    dn = {}
+    for k, sp in enumerate(inp.linelist.species):
+        U = pf[sp](lnT)
+        dU = pf[sp].derivative(lnT) / T
+        n = inp.n_div_U[k] * U
+        dn[sp] = dn.get(sp, 0.0) + g["n_div_U"][k] / U
+        dT += -g["n_div_U"][k] * n * dU / U ** 2
+    H1, He1, H2 = parse_species("H I"), parse_species("He I"), parse_species("H2")
+    dn[H1] = dn.get(H1, 0.0) + g["n_eff_vdW"] + g.get("nH_I", 0.0)
+    dn[He1] = dn.get(He1, 0.0) + C_HE * g["n_eff_vdW"] + g.get("nHe_I", 0.0)
+    dn[H2] = dn.get(H2, 0.0) + C_H2 * g["n_eff_vdW"]
+    if "UH_I" in g:
+        dT += g["UH_I"] * pf[H1].derivative(lnT) / T
+    dvmic = g["xi"] * 1e5
+    return {"T": dT, "ne": g["ne"], "n": dn, "vmic": float(np.sum(dvmic)) if vmic_scalar else dvmic,
+            "log_gf": g["log_gf"]}

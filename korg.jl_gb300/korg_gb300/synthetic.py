@@ -79,6 +79,36 @@ def config2(seed=0, n_atomic=50_000, n_mol=20_000):
                     (15000, 17000, 0.005), ll)
 
 
+def config3(seed=0, n_spectra=256, n_list=500_000, n_min=20_000, n_max=200_000, L=56,
+            wavelengths=(15000, 17000, 0.005)):
+    """Batched persistent launch: n_spectra atmospheres with Teff ~ U(3500, 7000) K,
+    logg ~ U(1, 5), [M/H] ~ U(-2.5, 0.5), each with its own pruned subset of n ~ U(n_min, n_max)
+    lines of one n_list-line atomic + molecular list (5:2) over the wavelength range
+    (15000-17000 A on the 0.005 A grid by default).
+
+    Each spectrum keeps a seeded random subset of n lines.  (A strength cut such as
+    prune_linelist's keeps a subset whose size varies per atmosphere; keeping the n strongest
+    of this synthetic list, whose log gf are uniform up to 0, would give cool dwarfs windows
+    spanning most of the grid for every line, which pruned real line lists do not have.)"""
+    rng = np.random.default_rng(seed)
+    na = n_list * 5 // 7
+    lo, hi = float(wavelengths[0]), float(wavelengths[1])
+    a = synthetic_linelist(na, lo, hi, seed=seed)
+    m = synthetic_linelist(n_list - na, lo, hi, seed=seed + 1, species=["CO", "OH", "CN"],
+                           loggf=(-8.0, -2.0), E_lower=(0.0, 3.0), molecular=True)
+    master = a.concat(m).sorted()
+    out = []
+    for k in range(n_spectra):
+        Teff = float(rng.uniform(3500, 7000))
+        logg = float(rng.uniform(1, 5))
+        m_H = float(rng.uniform(-2.5, 0.5))
+        n = int(rng.integers(n_min, n_max + 1))
+        keep = np.sort(rng.choice(len(master), size=min(n, len(master)), replace=False))
+        out.append(Workload(f"cfg3[{k}]: Teff {Teff:.0f} logg {logg:.2f} [M/H] {m_H:+.2f}, {n} lines", Teff, logg,
+                            m_H, L, wavelengths, master.subset(keep)))
+    return out
+
+
 def config4(seed=0, n_lines=1_000_000):
     """80 layers, Teff 3500, logg 1.0; 1M lines (40% atomic, 60% TiO/CO/OH/CN) over 3000-10000 A
     on a 0.01 A grid."""
@@ -88,6 +118,24 @@ def config4(seed=0, n_lines=1_000_000):
                            loggf=(-9.0, -1.0), E_lower=(0.0, 4.0), molecular=True)
     ll = a.concat(m).sorted()
     return Workload("cfg4: 80 layers, 1M lines, 3000-10000 A @ 0.01 A", 3500.0, 1.0, 0.0, 80, (3000, 10000), ll)
+
+
+def abundance_variants(inp, n_variants=16, seed=0, spread=0.3):
+    """n_variants copies of prepared inputs whose metal number densities are scaled by
+    10^U(-spread, spread) dex per species (the batch of abundance variants of one atmosphere).
+    Only the line-strength rows n/U change; the atmosphere, continuum and H lines are shared."""
+    import copy
+    from .species import parse_species
+    rng = np.random.default_rng(seed)
+    H = {parse_species("H I"), parse_species("H II"), parse_species("He I"), parse_species("He II"),
+         parse_species("H2")}
+    out = []
+    for v in range(n_variants):
+        c = copy.copy(inp)
+        scale = np.array([1.0 if s in H else 10.0 ** rng.uniform(-spread, spread) for s in inp.linelist.species])
+        c.n_div_U = np.ascontiguousarray(inp.n_div_U * scale[:, None])
+        out.append(c)
+    return out
 
 
 def prepare(work: Workload, **kwargs):

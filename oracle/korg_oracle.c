@@ -855,7 +855,9 @@ int ko_rt_general(const double *alpha, const double *S, int32_t L, int64_t nwl,
                 if (I_scheme == 0) I_linear(Ilay, tau, Scol, n);
                 else I_bezier(Ilay, tau, Scol, n);
                 *Iout = Ilay[0];
-                if (inward) Ibot[(size_t)(r + n_in) * nwl + j] = Ilay[n - 1];
+                /* the inward ray's intensity where it reaches its deepest layer (k = 0 on the
+                   reversed path) seeds outward ray r + n_in at the bottom (:196-198) */
+                if (inward) Ibot[(size_t)(r + n_in) * nwl + j] = Ilay[0];
             } else {
                 double add = I_scheme == 1 ? I_linear_flux_only(tau, Scol, n)
                                            : column_flux_expint(acol, Scol, n, fac, lt, tau, Ilay);

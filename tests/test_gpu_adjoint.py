@@ -1,0 +1,153 @@
+"""Reverse mode (korg_synthesize_vjp) against central finite differences.
+
+Loss: sum of squared rectified-flux residuals against a perturbed synthetic "observation".
+The plain FP64 gradient is checked against central differences of the GPU FP64 forward (many
+parameters) and of the FP64 oracle (a few, pinning the reference restatement); the mixed-precision
+gradient against the FP64 gradient.
+"""
+import copy
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+NT = os.cpu_count() or 1
+
+
+@pytest.fixture(scope="module")
+def ctx(gpu_lib):
+    c = gpu_lib.Context(0)
+    c.ensure_stark()
+    yield c
+    c.close()
+
+
+def _case(n_lines=600, wl=(5000.0, 5030.0), seed=7):
+    from korg_gb300 import synthetic
+    w = synthetic.config0(seed=seed, n_lines=n_lines)
+    w.wavelengths = wl
+    w.linelist = synthetic.synthetic_linelist(n_lines, wl[0] + 1, wl[1] - 1, seed=seed)
+    return synthetic.prepare(w)
+
+
+def _obs(inp, ctx):
+    """A seeded perturbed synthetic observation: log gf shifted by N(0, 0.1) dex."""
+    from korg_gb300.synthesize import synthesize_prepared
+    rng = np.random.default_rng(1)
+    o = copy.copy(inp)
+    o.linelist = copy.copy(inp.linelist)
+    o.linelist.log_gf = inp.linelist.log_gf + rng.normal(0, 0.1, len(inp.linelist))
+    r = synthesize_prepared(o, precision="fp64", ctx=ctx)
+    return r.flux / r.cntm
+
+
+def _loss(inp, obs, ctx, precision="fp64"):
+    from korg_gb300.synthesize import rectified_loss, synthesize_prepared
+    r = synthesize_prepared(inp, precision=precision, ctx=ctx)
+    return rectified_loss(r.flux, r.cntm, obs)[0]
+
+
+def _perturbed(inp, field, idx, delta):
+    c = copy.copy(inp)
+    if field == "log_gf":
+        c.linelist = copy.copy(inp.linelist)
+        a = inp.linelist.log_gf.copy()
+        a[idx] += delta
+        c.linelist.log_gf = a
+    else:
+        a = getattr(inp, field).copy()
+        a[idx] += delta
+        setattr(c, field, a)
+    return c
+
+
+def _fd(inp, obs, ctx, field, idx, rel=1e-6, loss=None):
+    loss = loss or (lambda x: _loss(x, obs, ctx))
+    v = (inp.linelist.log_gf if field == "log_gf" else getattr(inp, field))[idx]
+    h = rel * max(abs(v), 1e-300) if field != "log_gf" else 1e-6
+    return (loss(_perturbed(inp, field, idx, h)) - loss(_perturbed(inp, field, idx, -h))) / (2 * h)
+
+
+def _strong_lines(inp, k=4):
+    return list(np.argsort(-(inp.linelist.log_gf - 0.5 * inp.linelist.E_lower))[:k])
+
+
+PARAMS = [("T", 5), ("T", 25), ("T", 40), ("ne", 20), ("ne", 45), ("n_eff_vdW", 30), ("xi", 10), ("xi", 35),
+          ("n_div_U", (0, 30)), ("n_div_U", (1, 12)), ("nH_I", 38), ("UH_I", 38), ("alpha_ref_cntm", 30),
+          ("cntm_vals", (20, 3))]
+
+
+def test_vjp_fp64_matches_central_differences(ctx):
+    from korg_gb300.synthesize import loss_and_gradient
+    inp = _case()
+    obs = _obs(inp, ctx)
+    loss, g = loss_and_gradient(inp, obs, precision="fp64", ctx=ctx)
+    assert loss > 0
+    checks = PARAMS + [("log_gf", i) for i in _strong_lines(inp)]
+    for field, idx in checks:
+        fd = _fd(inp, obs, ctx, field, idx)
+        ad = g[field][idx]
+        scale = max(abs(fd), 1e-12 * np.max(np.abs(g[field])))
+        assert abs(ad - fd) <= 1e-4 * scale + 1e-7 * np.max(np.abs(g[field])), (field, idx, ad, fd)
+
+
+def test_vjp_mixed_close_to_fp64(ctx):
+    from korg_gb300.synthesize import loss_and_gradient
+    inp = _case(n_lines=1500, wl=(5000.0, 5060.0), seed=11)
+    obs = _obs(inp, ctx)
+    _, g64 = loss_and_gradient(inp, obs, precision="fp64", ctx=ctx)
+    _, g32 = loss_and_gradient(inp, obs, precision="mixed", ctx=ctx)
+    for k in ("T", "ne", "n_eff_vdW", "xi", "n_div_U", "log_gf", "cntm_vals", "alpha_ref_cntm"):
+        a, b = g32[k], g64[k]
+        err = np.max(np.abs(a - b)) / np.max(np.abs(b))
+        assert err <= 2e-3, (k, err)
+
+
+def test_vjp_without_hydrogen_holds_hydrogen_fixed(ctx):
+    from korg_gb300.synthesize import rectified_loss, synthesize_prepared, synthesize_vjp
+    inp = _case()
+    obs = _obs(inp, ctx)
+    r = synthesize_prepared(inp, precision="fp64", ctx=ctx)
+    _, dF, dC = rectified_loss(r.flux, r.cntm, obs)
+    g = synthesize_vjp(inp, dF, dC, precision="fp64", hydrogen=False, ctx=ctx)
+    assert np.all(g["nH_I"] == 0) and np.all(g["UH_I"] == 0)
+    gh = synthesize_vjp(inp, dF, dC, precision="fp64", hydrogen=True, ctx=ctx)
+    np.testing.assert_array_equal(g["log_gf"], gh["log_gf"])  # lines do not see the hydrogen part
+
+
+def test_vjp_pinned_to_oracle_differences(ctx, oracle_lib):
+    """Central differences of the FP64 oracle (the CPU restatement of the reference) agree with
+    the GPU reverse mode."""
+    from korg_gb300.data import stark_profiles
+    from korg_gb300.synthesize import loss_and_gradient, rectified_loss
+    inp = _case(n_lines=250, wl=(5000.0, 5010.0), seed=3)
+    obs = _obs(inp, ctx)
+    _, g = loss_and_gradient(inp, obs, precision="fp64", ctx=ctx)
+    st = stark_profiles()
+
+    def oracle_loss(x):
+        f, c, _, _, _ = oracle_lib.synthesize(x, x.linelist, x.linelist5, st, x.wls.all_wls, nthreads=NT)
+        return rectified_loss(f, c, obs)[0]
+
+    for field, idx in [("T", 30), ("ne", 30), ("xi", 30), ("log_gf", _strong_lines(inp, 1)[0])]:
+        fd = _fd(inp, obs, ctx, field, idx, loss=oracle_loss)
+        assert abs(g[field][idx] - fd) <= 1e-4 * abs(fd) + 1e-8 * np.max(np.abs(g[field])), (field, g[field][idx], fd)
+
+
+def test_torch_autograd_matches_vjp(ctx):
+    torch = pytest.importorskip("torch")
+    from korg_gb300.autograd import Synthesis
+    from korg_gb300.synthesize import loss_and_gradient
+    inp = _case(n_lines=400, wl=(5000.0, 5020.0), seed=5)
+    obs = _obs(inp, ctx)
+    _, g = loss_and_gradient(inp, obs, precision="fp64", ctx=ctx)
+    synth = Synthesis(inp, precision="fp64", ctx=ctx)
+    x = {k: v.clone().requires_grad_(True) for k, v in synth.initial().items()}
+    flux, cntm = synth(**x)
+    o = torch.as_tensor(obs, device=flux.device)
+    loss = torch.sum((flux / cntm - o) ** 2)
+    loss.backward()
+    for k in ("T", "ne", "n_eff_vdW", "xi", "n_div_U", "log_gf", "cntm_vals", "alpha_ref_cntm"):
+        np.testing.assert_allclose(x[k].grad.cpu().numpy(), g[k], rtol=1e-9, atol=1e-12 * np.max(np.abs(g[k])))

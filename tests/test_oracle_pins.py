@@ -121,3 +121,25 @@ def test_line_absorption_threads_agree(oracle_lib):
                                    inp.n_div_U, inp.cntm_knots, inp.cntm_vals, nthreads=nt)
         outs.append(a)
     np.testing.assert_allclose(outs[0], outs[1], rtol=1e-13, atol=0)
+
+
+def test_rt_spherical_limits(oracle_lib):
+    """A shell atmosphere of very large radius transfers like the plane-parallel one, and seeding
+    the outward rays from inward rays changes the flux only slightly (RadiativeTransfer.jl:196:
+    'the effect is immeasurable')."""
+    from korg_gb300 import synthetic
+    inp = synthetic.prepare(synthetic.config0(n_lines=20))
+    L = len(inp.T)
+    wl = inp.wls.all_wls[::2000]
+    alpha = np.ascontiguousarray(np.interp(wl, inp.cntm_knots, inp.cntm_vals[0])[:, None] *
+                                 (inp.cntm_vals[:, 0] / inp.cntm_vals[0, 0])[None, :])
+    S = np.array([[oracle_lib.blackbody(T, w) for T in inp.T] for w in wl])
+    mu, wts = np.polynomial.legendre.leggauss(10)
+    mu, wts = mu / 2 + 0.5, wts / 2
+    z = np.linspace(0, -1e8, L)
+    Fp = oracle_lib.rt_general(alpha, S, z, False, inp.tau_ref, inp.alpha_ref_cntm, mu, wts, False, 0, 0)
+    Fs = oracle_lib.rt_general(alpha, S, 1e16 + z, True, inp.tau_ref, inp.alpha_ref_cntm, mu, wts, False, 0, 0)
+    np.testing.assert_allclose(Fs, Fp, rtol=1e-6)
+    F1 = oracle_lib.rt_general(alpha, S, 7e10 + z, True, inp.tau_ref, inp.alpha_ref_cntm, mu, wts, False, 0, 0)
+    F2 = oracle_lib.rt_general(alpha, S, 7e10 + z, True, inp.tau_ref, inp.alpha_ref_cntm, mu, wts, True, 0, 0)
+    np.testing.assert_allclose(F2, F1, rtol=1e-3)
