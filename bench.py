@@ -10,6 +10,17 @@ grid (3000-10000 A at 0.01 A), mixed precision, inputs resident in HBM.  Prints 
 --impl reference times the FP64 CPU restatement of the reference (the oracle, all host cores)
 on a bounded sample of the same workload.
 
+    python bench.py --workload adjoint
+
+times the reverse mode on the adjoint configuration (72 layers, Teff 4500 K, logg 2.5,
+[M/H] -0.5, 50k atomic + 20k CO/OH/CN lines, 15000-17000 A at 0.005 A): one step = forward
+synthesis + rectified-flux loss + korg_synthesize_vjp_dev, against the forward alone.
+
+    python bench.py --workload variants
+
+times the large cool-star stress case: 80 layers, Teff 3500 K, logg 1.0, 1,000,000 lines (40%
+atomic, 60% TiO/CO/OH/CN), 3000-10000 A at 0.01 A, as one batch of 16 abundance variants.
+
     python bench.py --workload batch [--spectra 256]
 
 times the batched form instead: 256 atmospheres (Teff 3500-7000 K, logg 1-5, [M/H] -2.5..0.5),
@@ -48,7 +59,8 @@ def parse():
                     help="wavelength range in A (the full workload is 3000-10000)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--workload", default="synth", choices=["synth", "batch"])
+    ap.add_argument("--workload", default="synth", choices=["synth", "batch", "adjoint", "variants"])
+    ap.add_argument("--tile", default=None, help="force the line tile shape: tw,stage,split (e.g. 64,32,1)")
     ap.add_argument("--spectra", type=int, default=256, help="batch workload: number of spectra")
     return ap.parse_args()
 
@@ -226,6 +238,10 @@ def run_korg(args):
     ctx = _lib.Context(local)
     ctx.ensure_stark()
     ctx.check(ctx.lib.korg_set_timing(ctx.h, 1))
+    if args.tile:
+        tw, st, sp = (int(v) for v in args.tile.split(","))
+        for prec in (_lib.KORG_MIXED, _lib.KORG_FP64):
+            ctx.check(ctx.lib.korg_set_tile_config(ctx.h, len(inp.T), prec, tw, st, sp))
     s, l1, l5, w, keep = dev_inputs(inp, torch, dev)
     nwl, L = len(inp.wls), len(inp.T)
     flux = torch.empty(nwl, dtype=torch.float64, device=dev)
@@ -346,7 +362,7 @@ def run_korg(args):
                                f"@ 0.01 A ({nwl} points)",
                    "precision": "mixed",
                    "l2": f"flushed (256 MiB write) between steps; alpha {8 * L * nwl / 1e6:.0f} MB",
-                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
+                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU", "tile": args.tile or "default",
                    "host_prep_s": host_prep_s},
         "evals_per_step": evals,
         "evals_per_s": world * evals / (ms * 1e-3),
@@ -535,6 +551,173 @@ def run_batch(args):
     b.ctx.close()
 
 
+def run_variants(args):
+    import numpy as np
+    import torch
+    import build as korg_build
+    from korg_gb300 import synthetic
+    from korg_gb300.batch import BatchSynthesis
+    korg_build.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    t0 = time.perf_counter()
+    _progress("preparing the 1M-line cool giant")
+    base = synthetic.prepare(synthetic.config4())
+    inps = synthetic.abundance_variants(base, 16)
+    host_prep_s = time.perf_counter() - t0
+    nwl, L = len(base.wls), len(base.T)
+    b = BatchSynthesis(inps, precision="mixed", use_graph=True, autotune=True, max_scratch_bytes=160 << 30)
+    stream = torch.cuda.current_stream(dev)
+    for w in range(max(args.warmup, 3)):
+        b.run(stream)
+        torch.cuda.synchronize()
+        _progress(f"warm-up {w} done")
+    clk = Clocks(0)
+    times = []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.run(stream)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    clocks = clk.stop()
+    ms = statistics.mean(times)
+    evals = b.ctx.stats().line_evals
+    fm, cm = b.results()
+    _progress(f"timed: {ms:.1f} ms per batch of 16")
+    # plain FP64 of the first variant
+    one = BatchSynthesis(inps[:1], precision="fp64", use_graph=False, max_scratch_bytes=160 << 30)
+    one.run(stream)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    one.run(stream)
+    e1.record(stream)
+    e1.synchronize()
+    t64 = e0.elapsed_time(e1)
+    f64, c64 = one.results()
+    out = {"metric": METRIC, "value": 16 * 1000.0 / ms, "unit": "spectra/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32 profiles + f64 tau/flux (mixed)",
+           "data": "synthetic (seeded line list and stand-in atmosphere)",
+           "config": {"workload": f"16 abundance variants (n/U rows scaled by 10^U(-0.3, 0.3) dex per species) of an "
+                                  f"80-layer Teff 3500 logg 1.0 atmosphere, {len(base.linelist)} lines (40% atomic, "
+                                  f"60% TiO/CO/OH/CN), 3000-10000 A @ 0.01 A ({nwl} points); one step = the batch",
+                      "tile": b.tile_config(), "host_prep_s": host_prep_s},
+           "evals_per_step": evals, "evals_per_s": evals / (ms * 1e-3),
+           "fp64": {"spectra_per_s": 1000.0 / t64, "mixed_speedup": (t64 / 1.0) / (ms / 16),
+                    "mixed_max_rel_flux_err": float(np.max(np.abs(fm[0] / f64[0] - 1))),
+                    "mixed_rectified_rms": float(np.sqrt(np.mean((fm[0] / cm[0] - f64[0] / c64[0]) ** 2)))},
+           "clocks": clocks}
+    print(json.dumps(out), flush=True)
+
+
+def run_adjoint(args):
+    import numpy as np
+    import torch
+    import build as korg_build
+    from korg_gb300 import _lib, synthetic
+    from korg_gb300.synthesize import synthesize_prepared
+    korg_build.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    _progress("preparing the adjoint configuration")
+    inp = synthetic.prepare(synthetic.config2())
+    nwl, L = len(inp.wls), len(inp.T)
+    ctx = _lib.Context(0)
+    ctx.ensure_stark()
+    # observation: the same star with log gf perturbed by N(0, 0.1) dex
+    import copy
+    o = copy.copy(inp)
+    o.linelist = copy.copy(inp.linelist)
+    o.linelist.log_gf = inp.linelist.log_gf + np.random.default_rng(1).normal(0, 0.1, len(inp.linelist))
+    r = synthesize_prepared(o, precision="fp64", ctx=ctx)
+    obs = torch.as_tensor(r.flux / r.cntm, device=dev)
+    s, l1, l5, w, keep = dev_inputs(inp, torch, dev)
+    flux = torch.empty(nwl, dtype=torch.float64, device=dev)
+    cntm = torch.empty_like(flux)
+    shapes = {"T": L, "ne": L, "n_eff_vdW": L, "xi": L, "n_div_U": inp.n_div_U.size, "nH_I": L, "nHe_I": L,
+              "UH_I": L, "log_gf": len(inp.linelist), "cntm_vals": inp.cntm_vals.size, "alpha_ref_cntm": L}
+    gt = {k: torch.empty(n, dtype=torch.float64, device=dev) for k, n in shapes.items()}
+    grads = _lib.SynthGrads(*[C.cast(gt[k].data_ptr(), _lib._dp) for k in shapes])
+    stream = torch.cuda.current_stream(dev)
+    _progress("inputs resident")
+
+    def forward(prec):
+        ctx.check(ctx.lib.korg_synthesize_dev(ctx.h, C.byref(s), C.byref(l1), C.byref(l5), w.data_ptr(), nwl, prec,
+                                              flux.data_ptr(), cntm.data_ptr(), None, stream.cuda_stream))
+
+    def step(prec, flags=_lib.KORG_VJP_HYDROGEN):  # loss and its gradient w.r.t. every hot-path input
+        forward(prec)
+        rr = flux / cntm - obs
+        dF = 2 * rr / cntm
+        dC = -2 * rr * flux / cntm ** 2
+        ctx.check(ctx.lib.korg_synthesize_vjp_dev(ctx.h, C.byref(s), C.byref(l1), C.byref(l5), w.data_ptr(), nwl,
+                                                  prec, dF.data_ptr(), dC.data_ptr(), C.byref(grads), flags,
+                                                  stream.cuda_stream))
+        return torch.sum(rr * rr)
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return statistics.mean(ts)
+
+    res = {}
+    for name, prec in (("mixed", _lib.KORG_MIXED), ("fp64", _lib.KORG_FP64)):
+        reps = args.steps if name == "mixed" else 1
+        t_fwd = timed(lambda: forward(prec), reps)
+        clk = Clocks(0) if name == "mixed" else None
+        t_step = timed(lambda: step(prec), reps)
+        clocks = clk.stop() if clk else None
+        g = {k: v.cpu().numpy().copy() for k, v in gt.items()}
+        res[name] = (t_fwd, t_step, g, clocks)
+        _progress(f"{name}: forward {t_fwd:.1f} ms, forward + gradient {t_step:.1f} ms")
+    # stage times of one mixed step, and the step with the forward's opacity reused
+    reuse = _lib.KORG_VJP_HYDROGEN | _lib.KORG_VJP_REUSE_FORWARD
+    t_reuse = timed(lambda: step(_lib.KORG_MIXED, reuse), args.steps)
+    g_reuse = {k: v.cpu().numpy().copy() for k, v in gt.items()}
+    ctx.check(ctx.lib.korg_set_timing(ctx.h, 1))
+    step(_lib.KORG_MIXED)
+    torch.cuda.synchronize()
+    st = ctx.stats()
+    ctx.check(ctx.lib.korg_set_timing(ctx.h, 0))
+    vjp_stages = {"alpha_recompute": st.ms_vjp_alpha, "rt_adjoint": st.ms_vjp_rt, "hydrogen": st.ms_vjp_hydrogen,
+                  "lines": st.ms_vjp_lines}
+    stats = ctx.stats()
+    g32, g64 = res["mixed"][2], res["fp64"][2]
+    reuse_same = all(np.allclose(g_reuse[k], g32[k], rtol=1e-6, atol=0) for k in g32)
+    agree = {k: float(np.max(np.abs(g32[k] - g64[k])) / max(np.max(np.abs(g64[k])), 1e-300))
+             for k in ("T", "ne", "n_eff_vdW", "xi", "n_div_U", "log_gf")}
+    t_fwd, t_step = res["mixed"][0], res["mixed"][1]
+    out = {"metric": METRIC, "value": 1000.0 / t_step, "unit": "gradient steps/s (forward + loss + VJP)",
+           "n_gpus": 1, "steps": args.steps, "warmup": 1, "ms_per_step": t_step, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32 profiles + f64 tau/flux (mixed)",
+           "data": "synthetic (seeded line list and stand-in atmosphere)",
+           "config": {"workload": f"adjoint: 72 layers, Teff 4500 logg 2.5 [M/H] -0.5, {len(inp.linelist)} lines "
+                                  f"(50k atomic + 20k CO/OH/CN), 15000-17000 A @ 0.005 A ({nwl} points); loss = "
+                                  "sum of squared rectified-flux residuals; gradient w.r.t. T, ne, n_eff_vdW, xi, "
+                                  "n/U, log gf, continuum, H-line inputs"},
+           "forward_ms": t_fwd, "gradient_over_forward": (t_step - t_fwd) / t_fwd, "vjp_stages_ms": vjp_stages,
+           "reuse_forward": {"step_ms": t_reuse, "gradient_over_forward": (t_reuse - t_fwd) / t_fwd,
+                             "same_gradient": bool(reuse_same)},
+           "fp64": {"forward_ms": res["fp64"][0], "step_ms": res["fp64"][1],
+                    "gradient_over_forward": (res["fp64"][1] - res["fp64"][0]) / res["fp64"][0],
+                    "mixed_step_speedup": res["fp64"][1] / t_step},
+           "mixed_vs_fp64_gradient_max_rel": agree, "line_evals": stats.line_evals,
+           "clocks": res["mixed"][3]}
+    print(json.dumps(out), flush=True)
+    ctx.close()
+
+
 if __name__ == "__main__":
     a = parse()
     if a.steps is None:
@@ -543,5 +726,9 @@ if __name__ == "__main__":
         run_reference(a)
     elif a.workload == "batch":
         run_batch(a)
+    elif a.workload == "adjoint":
+        run_adjoint(a)
+    elif a.workload == "variants":
+        run_variants(a)
     else:
         run_korg(a)

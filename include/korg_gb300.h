@@ -112,6 +112,9 @@ typedef struct {
      * reference-wavelength lines, hydrogen lines, metal-line prologue (per-line constants,
      * windows, scans), metal-line tile kernel, both transfers, whole call */
     float ms_ref_lines, ms_hydrogen, ms_line_prep, ms_line_tile, ms_rt, ms_total;
+    /* the last korg_synthesize_vjp*: opacity recomputation, transfer adjoint, hydrogen-line
+     * derivatives, line adjoint (metal and reference-wavelength lines) */
+    float ms_vjp_alpha, ms_vjp_rt, ms_vjp_hydrogen, ms_vjp_lines;
 } korg_stats;
 
 typedef struct korg_ctx korg_ctx;
@@ -220,7 +223,10 @@ typedef struct {
     double *cntm_vals;
     double *alpha_ref_cntm;
 } korg_synth_grads;
-enum { KORG_VJP_HYDROGEN = 1 };
+/* KORG_VJP_REUSE_FORWARD: the previous call on this context was korg_synthesize[_dev] with the
+ * same inputs; its alpha (kept in the context when alpha_out was NULL), alpha_ref and line
+ * prologue are reused instead of recomputed. */
+enum { KORG_VJP_HYDROGEN = 1, KORG_VJP_REUSE_FORWARD = 2 };
 KORG_API int korg_synthesize_vjp(korg_ctx *ctx, const korg_synth_inputs *in, const korg_lines *lines,
                                  const korg_lines *lines5, const double *wls, int64_t nwl,
                                  int precision, const double *dflux, const double *dcntm,
@@ -230,6 +236,27 @@ KORG_API int korg_synthesize_vjp_dev(korg_ctx *ctx, const korg_synth_inputs *in,
                                      const double *wls, int64_t nwl, int precision,
                                      const double *dflux, const double *dcntm,
                                      const korg_synth_grads *grads, int flags, void *stream);
+
+/* MolecularCrossSection(linelist, wl_params; cutoff_alpha, vmic_vals, log_temp_vals) --
+ * src/molecular_cross_sections.jl:51-88: the absorption cross-section per molecule of one
+ * species' lines on a (vmic, T, wavelength) grid, with the line-opacity kernels.  Device
+ * pointers: lines (species row 0 for every line), wls[nwl], T[nT] = 10^log_temp_vals,
+ * inv_U[nT] = 1/U(T) of the species, vmic_vals[nv] in km/s; table[(v * nwl + j) * nT + t]. */
+KORG_API int korg_molecular_cross_section_dev(korg_ctx *ctx, const korg_lines *lines, const double *wls,
+                                              int64_t nwl, const double *T, const double *inv_U,
+                                              int32_t nT, const double *vmic_vals, int32_t nv,
+                                              double cutoff_alpha, int precision, double *table,
+                                              void *stream);
+/* interpolate_molecular_cross_sections! (src/molecular_cross_sections.jl:101-117) for one table:
+ * alpha[j * L + l] += table(vmic[l], log10 T[l], wls[j]) * n[l], trilinear on the table's grid,
+ * zero outside it.  Device pointers. */
+KORG_API int korg_interpolate_molecular_cross_section_dev(korg_ctx *ctx, double *alpha, const double *wls,
+                                                          int64_t nwl, int32_t L, const double *T,
+                                                          const double *vmic, const double *n,
+                                                          const double *table, const double *table_wls,
+                                                          int64_t ntw, const double *vmic_vals, int32_t nv,
+                                                          const double *log_temp_vals, int32_t nT,
+                                                          void *stream);
 
 /* Batched synthesis: many spectra on one wavelength grid, as the Fit module's repeated-synthesis
  * loop (src/Fit/fit_via_synthesis.jl:304-390) and grid building call synthesize.  Each item is
@@ -257,9 +284,13 @@ KORG_API int korg_synthesize_batch_dev(korg_ctx *ctx, int32_t nspec, const korg_
 KORG_API int korg_set_batch_options(korg_ctx *ctx, int use_graph, int autotune,
                                     int64_t max_scratch_bytes);
 /* The tile shape the context uses for (L, precision): wavelengths per CTA, lines per shared
- * memory batch, and whether it came from the autotuner. */
+ * memory batch, whether each CTA takes a single layer group (split), and whether it came from
+ * the autotuner (split and tuned may be NULL).  korg_set_tile_config fixes the shape instead
+ * (counts as tuned).  No counterpart in the reference. */
 KORG_API int korg_get_tile_config(korg_ctx *ctx, int32_t L, int precision, int32_t *tw,
-                                  int32_t *stage, int32_t *tuned);
+                                  int32_t *stage, int32_t *split, int32_t *tuned);
+KORG_API int korg_set_tile_config(korg_ctx *ctx, int32_t L, int precision, int32_t tw,
+                                  int32_t stage, int32_t split);
 
 /* Not a counterpart of any reference function: measures the device's sustained FP32
  * (fp64 == 0) or FP64 FMA throughput in TFLOP/s with independent FMA chains, the roofline

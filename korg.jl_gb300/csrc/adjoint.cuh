@@ -386,14 +386,53 @@ __device__ __forceinline__ int64_t adj_chunks(int tier, int64_t nwl) {
     return tier == 3 ? (nwl + ADJ_CHUNK - 1) / ADJ_CHUNK : (tier == 2 ? 33 : (tier == 1 ? 3 : 1));
 }
 
+__device__ __forceinline__ float fast_div(float p, float q) { return __fdividef(p, q); }
+__device__ __forceinline__ double fast_div(double p, double q) { return p / q; }
+
+// Compensated running sums of N values (mixed: FP32 partials enter Kahan-compensated totals;
+// FP64: plain sums).
+template <bool MIXED, int N>
+struct AdjSums {
+    using R = typename std::conditional<MIXED, float, double>::type;
+    R s[N], c[N];
+    __device__ __forceinline__ AdjSums() {
+#pragma unroll
+        for (int k = 0; k < N; k++) { s[k] = R(0); c[k] = R(0); }
+    }
+    __device__ __forceinline__ void add(const R* p) {
+#pragma unroll
+        for (int k = 0; k < N; k++) {
+            if (MIXED) {
+                const R y = p[k] - c[k], t = s[k] + y;
+                c[k] = (t - s[k]) - y;
+                s[k] = t;
+            } else {
+                s[k] += p[k];
+            }
+        }
+    }
+    __device__ __forceinline__ double get(int k) const { return double(s[k]) - double(c[k]); }
+};
+
+// One block per item: thread (l = tid mod L, jr = tid / L) walks every NJ-th wavelength of the
+// chunk for layer l, so a warp reads consecutive G entries (layer fastest) and no lane idles.
+// In the asymptotic wing (a <= 0.2, v >= 5: most evaluations of a wide window)
+// H = a/sqrt(pi) u (1 + 1.5u + 3.75u^2) with u = 1/v^2 = c t (c = 2 sigma^2, t = 1/|dl|^2), so
+// the three window sums follow from the moments M_k = sum G u^k, k = 1..3 (three FMAs per
+// evaluation):  sum G H = a/sqrt(pi) (M1 + 1.5 M2 + 3.75 M3),  sum G H_a = that / a,
+// sum G (a H_a + v H_v) = sum G H - 2 a/sqrt(pi) (M1 + 3 M2 + 11.25 M3).  Closer to the centre
+// every branch is differentiated with dual numbers.
 template <bool MIXED>
-__global__ void __launch_bounds__(128) line_adj_kernel(LineAdjArgs a) {
+__global__ void __launch_bounds__(512) line_adj_kernel(LineAdjArgs a) {
     using R = typename std::conditional<MIXED, float, double>::type;
     __shared__ long long s_item;
     __shared__ int64_t s_cnt[NTIER + 1];
-    __shared__ R s_x[ADJ_CHUNK];  // |wl_j - wl0| of the item's wavelengths
+    __shared__ R s_x[ADJ_CHUNK];       // |wl_j - wl0| of the item's wavelengths
+    extern __shared__ double s_red[];  // [6][NJ][L] partial sums
     const int L = a.L, Lp = a.Lp;
-    const int l = threadIdx.x;  // one layer per thread (blockDim.x >= L)
+    const int NJ = blockDim.x / L;
+    const int l = threadIdx.x % L, jr = threadIdx.x / L;
+    const bool active = jr < NJ;
     if (threadIdx.x == 0) {
         int64_t acc = 0;
         for (int t = NTIER - 1; t >= 0; t--) {
@@ -420,63 +459,102 @@ __global__ void __launch_bounds__(128) line_adj_kernel(LineAdjArgs a) {
         const double wl0 = a.wl[i];
         for (int64_t j = j0 + threadIdx.x; j <= j1; j += blockDim.x) s_x[j - j0] = R(fabs(a.wls[j] - wl0));
         __syncthreads();  // s_x filled; s_item read by everyone
-        if (j0 <= j1 && l < L) {
-            R s, av;  // 1/(sigma sqrt 2) and a of this (line, layer)
-            if (MIXED) {
-                const float4 p = reinterpret_cast<const float4*>(a.params)[i * Lp + l];
-                s = R(rsqrtf(p.x));
-                av = R(p.y);
-            } else {
-                const P64 p = reinterpret_cast<const P64*>(a.params)[i * Lp + l];
-                s = R(p.inv_s);
-                av = R(p.a);
-            }
-            // sums over the chunk of G * {H, a H_a + v H_v, H_a}
-            R sH = 0, sX = 0, sA = 0, cH = 0, cX = 0, cA = 0;
-            const int64_t nj = j1 - j0 + 1;
-            for (int64_t jj = 0; jj < nj; jj++) {
-                const int64_t e = (j0 + jj) * L + l;
-                const R g = a.g32 ? R(static_cast<const float*>(a.G)[e]) : R(static_cast<const double*>(a.G)[e]);
-                const R v = s_x[jj] * s;
-                R H, X, A;
-                if (av <= R(0.2) && v >= R(5)) {
-                    // asymptotic wing: H = a/sqrt(pi) u (1 + 1.5u + 3.75u^2), u = 1/v^2
-                    const R u = R(1) / (v * v);
-                    const R k = av * R(0.5641895835477563);
-                    H = k * u * (R(1) + u * (R(1.5) + R(3.75) * u));
-                    A = R(0.5641895835477563) * u * (R(1) + u * (R(1.5) + R(3.75) * u));  // H / a
-                    X = H - R(2) * u * k * (R(1) + u * (R(3) + R(11.25) * u));
+        if (j0 <= j1) {
+            AdjSums<MIXED, 3> cen;  // central evaluations: G H, G (a H_a + v H_v), G H_a
+            AdjSums<MIXED, 3> mom;  // wing moments M1, M2, M3
+            R s = R(1), av = R(0);
+            if (active) {
+                if (MIXED) {
+                    const float4 p = reinterpret_cast<const float4*>(a.params)[i * Lp + l];
+                    s = R(rsqrtf(p.x));
+                    av = R(p.y);
                 } else {
-                    const Dual<R> d = voigt_dual<R>(av, v);
-                    H = d.x;
-                    A = d.da;
-                    X = av * d.da + v * d.dv;
+                    const P64 p = reinterpret_cast<const P64*>(a.params)[i * Lp + l];
+                    s = R(p.inv_s);
+                    av = R(p.a);
                 }
-                if (MIXED) {  // compensated sums
-                    R y = g * H - cH, t = sH + y;
-                    cH = (t - sH) - y;
-                    sH = t;
-                    y = g * X - cX;
-                    t = sX + y;
-                    cX = (t - sX) - y;
-                    sX = t;
-                    y = g * A - cA;
-                    t = sA + y;
-                    cA = (t - sA) - y;
-                    sA = t;
-                } else {
-                    sH += g * H;
-                    sX += g * X;
-                    sA += g * A;
+                const R c2 = R(1) / (s * s);                         // 2 sigma^2
+                const R xw = av <= R(0.2) ? R(5) / s : R(3.0e38);    // wing starts at v = 5
+                const int64_t nj = j1 - j0 + 1;
+                const int64_t step = int64_t(NJ) * L;
+                const float* g32p = static_cast<const float*>(a.G) + (j0 + jr) * L + l;
+                const double* g64p = static_cast<const double*>(a.G) + (j0 + jr) * L + l;
+                R pc[3] = {0, 0, 0}, pm[3] = {0, 0, 0};
+                auto eval = [&](R g, R x) {
+                    if (x >= xw) {
+                        const R u = fast_div(c2, x * x);
+                        const R gu = g * u, gu2 = gu * u;
+                        pm[0] += gu;
+                        pm[1] += gu2;
+                        pm[2] += gu2 * u;
+                    } else {
+                        const Dual<R> d = voigt_dual<R>(av, x * s);
+                        pc[0] += g * d.x;
+                        pc[1] += g * (av * d.da + x * s * d.dv);
+                        pc[2] += g * d.da;
+                    }
+                };
+                // groups of 4 independent loads in flight, partial sums flushed every 32 terms
+                constexpr int U = 4;
+                int64_t jj = jr;
+                int cnt = 0;
+                for (; jj + (U - 1) * NJ < nj; jj += U * NJ) {
+                    R g[U];
+#pragma unroll
+                    for (int u = 0; u < U; u++)
+                        g[u] = a.g32 ? R(g32p[u * step]) : R(g64p[u * step]);
+                    g32p += U * step;
+                    g64p += U * step;
+#pragma unroll
+                    for (int u = 0; u < U; u++) eval(g[u], s_x[jj + u * NJ]);
+                    cnt += U;
+                    if (cnt >= 32) {
+                        cen.add(pc);
+                        mom.add(pm);
+                        pc[0] = pc[1] = pc[2] = pm[0] = pm[1] = pm[2] = R(0);
+                        cnt = 0;
+                    }
+                }
+                for (; jj < nj; jj += NJ) {
+                    eval(a.g32 ? R(*g32p) : R(*g64p), s_x[jj]);
+                    g32p += step;
+                    g64p += step;
+                }
+                cen.add(pc);
+                mom.add(pm);
+            }
+            // window sums of this thread: central + wing (from the moments)
+            if (active) {
+                const double k = 0.5641895835477563 * double(av);  // a / sqrt(pi)
+                const double M1 = mom.get(0), M2 = mom.get(1), M3 = mom.get(2);
+                const double wH = k * (M1 + 1.5 * M2 + 3.75 * M3);
+                const double wA = 0.5641895835477563 * (M1 + 1.5 * M2 + 3.75 * M3);
+                const double wX = wH - 2 * k * (M1 + 3 * M2 + 11.25 * M3);
+                s_red[(0 * NJ + jr) * L + l] = cen.get(0) + wH;
+                s_red[(1 * NJ + jr) * L + l] = cen.get(1) + wX;
+                s_red[(2 * NJ + jr) * L + l] = cen.get(2) + wA;
+            }
+            __syncthreads();
+            if (active && jr == 0) {
+                double* dp = a.dpar + (i * Lp + l) * 3;
+                for (int k = 0; k < 3; k++) {
+                    double t = 0.0;
+                    for (int r = 0; r < NJ; r++) t += s_red[(k * NJ + r) * L + l];
+                    atomicAdd(dp + k, t);
                 }
             }
-            double* dp = a.dpar + (i * Lp + l) * 3;
-            atomicAdd(dp + 0, double(sH));
-            atomicAdd(dp + 1, double(sX));
-            atomicAdd(dp + 2, double(sA));
         }
-        __syncthreads();  // s_x and s_item are rewritten for the next item
+        __syncthreads();  // s_x, s_red and s_item are rewritten for the next item
     }
+}
+
+// Threads per block of line_adj_kernel for L layers: L * NJ, the smallest multiple of 32 that
+// is at least 128 (at most 512).
+inline int adj_threads(int L) {
+    int nj = 1;
+    while (nj * L < 512 && ((nj * L) % 32 != 0 || nj * L < 128)) nj++;
+    if (nj * L > 512) nj = 512 / L;
+    return nj * L;
 }
 
 // Chain rule of the per-(line, layer) prologue (line_absorption.jl:86-106), FP64, one warp per

@@ -29,15 +29,15 @@ struct DevBuf {
     size_t cap = 0;
 };
 
-constexpr int NEV = 8;
+constexpr int NEV = 13;  // 0-7: forward stages and probes; 8-12: reverse-mode stages
 
 // Tile shape of the line tile kernel: wavelengths per CTA and lines per shared-memory batch
 // (0: the default for the precision).
 struct TileCfg {
-    int tw, stage;
+    int tw, stage, split;  // split: one layer group per CTA
 };
 struct TuneRecord {
-    int L, mixed, tw, stage;
+    int L, mixed, tw, stage, split;
     float ms;
 };
 
@@ -53,6 +53,7 @@ struct korg_ctx {
     DevBuf hrec, hQ, hQ32, hulb, huub;
     DevBuf stage_dev, aref, alpha, flux, cntm, math;
     DevBuf vjp_g, vjp_dpar, vjp_small, vjp_hfd;  // reverse mode
+    DevBuf mx_layers;                            // molecular cross-section layer inputs
     void* stage_host = nullptr;
     size_t stage_host_cap = 0;
     // batched synthesis: chunk alpha, per-spectrum line scratch, tile arguments + reference
@@ -80,6 +81,7 @@ struct korg_ctx {
     cudaEvent_t ev[NEV] = {};
     korg_stats stats{};
     bool stats_pending = false;
+    bool vjp_timed = false;
 };
 
 namespace {
@@ -272,21 +274,25 @@ int prep_lines(korg_ctx* ctx, const LineScratch& sc, const double* wls, int64_t 
 // Launch shape of the tile kernel: TW wavelengths x G layer groups per CTA, `stage` lines per
 // shared-memory batch.
 struct TileGeom {
-    int tw, threads, stage, region;
+    int tw, threads, stage, region, split, G;
     size_t smem;
 };
 
 bool tile_geom(bool mixed, int Lp, int G, TileCfg c, TileGeom* g) {
     const size_t psz = mixed ? sizeof(float4) : sizeof(P64);
     const int B = c.stage > 0 ? c.stage : (mixed ? STAGE_LINES : STAGE_LINES / 2);
-    if (c.tw < 32 || c.tw % 32 != 0 || c.tw * G > 512 || B < 1) return false;
-    size_t region = size_t(B) * Lp * psz;
-    region = std::max(region, (size_t(c.tw) * (Lp + 1) * sizeof(double) + 1) / 2);
+    const int Gc = c.split ? 1 : G;  // layer groups per CTA
+    const int SL = c.split ? Lp / G : Lp;
+    if (c.tw < 32 || c.tw % 32 != 0 || c.tw * Gc > 512 || B < 1) return false;
+    size_t region = size_t(B) * SL * psz;
+    region = std::max(region, (size_t(c.tw) * (SL + 1) * sizeof(double) + 1) / 2);
     region = (region + 15) & ~size_t(15);
     g->tw = c.tw;
-    g->threads = c.tw * G;
+    g->threads = c.tw * Gc;
     g->stage = B;
     g->region = int(region);
+    g->split = c.split ? 1 : 0;
+    g->G = G;
     g->smem = 2 * region + size_t(g->threads) * sizeof(LineStage);
     return g->smem <= 227 * 1024;
 }
@@ -295,6 +301,7 @@ template <bool MIXED, int KMAX, int MAXT, int MINB>
 int launch_tile(korg_ctx* ctx, TileArgs ta, const TileGeom& g, const TileQueue* q, cudaStream_t s) {
     ta.stage = g.stage;
     ta.region = g.region;
+    ta.split = g.split;
     if (q) {
         auto kern = line_tile_queue_kernel<MIXED, KMAX, MAXT, MINB>;
         KCUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g.smem)));
@@ -306,7 +313,7 @@ int launch_tile(korg_ctx* ctx, TileArgs ta, const TileGeom& g, const TileQueue* 
         auto kern = line_tile_kernel<MIXED, KMAX, MAXT, MINB>;
         KCUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g.smem)));
         const int64_t tiles = (ta.nwl + g.tw - 1) / g.tw;
-        kern<<<dim3(unsigned(tiles)), g.threads, g.smem, s>>>(ta);
+        kern<<<dim3(unsigned(tiles), g.split ? unsigned(g.G) : 1u), g.threads, g.smem, s>>>(ta);
     }
     KCUDA(cudaGetLastError());
     return KORG_OK;
@@ -329,7 +336,7 @@ int run_tiles(korg_ctx* ctx, const TileArgs& ta, int kmax, const TileGeom& g, co
 // The tile shape for (L, precision): the autotuned one when there is one, else the default.
 TileCfg tile_cfg(const korg_ctx* ctx, int L, bool mixed) {
     auto it = ctx->tuned.find(std::make_pair(L, int(mixed)));
-    return it != ctx->tuned.end() ? it->second : TileCfg{TILE_TW, 0};
+    return it != ctx->tuned.end() ? it->second : TileCfg{TILE_TW, 0, 1};  // one layer group per CTA
 }
 
 // Autotuner: times every candidate shape (TW in {32, 64, 128} x stage in {B/2, B}) on the real
@@ -344,12 +351,13 @@ int autotune_tiles(korg_ctx* ctx, const TileArgs& ta0, int kmax, bool mixed, cud
     TileArgs ta = ta0;
     ta.alpha = static_cast<double*>(ctx->tune_alpha.p);
     const int B0 = mixed ? STAGE_LINES : STAGE_LINES / 2;
-    TileCfg best{TILE_TW, 0};
+    TileCfg best{TILE_TW, 0, 0};
     float best_ms = 1e30f;
+    for (int split : {0, 1})
     for (int tw : {64, 32, 128})
         for (int B : {B0, B0 / 2}) {
             TileGeom g;
-            if (!tile_geom(mixed, Lp, G, TileCfg{tw, B}, &g)) continue;
+            if (!tile_geom(mixed, Lp, G, TileCfg{tw, B, split}, &g)) continue;
             float t = 1e30f;
             for (int rep = 0; rep < 3; rep++) {
                 KCUDA(cudaEventRecord(ctx->ev[6], s));
@@ -360,8 +368,8 @@ int autotune_tiles(korg_ctx* ctx, const TileArgs& ta0, int kmax, bool mixed, cud
                 KCUDA(cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]));
                 if (rep > 0) t = std::min(t, ms);
             }
-            ctx->tune_log.push_back({L, int(mixed), tw, B, t});
-            if (t < best_ms) { best_ms = t; best = TileCfg{tw, B}; }
+            ctx->tune_log.push_back({L, int(mixed), tw, B, split, t});
+            if (t < best_ms) { best_ms = t; best = TileCfg{tw, B, split}; }
         }
     ctx->tuned[key] = best;
     return KORG_OK;
@@ -609,7 +617,8 @@ int enqueue_batch(korg_ctx* ctx, const BatchPlan& p, int nspec, const korg_batch
             }
         }
         record(ctx, 2, s);
-        const TileQueue q{d_targs + s0, s1 - s0, int64_t(s1 - s0) * ntiles, d_ctr + c};
+        const int groups = p.geom.split ? p.G : 1;
+        const TileQueue q{d_targs + s0, s1 - s0, groups, int64_t(s1 - s0) * ntiles * groups, d_ctr + c};
         KCHECK(run_tiles(ctx, TileArgs{}, p.kmax, p.geom, &q, mixed, s));
         record(ctx, 5, s);
         for (int i = s0; i < s1; i++) {
@@ -650,6 +659,7 @@ void fill_batch_host(korg_ctx* ctx, const BatchPlan& p, int nspec, const korg_ba
         TileArgs ta = make_tile_args(sc, batch_alpha(ctx, p, i, nwl), wls, nwl, lines_dev(&it[i].lines), p.L, p.Lp, p.G);
         ta.stage = p.geom.stage;
         ta.region = p.geom.region;
+        ta.split = p.geom.split;
         targs[i] = ta;
         refwl[i] = it[i].in.ref_wl;
     }
@@ -676,6 +686,12 @@ std::vector<unsigned char> batch_key(korg_ctx* ctx, int nspec, const korg_batch_
 }
 
 // ------------------------------------------------------------------ reverse mode (VJP)
+// h[l] = sign * x[l] / 2 (hydro_fd_contract_kernel then divides by 2 h = sign * x)
+__global__ void hfd_half_kernel(const double* x, int L, double sign, double* h) {
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l < L) h[l] = sign * 0.5 * x[l];
+}
+
 // Perturbed copies of the per-layer hydrogen-line inputs: field `which` of {T, ne, nH_I, nHe_I,
 // UH_I, xi} scaled by (1 + sign * rel) in every layer; h[l] = rel * |value|.
 __global__ void hfd_perturb_kernel(HLayers src, int which, double rel, double sign, double* dst, double* h) {
@@ -737,17 +753,24 @@ int run_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& ln, cons
     KCHECK(zero(daref, L));
     KCHECK(reset_counters(ctx, s));
 
-    // 1. opacity, recomputed (src/synthesize.jl:249-306 as in the forward)
+    // 1. opacity, recomputed (src/synthesize.jl:249-306 as in the forward), unless the caller
+    //    states that the previous call on this context was korg_synthesize[_dev] of the same
+    //    inputs, whose alpha, alpha_ref and metal-line prologue are still in the scratch
+    record(ctx, 8, s);
     double* alpha = static_cast<double*>(ctx->alpha.p);
     double* aref = static_cast<double*>(ctx->aref.p);
-    alpha_init_kernel<<<unsigned((nwl + 63) / 64), 256, 0, s>>>(alpha, wls, nwl, L, cn);
-    KCUDA(cudaGetLastError());
-    KCUDA(cudaMemcpyAsync(aref, in->alpha_ref_cntm, sizeof(double) * L, cudaMemcpyDeviceToDevice, s));
     const CntmDev cref{1, nullptr, in->alpha_ref_cntm};
-    KCHECK(run_line_absorption(ctx, aref, ref_wl_dev, 1, ln5, lay, cref, in->cutoff_threshold, mixed, s));
     const HLayers hl{L, lay.T, lay.ne, in->nH_I, in->nHe_I, in->UH_I, lay.xi};
-    if (in->hydrogen_lines) KCHECK(run_hydrogen(ctx, alpha, wls, nwl, hl, in->hydrogen_window, in->use_MHD, mixed, s));
-    KCHECK(run_line_absorption(ctx, alpha, wls, nwl, ln, lay, cn, in->cutoff_threshold, mixed, s));
+    if (!(flags & KORG_VJP_REUSE_FORWARD)) {
+        alpha_init_kernel<<<unsigned((nwl + 63) / 64), 256, 0, s>>>(alpha, wls, nwl, L, cn);
+        KCUDA(cudaGetLastError());
+        KCUDA(cudaMemcpyAsync(aref, in->alpha_ref_cntm, sizeof(double) * L, cudaMemcpyDeviceToDevice, s));
+        KCHECK(run_line_absorption(ctx, aref, ref_wl_dev, 1, ln5, lay, cref, in->cutoff_threshold, mixed, s));
+        if (in->hydrogen_lines)
+            KCHECK(run_hydrogen(ctx, alpha, wls, nwl, hl, in->hydrogen_window, in->use_MHD, mixed, s));
+        KCHECK(run_line_absorption(ctx, alpha, wls, nwl, ln, lay, cn, in->cutoff_threshold, mixed, s));
+    }
+    record(ctx, 9, s);
 
     // 2. transfer adjoint: opacity cotangent G, dL/dT through the source function, dL/dalpha_ref
     RtAdjArgs ra{alpha, lay.T, wls, nwl, L, in->tau_ref, aref, static_cast<MathTables*>(ctx->math.p), cn, dflux,
@@ -759,8 +782,14 @@ int run_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& ln, cons
         rt_adjoint_kernel<<<unsigned(blocks), 32 * RTA_WARPS, smem, s>>>(ra);
         KCUDA(cudaGetLastError());
     }
+    record(ctx, 10, s);
 
-    // 3. hydrogen lines: layer-diagonal Jacobian by central differences of the FP64 kernel
+    // 3. hydrogen lines: layer-diagonal Jacobian.  alpha_H is proportional to nH_I / UH_I
+    //    (hydrogen_line_absorption.jl:110-111, 152-154); n(H I) also enters the ABO widths of
+    //    H alpha/beta/gamma (:130) and, with n(He I), the MHD occupation probabilities (:89).
+    //    So d/dUH_I = -alpha_H / UH_I always, d/dnH_I = alpha_H / nH_I when MHD is off and no ABO
+    //    line reaches the grid, d/dnHe_I = 0 when MHD is off; the rest (T, n_e, xi, and nH_I /
+    //    nHe_I otherwise) by central differences of the FP64 kernel, all layers perturbed at once.
     if (in->hydrogen_lines && (flags & KORG_VJP_HYDROGEN)) {
         KCHECK(ensure(ctx, ctx->vjp_hfd, sizeof(double) * 2 * nLw));
         double* ap = static_cast<double*>(ctx->vjp_hfd.p);
@@ -768,8 +797,39 @@ int run_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& ln, cons
         double* hin = reinterpret_cast<double*>(sm + o_hin);
         double* h = reinterpret_cast<double*>(sm + o_h);
         double* outs[6] = {dT, gr.ne, gr.nH_I, gr.nHe_I, gr.UH_I, gr.xi};
+        bool abo_near = false;  // H alpha, beta, gamma (6564.6, 4862.7, 4341.7 A in vacuum)
+        {
+            double wmin = 0, wmax = 0;
+            KCUDA(cudaMemcpyAsync(&wmin, wls, sizeof(double), cudaMemcpyDeviceToHost, s));
+            KCUDA(cudaMemcpyAsync(&wmax, wls + nwl - 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+            KCUDA(cudaStreamSynchronize(s));
+            for (double w0 : {6564.6e-8, 4862.7e-8, 4341.7e-8})
+                abo_near |= (w0 + 2 * in->hydrogen_window >= wmin) && (w0 - 2 * in->hydrogen_window <= wmax);
+        }
+        const bool linear_nH = !in->use_MHD && !abo_near;
+        if (outs[4] || (linear_nH && outs[2])) {
+            // one unperturbed FP64 evaluation, then alpha_H / UH_I and alpha_H / nH_I
+            KCUDA(cudaMemsetAsync(ap, 0, sizeof(double) * nLw, s));
+            KCHECK(run_hydrogen(ctx, ap, wls, nwl, hl, in->hydrogen_window, in->use_MHD, false, s));
+            KCUDA(cudaMemsetAsync(am, 0, sizeof(double) * nLw, s));
+            // hydro_fd_contract_kernel computes sum G (ap - am) / (2 h): with am = 0 and
+            // h = x / 2 (x = UH_I or nH_I) this is sum G alpha_H / x
+            if (outs[4]) {
+                hfd_half_kernel<<<(L + 127) / 128, 128, 0, s>>>(in->UH_I, L, -1.0, h);
+                hydro_fd_contract_kernel<<<ctx->sms * 4, 256, 0, s>>>(ctx->vjp_g.p, int32_t(mixed), ap, am, h, nwl, L,
+                                                                     outs[4]);
+            }
+            if (linear_nH && outs[2]) {
+                hfd_half_kernel<<<(L + 127) / 128, 128, 0, s>>>(in->nH_I, L, 1.0, h);
+                hydro_fd_contract_kernel<<<ctx->sms * 4, 256, 0, s>>>(ctx->vjp_g.p, int32_t(mixed), ap, am, h, nwl, L,
+                                                                     outs[2]);
+            }
+            KCUDA(cudaGetLastError());
+        }
         for (int k = 0; k < 6; k++) {
-            if (!outs[k]) continue;
+            if (!outs[k] || k == 4) continue;
+            if (k == 2 && linear_nH) continue;
+            if (k == 3 && !in->use_MHD) continue;  // n(He I) only enters the MHD probabilities
             const double rel = 1e-5;
             hfd_perturb_kernel<<<(L + 127) / 128, 128, 0, s>>>(hl, k, rel, +1.0, hin, h);
             hfd_perturb_kernel<<<(L + 127) / 128, 128, 0, s>>>(hl, k, rel, -1.0, hin + 6 * L, h);
@@ -785,6 +845,7 @@ int run_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& ln, cons
             KCUDA(cudaGetLastError());
         }
     }
+    record(ctx, 11, s);
 
     // 4. metal and molecular lines: window sums per (line, layer), then the prologue chain rule
     const LineAdjOut lo{dT, gr.ne, gr.n_eff_vdW, gr.xi, gr.n_div_U, gr.log_gf};
@@ -797,14 +858,15 @@ int run_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& ln, cons
         KCUDA(cudaMemsetAsync(dpar, 0, sizeof(double) * 3 * size_t(lns.n) * Lp, s));
         KCUDA(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), s));
         LineAdjArgs la{Gp, g32, w, nw, L, Lp, lns.wl, sc.params, sc.lb, sc.ub, sc.tier_idx, sc.tier_meta, dpar, ctr};
-        const int threads = ((L + 31) / 32) * 32;
+        const int threads = adj_threads(L);
+        const size_t smem = sizeof(double) * 3 * threads;
         int per_sm = 0;
         if (mixed) {
-            KCUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, line_adj_kernel<true>, threads, 0));
-            line_adj_kernel<true><<<ctx->sms * std::max(per_sm, 1), threads, 0, s>>>(la);
+            KCUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, line_adj_kernel<true>, threads, smem));
+            line_adj_kernel<true><<<ctx->sms * std::max(per_sm, 1), threads, smem, s>>>(la);
         } else {
-            KCUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, line_adj_kernel<false>, threads, 0));
-            line_adj_kernel<false><<<ctx->sms * std::max(per_sm, 1), threads, 0, s>>>(la);
+            KCUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, line_adj_kernel<false>, threads, smem));
+            line_adj_kernel<false><<<ctx->sms * std::max(per_sm, 1), threads, smem, s>>>(la);
         }
         KCUDA(cudaGetLastError());
         const size_t psmem = sizeof(double) * size_t(4 + S) * L;
@@ -827,8 +889,104 @@ int run_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& ln, cons
     }
     if (gr.alpha_ref_cntm)
         KCUDA(cudaMemcpyAsync(gr.alpha_ref_cntm, daref, sizeof(double) * L, cudaMemcpyDeviceToDevice, s));
+    record(ctx, 12, s);
+    ctx->vjp_timed = ctx->timing;
     ctx->stats_pending = true;
     return KORG_OK;
+}
+
+
+// ------------------------------------------------------------------ molecular cross-sections
+// Trilinear interpolation of a precomputed molecular cross-section table into alpha
+// (interpolate_molecular_cross_sections!, src/molecular_cross_sections.jl:101-117): Gridded
+// Linear in (vmic, log10 T, wavelength), zero outside the table (extrapolate(..., 0.0)).
+struct MolXsArgs {
+    double* alpha;             // [nwl][L] (+=)
+    const double* wls;         // [nwl]
+    int64_t nwl;
+    int32_t L;
+    const double *T, *vmic, *n;  // [L]: temperature, microturbulence (km/s), number density
+    const double* table;       // [nv][ntw][nT]
+    const double* twls;        // [ntw] table wavelengths
+    int64_t ntw;
+    const double* vmic_vals;   // [nv]
+    int32_t nv;
+    const double* logT_vals;   // [nT]
+    int32_t nT;
+};
+
+// knot interval and weight of x on increasing knots; false outside [k0, k_{n-1}]
+__device__ __forceinline__ bool grid_pos(const double* k, int64_t n, double x, int64_t* i, double* t) {
+    if (!(x >= k[0] && x <= k[n - 1])) return false;
+    if (n == 1) { *i = 0; *t = 0.0; return true; }
+    int64_t lo = search_last(k, n, x);
+    lo = lo < 0 ? 0 : (lo > n - 2 ? n - 2 : lo);
+    *i = lo;
+    *t = (x - k[lo]) / (k[lo + 1] - k[lo]);
+    return true;
+}
+
+__global__ void __launch_bounds__(256) molxs_interp_kernel(MolXsArgs a) {
+    __shared__ int64_t s_iw[64];
+    __shared__ double s_tw[64];
+    __shared__ int s_okw[64];
+    extern __shared__ double s_lay[];  // per layer: iv, tv, iT, tT, n, ok
+    const int L = a.L;
+    for (int l = threadIdx.x; l < L; l += blockDim.x) {
+        int64_t iv = 0, iT = 0;
+        double tv = 0, tT = 0;
+        const bool ok = grid_pos(a.vmic_vals, a.nv, a.vmic[l], &iv, &tv) &&
+                        grid_pos(a.logT_vals, a.nT, log10(a.T[l]), &iT, &tT);
+        double* p = s_lay + 6 * l;
+        p[0] = double(iv); p[1] = tv; p[2] = double(iT); p[3] = tT; p[4] = a.n[l]; p[5] = ok ? 1.0 : 0.0;
+    }
+    const int64_t j0 = int64_t(blockIdx.x) * 64;
+    const int64_t jn = min(int64_t(64), a.nwl - j0);
+    if (threadIdx.x < jn) {
+        int64_t iw = 0;
+        double tw = 0;
+        s_okw[threadIdx.x] = grid_pos(a.twls, a.ntw, a.wls[j0 + threadIdx.x], &iw, &tw);
+        s_iw[threadIdx.x] = iw;
+        s_tw[threadIdx.x] = tw;
+    }
+    __syncthreads();
+    for (int64_t e = threadIdx.x; e < jn * L; e += blockDim.x) {
+        const int jj = int(e / L), l = int(e % L);
+        const double* p = s_lay + 6 * l;
+        if (!s_okw[jj] || p[5] == 0.0) continue;
+        const int64_t iv = int64_t(p[0]), iT = int64_t(p[2]), iw = s_iw[jj];
+        const double tv = p[1], tT = p[3], tw = s_tw[jj];
+        const int64_t dv = (a.nv > 1) ? a.ntw * a.nT : 0, dw = (a.ntw > 1) ? a.nT : 0, dT = (a.nT > 1) ? 1 : 0;
+        const double* c = a.table + (iv * a.ntw + iw) * a.nT + iT;
+        const double c000 = c[0], c001 = c[dT], c010 = c[dw], c011 = c[dw + dT];
+        const double c100 = c[dv], c101 = c[dv + dT], c110 = c[dv + dw], c111 = c[dv + dw + dT];
+        const double c00 = c000 * (1 - tT) + c001 * tT, c01 = c010 * (1 - tT) + c011 * tT;
+        const double c10 = c100 * (1 - tT) + c101 * tT, c11 = c110 * (1 - tT) + c111 * tT;
+        const double c0 = c00 * (1 - tw) + c01 * tw, c1 = c10 * (1 - tw) + c11 * tw;
+        a.alpha[(j0 + jj) * L + l] += (c0 * (1 - tv) + c1 * tv) * p[4];
+    }
+}
+
+// per-temperature inputs of the cross-section precompute: n_e = 0, n_eff_vdW = NaN,
+// n/U = (1/cutoff_alpha) / U(T), continuum 1
+__global__ void molxs_layers_kernel(const double* inv_U, int nT, double cutoff_alpha, double* d) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nT) return;
+    d[t] = 0.0;
+    d[nT + t] = __longlong_as_double(0x7ff8000000000000LL);
+    d[2 * nT + t] = inv_U[t] / cutoff_alpha;
+    d[3 * nT + t] = 1.0;
+}
+
+// x[i] = *v * scale (a device scalar broadcast)
+__global__ void fill_kernel(double* x, int n, const double* v, double scale) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] = *v * scale;
+}
+
+__global__ void scale_kernel(double* x, int64_t n, double s) {
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+        x[i] *= s;
 }
 
 // ------------------------------------------------------------------ host staging
@@ -952,7 +1110,7 @@ KORG_API void korg_destroy(korg_ctx* ctx) {
     DevBuf* bufs[] = {&ctx->lines_scratch, &ctx->counters, &ctx->tune_alpha, &ctx->hrec, &ctx->hQ, &ctx->hQ32,
                       &ctx->hulb, &ctx->huub, &ctx->stage_dev, &ctx->aref, &ctx->alpha, &ctx->flux, &ctx->cntm,
                       &ctx->math, &ctx->b_alpha, &ctx->b_lines, &ctx->b_meta, &ctx->vjp_g, &ctx->vjp_dpar,
-                      &ctx->vjp_small, &ctx->vjp_hfd};
+                      &ctx->vjp_small, &ctx->vjp_hfd, &ctx->mx_layers};
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
     for (void* p : ctx->stark_allocs) cudaFree(p);
@@ -995,6 +1153,12 @@ KORG_API int korg_get_stats(korg_ctx* ctx, korg_stats* out) {
         ctx->stats.ms_line_tile = el(2, 5);
         ctx->stats.ms_rt = el(5, 6);
         ctx->stats.ms_total = el(0, 6);
+        if (ctx->vjp_timed) {
+            ctx->stats.ms_vjp_alpha = el(8, 9);
+            ctx->stats.ms_vjp_rt = el(9, 10);
+            ctx->stats.ms_vjp_hydrogen = el(10, 11);
+            ctx->stats.ms_vjp_lines = el(11, 12);
+        }
         cudaGetLastError();
     }
     *out = ctx->stats;
@@ -1436,6 +1600,59 @@ KORG_API int korg_synthesize_vjp(korg_ctx* ctx, const korg_synth_inputs* in, con
     return KORG_OK;
 }
 
+KORG_API int korg_molecular_cross_section_dev(korg_ctx* ctx, const korg_lines* lines, const double* wls,
+                                              int64_t nwl, const double* T, const double* inv_U, int32_t nT,
+                                              const double* vmic_vals, int32_t nv, double cutoff_alpha,
+                                              int precision, double* table, void* stream) {
+    if (!ctx) return KORG_EINVAL;
+    if (!lines || !wls || nwl < 1 || !T || !inv_U || nT < 1 || !vmic_vals || nv < 1 || !table || !(cutoff_alpha > 0))
+        return set_err(ctx, KORG_EINVAL, "bad arguments");
+    KCUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // the temperatures are the "layers" (src/molecular_cross_sections.jl:63-81): n_e = 0, the
+    // molecule's n / U = (1 / cutoff_alpha) / U(T), continuum 1 and cutoff threshold 1, so a line
+    // is truncated where its absorption coefficient per molecule falls to cutoff_alpha; the vdW
+    // perturber density is NaN (molecular lines have no vdW broadening)
+    const size_t bytes = sizeof(double) * 6 * size_t(nT);
+    KCHECK(ensure(ctx, ctx->mx_layers, bytes));
+    double* d = static_cast<double*>(ctx->mx_layers.p);
+    double* xi = d + 4 * nT;
+    molxs_layers_kernel<<<(nT + 127) / 128, 128, 0, s>>>(inv_U, nT, cutoff_alpha, d);
+    KCUDA(cudaGetLastError());
+    KCHECK(reset_counters(ctx, s));
+    const LayersDev lay{nT, 1, T, d, d + nT, xi, d + 2 * nT};
+    const CntmDev cn{1, nullptr, d + 3 * nT};
+    const size_t slice = size_t(nwl) * nT;
+    KCUDA(cudaMemsetAsync(table, 0, sizeof(double) * slice * nv, s));
+    for (int v = 0; v < nv; v++) {
+        fill_kernel<<<(nT + 127) / 128, 128, 0, s>>>(xi, nT, vmic_vals + v, 1e5);  // km/s -> cm/s
+        KCUDA(cudaGetLastError());
+        KCHECK(run_line_absorption(ctx, table + v * slice, wls, nwl, lines_dev(lines), lay, cn, 1.0,
+                                   precision == KORG_MIXED, s));
+    }
+    scale_kernel<<<ctx->sms * 4, 256, 0, s>>>(table, int64_t(slice) * nv, cutoff_alpha);
+    KCUDA(cudaGetLastError());
+    return KORG_OK;
+}
+
+KORG_API int korg_interpolate_molecular_cross_section_dev(korg_ctx* ctx, double* alpha, const double* wls,
+                                                          int64_t nwl, int32_t L, const double* T,
+                                                          const double* vmic, const double* n,
+                                                          const double* table, const double* table_wls,
+                                                          int64_t ntw, const double* vmic_vals, int32_t nv,
+                                                          const double* log_temp_vals, int32_t nT, void* stream) {
+    if (!ctx) return KORG_EINVAL;
+    if (!alpha || !wls || nwl < 1 || L < 1 || !T || !vmic || !n || !table || !table_wls || ntw < 1 || !vmic_vals ||
+        nv < 1 || !log_temp_vals || nT < 1)
+        return set_err(ctx, KORG_EINVAL, "bad arguments");
+    KCUDA(cudaSetDevice(ctx->device));
+    const MolXsArgs ma{alpha, wls, nwl, L, T, vmic, n, table, table_wls, ntw, vmic_vals, nv, log_temp_vals, nT};
+    const size_t smem = sizeof(double) * 6 * size_t(L);
+    molxs_interp_kernel<<<unsigned((nwl + 63) / 64), 256, smem, static_cast<cudaStream_t>(stream)>>>(ma);
+    KCUDA(cudaGetLastError());
+    return KORG_OK;
+}
+
 KORG_API int korg_set_batch_options(korg_ctx* ctx, int use_graph, int autotune, int64_t max_scratch_bytes) {
     if (!ctx) return KORG_EINVAL;
     if (max_scratch_bytes < 0) return set_err(ctx, KORG_EINVAL, "negative scratch budget");
@@ -1447,13 +1664,29 @@ KORG_API int korg_set_batch_options(korg_ctx* ctx, int use_graph, int autotune, 
 }
 
 KORG_API int korg_get_tile_config(korg_ctx* ctx, int32_t L, int precision, int32_t* tw, int32_t* stage,
-                                  int32_t* tuned) {
+                                  int32_t* split, int32_t* tuned) {
     if (!ctx || !tw || !stage) return KORG_EINVAL;
     const bool mixed = precision == KORG_MIXED;
     const TileCfg c = tile_cfg(ctx, L, mixed);
     *tw = c.tw;
     *stage = c.stage > 0 ? c.stage : (mixed ? STAGE_LINES : STAGE_LINES / 2);
+    if (split) *split = c.split;
     if (tuned) *tuned = ctx->tuned.count(std::make_pair(int(L), int(mixed))) ? 1 : 0;
+    return KORG_OK;
+}
+
+KORG_API int korg_set_tile_config(korg_ctx* ctx, int32_t L, int precision, int32_t tw, int32_t stage,
+                                  int32_t split) {
+    if (!ctx) return KORG_EINVAL;
+    const bool mixed = precision == KORG_MIXED;
+    int kmax = 0;
+    const int G = layer_groups(L, &kmax);
+    TileGeom g;
+    if (G < 0 || !tile_geom(mixed, G * kmax, G, TileCfg{tw, stage, split ? 1 : 0}, &g))
+        return set_err(ctx, KORG_EINVAL, "tile shape (tw %d, stage %d, split %d) is not valid for %d layers", tw,
+                       stage, split, L);
+    drop_graph(ctx);
+    ctx->tuned[std::make_pair(int(L), int(mixed))] = TileCfg{tw, stage, split ? 1 : 0};
     return KORG_OK;
 }
 
@@ -1669,30 +1902,27 @@ int noalloc_setup(int dev, unsigned char** out) {
     return KORG_OK;
 }
 
+// The context's default tile shape (TILE_TW wavelengths, one layer group per CTA), so results
+// equal korg_line_absorption_dev's.
 template <bool MIXED, int KMAX, int MAXT, int MINB>
 int noalloc_launch_tile(TileArgs ta, int G, cudaStream_t s) {
-    using P = typename ParamT<MIXED>::type;
-    const int Lp = ta.Lp;
-    const int B = MIXED ? STAGE_LINES : STAGE_LINES / 2;
-    ta.stage = B;
+    TileGeom g;
+    if (!tile_geom(MIXED, ta.Lp, G, TileCfg{TILE_TW, 0, 1}, &g)) return KORG_EINVAL;
+    ta.stage = g.stage;
+    ta.region = g.region;
+    ta.split = g.split;
     ta.G = G;
-    const int TW = TILE_TW, threads = TW * G;
-    size_t region = size_t(B) * Lp * sizeof(P);
-    region = std::max(region, (size_t(TW) * (Lp + 1) * sizeof(double) + 1) / 2);
-    region = (region + 15) & ~size_t(15);
-    ta.region = int(region);
-    const size_t smem = 2 * region + size_t(threads) * sizeof(LineStage);
     auto kern = line_tile_kernel<MIXED, KMAX, MAXT, MINB>;
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess)
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g.smem)) != cudaSuccess)
         return KORG_ECUDA;
-    kern<<<dim3(unsigned((ta.nwl + TW - 1) / TW)), threads, smem, s>>>(ta);
+    kern<<<dim3(unsigned((ta.nwl + g.tw - 1) / g.tw), unsigned(G)), g.threads, g.smem, s>>>(ta);
     return cudaGetLastError() == cudaSuccess ? KORG_OK : KORG_ECUDA;
 }
 
 template <bool MIXED>
 int noalloc_dispatch_tile(const TileArgs& ta, int G, int kmax, cudaStream_t s) {
-    if (kmax == 14 && G <= 4) return noalloc_launch_tile<MIXED, 14, 256, MIXED ? 3 : 2>(ta, G, s);
-    if (kmax == 14) return noalloc_launch_tile<MIXED, 14, 512, 1>(ta, G, s);
+    // one layer group per CTA: TILE_TW threads, the variant run_tiles picks for that count
+    if (kmax == 14) return noalloc_launch_tile<MIXED, 14, 256, MIXED ? 3 : 2>(ta, G, s);
     if (kmax == 16) return noalloc_launch_tile<MIXED, 16, 512, 1>(ta, G, s);
     return noalloc_launch_tile<MIXED, 32, 512, 1>(ta, G, s);
 }

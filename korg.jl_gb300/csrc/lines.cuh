@@ -482,6 +482,7 @@ struct TileArgs {
     const double* wls;
     int64_t nwl;
     int32_t L, Lp, G, stage;  // layers, padded layers (G * K), layer groups, lines per batch
+    int32_t split;            // 1: each CTA takes one layer group of the tile (blockIdx.y / queue)
     int32_t region;           // bytes of one shared buffer of line constants (x2, double buffered)
     int64_t n;
     const double* wl;     // line centres
@@ -543,17 +544,21 @@ __device__ __forceinline__ double far_lorentz64(const P64& p, double x2) {
 // owns wavelength j and the K consecutive (padded) layers g*K .. g*K+K-1.  `smem` is the
 // dynamic shared memory of the launch (two line-constant buffers, then the LineStage array).
 template <bool MIXED, int K>
-__device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, unsigned char* smem) {
+__device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, int gsplit, unsigned char* smem) {
     using P = typename ParamT<MIXED>::type;
     const int L = a.L, Lp = a.Lp, G = a.G, B = a.stage;
-    double* s_alpha = reinterpret_cast<double*>(smem);                          // [TW][Lp+1], at the end
+    double* s_alpha = reinterpret_cast<double*>(smem);                          // [TW][SL+1], at the end
     LineStage* s_ln = reinterpret_cast<LineStage*>(smem + 2 * size_t(a.region));  // [blockDim]
     __shared__ int32_t s_warp[32];
     __shared__ int32_t s_count;
 
+    // gsplit >= 0: this CTA computes layer group gsplit only (its own candidate list, constants
+    // and barriers), so groups of cheap and expensive layers do not wait for each other
     const int tid = threadIdx.x, nthr = blockDim.x;
-    const int TW = nthr / G;
-    const int jl = tid % TW, g = tid / TW;
+    const int TW = gsplit >= 0 ? nthr : nthr / G;
+    const int jl = tid % TW, g = gsplit >= 0 ? gsplit : tid / TW;
+    const int SL = gsplit >= 0 ? K : Lp;       // layers of one staged line
+    const int goff = gsplit >= 0 ? 0 : g * K;  // this thread's first layer within a staged line
     const int64_t j0 = tile * TW;
     const int64_t jg = j0 + jl;
     const int64_t jlast = min(j0 + TW, a.nwl) - 1;
@@ -588,7 +593,8 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
     for (int k = 0; k < K; k++) { acc[k] = Acc(0); comp[k] = Acc(0); }
 
     const int warp = tid >> 5, lane = tid & 31, nwarps = nthr >> 5;
-    const int chunks16 = Lp * int(sizeof(P) / 16);  // 16-byte pieces of one line's constants
+    const int chunks16 = SL * int(sizeof(P) / 16);  // 16-byte pieces of one line's staged constants
+    const int64_t src0 = gsplit >= 0 ? int64_t(g) * K * int64_t(sizeof(P) / 16) : 0;
     for (int tier = 0; tier < NTIER; tier++)
     for (int64_t base = s_tier[tier][0]; base < s_tier[tier][1]; base += nthr) {
         const int64_t pidx = base + tid;
@@ -643,7 +649,8 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
                     const int b = e / chunks16, r = e - b * chunks16;
                     const int64_t li = s_ln[b0 + b].li;
                     cp_async16(buf + (size_t(b) * chunks16 + r) * 16,
-                               reinterpret_cast<const unsigned char*>(a.params) + (li * chunks16 + r) * 16);
+                               reinterpret_cast<const unsigned char*>(a.params) +
+                                   (li * Lp * int64_t(sizeof(P) / 16) + src0 + r) * 16);
                 }
             }
             cp_async_commit();
@@ -666,7 +673,7 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
                         const float x = fabsf((xj_hi - st.dhi) + (xj_lo - st.dlo));
                         const float x2 = x * x;
                         const float t = __fdividef(1.f, x2);
-                        const float4* pr = reinterpret_cast<const float4*>(s_par) + b * Lp + g * K;
+                        const float4* pr = reinterpret_cast<const float4*>(s_par) + b * SL + goff;
                         const uint32_t cls = (st.cls >> (2 * g)) & 3u;
                         if (cls == 1u) {
                             // every layer in the asymptotic wing: w/v^2 (1 + 1.5/v^2 + 3.75/v^4), 1/v^2 = c t
@@ -706,7 +713,7 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
                         const LineStage& st = s_ln[b0 + b];
                         if (jg < st.lb || jg > st.ub) continue;
                         const double x = fabs(wl_j - st.wl);
-                        const P64* pr = reinterpret_cast<const P64*>(s_par) + b * Lp + g * K;
+                        const P64* pr = reinterpret_cast<const P64*>(s_par) + b * SL + goff;
                         const uint32_t cls = (st.cls >> (2 * g)) & 3u;
                         if (cls != 0u) {
                             const double x2 = x * x, t = 1 / x2;
@@ -730,16 +737,24 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
         }
     }
     // alpha += accumulated lines, staged through shared memory for coalesced updates
-    const int stride = Lp + 1;
+    const int stride = SL + 1;
 #pragma unroll
     for (int k = 0; k < K; k++)
-        s_alpha[jl * stride + g * K + k] = MIXED ? double(acc[k]) - double(comp[k]) : double(acc[k]);
+        s_alpha[jl * stride + goff + k] = MIXED ? double(acc[k]) - double(comp[k]) : double(acc[k]);
     __syncthreads();
     const int64_t nj = jlast - j0 + 1;
     double* dst = a.alpha + j0 * L;
-    for (int64_t e = tid; e < nj * L; e += nthr) {
-        const int j = int(e / L), l = int(e - int64_t(j) * L);
-        dst[e] = dst[e] + s_alpha[j * stride + l];
+    if (gsplit >= 0) {
+        const int l0 = g * K, nk = min(K, L - l0);
+        for (int64_t e = tid; e < nj * nk; e += nthr) {
+            const int j = int(e / nk), k = int(e - int64_t(j) * nk);
+            dst[int64_t(j) * L + l0 + k] += s_alpha[j * stride + k];
+        }
+    } else {
+        for (int64_t e = tid; e < nj * L; e += nthr) {
+            const int j = int(e / L), l = int(e - int64_t(j) * L);
+            dst[e] = dst[e] + s_alpha[j * stride + l];
+        }
     }
 }
 
@@ -747,7 +762,7 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
 template <bool MIXED, int K, int MAXT, int MINB>
 __global__ void __launch_bounds__(MAXT, MINB) line_tile_kernel(TileArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
-    line_tile_body<MIXED, K>(a, blockIdx.x, smem);
+    line_tile_body<MIXED, K>(a, blockIdx.x, a.split ? int(blockIdx.y) : -1, smem);
 }
 
 // Work queue of (spectrum, tile) items for a batch of spectra on one wavelength grid.  Item k
@@ -756,7 +771,8 @@ __global__ void __launch_bounds__(MAXT, MINB) line_tile_kernel(TileArgs a) {
 struct TileQueue {
     const TileArgs* spec;        // [nspec], device
     int32_t nspec;
-    int64_t nitems;              // nspec * tiles
+    int32_t groups;              // layer groups per tile item (G when split, else 1)
+    int64_t nitems;              // nspec * tiles * groups
     unsigned long long* next;    // item counter, zero before the launch
 };
 
@@ -776,7 +792,8 @@ __global__ void __launch_bounds__(MAXT, MINB) line_tile_queue_kernel(TileQueue q
         __syncthreads();
         const long long it = s_item;
         if (it >= q.nitems) break;
-        line_tile_body<MIXED, K>(s_a, it / q.nspec, smem);
+        const long long r = it / q.nspec;
+        line_tile_body<MIXED, K>(s_a, r / q.groups, q.groups > 1 ? int(r % q.groups) : -1, smem);
         __syncthreads();  // s_a and s_item are rewritten for the next item
     }
 }

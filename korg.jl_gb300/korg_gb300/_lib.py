@@ -62,7 +62,7 @@ class SynthGrads(C.Structure):
                 ("nHe_I", _dp), ("UH_I", _dp), ("log_gf", _dp), ("cntm_vals", _dp), ("alpha_ref_cntm", _dp)]
 
 
-KORG_VJP_HYDROGEN = 1
+KORG_VJP_HYDROGEN, KORG_VJP_REUSE_FORWARD = 1, 2
 
 
 class BatchItem(C.Structure):
@@ -72,7 +72,8 @@ class BatchItem(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("line_evals", C.c_int64), ("lines_in_window", C.c_int64), ("ms_ref_lines", C.c_float),
                 ("ms_hydrogen", C.c_float), ("ms_line_prep", C.c_float), ("ms_line_tile", C.c_float),
-                ("ms_rt", C.c_float), ("ms_total", C.c_float)]
+                ("ms_rt", C.c_float), ("ms_total", C.c_float), ("ms_vjp_alpha", C.c_float),
+                ("ms_vjp_rt", C.c_float), ("ms_vjp_hydrogen", C.c_float), ("ms_vjp_lines", C.c_float)]
 
 
 _lib = None
@@ -116,13 +117,19 @@ def lib():
                                                        C.POINTER(Cntm), C.c_double, C.c_int, vp]
             L.korg_radiative_transfer_general.argtypes = [vp, _dp, _dp, C.c_int32, C.c_int64, _dp, C.c_int, _dp, _dp,
                                                           _dp, _dp, C.c_int32, C.c_int, C.c_int, C.c_int, _dp, _dp]
+            L.korg_molecular_cross_section_dev.argtypes = [vp, C.POINTER(Lines), vp, C.c_int64, vp, vp, C.c_int32, vp,
+                                                           C.c_int32, C.c_double, C.c_int, vp, vp]
+            L.korg_interpolate_molecular_cross_section_dev.argtypes = [vp, vp, vp, C.c_int64, C.c_int32, vp, vp, vp,
+                                                                       vp, vp, C.c_int64, vp, C.c_int32, vp,
+                                                                       C.c_int32, vp]
             L.korg_synthesize_vjp.argtypes = [vp, C.POINTER(SynthInputs), C.POINTER(Lines), C.POINTER(Lines), _dp,
                                               C.c_int64, C.c_int, _dp, _dp, C.POINTER(SynthGrads), C.c_int]
             L.korg_synthesize_vjp_dev.argtypes = [vp, C.POINTER(SynthInputs), C.POINTER(Lines), C.POINTER(Lines), vp,
                                                   C.c_int64, C.c_int, vp, vp, C.POINTER(SynthGrads), C.c_int, vp]
             L.korg_synthesize_batch_dev.argtypes = [vp, C.c_int32, C.POINTER(BatchItem), vp, C.c_int64, C.c_int, vp]
             L.korg_set_batch_options.argtypes = [vp, C.c_int, C.c_int, C.c_int64]
-            L.korg_get_tile_config.argtypes = [vp, C.c_int32, C.c_int, _ip, _ip, _ip]
+            L.korg_get_tile_config.argtypes = [vp, C.c_int32, C.c_int, _ip, _ip, _ip, _ip]
+            L.korg_set_tile_config.argtypes = [vp, C.c_int32, C.c_int, C.c_int32, C.c_int32, C.c_int32]
             _lib = L
     return _lib
 
@@ -134,8 +141,9 @@ def exported_symbols():
             "korg_hydrogen_line_absorption", "korg_hydrogen_lines_dev", "korg_radiative_transfer",
             "korg_radiative_transfer_dev", "korg_synthesize", "korg_synthesize_dev", "korg_probe_flops",
             "korg_math_selftest", "korg_line_absorption_noalloc", "korg_synthesize_batch_dev",
-            "korg_set_batch_options", "korg_get_tile_config", "korg_synthesize_vjp", "korg_synthesize_vjp_dev",
-            "korg_radiative_transfer_general"]
+            "korg_set_batch_options", "korg_get_tile_config", "korg_set_tile_config", "korg_synthesize_vjp", "korg_synthesize_vjp_dev",
+            "korg_radiative_transfer_general", "korg_molecular_cross_section_dev",
+            "korg_interpolate_molecular_cross_section_dev"]
 
 
 def _p(a, kind=_dp):

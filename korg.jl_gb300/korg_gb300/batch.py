@@ -136,7 +136,7 @@ class BatchSynthesis:
         return self.flux.cpu().numpy(), self.cntm.cpu().numpy()
 
     def tile_config(self):
-        tw, st, tu = C.c_int32(), C.c_int32(), C.c_int32()
+        tw, st, sp, tu = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
         self.ctx.check(self.ctx.lib.korg_get_tile_config(self.ctx.h, len(self.inputs[0].T), self.prec, C.byref(tw),
-                                                         C.byref(st), C.byref(tu)))
-        return {"tw": tw.value, "stage": st.value, "tuned": bool(tu.value)}
+                                                         C.byref(st), C.byref(sp), C.byref(tu)))
+        return {"tw": tw.value, "stage": st.value, "split": bool(sp.value), "tuned": bool(tu.value)}

@@ -366,10 +366,12 @@ GRAD_FIELDS = ("T", "ne", "n_eff_vdW", "xi", "n_div_U", "nH_I", "nHe_I", "UH_I",
 
 
 def synthesize_vjp(inp: SynthesisInputs, dflux, dcntm=None, precision="fp64", hydrogen=True, wanted=GRAD_FIELDS,
-                   ctx=None):
+                   reuse_forward=False, ctx=None):
     """Vector-Jacobian product of :func:`synthesize_prepared` (korg_synthesize_vjp): the
     gradient of sum(dflux * flux + dcntm * cntm) with respect to the hot-path inputs, as a dict
-    keyed by GRAD_FIELDS (shapes: [L], n_div_U [S, L], log_gf [n lines], cntm_vals [L, nk])."""
+    keyed by GRAD_FIELDS (shapes: [L], n_div_U [S, L], log_gf [n lines], cntm_vals [L, nk]).
+    reuse_forward: the previous call on ``ctx`` was synthesize_prepared of the same inputs and
+    precision; its opacity is reused instead of recomputed."""
     ctx = ctx or _lib.default_context()
     if inp.hydrogen_lines:
         ctx.ensure_stark()
@@ -386,7 +388,8 @@ def synthesize_vjp(inp: SynthesisInputs, dflux, dcntm=None, precision="fp64", hy
     w = keep.f64(inp.wls.all_wls)
     ctx.check(ctx.lib.korg_synthesize_vjp(ctx.h, C.byref(s), C.byref(lines), C.byref(lines5), _lib._p(w), nwl,
                                           _prec(precision), _lib._p(df), _lib._p(dc), C.byref(g),
-                                          _lib.KORG_VJP_HYDROGEN if hydrogen else 0))
+                                          (_lib.KORG_VJP_HYDROGEN if hydrogen else 0) |
+                                          (_lib.KORG_VJP_REUSE_FORWARD if reuse_forward else 0)))
     return out
 
 
@@ -396,12 +399,14 @@ def rectified_loss(flux, cntm, obs):
     return float(np.sum(r * r)), 2 * r / cntm, -2 * r * flux / cntm ** 2
 
 
-def loss_and_gradient(inp: SynthesisInputs, obs, precision="fp64", hydrogen=True, ctx=None):
+def loss_and_gradient(inp: SynthesisInputs, obs, precision="fp64", hydrogen=True, reuse_forward=False, ctx=None):
     """Rectified-flux least squares against ``obs`` and its gradient with respect to the
     hot-path inputs (a forward synthesis, then the reverse mode)."""
+    ctx = ctx or _lib.default_context()
     res = synthesize_prepared(inp, precision=precision, ctx=ctx)
     loss, dF, dC = rectified_loss(res.flux, res.cntm, obs)
-    return loss, synthesize_vjp(inp, dF, dC, precision=precision, hydrogen=hydrogen, ctx=ctx)
+    return loss, synthesize_vjp(inp, dF, dC, precision=precision, hydrogen=hydrogen, reuse_forward=reuse_forward,
+                                ctx=ctx)
 
 
 def physical_gradient(inp: SynthesisInputs, g, vmic_scalar=True):

@@ -82,3 +82,31 @@ def test_batch_autotuner_picks_a_shape_and_keeps_results(gpu_lib):
     # another tile shape changes the FP32 rounding of the offsets and the Kahan batches only
     np.testing.assert_allclose(f1, f0, rtol=2e-6, atol=0)
     np.testing.assert_allclose(c1, c0, rtol=2e-6, atol=0)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_tile_shapes_give_identical_opacity(gpu_lib, precision):
+    """Splitting the layer groups over CTAs keeps every thread's accumulation order: the FP64
+    opacity is bitwise unchanged (mixed: to FP32 rounding, the compiler may contract the split
+    path differently).  Other tile widths move the tile origins (mixed offsets) and the batch
+    boundaries only."""
+    import ctypes as C
+    from korg_gb300 import synthetic
+    from korg_gb300.synthesize import synthesize_prepared
+    inp = synthetic.prepare(synthetic.config0(n_lines=3000))
+    prec = gpu_lib.KORG_MIXED if precision == "mixed" else gpu_lib.KORG_FP64
+    L = len(inp.T)
+    out = {}
+    for cfg in ((64, 0, 0), (64, 0, 1), (32, 16, 1), (128, 0, 0)):
+        ctx = gpu_lib.Context(0)
+        ctx.check(ctx.lib.korg_set_tile_config(ctx.h, L, prec, *cfg))
+        r = synthesize_prepared(inp, precision=precision, return_alpha=True, ctx=ctx)
+        out[cfg] = r
+        ctx.close()
+    base = out[(64, 0, 0)]
+    if precision == "fp64":
+        assert np.array_equal(out[(64, 0, 1)].alpha, base.alpha)
+    else:
+        np.testing.assert_allclose(out[(64, 0, 1)].alpha, base.alpha, rtol=1e-6)
+    for cfg in ((32, 16, 1), (128, 0, 0)):
+        np.testing.assert_allclose(out[cfg].alpha, base.alpha, rtol=1e-5 if precision == "mixed" else 1e-13)
