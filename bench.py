@@ -62,6 +62,7 @@ def parse():
     ap.add_argument("--workload", default="synth", choices=["synth", "batch", "adjoint", "variants"])
     ap.add_argument("--tile", default=None, help="force the line tile shape: tw,stage,split (e.g. 64,32,1)")
     ap.add_argument("--spectra", type=int, default=256, help="batch workload: number of spectra")
+    ap.add_argument("--adj-scale", type=float, default=1.0, help="adjoint workload: fraction of its 70k lines")
     return ap.parse_args()
 
 
@@ -623,7 +624,8 @@ def run_adjoint(args):
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
     _progress("preparing the adjoint configuration")
-    inp = synthetic.prepare(synthetic.config2())
+    inp = synthetic.prepare(synthetic.config2(n_atomic=int(50_000 * args.adj_scale),
+                                              n_mol=int(20_000 * args.adj_scale)))
     nwl, L = len(inp.wls), len(inp.T)
     ctx = _lib.Context(0)
     ctx.ensure_stark()

@@ -41,9 +41,11 @@ template <class R>
 __device__ __forceinline__ Dual<R> operator*(Dual<R> p, Dual<R> q) {
     return {p.x * q.x, p.da * q.x + p.x * q.da, p.dv * q.x + p.x * q.dv};
 }
+__device__ __forceinline__ float recip(float x) { return __fdividef(1.f, x); }
+__device__ __forceinline__ double recip(double x) { return 1.0 / x; }
 template <class R>
 __device__ __forceinline__ Dual<R> operator/(Dual<R> p, Dual<R> q) {
-    const R inv = R(1) / q.x, r = p.x * inv;
+    const R inv = recip(q.x), r = p.x * inv;
     return {r, (p.da - r * q.da) * inv, (p.dv - r * q.dv) * inv};
 }
 template <class R>
@@ -60,8 +62,8 @@ template <class R>
 __device__ __forceinline__ Dual<R> operator*(Dual<R> p, R c) { return {c * p.x, c * p.da, c * p.dv}; }
 template <class R>
 __device__ __forceinline__ Dual<R> operator/(R c, Dual<R> q) {
-    const R r = c / q.x;
-    return {r, -r / q.x * q.da, -r / q.x * q.dv};
+    const R iq = recip(q.x), r = c * iq;
+    return {r, -r * iq * q.da, -r * iq * q.dv};
 }
 __device__ __forceinline__ double dexp(double x) { return exp(x); }
 __device__ __forceinline__ float dexp(float x) { return __expf(x); }
@@ -414,8 +416,20 @@ struct AdjSums {
     __device__ __forceinline__ double get(int k) const { return double(s[k]) - double(c[k]); }
 };
 
-// One block per item: thread (l = tid mod L, jr = tid / L) walks every NJ-th wavelength of the
-// chunk for layer l, so a warp reads consecutive G entries (layer fastest) and no lane idles.
+__device__ __forceinline__ void cp_async4(void* smem_dst, const void* gmem_src) {
+    const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* smem_dst, const void* gmem_src) {
+    const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(gmem_src) : "memory");
+}
+
+constexpr int ADJ_SUB = 64;  // wavelengths of G staged in shared memory at a time
+
+// One block per item.  The item's G rows (contiguous: ADJ_SUB wavelengths x L layers) are
+// copied to shared memory with cp.async, double buffered, and thread (l = tid mod L,
+// jr = tid / L) walks every NJ-th staged wavelength for layer l.
 // In the asymptotic wing (a <= 0.2, v >= 5: most evaluations of a wide window)
 // H = a/sqrt(pi) u (1 + 1.5u + 3.75u^2) with u = 1/v^2 = c t (c = 2 sigma^2, t = 1/|dl|^2), so
 // the three window sums follow from the moments M_k = sum G u^k, k = 1..3 (three FMAs per
@@ -425,14 +439,17 @@ struct AdjSums {
 template <bool MIXED>
 __global__ void __launch_bounds__(512) line_adj_kernel(LineAdjArgs a) {
     using R = typename std::conditional<MIXED, float, double>::type;
+    using GT = typename std::conditional<MIXED, float, double>::type;  // G element (g32 == MIXED)
     __shared__ long long s_item;
     __shared__ int64_t s_cnt[NTIER + 1];
-    __shared__ R s_x[ADJ_CHUNK];       // |wl_j - wl0| of the item's wavelengths
-    extern __shared__ double s_red[];  // [6][NJ][L] partial sums
+    __shared__ R s_x[2][ADJ_SUB];
+    extern __shared__ __align__(16) unsigned char s_adj[];  // [2][ADJ_SUB][L] G, then [3][NJ][L] sums
     const int L = a.L, Lp = a.Lp;
     const int NJ = blockDim.x / L;
     const int l = threadIdx.x % L, jr = threadIdx.x / L;
     const bool active = jr < NJ;
+    GT* s_g = reinterpret_cast<GT*>(s_adj);
+    double* s_red = reinterpret_cast<double*>(s_adj + sizeof(GT) * 2 * ADJ_SUB * L);
     if (threadIdx.x == 0) {
         int64_t acc = 0;
         for (int t = NTIER - 1; t >= 0; t--) {
@@ -443,10 +460,12 @@ __global__ void __launch_bounds__(512) line_adj_kernel(LineAdjArgs a) {
     }
     __syncthreads();
     const int64_t total = s_cnt[NTIER];
+    const GT* G = static_cast<const GT*>(a.G);
     for (;;) {
         if (threadIdx.x == 0) s_item = (long long)atomicAdd(a.next, 1ull);
         __syncthreads();
         const int64_t it = s_item;
+        __syncthreads();  // everyone has read s_item
         if (it >= total) break;
         int q = 0;
         while (it >= s_cnt[q + 1]) q++;
@@ -456,31 +475,60 @@ __global__ void __launch_bounds__(512) line_adj_kernel(LineAdjArgs a) {
         const int64_t i = a.tier_idx[a.tier_start[tier] + rel / nch];
         const int64_t j0 = int64_t(a.lb[i]) + (rel % nch) * ADJ_CHUNK;
         const int64_t j1 = min(int64_t(a.ub[i]), j0 + ADJ_CHUNK - 1);
+        if (j0 > j1) continue;  // uniform across the block
         const double wl0 = a.wl[i];
-        for (int64_t j = j0 + threadIdx.x; j <= j1; j += blockDim.x) s_x[j - j0] = R(fabs(a.wls[j] - wl0));
-        __syncthreads();  // s_x filled; s_item read by everyone
-        if (j0 <= j1) {
-            AdjSums<MIXED, 3> cen;  // central evaluations: G H, G (a H_a + v H_v), G H_a
-            AdjSums<MIXED, 3> mom;  // wing moments M1, M2, M3
-            R s = R(1), av = R(0);
-            if (active) {
-                if (MIXED) {
-                    const float4 p = reinterpret_cast<const float4*>(a.params)[i * Lp + l];
-                    s = R(rsqrtf(p.x));
-                    av = R(p.y);
+        const int64_t nj = j1 - j0 + 1;
+        const int nsub = int((nj + ADJ_SUB - 1) / ADJ_SUB);
+        // stage sub-chunk q of the item's wavelengths into buffer q & 1
+        auto issue = [&](int sq) {
+            if (sq < nsub) {
+                const int64_t js = j0 + int64_t(sq) * ADJ_SUB;
+                const int nw = int(min(int64_t(ADJ_SUB), j1 - js + 1));
+                GT* dst = s_g + size_t(sq & 1) * ADJ_SUB * L;
+                const GT* src = G + js * L;
+                const int ne = nw * L;
+                if ((L * int(sizeof(GT))) % 16 == 0) {  // every row start is 16-byte aligned
+                    constexpr int V = 16 / int(sizeof(GT));
+                    for (int e = threadIdx.x * V; e < ne; e += blockDim.x * V) cp_async16(dst + e, src + e);
                 } else {
-                    const P64 p = reinterpret_cast<const P64*>(a.params)[i * Lp + l];
-                    s = R(p.inv_s);
-                    av = R(p.a);
+                    for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+                        if (MIXED) cp_async4(dst + e, src + e);
+                        else cp_async8(dst + e, src + e);
+                    }
                 }
-                const R c2 = R(1) / (s * s);                         // 2 sigma^2
-                const R xw = av <= R(0.2) ? R(5) / s : R(3.0e38);    // wing starts at v = 5
-                const int64_t nj = j1 - j0 + 1;
-                const int64_t step = int64_t(NJ) * L;
-                const float* g32p = static_cast<const float*>(a.G) + (j0 + jr) * L + l;
-                const double* g64p = static_cast<const double*>(a.G) + (j0 + jr) * L + l;
+                if (threadIdx.x < nw) s_x[sq & 1][threadIdx.x] = R(fabs(a.wls[js + threadIdx.x] - wl0));
+            }
+            cp_async_commit();
+        };
+        AdjSums<MIXED, 3> cen;  // central evaluations: G H, G (a H_a + v H_v), G H_a
+        AdjSums<MIXED, 3> mom;  // wing moments M1, M2, M3
+        R s = R(1), av = R(0), c2 = R(1), xw = R(3.0e38);
+        if (active) {
+            if (MIXED) {
+                const float4 p = reinterpret_cast<const float4*>(a.params)[i * Lp + l];
+                s = R(rsqrtf(p.x));
+                av = R(p.y);
+            } else {
+                const P64 p = reinterpret_cast<const P64*>(a.params)[i * Lp + l];
+                s = R(p.inv_s);
+                av = R(p.a);
+            }
+            c2 = R(1) / (s * s);                   // 2 sigma^2
+            if (av <= R(0.2)) xw = R(5) / s;       // the wing starts at v = 5
+        }
+        issue(0);
+        for (int sq = 0; sq < nsub; sq++) {
+            issue(sq + 1);
+            cp_async_wait_1();
+            __syncthreads();
+            const int nw = int(min(int64_t(ADJ_SUB), nj - int64_t(sq) * ADJ_SUB));
+            const GT* gb = s_g + size_t(sq & 1) * ADJ_SUB * L;
+            const R* xb = s_x[sq & 1];
+            if (active) {
                 R pc[3] = {0, 0, 0}, pm[3] = {0, 0, 0};
-                auto eval = [&](R g, R x) {
+                for (int jj = jr; jj < nw; jj += NJ) {
+                    const R g = R(gb[jj * L + l]);
+                    const R x = xb[jj];
                     if (x >= xw) {
                         const R u = fast_div(c2, x * x);
                         const R gu = g * u, gu2 = gu * u;
@@ -493,59 +541,39 @@ __global__ void __launch_bounds__(512) line_adj_kernel(LineAdjArgs a) {
                         pc[1] += g * (av * d.da + x * s * d.dv);
                         pc[2] += g * d.da;
                     }
-                };
-                // groups of 4 independent loads in flight, partial sums flushed every 32 terms
-                constexpr int U = 4;
-                int64_t jj = jr;
-                int cnt = 0;
-                for (; jj + (U - 1) * NJ < nj; jj += U * NJ) {
-                    R g[U];
-#pragma unroll
-                    for (int u = 0; u < U; u++)
-                        g[u] = a.g32 ? R(g32p[u * step]) : R(g64p[u * step]);
-                    g32p += U * step;
-                    g64p += U * step;
-#pragma unroll
-                    for (int u = 0; u < U; u++) eval(g[u], s_x[jj + u * NJ]);
-                    cnt += U;
-                    if (cnt >= 32) {
-                        cen.add(pc);
-                        mom.add(pm);
-                        pc[0] = pc[1] = pc[2] = pm[0] = pm[1] = pm[2] = R(0);
-                        cnt = 0;
-                    }
-                }
-                for (; jj < nj; jj += NJ) {
-                    eval(a.g32 ? R(*g32p) : R(*g64p), s_x[jj]);
-                    g32p += step;
-                    g64p += step;
                 }
                 cen.add(pc);
                 mom.add(pm);
             }
-            // window sums of this thread: central + wing (from the moments)
-            if (active) {
-                const double k = 0.5641895835477563 * double(av);  // a / sqrt(pi)
-                const double M1 = mom.get(0), M2 = mom.get(1), M3 = mom.get(2);
-                const double wH = k * (M1 + 1.5 * M2 + 3.75 * M3);
-                const double wA = 0.5641895835477563 * (M1 + 1.5 * M2 + 3.75 * M3);
-                const double wX = wH - 2 * k * (M1 + 3 * M2 + 11.25 * M3);
-                s_red[(0 * NJ + jr) * L + l] = cen.get(0) + wH;
-                s_red[(1 * NJ + jr) * L + l] = cen.get(1) + wX;
-                s_red[(2 * NJ + jr) * L + l] = cen.get(2) + wA;
-            }
-            __syncthreads();
-            if (active && jr == 0) {
-                double* dp = a.dpar + (i * Lp + l) * 3;
-                for (int k = 0; k < 3; k++) {
-                    double t = 0.0;
-                    for (int r = 0; r < NJ; r++) t += s_red[(k * NJ + r) * L + l];
-                    atomicAdd(dp + k, t);
-                }
+            __syncthreads();  // buffer sq & 1 is refilled by issue(sq + 2)
+        }
+        // window sums of this thread: central + wing (from the moments)
+        if (active) {
+            const double k = 0.5641895835477563 * double(av);  // a / sqrt(pi)
+            const double M1 = mom.get(0), M2 = mom.get(1), M3 = mom.get(2);
+            const double wH = k * (M1 + 1.5 * M2 + 3.75 * M3);
+            const double wA = 0.5641895835477563 * (M1 + 1.5 * M2 + 3.75 * M3);
+            const double wX = wH - 2 * k * (M1 + 3 * M2 + 11.25 * M3);
+            s_red[(0 * NJ + jr) * L + l] = cen.get(0) + wH;
+            s_red[(1 * NJ + jr) * L + l] = cen.get(1) + wX;
+            s_red[(2 * NJ + jr) * L + l] = cen.get(2) + wA;
+        }
+        __syncthreads();
+        if (active && jr == 0) {
+            double* dp = a.dpar + (i * Lp + l) * 3;
+            for (int k = 0; k < 3; k++) {
+                double t = 0.0;
+                for (int r = 0; r < NJ; r++) t += s_red[(k * NJ + r) * L + l];
+                atomicAdd(dp + k, t);
             }
         }
-        __syncthreads();  // s_x, s_red and s_item are rewritten for the next item
+        __syncthreads();  // s_red is rewritten by the next item
     }
+}
+
+// Dynamic shared memory of line_adj_kernel: two staged G buffers and the partial sums.
+inline size_t adj_smem(int L, int threads, bool mixed) {
+    return (mixed ? sizeof(float) : sizeof(double)) * 2 * ADJ_SUB * size_t(L) + sizeof(double) * 3 * size_t(threads);
 }
 
 // Threads per block of line_adj_kernel for L layers: L * NJ, the smallest multiple of 32 that

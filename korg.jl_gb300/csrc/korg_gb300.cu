@@ -686,6 +686,11 @@ std::vector<unsigned char> batch_key(korg_ctx* ctx, int nspec, const korg_batch_
 }
 
 // ------------------------------------------------------------------ reverse mode (VJP)
+__global__ void to_float_kernel(const double* x, int64_t n, float* y) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = float(x[i]);
+}
+
 // h[l] = sign * x[l] / 2 (hydro_fd_contract_kernel then divides by 2 h = sign * x)
 __global__ void hfd_half_kernel(const double* x, int L, double sign, double* h) {
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
@@ -729,7 +734,7 @@ int run_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& ln, cons
     KCHECK(ensure(ctx, ctx->vjp_dpar, sizeof(double) * 3 * size_t(nmax) * Lp));
     // small pieces: daref [L], a scratch dT [L], hydrogen FD inputs [2][6][L], steps [L], counter
     const size_t o_dar = 0, o_dT = a256(8 * L), o_hin = o_dT + a256(8 * L), o_h = o_hin + a256(8 * 12 * L),
-                 o_ctr = o_h + a256(8 * L), small = o_ctr + 256;
+                 o_ctr = o_h + a256(8 * L), o_g32 = o_ctr + 256, small = o_g32 + a256(4 * L);
     KCHECK(ensure(ctx, ctx->vjp_small, small));
     unsigned char* sm = static_cast<unsigned char*>(ctx->vjp_small.p);
     double* daref = reinterpret_cast<double*>(sm + o_dar);
@@ -849,22 +854,34 @@ int run_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& ln, cons
 
     // 4. metal and molecular lines: window sums per (line, layer), then the prologue chain rule
     const LineAdjOut lo{dT, gr.ne, gr.n_eff_vdW, gr.xi, gr.n_div_U, gr.log_gf};
-    auto line_adjoint = [&](const LinesDev& lns, const void* Gp, int g32, const double* w, int64_t nw,
+    auto line_adjoint = [&](const LinesDev& lns, const void* Gp, int g32_in, const double* w, int64_t nw,
                             const LineAdjOut& out) -> int {
         if (lns.n == 0) return KORG_OK;
+        if (mixed && !g32_in) {  // the mixed kernel stages float G: convert (a few values)
+            float* g32buf = reinterpret_cast<float*>(sm + o_g32);
+            to_float_kernel<<<unsigned((nw * L + 255) / 256), 256, 0, s>>>(static_cast<const double*>(Gp), nw * L,
+                                                                         g32buf);
+            KCUDA(cudaGetLastError());
+            Gp = g32buf;
+            g32_in = 1;
+        }
         LineScratch sc;
         line_scratch(static_cast<unsigned char*>(ctx->lines_scratch.p), lns.n, L, Lp, G, mixed, &sc);
         double* dpar = static_cast<double*>(ctx->vjp_dpar.p);
         KCUDA(cudaMemsetAsync(dpar, 0, sizeof(double) * 3 * size_t(lns.n) * Lp, s));
         KCUDA(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), s));
-        LineAdjArgs la{Gp, g32, w, nw, L, Lp, lns.wl, sc.params, sc.lb, sc.ub, sc.tier_idx, sc.tier_meta, dpar, ctr};
+        LineAdjArgs la{Gp, g32_in, w, nw, L, Lp, lns.wl, sc.params, sc.lb, sc.ub, sc.tier_idx, sc.tier_meta, dpar,
+                       ctr};
         const int threads = adj_threads(L);
-        const size_t smem = sizeof(double) * 3 * threads;
+        if ((g32_in != 0) != mixed) return set_err(ctx, KORG_EINVAL, "opacity cotangent precision mismatch");
+        const size_t smem = adj_smem(L, threads, mixed);
         int per_sm = 0;
         if (mixed) {
+            KCUDA(cudaFuncSetAttribute(line_adj_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
             KCUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, line_adj_kernel<true>, threads, smem));
             line_adj_kernel<true><<<ctx->sms * std::max(per_sm, 1), threads, smem, s>>>(la);
         } else {
+            KCUDA(cudaFuncSetAttribute(line_adj_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
             KCUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, line_adj_kernel<false>, threads, smem));
             line_adj_kernel<false><<<ctx->sms * std::max(per_sm, 1), threads, smem, s>>>(la);
         }

@@ -565,6 +565,7 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
     const bool live = jg < a.nwl;
     const double wl_j = live ? a.wls[jg] : 0.0;
     const double wl_ref = a.wls[j0], wl_last = a.wls[jlast];
+    const float span32 = float(wl_last - wl_ref);
     // mixed precision: offsets from the tile's first wavelength formed in FP64 and kept as
     // FP32 hi + lo pairs, so |wl_j - wl0| is recovered in FP32 to about one rounding
     const float xj_hi = float(wl_j - wl_ref);
@@ -620,12 +621,17 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
             LineStage st;
             const double wl0 = a.wl[i], d = wl0 - wl_ref;
             const float dh = float(d);
-            const double dist = wl0 < wl_ref ? wl_ref - wl0 : (wl0 > wl_last ? wl0 - wl_last : 0.0);
+            // distance of the centre from the tile; in FP32 for the mixed form (xfar carries a
+            // 1e-4 relative margin, far above the rounding), so only the offset itself is FP64
+            const float fdist = dh < 0.f ? -dh : (dh > span32 ? dh - span32 : 0.f);
+            const double dist = MIXED ? double(fdist)
+                                      : (wl0 < wl_ref ? wl_ref - wl0 : (wl0 > wl_last ? wl0 - wl_last : 0.0));
             const uint32_t am = a.amask[i];
             uint32_t cls = 0;
-            for (int gg = 0; gg < G; gg++) {
+            const int g_lo = gsplit >= 0 ? gsplit : 0, g_hi = gsplit >= 0 ? gsplit + 1 : G;
+            for (int gg = g_lo; gg < g_hi; gg++) {
                 const float xf = a.xfar[i * G + gg];
-                if (dist > double(xf)) cls |= (((am >> gg) & 1u) ? 1u : 2u) << (2 * gg);
+                if (MIXED ? fdist > xf : dist > double(xf)) cls |= (((am >> gg) & 1u) ? 1u : 2u) << (2 * gg);
             }
             st.wl = wl0;
             st.dhi = dh;
