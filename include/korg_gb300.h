@@ -213,7 +213,8 @@ KORG_API int korg_synthesize_dev(korg_ctx *ctx, const korg_synth_inputs *in,
  * equilibrium, partition functions and continuum (T -> n, U, alpha_cntm) is the caller's.
  * alpha is recomputed (not stored by the forward call); the line windows carry no derivative,
  * as under ForwardDiff.  With KORG_VJP_HYDROGEN the hydrogen-line opacity contributes too,
- * through central differences of the FP64 hydrogen kernel (its Jacobian is layer diagonal);
+ * through forward differences of the FP64 hydrogen kernel (its Jacobian is layer diagonal;
+ * the U(H I) and, without MHD, n(H I) derivatives are exact);
  * without it, hydrogen lines are held fixed. */
 typedef struct {
     double *T, *ne, *n_eff_vdW, *xi;

@@ -425,24 +425,67 @@ __device__ __forceinline__ void cp_async8(void* smem_dst, const void* gmem_src) 
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(gmem_src) : "memory");
 }
 
+// Far-Lorentz branch of voigt_hjerting (line_absorption.jl:305-308: a > 1.4, or a > 0.2 with
+// a + v >= 3.2) with its derivatives in closed form: H, X = a H_a + v H_v and A = H_a.  With
+// r^2 = v^2/a^2 (degree 0) and au = 1/(sqrt2 a (1 + r^2)) (degree -1), H = C au (1 + P b + Q b^2),
+// b = au^2, P = 3r^2 - 1, Q = 15r^4 - 30r^2 + 2:  X = -C au (1 + 3P b + 5Q b^2), and
+// A = C au/a [w (1 + P b + Q b^2) + b (-6r^2 + 2P w) + b^2 (-60 r^2 (r^2 - 1) + 4Q w)] with
+// w = (r^2 - 1)/(r^2 + 1).
+template <class R>
+__device__ __forceinline__ void far_lorentz_d(R a, R v, R& H, R& X, R& A) {
+    const R ia = recip(a);
+    const R r2 = v * v * ia * ia;
+    const R iz = recip(R(1) + r2);
+    const R au = R(0.70710678118654752) * ia * iz;
+    const R b = au * au;
+    const R P = R(3) * r2 - R(1);
+    const R Q = (r2 - R(2)) * R(15) * r2 + R(2);
+    const R Cau = R(0.7978845608028654) * au;
+    const R poly = R(1) + (P + Q * b) * b;
+    const R w = (r2 - R(1)) * iz;
+    H = Cau * poly;
+    X = -Cau * (R(1) + (R(3) * P + R(5) * Q * b) * b);
+    A = Cau * ia * (w * poly + (R(-6) * r2 + R(2) * P * w) * b + (R(-60) * r2 * (r2 - R(1)) + R(4) * Q * w) * b * b);
+}
+
+// H, a H_a + v H_v and H_a of every branch but the asymptotic wing: far Lorentz in closed form,
+// the Harris branches through dual numbers.
+template <class R>
+__device__ __forceinline__ void central_derivs(R av, R v, R* out) {
+    R H, X, A;
+    if (av > R(0.2) && (av > R(1.4) || av + v >= R(3.2))) {
+        far_lorentz_d<R>(av, v, H, X, A);
+    } else {
+        const Dual<R> d = voigt_dual<R>(av, v);
+        H = d.x;
+        A = d.da;
+        X = av * d.da + v * d.dv;
+    }
+    out[0] = H;
+    out[1] = X;
+    out[2] = A;
+}
+
 constexpr int ADJ_SUB = 64;  // wavelengths of G staged in shared memory at a time
 
-// One block per item.  The item's G rows (contiguous: ADJ_SUB wavelengths x L layers) are
-// copied to shared memory with cp.async, double buffered, and thread (l = tid mod L,
-// jr = tid / L) walks every NJ-th staged wavelength for layer l.
+// One block per item (a line and a chunk of its window).  The item's G rows (ADJ_SUB wavelengths
+// x L layers, contiguous in global memory) are copied to shared memory with cp.async, double
+// buffered, with 1/|dl|^2 of every staged wavelength; thread (l = tid mod L, jr = tid / L)
+// walks every NJ-th staged wavelength for layer l, so a warp reads consecutive G entries.
 // In the asymptotic wing (a <= 0.2, v >= 5: most evaluations of a wide window)
 // H = a/sqrt(pi) u (1 + 1.5u + 3.75u^2) with u = 1/v^2 = c t (c = 2 sigma^2, t = 1/|dl|^2), so
 // the three window sums follow from the moments M_k = sum G u^k, k = 1..3 (three FMAs per
 // evaluation):  sum G H = a/sqrt(pi) (M1 + 1.5 M2 + 3.75 M3),  sum G H_a = that / a,
-// sum G (a H_a + v H_v) = sum G H - 2 a/sqrt(pi) (M1 + 3 M2 + 11.25 M3).  Closer to the centre
-// every branch is differentiated with dual numbers.
+// sum G (a H_a + v H_v) = sum G H - 2 a/sqrt(pi) (M1 + 3 M2 + 11.25 M3).  Nearer the centre
+// central_derivs differentiates the far-Lorentz branch in closed form and the Harris branches
+// with dual numbers.
 template <bool MIXED>
 __global__ void __launch_bounds__(512) line_adj_kernel(LineAdjArgs a) {
     using R = typename std::conditional<MIXED, float, double>::type;
     using GT = typename std::conditional<MIXED, float, double>::type;  // G element (g32 == MIXED)
     __shared__ long long s_item;
     __shared__ int64_t s_cnt[NTIER + 1];
-    __shared__ R s_x[2][ADJ_SUB];
+    __shared__ R s_x[2][ADJ_SUB], s_t[2][ADJ_SUB];
     extern __shared__ __align__(16) unsigned char s_adj[];  // [2][ADJ_SUB][L] G, then [3][NJ][L] sums
     const int L = a.L, Lp = a.Lp;
     const int NJ = blockDim.x / L;
@@ -496,7 +539,11 @@ __global__ void __launch_bounds__(512) line_adj_kernel(LineAdjArgs a) {
                         else cp_async8(dst + e, src + e);
                     }
                 }
-                if (threadIdx.x < nw) s_x[sq & 1][threadIdx.x] = R(fabs(a.wls[js + threadIdx.x] - wl0));
+                if (threadIdx.x < nw) {
+                    const double dx = fabs(a.wls[js + threadIdx.x] - wl0);
+                    s_x[sq & 1][threadIdx.x] = R(dx);
+                    s_t[sq & 1][threadIdx.x] = R(1.0 / (dx * dx));
+                }
             }
             cp_async_commit();
         };
@@ -524,22 +571,24 @@ __global__ void __launch_bounds__(512) line_adj_kernel(LineAdjArgs a) {
             const int nw = int(min(int64_t(ADJ_SUB), nj - int64_t(sq) * ADJ_SUB));
             const GT* gb = s_g + size_t(sq & 1) * ADJ_SUB * L;
             const R* xb = s_x[sq & 1];
+            const R* tb = s_t[sq & 1];
             if (active) {
                 R pc[3] = {0, 0, 0}, pm[3] = {0, 0, 0};
                 for (int jj = jr; jj < nw; jj += NJ) {
                     const R g = R(gb[jj * L + l]);
                     const R x = xb[jj];
                     if (x >= xw) {
-                        const R u = fast_div(c2, x * x);
+                        const R u = c2 * tb[jj];
                         const R gu = g * u, gu2 = gu * u;
                         pm[0] += gu;
                         pm[1] += gu2;
                         pm[2] += gu2 * u;
                     } else {
-                        const Dual<R> d = voigt_dual<R>(av, x * s);
-                        pc[0] += g * d.x;
-                        pc[1] += g * (av * d.da + x * s * d.dv);
-                        pc[2] += g * d.da;
+                        R d[3];
+                        central_derivs<R>(av, x * s, d);
+                        pc[0] += g * d[0];
+                        pc[1] += g * d[1];
+                        pc[2] += g * d[2];
                     }
                 }
                 cen.add(pc);

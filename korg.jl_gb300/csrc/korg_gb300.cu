@@ -794,11 +794,13 @@ int run_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& ln, cons
     //    H alpha/beta/gamma (:130) and, with n(He I), the MHD occupation probabilities (:89).
     //    So d/dUH_I = -alpha_H / UH_I always, d/dnH_I = alpha_H / nH_I when MHD is off and no ABO
     //    line reaches the grid, d/dnHe_I = 0 when MHD is off; the rest (T, n_e, xi, and nH_I /
-    //    nHe_I otherwise) by central differences of the FP64 kernel, all layers perturbed at once.
+    //    nHe_I otherwise) by forward differences (relative step 1e-7: truncation ~1e-7, rounding
+    //    ~1e-9 of the derivative) of the FP64 kernel against the unperturbed evaluation, all
+    //    layers perturbed at once.
     if (in->hydrogen_lines && (flags & KORG_VJP_HYDROGEN)) {
         KCHECK(ensure(ctx, ctx->vjp_hfd, sizeof(double) * 2 * nLw));
-        double* ap = static_cast<double*>(ctx->vjp_hfd.p);
-        double* am = ap + nLw;
+        double* a0 = static_cast<double*>(ctx->vjp_hfd.p);
+        double* a1 = a0 + nLw;
         double* hin = reinterpret_cast<double*>(sm + o_hin);
         double* h = reinterpret_cast<double*>(sm + o_h);
         double* outs[6] = {dT, gr.ne, gr.nH_I, gr.nHe_I, gr.UH_I, gr.xi};
@@ -812,21 +814,20 @@ int run_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& ln, cons
                 abo_near |= (w0 + 2 * in->hydrogen_window >= wmin) && (w0 - 2 * in->hydrogen_window <= wmax);
         }
         const bool linear_nH = !in->use_MHD && !abo_near;
+        // the unperturbed FP64 evaluation (hydro_fd_contract_kernel computes sum G (x - y) / (2 h))
+        KCUDA(cudaMemsetAsync(a0, 0, sizeof(double) * nLw, s));
+        KCHECK(run_hydrogen(ctx, a0, wls, nwl, hl, in->hydrogen_window, in->use_MHD, false, s));
         if (outs[4] || (linear_nH && outs[2])) {
-            // one unperturbed FP64 evaluation, then alpha_H / UH_I and alpha_H / nH_I
-            KCUDA(cudaMemsetAsync(ap, 0, sizeof(double) * nLw, s));
-            KCHECK(run_hydrogen(ctx, ap, wls, nwl, hl, in->hydrogen_window, in->use_MHD, false, s));
-            KCUDA(cudaMemsetAsync(am, 0, sizeof(double) * nLw, s));
-            // hydro_fd_contract_kernel computes sum G (ap - am) / (2 h): with am = 0 and
-            // h = x / 2 (x = UH_I or nH_I) this is sum G alpha_H / x
+            // x = alpha_H, y = 0, h = -UH_I / 2 or nH_I / 2: sum G alpha_H / (-UH_I) or / nH_I
+            KCUDA(cudaMemsetAsync(a1, 0, sizeof(double) * nLw, s));
             if (outs[4]) {
                 hfd_half_kernel<<<(L + 127) / 128, 128, 0, s>>>(in->UH_I, L, -1.0, h);
-                hydro_fd_contract_kernel<<<ctx->sms * 4, 256, 0, s>>>(ctx->vjp_g.p, int32_t(mixed), ap, am, h, nwl, L,
+                hydro_fd_contract_kernel<<<ctx->sms * 4, 256, 0, s>>>(ctx->vjp_g.p, int32_t(mixed), a0, a1, h, nwl, L,
                                                                      outs[4]);
             }
             if (linear_nH && outs[2]) {
                 hfd_half_kernel<<<(L + 127) / 128, 128, 0, s>>>(in->nH_I, L, 1.0, h);
-                hydro_fd_contract_kernel<<<ctx->sms * 4, 256, 0, s>>>(ctx->vjp_g.p, int32_t(mixed), ap, am, h, nwl, L,
+                hydro_fd_contract_kernel<<<ctx->sms * 4, 256, 0, s>>>(ctx->vjp_g.p, int32_t(mixed), a0, a1, h, nwl, L,
                                                                      outs[2]);
             }
             KCUDA(cudaGetLastError());
@@ -835,17 +836,14 @@ int run_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& ln, cons
             if (!outs[k] || k == 4) continue;
             if (k == 2 && linear_nH) continue;
             if (k == 3 && !in->use_MHD) continue;  // n(He I) only enters the MHD probabilities
-            const double rel = 1e-5;
-            hfd_perturb_kernel<<<(L + 127) / 128, 128, 0, s>>>(hl, k, rel, +1.0, hin, h);
-            hfd_perturb_kernel<<<(L + 127) / 128, 128, 0, s>>>(hl, k, rel, -1.0, hin + 6 * L, h);
+            // x = alpha_H(p + dp), y = alpha_H(p), h = dp / 2
+            hfd_perturb_kernel<<<(L + 127) / 128, 128, 0, s>>>(hl, k, 1e-7, +1.0, hin, h);
+            hfd_half_kernel<<<(L + 127) / 128, 128, 0, s>>>(h, L, 1.0, h);
             KCUDA(cudaGetLastError());
-            KCUDA(cudaMemsetAsync(ap, 0, sizeof(double) * 2 * nLw, s));
+            KCUDA(cudaMemsetAsync(a1, 0, sizeof(double) * nLw, s));
             const HLayers hp{L, hin, hin + L, hin + 2 * L, hin + 3 * L, hin + 4 * L, hin + 5 * L};
-            const double* hm0 = hin + 6 * L;
-            const HLayers hm{L, hm0, hm0 + L, hm0 + 2 * L, hm0 + 3 * L, hm0 + 4 * L, hm0 + 5 * L};
-            KCHECK(run_hydrogen(ctx, ap, wls, nwl, hp, in->hydrogen_window, in->use_MHD, false, s));
-            KCHECK(run_hydrogen(ctx, am, wls, nwl, hm, in->hydrogen_window, in->use_MHD, false, s));
-            hydro_fd_contract_kernel<<<ctx->sms * 4, 256, 0, s>>>(ctx->vjp_g.p, int32_t(mixed), ap, am, h, nwl, L,
+            KCHECK(run_hydrogen(ctx, a1, wls, nwl, hp, in->hydrogen_window, in->use_MHD, false, s));
+            hydro_fd_contract_kernel<<<ctx->sms * 4, 256, 0, s>>>(ctx->vjp_g.p, int32_t(mixed), a1, a0, h, nwl, L,
                                                                  outs[k]);
             KCUDA(cudaGetLastError());
         }
