@@ -40,7 +40,8 @@ typedef enum {
     KORG_ECUDA = 2,    /* a CUDA runtime call failed; korg_last_error() has the message */
     KORG_ENOMEM = 3,   /* device allocation failed */
     KORG_ENOTABLES = 4, /* hydrogen lines requested before korg_set_stark_tables() */
-    KORG_ETOOBIG = 5    /* the problem needs more scratch than KORG_NOALLOC_SCRATCH_BYTES */
+    KORG_ETOOBIG = 5,   /* the problem needs more scratch than KORG_NOALLOC_SCRATCH_BYTES */
+    KORG_ETIMEOUT = 6   /* a device-side wait for staged data ran past its limit (results invalid) */
 } korg_status;
 
 enum { KORG_FP64 = 0, KORG_MIXED = 1 };
@@ -237,6 +238,11 @@ KORG_API int korg_synthesize_vjp_dev(korg_ctx *ctx, const korg_synth_inputs *in,
                                      const double *wls, int64_t nwl, int precision,
                                      const double *dflux, const double *dcntm,
                                      const korg_synth_grads *grads, int flags, void *stream);
+
+/* Waits for all work on the context's device and reports KORG_ETIMEOUT (once) if a kernel of
+ * an earlier asynchronous (_dev) call gave up a bounded wait for staged data; korg_synthesize_vjp
+ * makes this check itself.  No counterpart in the reference (Julia has no device waits). */
+KORG_API int korg_device_status(korg_ctx *ctx);
 
 /* MolecularCrossSection(linelist, wl_params; cutoff_alpha, vmic_vals, log_temp_vals) --
  * src/molecular_cross_sections.jl:51-88: the absorption cross-section per molecule of one

@@ -10,8 +10,8 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "libkorg_gb300.so")
-SOURCES = [os.path.join(HERE, "csrc", f) for f in
-           ("korg_gb300.cu", "lines.cuh", "hydrogen.cuh", "rt.cuh", "physics.cuh")]
+SOURCES = sorted(os.path.join(HERE, "csrc", f) for f in os.listdir(os.path.join(HERE, "csrc"))
+                 if f.endswith((".cu", ".cuh")))
 HEADER = os.path.join(HERE, "..", "include", "korg_gb300.h")
 
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",

@@ -366,26 +366,96 @@ __global__ void __launch_bounds__(32 * RTA_WARPS) rt_adjoint_kernel(RtAdjArgs a)
 }
 
 // ---------------------------------------------------------------- line adjoint
+constexpr int ADJ_CHUNK = 4096;  // wavelengths per chunk; an item is (chunk, line)
+
 struct LineAdjArgs {
     const void* G;            // [nwl][L] opacity cotangent (float when g32)
     int32_t g32;
     const double* wls;
+    const float2* wl2;        // wavelengths as FP32 (hi, lo) pairs (mixed)
     int64_t nwl;
     int32_t L, Lp;
     const double* wl;         // line centres
     const void* params;       // forward constants [n][Lp]: float4 {2 sigma^2, a, w, scale} or P64
     const int32_t *lb, *ub;
-    const int32_t *tier_idx, *tier_start;  // lines with non-empty windows, by width tier
+    const int32_t* tier_idx;  // lines with non-empty windows, by width tier
+    const int32_t* ilo;       // [npairs] first candidate of each (chunk, tier), in the tier lists
+    const int64_t* ipre;      // [npairs + 1] items before each (chunk, tier)
+    int32_t npairs;
     double* dpar;             // out [n][Lp][3] (+=): window sums of G H, G (a H_a + v H_v), G H_a
     unsigned long long* next; // item counter (zero before the launch)
+    int32_t Ls;               // largest staged row stride (elements)
+    int32_t bulk;             // rows of G start on 16-byte boundaries: one bulk copy per stage
+    int* err;                 // set to 1 when a wait for staged data runs past its limit
 };
 
-constexpr int ADJ_CHUNK = 4096;  // wavelengths per item
+// The items of line_adj_kernel, chunk-major so that the blocks running at any time share one
+// chunk of G in L2: pair p = k NTIER + t lists the lines of tier t whose centre index lies within
+// the tier's widest half-width of chunk k (a contiguous run of the tier list, which keeps list
+// order).  One block: the per-tier widest half-width, two binary searches per pair, an
+// exclusive scan of the counts.  Unsorted lists take whole tiers.
+__global__ void __launch_bounds__(1024) adj_items_kernel(const int32_t* tier_idx, const int32_t* tier_ci,
+                                                         const int32_t* tmeta, const int32_t* lb, const int32_t* ub,
+                                                         int64_t nwl, int32_t* ilo, int64_t* ipre) {
+    __shared__ int s_hw[NTIER];
+    __shared__ int64_t s_part[1024];
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int nck = int((nwl + ADJ_CHUNK - 1) / ADJ_CHUNK), np = nck * NTIER;
+    if (tid < NTIER) s_hw[tid] = 0;
+    __syncthreads();
+    const int n = tmeta[NTIER];
+    for (int p = tid; p < n; p += nt) {
+        int t = 0;
+        while (t < NTIER - 1 && p >= tmeta[t + 1]) t++;
+        const int i = tier_idx[p], c = tier_ci[p];
+        atomicMax(&s_hw[t], max(c - lb[i], ub[i] - c));
+    }
+    __syncthreads();
+    const bool unsorted = tmeta[NTIER + 1] != 0;
+    const int seg = (np + nt - 1) / nt;
+    const int p0 = min(tid * seg, np), p1 = min(p0 + seg, np);
+    int64_t sum = 0;
+    for (int p = p0; p < p1; p++) {
+        const int t = p % NTIER;
+        const int64_t k0 = int64_t(p / NTIER) * ADJ_CHUNK;
+        int64_t lo = tmeta[t], hi = tmeta[t + 1];
+        if (!unsorted && hi > lo) {
+            const int64_t cmin = k0 - s_hw[t] - 1, cmax = k0 + ADJ_CHUNK + s_hw[t];
+            const int32_t vmin = int32_t(cmin < INT32_MIN ? int64_t(INT32_MIN) : cmin);
+            const int32_t vmax = int32_t(cmax > INT32_MAX ? int64_t(INT32_MAX) : cmax);
+            const int64_t l0 = lower_bound_i32(tier_ci, lo, hi, vmin);
+            hi = upper_bound_i32(tier_ci, l0, hi, vmax);
+            lo = l0;
+        }
+        ilo[p] = int32_t(lo);
+        ipre[p] = hi - lo;  // count, turned into the prefix below
+        sum += hi - lo;
+    }
+    s_part[tid] = sum;
+    __syncthreads();
+    for (int o = 1; o < nt; o <<= 1) {
+        const int64_t v = tid >= o ? s_part[tid - o] : 0;
+        __syncthreads();
+        s_part[tid] += v;
+        __syncthreads();
+    }
+    int64_t run = s_part[tid] - sum;
+    for (int p = p0; p < p1; p++) {
+        const int64_t c = ipre[p];
+        ipre[p] = run;
+        run += c;
+    }
+    if (tid == nt - 1) ipre[np] = s_part[nt - 1];
+}
 
-// Items: tier 3 lines x ceil(nwl / CHUNK) chunks first, then tier 2 x 33, tier 1 x 3, tier 0 x 1
-// (window half-widths of at most 65536, 4096 and 256 points bound the chunks per line).
-__device__ __forceinline__ int64_t adj_chunks(int tier, int64_t nwl) {
-    return tier == 3 ? (nwl + ADJ_CHUNK - 1) / ADJ_CHUNK : (tier == 2 ? 33 : (tier == 1 ? 3 : 1));
+// Wavelengths as FP32 (hi, lo) pairs: |wl - centre| = (hi - chi) + (lo - clo) in FP32 keeps the
+// full offset accuracy without FP64 arithmetic.
+__global__ void wl_pairs_kernel(const double* w, int64_t n, float2* out) {
+    const int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j < n) {
+        const float hi = float(w[j]);
+        out[j] = make_float2(hi, float(w[j] - double(hi)));
+    }
 }
 
 __device__ __forceinline__ float fast_div(float p, float q) { return __fdividef(p, q); }
@@ -423,6 +493,43 @@ __device__ __forceinline__ void cp_async4(void* smem_dst, const void* gmem_src) 
 __device__ __forceinline__ void cp_async8(void* smem_dst, const void* gmem_src) {
     const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(gmem_src) : "memory");
+}
+
+// mbarrier + bulk-copy (TMA) helpers.  Every wait is bounded: mbar_wait gives up after 2^22
+// polls (each try_wait suspends the thread for a while), and the caller reports the timeout.
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return static_cast<unsigned>(__cvta_generic_to_shared(p)); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}\n" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+// one contiguous global -> shared copy by the bulk-copy engine; completes bytes on bar
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+// arrive on bar once this thread's earlier cp.async copies have landed (counted in the init count)
+__device__ __forceinline__ void cp_async_mbar_arrive(uint64_t* bar) {
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];\n" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(ok)
+                 : "r"(smem_u32(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+    for (int k = 0; k < (1 << 22); k++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
 }
 
 // Far-Lorentz branch of voigt_hjerting (line_absorption.jl:305-308: a > 1.4, or a > 0.2 with
@@ -466,172 +573,335 @@ __device__ __forceinline__ void central_derivs(R av, R v, R* out) {
     out[2] = A;
 }
 
-constexpr int ADJ_SUB = 64;  // wavelengths of G staged in shared memory at a time
+constexpr int ADJ_SUB = 64;     // wavelengths of G staged in shared memory per stage
+constexpr int ADJ_STAGES = 4;   // ring of staged blocks: one barrier per stage, three in flight
 
-// One block per item (a line and a chunk of its window).  The item's G rows (ADJ_SUB wavelengths
-// x L layers, contiguous in global memory) are copied to shared memory with cp.async, double
-// buffered, with 1/|dl|^2 of every staged wavelength; thread (l = tid mod L, jr = tid / L)
-// walks every NJ-th staged wavelength for layer l, so a warp reads consecutive G entries.
-// In the asymptotic wing (a <= 0.2, v >= 5: most evaluations of a wide window)
-// H = a/sqrt(pi) u (1 + 1.5u + 3.75u^2) with u = 1/v^2 = c t (c = 2 sigma^2, t = 1/|dl|^2), so
-// the three window sums follow from the moments M_k = sum G u^k, k = 1..3 (three FMAs per
-// evaluation):  sum G H = a/sqrt(pi) (M1 + 1.5 M2 + 3.75 M3),  sum G H_a = that / a,
-// sum G (a H_a + v H_v) = sum G H - 2 a/sqrt(pi) (M1 + 3 M2 + 11.25 M3).  Nearer the centre
-// central_derivs differentiates the far-Lorentz branch in closed form and the Harris branches
-// with dual numbers.
+// One staged wavelength: x = |dl|, t1 = cref / dl^2 and its square and cube (cref = 2 sigma^2 of
+// the item's line in layer 0, which keeps t1^3 within FP32 range over any window).
+template <class R>
+struct __align__(4 * sizeof(R)) AdjW {
+    R x, t1, t2, t3;
+};
+
+// One block per item (a line and one ADJ_CHUNK-wavelength chunk of the grid that its window
+// meets); items run chunk-major, so the blocks at work share a chunk of G in L2.  The item's G
+// rows (ADJ_SUB wavelengths x L layers, one contiguous block of global memory) go to shared
+// memory in an ADJ_STAGES ring filled by the bulk-copy engine (one cp.async.bulk per stage,
+// issued by one thread, completion counted on the slot's mbarrier), three stages ahead of the
+// one being summed.  When rows are not 16-byte multiples, every thread copies elements with
+// cp.async into rows padded to Ls (chosen so that the NJ-strided reads below hit distinct
+// banks) and arrives on the same mbarrier.  The wavelength table AdjW of a stage is written two
+// stages ahead from wavelengths loaded one stage before that, so no global load sits between
+// two barriers.
+//
+// Work balance.  A layer with a <= 0.2 ("wing layer") spends most of a wide window in the
+// asymptotic wing, three FMAs per evaluation; a layer with a > 0.2 has no asymptotic wing and
+// evaluates the far-Lorentz (or Harris) branch at every wavelength, several times the work.  Per
+// item the block lists the a > 0.2 layers first and gives each NJs threads, then each wing
+// layer NJf threads (powers of two, NJs >= NJf, chosen so that both kinds finish together);
+// thread (layer, jr) walks every NJ-th staged wavelength, and the NJ partial sums of a layer
+// meet by warp shuffles.
+//
+// In the asymptotic wing (a <= 0.2, v >= 5) H = a/sqrt(pi) u (1 + 1.5u + 3.75u^2) with
+// u = 1/v^2 = rho t1 (rho = 2 sigma_l^2 / cref), so the three window sums follow from the
+// moments M_k = rho^k sum G t1^k, k = 1..3:  sum G H = a/sqrt(pi) (M1 + 1.5 M2 + 3.75 M3),
+// sum G H_a = that / a,  sum G (a H_a + v H_v) = sum G H - 2 a/sqrt(pi) (M1 + 3 M2 + 11.25 M3).
+// A stage whose nearest wavelength is already in the layer's wing takes a branch-free loop.
+// Elsewhere central_derivs differentiates the far-Lorentz branch in closed form and the Harris
+// branches with dual numbers.
 template <bool MIXED>
-__global__ void __launch_bounds__(512) line_adj_kernel(LineAdjArgs a) {
+__global__ void __launch_bounds__(512, MIXED ? 2 : 1) line_adj_kernel(LineAdjArgs a) {
     using R = typename std::conditional<MIXED, float, double>::type;
     using GT = typename std::conditional<MIXED, float, double>::type;  // G element (g32 == MIXED)
+    using WP = typename std::conditional<MIXED, float2, double>::type; // a wavelength as loaded
+    using W = AdjW<R>;
+    constexpr int MAXW = 16;  // warps per block (512 threads)
+    constexpr int TW = ADJ_SUB / 32;  // warps that write a stage's table
     __shared__ long long s_item;
-    __shared__ int64_t s_cnt[NTIER + 1];
-    __shared__ R s_x[2][ADJ_SUB], s_t[2][ADJ_SUB];
-    extern __shared__ __align__(16) unsigned char s_adj[];  // [2][ADJ_SUB][L] G, then [3][NJ][L] sums
+    __shared__ int64_t s_i, s_j0, s_j1;
+    __shared__ __align__(8) uint64_t s_full[ADJ_STAGES];
+    __shared__ W s_w[ADJ_STAGES][ADJ_SUB];
+    __shared__ R s_xmin[ADJ_STAGES][TW];
+    __shared__ int s_wslow[MAXW];            // a > 0.2 layers per warp of layer indices
+    __shared__ int s_ns, s_lnf, s_lns, s_Ls;
+    extern __shared__ __align__(16) unsigned char s_adj[];  // [ADJ_STAGES][ADJ_SUB][<= Lsmax] G, then [L] order
     const int L = a.L, Lp = a.Lp;
-    const int NJ = blockDim.x / L;
-    const int l = threadIdx.x % L, jr = threadIdx.x / L;
-    const bool active = jr < NJ;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     GT* s_g = reinterpret_cast<GT*>(s_adj);
-    double* s_red = reinterpret_cast<double*>(s_adj + sizeof(GT) * 2 * ADJ_SUB * L);
+    int* s_order = reinterpret_cast<int*>(s_adj + sizeof(GT) * ADJ_STAGES * ADJ_SUB * a.Ls);
+    const int64_t total = a.ipre[a.npairs];
+    const GT* G = static_cast<const GT*>(a.G);
+    const bool bulk = a.bulk != 0;
     if (threadIdx.x == 0) {
-        int64_t acc = 0;
-        for (int t = NTIER - 1; t >= 0; t--) {
-            s_cnt[NTIER - 1 - t] = acc;
-            acc += int64_t(a.tier_start[t + 1] - a.tier_start[t]) * adj_chunks(t, a.nwl);
-        }
-        s_cnt[NTIER] = acc;
+        for (int b = 0; b < ADJ_STAGES; b++) mbar_init(&s_full[b], bulk ? 1u : blockDim.x);
+        mbar_fence_init();
     }
     __syncthreads();
-    const int64_t total = s_cnt[NTIER];
-    const GT* G = static_cast<const GT*>(a.G);
+    unsigned phase = 0;  // bit b: parity of the next completion of ring slot b
+    int pcur = 0;  // thread 0: the (chunk, tier) pair of the last item (items arrive in increasing order)
     for (;;) {
-        if (threadIdx.x == 0) s_item = (long long)atomicAdd(a.next, 1ull);
+        if (threadIdx.x == 0) {
+            const long long it = (long long)atomicAdd(a.next, 1ull);
+            s_item = it;
+            if (it < total) {
+                while (a.ipre[pcur + 1] <= it) pcur++;
+                const int64_t i = a.tier_idx[a.ilo[pcur] + (it - a.ipre[pcur])];
+                const int64_t k0 = int64_t(pcur / NTIER) * ADJ_CHUNK;
+                s_i = i;
+                s_j0 = max(int64_t(a.lb[i]), k0);
+                s_j1 = min(int64_t(a.ub[i]), k0 + ADJ_CHUNK - 1);
+            }
+        }
         __syncthreads();
-        const int64_t it = s_item;
-        __syncthreads();  // everyone has read s_item
-        if (it >= total) break;
-        int q = 0;
-        while (it >= s_cnt[q + 1]) q++;
-        const int tier = NTIER - 1 - q;
-        const int64_t nch = adj_chunks(tier, a.nwl);
-        const int64_t rel = it - s_cnt[q];
-        const int64_t i = a.tier_idx[a.tier_start[tier] + rel / nch];
-        const int64_t j0 = int64_t(a.lb[i]) + (rel % nch) * ADJ_CHUNK;
-        const int64_t j1 = min(int64_t(a.ub[i]), j0 + ADJ_CHUNK - 1);
-        if (j0 > j1) continue;  // uniform across the block
+        if (s_item >= total) break;
+        const int64_t i = s_i, j0 = s_j0, j1 = s_j1;
+        if (j0 > j1) {  // the window misses this chunk (uniform across the block)
+            __syncthreads();  // everyone has read the item
+            continue;
+        }
+        // classify the layers: a > 0.2 ("slow") or not, counted per warp of layer indices
+        bool slow_l = false;
+        unsigned ball = 0;
+        if (warp * 32 < L) {
+            if (threadIdx.x < L) {
+                slow_l = MIXED ? reinterpret_cast<const float4*>(a.params)[i * Lp + threadIdx.x].y > 0.2f
+                               : reinterpret_cast<const P64*>(a.params)[i * Lp + threadIdx.x].a > 0.2;
+            }
+            ball = __ballot_sync(0xffffffffu, slow_l);
+            if (lane == 0) s_wslow[warp] = __popc(ball);
+        }
+        __syncthreads();  // the item read by all; s_wslow complete
+        if (threadIdx.x < L) {
+            int before = 0;
+            for (int w = 0; w < warp; w++) before += s_wslow[w];
+            const int sr = before + __popc(ball & ((1u << lane) - 1u));  // slow layers below this one
+            int ns = 0;
+            for (int w = 0; w * 32 < L; w++) ns += s_wslow[w];
+            s_order[slow_l ? sr : ns + (int(threadIdx.x) - sr)] = int(threadIdx.x);
+            if (threadIdx.x == 0) {
+                // thread shares: slow layers NJs = 2^lns threads, wing layers NJf = 2^lnf, minimising
+                // the larger of 1/NJf and 6/NJs (the evaluation cost ratio) within the block
+                const int nf = L - ns, T = int(blockDim.x);
+                int bf = 0, bs = 0;
+                float best = 3.0e38f;
+                for (int lf = 0; lf <= 3; lf++)
+                    for (int ls = lf; ls <= 5; ls++) {
+                        if (nf * (1 << lf) + ns * (1 << ls) > T) continue;
+                        const float c = fmaxf(nf ? 1.0f / float(1 << lf) : 0.f, ns ? 6.0f / float(1 << ls) : 0.f);
+                        if (c < best) { best = c; bf = lf; bs = ls; }
+                    }
+                s_ns = ns;
+                s_lnf = bf;
+                s_lns = bs;
+                // staged row stride: dense for bulk copies; else, for NJf >= 2, Ls = 32/NJf
+                // (mod 64/NJf) spreads a wing warp's reads over 32 banks
+                const int nj = 1 << bf;
+                int Ls = (L + 3) & ~3;
+                if (nj >= 2)
+                    while (Ls % (64 / nj) != 32 / nj) Ls += 4;
+                s_Ls = bulk ? L : Ls;
+            }
+        }
+        __syncthreads();
+        const int ns = s_ns, lnf = s_lnf, lns = s_lns, Ls = s_Ls;
+        int l = -1, lnj = 0;
+        {
+            const int slot = int(threadIdx.x), cs = ns << lns;
+            if (slot < cs) {
+                l = s_order[slot >> lns];
+                lnj = lns;
+            } else if (slot - cs < ((L - ns) << lnf)) {
+                l = s_order[ns + ((slot - cs) >> lnf)];
+                lnj = lnf;
+            }
+        }
+        const bool active = l >= 0;
+        const int NJ = 1 << lnj, jr = int(threadIdx.x) & (NJ - 1);
         const double wl0 = a.wl[i];
+        const float chi = float(wl0), clo = float(wl0 - double(chi));
         const int64_t nj = j1 - j0 + 1;
         const int nsub = int((nj + ADJ_SUB - 1) / ADJ_SUB);
-        // stage sub-chunk q of the item's wavelengths into buffer q & 1
+        const double cref = MIXED ? double(reinterpret_cast<const float4*>(a.params)[i * Lp].x)
+                                  : reinterpret_cast<const P64*>(a.params)[i * Lp].c;
+        const R cref_r = R(cref);
+        // G rows of sub-chunk sq into ring slot sq mod ADJ_STAGES
         auto issue = [&](int sq) {
-            if (sq < nsub) {
-                const int64_t js = j0 + int64_t(sq) * ADJ_SUB;
-                const int nw = int(min(int64_t(ADJ_SUB), j1 - js + 1));
-                GT* dst = s_g + size_t(sq & 1) * ADJ_SUB * L;
-                const GT* src = G + js * L;
-                const int ne = nw * L;
-                if ((L * int(sizeof(GT))) % 16 == 0) {  // every row start is 16-byte aligned
-                    constexpr int V = 16 / int(sizeof(GT));
-                    for (int e = threadIdx.x * V; e < ne; e += blockDim.x * V) cp_async16(dst + e, src + e);
-                } else {
-                    for (int e = threadIdx.x; e < ne; e += blockDim.x) {
-                        if (MIXED) cp_async4(dst + e, src + e);
-                        else cp_async8(dst + e, src + e);
+            if (sq >= nsub) return;
+            const int b = sq % ADJ_STAGES;
+            const int64_t js = j0 + int64_t(sq) * ADJ_SUB;
+            const int nw = int(min(int64_t(ADJ_SUB), j1 - js + 1));
+            GT* dst = s_g + size_t(b) * ADJ_SUB * Ls;
+            const GT* src = G + js * L;
+            if (bulk) {
+                if (threadIdx.x == 0) {
+                    const unsigned bytes = unsigned(nw) * unsigned(L) * unsigned(sizeof(GT));
+                    mbar_expect_tx(&s_full[b], bytes);
+                    bulk_load(dst, src, bytes, &s_full[b]);
+                }
+            } else {
+                for (int r = warp; r < nw; r += nwarps)
+                    for (int c = lane; c < L; c += 32) {
+                        if (MIXED) cp_async4(dst + r * Ls + c, src + int64_t(r) * L + c);
+                        else cp_async8(dst + r * Ls + c, src + int64_t(r) * L + c);
                     }
-                }
-                if (threadIdx.x < nw) {
-                    const double dx = fabs(a.wls[js + threadIdx.x] - wl0);
-                    s_x[sq & 1][threadIdx.x] = R(dx);
-                    s_t[sq & 1][threadIdx.x] = R(1.0 / (dx * dx));
-                }
+                cp_async_mbar_arrive(&s_full[b]);
             }
-            cp_async_commit();
+        };
+        // wavelength of sub-chunk sq for table thread threadIdx.x (< ADJ_SUB)
+        auto load_wl = [&](int sq) -> WP {
+            const int64_t j = min(j0 + int64_t(sq) * ADJ_SUB + threadIdx.x, j1);
+            if constexpr (MIXED) return a.wl2[j];
+            else return a.wls[j];
+        };
+        // table of sub-chunk sq from its loaded wavelength, and the stage's nearest offset
+        auto make_table = [&](int sq, WP v) {
+            if (sq >= nsub) return;
+            const int b = sq % ADJ_STAGES;
+            const bool in = j0 + int64_t(sq) * ADJ_SUB + threadIdx.x <= j1;
+            R x;
+            if constexpr (MIXED) x = fabsf((v.x - chi) + (v.y - clo));
+            else x = fabs(v - wl0);
+            const R t1 = fast_div(cref_r, x * x);
+            if (in) s_w[b][threadIdx.x] = W{x, t1, t1 * t1, t1 * t1 * t1};
+            R m = in ? x : R(3.0e38);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const R q = __shfl_xor_sync(0xffffffffu, m, o);
+                m = q < m ? q : m;
+            }
+            if (lane == 0) s_xmin[b][warp] = m;
         };
         AdjSums<MIXED, 3> cen;  // central evaluations: G H, G (a H_a + v H_v), G H_a
-        AdjSums<MIXED, 3> mom;  // wing moments M1, M2, M3
-        R s = R(1), av = R(0), c2 = R(1), xw = R(3.0e38);
+        AdjSums<MIXED, 3> mom;  // wing sums S_k = sum G t1^k
+        R s = R(1), av = R(0), xw = R(3.0e38);
+        double rho = 1.0;
         if (active) {
+            double c2;
             if (MIXED) {
                 const float4 p = reinterpret_cast<const float4*>(a.params)[i * Lp + l];
                 s = R(rsqrtf(p.x));
                 av = R(p.y);
+                c2 = double(p.x);
             } else {
                 const P64 p = reinterpret_cast<const P64*>(a.params)[i * Lp + l];
                 s = R(p.inv_s);
                 av = R(p.a);
+                c2 = p.c;
             }
-            c2 = R(1) / (s * s);                   // 2 sigma^2
+            rho = c2 / cref;
             if (av <= R(0.2)) xw = R(5) / s;       // the wing starts at v = 5
         }
-        issue(0);
+        const bool tab = threadIdx.x < ADJ_SUB;  // whole warps
+        WP pf{};
+        for (int sq = 0; sq < ADJ_STAGES - 1; sq++) issue(sq);
+        if (tab) {
+            make_table(0, load_wl(0));
+            make_table(1, load_wl(1));
+            pf = load_wl(2);
+        }
         for (int sq = 0; sq < nsub; sq++) {
-            issue(sq + 1);
-            cp_async_wait_1();
-            __syncthreads();
+            const int bw = sq % ADJ_STAGES;
+            const bool ok = mbar_wait(&s_full[bw], (phase >> bw) & 1u);
+            // slot sq complete; every thread is past stage sq - 1, whose slot refills next
+            if (__syncthreads_or(!ok)) {
+                // staged data never arrived: report, wait (bounded) for the copies still in flight, stop
+                if (threadIdx.x == 0) *reinterpret_cast<volatile int*>(a.err) = 1;
+                for (int u = sq; u < nsub && u < sq + ADJ_STAGES - 1; u++)
+                    mbar_wait(&s_full[u % ADJ_STAGES], (phase >> (u % ADJ_STAGES)) & 1u);
+                return;
+            }
+            phase ^= 1u << bw;
+            issue(sq + ADJ_STAGES - 1);
+            if (tab) {
+                make_table(sq + 2, pf);
+                pf = load_wl(sq + 3);
+            }
+            const int b = sq % ADJ_STAGES;
             const int nw = int(min(int64_t(ADJ_SUB), nj - int64_t(sq) * ADJ_SUB));
-            const GT* gb = s_g + size_t(sq & 1) * ADJ_SUB * L;
-            const R* xb = s_x[sq & 1];
-            const R* tb = s_t[sq & 1];
+            const GT* gb = s_g + size_t(b) * ADJ_SUB * Ls + (active ? l : 0);
+            const W* wb = s_w[b];
             if (active) {
+                R xmin = s_xmin[b][0];
+#pragma unroll
+                for (int w = 1; w < TW; w++) xmin = s_xmin[b][w] < xmin ? s_xmin[b][w] : xmin;
                 R pc[3] = {0, 0, 0}, pm[3] = {0, 0, 0};
-                for (int jj = jr; jj < nw; jj += NJ) {
-                    const R g = R(gb[jj * L + l]);
-                    const R x = xb[jj];
-                    if (x >= xw) {
-                        const R u = c2 * tb[jj];
-                        const R gu = g * u, gu2 = gu * u;
-                        pm[0] += gu;
-                        pm[1] += gu2;
-                        pm[2] += gu2 * u;
-                    } else {
-                        R d[3];
-                        central_derivs<R>(av, x * s, d);
-                        pc[0] += g * d[0];
-                        pc[1] += g * d[1];
-                        pc[2] += g * d[2];
+                if (xmin >= xw) {  // every staged wavelength in the asymptotic wing
+#pragma unroll 4
+                    for (int jj = jr; jj < nw; jj += NJ) {
+                        const R g = R(gb[jj * Ls]);
+                        const W w = wb[jj];
+                        pm[0] += g * w.t1;
+                        pm[1] += g * w.t2;
+                        pm[2] += g * w.t3;
+                    }
+                } else {
+                    for (int jj = jr; jj < nw; jj += NJ) {
+                        const R g = R(gb[jj * Ls]);
+                        const W w = wb[jj];
+                        if (w.x >= xw) {
+                            pm[0] += g * w.t1;
+                            pm[1] += g * w.t2;
+                            pm[2] += g * w.t3;
+                        } else {
+                            R d[3];
+                            central_derivs<R>(av, w.x * s, d);
+                            pc[0] += g * d[0];
+                            pc[1] += g * d[1];
+                            pc[2] += g * d[2];
+                        }
                     }
                 }
                 cen.add(pc);
                 mom.add(pm);
             }
-            __syncthreads();  // buffer sq & 1 is refilled by issue(sq + 2)
         }
         // window sums of this thread: central + wing (from the moments)
+        double v3[3] = {0.0, 0.0, 0.0};
         if (active) {
             const double k = 0.5641895835477563 * double(av);  // a / sqrt(pi)
-            const double M1 = mom.get(0), M2 = mom.get(1), M3 = mom.get(2);
-            const double wH = k * (M1 + 1.5 * M2 + 3.75 * M3);
+            const double M1 = rho * mom.get(0), M2 = rho * rho * mom.get(1), M3 = rho * rho * rho * mom.get(2);
             const double wA = 0.5641895835477563 * (M1 + 1.5 * M2 + 3.75 * M3);
+            const double wH = k * (M1 + 1.5 * M2 + 3.75 * M3);
             const double wX = wH - 2 * k * (M1 + 3 * M2 + 11.25 * M3);
-            s_red[(0 * NJ + jr) * L + l] = cen.get(0) + wH;
-            s_red[(1 * NJ + jr) * L + l] = cen.get(1) + wX;
-            s_red[(2 * NJ + jr) * L + l] = cen.get(2) + wA;
+            v3[0] = cen.get(0) + wH;
+            v3[1] = cen.get(1) + wX;
+            v3[2] = cen.get(2) + wA;
         }
-        __syncthreads();
-        if (active && jr == 0) {
-            double* dp = a.dpar + (i * Lp + l) * 3;
+        // the NJ threads of a layer are aligned lanes of one warp
+        for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
             for (int k = 0; k < 3; k++) {
-                double t = 0.0;
-                for (int r = 0; r < NJ; r++) t += s_red[(k * NJ + r) * L + l];
-                atomicAdd(dp + k, t);
+                const double o = __shfl_xor_sync(0xffffffffu, v3[k], off);
+                if (off < NJ) v3[k] += o;
             }
         }
-        __syncthreads();  // s_red is rewritten by the next item
+        if (active && jr == 0) {
+            double* dp = a.dpar + (i * Lp + l) * 3;
+#pragma unroll
+            for (int k = 0; k < 3; k++) atomicAdd(dp + k, v3[k]);
+        }
+        __syncthreads();  // the item, s_order, s_ns, s_Ls and the ring are reused by the next item
     }
 }
 
-// Dynamic shared memory of line_adj_kernel: two staged G buffers and the partial sums.
-inline size_t adj_smem(int L, int threads, bool mixed) {
-    return (mixed ? sizeof(float) : sizeof(double)) * 2 * ADJ_SUB * size_t(L) + sizeof(double) * 3 * size_t(threads);
+// Block shape of line_adj_kernel for L layers (1 <= L <= 512): about 5 threads per layer, a
+// whole number of warps, at most 512; Ls is the largest staged row stride an item may pick
+// (L itself when G rows are bulk-copied).
+struct AdjShape {
+    int Ls, threads, bulk;
+};
+inline AdjShape adj_shape(int L, const void* G, bool mixed) {
+    int t = ((5 * L + 31) / 32) * 32;
+    t = t < 128 ? 128 : (t > 512 ? 512 : t);
+    if (t < L) t = ((L + 31) / 32) * 32;
+    const bool bulk = (size_t(L) * (mixed ? 4 : 8)) % 16 == 0 && (reinterpret_cast<uintptr_t>(G) & 15) == 0;
+    return {bulk ? L : ((L + 3) & ~3) + 32, t, int(bulk)};
 }
 
-// Threads per block of line_adj_kernel for L layers: L * NJ, the smallest multiple of 32 that
-// is at least 128 (at most 512).
-inline int adj_threads(int L) {
-    int nj = 1;
-    while (nj * L < 512 && ((nj * L) % 32 != 0 || nj * L < 128)) nj++;
-    if (nj * L > 512) nj = 512 / L;
-    return nj * L;
+// Dynamic shared memory of line_adj_kernel: the staged G ring, then the per-item layer order.
+inline size_t adj_smem(const AdjShape& sh, bool mixed) {
+    return (mixed ? sizeof(float) : sizeof(double)) * ADJ_STAGES * ADJ_SUB * size_t(sh.Ls) +
+           sizeof(int) * size_t(sh.Ls);
 }
 
 // Chain rule of the per-(line, layer) prologue (line_absorption.jl:86-106), FP64, one warp per

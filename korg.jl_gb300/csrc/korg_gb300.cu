@@ -56,6 +56,8 @@ struct korg_ctx {
     DevBuf mx_layers;                            // molecular cross-section layer inputs
     void* stage_host = nullptr;
     size_t stage_host_cap = 0;
+    int* dev_err_host = nullptr;  // mapped host word: set by kernels whose bounded waits ran out
+    int* dev_err_dev = nullptr;
     // batched synthesis: chunk alpha, per-spectrum line scratch, tile arguments + reference
     // wavelengths + queue counters (device), their host staging (pinned, batch-only)
     DevBuf b_alpha, b_lines, b_meta;
@@ -734,7 +736,11 @@ int run_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& ln, cons
     KCHECK(ensure(ctx, ctx->vjp_dpar, sizeof(double) * 3 * size_t(nmax) * Lp));
     // small pieces: daref [L], a scratch dT [L], hydrogen FD inputs [2][6][L], steps [L], counter
     const size_t o_dar = 0, o_dT = a256(8 * L), o_hin = o_dT + a256(8 * L), o_h = o_hin + a256(8 * 12 * L),
-                 o_ctr = o_h + a256(8 * L), o_g32 = o_ctr + 256, small = o_g32 + a256(4 * L);
+                 o_ctr = o_h + a256(8 * L), o_g32 = o_ctr + 256;
+    // line-adjoint items ((chunk, tier) pairs) and the wavelengths as FP32 pairs
+    const int np_max = int((nwl + ADJ_CHUNK - 1) / ADJ_CHUNK) * NTIER;
+    const size_t o_ilo = o_g32 + a256(4 * L), o_ipre = o_ilo + a256(4 * size_t(np_max)),
+                 o_wl2 = o_ipre + a256(8 * size_t(np_max + 1)), small = o_wl2 + a256(8 * size_t(nwl));
     KCHECK(ensure(ctx, ctx->vjp_small, small));
     unsigned char* sm = static_cast<unsigned char*>(ctx->vjp_small.p);
     double* daref = reinterpret_cast<double*>(sm + o_dar);
@@ -868,11 +874,22 @@ int run_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& ln, cons
         double* dpar = static_cast<double*>(ctx->vjp_dpar.p);
         KCUDA(cudaMemsetAsync(dpar, 0, sizeof(double) * 3 * size_t(lns.n) * Lp, s));
         KCUDA(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), s));
-        LineAdjArgs la{Gp, g32_in, w, nw, L, Lp, lns.wl, sc.params, sc.lb, sc.ub, sc.tier_idx, sc.tier_meta, dpar,
-                       ctr};
-        const int threads = adj_threads(L);
+        const AdjShape sh = adj_shape(L, Gp, mixed);
+        auto* ilo = reinterpret_cast<int32_t*>(sm + o_ilo);
+        auto* ipre = reinterpret_cast<int64_t*>(sm + o_ipre);
+        auto* wl2 = reinterpret_cast<float2*>(sm + o_wl2);
+        const int npairs = int((nw + ADJ_CHUNK - 1) / ADJ_CHUNK) * NTIER;
+        adj_items_kernel<<<1, 1024, 0, s>>>(sc.tier_idx, sc.tier_ci, sc.tier_meta, sc.lb, sc.ub, nw, ilo, ipre);
+        KCUDA(cudaGetLastError());
+        if (mixed) {
+            wl_pairs_kernel<<<unsigned((nw + 255) / 256), 256, 0, s>>>(w, nw, wl2);
+            KCUDA(cudaGetLastError());
+        }
+        LineAdjArgs la{Gp, g32_in, w, wl2, nw, L, Lp, lns.wl, sc.params, sc.lb, sc.ub, sc.tier_idx, ilo, ipre, npairs,
+                       dpar, ctr, sh.Ls, sh.bulk, ctx->dev_err_dev};
+        const int threads = sh.threads;
         if ((g32_in != 0) != mixed) return set_err(ctx, KORG_EINVAL, "opacity cotangent precision mismatch");
-        const size_t smem = adj_smem(L, threads, mixed);
+        const size_t smem = adj_smem(sh, mixed);
         int per_sm = 0;
         if (mixed) {
             KCUDA(cudaFuncSetAttribute(line_adj_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
@@ -1100,6 +1117,11 @@ KORG_API int korg_create(korg_ctx** out, int device) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     for (int i = 0; e == cudaSuccess && i < NEV; i++) e = cudaEventCreate(&ctx->ev[i]);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->b_host_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaHostAlloc(reinterpret_cast<void**>(&ctx->dev_err_host), sizeof(int), cudaHostAllocMapped);
+    if (e == cudaSuccess) {
+        *ctx->dev_err_host = 0;
+        e = cudaHostGetDevicePointer(reinterpret_cast<void**>(&ctx->dev_err_dev), ctx->dev_err_host, 0);
+    }
     if (e == cudaSuccess) {
         MathTables t;
         fill_math_tables(t);
@@ -1131,6 +1153,7 @@ KORG_API void korg_destroy(korg_ctx* ctx) {
     for (void* p : ctx->stark_allocs) cudaFree(p);
     if (ctx->stage_host) cudaFreeHost(ctx->stage_host);
     if (ctx->b_host) cudaFreeHost(ctx->b_host);
+    if (ctx->dev_err_host) cudaFreeHost(ctx->dev_err_host);
     for (int i = 0; i < NEV; i++)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
     if (ctx->b_host_ev) cudaEventDestroy(ctx->b_host_ev);
@@ -1529,6 +1552,23 @@ KORG_API int korg_synthesize(korg_ctx* ctx, const korg_synth_inputs* in, const k
 }
 
 
+// A kernel whose bounded wait for staged data ran out sets the mapped error word; read and clear
+// it (the caller has synchronised).
+int take_device_error(korg_ctx* ctx) {
+    if (ctx->dev_err_host && *reinterpret_cast<volatile int*>(ctx->dev_err_host)) {
+        *reinterpret_cast<volatile int*>(ctx->dev_err_host) = 0;
+        return set_err(ctx, KORG_ETIMEOUT, "a device-side wait for staged data ran past its limit; results are invalid");
+    }
+    return KORG_OK;
+}
+
+KORG_API int korg_device_status(korg_ctx* ctx) {
+    if (!ctx) return KORG_EINVAL;
+    KCUDA(cudaSetDevice(ctx->device));
+    KCUDA(cudaDeviceSynchronize());
+    return take_device_error(ctx);
+}
+
 KORG_API int korg_synthesize_vjp_dev(korg_ctx* ctx, const korg_synth_inputs* in, const korg_lines* lines,
                                      const korg_lines* lines5, const double* wls, int64_t nwl, int precision,
                                      const double* dflux, const double* dcntm, const korg_synth_grads* grads,
@@ -1612,7 +1652,7 @@ KORG_API int korg_synthesize_vjp(korg_ctx* ctx, const korg_synth_inputs* in, con
         if (host_out[k] && sizes[k])
             KCUDA(cudaMemcpyAsync(host_out[k], dev_out[k], 8 * sizes[k], cudaMemcpyDeviceToHost, ctx->stream));
     KCUDA(cudaStreamSynchronize(ctx->stream));
-    return KORG_OK;
+    return take_device_error(ctx);
 }
 
 KORG_API int korg_molecular_cross_section_dev(korg_ctx* ctx, const korg_lines* lines, const double* wls,

@@ -19,7 +19,8 @@ _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
 _lp = C.POINTER(C.c_int64)
 
-ERRORS = {1: "KORG_EINVAL", 2: "KORG_ECUDA", 3: "KORG_ENOMEM", 4: "KORG_ENOTABLES", 5: "KORG_ETOOBIG"}
+ERRORS = {1: "KORG_EINVAL", 2: "KORG_ECUDA", 3: "KORG_ENOMEM", 4: "KORG_ENOTABLES", 5: "KORG_ETOOBIG",
+          6: "KORG_ETIMEOUT"}
 
 
 class KorgError(RuntimeError):
@@ -130,6 +131,7 @@ def lib():
             L.korg_set_batch_options.argtypes = [vp, C.c_int, C.c_int, C.c_int64]
             L.korg_get_tile_config.argtypes = [vp, C.c_int32, C.c_int, _ip, _ip, _ip, _ip]
             L.korg_set_tile_config.argtypes = [vp, C.c_int32, C.c_int, C.c_int32, C.c_int32, C.c_int32]
+            L.korg_device_status.argtypes = [vp]
             _lib = L
     return _lib
 
@@ -143,7 +145,7 @@ def exported_symbols():
             "korg_math_selftest", "korg_line_absorption_noalloc", "korg_synthesize_batch_dev",
             "korg_set_batch_options", "korg_get_tile_config", "korg_set_tile_config", "korg_synthesize_vjp", "korg_synthesize_vjp_dev",
             "korg_radiative_transfer_general", "korg_molecular_cross_section_dev",
-            "korg_interpolate_molecular_cross_section_dev"]
+            "korg_interpolate_molecular_cross_section_dev", "korg_device_status"]
 
 
 def _p(a, kind=_dp):
