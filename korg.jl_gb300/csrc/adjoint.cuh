@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(32 * RTA_WARPS) rt_adjoint_kernel(RtAdjArgs a)
 }
 
 // ---------------------------------------------------------------- line adjoint
-constexpr int ADJ_CHUNK = 4096;  // wavelengths per chunk; an item is (chunk, line)
+constexpr int ADJ_CHUNK = 16384;  // wavelengths per chunk; an item is (chunk, line)
 
 struct LineAdjArgs {
     const void* G;            // [nwl][L] opacity cotangent (float when g32)
@@ -539,9 +539,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
 // A = C au/a [w (1 + P b + Q b^2) + b (-6r^2 + 2P w) + b^2 (-60 r^2 (r^2 - 1) + 4Q w)] with
 // w = (r^2 - 1)/(r^2 + 1).
 template <class R>
-__device__ __forceinline__ void far_lorentz_d(R a, R v, R& H, R& X, R& A) {
-    const R ia = recip(a);
-    const R r2 = v * v * ia * ia;
+__device__ __forceinline__ void far_lorentz_r2(R r2, R ia, R& H, R& X, R& A) {
     const R iz = recip(R(1) + r2);
     const R au = R(0.70710678118654752) * ia * iz;
     const R b = au * au;
@@ -553,6 +551,11 @@ __device__ __forceinline__ void far_lorentz_d(R a, R v, R& H, R& X, R& A) {
     H = Cau * poly;
     X = -Cau * (R(1) + (R(3) * P + R(5) * Q * b) * b);
     A = Cau * ia * (w * poly + (R(-6) * r2 + R(2) * P * w) * b + (R(-60) * r2 * (r2 - R(1)) + R(4) * Q * w) * b * b);
+}
+template <class R>
+__device__ __forceinline__ void far_lorentz_d(R a, R v, R& H, R& X, R& A) {
+    const R ia = recip(a);
+    far_lorentz_r2<R>(v * v * ia * ia, ia, H, X, A);
 }
 
 // H, a H_a + v H_v and H_a of every branch but the asymptotic wing: far Lorentz in closed form,
@@ -573,8 +576,9 @@ __device__ __forceinline__ void central_derivs(R av, R v, R* out) {
     out[2] = A;
 }
 
-constexpr int ADJ_SUB = 64;     // wavelengths of G staged in shared memory per stage
-constexpr int ADJ_STAGES = 4;   // ring of staged blocks: one barrier per stage, three in flight
+constexpr int ADJ_SUB = 96;     // wavelengths of G staged in shared memory per stage
+constexpr int ADJ_STAGES = 3;   // ring of staged blocks: one barrier per stage, two in flight
+static_assert(ADJ_SUB % 32 == 0, "the stage table is written by whole warps");
 
 // One staged wavelength: x = |dl|, t1 = cref / dl^2 and its square and cube (cref = 2 sigma^2 of
 // the item's line in layer 0, which keeps t1^3 within FP32 range over any window).
@@ -587,7 +591,7 @@ struct __align__(4 * sizeof(R)) AdjW {
 // meets); items run chunk-major, so the blocks at work share a chunk of G in L2.  The item's G
 // rows (ADJ_SUB wavelengths x L layers, one contiguous block of global memory) go to shared
 // memory in an ADJ_STAGES ring filled by the bulk-copy engine (one cp.async.bulk per stage,
-// issued by one thread, completion counted on the slot's mbarrier), three stages ahead of the
+// issued by one thread, completion counted on the slot's mbarrier), ADJ_STAGES - 1 stages ahead of the
 // one being summed.  When rows are not 16-byte multiples, every thread copies elements with
 // cp.async into rows padded to Ls (chosen so that the NJ-strided reads below hit distinct
 // banks) and arrives on the same mbarrier.  The wavelength table AdjW of a stage is written two
@@ -640,25 +644,23 @@ __global__ void __launch_bounds__(512, MIXED ? 2 : 1) line_adj_kernel(LineAdjArg
     unsigned phase = 0;  // bit b: parity of the next completion of ring slot b
     int pcur = 0;  // thread 0: the (chunk, tier) pair of the last item (items arrive in increasing order)
     for (;;) {
-        if (threadIdx.x == 0) {
-            const long long it = (long long)atomicAdd(a.next, 1ull);
-            s_item = it;
-            if (it < total) {
+        if (threadIdx.x == 0) {  // the next item whose window meets its chunk
+            for (;;) {
+                const long long it = (long long)atomicAdd(a.next, 1ull);
+                s_item = it;
+                if (it >= total) break;
                 while (a.ipre[pcur + 1] <= it) pcur++;
                 const int64_t i = a.tier_idx[a.ilo[pcur] + (it - a.ipre[pcur])];
                 const int64_t k0 = int64_t(pcur / NTIER) * ADJ_CHUNK;
                 s_i = i;
                 s_j0 = max(int64_t(a.lb[i]), k0);
                 s_j1 = min(int64_t(a.ub[i]), k0 + ADJ_CHUNK - 1);
+                if (s_j0 <= s_j1) break;
             }
         }
         __syncthreads();
         if (s_item >= total) break;
         const int64_t i = s_i, j0 = s_j0, j1 = s_j1;
-        if (j0 > j1) {  // the window misses this chunk (uniform across the block)
-            __syncthreads();  // everyone has read the item
-            continue;
-        }
         // classify the layers: a > 0.2 ("slow") or not, counted per warp of layer indices
         bool slow_l = false;
         unsigned ball = 0;
@@ -824,7 +826,7 @@ __global__ void __launch_bounds__(512, MIXED ? 2 : 1) line_adj_kernel(LineAdjArg
                 R xmin = s_xmin[b][0];
 #pragma unroll
                 for (int w = 1; w < TW; w++) xmin = s_xmin[b][w] < xmin ? s_xmin[b][w] : xmin;
-                R pc[3] = {0, 0, 0}, pm[3] = {0, 0, 0};
+                R pm[3] = {0, 0, 0};
                 if (xmin >= xw) {  // every staged wavelength in the asymptotic wing
 #pragma unroll 4
                     for (int jj = jr; jj < nw; jj += NJ) {
@@ -834,7 +836,23 @@ __global__ void __launch_bounds__(512, MIXED ? 2 : 1) line_adj_kernel(LineAdjArg
                         pm[1] += g * w.t2;
                         pm[2] += g * w.t3;
                     }
+                } else if (av > R(0.2) && (av > R(1.4) || av + xmin * s >= R(3.2))) {
+                    // every staged wavelength in the far-Lorentz branch (r = v / a = x s / a)
+                    const R ia = recip(av), k1 = s * ia;
+                    R pc[3] = {0, 0, 0};
+#pragma unroll 2
+                    for (int jj = jr; jj < nw; jj += NJ) {
+                        const R g = R(gb[jj * Ls]);
+                        const R r = wb[jj].x * k1;
+                        R H, X, A;
+                        far_lorentz_r2<R>(r * r, ia, H, X, A);
+                        pc[0] += g * H;
+                        pc[1] += g * X;
+                        pc[2] += g * A;
+                    }
+                    cen.add(pc);
                 } else {
+                    R pc[3] = {0, 0, 0};
                     for (int jj = jr; jj < nw; jj += NJ) {
                         const R g = R(gb[jj * Ls]);
                         const W w = wb[jj];
@@ -850,8 +868,8 @@ __global__ void __launch_bounds__(512, MIXED ? 2 : 1) line_adj_kernel(LineAdjArg
                             pc[2] += g * d[2];
                         }
                     }
+                    cen.add(pc);
                 }
-                cen.add(pc);
                 mom.add(pm);
             }
         }
