@@ -514,6 +514,9 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned b
                  "l"(src), "r"(bytes), "r"(smem_u32(bar))
                  : "memory");
 }
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(smem_u32(bar)) : "memory");
+}
 // arrive on bar once this thread's earlier cp.async copies have landed (counted in the init count)
 __device__ __forceinline__ void cp_async_mbar_arrive(uint64_t* bar) {
     asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];\n" ::"r"(smem_u32(bar)) : "memory");
@@ -588,21 +591,25 @@ struct __align__(4 * sizeof(R)) AdjW {
 };
 
 // One block per item (a line and one ADJ_CHUNK-wavelength chunk of the grid that its window
-// meets); items run chunk-major, so the blocks at work share a chunk of G in L2.  The item's G
-// rows (ADJ_SUB wavelengths x L layers, one contiguous block of global memory) go to shared
-// memory in an ADJ_STAGES ring filled by the bulk-copy engine (one cp.async.bulk per stage,
-// issued by one thread, completion counted on the slot's mbarrier), ADJ_STAGES - 1 stages ahead of the
-// one being summed.  When rows are not 16-byte multiples, every thread copies elements with
-// cp.async into rows padded to Ls (chosen so that the NJ-strided reads below hit distinct
-// banks) and arrives on the same mbarrier.  The wavelength table AdjW of a stage is written two
-// stages ahead from wavelengths loaded one stage before that, so no global load sits between
-// two barriers.
+// meets); items run chunk-major, so the blocks at work share a chunk of G in L2.
+//
+// Pipeline.  The last warp of the block is the producer: for every stage (ADJ_SUB wavelengths
+// of the item) it waits until the ring slot is empty, has the bulk-copy engine fetch the stage's
+// G rows (ADJ_SUB x L values, one contiguous block of global memory) with one cp.async.bulk
+// completing on the slot's "full" mbarrier, writes the stage's wavelength table AdjW from
+// wavelengths it loaded one stage earlier, and arrives on "full".  The other warps consume: wait
+// for "full", sum, and arrive on the slot's "empty" mbarrier.  No block-wide barrier separates
+// stages, so warps drift apart by up to ADJ_STAGES stages.  When rows are not 16-byte multiples
+// the producer copies elements with cp.async into rows padded to Ls (chosen so that the
+// NJ-strided reads below hit distinct banks) and each lane arrives through
+// cp.async.mbarrier.arrive.  Every wait is bounded; a wait that runs out sets the error word,
+// and the block finishes the item without waiting further and stops.
 //
 // Work balance.  A layer with a <= 0.2 ("wing layer") spends most of a wide window in the
 // asymptotic wing, three FMAs per evaluation; a layer with a > 0.2 has no asymptotic wing and
 // evaluates the far-Lorentz (or Harris) branch at every wavelength, several times the work.  Per
-// item the block lists the a > 0.2 layers first and gives each NJs threads, then each wing
-// layer NJf threads (powers of two, NJs >= NJf, chosen so that both kinds finish together);
+// item the block lists the a > 0.2 layers first and gives each NJs consumer threads, then each
+// wing layer NJf (powers of two, NJs >= NJf, chosen so that both kinds finish together);
 // thread (layer, jr) walks every NJ-th staged wavelength, and the NJ partial sums of a layer
 // meet by warp shuffles.
 //
@@ -610,39 +617,54 @@ struct __align__(4 * sizeof(R)) AdjW {
 // u = 1/v^2 = rho t1 (rho = 2 sigma_l^2 / cref), so the three window sums follow from the
 // moments M_k = rho^k sum G t1^k, k = 1..3:  sum G H = a/sqrt(pi) (M1 + 1.5 M2 + 3.75 M3),
 // sum G H_a = that / a,  sum G (a H_a + v H_v) = sum G H - 2 a/sqrt(pi) (M1 + 3 M2 + 11.25 M3).
-// A stage whose nearest wavelength is already in the layer's wing takes a branch-free loop.
-// Elsewhere central_derivs differentiates the far-Lorentz branch in closed form and the Harris
-// branches with dual numbers.
+// A stage whose nearest wavelength is already in the layer's wing takes a branch-free loop, and
+// so does a stage entirely in the far-Lorentz branch.  Elsewhere central_derivs differentiates
+// the far-Lorentz branch in closed form and the Harris branches with dual numbers.
 template <bool MIXED>
 __global__ void __launch_bounds__(512, MIXED ? 2 : 1) line_adj_kernel(LineAdjArgs a) {
     using R = typename std::conditional<MIXED, float, double>::type;
     using GT = typename std::conditional<MIXED, float, double>::type;  // G element (g32 == MIXED)
     using WP = typename std::conditional<MIXED, float2, double>::type; // a wavelength as loaded
     using W = AdjW<R>;
-    constexpr int MAXW = 16;  // warps per block (512 threads)
-    constexpr int TW = ADJ_SUB / 32;  // warps that write a stage's table
+    constexpr int MAXW = 16;                 // warps per block (512 threads)
+    constexpr int PER = ADJ_SUB / 32;        // table entries per producer lane
     __shared__ long long s_item;
     __shared__ int64_t s_i, s_j0, s_j1;
-    __shared__ __align__(8) uint64_t s_full[ADJ_STAGES];
+    __shared__ __align__(8) uint64_t s_full[ADJ_STAGES], s_empty[ADJ_STAGES];
     __shared__ W s_w[ADJ_STAGES][ADJ_SUB];
-    __shared__ R s_xmin[ADJ_STAGES][TW];
+    __shared__ R s_xmin[ADJ_STAGES];
     __shared__ int s_wslow[MAXW];            // a > 0.2 layers per warp of layer indices
     __shared__ int s_ns, s_lnf, s_lns, s_Ls;
+    __shared__ volatile int s_abort;
     extern __shared__ __align__(16) unsigned char s_adj[];  // [ADJ_STAGES][ADJ_SUB][<= Lsmax] G, then [L] order
     const int L = a.L, Lp = a.Lp;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int PW = nwarps - 1;               // the producer warp
+    const int TC = PW * 32;                  // consumer threads
     GT* s_g = reinterpret_cast<GT*>(s_adj);
     int* s_order = reinterpret_cast<int*>(s_adj + sizeof(GT) * ADJ_STAGES * ADJ_SUB * a.Ls);
     const int64_t total = a.ipre[a.npairs];
     const GT* G = static_cast<const GT*>(a.G);
     const bool bulk = a.bulk != 0;
     if (threadIdx.x == 0) {
-        for (int b = 0; b < ADJ_STAGES; b++) mbar_init(&s_full[b], bulk ? 1u : blockDim.x);
+        for (int b = 0; b < ADJ_STAGES; b++) {
+            mbar_init(&s_full[b], bulk ? 2u : 33u);  // expect_tx + table arrive, or 32 copy lanes + table
+            mbar_init(&s_empty[b], unsigned(PW));    // one arrive per consumer warp
+        }
         mbar_fence_init();
+        s_abort = 0;
     }
     __syncthreads();
-    unsigned phase = 0;  // bit b: parity of the next completion of ring slot b
-    int pcur = 0;  // thread 0: the (chunk, tier) pair of the last item (items arrive in increasing order)
+    int64_t g0 = 0;  // stages this block has run before the current item (ring slot = stage mod ADJ_STAGES)
+    int pcur = 0;    // thread 0: the (chunk, tier) pair of the last item (items arrive in increasing order)
+    // bounded wait; a wait that runs out marks the block aborted and reports it
+    auto wait = [&](uint64_t* bar, unsigned parity) {
+        if (s_abort) return;
+        if (!mbar_wait(bar, parity)) {
+            s_abort = 1;
+            *reinterpret_cast<volatile int*>(a.err) = 1;
+        }
+    };
     for (;;) {
         if (threadIdx.x == 0) {  // the next item whose window meets its chunk
             for (;;) {
@@ -659,7 +681,7 @@ __global__ void __launch_bounds__(512, MIXED ? 2 : 1) line_adj_kernel(LineAdjArg
             }
         }
         __syncthreads();
-        if (s_item >= total) break;
+        if (s_item >= total || s_abort) break;
         const int64_t i = s_i, j0 = s_j0, j1 = s_j1;
         // classify the layers: a > 0.2 ("slow") or not, counted per warp of layer indices
         bool slow_l = false;
@@ -681,14 +703,14 @@ __global__ void __launch_bounds__(512, MIXED ? 2 : 1) line_adj_kernel(LineAdjArg
             for (int w = 0; w * 32 < L; w++) ns += s_wslow[w];
             s_order[slow_l ? sr : ns + (int(threadIdx.x) - sr)] = int(threadIdx.x);
             if (threadIdx.x == 0) {
-                // thread shares: slow layers NJs = 2^lns threads, wing layers NJf = 2^lnf, minimising
-                // the larger of 1/NJf and 6/NJs (the evaluation cost ratio) within the block
-                const int nf = L - ns, T = int(blockDim.x);
+                // consumer-thread shares: slow layers NJs = 2^lns, wing layers NJf = 2^lnf,
+                // minimising the larger of 1/NJf and 6/NJs (the evaluation cost ratio)
+                const int nf = L - ns;
                 int bf = 0, bs = 0;
                 float best = 3.0e38f;
                 for (int lf = 0; lf <= 3; lf++)
                     for (int ls = lf; ls <= 5; ls++) {
-                        if (nf * (1 << lf) + ns * (1 << ls) > T) continue;
+                        if (nf * (1 << lf) + ns * (1 << ls) > TC) continue;
                         const float c = fmaxf(nf ? 1.0f / float(1 << lf) : 0.f, ns ? 6.0f / float(1 << ls) : 0.f);
                         if (c < best) { best = c; bf = lf; bs = ls; }
                     }
@@ -706,214 +728,209 @@ __global__ void __launch_bounds__(512, MIXED ? 2 : 1) line_adj_kernel(LineAdjArg
         }
         __syncthreads();
         const int ns = s_ns, lnf = s_lnf, lns = s_lns, Ls = s_Ls;
-        int l = -1, lnj = 0;
-        {
-            const int slot = int(threadIdx.x), cs = ns << lns;
-            if (slot < cs) {
-                l = s_order[slot >> lns];
-                lnj = lns;
-            } else if (slot - cs < ((L - ns) << lnf)) {
-                l = s_order[ns + ((slot - cs) >> lnf)];
-                lnj = lnf;
-            }
-        }
-        const bool active = l >= 0;
-        const int NJ = 1 << lnj, jr = int(threadIdx.x) & (NJ - 1);
-        const double wl0 = a.wl[i];
-        const float chi = float(wl0), clo = float(wl0 - double(chi));
         const int64_t nj = j1 - j0 + 1;
         const int nsub = int((nj + ADJ_SUB - 1) / ADJ_SUB);
+        const double wl0 = a.wl[i];
         const double cref = MIXED ? double(reinterpret_cast<const float4*>(a.params)[i * Lp].x)
                                   : reinterpret_cast<const P64*>(a.params)[i * Lp].c;
-        const R cref_r = R(cref);
-        // G rows of sub-chunk sq into ring slot sq mod ADJ_STAGES
-        auto issue = [&](int sq) {
-            if (sq >= nsub) return;
-            const int b = sq % ADJ_STAGES;
-            const int64_t js = j0 + int64_t(sq) * ADJ_SUB;
-            const int nw = int(min(int64_t(ADJ_SUB), j1 - js + 1));
-            GT* dst = s_g + size_t(b) * ADJ_SUB * Ls;
-            const GT* src = G + js * L;
-            if (bulk) {
-                if (threadIdx.x == 0) {
-                    const unsigned bytes = unsigned(nw) * unsigned(L) * unsigned(sizeof(GT));
-                    mbar_expect_tx(&s_full[b], bytes);
-                    bulk_load(dst, src, bytes, &s_full[b]);
+        if (warp == PW) {
+            // ---------------- producer: G rows by the bulk-copy engine, the wavelength table
+            const float chi = float(wl0), clo = float(wl0 - double(chi));
+            const R cref_r = R(cref);
+            auto load_wl = [&](int sq, WP* v) {
+#pragma unroll
+                for (int k = 0; k < PER; k++) {
+                    const int64_t j = min(j0 + int64_t(sq) * ADJ_SUB + lane + 32 * k, j1);
+                    if constexpr (MIXED) v[k] = a.wl2[j];
+                    else v[k] = a.wls[j];
                 }
-            } else {
-                for (int r = warp; r < nw; r += nwarps)
-                    for (int c = lane; c < L; c += 32) {
-                        if (MIXED) cp_async4(dst + r * Ls + c, src + int64_t(r) * L + c);
-                        else cp_async8(dst + r * Ls + c, src + int64_t(r) * L + c);
+            };
+            WP pf[PER];
+            load_wl(0, pf);
+            for (int sq = 0; sq < nsub; sq++) {
+                const int64_t gq = g0 + sq;
+                const int b = int(gq % ADJ_STAGES);
+                if (gq >= ADJ_STAGES) wait(&s_empty[b], unsigned((gq / ADJ_STAGES - 1) & 1));
+                const int64_t js = j0 + int64_t(sq) * ADJ_SUB;
+                const int nw = int(min(int64_t(ADJ_SUB), j1 - js + 1));
+                GT* dst = s_g + size_t(b) * ADJ_SUB * Ls;
+                const GT* src = G + js * L;
+                if (bulk) {
+                    if (lane == 0) {
+                        const unsigned bytes = unsigned(nw) * unsigned(L) * unsigned(sizeof(GT));
+                        mbar_expect_tx(&s_full[b], bytes);
+                        bulk_load(dst, src, bytes, &s_full[b]);
                     }
-                cp_async_mbar_arrive(&s_full[b]);
-            }
-        };
-        // wavelength of sub-chunk sq for table thread threadIdx.x (< ADJ_SUB)
-        auto load_wl = [&](int sq) -> WP {
-            const int64_t j = min(j0 + int64_t(sq) * ADJ_SUB + threadIdx.x, j1);
-            if constexpr (MIXED) return a.wl2[j];
-            else return a.wls[j];
-        };
-        // table of sub-chunk sq from its loaded wavelength, and the stage's nearest offset
-        auto make_table = [&](int sq, WP v) {
-            if (sq >= nsub) return;
-            const int b = sq % ADJ_STAGES;
-            const bool in = j0 + int64_t(sq) * ADJ_SUB + threadIdx.x <= j1;
-            R x;
-            if constexpr (MIXED) x = fabsf((v.x - chi) + (v.y - clo));
-            else x = fabs(v - wl0);
-            const R t1 = fast_div(cref_r, x * x);
-            if (in) s_w[b][threadIdx.x] = W{x, t1, t1 * t1, t1 * t1 * t1};
-            R m = in ? x : R(3.0e38);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const R q = __shfl_xor_sync(0xffffffffu, m, o);
-                m = q < m ? q : m;
-            }
-            if (lane == 0) s_xmin[b][warp] = m;
-        };
-        AdjSums<MIXED, 3> cen;  // central evaluations: G H, G (a H_a + v H_v), G H_a
-        AdjSums<MIXED, 3> mom;  // wing sums S_k = sum G t1^k
-        R s = R(1), av = R(0), xw = R(3.0e38);
-        double rho = 1.0;
-        if (active) {
-            double c2;
-            if (MIXED) {
-                const float4 p = reinterpret_cast<const float4*>(a.params)[i * Lp + l];
-                s = R(rsqrtf(p.x));
-                av = R(p.y);
-                c2 = double(p.x);
-            } else {
-                const P64 p = reinterpret_cast<const P64*>(a.params)[i * Lp + l];
-                s = R(p.inv_s);
-                av = R(p.a);
-                c2 = p.c;
-            }
-            rho = c2 / cref;
-            if (av <= R(0.2)) xw = R(5) / s;       // the wing starts at v = 5
-        }
-        const bool tab = threadIdx.x < ADJ_SUB;  // whole warps
-        WP pf{};
-        for (int sq = 0; sq < ADJ_STAGES - 1; sq++) issue(sq);
-        if (tab) {
-            make_table(0, load_wl(0));
-            make_table(1, load_wl(1));
-            pf = load_wl(2);
-        }
-        for (int sq = 0; sq < nsub; sq++) {
-            const int bw = sq % ADJ_STAGES;
-            const bool ok = mbar_wait(&s_full[bw], (phase >> bw) & 1u);
-            // slot sq complete; every thread is past stage sq - 1, whose slot refills next
-            if (__syncthreads_or(!ok)) {
-                // staged data never arrived: report, wait (bounded) for the copies still in flight, stop
-                if (threadIdx.x == 0) *reinterpret_cast<volatile int*>(a.err) = 1;
-                for (int u = sq; u < nsub && u < sq + ADJ_STAGES - 1; u++)
-                    mbar_wait(&s_full[u % ADJ_STAGES], (phase >> (u % ADJ_STAGES)) & 1u);
-                return;
-            }
-            phase ^= 1u << bw;
-            issue(sq + ADJ_STAGES - 1);
-            if (tab) {
-                make_table(sq + 2, pf);
-                pf = load_wl(sq + 3);
-            }
-            const int b = sq % ADJ_STAGES;
-            const int nw = int(min(int64_t(ADJ_SUB), nj - int64_t(sq) * ADJ_SUB));
-            const GT* gb = s_g + size_t(b) * ADJ_SUB * Ls + (active ? l : 0);
-            const W* wb = s_w[b];
-            if (active) {
-                R xmin = s_xmin[b][0];
-#pragma unroll
-                for (int w = 1; w < TW; w++) xmin = s_xmin[b][w] < xmin ? s_xmin[b][w] : xmin;
-                R pm[3] = {0, 0, 0};
-                if (xmin >= xw) {  // every staged wavelength in the asymptotic wing
-#pragma unroll 4
-                    for (int jj = jr; jj < nw; jj += NJ) {
-                        const R g = R(gb[jj * Ls]);
-                        const W w = wb[jj];
-                        pm[0] += g * w.t1;
-                        pm[1] += g * w.t2;
-                        pm[2] += g * w.t3;
-                    }
-                } else if (av > R(0.2) && (av > R(1.4) || av + xmin * s >= R(3.2))) {
-                    // every staged wavelength in the far-Lorentz branch (r = v / a = x s / a)
-                    const R ia = recip(av), k1 = s * ia;
-                    R pc[3] = {0, 0, 0};
-#pragma unroll 2
-                    for (int jj = jr; jj < nw; jj += NJ) {
-                        const R g = R(gb[jj * Ls]);
-                        const R r = wb[jj].x * k1;
-                        R H, X, A;
-                        far_lorentz_r2<R>(r * r, ia, H, X, A);
-                        pc[0] += g * H;
-                        pc[1] += g * X;
-                        pc[2] += g * A;
-                    }
-                    cen.add(pc);
                 } else {
-                    R pc[3] = {0, 0, 0};
-                    for (int jj = jr; jj < nw; jj += NJ) {
-                        const R g = R(gb[jj * Ls]);
-                        const W w = wb[jj];
-                        if (w.x >= xw) {
+                    for (int r = 0; r < nw; r++)
+                        for (int c = lane; c < L; c += 32) {
+                            if (MIXED) cp_async4(dst + r * Ls + c, src + int64_t(r) * L + c);
+                            else cp_async8(dst + r * Ls + c, src + int64_t(r) * L + c);
+                        }
+                    cp_async_mbar_arrive(&s_full[b]);
+                }
+                WP cur[PER];
+#pragma unroll
+                for (int k = 0; k < PER; k++) cur[k] = pf[k];
+                if (sq + 1 < nsub) load_wl(sq + 1, pf);  // lands while this stage's table is written
+                R m = R(3.0e38);
+#pragma unroll
+                for (int k = 0; k < PER; k++) {
+                    const int e = lane + 32 * k;
+                    R x;
+                    if constexpr (MIXED) x = fabsf((cur[k].x - chi) + (cur[k].y - clo));
+                    else x = fabs(cur[k] - wl0);
+                    const R t1 = fast_div(cref_r, x * x);
+                    if (e < nw) {
+                        s_w[b][e] = W{x, t1, t1 * t1, t1 * t1 * t1};
+                        m = x < m ? x : m;
+                    }
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const R q = __shfl_xor_sync(0xffffffffu, m, o);
+                    m = q < m ? q : m;
+                }
+                if (lane == 0) s_xmin[b] = m;
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&s_full[b]);
+            }
+        } else {
+            // ---------------- consumers
+            int l = -1, lnj = 0;
+            {
+                const int slot = int(threadIdx.x), cs = ns << lns;
+                if (slot < cs) {
+                    l = s_order[slot >> lns];
+                    lnj = lns;
+                } else if (slot - cs < ((L - ns) << lnf)) {
+                    l = s_order[ns + ((slot - cs) >> lnf)];
+                    lnj = lnf;
+                }
+            }
+            const bool active = l >= 0;
+            const int NJ = 1 << lnj, jr = int(threadIdx.x) & (NJ - 1);
+            AdjSums<MIXED, 3> cen;  // central evaluations: G H, G (a H_a + v H_v), G H_a
+            AdjSums<MIXED, 3> mom;  // wing sums S_k = sum G t1^k
+            R s = R(1), av = R(0), xw = R(3.0e38);
+            double rho = 1.0;
+            if (active) {
+                double c2;
+                if (MIXED) {
+                    const float4 p = reinterpret_cast<const float4*>(a.params)[i * Lp + l];
+                    s = R(rsqrtf(p.x));
+                    av = R(p.y);
+                    c2 = double(p.x);
+                } else {
+                    const P64 p = reinterpret_cast<const P64*>(a.params)[i * Lp + l];
+                    s = R(p.inv_s);
+                    av = R(p.a);
+                    c2 = p.c;
+                }
+                rho = c2 / cref;
+                if (av <= R(0.2)) xw = R(5) / s;  // the wing starts at v = 5
+            }
+            const R ia = recip(av), k1 = s * ia;  // far Lorentz: r = v / a = x s / a
+            for (int sq = 0; sq < nsub; sq++) {
+                const int64_t gq = g0 + sq;
+                const int b = int(gq % ADJ_STAGES);
+                wait(&s_full[b], unsigned((gq / ADJ_STAGES) & 1));
+                const int nw = int(min(int64_t(ADJ_SUB), nj - int64_t(sq) * ADJ_SUB));
+                const GT* gb = s_g + size_t(b) * ADJ_SUB * Ls + (active ? l : 0);
+                const W* wb = s_w[b];
+                if (active) {
+                    const R xmin = s_xmin[b];
+                    R pm[3] = {0, 0, 0};
+                    if (xmin >= xw) {  // every staged wavelength in the asymptotic wing
+#pragma unroll 4
+                        for (int jj = jr; jj < nw; jj += NJ) {
+                            const R g = R(gb[jj * Ls]);
+                            const W w = wb[jj];
                             pm[0] += g * w.t1;
                             pm[1] += g * w.t2;
                             pm[2] += g * w.t3;
-                        } else {
-                            R d[3];
-                            central_derivs<R>(av, w.x * s, d);
-                            pc[0] += g * d[0];
-                            pc[1] += g * d[1];
-                            pc[2] += g * d[2];
                         }
+                    } else if (av > R(0.2) && (av > R(1.4) || av + xmin * s >= R(3.2))) {
+                        // every staged wavelength in the far-Lorentz branch
+                        R pc[3] = {0, 0, 0};
+#pragma unroll 2
+                        for (int jj = jr; jj < nw; jj += NJ) {
+                            const R g = R(gb[jj * Ls]);
+                            const R r = wb[jj].x * k1;
+                            R H, X, A;
+                            far_lorentz_r2<R>(r * r, ia, H, X, A);
+                            pc[0] += g * H;
+                            pc[1] += g * X;
+                            pc[2] += g * A;
+                        }
+                        cen.add(pc);
+                    } else {
+                        R pc[3] = {0, 0, 0};
+                        for (int jj = jr; jj < nw; jj += NJ) {
+                            const R g = R(gb[jj * Ls]);
+                            const W w = wb[jj];
+                            if (w.x >= xw) {
+                                pm[0] += g * w.t1;
+                                pm[1] += g * w.t2;
+                                pm[2] += g * w.t3;
+                            } else {
+                                R d[3];
+                                central_derivs<R>(av, w.x * s, d);
+                                pc[0] += g * d[0];
+                                pc[1] += g * d[1];
+                                pc[2] += g * d[2];
+                            }
+                        }
+                        cen.add(pc);
                     }
-                    cen.add(pc);
+                    mom.add(pm);
                 }
-                mom.add(pm);
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&s_empty[b]);
+            }
+            // window sums of this thread: central + wing (from the moments)
+            double v3[3] = {0.0, 0.0, 0.0};
+            if (active) {
+                const double k = 0.5641895835477563 * double(av);  // a / sqrt(pi)
+                const double M1 = rho * mom.get(0), M2 = rho * rho * mom.get(1), M3 = rho * rho * rho * mom.get(2);
+                const double wA = 0.5641895835477563 * (M1 + 1.5 * M2 + 3.75 * M3);
+                const double wH = k * (M1 + 1.5 * M2 + 3.75 * M3);
+                const double wX = wH - 2 * k * (M1 + 3 * M2 + 11.25 * M3);
+                v3[0] = cen.get(0) + wH;
+                v3[1] = cen.get(1) + wX;
+                v3[2] = cen.get(2) + wA;
+            }
+            // the NJ threads of a layer are aligned lanes of one warp
+            for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    const double o = __shfl_xor_sync(0xffffffffu, v3[k], off);
+                    if (off < NJ) v3[k] += o;
+                }
+            }
+            if (active && jr == 0 && !s_abort) {
+                double* dp = a.dpar + (i * Lp + l) * 3;
+#pragma unroll
+                for (int k = 0; k < 3; k++) atomicAdd(dp + k, v3[k]);
             }
         }
-        // window sums of this thread: central + wing (from the moments)
-        double v3[3] = {0.0, 0.0, 0.0};
-        if (active) {
-            const double k = 0.5641895835477563 * double(av);  // a / sqrt(pi)
-            const double M1 = rho * mom.get(0), M2 = rho * rho * mom.get(1), M3 = rho * rho * rho * mom.get(2);
-            const double wA = 0.5641895835477563 * (M1 + 1.5 * M2 + 3.75 * M3);
-            const double wH = k * (M1 + 1.5 * M2 + 3.75 * M3);
-            const double wX = wH - 2 * k * (M1 + 3 * M2 + 11.25 * M3);
-            v3[0] = cen.get(0) + wH;
-            v3[1] = cen.get(1) + wX;
-            v3[2] = cen.get(2) + wA;
-        }
-        // the NJ threads of a layer are aligned lanes of one warp
-        for (int off = 16; off > 0; off >>= 1) {
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                const double o = __shfl_xor_sync(0xffffffffu, v3[k], off);
-                if (off < NJ) v3[k] += o;
-            }
-        }
-        if (active && jr == 0) {
-            double* dp = a.dpar + (i * Lp + l) * 3;
-#pragma unroll
-            for (int k = 0; k < 3; k++) atomicAdd(dp + k, v3[k]);
-        }
-        __syncthreads();  // the item, s_order, s_ns, s_Ls and the ring are reused by the next item
+        g0 += nsub;
+        __syncthreads();  // the item, s_order, s_ns and s_Ls are rewritten by the next item
     }
 }
 
-// Block shape of line_adj_kernel for L layers (1 <= L <= 512): about 5 threads per layer, a
-// whole number of warps, at most 512; Ls is the largest staged row stride an item may pick
-// (L itself when G rows are bulk-copied).
+// Block shape of line_adj_kernel for L layers (1 <= L <= 480): consumer warps for about 5
+// threads per layer (at least 4 warps, at most 15) and one producer warp; Ls is the largest
+// staged row stride an item may pick (L itself when G rows are bulk-copied).
 struct AdjShape {
     int Ls, threads, bulk;
 };
 inline AdjShape adj_shape(int L, const void* G, bool mixed) {
     int t = ((5 * L + 31) / 32) * 32;
-    t = t < 128 ? 128 : (t > 512 ? 512 : t);
+    t = t < 128 ? 128 : (t > 480 ? 480 : t);
     if (t < L) t = ((L + 31) / 32) * 32;
     const bool bulk = (size_t(L) * (mixed ? 4 : 8)) % 16 == 0 && (reinterpret_cast<uintptr_t>(G) & 15) == 0;
-    return {bulk ? L : ((L + 3) & ~3) + 32, t, int(bulk)};
+    return {bulk ? L : ((L + 3) & ~3) + 32, t + 32, int(bulk)};
 }
 
 // Dynamic shared memory of line_adj_kernel: the staged G ring, then the per-item layer order.
