@@ -315,8 +315,8 @@ KORG_API int korg_math_selftest(korg_ctx *ctx, int64_t n, double *max_ulp_exp, d
  * arguments and results as korg_line_absorption_dev (device pointers, alpha accumulated in
  * place on `stream`), but no context and no cudaMalloc / cudaFree / allocating library call:
  * all scratch lives in one file-scope device array of KORG_NOALLOC_SCRATCH_BYTES (64 MiB) that
- * every GPU loading the library holds until exit.  That is enough for about 70,000 lines of a
- * 56-layer atmosphere in KORG_MIXED (constants take layers x 16 bytes per line, 48 in
+ * every GPU loading the library holds until exit.  That is enough for about 35,000 lines of a
+ * 56-layer atmosphere in KORG_MIXED (constants take layers x 32 bytes per line, 48 in
  * KORG_FP64); larger problems return KORG_ETOOBIG without launching anything.
  * The first call on a device looks up the array's address and writes lookup tables into it
  * with a synchronous copy: make that first call before any stream capture.  Every call shares

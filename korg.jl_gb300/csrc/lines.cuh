@@ -79,6 +79,7 @@ struct PrepOut {
     int32_t Lp, K, G;
     unsigned long long* evals;   // running totals: evaluations, lines in window
     unsigned long long* nlines;
+    float4* params_w;        // [n][Lp] mixed, or null: asymptotic-wing coefficients {A1, A2, A3, cref}
 };
 
 // Per-line quantities shared by every layer (line_absorption.jl:83,101,105,219).
@@ -253,6 +254,7 @@ __device__ __forceinline__ void argmax_reduce(float& v, int& idx) {
 struct LinePrep32 {
     double El, Eu, strength;   // FP64 line-strength inputs
     float wlc, k_m, wl2c, grad, gstark, v1, abo_pre, vexp, invmu, t32;
+    float cref;                // 2 sigma^2 in layer 0: the scale of the wing coefficients
     int32_t flags, sp, ki;     // flags: 1 molecule, 2 ABO broadening; ki: continuum knot interval
 };
 constexpr int PREP_WARPS = 8;
@@ -294,6 +296,11 @@ __global__ void __launch_bounds__(32 * PREP_WARPS) line_prep_mixed_kernel(LinesD
         p.vexp = float(1 - q.v2);
         p.invmu = float(1 / (1.008 * AMU_CGS)) + 1.f / float(q.m);
         p.t32 = float(kp_mine.t);
+        {
+            const LayerConst c0 = lc[0];
+            const float sigma0 = p.wlc * sqrtf(p.k_m * c0.T32 + 0.5f * c0.xi32 * c0.xi32);
+            p.cref = 2.f * sigma0 * sigma0;
+        }
         p.flags = (q.mol ? 1 : 0) | ((!q.mol && q.v2 != -1) ? 2 : 0);
         p.sp = q.sp;
         p.ki = int32_t(kp_mine.i);
@@ -309,9 +316,11 @@ __global__ void __launch_bounds__(32 * PREP_WARPS) line_prep_mixed_kernel(LinesD
         float dmax = -1.f, lmax = -1.f;
         int dl = 0, ll = 0;
         float4* dst = reinterpret_cast<float4*>(out.params) + i * Lp;
+        float4* dstw = out.params_w ? out.params_w + i * Lp : nullptr;
         for (int l = lane; l < Lp; l += 32) {
             if (l >= L) {
                 dst[l] = make_float4(1.f, 0.f, 0.f, 0.f);
+                if (dstw) dstw[l] = make_float4(0.f, 0.f, 0.f, q.cref);
                 s_bnd[l] = 0.f;
                 s_cls[l] = 1;
                 continue;
@@ -349,6 +358,18 @@ __global__ void __launch_bounds__(32 * PREP_WARPS) line_prep_mixed_kernel(LinesD
             p.z = A ? a * 0.56418958f * scale : 1.f / (gamma * gamma);
             p.w = scale;
             dst[l] = p;
+            if (dstw) {
+                // asymptotic wing as a cubic in t' = cref / dl^2:  w u (1 + 1.5 u + 3.75 u^2) with
+                // u = 1/v^2 = rho t', rho = c / cref, is A1 t' + A2 t'^2 + A3 t'^3
+                float4 pw = make_float4(0.f, 0.f, 0.f, q.cref);
+                if (A) {
+                    const float rho = p.x / q.cref;
+                    pw.x = p.z * rho;
+                    pw.y = 1.5f * pw.x * rho;
+                    pw.z = 2.5f * pw.y * rho;
+                }
+                dstw[l] = pw;
+            }
             // v >= 5 (a <= 0.2) or a + v >= 3.2 (0.2 < a <= 1.4) or any v (a > 1.4), v = x / sqrt(c)
             s_bnd[l] = (A ? 5.f : (a <= 1.4f ? 3.2f - a : 0.f)) * sqrtf(p.x) * 1.0001f;
             s_cls[l] = A;
@@ -491,6 +512,7 @@ struct TileArgs {
     const uint32_t* amask;
     const int32_t *lb, *ub;
     const int32_t *tier_idx, *tier_ci, *tier_start, *unsorted;
+    const float4* params_w;   // mixed, or null: asymptotic-wing coefficients {A1, A2, A3, cref}
 };
 
 // first index in [lo, hi) with a[i] >= v (a non-decreasing)
@@ -517,6 +539,7 @@ struct LineStage {
     int32_t lb, ub;
     uint32_t cls;     // 2 bits per layer group: 1 = pure asymptotic wing, 2 = wing branches, 0 = general
     int32_t li;       // line index
+    float cref;       // scale of the wing coefficients (mixed, split tiles)
 };
 
 __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
@@ -544,6 +567,8 @@ __device__ __forceinline__ double far_lorentz64(const P64& p, double x2) {
 // One tile of TW = blockDim.x / G wavelengths x all layers, computed by one CTA.  Thread (j, g)
 // owns wavelength j and the K consecutive (padded) layers g*K .. g*K+K-1.  `smem` is the
 // dynamic shared memory of the launch (two line-constant buffers, then the LineStage array).
+// In the mixed split form a line whose layers of the group are all in the asymptotic wing over
+// the tile is staged as its wing coefficients: three FMAs per evaluation.
 template <bool MIXED, int K>
 __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, int gsplit, unsigned char* smem) {
     using P = typename ParamT<MIXED>::type;
@@ -596,6 +621,7 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
 
     const int warp = tid >> 5, lane = tid & 31, nwarps = nthr >> 5;
     const int chunks16 = SL * int(sizeof(P) / 16);  // 16-byte pieces of one line's staged constants
+    const bool wcoef = MIXED && gsplit >= 0 && a.params_w != nullptr;
     const int64_t src0 = gsplit >= 0 ? int64_t(g) * K * int64_t(sizeof(P) / 16) : 0;
     for (int tier = 0; tier < NTIER; tier++)
     for (int64_t base = s_tier[tier][0]; base < s_tier[tier][1]; base += nthr) {
@@ -641,6 +667,7 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
             st.ub = ubi;
             st.cls = cls;
             st.li = int32_t(i);
+            st.cref = wcoef ? a.params_w[i * Lp].w : 0.f;
             s_ln[s_warp[warp] + __popc(m & ((1u << lane) - 1))] = st;
         }
         const int cnt = s_count;
@@ -654,9 +681,12 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
                 unsigned char* buf = smem + size_t(q & 1) * a.region;
                 for (int e = tid; e < nb * chunks16; e += nthr) {
                     const int b = e / chunks16, r = e - b * chunks16;
-                    const int64_t li = s_ln[b0 + b].li;
+                    const LineStage& sl = s_ln[b0 + b];
+                    const int64_t li = sl.li;
+                    const void* src = (wcoef && ((sl.cls >> (2 * g)) & 3u) == 1u) ? static_cast<const void*>(a.params_w)
+                                                                                  : a.params;
                     cp_async16(buf + (size_t(b) * chunks16 + r) * 16,
-                               reinterpret_cast<const unsigned char*>(a.params) +
+                               reinterpret_cast<const unsigned char*>(src) +
                                    (li * Lp * int64_t(sizeof(P) / 16) + src0 + r) * 16);
                 }
             }
@@ -682,7 +712,15 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
                         const float t = __fdividef(1.f, x2);
                         const float4* pr = reinterpret_cast<const float4*>(s_par) + b * SL + goff;
                         const uint32_t cls = (st.cls >> (2 * g)) & 3u;
-                        if (cls == 1u) {
+                        if (cls == 1u && wcoef) {
+                            // every layer in the asymptotic wing, staged as A1 t' + A2 t'^2 + A3 t'^3
+                            const float tp = t * st.cref;
+#pragma unroll
+                            for (int k = 0; k < K; k++) {
+                                const float4 p = pr[k];
+                                part[k] = fmaf(tp, fmaf(tp, fmaf(tp, p.z, p.y), p.x), part[k]);
+                            }
+                        } else if (cls == 1u) {
                             // every layer in the asymptotic wing: w/v^2 (1 + 1.5/v^2 + 3.75/v^4), 1/v^2 = c t
 #pragma unroll
                             for (int k = 0; k < K; k++) {
