@@ -243,6 +243,11 @@ KORG_API int korg_synthesize_vjp_dev(korg_ctx *ctx, const korg_synth_inputs *in,
  * an earlier asynchronous (_dev) call gave up a bounded wait for staged data; korg_synthesize_vjp
  * makes this check itself.  No counterpart in the reference (Julia has no device waits). */
 KORG_API int korg_device_status(korg_ctx *ctx);
+/* Self-test of that path, no counterpart in the reference: one block waits (at most `polls`
+ * polls) on an mbarrier that nothing arrives on, the way the line adjoint waits for staged data,
+ * sets the error word and returns; the call returns korg_device_status, i.e. KORG_ETIMEOUT, and
+ * leaves the context usable. */
+KORG_API int korg_selftest_wait_timeout(korg_ctx *ctx, int polls);
 
 /* MolecularCrossSection(linelist, wl_params; cutoff_alpha, vmic_vals, log_temp_vals) --
  * src/molecular_cross_sections.jl:51-88: the absorption cross-section per molecule of one

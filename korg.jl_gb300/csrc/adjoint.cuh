@@ -529,10 +529,23 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
                  : "memory");
     return ok != 0;
 }
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
-    for (int k = 0; k < (1 << 22); k++)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int limit = 1 << 22) {
+    for (int k = 0; k < limit; k++)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
+}
+
+// A bounded wait on an mbarrier that nothing arrives on: exercises the timeout path of the
+// staged-data waits (the error word is set and the kernel returns) without a fault or hang.
+__global__ void wait_timeout_selftest_kernel(int* err, int limit) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    const bool ok = mbar_wait(&bar, 0u, limit);
+    if (__syncthreads_or(!ok) && threadIdx.x == 0) *reinterpret_cast<volatile int*>(err) = 1;
 }
 
 // Far-Lorentz branch of voigt_hjerting (line_absorption.jl:305-308: a > 1.4, or a > 0.2 with

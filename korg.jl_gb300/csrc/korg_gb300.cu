@@ -1572,6 +1572,14 @@ KORG_API int korg_device_status(korg_ctx* ctx) {
     return take_device_error(ctx);
 }
 
+KORG_API int korg_selftest_wait_timeout(korg_ctx* ctx, int polls) {
+    if (!ctx || polls < 1) return KORG_EINVAL;
+    KCUDA(cudaSetDevice(ctx->device));
+    wait_timeout_selftest_kernel<<<1, 64, 0, ctx->stream>>>(ctx->dev_err_dev, polls);
+    KCUDA(cudaGetLastError());
+    return korg_device_status(ctx);
+}
+
 KORG_API int korg_synthesize_vjp_dev(korg_ctx* ctx, const korg_synth_inputs* in, const korg_lines* lines,
                                      const korg_lines* lines5, const double* wls, int64_t nwl, int precision,
                                      const double* dflux, const double* dcntm, const korg_synth_grads* grads,

@@ -132,6 +132,7 @@ def lib():
             L.korg_get_tile_config.argtypes = [vp, C.c_int32, C.c_int, _ip, _ip, _ip, _ip]
             L.korg_set_tile_config.argtypes = [vp, C.c_int32, C.c_int, C.c_int32, C.c_int32, C.c_int32]
             L.korg_device_status.argtypes = [vp]
+            L.korg_selftest_wait_timeout.argtypes = [vp, C.c_int]
             _lib = L
     return _lib
 
@@ -145,7 +146,8 @@ def exported_symbols():
             "korg_math_selftest", "korg_line_absorption_noalloc", "korg_synthesize_batch_dev",
             "korg_set_batch_options", "korg_get_tile_config", "korg_set_tile_config", "korg_synthesize_vjp", "korg_synthesize_vjp_dev",
             "korg_radiative_transfer_general", "korg_molecular_cross_section_dev",
-            "korg_interpolate_molecular_cross_section_dev", "korg_device_status"]
+            "korg_interpolate_molecular_cross_section_dev", "korg_device_status",
+            "korg_selftest_wait_timeout"]
 
 
 def _p(a, kind=_dp):
