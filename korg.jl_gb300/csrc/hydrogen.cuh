@@ -356,7 +356,7 @@ struct HTileArgs {
 };
 
 template <bool MIXED, int KMAX>
-__global__ void __launch_bounds__(512, 1) hline_tile_kernel(HTileArgs a) {
+__global__ void __launch_bounds__(512, (MIXED && KMAX <= 16) ? 2 : 1) hline_tile_kernel(HTileArgs a) {
     const int tid = threadIdx.x;
     const int L = a.L, G = a.G;
     const int TW = blockDim.x / G;
@@ -379,6 +379,7 @@ __global__ void __launch_bounds__(512, 1) hline_tile_kernel(HTileArgs a) {
         if (!live) continue;
         const double* kd = t < a.ntrans ? a.logdnu + a.d_off[t] : nullptr;
         const float* kd32 = t < a.ntrans ? a.logdnu32 + a.d_off[t] : nullptr;
+        int hint = -1;  // knot interval of the previous layer of this transition (mixed)
 #pragma unroll
         for (int k = 0; k < KMAX; k++) {
             const int l = g + G * k;
@@ -419,11 +420,25 @@ __global__ void __launch_bounds__(512, 1) hline_tile_kernel(HTileArgs a) {
                 } else if (x >= kd32[nDt - 1]) {
                     v = Q[nDt - 1];
                 } else {
-                    int lo = 1, hi = nDt - 1;  // kd32[lo] < x < kd32[hi]
-                    while (hi - lo > 1) {
-                        const int mid = (lo + hi) >> 1;
-                        if (kd32[mid] <= x) lo = mid; else hi = mid;
+                    // kd32[1] < x < kd32[nDt - 1]: the interval with kd32[lo] <= x < kd32[lo + 1].
+                    // Neighbouring layers differ little in log(dnu / F0), so after the first
+                    // layer the interval is found by walking from the previous one (both walks
+                    // stop inside [1, nDt - 2] by the bounds on x); the result is the binary
+                    // search's.
+                    int lo;
+                    if (hint < 0) {
+                        lo = 1;
+                        int hi = nDt - 1;
+                        while (hi - lo > 1) {
+                            const int mid = (lo + hi) >> 1;
+                            if (kd32[mid] <= x) lo = mid; else hi = mid;
+                        }
+                    } else {
+                        lo = min(max(hint, 1), nDt - 2);
+                        while (kd32[lo] > x) lo--;
+                        while (kd32[lo + 1] <= x) lo++;
                     }
+                    hint = lo;
                     const float w = (x - kd32[lo]) / (kd32[lo + 1] - kd32[lo]);
                     v = (1.f - w) * Q[lo] + w * Q[lo + 1];
                 }
