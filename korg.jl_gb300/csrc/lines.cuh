@@ -79,7 +79,8 @@ struct PrepOut {
     int32_t Lp, K, G;
     unsigned long long* evals;   // running totals: evaluations, lines in window
     unsigned long long* nlines;
-    float4* params_w;        // [n][Lp] mixed, or null: asymptotic-wing coefficients {A1, A2, A3, cref}
+    float4* params_w;        // [n][Lp] mixed, or null: wing constants ({A1, A2, A3, -cref} for an
+                             //   asymptotic-branch layer, the packed constants for a far-Lorentz one)
 };
 
 // Per-line quantities shared by every layer (line_absorption.jl:83,101,105,219).
@@ -254,7 +255,6 @@ __device__ __forceinline__ void argmax_reduce(float& v, int& idx) {
 struct LinePrep32 {
     double El, Eu, strength;   // FP64 line-strength inputs
     float wlc, k_m, wl2c, grad, gstark, v1, abo_pre, vexp, invmu, t32;
-    float cref;                // 2 sigma^2 in layer 0: the scale of the wing coefficients
     int32_t flags, sp, ki;     // flags: 1 molecule, 2 ABO broadening; ki: continuum knot interval
 };
 constexpr int PREP_WARPS = 8;
@@ -296,11 +296,6 @@ __global__ void __launch_bounds__(32 * PREP_WARPS) line_prep_mixed_kernel(LinesD
         p.vexp = float(1 - q.v2);
         p.invmu = float(1 / (1.008 * AMU_CGS)) + 1.f / float(q.m);
         p.t32 = float(kp_mine.t);
-        {
-            const LayerConst c0 = lc[0];
-            const float sigma0 = p.wlc * sqrtf(p.k_m * c0.T32 + 0.5f * c0.xi32 * c0.xi32);
-            p.cref = 2.f * sigma0 * sigma0;
-        }
         p.flags = (q.mol ? 1 : 0) | ((!q.mol && q.v2 != -1) ? 2 : 0);
         p.sp = q.sp;
         p.ki = int32_t(kp_mine.i);
@@ -317,62 +312,68 @@ __global__ void __launch_bounds__(32 * PREP_WARPS) line_prep_mixed_kernel(LinesD
         int dl = 0, ll = 0;
         float4* dst = reinterpret_cast<float4*>(out.params) + i * Lp;
         float4* dstw = out.params_w ? out.params_w + i * Lp : nullptr;
-        for (int l = lane; l < Lp; l += 32) {
-            if (l >= L) {
-                dst[l] = make_float4(1.f, 0.f, 0.f, 0.f);
-                if (dstw) dstw[l] = make_float4(0.f, 0.f, 0.f, q.cref);
+        float cref = 0.f;
+        for (int l0 = 0; l0 < Lp; l0 += 32) {
+            const int l = l0 + lane;
+            float4 p = make_float4(1.f, 0.f, 0.f, 0.f);  // padding layers contribute nothing
+            bool A = true;
+            if (l < L) {
+                const LayerConst c = lc[l];
+                const float sigma = q.wlc * sqrtf(q.k_m * c.T32 + 0.5f * c.xi32 * c.xi32);
+                float G = q.grad;
+                if (!mol) {
+                    float vdw;
+                    if (!abo) {
+                        vdw = q.v1 * c.vdw3_32;
+                    } else {
+                        const float vbar = sqrtf(float(8 * KBOLTZ_CGS / PI) * c.T32 * q.invmu);
+                        vdw = q.abo_pre * powf(vbar * 1e-6f, q.vexp);
+                    }
+                    G = G + c.ne32 * (q.gstark * c.stark6_32) + c.nv32 * vdw;
+                }
+                const float gamma = G * q.wl2c;
+                const double levels = fexp64(-c.beta * q.El, s_math) - fexp64(-c.beta * q.Eu, s_math);  // FP64
+                const float amp = float(q.strength * levels * lay.n_div_U[int64_t(q.sp) * L + l]);
+                const double* row = cn.vals + int64_t(l) * cn.nk;
+                const float acntm = cn.nk == 1 ? float(row[0])
+                                               : float(row[q.ki]) * (1.f - q.t32) + float(row[q.ki + 1]) * q.t32;
+                const float rho = acntm * float(cutoff) / amp;
+                const float dw = inverse_gaussian32(rho, sigma), lw = inverse_lorentz32(rho, gamma);
+                if (dw > dmax) { dmax = dw; dl = l; }
+                if (lw > lmax) { lmax = lw; ll = l; }
+                const float s = 1.f / (sigma * 1.41421356f);
+                const float a = gamma * s;
+                const float scale = s * 0.56418958f * amp;  // 1/sqrt(pi)
+                A = a <= 0.2f;
+                p.x = 2.f * sigma * sigma;
+                p.y = a;
+                p.z = A ? a * 0.56418958f * scale : 1.f / (gamma * gamma);
+                p.w = scale;
+                // v >= 5 (a <= 0.2) or a + v >= 3.2 (0.2 < a <= 1.4) or any v (a > 1.4), v = x / sqrt(c)
+                s_bnd[l] = (A ? 5.f : (a <= 1.4f ? 3.2f - a : 0.f)) * sqrtf(p.x) * 1.0001f;
+                s_cls[l] = A;
+            } else if (l < Lp) {
                 s_bnd[l] = 0.f;
                 s_cls[l] = 1;
-                continue;
             }
-            const LayerConst c = lc[l];
-            const float sigma = q.wlc * sqrtf(q.k_m * c.T32 + 0.5f * c.xi32 * c.xi32);
-            float G = q.grad;
-            if (!mol) {
-                float vdw;
-                if (!abo) {
-                    vdw = q.v1 * c.vdw3_32;
-                } else {
-                    const float vbar = sqrtf(float(8 * KBOLTZ_CGS / PI) * c.T32 * q.invmu);
-                    vdw = q.abo_pre * powf(vbar * 1e-6f, q.vexp);
+            if (l0 == 0) cref = __shfl_sync(0xffffffffu, p.x, 0);  // 2 sigma^2 of layer 0
+            if (l < Lp) {
+                dst[l] = p;
+                if (dstw) {
+                    // wing constants: a layer in the asymptotic branch as a cubic in t' = cref / dl^2,
+                    // w u (1 + 1.5 u + 3.75 u^2) = A1 t' + A2 t'^2 + A3 t'^3 with u = 1/v^2 = (c / cref) t',
+                    // marked by .w = -cref; a far-Lorentz layer keeps its packed constants (.w >= 0)
+                    float4 pw = p;
+                    if (A) {
+                        const float rr = p.x / cref;
+                        pw.x = p.z * rr;
+                        pw.y = 1.5f * pw.x * rr;
+                        pw.z = 2.5f * pw.y * rr;
+                        pw.w = -cref;
+                    }
+                    dstw[l] = pw;
                 }
-                G = G + c.ne32 * (q.gstark * c.stark6_32) + c.nv32 * vdw;
             }
-            const float gamma = G * q.wl2c;
-            const double levels = fexp64(-c.beta * q.El, s_math) - fexp64(-c.beta * q.Eu, s_math);  // FP64
-            const float amp = float(q.strength * levels * lay.n_div_U[int64_t(q.sp) * L + l]);
-            const double* row = cn.vals + int64_t(l) * cn.nk;
-            const float acntm = cn.nk == 1 ? float(row[0])
-                                           : float(row[q.ki]) * (1.f - q.t32) + float(row[q.ki + 1]) * q.t32;
-            const float rho = acntm * float(cutoff) / amp;
-            const float dw = inverse_gaussian32(rho, sigma), lw = inverse_lorentz32(rho, gamma);
-            if (dw > dmax) { dmax = dw; dl = l; }
-            if (lw > lmax) { lmax = lw; ll = l; }
-            const float s = 1.f / (sigma * 1.41421356f);
-            const float a = gamma * s;
-            const float scale = s * 0.56418958f * amp;  // 1/sqrt(pi)
-            const bool A = a <= 0.2f;
-            float4 p;
-            p.x = 2.f * sigma * sigma;
-            p.y = a;
-            p.z = A ? a * 0.56418958f * scale : 1.f / (gamma * gamma);
-            p.w = scale;
-            dst[l] = p;
-            if (dstw) {
-                // asymptotic wing as a cubic in t' = cref / dl^2:  w u (1 + 1.5 u + 3.75 u^2) with
-                // u = 1/v^2 = rho t', rho = c / cref, is A1 t' + A2 t'^2 + A3 t'^3
-                float4 pw = make_float4(0.f, 0.f, 0.f, q.cref);
-                if (A) {
-                    const float rho = p.x / q.cref;
-                    pw.x = p.z * rho;
-                    pw.y = 1.5f * pw.x * rho;
-                    pw.z = 2.5f * pw.y * rho;
-                }
-                dstw[l] = pw;
-            }
-            // v >= 5 (a <= 0.2) or a + v >= 3.2 (0.2 < a <= 1.4) or any v (a > 1.4), v = x / sqrt(c)
-            s_bnd[l] = (A ? 5.f : (a <= 1.4f ? 3.2f - a : 0.f)) * sqrtf(p.x) * 1.0001f;
-            s_cls[l] = A;
         }
         __syncwarp();
         argmax_reduce(dmax, dl);
@@ -512,7 +513,7 @@ struct TileArgs {
     const uint32_t* amask;
     const int32_t *lb, *ub;
     const int32_t *tier_idx, *tier_ci, *tier_start, *unsorted;
-    const float4* params_w;   // mixed, or null: asymptotic-wing coefficients {A1, A2, A3, cref}
+    const float4* params_w;   // mixed, or null: wing constants (see PrepOut)
 };
 
 // first index in [lo, hi) with a[i] >= v (a non-decreasing)
@@ -567,8 +568,8 @@ __device__ __forceinline__ double far_lorentz64(const P64& p, double x2) {
 // One tile of TW = blockDim.x / G wavelengths x all layers, computed by one CTA.  Thread (j, g)
 // owns wavelength j and the K consecutive (padded) layers g*K .. g*K+K-1.  `smem` is the
 // dynamic shared memory of the launch (two line-constant buffers, then the LineStage array).
-// In the mixed split form a line whose layers of the group are all in the asymptotic wing over
-// the tile is staged as its wing coefficients: three FMAs per evaluation.
+// In the mixed split form a line whose layers of the group are all in wing branches over the
+// tile is staged as its wing constants: three FMAs per asymptotic-branch evaluation.
 template <bool MIXED, int K>
 __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, int gsplit, unsigned char* smem) {
     using P = typename ParamT<MIXED>::type;
@@ -667,7 +668,7 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
             st.ub = ubi;
             st.cls = cls;
             st.li = int32_t(i);
-            st.cref = wcoef ? a.params_w[i * Lp].w : 0.f;
+            st.cref = wcoef ? reinterpret_cast<const float4*>(a.params)[i * Lp].x : 0.f;  // 2 sigma^2, layer 0
             s_ln[s_warp[warp] + __popc(m & ((1u << lane) - 1))] = st;
         }
         const int cnt = s_count;
@@ -683,7 +684,7 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
                     const int b = e / chunks16, r = e - b * chunks16;
                     const LineStage& sl = s_ln[b0 + b];
                     const int64_t li = sl.li;
-                    const void* src = (wcoef && ((sl.cls >> (2 * g)) & 3u) == 1u) ? static_cast<const void*>(a.params_w)
+                    const void* src = (wcoef && ((sl.cls >> (2 * g)) & 3u) != 0u) ? static_cast<const void*>(a.params_w)
                                                                                   : a.params;
                     cp_async16(buf + (size_t(b) * chunks16 + r) * 16,
                                reinterpret_cast<const unsigned char*>(src) +
@@ -727,6 +728,17 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
                                 const float4 p = pr[k];
                                 const float iv = t * p.x;
                                 part[k] = fmaf(p.z * iv, fmaf(fmaf(3.75f, iv, 1.5f), iv, 1.f), part[k]);
+                            }
+                        } else if (cls == 2u && wcoef) {
+                            // every layer in a wing branch: the asymptotic cubic (.w < 0) or far Lorentz
+                            const float tp = t * st.cref;
+#pragma unroll
+                            for (int k = 0; k < K; k++) {
+                                const float4 p = pr[k];
+                                if (p.w < 0.f)
+                                    part[k] = fmaf(tp, fmaf(tp, fmaf(tp, p.z, p.y), p.x), part[k]);
+                                else
+                                    part[k] += far_lorentz32(p, x2);
                             }
                         } else if (cls == 2u) {
                             // every layer in a wing branch, chosen per layer (uniform across the warp)
