@@ -349,7 +349,7 @@ def synthesize_prepared(inp: SynthesisInputs, precision="mixed", return_alpha=Fa
     ctx.check(ctx.lib.korg_synthesize(ctx.h, C.byref(s), C.byref(lines), C.byref(lines5), _lib._p(w), nwl,
                                       _prec(precision), _lib._p(flux), _lib._p(cntm), _lib._p(alpha), _lib._p(aref)))
     return SynthesisResult(flux=flux, cntm=cntm, alpha=None if alpha is None else alpha.T, alpha_ref=aref,
-                           wavelengths=inp.wls.all_wls * 1e8, subspectra=inp.wls.subspectrum_indices(),
+                           wavelengths=inp.wls.all_wls_angstrom, subspectra=inp.wls.subspectrum_indices(),
                            line_evals=ctx.stats().line_evals)
 
 

@@ -162,6 +162,16 @@ class Wavelengths:
             i += n
         return out
 
+    @property
+    def all_wls_angstrom(self):
+        """every grid point in Angstrom (computed once, shared read-only)"""
+        a = self.__dict__.get("_all_wls_A")
+        if a is None or len(a) != len(self.all_wls):
+            a = self.all_wls * 1e8
+            a.flags.writeable = False
+            self.__dict__["_all_wls_A"] = a
+        return a
+
     def subspectrum_indices(self):
         out, i = [], 0
         for _, _, n in self.ranges:
