@@ -623,6 +623,8 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
     const int warp = tid >> 5, lane = tid & 31, nwarps = nthr >> 5;
     const int chunks16 = SL * int(sizeof(P) / 16);  // 16-byte pieces of one line's staged constants
     const bool wcoef = MIXED && gsplit >= 0 && a.params_w != nullptr;
+    const int cb0 = tid / chunks16, cr0 = tid - cb0 * chunks16;       // this thread's first staged piece
+    const int cdb = nthr / chunks16, cdr = nthr - cdb * chunks16;     // and the step between its pieces
     const int64_t src0 = gsplit >= 0 ? int64_t(g) * K * int64_t(sizeof(P) / 16) : 0;
     for (int tier = 0; tier < NTIER; tier++)
     for (int64_t base = s_tier[tier][0]; base < s_tier[tier][1]; base += nthr) {
@@ -680,8 +682,10 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
             if (q < nq) {
                 const int b0 = q * B, nb = min(B, cnt - b0);
                 unsigned char* buf = smem + size_t(q & 1) * a.region;
+                // piece e = tid + k nthr of the batch is (line b, chunk r) = divmod(e, chunks16),
+                // stepped without a division
+                int b = cb0, r = cr0;
                 for (int e = tid; e < nb * chunks16; e += nthr) {
-                    const int b = e / chunks16, r = e - b * chunks16;
                     const LineStage& sl = s_ln[b0 + b];
                     const int64_t li = sl.li;
                     const void* src = (wcoef && ((sl.cls >> (2 * g)) & 3u) != 0u) ? static_cast<const void*>(a.params_w)
@@ -689,6 +693,12 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
                     cp_async16(buf + (size_t(b) * chunks16 + r) * 16,
                                reinterpret_cast<const unsigned char*>(src) +
                                    (li * Lp * int64_t(sizeof(P) / 16) + src0 + r) * 16);
+                    b += cdb;
+                    r += cdr;
+                    if (r >= chunks16) {
+                        r -= chunks16;
+                        b++;
+                    }
                 }
             }
             cp_async_commit();
