@@ -362,8 +362,9 @@ __global__ void __launch_bounds__(32 * PREP_WARPS) line_prep_mixed_kernel(LinesD
                 if (dstw) {
                     // wing constants: a layer in the asymptotic branch as a cubic in t' = cref / dl^2,
                     // w u (1 + 1.5 u + 3.75 u^2) = A1 t' + A2 t'^2 + A3 t'^3 with u = 1/v^2 = (c / cref) t',
-                    // marked by .w = -cref; a far-Lorentz layer keeps its packed constants (.w >= 0)
-                    float4 pw = p;
+                    // marked by .w = -cref; a far-Lorentz layer as {1/gamma^2, 1/(sqrt2 a), 0,
+                    // sqrt(2/pi) scale} (.w >= 0), see far_lorentz32w
+                    float4 pw = make_float4(p.z, 0.70710678118654752f / p.y, 0.f, 0.7978845608028654f * p.w);
                     if (A) {
                         const float rr = p.x / cref;
                         pw.x = p.z * rr;
@@ -558,6 +559,15 @@ __device__ __forceinline__ float far_lorentz32(float4 p, float x2) {
     const float au2 = au * au;
     return 0.7978845608028654f * au * (1.f + (3.f * r2 - 1.f + ((r2 - 2.f) * 15.f * r2 + 2.f) * au2) * au2) * p.w;
 }
+// The same from the wing constants {1/gamma^2, 1/(sqrt2 a), -, sqrt(2/pi) scale}, accumulated:
+// au = 1/(sqrt2 a (1 + r^2)), H scale = sqrt(2/pi) scale au (1 + (3r^2 - 1 + (15r^4 - 30r^2 + 2) au^2) au^2).
+__device__ __forceinline__ float far_lorentz32w(float4 p, float x2, float acc) {
+    const float r2 = x2 * p.x;
+    const float au = __fdividef(p.y, r2 + 1.f);
+    const float au2 = au * au;
+    const float poly = fmaf(fmaf(fmaf(fmaf(15.f, r2, -30.f), r2, 2.f), au2, fmaf(3.f, r2, -1.f)), au2, 1.f);
+    return fmaf(au * p.w, poly, acc);
+}
 __device__ __forceinline__ double far_lorentz64(const P64& p, double x2) {
     const double r2 = x2 * p.w;
     const double au = 1 / SQRT_2 / ((r2 + 1) * p.a);
@@ -748,7 +758,7 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
                                 if (p.w < 0.f)
                                     part[k] = fmaf(tp, fmaf(tp, fmaf(tp, p.z, p.y), p.x), part[k]);
                                 else
-                                    part[k] += far_lorentz32(p, x2);
+                                    part[k] = far_lorentz32w(p, x2, part[k]);
                             }
                         } else if (cls == 2u) {
                             // every layer in a wing branch, chosen per layer (uniform across the warp)
