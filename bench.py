@@ -137,6 +137,17 @@ class Clocks:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def replica_rate(ms, world, device, tdist=None):
+    """Whole-job rate of `world` independent replicas (one spectrum per step each): the slowest
+    rank's mean step time (max over ranks) and world spectra per that time."""
+    if tdist is not None and world > 1:
+        import torch
+        t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, world * 1000.0 / ms
+
+
 def traffic_from_profiles():
     """DRAM bytes per launch of the tile kernel from the committed ncu summary, if present."""
     path = os.path.join(ROOT, "profiles", "ncu_line_tile_kernel_cfg1.md")
@@ -277,11 +288,7 @@ def run_korg(args):
     if dist:
         tdist.barrier()
     clocks = clk.stop()
-    ms = statistics.mean(times)
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms, value = replica_rate(statistics.mean(times), world, dev, tdist if dist else None)
     flux32 = flux.cpu().numpy().copy()
     cntm32 = cntm.cpu().numpy().copy()
     evals = stats.line_evals
@@ -347,7 +354,7 @@ def run_korg(args):
     launches_per_step = 1 + 5 + (3 if inp.hydrogen_lines else 0) + 5 + 1
     out = {
         "metric": METRIC,
-        "value": world * 1000.0 / ms,
+        "value": value,
         "unit": "spectra/s",
         "n_gpus": world,
         "steps": args.steps,
