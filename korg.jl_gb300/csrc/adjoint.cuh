@@ -387,6 +387,7 @@ struct LineAdjArgs {
     int32_t Ls;               // largest staged row stride (elements)
     int32_t bulk;             // rows of G start on 16-byte boundaries: one bulk copy per stage
     int* err;                 // set to 1 when a wait for staged data runs past its limit
+    int32_t sub;              // wavelengths per stage
 };
 
 // The items of line_adj_kernel, chunk-major so that the blocks running at any time share one
@@ -655,7 +656,8 @@ __global__ void __launch_bounds__(512, MIXED ? 2 : 1) line_adj_kernel(LineAdjArg
     const int PW = nwarps - 1;               // the producer warp
     const int TC = PW * 32;                  // consumer threads
     GT* s_g = reinterpret_cast<GT*>(s_adj);
-    int* s_order = reinterpret_cast<int*>(s_adj + sizeof(GT) * ADJ_STAGES * ADJ_SUB * a.Ls);
+    const int SUB = a.sub;                   // wavelengths per stage (<= ADJ_SUB, a multiple of 32)
+    int* s_order = reinterpret_cast<int*>(s_adj + sizeof(GT) * ADJ_STAGES * SUB * a.Ls);
     const int64_t total = a.ipre[a.npairs];
     const GT* G = static_cast<const GT*>(a.G);
     const bool bulk = a.bulk != 0;
@@ -742,7 +744,7 @@ __global__ void __launch_bounds__(512, MIXED ? 2 : 1) line_adj_kernel(LineAdjArg
         __syncthreads();
         const int ns = s_ns, lnf = s_lnf, lns = s_lns, Ls = s_Ls;
         const int64_t nj = j1 - j0 + 1;
-        const int nsub = int((nj + ADJ_SUB - 1) / ADJ_SUB);
+        const int nsub = int((nj + SUB - 1) / SUB);
         const double wl0 = a.wl[i];
         const double cref = MIXED ? double(reinterpret_cast<const float4*>(a.params)[i * Lp].x)
                                   : reinterpret_cast<const P64*>(a.params)[i * Lp].c;
@@ -753,7 +755,7 @@ __global__ void __launch_bounds__(512, MIXED ? 2 : 1) line_adj_kernel(LineAdjArg
             auto load_wl = [&](int sq, WP* v) {
 #pragma unroll
                 for (int k = 0; k < PER; k++) {
-                    const int64_t j = min(j0 + int64_t(sq) * ADJ_SUB + lane + 32 * k, j1);
+                    const int64_t j = min(j0 + int64_t(sq) * SUB + lane + 32 * k, j1);
                     if constexpr (MIXED) v[k] = a.wl2[j];
                     else v[k] = a.wls[j];
                 }
@@ -764,9 +766,9 @@ __global__ void __launch_bounds__(512, MIXED ? 2 : 1) line_adj_kernel(LineAdjArg
                 const int64_t gq = g0 + sq;
                 const int b = int(gq % ADJ_STAGES);
                 if (gq >= ADJ_STAGES) wait(&s_empty[b], unsigned((gq / ADJ_STAGES - 1) & 1));
-                const int64_t js = j0 + int64_t(sq) * ADJ_SUB;
-                const int nw = int(min(int64_t(ADJ_SUB), j1 - js + 1));
-                GT* dst = s_g + size_t(b) * ADJ_SUB * Ls;
+                const int64_t js = j0 + int64_t(sq) * SUB;
+                const int nw = int(min(int64_t(SUB), j1 - js + 1));
+                GT* dst = s_g + size_t(b) * SUB * Ls;
                 const GT* src = G + js * L;
                 if (bulk) {
                     if (lane == 0) {
@@ -848,8 +850,8 @@ __global__ void __launch_bounds__(512, MIXED ? 2 : 1) line_adj_kernel(LineAdjArg
                 const int64_t gq = g0 + sq;
                 const int b = int(gq % ADJ_STAGES);
                 wait(&s_full[b], unsigned((gq / ADJ_STAGES) & 1));
-                const int nw = int(min(int64_t(ADJ_SUB), nj - int64_t(sq) * ADJ_SUB));
-                const GT* gb = s_g + size_t(b) * ADJ_SUB * Ls + (active ? l : 0);
+                const int nw = int(min(int64_t(SUB), nj - int64_t(sq) * SUB));
+                const GT* gb = s_g + size_t(b) * SUB * Ls + (active ? l : 0);
                 const W* wb = s_w[b];
                 if (active) {
                     const R xmin = s_xmin[b];
@@ -936,19 +938,25 @@ __global__ void __launch_bounds__(512, MIXED ? 2 : 1) line_adj_kernel(LineAdjArg
 // threads per layer (at least 4 warps, at most 15) and one producer warp; Ls is the largest
 // staged row stride an item may pick (L itself when G rows are bulk-copied).
 struct AdjShape {
-    int Ls, threads, bulk;
+    int Ls, threads, bulk, sub;
 };
 inline AdjShape adj_shape(int L, const void* G, bool mixed) {
     int t = ((5 * L + 31) / 32) * 32;
     t = t < 128 ? 128 : (t > 480 ? 480 : t);
     if (t < L) t = ((L + 31) / 32) * 32;
-    const bool bulk = (size_t(L) * (mixed ? 4 : 8)) % 16 == 0 && (reinterpret_cast<uintptr_t>(G) & 15) == 0;
-    return {bulk ? L : ((L + 3) & ~3) + 32, t + 32, int(bulk)};
+    const size_t esz = mixed ? 4 : 8;
+    const bool bulk = (size_t(L) * esz) % 16 == 0 && (reinterpret_cast<uintptr_t>(G) & 15) == 0;
+    const int Ls = bulk ? L : ((L + 3) & ~3) + 32;
+    // stages of ADJ_SUB wavelengths, fewer (whole warps of table entries) when the ring would
+    // not fit in a block's shared memory beside the static arrays (many layers in FP64)
+    int sub = ADJ_SUB;
+    while (sub > 32 && esz * ADJ_STAGES * size_t(sub) * Ls + sizeof(int) * size_t(Ls) > size_t(216) * 1024) sub -= 32;
+    return {Ls, t + 32, int(bulk), sub};
 }
 
 // Dynamic shared memory of line_adj_kernel: the staged G ring, then the per-item layer order.
 inline size_t adj_smem(const AdjShape& sh, bool mixed) {
-    return (mixed ? sizeof(float) : sizeof(double)) * ADJ_STAGES * ADJ_SUB * size_t(sh.Ls) +
+    return (mixed ? sizeof(float) : sizeof(double)) * ADJ_STAGES * size_t(sh.sub) * size_t(sh.Ls) +
            sizeof(int) * size_t(sh.Ls);
 }
 

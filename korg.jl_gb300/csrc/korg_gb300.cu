@@ -891,7 +891,7 @@ int run_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& ln, cons
             KCUDA(cudaGetLastError());
         }
         LineAdjArgs la{Gp, g32_in, w, wl2, nw, L, Lp, lns.wl, sc.params, sc.lb, sc.ub, sc.tier_idx, ilo, ipre, npairs,
-                       dpar, ctr, sh.Ls, sh.bulk, ctx->dev_err_dev};
+                       dpar, ctr, sh.Ls, sh.bulk, ctx->dev_err_dev, sh.sub};
         const int threads = sh.threads;
         if ((g32_in != 0) != mixed) return set_err(ctx, KORG_EINVAL, "opacity cotangent precision mismatch");
         const size_t smem = adj_smem(sh, mixed);

@@ -165,3 +165,26 @@ def test_vjp_reusing_the_forward_opacity(ctx, precision):
     _, g1 = loss_and_gradient(inp, obs, precision=precision, reuse_forward=True, ctx=ctx)
     for k in g0:
         np.testing.assert_allclose(g1[k], g0[k], rtol=1e-9, atol=1e-14 * np.max(np.abs(g0[k])) + 1e-300)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_vjp_many_layers(ctx, precision):
+    """128 layers, the most the reverse mode takes: the staged-G ring of the FP64 line adjoint
+    shrinks its stages to fit shared memory (rows of 1 kB)."""
+    from korg_gb300 import synthetic
+    from korg_gb300.synthesize import loss_and_gradient
+    w = synthetic.config0(seed=4, n_lines=300)
+    w.L = 128
+    w.wavelengths = (5000.0, 5015.0)
+    w.linelist = synthetic.synthetic_linelist(300, 5001.0, 5014.0, seed=4)
+    inp = synthetic.prepare(w)
+    obs = _obs(inp, ctx)
+    _, g = loss_and_gradient(inp, obs, precision=precision, ctx=ctx)
+    if precision == "fp64":
+        for field, idx in [("T", 100), ("log_gf", _strong_lines(inp, 1)[0])]:
+            fd, floor = _fd(inp, obs, ctx, field, idx, noise=True)
+            assert abs(g[field][idx] - fd) <= 1e-4 * abs(fd) + 1e-7 * np.max(np.abs(g[field])) + floor, (field, fd)
+    else:
+        _, g64 = loss_and_gradient(inp, obs, precision="fp64", ctx=ctx)
+        for k in ("T", "ne", "log_gf"):
+            assert np.max(np.abs(g[k] - g64[k])) <= 2e-3 * np.max(np.abs(g64[k])), k
