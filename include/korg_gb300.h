@@ -249,6 +249,50 @@ KORG_API int korg_device_status(korg_ctx *ctx);
  * leaves the context usable. */
 KORG_API int korg_selftest_wait_timeout(korg_ctx *ctx, int polls);
 
+/* Spectral post-processing (src/utils.jl), device pointers, FP64, stream-ordered.
+ *
+ * korg_apply_lsf_dev: apply_LSF / compute_LSF_matrix(...) * flux (src/utils.jl:45-58, 94-155).
+ * Each output wavelength out_wls[i] (cm) gets the Gaussian of FWHM out_wls[i] / R cut at
+ * window_size sigma and renormalised over the window, applied to flux [nspec][nwl] on the sorted
+ * grid wls [nwl] (cm): out [nspec][nout].  R has one value (nR = 1) or one per output
+ * (nR = nout; the reference's R(lambda) function evaluated by the caller at out_wls in A).
+ * apply_LSF is the case out_wls = wls.
+ * korg_apply_lsf_vjp_dev: reverse mode, dflux [nspec][nwl] += L^T dout [nspec][nout].
+ * korg_lsf_windows_dev / korg_lsf_matrix_values_dev: compute_LSF_matrix in CSR form -- the
+ * window [lb[i], ub[i]] (0-based, inclusive) of every output, then, with row_ptr the exclusive
+ * scan of ub - lb + 1, the normalised weights vals[row_ptr[i] + j - lb[i]]. */
+KORG_API int korg_apply_lsf_dev(korg_ctx *ctx, const double *wls, int64_t nwl, const double *out_wls,
+                                int64_t nout, const double *R, int64_t nR, double window_size,
+                                const double *flux, int32_t nspec, double *out, void *stream);
+KORG_API int korg_apply_lsf_vjp_dev(korg_ctx *ctx, const double *wls, int64_t nwl, const double *out_wls,
+                                    int64_t nout, const double *R, int64_t nR, double window_size,
+                                    const double *dout, int32_t nspec, double *dflux, void *stream);
+KORG_API int korg_lsf_windows_dev(korg_ctx *ctx, const double *wls, int64_t nwl, const double *out_wls,
+                                  int64_t nout, const double *R, int64_t nR, double window_size,
+                                  int64_t *lb, int64_t *ub, void *stream);
+KORG_API int korg_lsf_matrix_values_dev(korg_ctx *ctx, const double *wls, int64_t nwl,
+                                        const double *out_wls, int64_t nout, const double *R, int64_t nR,
+                                        double window_size, const int64_t *row_ptr, double *vals,
+                                        void *stream);
+/* korg_apply_rotation_dev: apply_rotation(flux, wls, vsini, eps) (src/utils.jl:168-240) --
+ * rotational broadening with linear limb darkening, each uniform wavelength range separately.
+ * wls [nwl] (cm) are the grid values; ranges (a host array of at most 64) give each range's
+ * length and step (cm), in order, covering the grid; vsini in km/s.  flux, out [nspec][nwl].
+ * korg_apply_rotation_vjp_dev: reverse mode, dflux += R^T dout. */
+typedef struct {
+    int64_t n;      /* points of the range */
+    double start;   /* first wavelength (cm) */
+    double step;    /* step (cm) */
+} korg_wl_range;
+KORG_API int korg_apply_rotation_dev(korg_ctx *ctx, const double *wls, int64_t nwl,
+                                     const korg_wl_range *ranges, int32_t nranges, double vsini,
+                                     double eps, const double *flux, int32_t nspec, double *out,
+                                     void *stream);
+KORG_API int korg_apply_rotation_vjp_dev(korg_ctx *ctx, const double *wls, int64_t nwl,
+                                         const korg_wl_range *ranges, int32_t nranges, double vsini,
+                                         double eps, const double *dout, int32_t nspec, double *dflux,
+                                         void *stream);
+
 /* MolecularCrossSection(linelist, wl_params; cutoff_alpha, vmic_vals, log_temp_vals) --
  * src/molecular_cross_sections.jl:51-88: the absorption cross-section per molecule of one
  * species' lines on a (vmic, T, wavelength) grid, with the line-opacity kernels.  Device

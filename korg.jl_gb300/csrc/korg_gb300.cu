@@ -19,6 +19,7 @@
 #include "adjoint.cuh"
 #include "hydrogen.cuh"
 #include "lines.cuh"
+#include "postprocess.cuh"
 #include "physics.cuh"
 #include "rt.cuh"
 
@@ -1703,6 +1704,137 @@ KORG_API int korg_synthesize_vjp(korg_ctx* ctx, const korg_synth_inputs* in, con
             KCUDA(cudaMemcpyAsync(host_out[k], dev_out[k], 8 * sizes[k], cudaMemcpyDeviceToHost, ctx->stream));
     KCUDA(cudaStreamSynchronize(ctx->stream));
     return take_device_error(ctx);
+}
+
+// ------------------------------------------------------------------ post-processing
+// Gaussian LSF and rotational broadening (src/utils.jl:45-240); kernels in postprocess.cuh.
+namespace {
+int lsf_args(korg_ctx* ctx, const double* wls, int64_t nwl, const double* owl, int64_t nout, const double* R,
+             int64_t nR, double window, LsfArgs* a) {
+    if (!wls || nwl < 1 || !owl || nout < 1 || !R || (nR != 1 && nR != nout) || !(window > 0))
+        return set_err(ctx, KORG_EINVAL, "bad LSF arguments");
+    *a = LsfArgs{wls, nwl, owl, nout, R, nR == nout && nout > 1 ? 1 : 0, window, 2 * std::sqrt(2 * std::log(2.0))};
+    return KORG_OK;
+}
+int rot_args(korg_ctx* ctx, const double* wls, int64_t nwl, const korg_wl_range* ranges, int32_t nranges,
+             double vsini, double eps, RotArgs* a) {
+    if (!wls || nwl < 1 || !ranges || nranges < 1 || nranges > ROT_MAX_RANGES || !(vsini >= 0))
+        return set_err(ctx, KORG_EINVAL, "bad rotation arguments (at most %d wavelength ranges)", ROT_MAX_RANGES);
+    *a = RotArgs{};
+    a->wls = wls;
+    a->nwl = nwl;
+    a->nranges = nranges;
+    int64_t first = 0;
+    for (int k = 0; k < nranges; k++) {
+        if (ranges[k].n < 1) return set_err(ctx, KORG_EINVAL, "empty wavelength range");
+        a->r[k] = RotRange{first, ranges[k].n, ranges[k].step};
+        first += ranges[k].n;
+    }
+    if (first != nwl) return set_err(ctx, KORG_EINVAL, "the ranges do not cover the %lld wavelengths", (long long)nwl);
+    a->v_over_c = vsini * 1e5 / C_CGS;  // km/s -> cm/s (:198)
+    a->c1 = 2 * (1 - eps);              // :205-209
+    a->c2 = PI * eps / 2;
+    a->c3 = PI * (1 - eps / 3);
+    return KORG_OK;
+}
+__global__ void add_kernel(double* dst, const double* src, int64_t n) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] += src[i];
+}
+unsigned warp_blocks(int64_t n) { return unsigned((n * 32 + 255) / 256); }
+}  // namespace
+
+KORG_API int korg_apply_lsf_dev(korg_ctx* ctx, const double* wls, int64_t nwl, const double* out_wls, int64_t nout,
+                                const double* R, int64_t nR, double window_size, const double* flux, int32_t nspec,
+                                double* out, void* stream) {
+    if (!ctx) return KORG_EINVAL;
+    LsfArgs a;
+    KCHECK(lsf_args(ctx, wls, nwl, out_wls, nout, R, nR, window_size, &a));
+    if (!flux || !out || nspec < 1) return set_err(ctx, KORG_EINVAL, "bad LSF arguments");
+    KCUDA(cudaSetDevice(ctx->device));
+    lsf_apply_kernel<<<dim3(warp_blocks(nout), unsigned((nspec + LSF_SPEC - 1) / LSF_SPEC)), 256, 0,
+                       static_cast<cudaStream_t>(stream)>>>(a, flux, nspec, out);
+    KCUDA(cudaGetLastError());
+    return KORG_OK;
+}
+
+KORG_API int korg_apply_lsf_vjp_dev(korg_ctx* ctx, const double* wls, int64_t nwl, const double* out_wls,
+                                    int64_t nout, const double* R, int64_t nR, double window_size, const double* dout,
+                                    int32_t nspec, double* dflux, void* stream) {
+    if (!ctx) return KORG_EINVAL;
+    LsfArgs a;
+    KCHECK(lsf_args(ctx, wls, nwl, out_wls, nout, R, nR, window_size, &a));
+    if (!dout || !dflux || nspec < 1) return set_err(ctx, KORG_EINVAL, "bad LSF arguments");
+    KCUDA(cudaSetDevice(ctx->device));
+    lsf_vjp_kernel<<<dim3(warp_blocks(nout), unsigned((nspec + LSF_SPEC - 1) / LSF_SPEC)), 256, 0,
+                     static_cast<cudaStream_t>(stream)>>>(a, dout, nspec, dflux);
+    KCUDA(cudaGetLastError());
+    return KORG_OK;
+}
+
+KORG_API int korg_lsf_windows_dev(korg_ctx* ctx, const double* wls, int64_t nwl, const double* out_wls, int64_t nout,
+                                  const double* R, int64_t nR, double window_size, int64_t* lb, int64_t* ub,
+                                  void* stream) {
+    if (!ctx) return KORG_EINVAL;
+    LsfArgs a;
+    KCHECK(lsf_args(ctx, wls, nwl, out_wls, nout, R, nR, window_size, &a));
+    if (!lb || !ub) return set_err(ctx, KORG_EINVAL, "bad LSF arguments");
+    KCUDA(cudaSetDevice(ctx->device));
+    lsf_windows_kernel<<<unsigned((nout + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(a, lb, ub);
+    KCUDA(cudaGetLastError());
+    return KORG_OK;
+}
+
+KORG_API int korg_lsf_matrix_values_dev(korg_ctx* ctx, const double* wls, int64_t nwl, const double* out_wls,
+                                        int64_t nout, const double* R, int64_t nR, double window_size,
+                                        const int64_t* row_ptr, double* vals, void* stream) {
+    if (!ctx) return KORG_EINVAL;
+    LsfArgs a;
+    KCHECK(lsf_args(ctx, wls, nwl, out_wls, nout, R, nR, window_size, &a));
+    if (!row_ptr || !vals) return set_err(ctx, KORG_EINVAL, "bad LSF arguments");
+    KCUDA(cudaSetDevice(ctx->device));
+    lsf_values_kernel<<<warp_blocks(nout), 256, 0, static_cast<cudaStream_t>(stream)>>>(a, row_ptr, vals);
+    KCUDA(cudaGetLastError());
+    return KORG_OK;
+}
+
+KORG_API int korg_apply_rotation_dev(korg_ctx* ctx, const double* wls, int64_t nwl, const korg_wl_range* ranges,
+                                     int32_t nranges, double vsini, double eps, const double* flux, int32_t nspec,
+                                     double* out, void* stream) {
+    if (!ctx) return KORG_EINVAL;
+    RotArgs a;
+    KCHECK(rot_args(ctx, wls, nwl, ranges, nranges, vsini, eps, &a));
+    if (!flux || !out || nspec < 1) return set_err(ctx, KORG_EINVAL, "bad rotation arguments");
+    KCUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (vsini == 0) {  // :196-198
+        KCUDA(cudaMemcpyAsync(out, flux, sizeof(double) * size_t(nwl) * nspec, cudaMemcpyDeviceToDevice, s));
+        return KORG_OK;
+    }
+    rotation_kernel<false><<<dim3(unsigned((nwl + 127) / 128), unsigned((nspec + ROT_SPEC - 1) / ROT_SPEC)), 128, 0,
+                             s>>>(a, flux, nspec, out);
+    KCUDA(cudaGetLastError());
+    return KORG_OK;
+}
+
+KORG_API int korg_apply_rotation_vjp_dev(korg_ctx* ctx, const double* wls, int64_t nwl, const korg_wl_range* ranges,
+                                         int32_t nranges, double vsini, double eps, const double* dout, int32_t nspec,
+                                         double* dflux, void* stream) {
+    if (!ctx) return KORG_EINVAL;
+    RotArgs a;
+    KCHECK(rot_args(ctx, wls, nwl, ranges, nranges, vsini, eps, &a));
+    if (!dout || !dflux || nspec < 1) return set_err(ctx, KORG_EINVAL, "bad rotation arguments");
+    KCUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (vsini == 0) {
+        const int64_t n = nwl * nspec;
+        add_kernel<<<unsigned((n + 255) / 256), 256, 0, s>>>(dflux, dout, n);
+    } else {
+        rotation_kernel<true><<<dim3(unsigned((nwl + 127) / 128), unsigned((nspec + ROT_SPEC - 1) / ROT_SPEC)), 128,
+                                0, s>>>(a, dout, nspec, dflux);
+    }
+    KCUDA(cudaGetLastError());
+    return KORG_OK;
 }
 
 KORG_API int korg_molecular_cross_section_dev(korg_ctx* ctx, const korg_lines* lines, const double* wls,

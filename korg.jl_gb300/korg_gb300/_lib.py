@@ -133,6 +133,14 @@ def lib():
             L.korg_set_tile_config.argtypes = [vp, C.c_int32, C.c_int, C.c_int32, C.c_int32, C.c_int32]
             L.korg_device_status.argtypes = [vp]
             L.korg_selftest_wait_timeout.argtypes = [vp, C.c_int]
+            lsf = [vp, vp, C.c_int64, vp, C.c_int64, vp, C.c_int64, C.c_double]
+            L.korg_apply_lsf_dev.argtypes = lsf + [vp, C.c_int32, vp, vp]
+            L.korg_apply_lsf_vjp_dev.argtypes = lsf + [vp, C.c_int32, vp, vp]
+            L.korg_lsf_windows_dev.argtypes = lsf + [vp, vp, vp]
+            L.korg_lsf_matrix_values_dev.argtypes = lsf + [vp, vp, vp]
+            rot = [vp, vp, C.c_int64, C.POINTER(WlRange), C.c_int32, C.c_double, C.c_double]
+            L.korg_apply_rotation_dev.argtypes = rot + [vp, C.c_int32, vp, vp]
+            L.korg_apply_rotation_vjp_dev.argtypes = rot + [vp, C.c_int32, vp, vp]
             _lib = L
     return _lib
 
@@ -147,7 +155,8 @@ def exported_symbols():
             "korg_set_batch_options", "korg_get_tile_config", "korg_set_tile_config", "korg_synthesize_vjp", "korg_synthesize_vjp_dev",
             "korg_radiative_transfer_general", "korg_molecular_cross_section_dev",
             "korg_interpolate_molecular_cross_section_dev", "korg_device_status",
-            "korg_selftest_wait_timeout"]
+            "korg_selftest_wait_timeout", "korg_apply_lsf_dev", "korg_apply_lsf_vjp_dev", "korg_lsf_windows_dev",
+            "korg_lsf_matrix_values_dev", "korg_apply_rotation_dev", "korg_apply_rotation_vjp_dev"]
 
 
 def _p(a, kind=_dp):
@@ -187,6 +196,11 @@ def stark_struct(st, keep: Keep) -> StarkTables:
     return StarkTables(st["ntrans"], *[_p(keep.i32(st[k]), _ip) for k in ["lower", "upper", "nT", "nNe", "nD"]],
                        *[_p(keep.i64(st[k]), _lp) for k in ["t_off", "ne_off", "d_off", "p_off", "l_off"]],
                        *[_p(keep.f64(st[k])) for k in ["log_gf", "temps", "nes", "logdnu", "logP", "lambda0"]])
+
+
+class WlRange(C.Structure):
+    """korg_wl_range: one uniform wavelength range (points, first wavelength and step in cm)."""
+    _fields_ = [("n", C.c_int64), ("start", C.c_double), ("step", C.c_double)]
 
 
 class Context:
