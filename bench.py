@@ -27,6 +27,11 @@ times the batched form instead: 256 atmospheres (Teff 3500-7000 K, logg 1-5, [M/
 each with its own random 20k-200k-line subset of a 500k-line atomic + molecular list, on the
 400,001-point 15000-17000 A grid; one step = the whole batch through korg_synthesize_batch_dev
 (CUDA-graph replay, autotuned tile shape).
+
+    python bench.py --workload postprocess
+
+times the post-processing of 64 synthesised spectra on that grid: rotational broadening
+(apply_rotation) then the Gaussian LSF (R = 22,500) onto a 0.2 A observed grid.
 """
 import argparse
 import ctypes as C
@@ -59,7 +64,7 @@ def parse():
                     help="wavelength range in A (the full workload is 3000-10000)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--workload", default="synth", choices=["synth", "batch", "adjoint", "variants"])
+    ap.add_argument("--workload", default="synth", choices=["synth", "batch", "adjoint", "variants", "postprocess"])
     ap.add_argument("--tile", default=None, help="force the line tile shape: tw,stage,split (e.g. 64,32,1)")
     ap.add_argument("--spectra", type=int, default=256, help="batch workload: number of spectra")
     ap.add_argument("--adj-scale", type=float, default=1.0, help="adjoint workload: fraction of its 70k lines")
@@ -559,6 +564,97 @@ def run_batch(args):
     b.ctx.close()
 
 
+def run_postprocess(args):
+    """Post-processing of a stack of synthesised spectra, as a Fit loop does per evaluation:
+    rotational broadening on the synthesis grid, then the Gaussian LSF onto the observed grid."""
+    import numpy as np
+    import torch
+    import build as korg_build
+    from korg_gb300 import _lib
+    from korg_gb300.wavelengths import Wavelengths
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    korg_build.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    nspec, vsini, eps, R = 64, 10.0, 0.6, 22_500.0
+    g = Wavelengths((15000, 17000, 0.005))
+    obs = Wavelengths((15100, 16900, 0.2)).all_wls
+    nwl, nout = len(g), len(obs)
+    rng = np.random.default_rng(0)
+    host = torch.as_tensor(1 - 0.5 * rng.random((nspec, nwl)) ** 8).pin_memory()
+    ctx = _lib.Context(0)
+    w, o = torch.as_tensor(g.all_wls, device=dev), torch.as_tensor(obs, device=dev)
+    tR = torch.tensor([R], dtype=torch.float64, device=dev)
+    rg = (_lib.WlRange * len(g.ranges))(*[_lib.WlRange(n, a, b) for a, b, n in g.ranges])
+    flux = host.to(dev)
+    rot = torch.empty_like(flux)
+    out = torch.empty((nspec, nout), dtype=torch.float64, device=dev)
+    out_host = torch.empty((nspec, nout), dtype=torch.float64).pin_memory()
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        ctx.check(ctx.lib.korg_apply_rotation_dev(ctx.h, w.data_ptr(), nwl, rg, len(g.ranges), vsini, eps,
+                                                  flux.data_ptr(), nspec, rot.data_ptr(), stream.cuda_stream))
+        ctx.check(ctx.lib.korg_apply_lsf_dev(ctx.h, w.data_ptr(), nwl, o.data_ptr(), nout, tR.data_ptr(), 1, 4.0,
+                                             rot.data_ptr(), nspec, out.data_ptr(), stream.cuda_stream))
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    clk = Clocks(0)
+    times = []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    clocks = clk.stop()
+    ms = statistics.mean(times)
+    # end to end: host stack in, observed-grid spectra out
+    e2e = []
+    for _ in range(max(2, args.steps)):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        flux.copy_(host, non_blocking=True)
+        step()
+        out_host.copy_(out, non_blocking=True)
+        torch.cuda.synchronize()
+        e2e.append(time.perf_counter() - t1)
+    e2e_s = statistics.mean(e2e)
+    # CPU: the FP64 restatement on a sample (one spectrum: 20,000 points rotated, 500 LSF outputs),
+    # scaled to the stack by the point counts
+    import postprocess_oracle as po
+    f0 = host[0].numpy()
+    sub = Wavelengths((15000, 15100, 0.005))
+    t1 = time.perf_counter()
+    po.apply_rotation(f0[:len(sub)], sub.all_wls, sub.ranges, vsini, eps)
+    t_rot = (time.perf_counter() - t1) * nwl / len(sub)
+    t1 = time.perf_counter()
+    for i in range(500):
+        lb, ub, phi = po.lsf_bounds_and_kernel(g.all_wls, obs[i], R, 4)
+        float(np.sum(f0[lb:ub + 1] * phi))
+    t_lsf = (time.perf_counter() - t1) * nout / 500
+    cpu_s = nspec * (t_rot + t_lsf)
+    out_json = {"metric": METRIC, "value": nspec * 1000.0 / ms, "unit": "spectra/s (post-processing)", "n_gpus": 1,
+                "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded spectra)",
+                "config": {"workload": f"{nspec} spectra on 15000-17000 A @ 0.005 A ({nwl} points): rotation "
+                                       f"(vsini {vsini} km/s, eps {eps}) then Gaussian LSF R={R:.0f} onto "
+                                       f"15100-16900 A @ 0.2 A ({nout} points)",
+                           "l2": f"stack {8 * nspec * nwl / 1e6:.0f} MB > L2"},
+                "e2e": {"value": nspec / e2e_s, "unit": "spectra/s (post-processing)",
+                        "h2d_bytes_per_step": 8 * nspec * nwl, "d2h_bytes_per_step": 8 * nspec * nout},
+                "gpu_launches": 2,
+                "cpu_baseline": {"value": nspec / cpu_s, "unit": "spectra/s (post-processing)", "cores": 1,
+                                 "kind": "port", "sample": "one spectrum: 20,000 points rotated and 500 LSF outputs "
+                                                           "(numpy restatement), scaled by the point counts"},
+                "clocks": clocks}
+    print(json.dumps(out_json), flush=True)
+    ctx.close()
+
+
 def run_variants(args):
     import numpy as np
     import torch
@@ -735,6 +831,8 @@ if __name__ == "__main__":
         run_reference(a)
     elif a.workload == "batch":
         run_batch(a)
+    elif a.workload == "postprocess":
+        run_postprocess(a)
     elif a.workload == "adjoint":
         run_adjoint(a)
     elif a.workload == "variants":
