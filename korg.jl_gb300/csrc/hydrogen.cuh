@@ -387,8 +387,9 @@ __global__ void __launch_bounds__(512, (MIXED && KMAX <= 16) ? 2 : 1) hline_tile
             const HRec& r = a.rec[int64_t(t) * L + l];
             if (r.kind == HK_OFF || jg < r.lb || jg > r.ub) continue;
             if (r.kind == HK_BRACKETT) {
-                // linear_interpolation over the 201-point range grid (:249, :160)
-                const double u = MIXED ? (wl - r.wl0) * r.a : (wl - r.wl0) / r.inv_s;
+                // linear_interpolation over the 201-point range grid (:249, :160); the position on
+                // the grid by the reciprocal step (one rounding more than a division, no FP64 divide)
+                const double u = (wl - r.wl0) * r.a;
                 int i = int(floor(u));
                 i = i < 0 ? 0 : (i > BR_NP - 2 ? BR_NP - 2 : i);
                 const double d = u - i;
