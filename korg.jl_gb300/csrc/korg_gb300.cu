@@ -1811,8 +1811,7 @@ KORG_API int korg_apply_rotation_dev(korg_ctx* ctx, const double* wls, int64_t n
         KCUDA(cudaMemcpyAsync(out, flux, sizeof(double) * size_t(nwl) * nspec, cudaMemcpyDeviceToDevice, s));
         return KORG_OK;
     }
-    rotation_kernel<false><<<dim3(unsigned((nwl + 127) / 128), unsigned((nspec + ROT_SPEC - 1) / ROT_SPEC)), 128, 0,
-                             s>>>(a, flux, nspec, out);
+    rotation_fwd_kernel<<<unsigned((nwl + ROT_TP - 1) / ROT_TP), ROT_TP, 0, s>>>(a, flux, nspec, out);
     KCUDA(cudaGetLastError());
     return KORG_OK;
 }

@@ -7,7 +7,9 @@
 //                      Gaussian weights by lanes, their sum by shuffles; a block of up to
 //                      LSF_SPEC spectra per warp shares the weights.
 //   rotation kernels:  one thread per output wavelength: a walk over the window carrying the
-//                      previous kernel integral, for a block of up to ROT_SPEC spectra.
+//                      previous kernel integral; the forward keeps each chunk's weights in
+//                      shared memory and applies them to every spectrum, the reverse mode
+//                      scatters them for a block of up to ROT_SPEC spectra.
 //
 // Everything is FP64, as in the reference (post-processing of the FP64 flux).
 #pragma once
@@ -201,6 +203,49 @@ __global__ void __launch_bounds__(128) rotation_kernel(RotArgs a, const double* 
 #pragma unroll
         for (int k = 0; k < ROT_SPEC; k++)
             if (k < ns) out[int64_t(s0 + k) * a.nwl + i] = hi[k] - lo[k];
+    }
+}
+
+// Forward rotation, all spectra at once: each thread owns one output wavelength and walks its
+// window in chunks of ROT_CH points, keeping the chunk's weights K_{k+1} - K_k (one asin/sqrt
+// pair per window point, whatever the number of spectra) in its own column of shared memory,
+// then applies them to every spectrum, accumulating across chunks in the output.
+constexpr int ROT_TP = 64;  // threads (output wavelengths) per block
+constexpr int ROT_CH = 64;  // window points per chunk
+__global__ void __launch_bounds__(ROT_TP) rotation_fwd_kernel(RotArgs a, const double* in, int32_t nspec,
+                                                              double* out) {
+    __shared__ double s_w[ROT_CH][ROT_TP];  // column t: this thread's weights
+    const int t = threadIdx.x;
+    const int64_t i = int64_t(blockIdx.x) * ROT_TP + t;
+    if (i >= a.nwl) return;  // no block-wide synchronisation below
+    const RotRange& rg = rot_range(a, i);
+    const double* w = a.wls + rg.first;
+    const int64_t ii = i - rg.first;
+    const double dl = a.wls[i] * a.v_over_c;
+    const int64_t lb = search_first(w, rg.n, a.wls[i] - dl), ub = search_last(w, rg.n, a.wls[i] + dl);
+    const int64_t nwin = ub - lb + 1;
+    const double c3dl = a.c3 * dl;
+    double Kp = rot_kernel_integral(a, c3dl, -dl, dl);
+    for (int64_t c0 = 0; c0 < nwin; c0 += ROT_CH) {
+        const int nq = int(min(int64_t(ROT_CH), nwin - c0));
+        for (int q = 0; q < nq; q++) {
+            const int64_t m = lb + c0 + q;
+            const double d = m < ub ? (double(m - ii) + 0.5) * rg.step : dl;
+            const double Kn = rot_kernel_integral(a, c3dl, d, dl);
+            s_w[q][t] = Kn - Kp;
+            Kp = Kn;
+        }
+        const double* f0 = in + rg.first + lb + c0;
+        for (int s = 0; s < nspec; s++) {
+            const double* f = f0 + int64_t(s) * a.nwl;
+            double acc = 0.0;
+            for (int q = 0; q < nq; q++) acc += s_w[q][t] * f[q];
+            double* o = out + int64_t(s) * a.nwl + i;
+            *o = c0 == 0 ? acc : *o + acc;
+        }
+    }
+    if (nwin <= 0) {  // empty window (cannot happen for a grid point, which is inside its own window)
+        for (int s = 0; s < nspec; s++) out[int64_t(s) * a.nwl + i] = 0.0;
     }
 }
 
