@@ -1752,8 +1752,7 @@ KORG_API int korg_apply_lsf_dev(korg_ctx* ctx, const double* wls, int64_t nwl, c
     KCHECK(lsf_args(ctx, wls, nwl, out_wls, nout, R, nR, window_size, &a));
     if (!flux || !out || nspec < 1) return set_err(ctx, KORG_EINVAL, "bad LSF arguments");
     KCUDA(cudaSetDevice(ctx->device));
-    lsf_apply_kernel<<<dim3(warp_blocks(nout), unsigned((nspec + LSF_SPEC - 1) / LSF_SPEC)), 256, 0,
-                       static_cast<cudaStream_t>(stream)>>>(a, flux, nspec, out);
+    lsf_apply_kernel<<<warp_blocks(nout), 256, 0, static_cast<cudaStream_t>(stream)>>>(a, flux, nspec, out);
     KCUDA(cudaGetLastError());
     return KORG_OK;
 }

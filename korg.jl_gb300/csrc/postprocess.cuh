@@ -4,8 +4,9 @@
 // linear in the flux, so the reverse mode is the transposed map).
 //
 //   lsf kernels:       one warp per output wavelength: the window by two binary searches, the
-//                      Gaussian weights by lanes, their sum by shuffles; a block of up to
-//                      LSF_SPEC spectra per warp shares the weights.
+//                      Gaussian weights by lanes, their sum by shuffles; the forward applies
+//                      each chunk of weights to every spectrum, the reverse mode scatters them
+//                      for a block of up to LSF_SPEC spectra.
 //   rotation kernels:  one thread per output wavelength: a walk over the window carrying the
 //                      previous kernel integral; the forward keeps each chunk's weights in
 //                      shared memory and applies them to every spectrum, the reverse mode
@@ -57,32 +58,45 @@ __device__ __forceinline__ double lsf_norm(const LsfArgs& a, int64_t lb, int64_t
     return s;
 }
 
-// out[s][i] = sum_j flux[s][j] phi_j / sum phi  (apply_LSF :94-106, compute_LSF_matrix * flux)
+// out[s][i] = sum_j flux[s][j] phi_j / sum phi  (apply_LSF :94-106, compute_LSF_matrix * flux).
+// The window is taken in chunks of 32 LSF_CW points; each lane keeps its LSF_CW normalised
+// weights of the chunk in registers and applies them to every spectrum, so the Gaussian is
+// evaluated twice per window point (sum, then weights) whatever the number of spectra.
+constexpr int LSF_CW = 8;
 __global__ void __launch_bounds__(256) lsf_apply_kernel(LsfArgs a, const double* flux, int32_t nspec, double* out) {
     const int lane = threadIdx.x & 31;
     const int64_t i = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    const int s0 = blockIdx.y * LSF_SPEC;
     if (i >= a.nout) return;  // uniform across the warp
     int64_t lb, ub;
     double wl0, sigma;
     lsf_window(a, i, lb, ub, wl0, sigma);
     const double norm = lsf_norm(a, lb, ub, wl0, sigma, lane);
-    const int ns = min(LSF_SPEC, nspec - s0);
-    double acc[LSF_SPEC];
-#pragma unroll
-    for (int k = 0; k < LSF_SPEC; k++) acc[k] = 0.0;
-    for (int64_t j = lb + lane; j <= ub; j += 32) {
-        const double w = lsf_phi(a.wls[j] - wl0, sigma) / norm;
-#pragma unroll
-        for (int k = 0; k < LSF_SPEC; k++)
-            if (k < ns) acc[k] += flux[int64_t(s0 + k) * a.nwl + j] * w;
+    if (ub < lb) {  // empty window: an empty sum
+        for (int s = lane; s < nspec; s += 32) out[int64_t(s) * a.nout + i] = 0.0;
+        return;
     }
+    for (int64_t c0 = lb; c0 <= ub; c0 += 32 * LSF_CW) {
+        double w[LSF_CW];
 #pragma unroll
-    for (int k = 0; k < LSF_SPEC; k++) {
-        double v = acc[k];
+        for (int k = 0; k < LSF_CW; k++) {
+            const int64_t j = c0 + lane + 32 * k;
+            w[k] = j <= ub ? lsf_phi(a.wls[j] - wl0, sigma) / norm : 0.0;
+        }
+        for (int s = 0; s < nspec; s++) {
+            const double* f = flux + int64_t(s) * a.nwl;
+            double v = 0.0;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0 && k < ns) out[int64_t(s0 + k) * a.nout + i] = v;
+            for (int k = 0; k < LSF_CW; k++) {
+                const int64_t j = c0 + lane + 32 * k;
+                if (j <= ub) v += f[j] * w[k];
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) {
+                double* dst = out + int64_t(s) * a.nout + i;
+                *dst = c0 == lb ? v : *dst + v;
+            }
+        }
     }
 }
 
