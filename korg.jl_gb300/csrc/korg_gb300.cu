@@ -187,7 +187,7 @@ LayersDev layers_dev(const korg_layers* y) {
 }
 
 // ------------------------------------------------------------------ line opacity
-constexpr int TILE_TW = 64;  // default wavelengths per CTA of the line tile kernel
+constexpr int TILE_TW = 128;  // default wavelengths per CTA of the line tile kernel
 
 // Pieces of the per-spectrum scratch of the line prologue and candidate lists.
 struct LineScratch {
