@@ -1828,8 +1828,8 @@ KORG_API int korg_apply_rotation_vjp_dev(korg_ctx* ctx, const double* wls, int64
         const int64_t n = nwl * nspec;
         add_kernel<<<unsigned((n + 255) / 256), 256, 0, s>>>(dflux, dout, n);
     } else {
-        rotation_kernel<true><<<dim3(unsigned((nwl + 127) / 128), unsigned((nspec + ROT_SPEC - 1) / ROT_SPEC)), 128,
-                                0, s>>>(a, dout, nspec, dflux);
+        rotation_vjp_kernel<<<dim3(unsigned((nwl + 127) / 128), unsigned((nspec + ROT_SPEC - 1) / ROT_SPEC)), 128, 0,
+                              s>>>(a, dout, nspec, dflux);
     }
     KCUDA(cudaGetLastError());
     return KORG_OK;

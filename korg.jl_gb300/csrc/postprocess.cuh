@@ -173,12 +173,12 @@ __device__ __forceinline__ const RotRange& rot_range(const RotArgs& a, int64_t i
     return a.r[k];
 }
 
-// Output i of its range, for spectra s0 .. s0 + ns - 1 (_apply_rotation_core, :204-228):
-// detunings [-dl, (lb - i + 1/2 .. ub - i - 1/2) step, dl], kernel integrals K_0 .. K_m+1,
-// new F_i = sum K_{k+1} F_{lb+k} - sum K_k F_{lb+k}.  The reverse mode scatters
-// dout_i (K_{k+1} - K_k) to F_{lb+k}.
-template <bool VJP>
-__global__ void __launch_bounds__(128) rotation_kernel(RotArgs a, const double* in, int32_t nspec, double* out) {
+// Reverse mode of the rotation of output i (_apply_rotation_core, :204-228: detunings
+// [-dl, (lb - i + 1/2 .. ub - i - 1/2) step, dl], kernel integrals K_0 .. K_m+1, new
+// F_i = sum K_{k+1} F_{lb+k} - sum K_k F_{lb+k}): dout_i (K_{k+1} - K_k) is scattered to
+// dF_{lb+k}, for spectra s0 .. s0 + ns - 1.
+__global__ void __launch_bounds__(128) rotation_vjp_kernel(RotArgs a, const double* dout, int32_t nspec,
+                                                           double* dflux) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const int s0 = blockIdx.y * ROT_SPEC;
     if (i >= a.nwl) return;
@@ -189,34 +189,18 @@ __global__ void __launch_bounds__(128) rotation_kernel(RotArgs a, const double* 
     const double dl = a.wls[i] * a.v_over_c;
     const int64_t lb = search_first(w, rg.n, a.wls[i] - dl), ub = search_last(w, rg.n, a.wls[i] + dl);
     const double c3dl = a.c3 * dl;
-    double hi[ROT_SPEC], lo[ROT_SPEC], g[ROT_SPEC];
+    double g[ROT_SPEC];
 #pragma unroll
-    for (int k = 0; k < ROT_SPEC; k++) {
-        hi[k] = lo[k] = 0.0;
-        g[k] = (VJP && k < ns) ? in[int64_t(s0 + k) * a.nwl + i] : 0.0;
-    }
+    for (int k = 0; k < ROT_SPEC; k++) g[k] = k < ns ? dout[int64_t(s0 + k) * a.nwl + i] : 0.0;
     double Kp = rot_kernel_integral(a, c3dl, -dl, dl);
     for (int64_t m = lb; m <= ub; m++) {
         const double d = m < ub ? (double(m - ii) + 0.5) * rg.step : dl;
         const double Kn = rot_kernel_integral(a, c3dl, d, dl);
         const int64_t j = rg.first + m;
 #pragma unroll
-        for (int k = 0; k < ROT_SPEC; k++) {
-            if (k >= ns) continue;
-            if (VJP) {
-                atomicAdd(out + int64_t(s0 + k) * a.nwl + j, g[k] * (Kn - Kp));
-            } else {
-                const double f = in[int64_t(s0 + k) * a.nwl + j];
-                hi[k] += Kn * f;
-                lo[k] += Kp * f;
-            }
-        }
-        Kp = Kn;
-    }
-    if (!VJP) {
-#pragma unroll
         for (int k = 0; k < ROT_SPEC; k++)
-            if (k < ns) out[int64_t(s0 + k) * a.nwl + i] = hi[k] - lo[k];
+            if (k < ns) atomicAdd(dflux + int64_t(s0 + k) * a.nwl + j, g[k] * (Kn - Kp));
+        Kp = Kn;
     }
 }
 
