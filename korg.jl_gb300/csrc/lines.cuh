@@ -550,7 +550,6 @@ __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src)
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 // Far-Lorentz branch of voigt_hjerting (line_absorption.jl:305-308) with r^2 = x^2/gamma^2.
 __device__ __forceinline__ float far_lorentz32(float4 p, float x2) {
