@@ -48,10 +48,10 @@ sys.path.insert(0, os.path.join(ROOT, "korg.jl_gb300"))
 
 METRIC = "spectra/s & line-layer-lambda evals/s, mixed vs plain FP64 at 1e-4 flux err"
 FLOP_PER_EVAL = 24  # FP32 flop per Voigt evaluation (Harris branch, FMA = 2)
-# bounded sample of the workload for the CPU baseline: 20 windows of 70 A spread evenly over
-# 3000-10000 A (20% of the grid)
-CPU_SAMPLE = [(3140.0 + 350.0 * k, 3210.0 + 350.0 * k) for k in range(20)]
-
+# bounded sample of the workload for the CPU baseline and the oracle comparison: the same range
+# on a 0.05 A grid, whose wavelengths are exactly every 5th point of the 0.01 A grid (20% of the
+# points, spread over the whole range, so line density and hydrogen windows are sampled evenly)
+CPU_SAMPLE_STEP = 0.05
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -63,7 +63,10 @@ def parse():
     ap.add_argument("--wl", type=float, nargs=2, default=[3000.0, 10000.0],
                     help="wavelength range in A (the full workload is 3000-10000)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
-    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample (and the oracle comparisons)")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the oracle comparison of the adjoint, batch and cool-star configurations")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the reverse-mode measurement")
     ap.add_argument("--workload", default="synth", choices=["synth", "batch", "adjoint", "variants", "postprocess"])
     ap.add_argument("--tile", default=None, help="force the line tile shape: tw,stage,split (e.g. 64,32,1)")
     ap.add_argument("--spectra", type=int, default=256, help="batch workload: number of spectra")
@@ -76,32 +79,57 @@ def workload(n_lines, wl=(3000, 10000)):
     return synthetic.config1(n_lines=n_lines, wl=tuple(wl))
 
 
-def cpu_sample(n_lines, threads, _cache={}):
-    """Time the oracle on the CPU sample; returns (spectra/s extrapolated, seconds, evals, info).
+def strided(inp, step_A):
+    """Copy of prepared inputs on the same range(s) with a coarser step; its wavelengths are a
+    subset of the original grid's (checked), every stride-th point."""
+    import copy
+    import numpy as np
+    from korg_gb300.wavelengths import Wavelengths
+    s = copy.copy(inp)
+    a, b = inp.wls.eachwindow()[0]
+    s.wls = Wavelengths((round(a * 1e8, 6), round(b * 1e8, 6), step_A))
+    stride = (len(inp.wls) - 1) // (len(s.wls) - 1)
+    assert len(inp.wls.ranges) == 1 and np.array_equal(s.wls.all_wls, inp.wls.all_wls[::stride])
+    return s, stride
 
-    The sample is the full workload (all lines, the same continuum and atmosphere) evaluated on
-    20% of the grid points: 20 windows of 70 A spread evenly over 3000-10000 A."""
+
+def oracle_flux(inp, threads):
+    """The FP64 oracle's synthesis of prepared inputs: (flux, cntm, evals, seconds)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
-    from korg_gb300 import synthetic
     from korg_gb300.data import stark_profiles
-    from korg_gb300.wavelengths import Wavelengths
     oracle.build()
+    t0 = time.perf_counter()
+    flux, cntm, _, _, ev = oracle.synthesize(inp, inp.linelist, inp.linelist5, stark_profiles(), inp.wls.all_wls,
+                                             nthreads=threads)
+    return flux, cntm, ev, time.perf_counter() - t0
+
+
+def cpu_sample(n_lines, threads, _cache={}):
+    """Time the oracle on the CPU sample; returns (spectra/s, seconds, evals, info, flux, cntm).
+
+    The sample is the full workload (all lines, the same continuum and atmosphere) on the same
+    3000-10000 A range at 0.05 A: every 5th point of the 0.01 A grid, 20% of the points."""
+    from korg_gb300 import synthetic
     key = n_lines
     if key not in _cache:
         inp = synthetic.prepare(workload(n_lines))
-        full_points = len(inp.wls)
-        inp.wls = Wavelengths(CPU_SAMPLE)
-        _cache[key] = (inp, full_points)
+        _cache[key] = (strided(inp, CPU_SAMPLE_STEP)[0], len(inp.wls))
     inp, full_points = _cache[key]
     frac = len(inp.wls) / full_points
-    t0 = time.perf_counter()
-    _, _, _, _, ev = oracle.synthesize(inp, inp.linelist, inp.linelist5, stark_profiles(), inp.wls.all_wls,
-                                       nthreads=threads)
-    dt = time.perf_counter() - t0
-    return frac / dt, dt, ev, (f"the full workload ({len(inp.linelist)} lines, H lines) evaluated on 20 windows "
-                               f"of 70 A spread over 3000-10000 A ({len(inp.wls)} of {full_points} points, "
-                               f"fraction {frac:.4f}); spectra/s = fraction / seconds")
+    flux, cntm, ev, dt = oracle_flux(inp, threads)
+    return frac / dt, dt, ev, (f"the full workload ({len(inp.linelist)} lines, H lines) on the same range at "
+                               f"{CPU_SAMPLE_STEP} A, i.e. every 5th point of the grid ({len(inp.wls)} of "
+                               f"{full_points} points, fraction {frac:.4f}); spectra/s = fraction / seconds"), flux, cntm
+
+
+def flux_errors(flux, cntm, ref_flux, ref_cntm):
+    """max relative flux error and rectified-flux RMS / max error of (flux, cntm) against a reference."""
+    import numpy as np
+    r, rr = flux / cntm, ref_flux / ref_cntm
+    return {"max_rel_flux_err": float(np.max(np.abs(flux / ref_flux - 1))),
+            "rectified_rms": float(np.sqrt(np.mean((r - rr) ** 2))),
+            "max_rectified_err": float(np.max(np.abs(r - rr)))}
 
 
 class Clocks:
@@ -177,7 +205,7 @@ def run_reference(args):
     secs, vals = [], []
     info, ev = "", 0
     for _ in range(args.steps):
-        v, dt, ev, info = cpu_sample(args.lines, threads)
+        v, dt, ev, info, _, _ = cpu_sample(args.lines, threads)
         secs.append(dt)
         vals.append(v)
     dt = statistics.mean(secs)
@@ -233,7 +261,7 @@ def run_korg(args):
     import torch
     import build as korg_build
     from korg_gb300 import _lib
-    from korg_gb300.synthesize import synthesize_prepared
+    from korg_gb300.api import synthesize_prepared
     from korg_gb300 import synthetic
 
     rank = int(os.environ.get("RANK", "0"))
@@ -301,7 +329,7 @@ def run_korg(args):
              "line_tile": stats.ms_line_tile, "rt_both_passes": stats.ms_rt}
 
     # plain FP64 form of the same synthesis
-    fp64 = None
+    fp64, f64, c64 = None, None, None
     if not args.no_fp64:
         step(_lib.KORG_FP64)
         torch.cuda.synchronize()
@@ -315,8 +343,8 @@ def run_korg(args):
             e1.synchronize()
             t64.append(e0.elapsed_time(e1))
         st64 = ctx.stats()
-        f64 = flux.cpu().numpy()
-        c64 = cntm.cpu().numpy()
+        f64 = flux.cpu().numpy().copy()
+        c64 = cntm.cpu().numpy().copy()
         err = float(np.max(np.abs(flux32 / f64 - 1)))
         rms = float(np.sqrt(np.mean((flux32 / cntm32 - f64 / c64) ** 2)))
         fp64 = {"spectra_per_s": 1000.0 / statistics.mean(t64), "ms_per_step": statistics.mean(t64),
@@ -348,12 +376,25 @@ def run_korg(args):
     rt_flop = 2 * L * nwl * 35
     rt_achieved = rt_flop / (stats.ms_rt * 1e-3) / 1e12
 
-    cpu = None
+    cpu, parity = None, {}
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        v, dt, ev_cpu, info = cpu_sample(args.lines, threads)
+        v, dt, ev_cpu, info, oflux, ocntm = cpu_sample(args.lines, threads)
         cpu = {"value": v, "unit": "spectra/s", "cores": threads, "kind": "port", "sample": info,
                "evals_per_s": ev_cpu / dt, "seconds": dt}
+        # the headline's flux against the FP64 oracle at the sample's points (every 5th point)
+        m = flux_errors(flux32[::5], cntm32[::5], oflux, ocntm)
+        h = {"points": len(oflux), "mixed_max_rel_flux_err_vs_oracle": m["max_rel_flux_err"],
+             "mixed_rectified_rms_vs_oracle": m["rectified_rms"],
+             "mixed_max_rectified_err_vs_oracle": m["max_rectified_err"]}
+        if f64 is not None:
+            h["fp64_max_rel_flux_err_vs_oracle"] = flux_errors(f64[::5], c64[::5], oflux, ocntm)["max_rel_flux_err"]
+            h["fp64_cntm_max_rel_err_vs_oracle"] = float(np.max(np.abs(c64[::5] / ocntm - 1)))
+        parity["cfg1_full_optical"] = h
+        _progress("headline CPU sample and oracle comparison done")
+        if not args.no_configs:
+            parity.update(configs_vs_oracle(ctx, threads))
+    adj = adjoint_measure(ctx, torch, dev, steps=5) if rank == 0 and not args.no_adjoint else None
 
     # alpha init, reference-wavelength lines (5), hydrogen (3), metal lines (5), transfer
     launches_per_step = 1 + 5 + (3 if inp.hydrogen_lines else 0) + 5 + 1
@@ -381,6 +422,7 @@ def run_korg(args):
         "evals_per_s": world * evals / (ms * 1e-3),
         "stages_ms": stage,
         "fp64": fp64,
+        **{k: v for k, v in parity.get("cfg1_full_optical", {}).items() if k.endswith("_vs_oracle")},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
                      "frac": achieved / peak.value, "traffic": traffic_from_profiles(),
                      "kernel": "line_tile_kernel<mixed> (metal lines)",
@@ -391,6 +433,8 @@ def run_korg(args):
                                  "frac": rt_achieved / peak64.value,
                                  "algorithmic": "35 FP64 flop x 2 passes x L x nwl"}},
         "cpu_baseline": cpu,
+        "parity_vs_oracle": parity,
+        "adjoint": adj,
         "e2e": {"value": world / e2e_s, "unit": "spectra/s", "h2d_bytes_per_step": host_bytes(inp),
                 "d2h_bytes_per_step": 16 * nwl},
         "gpu_launches": launches_per_step * args.steps,
@@ -717,86 +761,163 @@ def run_variants(args):
     print(json.dumps(out), flush=True)
 
 
-def run_adjoint(args):
-    import numpy as np
-    import torch
-    import build as korg_build
-    from korg_gb300 import _lib, synthetic
-    from korg_gb300.synthesize import synthesize_prepared
-    korg_build.build()
-    dev = torch.device("cuda", 0)
-    torch.cuda.set_device(dev)
-    _progress("preparing the adjoint configuration")
-    inp = synthetic.prepare(synthetic.config2(n_atomic=int(50_000 * args.adj_scale),
-                                              n_mol=int(20_000 * args.adj_scale)))
-    nwl, L = len(inp.wls), len(inp.T)
-    ctx = _lib.Context(0)
-    ctx.ensure_stark()
-    # observation: the same star with log gf perturbed by N(0, 0.1) dex
-    import copy
-    o = copy.copy(inp)
-    o.linelist = copy.copy(inp.linelist)
-    o.linelist.log_gf = inp.linelist.log_gf + np.random.default_rng(1).normal(0, 0.1, len(inp.linelist))
-    r = synthesize_prepared(o, precision="fp64", ctx=ctx)
-    obs = torch.as_tensor(r.flux / r.cntm, device=dev)
-    s, l1, l5, w, keep = dev_inputs(inp, torch, dev)
-    flux = torch.empty(nwl, dtype=torch.float64, device=dev)
-    cntm = torch.empty_like(flux)
-    shapes = {"T": L, "ne": L, "n_eff_vdW": L, "xi": L, "n_div_U": inp.n_div_U.size, "nH_I": L, "nHe_I": L,
-              "UH_I": L, "log_gf": len(inp.linelist), "cntm_vals": inp.cntm_vals.size, "alpha_ref_cntm": L}
-    gt = {k: torch.empty(n, dtype=torch.float64, device=dev) for k, n in shapes.items()}
-    grads = _lib.SynthGrads(*[C.cast(gt[k].data_ptr(), _lib._dp) for k in shapes])
-    stream = torch.cuda.current_stream(dev)
-    _progress("inputs resident")
+class AdjointCase:
+    """The adjoint configuration (72 layers, Teff 4500 K, logg 2.5, [M/H] -0.5, 50k atomic + 20k
+    CO/OH/CN lines, 15000-17000 A at 0.005 A) resident on the device: forward synthesis, and
+    forward + rectified-flux loss + korg_synthesize_vjp_dev against a seeded observation (the
+    same star with log gf perturbed by N(0, 0.1) dex)."""
 
-    def forward(prec):
-        ctx.check(ctx.lib.korg_synthesize_dev(ctx.h, C.byref(s), C.byref(l1), C.byref(l5), w.data_ptr(), nwl, prec,
-                                              flux.data_ptr(), cntm.data_ptr(), None, stream.cuda_stream))
+    def __init__(self, ctx, torch, dev, scale=1.0):
+        import copy
+        import numpy as np
+        from korg_gb300 import _lib, synthetic
+        from korg_gb300.api import synthesize_prepared
+        self.torch, self.ctx, self.lib = torch, ctx, _lib
+        inp = synthetic.prepare(synthetic.config2(n_atomic=int(50_000 * scale), n_mol=int(20_000 * scale)))
+        self.inp = inp
+        self.nwl, L = len(inp.wls), len(inp.T)
+        ctx.ensure_stark()
+        o = copy.copy(inp)
+        o.linelist = copy.copy(inp.linelist)
+        o.linelist.log_gf = inp.linelist.log_gf + np.random.default_rng(1).normal(0, 0.1, len(inp.linelist))
+        r = synthesize_prepared(o, precision="fp64", ctx=ctx)
+        self.obs = torch.as_tensor(r.flux / r.cntm, device=dev)
+        self.s, self.l1, self.l5, self.w, self.keep = dev_inputs(inp, torch, dev)
+        self.flux = torch.empty(self.nwl, dtype=torch.float64, device=dev)
+        self.cntm = torch.empty_like(self.flux)
+        shapes = {"T": L, "ne": L, "n_eff_vdW": L, "xi": L, "n_div_U": inp.n_div_U.size, "nH_I": L, "nHe_I": L,
+                  "UH_I": L, "log_gf": len(inp.linelist), "cntm_vals": inp.cntm_vals.size, "alpha_ref_cntm": L}
+        self.gt = {k: torch.empty(n, dtype=torch.float64, device=dev) for k, n in shapes.items()}
+        self.grads = _lib.SynthGrads(*[C.cast(self.gt[k].data_ptr(), _lib._dp) for k in shapes])
+        self.stream = torch.cuda.current_stream(dev)
 
-    def step(prec, flags=_lib.KORG_VJP_HYDROGEN):  # loss and its gradient w.r.t. every hot-path input
-        forward(prec)
-        rr = flux / cntm - obs
+    def forward(self, prec):
+        c = self.ctx
+        c.check(c.lib.korg_synthesize_dev(c.h, C.byref(self.s), C.byref(self.l1), C.byref(self.l5), self.w.data_ptr(),
+                                          self.nwl, prec, self.flux.data_ptr(), self.cntm.data_ptr(), None,
+                                          self.stream.cuda_stream))
+
+    def step(self, prec, flags=None):
+        """loss and its gradient w.r.t. every hot-path input"""
+        flags = self.lib.KORG_VJP_HYDROGEN if flags is None else flags
+        self.forward(prec)
+        flux, cntm, c = self.flux, self.cntm, self.ctx
+        rr = flux / cntm - self.obs
         dF = 2 * rr / cntm
         dC = -2 * rr * flux / cntm ** 2
-        ctx.check(ctx.lib.korg_synthesize_vjp_dev(ctx.h, C.byref(s), C.byref(l1), C.byref(l5), w.data_ptr(), nwl,
-                                                  prec, dF.data_ptr(), dC.data_ptr(), C.byref(grads), flags,
-                                                  stream.cuda_stream))
-        return torch.sum(rr * rr)
+        c.check(c.lib.korg_synthesize_vjp_dev(c.h, C.byref(self.s), C.byref(self.l1), C.byref(self.l5),
+                                              self.w.data_ptr(), self.nwl, prec, dF.data_ptr(), dC.data_ptr(),
+                                              C.byref(self.grads), flags, self.stream.cuda_stream))
+        return self.torch.sum(rr * rr)
 
-    def timed(fn, reps):
+    def timed(self, fn, reps):
         fn()
-        torch.cuda.synchronize()
+        self.torch.cuda.synchronize()
         ts = []
         for _ in range(reps):
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
+            e0, e1 = self.torch.cuda.Event(enable_timing=True), self.torch.cuda.Event(enable_timing=True)
+            e0.record(self.stream)
             fn()
-            e1.record(stream)
+            e1.record(self.stream)
             e1.synchronize()
             ts.append(e0.elapsed_time(e1))
         return statistics.mean(ts)
 
+    def grads_host(self):
+        return {k: v.cpu().numpy().copy() for k, v in self.gt.items()}
+
+    def vjp_stages(self, prec):
+        c = self.ctx
+        c.check(c.lib.korg_set_timing(c.h, 1))
+        self.step(prec)
+        self.torch.cuda.synchronize()
+        st = c.stats()
+        c.check(c.lib.korg_set_timing(c.h, 0))
+        return {"alpha_recompute": st.ms_vjp_alpha, "rt_adjoint": st.ms_vjp_rt, "hydrogen": st.ms_vjp_hydrogen,
+                "lines": st.ms_vjp_lines}
+
+
+def adjoint_measure(ctx, torch, dev, steps=5):
+    """Cost of the gradient on the adjoint configuration (mixed precision), for the default line:
+    forward alone, forward + loss + gradient, and the same reusing the forward's opacity."""
+    a = AdjointCase(ctx, torch, dev)
+    mixed = a.lib.KORG_MIXED
+    t_fwd = a.timed(lambda: a.forward(mixed), steps)
+    t_step = a.timed(lambda: a.step(mixed), steps)
+    reuse = a.lib.KORG_VJP_HYDROGEN | a.lib.KORG_VJP_REUSE_FORWARD
+    t_reuse = a.timed(lambda: a.step(mixed, reuse), steps)
+    stages = a.vjp_stages(mixed)
+    _progress(f"adjoint: forward {t_fwd:.1f} ms, forward + gradient {t_step:.1f} ms")
+    return {"workload": f"72 layers, Teff 4500 logg 2.5 [M/H] -0.5, {len(a.inp.linelist)} lines (50k atomic + 20k "
+                        f"CO/OH/CN), 15000-17000 A @ 0.005 A ({a.nwl} points), mixed precision; loss = sum of squared "
+                        "rectified-flux residuals; gradient w.r.t. T, ne, n_eff_vdW, xi, n/U, log gf, continuum "
+                        "knots, alpha_ref continuum, H-line inputs",
+            "steps": steps, "forward_ms": t_fwd, "forward_and_gradient_ms": t_step,
+            "gradient_over_forward": (t_step - t_fwd) / t_fwd, "vjp_stages_ms": stages,
+            "reuse_forward": {"step_ms": t_reuse, "gradient_over_forward": (t_reuse - t_fwd) / t_fwd}}
+
+
+def configs_vs_oracle(ctx, threads):
+    """The plain FP64 and mixed GPU syntheses of the other configurations over their whole grids,
+    compared with the FP64 oracle on a strided subset of the same grid (every 20th point of the
+    0.005 A infrared grids, every 50th of the 0.01 A optical one)."""
+    from korg_gb300 import synthetic
+    from korg_gb300.api import synthesize_prepared
+    cases = [("cfg2_adjoint_forward", lambda: synthetic.prepare(synthetic.config2()), 0.1),
+             ("cfg3_batch_spectrum0", lambda: synthetic.prepare(synthetic.config3(n_spectra=1)[0]), 0.1),
+             ("cfg4_cool_star_variant0",
+              lambda: synthetic.abundance_variants(synthetic.prepare(synthetic.config4()), 1)[0], 0.5)]
+    out = {}
+    ctx.ensure_stark()
+    for name, make, step in cases:
+        inp = make()
+        res = {}
+        ctx.check(ctx.lib.korg_set_timing(ctx.h, 1))
+        for prec in ("fp64", "mixed"):
+            r = synthesize_prepared(inp, precision=prec, ctx=ctx)
+            res[prec] = (r.flux, r.cntm, ctx.stats().ms_total)
+        ctx.check(ctx.lib.korg_set_timing(ctx.h, 0))
+        sub, stride = strided(inp, step)
+        of, oc, ev, dt = oracle_flux(sub, threads)
+        e64 = flux_errors(res["fp64"][0][::stride], res["fp64"][1][::stride], of, oc)
+        e32 = flux_errors(res["mixed"][0][::stride], res["mixed"][1][::stride], of, oc)
+        out[name] = {"lines": len(inp.linelist), "layers": len(inp.T), "points": len(inp.wls),
+                     "compared_points": len(of), "fp64_max_rel_flux_err_vs_oracle": e64["max_rel_flux_err"],
+                     "mixed_max_rel_flux_err_vs_oracle": e32["max_rel_flux_err"],
+                     "mixed_rectified_rms_vs_oracle": e32["rectified_rms"],
+                     "mixed_max_rectified_err_vs_oracle": e32["max_rectified_err"],
+                     "gpu_fp64_ms": res["fp64"][2], "gpu_mixed_ms": res["mixed"][2], "oracle_s": dt}
+        _progress(f"{name}: fp64 vs oracle {e64['max_rel_flux_err']:.2e}, mixed {e32['max_rel_flux_err']:.2e}")
+    return out
+
+
+def run_adjoint(args):
+    import numpy as np
+    import torch
+    import build as korg_build
+    from korg_gb300 import _lib
+    korg_build.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    _progress("preparing the adjoint configuration")
+    ctx = _lib.Context(0)
+    a = AdjointCase(ctx, torch, dev, args.adj_scale)
+    inp, nwl = a.inp, a.nwl
+    _progress("inputs resident")
     res = {}
     for name, prec in (("mixed", _lib.KORG_MIXED), ("fp64", _lib.KORG_FP64)):
         reps = args.steps if name == "mixed" else 1
-        t_fwd = timed(lambda: forward(prec), reps)
+        t_fwd = a.timed(lambda: a.forward(prec), reps)
         clk = Clocks(0) if name == "mixed" else None
-        t_step = timed(lambda: step(prec), reps)
+        t_step = a.timed(lambda: a.step(prec), reps)
         clocks = clk.stop() if clk else None
-        g = {k: v.cpu().numpy().copy() for k, v in gt.items()}
-        res[name] = (t_fwd, t_step, g, clocks)
+        res[name] = (t_fwd, t_step, a.grads_host(), clocks)
         _progress(f"{name}: forward {t_fwd:.1f} ms, forward + gradient {t_step:.1f} ms")
     # stage times of one mixed step, and the step with the forward's opacity reused
     reuse = _lib.KORG_VJP_HYDROGEN | _lib.KORG_VJP_REUSE_FORWARD
-    t_reuse = timed(lambda: step(_lib.KORG_MIXED, reuse), args.steps)
-    g_reuse = {k: v.cpu().numpy().copy() for k, v in gt.items()}
-    ctx.check(ctx.lib.korg_set_timing(ctx.h, 1))
-    step(_lib.KORG_MIXED)
-    torch.cuda.synchronize()
-    st = ctx.stats()
-    ctx.check(ctx.lib.korg_set_timing(ctx.h, 0))
-    vjp_stages = {"alpha_recompute": st.ms_vjp_alpha, "rt_adjoint": st.ms_vjp_rt, "hydrogen": st.ms_vjp_hydrogen,
-                  "lines": st.ms_vjp_lines}
+    t_reuse = a.timed(lambda: a.step(_lib.KORG_MIXED, reuse), args.steps)
+    g_reuse = a.grads_host()
+    vjp_stages = a.vjp_stages(_lib.KORG_MIXED)
     stats = ctx.stats()
     g32, g64 = res["mixed"][2], res["fp64"][2]
     reuse_same = all(np.allclose(g_reuse[k], g32[k], rtol=1e-6, atol=0) for k in g32)

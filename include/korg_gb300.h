@@ -44,6 +44,7 @@ typedef enum {
     KORG_ETIMEOUT = 6   /* a device-side wait for staged data ran past its limit (results invalid) */
 } korg_status;
 
+/* Every call taking a `precision` returns KORG_EINVAL for any other value. */
 enum { KORG_FP64 = 0, KORG_MIXED = 1 };
 
 /* Line list (Korg.Line, src/linelist.jl:5-14), sorted by wl. */
@@ -367,8 +368,10 @@ KORG_API int korg_math_selftest(korg_ctx *ctx, int64_t n, double *max_ulp_exp, d
  * every GPU loading the library holds until exit.  That is enough for about 35,000 lines of a
  * 56-layer atmosphere in KORG_MIXED (constants take layers x 32 bytes per line, 48 in
  * KORG_FP64); larger problems return KORG_ETOOBIG without launching anything.
- * The first call on a device looks up the array's address and writes lookup tables into it
- * with a synchronous copy: make that first call before any stream capture.  Every call shares
+ * The first call in each CUDA context -- the first call on a device, and the first one again
+ * after cudaDeviceReset or in another driver-API context -- looks up the array's address and
+ * writes lookup tables into it with a synchronous copy: make that first call before any stream
+ * capture.  Every call shares
  * the one array (its counters are cleared at the start of each call, the rest is overwritten),
  * so calls whose work overlaps on the GPU -- different streams, or threads without ordering --
  * race; serialise them on one stream. */

@@ -670,15 +670,19 @@ __global__ void __launch_bounds__(512, MIXED ? 2 : 1) line_adj_kernel(LineAdjArg
         s_abort = 0;
     }
     __syncthreads();
-    int64_t g0 = 0;  // stages this block has run before the current item (ring slot = stage mod ADJ_STAGES)
-    int pcur = 0;    // thread 0: the (chunk, tier) pair of the last item (items arrive in increasing order)
-    // bounded wait; a wait that runs out marks the block aborted and reports it
-    auto wait = [&](uint64_t* bar, unsigned parity) {
-        if (s_abort) return;
+    int64_t g0 = 0;      // stages this block has run before the current item (ring slot = stage mod ADJ_STAGES)
+    int64_t issued = 0;  // producer warp: stages whose copies it has issued (all items so far)
+    int pcur = 0;        // thread 0: the (chunk, tier) pair of the last item (items arrive in increasing order)
+    // bounded wait; a wait that runs out marks the block aborted and reports it.  Returns false
+    // once the block is aborted (the caller then stops waiting).
+    auto wait = [&](uint64_t* bar, unsigned parity) -> bool {
+        if (s_abort) return false;
         if (!mbar_wait(bar, parity)) {
             s_abort = 1;
             *reinterpret_cast<volatile int*>(a.err) = 1;
+            return false;
         }
+        return true;
     };
     for (;;) {
         if (threadIdx.x == 0) {  // the next item whose window meets its chunk
@@ -696,7 +700,17 @@ __global__ void __launch_bounds__(512, MIXED ? 2 : 1) line_adj_kernel(LineAdjArg
             }
         }
         __syncthreads();
-        if (s_item >= total || s_abort) break;
+        if (s_item >= total || s_abort) {
+            // An aborted block may have bulk copies in flight into its ring (the producer stops
+            // issuing once it sees the abort, but the consumers stopped waiting for the last
+            // stages).  Before the block's shared memory is released, the producer waits, with
+            // the same bound, for the full barriers of the last stages it issued; earlier stages
+            // were waited for by the consumers before the abort.
+            if (s_abort && warp == PW && lane == 0)
+                for (int64_t gq = issued > ADJ_STAGES ? issued - ADJ_STAGES : 0; gq < issued; gq++)
+                    mbar_wait(&s_full[gq % ADJ_STAGES], unsigned((gq / ADJ_STAGES) & 1));
+            break;
+        }
         const int64_t i = s_i, j0 = s_j0, j1 = s_j1;
         // classify the layers: a > 0.2 ("slow") or not, counted per warp of layer indices
         bool slow_l = false;
@@ -765,7 +779,11 @@ __global__ void __launch_bounds__(512, MIXED ? 2 : 1) line_adj_kernel(LineAdjArg
             for (int sq = 0; sq < nsub; sq++) {
                 const int64_t gq = g0 + sq;
                 const int b = int(gq % ADJ_STAGES);
-                if (gq >= ADJ_STAGES) wait(&s_empty[b], unsigned((gq / ADJ_STAGES - 1) & 1));
+                bool ok = true;
+                if (gq >= ADJ_STAGES) ok = wait(&s_empty[b], unsigned((gq / ADJ_STAGES - 1) & 1));
+                // warp-uniform: no copy is issued once any wait has failed or the block is aborted
+                if (__any_sync(0xffffffffu, !ok || s_abort != 0)) break;
+                issued = gq + 1;
                 const int64_t js = j0 + int64_t(sq) * SUB;
                 const int nw = int(min(int64_t(SUB), j1 - js + 1));
                 GT* dst = s_g + size_t(b) * SUB * Ls;

@@ -1,5 +1,7 @@
 // korg_gb300.cu -- C ABI, context, scratch arena and launch orchestration of the GB300
 // synthesis hot path.  Kernels live in lines.cuh, hydrogen.cuh and rt.cuh.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -12,7 +14,6 @@
 #include <string>
 #include <thread>
 #include <type_traits>
-#include <vector>
 #include <vector>
 
 #include "../../include/korg_gb300.h"
@@ -113,6 +114,14 @@ int set_err(korg_ctx* c, int code, const char* fmt, ...) {
     do {                              \
         int r_ = (expr);              \
         if (r_ != KORG_OK) return r_; \
+    } while (0)
+
+// precision must be KORG_FP64 or KORG_MIXED; anything else is a caller error, not the FP64 form
+#define KPREC(prec)                                                                          \
+    do {                                                                                     \
+        if ((prec) != KORG_FP64 && (prec) != KORG_MIXED)                                     \
+            return set_err(ctx, KORG_EINVAL, "precision must be KORG_FP64 (0) or KORG_MIXED (1), got %d", \
+                           int(prec));                                                       \
     } while (0)
 
 void drop_graph(korg_ctx* ctx) {
@@ -1305,6 +1314,7 @@ KORG_API int korg_line_absorption_dev(korg_ctx* ctx, double* alpha, const double
                                       double cutoff, int precision, void* stream) {
     if (!ctx || !alpha || !wls || nwl < 1 || !lines || !layers || !cntm || cntm->nk < 1)
         return ctx ? set_err(ctx, KORG_EINVAL, "bad arguments") : KORG_EINVAL;
+    KPREC(precision);
     KCUDA(cudaSetDevice(ctx->device));
     KCHECK(reset_counters(ctx, static_cast<cudaStream_t>(stream)));
     return run_line_absorption(ctx, alpha, wls, nwl, lines_dev(lines), layers_dev(layers),
@@ -1316,6 +1326,7 @@ KORG_API int korg_line_absorption(korg_ctx* ctx, double* alpha, const double* wl
                                   const korg_lines* lines, const korg_layers* layers, const korg_cntm* cntm,
                                   double cutoff, int precision, int64_t* n_evals) {
     if (!ctx) return KORG_EINVAL;
+    KPREC(precision);
     if (!alpha || !cntm || cntm->nk < 1 || !cntm->vals || (cntm->nk > 1 && !cntm->knots))
         return set_err(ctx, KORG_EINVAL, "bad alpha / continuum arguments");
     KCHECK(check_wls(ctx, wls, nwl));
@@ -1359,6 +1370,7 @@ KORG_API int korg_hydrogen_lines_dev(korg_ctx* ctx, double* alpha, const double*
                                      int precision, void* stream) {
     if (!ctx || !alpha || !wls || nwl < 1 || L < 1 || !T || !ne || !nH_I || !nHe_I || !UH_I || !xi)
         return ctx ? set_err(ctx, KORG_EINVAL, "bad arguments") : KORG_EINVAL;
+    KPREC(precision);
     KCUDA(cudaSetDevice(ctx->device));
     const HLayers hl{L, T, ne, nH_I, nHe_I, UH_I, xi};
     return run_hydrogen(ctx, alpha, wls, nwl, hl, window, use_MHD, precision == KORG_MIXED,
@@ -1369,6 +1381,7 @@ KORG_API int korg_hydrogen_line_absorption(korg_ctx* ctx, double* alphas, const 
                                            double T, double ne, double nH_I, double nHe_I, double UH_I, double xi,
                                            double window, int use_MHD, int precision) {
     if (!ctx) return KORG_EINVAL;
+    KPREC(precision);
     if (!alphas) return set_err(ctx, KORG_EINVAL, "null alphas");
     KCHECK(check_wls(ctx, wls, nwl));
     KCUDA(cudaSetDevice(ctx->device));
@@ -1514,6 +1527,7 @@ KORG_API int korg_synthesize_dev(korg_ctx* ctx, const korg_synth_inputs* in, con
                                  double* flux, double* cntm, double* alpha_out, void* stream) {
     if (!ctx || !in || !lines || !lines5 || !wls || nwl < 1 || !flux || !cntm)
         return ctx ? set_err(ctx, KORG_EINVAL, "bad arguments") : KORG_EINVAL;
+    KPREC(precision);
     if (in->cntm.nk < 2 || in->layers.L < 1)
         return set_err(ctx, KORG_EINVAL, "synthesize needs a continuum grid of at least 2 knots");
     KCUDA(cudaSetDevice(ctx->device));
@@ -1536,6 +1550,7 @@ KORG_API int korg_synthesize(korg_ctx* ctx, const korg_synth_inputs* in, const k
                              const korg_lines* lines5, const double* wls, int64_t nwl, int precision, double* flux,
                              double* cntm, double* alpha_out, double* alpha_ref_out) {
     if (!ctx) return KORG_EINVAL;
+    KPREC(precision);
     if (!in || !flux || !cntm) return set_err(ctx, KORG_EINVAL, "bad arguments");
     KCHECK(check_wls(ctx, wls, nwl));
     KCHECK(check_layers(ctx, &in->layers));
@@ -1625,6 +1640,7 @@ KORG_API int korg_synthesize_vjp_dev(korg_ctx* ctx, const korg_synth_inputs* in,
                                      const double* dflux, const double* dcntm, const korg_synth_grads* grads,
                                      int flags, void* stream) {
     if (!ctx) return KORG_EINVAL;
+    KPREC(precision);
     if (!in || !lines || !lines5 || !wls || nwl < 1 || !grads || (!dflux && !dcntm))
         return set_err(ctx, KORG_EINVAL, "bad arguments");
     if (in->cntm.nk < 2 || in->layers.L < 1)
@@ -1645,6 +1661,7 @@ KORG_API int korg_synthesize_vjp(korg_ctx* ctx, const korg_synth_inputs* in, con
                                  const korg_lines* lines5, const double* wls, int64_t nwl, int precision,
                                  const double* dflux, const double* dcntm, const korg_synth_grads* grads, int flags) {
     if (!ctx) return KORG_EINVAL;
+    KPREC(precision);
     if (!in || !grads || (!dflux && !dcntm)) return set_err(ctx, KORG_EINVAL, "bad arguments");
     KCHECK(check_wls(ctx, wls, nwl));
     KCHECK(check_layers(ctx, &in->layers));
@@ -1840,6 +1857,7 @@ KORG_API int korg_molecular_cross_section_dev(korg_ctx* ctx, const korg_lines* l
                                               const double* vmic_vals, int32_t nv, double cutoff_alpha,
                                               int precision, double* table, void* stream) {
     if (!ctx) return KORG_EINVAL;
+    KPREC(precision);
     if (!lines || !wls || nwl < 1 || !T || !inv_U || nT < 1 || !vmic_vals || nv < 1 || !table || !(cutoff_alpha > 0))
         return set_err(ctx, KORG_EINVAL, "bad arguments");
     KCUDA(cudaSetDevice(ctx->device));
@@ -1901,6 +1919,7 @@ KORG_API int korg_set_batch_options(korg_ctx* ctx, int use_graph, int autotune, 
 KORG_API int korg_get_tile_config(korg_ctx* ctx, int32_t L, int precision, int32_t* tw, int32_t* stage,
                                   int32_t* split, int32_t* tuned) {
     if (!ctx || !tw || !stage) return KORG_EINVAL;
+    KPREC(precision);
     const bool mixed = precision == KORG_MIXED;
     const TileCfg c = tile_cfg(ctx, L, mixed);
     *tw = c.tw;
@@ -1913,6 +1932,7 @@ KORG_API int korg_get_tile_config(korg_ctx* ctx, int32_t L, int precision, int32
 KORG_API int korg_set_tile_config(korg_ctx* ctx, int32_t L, int precision, int32_t tw, int32_t stage,
                                   int32_t split) {
     if (!ctx) return KORG_EINVAL;
+    KPREC(precision);
     const bool mixed = precision == KORG_MIXED;
     int kmax = 0;
     const int G = layer_groups(L, &kmax);
@@ -1928,6 +1948,7 @@ KORG_API int korg_set_tile_config(korg_ctx* ctx, int32_t L, int precision, int32
 KORG_API int korg_synthesize_batch_dev(korg_ctx* ctx, int32_t nspec, const korg_batch_item* items,
                                        const double* wls, int64_t nwl, int precision, void* stream) {
     if (!ctx) return KORG_EINVAL;
+    KPREC(precision);
     if (nspec < 1 || !items || !wls || nwl < 1 || nwl > INT32_MAX - 1)
         return set_err(ctx, KORG_EINVAL, "bad batch arguments");
     KCUDA(cudaSetDevice(ctx->device));
@@ -2114,26 +2135,56 @@ namespace {
 constexpr size_t NOALLOC_SCRATCH_BYTES = size_t(64) << 20;  // KORG_NOALLOC_SCRATCH_BYTES in the header
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
 
-constexpr int NOALLOC_MAX_DEVICES = 64;
 std::mutex g_noalloc_mutex;
-unsigned char* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};  // device address of the array, per device
+// Device address of the array per CUDA context, keyed by the driver's process-unique context
+// id: a device reset (or another driver-API context on the same device) gets a new id, and so
+// a fresh lookup and a fresh copy of the math tables, instead of a stale address.
+std::map<unsigned long long, unsigned char*> g_noalloc_ptr;
+PFN_cuCtxGetCurrent_v4000 g_cu_ctx_get_current = nullptr;
+PFN_cuCtxGetId_v12000 g_cu_ctx_get_id = nullptr;
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
-// Device address of the scratch array for the current device; the first call on a device looks
-// it up and writes the math tables into it (a synchronous copy, hence before any capture).
-int noalloc_setup(int dev, unsigned char** out) {
+// Id of the current context (made current by the runtime if no context is current yet).
+int noalloc_context_id(unsigned long long* id) {
+    if (!g_cu_ctx_get_current || !g_cu_ctx_get_id) {
+        cudaDriverEntryPointQueryResult q1, q2;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", reinterpret_cast<void**>(&g_cu_ctx_get_current),
+                                             12000, cudaEnableDefault, &q1) != cudaSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", reinterpret_cast<void**>(&g_cu_ctx_get_id), 12000,
+                                             cudaEnableDefault, &q2) != cudaSuccess ||
+            q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess) {
+            g_cu_ctx_get_current = nullptr;
+            return KORG_ECUDA;
+        }
+    }
+    CUcontext c = nullptr;
+    if (g_cu_ctx_get_current(&c) != CUDA_SUCCESS) return KORG_ECUDA;
+    if (!c) {  // no context yet: the runtime makes the current device's primary context current
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaSetDevice(dev) != cudaSuccess) return KORG_ECUDA;
+        if (g_cu_ctx_get_current(&c) != CUDA_SUCCESS || !c) return KORG_ECUDA;
+    }
+    return g_cu_ctx_get_id(c, id) == CUDA_SUCCESS ? KORG_OK : KORG_ECUDA;
+}
+
+// Device address of the scratch array in the current context; the first call in a context
+// looks it up and writes the math tables into it (a synchronous copy, hence before any capture).
+int noalloc_setup(unsigned char** out) {
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return KORG_EINVAL;
-    if (!g_noalloc_ptr[dev]) {
+    unsigned long long id = 0;
+    const int rc = noalloc_context_id(&id);
+    if (rc != KORG_OK) return rc;
+    auto it = g_noalloc_ptr.find(id);
+    if (it == g_noalloc_ptr.end()) {
         void* p = nullptr;
         if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return KORG_ECUDA;
         MathTables t;
         fill_math_tables(t);
         if (cudaMemcpy(p, &t, sizeof t, cudaMemcpyHostToDevice) != cudaSuccess) return KORG_ECUDA;
-        g_noalloc_ptr[dev] = static_cast<unsigned char*>(p);
+        it = g_noalloc_ptr.emplace(id, static_cast<unsigned char*>(p)).first;
     }
-    *out = g_noalloc_ptr[dev];
+    *out = it->second;
     return KORG_OK;
 }
 
@@ -2169,6 +2220,7 @@ extern "C" KORG_API int korg_line_absorption_noalloc(double* alpha, const double
                                                     const korg_cntm* cntm, double cutoff, int precision,
                                                     void* stream) {
     if (!alpha || !wls || nwl < 1 || !lines || !layers || !cntm || cntm->nk < 1 || lines->n < 0) return KORG_EINVAL;
+    if (precision != KORG_FP64 && precision != KORG_MIXED) return KORG_EINVAL;
     if (lines->n == 0) return KORG_OK;  // src/line_absorption.jl:35-37: alpha untouched
     const bool mixed = precision == KORG_MIXED;
     const int L = layers->L;
@@ -2193,10 +2245,8 @@ extern "C" KORG_API int korg_line_absorption_noalloc(double* alpha, const double
     const size_t o_tc = off; off += align256(sizeof(int32_t) * size_t(n));
     const size_t o_meta = off; off += align256(sizeof(int32_t) * (NTIER * size_t(nblk) + NTIER + 2));
     if (off > NOALLOC_SCRATCH_BYTES) return KORG_ETOOBIG;
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return KORG_ECUDA;
     unsigned char* sp = nullptr;
-    int rc = noalloc_setup(dev, &sp);
+    int rc = noalloc_setup(&sp);
     if (rc != KORG_OK) return rc;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     auto* ctr = reinterpret_cast<unsigned long long*>(sp + o_ctr);

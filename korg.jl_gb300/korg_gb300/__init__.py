@@ -15,13 +15,14 @@ __all__ = ["Wavelengths", "LineList", "make_line", "filter_linelist", "alpha_500
            "radiative_transfer", "synthesize", "prepare_synthesis", "synthesize_prepared"]
 
 
+_API = ("line_absorption_", "hydrogen_line_absorption_", "radiative_transfer", "synthesize", "prepare_synthesis",
+        "synthesize_prepared", "SynthesisInputs", "SynthesisResult", "ContinuumInterpolant", "synthesize_vjp",
+        "loss_and_gradient", "physical_gradient")
+
+
 def __getattr__(name):
-    # the API module is imported on first use (it loads the CUDA library binding); importing it
-    # binds the package attribute `synthesize` to the module, whose synthesize() is the function
-    if name in ("line_absorption_", "hydrogen_line_absorption_", "radiative_transfer", "synthesize",
-                "prepare_synthesis", "synthesize_prepared", "SynthesisInputs", "SynthesisResult",
-                "ContinuumInterpolant", "synthesize_vjp", "loss_and_gradient", "physical_gradient"):
+    # the API module (which loads the CUDA library binding on first call) is imported on first use
+    if name in _API:
         import importlib
-        _s = importlib.import_module(".synthesize", __name__)
-        return _s if name == "synthesize" else getattr(_s, name)
+        return getattr(importlib.import_module(".api", __name__), name)
     raise AttributeError(name)

@@ -14,7 +14,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from .synthesize import SynthesisInputs, _prec
+from .api import SynthesisInputs, _prec
 
 FIELDS = ("T", "ne", "n_eff_vdW", "xi", "n_div_U", "log_gf", "cntm_vals", "alpha_ref_cntm")
 

@@ -15,7 +15,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from .synthesize import SynthesisInputs, _prec
+from .api import SynthesisInputs, _prec
 
 
 class _Packer:

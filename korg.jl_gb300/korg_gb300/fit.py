@@ -12,7 +12,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from .synthesize import SynthesisInputs
+from .api import SynthesisInputs
 
 
 def _obs_cm(obs):

@@ -140,7 +140,7 @@ def abundance_variants(inp, n_variants=16, seed=0, spread=0.3):
 
 def prepare(work: Workload, **kwargs):
     """Synthetic atmosphere + host precompute for a workload."""
-    from .synthesize import prepare_synthesis
+    from .api import prepare_synthesis
     atm, A_X = standin.synthetic_atmosphere(work.Teff, work.logg, work.m_H, work.L)
     return prepare_synthesis(atm, work.linelist, A_X, work.wavelengths, vmic=work.vmic,
                              hydrogen_lines=work.hydrogen_lines, **kwargs)

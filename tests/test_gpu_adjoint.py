@@ -34,7 +34,7 @@ def _case(n_lines=600, wl=(5000.0, 5030.0), seed=7):
 
 def _obs(inp, ctx):
     """A seeded perturbed synthetic observation: log gf shifted by N(0, 0.1) dex."""
-    from korg_gb300.synthesize import synthesize_prepared
+    from korg_gb300.api import synthesize_prepared
     rng = np.random.default_rng(1)
     o = copy.copy(inp)
     o.linelist = copy.copy(inp.linelist)
@@ -44,7 +44,7 @@ def _obs(inp, ctx):
 
 
 def _loss(inp, obs, ctx, precision="fp64"):
-    from korg_gb300.synthesize import rectified_loss, synthesize_prepared
+    from korg_gb300.api import rectified_loss, synthesize_prepared
     r = synthesize_prepared(inp, precision=precision, ctx=ctx)
     return rectified_loss(r.flux, r.cntm, obs)[0]
 
@@ -84,7 +84,7 @@ PARAMS = [("T", 5), ("T", 25), ("T", 40), ("ne", 20), ("ne", 45), ("n_eff_vdW", 
 
 
 def test_vjp_fp64_matches_central_differences(ctx):
-    from korg_gb300.synthesize import loss_and_gradient
+    from korg_gb300.api import loss_and_gradient
     inp = _case()
     obs = _obs(inp, ctx)
     loss, g = loss_and_gradient(inp, obs, precision="fp64", ctx=ctx)
@@ -97,7 +97,7 @@ def test_vjp_fp64_matches_central_differences(ctx):
 
 
 def test_vjp_mixed_close_to_fp64(ctx):
-    from korg_gb300.synthesize import loss_and_gradient
+    from korg_gb300.api import loss_and_gradient
     inp = _case(n_lines=1500, wl=(5000.0, 5060.0), seed=11)
     obs = _obs(inp, ctx)
     _, g64 = loss_and_gradient(inp, obs, precision="fp64", ctx=ctx)
@@ -109,7 +109,7 @@ def test_vjp_mixed_close_to_fp64(ctx):
 
 
 def test_vjp_without_hydrogen_holds_hydrogen_fixed(ctx):
-    from korg_gb300.synthesize import rectified_loss, synthesize_prepared, synthesize_vjp
+    from korg_gb300.api import rectified_loss, synthesize_prepared, synthesize_vjp
     inp = _case()
     obs = _obs(inp, ctx)
     r = synthesize_prepared(inp, precision="fp64", ctx=ctx)
@@ -124,7 +124,7 @@ def test_vjp_pinned_to_oracle_differences(ctx, oracle_lib):
     """Central differences of the FP64 oracle (the CPU restatement of the reference) agree with
     the GPU reverse mode."""
     from korg_gb300.data import stark_profiles
-    from korg_gb300.synthesize import loss_and_gradient, rectified_loss
+    from korg_gb300.api import loss_and_gradient, rectified_loss
     inp = _case(n_lines=250, wl=(5000.0, 5010.0), seed=3)
     obs = _obs(inp, ctx)
     _, g = loss_and_gradient(inp, obs, precision="fp64", ctx=ctx)
@@ -142,7 +142,7 @@ def test_vjp_pinned_to_oracle_differences(ctx, oracle_lib):
 def test_torch_autograd_matches_vjp(ctx):
     torch = pytest.importorskip("torch")
     from korg_gb300.autograd import Synthesis
-    from korg_gb300.synthesize import loss_and_gradient
+    from korg_gb300.api import loss_and_gradient
     inp = _case(n_lines=400, wl=(5000.0, 5020.0), seed=5)
     obs = _obs(inp, ctx)
     _, g = loss_and_gradient(inp, obs, precision="fp64", ctx=ctx)
@@ -158,7 +158,7 @@ def test_torch_autograd_matches_vjp(ctx):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_vjp_reusing_the_forward_opacity(ctx, precision):
-    from korg_gb300.synthesize import loss_and_gradient
+    from korg_gb300.api import loss_and_gradient
     inp = _case(n_lines=500, wl=(5000.0, 5025.0), seed=9)
     obs = _obs(inp, ctx)
     _, g0 = loss_and_gradient(inp, obs, precision=precision, ctx=ctx)
@@ -172,7 +172,7 @@ def test_vjp_many_layers(ctx, precision):
     """128 layers, the most the reverse mode takes: the staged-G ring of the FP64 line adjoint
     shrinks its stages to fit shared memory (rows of 1 kB)."""
     from korg_gb300 import synthetic
-    from korg_gb300.synthesize import loss_and_gradient
+    from korg_gb300.api import loss_and_gradient
     w = synthetic.config0(seed=4, n_lines=300)
     w.L = 128
     w.wavelengths = (5000.0, 5015.0)

@@ -17,7 +17,7 @@ def _inputs(specs):
 
 
 def _single(inp, precision, ctx):
-    from korg_gb300.synthesize import synthesize_prepared
+    from korg_gb300.api import synthesize_prepared
     r = synthesize_prepared(inp, precision=precision, ctx=ctx)
     return r.flux, r.cntm
 
@@ -92,7 +92,7 @@ def test_tile_shapes_give_identical_opacity(gpu_lib, precision):
     boundaries only."""
     import ctypes as C
     from korg_gb300 import synthetic
-    from korg_gb300.synthesize import synthesize_prepared
+    from korg_gb300.api import synthesize_prepared
     inp = synthetic.prepare(synthetic.config0(n_lines=3000))
     prec = gpu_lib.KORG_MIXED if precision == "mixed" else gpu_lib.KORG_FP64
     L = len(inp.T)

@@ -15,7 +15,7 @@ KORG_ETIMEOUT = 6
 
 def test_bounded_wait_reports_timeout_and_context_stays_usable(gpu_lib):
     from korg_gb300 import synthetic
-    from korg_gb300.synthesize import synthesize_prepared
+    from korg_gb300.api import synthesize_prepared
     ctx = gpu_lib.Context(0)
     ctx.ensure_stark()
     lib = ctx.lib

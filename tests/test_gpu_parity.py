@@ -208,7 +208,7 @@ def test_lyman_golden_gpu(ctx):
 
 def test_synthesize_fp64_parity(ctx, cfg0, oracle_lib):
     from korg_gb300.data import stark_profiles
-    from korg_gb300.synthesize import synthesize_prepared
+    from korg_gb300.api import synthesize_prepared
     flux, cntm, alpha, aref, ev = oracle_lib.synthesize(cfg0, cfg0.linelist, cfg0.linelist5, stark_profiles(),
                                                         cfg0.wls.all_wls, nthreads=NT)
     res = synthesize_prepared(cfg0, precision="fp64", return_alpha=True, ctx=ctx)
@@ -221,7 +221,7 @@ def test_synthesize_fp64_parity(ctx, cfg0, oracle_lib):
 
 def test_synthesize_mixed_error_budget(ctx, cfg0, oracle_lib):
     from korg_gb300.data import stark_profiles
-    from korg_gb300.synthesize import synthesize_prepared
+    from korg_gb300.api import synthesize_prepared
     flux, cntm, _, _, _ = oracle_lib.synthesize(cfg0, cfg0.linelist, cfg0.linelist5, stark_profiles(),
                                                 cfg0.wls.all_wls, nthreads=NT)
     res = synthesize_prepared(cfg0, precision="mixed", ctx=ctx)
@@ -235,7 +235,7 @@ def test_synthesize_mixed_error_budget(ctx, cfg0, oracle_lib):
 def test_synthesize_multi_range_and_determinism(ctx, oracle_lib):
     from korg_gb300 import synthetic
     from korg_gb300.data import stark_profiles
-    from korg_gb300.synthesize import synthesize_prepared
+    from korg_gb300.api import synthesize_prepared
     w = synthetic.config0(n_lines=400)
     w.wavelengths = [(5000, 5020), (5050, 5070)]
     inp = synthetic.prepare(w)
@@ -252,7 +252,7 @@ def test_synthesize_device_pointers_match_host(ctx, cfg0):
     """korg_synthesize_dev on torch-allocated device buffers gives the host call's answer."""
     torch = pytest.importorskip("torch")
     from korg_gb300 import _lib
-    from korg_gb300.synthesize import synthesize_prepared
+    from korg_gb300.api import synthesize_prepared
     host = synthesize_prepared(cfg0, precision="mixed", ctx=ctx)
     dev = torch.device("cuda:0")
     keep = []

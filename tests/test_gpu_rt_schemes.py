@@ -76,7 +76,7 @@ def test_python_radiative_transfer_dispatch(gpu_lib, column):
     and the general kernel otherwise; with anchored tau every formal solution lands within the
     reference's 16% of it (Bezier tau integrates over the geometric heights, which this
     synthetic column does not have consistently with tau_ref, so it is only run)."""
-    from korg_gb300.synthesize import radiative_transfer
+    from korg_gb300.api import radiative_transfer
 
     inp, alpha, S = column
 

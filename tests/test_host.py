@@ -109,3 +109,19 @@ def test_no_oracle_in_product():
             if fn.endswith((".py", ".cu", ".cuh", ".h", ".jl")):
                 src = open(os.path.join(dirpath, fn)).read()
                 assert "korg_oracle" not in src and "import oracle" not in src, fn
+
+
+def test_reference_signature_entry_points_are_functions():
+    """korg_gb300.synthesize is the function synthesize(atm, linelist, A_X, wavelengths; ...) of
+    src/synthesize.jl:138, not a module; the other mirrors of the reference API likewise."""
+    import inspect
+    import korg_gb300
+    for name in ("synthesize", "line_absorption_", "hydrogen_line_absorption_", "radiative_transfer",
+                 "prepare_synthesis", "synthesize_prepared", "synthesize_vjp"):
+        f = getattr(korg_gb300, name)
+        assert callable(f) and inspect.isfunction(f), name
+    params = list(inspect.signature(korg_gb300.synthesize).parameters)
+    assert params[:4] == ["atm", "linelist", "A_X", "wavelengths"]
+    params = list(inspect.signature(korg_gb300.line_absorption_).parameters)
+    assert params[:9] == ["alpha", "linelist", "wls", "temps", "ne", "n_densities", "partition_fns", "xi",
+                          "alpha_cntm"]

@@ -4,7 +4,10 @@ It exists for callers that cannot allocate device memory -- code running inside 
 or arena it does not own, a process whose allocator is locked after start-up, or a caller in
 the middle of stream capture.  It must give the same alpha as korg_line_absorption_dev, the
 ordinary device-pointer entry point, call after call, even though every call reuses one
-fixed device array for its scratch.  This file is named so that pytest collects it last.
+fixed device array for its scratch.  Both run the same kernels with the same tile shape, so
+the results must be bitwise equal: a value left behind in the shared array (a stale counter or
+sortedness flag that changed the order of additions) would show up here.  This file is named so
+that pytest collects it last.
 """
 import ctypes as C
 
@@ -60,21 +63,69 @@ def test_noalloc_matches_device_entry_point(gpu_lib):
                                                   stream)
             assert rc == 0, f"precision {precision}, call {call}: status {rc}"
             torch.cuda.synchronize()
-            np.testing.assert_allclose(got.cpu().numpy(), ref, rtol=1e-9, atol=0)
+            np.testing.assert_array_equal(got.cpu().numpy(), ref)
+    ctx.close()
+
+
+def _noalloc(lib, alpha, wls, lines, lay, cn, inp, precision, stream):
+    return lib.korg_line_absorption_noalloc(alpha.data_ptr(), wls.data_ptr(), len(wls), C.byref(lines), C.byref(lay),
+                                            C.byref(cn), inp.cutoff_threshold, precision, stream)
+
+
+def test_noalloc_under_stream_capture(gpu_lib):
+    """A caller in the middle of stream capture: after one ordinary call (the per-context set-up),
+    a call captured into a CUDA graph on a side stream replays to the device entry point's alpha."""
+    torch = pytest.importorskip("torch")
+    from korg_gb300 import synthetic
+    w = synthetic.config0(n_lines=600)
+    w.wavelengths = (5000, 5040)
+    inp = synthetic.prepare(w)
+    dev = torch.device("cuda:0")
+    lines, lay, cn, wls, alpha0, keep = _device_inputs(torch, inp, dev)
+    ctx = gpu_lib.Context(0)
+    lib = ctx.lib
+    main = torch.cuda.current_stream(dev)
+    for precision in (gpu_lib.KORG_MIXED, gpu_lib.KORG_FP64):
+        ref = alpha0.clone()
+        assert lib.korg_line_absorption_dev(ctx.h, ref.data_ptr(), wls.data_ptr(), len(wls), C.byref(lines),
+                                            C.byref(lay), C.byref(cn), inp.cutoff_threshold, precision,
+                                            main.cuda_stream) == 0
+        got = alpha0.clone()
+        assert _noalloc(lib, got, wls, lines, lay, cn, inp, precision, main.cuda_stream) == 0  # set-up call
+        torch.cuda.synchronize()
+        ref = ref.cpu().numpy()
+        np.testing.assert_array_equal(got.cpu().numpy(), ref)
+        graph = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(main)
+        rcs = []
+        with torch.cuda.graph(graph, stream=side):
+            rcs.append(_noalloc(lib, got, wls, lines, lay, cn, inp, precision, side.cuda_stream))
+        assert rcs == [0]
+        for replay in range(2):
+            got.copy_(alpha0)
+            graph.replay()
+            torch.cuda.synchronize()
+            np.testing.assert_array_equal(got.cpu().numpy(), ref, err_msg=f"precision {precision}, replay {replay}")
+        del graph
     ctx.close()
 
 
 def test_noalloc_rejects_problems_larger_than_its_array(gpu_lib):
     torch = pytest.importorskip("torch")
     from korg_gb300 import synthetic
-    w = synthetic.config0(n_lines=100_000)  # 100k lines x 56 layers x 48 B of FP64 constants > 64 MiB
+    # 100k lines x 56 layers: 48 B of FP64 constants (269 MB) or 32 B of mixed ones (179 MB) per
+    # line and layer, both above the 64 MiB array
+    w = synthetic.config0(n_lines=100_000)
     inp = synthetic.prepare(w)
     dev = torch.device("cuda:0")
     lines, lay, cn, wls, alpha0, keep = _device_inputs(torch, inp, dev)
+    lib = gpu_lib.lib()
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    for precision in (gpu_lib.KORG_FP64, gpu_lib.KORG_MIXED):
+        got = alpha0.clone()
+        assert _noalloc(lib, got, wls, lines, lay, cn, inp, precision, stream) == 5  # KORG_ETOOBIG
+        torch.cuda.synchronize()
+        assert torch.equal(got, alpha0)  # nothing was launched
     got = alpha0.clone()
-    rc = gpu_lib.lib().korg_line_absorption_noalloc(got.data_ptr(), wls.data_ptr(), len(wls), C.byref(lines),
-                                                    C.byref(lay), C.byref(cn), inp.cutoff_threshold,
-                                                    gpu_lib.KORG_FP64, torch.cuda.current_stream(dev).cuda_stream)
-    assert rc == 5  # KORG_ETOOBIG
-    torch.cuda.synchronize()
-    assert torch.equal(got, alpha0)  # nothing was launched
+    assert _noalloc(lib, got, wls, lines, lay, cn, inp, 2, stream) == 1  # KORG_EINVAL: not a precision
