@@ -205,7 +205,8 @@ struct LineScratch {
     float* xfar = nullptr;
     uint32_t* amask = nullptr;
     int32_t *lb = nullptr, *ub = nullptr, *ci = nullptr, *tier_idx = nullptr, *tier_ci = nullptr, *tier_meta = nullptr;
-    float4* params_w = nullptr;  // mixed: wing coefficients, after the packed constants
+    float4* params_w = nullptr;  // mixed: wing cubics, after the packed constants
+    float* xcub = nullptr;       // mixed: cubic boundaries [n][G], after xfar
 };
 
 size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -216,7 +217,8 @@ int part_blocks(int64_t n) { return int((n + PART_CHUNK - 1) / PART_CHUNK); }
 size_t line_scratch(unsigned char* base, int64_t n, int L, int Lp, int G, bool mixed, LineScratch* out) {
     const size_t nn = size_t(std::max<int64_t>(n, 1));
     const size_t sz[10] = {sizeof(LayerConst) * L, (mixed ? 2 * sizeof(float4) : sizeof(P64)) * nn * Lp,
-                           sizeof(float) * nn * G, sizeof(uint32_t) * nn, 4 * nn, 4 * nn, 4 * nn, 4 * nn, 4 * nn,
+                           sizeof(float) * nn * G * (mixed ? 2 : 1), sizeof(uint32_t) * nn, 4 * nn, 4 * nn, 4 * nn,
+                           4 * nn, 4 * nn,
                            sizeof(int32_t) * (NTIER * size_t(part_blocks(n)) + NTIER + 2)};
     size_t off[10], tot = 0;
     for (int i = 0; i < 10; i++) { off[i] = tot; tot += a256(sz[i]); }
@@ -225,6 +227,7 @@ size_t line_scratch(unsigned char* base, int64_t n, int L, int Lp, int G, bool m
         out->params = base + off[1];
         out->params_w = mixed ? reinterpret_cast<float4*>(base + off[1]) + nn * Lp : nullptr;
         out->xfar = reinterpret_cast<float*>(base + off[2]);
+        out->xcub = mixed ? out->xfar + nn * G : nullptr;
         out->amask = reinterpret_cast<uint32_t*>(base + off[3]);
         out->lb = reinterpret_cast<int32_t*>(base + off[4]);
         out->ub = reinterpret_cast<int32_t*>(base + off[5]);
@@ -252,6 +255,7 @@ TileArgs make_tile_args(const LineScratch& sc, double* alpha, const double* wls,
     ta.wl = ln.wl;
     ta.params = sc.params;
     ta.params_w = sc.params_w;
+    ta.xcub = sc.xcub;
     ta.lb = sc.lb;
     ta.ub = sc.ub;
     ta.tier_idx = sc.tier_idx;
@@ -268,7 +272,7 @@ int prep_lines(korg_ctx* ctx, const LineScratch& sc, const double* wls, int64_t 
     const int L = lay.L, Lp = G * kmax;
     auto* ctr = static_cast<unsigned long long*>(ctx->counters.p);
     layer_const_kernel<<<(L + 127) / 128, 128, 0, s>>>(lay, sc.lc);
-    PrepOut po{sc.params, sc.lb, sc.ub, sc.ci, sc.xfar, sc.amask, Lp, kmax, G, ctr, ctr + 1, sc.params_w};
+    PrepOut po{sc.params, sc.lb, sc.ub, sc.ci, sc.xfar, sc.amask, Lp, kmax, G, ctr, ctr + 1, sc.params_w, sc.xcub};
     const size_t prep_smem = size_t(256 / 32) * Lp * (sizeof(float) + sizeof(int));
     const unsigned pblocks = unsigned((ln.n * 32 + 255) / 256);
     auto* math = static_cast<MathTables*>(ctx->math.p);
@@ -2236,7 +2240,7 @@ extern "C" KORG_API int korg_line_absorption_noalloc(double* alpha, const double
     const size_t o_ctr = off; off += align256(4 * sizeof(unsigned long long));
     const size_t o_lc = off; off += align256(sizeof(LayerConst) * L);
     const size_t o_par = off; off += align256((mixed ? 2 * sizeof(float4) : sizeof(P64)) * size_t(n) * Lp);
-    const size_t o_xfar = off; off += align256(sizeof(float) * size_t(n) * G);
+    const size_t o_xfar = off; off += align256(sizeof(float) * size_t(n) * G * (mixed ? 2 : 1));
     const size_t o_am = off; off += align256(sizeof(uint32_t) * size_t(n));
     const size_t o_lb = off; off += align256(sizeof(int32_t) * size_t(n));
     const size_t o_ub = off; off += align256(sizeof(int32_t) * size_t(n));
@@ -2263,7 +2267,8 @@ extern "C" KORG_API int korg_line_absorption_noalloc(double* alpha, const double
     PrepOut po{sp + o_par, reinterpret_cast<int32_t*>(sp + o_lb), reinterpret_cast<int32_t*>(sp + o_ub),
                reinterpret_cast<int32_t*>(sp + o_ci), reinterpret_cast<float*>(sp + o_xfar),
                reinterpret_cast<uint32_t*>(sp + o_am), Lp, kmax, G, ctr, ctr + 1,
-               mixed ? reinterpret_cast<float4*>(sp + o_par) + size_t(n) * Lp : nullptr};
+               mixed ? reinterpret_cast<float4*>(sp + o_par) + size_t(n) * Lp : nullptr,
+               mixed ? reinterpret_cast<float*>(sp + o_xfar) + size_t(n) * G : nullptr};
     const size_t prep_smem = size_t(256 / 32) * Lp * (sizeof(float) + sizeof(int));
     const unsigned pblocks = unsigned((n * 32 + 255) / 256);
     if (mixed)
@@ -2288,6 +2293,7 @@ extern "C" KORG_API int korg_line_absorption_noalloc(double* alpha, const double
     ta.wl = ln.wl;
     ta.params = po.params;
     ta.params_w = po.params_w;
+    ta.xcub = po.xcub;
     ta.lb = po.lb;
     ta.ub = po.ub;
     ta.tier_idx = tl.idx;

@@ -79,8 +79,10 @@ struct PrepOut {
     int32_t Lp, K, G;
     unsigned long long* evals;   // running totals: evaluations, lines in window
     unsigned long long* nlines;
-    float4* params_w;        // [n][Lp] mixed, or null: wing constants ({A1, A2, A3, -cref} for an
-                             //   asymptotic-branch layer, the packed constants for a far-Lorentz one)
+    float4* params_w;        // [n][Lp] mixed, or null: wing cubic {A1, A2, A3, 0} in t' = cref / dl^2
+                             //   (cref = 2 sigma^2 of layer 0), valid beyond the layer's cubic boundary
+    float* xcub;             // [n][G] mixed, or null: |wl - wl0| beyond which every layer of group g
+                             //   is given by its wing cubic to FP32 rounding
 };
 
 // Per-line quantities shared by every layer (line_absorption.jl:83,101,105,219).
@@ -241,6 +243,20 @@ __device__ __forceinline__ void argmax_reduce(float& v, int& idx) {
     }
 }
 
+// Distance (in units of gamma) beyond which the far-Lorentz branch of voigt_hjerting
+// (line_absorption.jl:305-308) equals its cubic series in w = 1/r^2 = gamma^2/dl^2 to FP32
+// rounding.  With q = 1/(sqrt2 a) and u = 1/(1 + r^2) the branch is
+//   H = sqrt(2/pi) q u (1 + (3 r^2 - 1 + (15 r^4 - 30 r^2 + 2) q^2 u^2) q^2 u^2)
+//     = sqrt(2/pi) [q w + (3q^3 - q) w^2 + (q - 10q^3 + 15q^5) w^3 + (-q + 21q^3 - 105q^5) w^4 + ...]
+// (u = w - w^2 + w^3 - ...), so the cubic's relative error is about C4 w^3 with
+// C4 = |-1 + 21 q^2 - 105 q^4|; w^3 C4 <= 2^-26 gives r >= (2^26 C4)^(1/6).  C4 is clamped at 1
+// so that the next term stays negligible near its root (a ~ 2).
+__device__ __forceinline__ float far_lorentz_cubic_rmin(float a) {
+    const float q2 = 0.5f / (a * a);
+    const float C4 = fmaxf(fabsf(fmaf(fmaf(-105.f, q2, 21.f), q2, -1.f)), 1.f);
+    return powf(67108864.f * C4, 1.f / 6.f);
+}
+
 // Mixed-precision prologue.  sigma, gamma and the profile constants are FP32; the line
 // strength (Boltzmann factor, 10^loggf sigma_line, n/U) is FP64 (line_absorption.jl:101-106).
 // The window is the FP64 window of the reference rule: FP32 locates the layers with the widest
@@ -266,7 +282,7 @@ __global__ void __launch_bounds__(32 * PREP_WARPS) line_prep_mixed_kernel(LinesD
                                                                           const MathTables* math) {
     __shared__ MathTables s_math;
     __shared__ LinePrep32 s_line[PREP_WARPS][32];
-    extern __shared__ float s_dyn[];  // [warps][Lp] boundaries, then [warps][Lp] class flags
+    extern __shared__ float s_dyn[];  // [warps][Lp] boundaries, [warps][Lp] class flags, [warps][Lp] cubic boundaries
     load_math_tables(s_math, math);
     __syncthreads();
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -276,6 +292,7 @@ __global__ void __launch_bounds__(32 * PREP_WARPS) line_prep_mixed_kernel(LinesD
     const int L = lay.L, Lp = out.Lp;
     float* s_bnd = s_dyn + wib * Lp;
     int* s_cls = reinterpret_cast<int*>(s_dyn + PREP_WARPS * Lp) + wib * Lp;
+    float* s_cub = s_dyn + 2 * PREP_WARPS * Lp + wib * Lp;
     // phase A: one lane per line
     KnotPos kp_mine{0, 0.0};
     if (lane < nl) {
@@ -352,25 +369,37 @@ __global__ void __launch_bounds__(32 * PREP_WARPS) line_prep_mixed_kernel(LinesD
                 // v >= 5 (a <= 0.2) or a + v >= 3.2 (0.2 < a <= 1.4) or any v (a > 1.4), v = x / sqrt(c)
                 s_bnd[l] = (A ? 5.f : (a <= 1.4f ? 3.2f - a : 0.f)) * sqrtf(p.x) * 1.0001f;
                 s_cls[l] = A;
+                // the layer's cubic boundary: the asymptotic branch is exactly a cubic in 1/v^2; the
+                // far-Lorentz branch is one beyond r_min gamma (far_lorentz_cubic_rmin)
+                s_cub[l] = A ? s_bnd[l] : fmaxf(s_bnd[l], far_lorentz_cubic_rmin(a) * gamma * 1.0001f);
             } else if (l < Lp) {
                 s_bnd[l] = 0.f;
                 s_cls[l] = 1;
+                s_cub[l] = 0.f;
             }
             if (l0 == 0) cref = __shfl_sync(0xffffffffu, p.x, 0);  // 2 sigma^2 of layer 0
             if (l < Lp) {
                 dst[l] = p;
                 if (dstw) {
-                    // wing constants: a layer in the asymptotic branch as a cubic in t' = cref / dl^2,
-                    // w u (1 + 1.5 u + 3.75 u^2) = A1 t' + A2 t'^2 + A3 t'^3 with u = 1/v^2 = (c / cref) t',
-                    // marked by .w = -cref; a far-Lorentz layer as {1/gamma^2, 1/(sqrt2 a), 0,
-                    // sqrt(2/pi) scale} (.w >= 0), see far_lorentz32w
-                    float4 pw = make_float4(p.z, 0.70710678118654752f / p.y, 0.f, 0.7978845608028654f * p.w);
-                    if (A) {
-                        const float rr = p.x / cref;
-                        pw.x = p.z * rr;
-                        pw.y = 1.5f * pw.x * rr;
-                        pw.z = 2.5f * pw.y * rr;
-                        pw.w = -cref;
+                    // wing cubic in t' = cref / dl^2: A1 t' + A2 t'^2 + A3 t'^3.  Asymptotic branch:
+                    // w u (1 + 1.5 u + 3.75 u^2) with u = 1/v^2 = (c / cref) t'.  Far-Lorentz branch:
+                    // sqrt(2/pi) scale [q w + (3q^3 - q) w^2 + (q - 10q^3 + 15q^5) w^3] with
+                    // w = gamma^2 / dl^2 = (gamma^2 / cref) t' (see far_lorentz_cubic_rmin).
+                    float4 pw = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (l < L) {
+                        if (A) {
+                            const float rr = p.x / cref;
+                            pw.x = p.z * rr;
+                            pw.y = 1.5f * pw.x * rr;
+                            pw.z = 2.5f * pw.y * rr;
+                        } else {
+                            const float q = 0.70710678118654752f / p.y, q2 = q * q;
+                            const float kap = (1.f / p.z) / cref;  // gamma^2 / cref
+                            const float k0 = 0.7978845608028654f * p.w;
+                            pw.x = k0 * q * kap;
+                            pw.y = k0 * q * fmaf(3.f, q2, -1.f) * kap * kap;
+                            pw.z = k0 * q * fmaf(fmaf(15.f, q2, -10.f), q2, 1.f) * kap * kap * kap;
+                        }
                     }
                     dstw[l] = pw;
                 }
@@ -380,7 +409,12 @@ __global__ void __launch_bounds__(32 * PREP_WARPS) line_prep_mixed_kernel(LinesD
         argmax_reduce(dmax, dl);
         argmax_reduce(lmax, ll);
         group_bounds(out, i, s_bnd, s_cls, lane);
-        __syncwarp();  // s_bnd / s_cls are rewritten by the next line
+        if (out.xcub && lane < out.G) {
+            float mx = 0.f;
+            for (int k = 0; k < out.K; k++) mx = fmaxf(mx, s_cub[lane * out.K + k]);
+            out.xcub[i * out.G + lane] = mx;
+        }
+        __syncwarp();  // s_bnd / s_cls / s_cub are rewritten by the next line
         if (lane == t) { my_dl = dl; my_ll = ll; }
     }
     // phase C: the exact FP64 window of each line at its two widest layers, one lane per line
@@ -395,7 +429,7 @@ __global__ void __launch_bounds__(32 * PREP_WARPS) line_prep_mixed_kernel(LinesD
 
 // Launch geometry of line_prep_mixed_kernel for n lines.
 inline unsigned prep_mixed_blocks(int64_t n) { return unsigned((n + 32 * PREP_WARPS - 1) / (32 * PREP_WARPS)); }
-inline size_t prep_mixed_smem(int Lp) { return size_t(PREP_WARPS) * Lp * (sizeof(float) + sizeof(int)); }
+inline size_t prep_mixed_smem(int Lp) { return size_t(PREP_WARPS) * Lp * (2 * sizeof(float) + sizeof(int)); }
 
 // Candidate lists.  Lines are split by window half-width into tiers (at most 256, 4096, 65536
 // wavelength points, and wider).  Within a tier the lines keep list order, so their centre
@@ -514,7 +548,8 @@ struct TileArgs {
     const uint32_t* amask;
     const int32_t *lb, *ub;
     const int32_t *tier_idx, *tier_ci, *tier_start, *unsorted;
-    const float4* params_w;   // mixed, or null: wing constants (see PrepOut)
+    const float4* params_w;   // mixed, or null: wing cubics (see PrepOut)
+    const float* xcub;        // mixed, or null: cubic boundaries (see PrepOut)
 };
 
 // first index in [lo, hi) with a[i] >= v (a non-decreasing)
@@ -539,9 +574,10 @@ struct LineStage {
     double wl;        // centre (FP64 path)
     float dhi, dlo;   // centre - first wavelength of the tile, as an FP32 pair (mixed path)
     int32_t lb, ub;
-    uint32_t cls;     // 2 bits per layer group: 1 = pure asymptotic wing, 2 = wing branches, 0 = general
+    uint32_t cls;     // 2 bits per layer group: 1 = every layer given by its wing cubic (mixed),
+                      // 2 = every layer in a closed-form wing branch, 0 = general
     int32_t li;       // line index
-    float cref;       // scale of the wing coefficients (mixed, split tiles)
+    float cref;       // scale of the wing cubics' variable t' = cref / dl^2 (mixed)
 };
 
 __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
@@ -558,15 +594,6 @@ __device__ __forceinline__ float far_lorentz32(float4 p, float x2) {
     const float au2 = au * au;
     return 0.7978845608028654f * au * (1.f + (3.f * r2 - 1.f + ((r2 - 2.f) * 15.f * r2 + 2.f) * au2) * au2) * p.w;
 }
-// The same from the wing constants {1/gamma^2, 1/(sqrt2 a), -, sqrt(2/pi) scale}, accumulated:
-// au = 1/(sqrt2 a (1 + r^2)), H scale = sqrt(2/pi) scale au (1 + (3r^2 - 1 + (15r^4 - 30r^2 + 2) au^2) au^2).
-__device__ __forceinline__ float far_lorentz32w(float4 p, float x2, float acc) {
-    const float r2 = x2 * p.x;
-    const float au = __fdividef(p.y, r2 + 1.f);
-    const float au2 = au * au;
-    const float poly = fmaf(fmaf(fmaf(fmaf(15.f, r2, -30.f), r2, 2.f), au2, fmaf(3.f, r2, -1.f)), au2, 1.f);
-    return fmaf(au * p.w, poly, acc);
-}
 __device__ __forceinline__ double far_lorentz64(const P64& p, double x2) {
     const double r2 = x2 * p.w;
     const double au = 1 / SQRT_2 / ((r2 + 1) * p.a);
@@ -577,8 +604,9 @@ __device__ __forceinline__ double far_lorentz64(const P64& p, double x2) {
 // One tile of TW = blockDim.x / G wavelengths x all layers, computed by one CTA.  Thread (j, g)
 // owns wavelength j and the K consecutive (padded) layers g*K .. g*K+K-1.  `smem` is the
 // dynamic shared memory of the launch (two line-constant buffers, then the LineStage array).
-// In the mixed split form a line whose layers of the group are all in wing branches over the
-// tile is staged as its wing constants: three FMAs per asymptotic-branch evaluation.
+// In the mixed form a line whose layers of the group are all in their cubic regime over the
+// tile (asymptotic branch, or far-Lorentz branch far enough out) is staged as its wing cubics:
+// three FMAs per evaluation.
 template <bool MIXED, int K>
 __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, int gsplit, unsigned char* smem) {
     using P = typename ParamT<MIXED>::type;
@@ -631,7 +659,7 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
 
     const int warp = tid >> 5, lane = tid & 31, nwarps = nthr >> 5;
     const int chunks16 = SL * int(sizeof(P) / 16);  // 16-byte pieces of one line's staged constants
-    const bool wcoef = MIXED && gsplit >= 0 && a.params_w != nullptr;
+    const bool wcoef = MIXED && a.params_w != nullptr && a.xcub != nullptr;
     const int cb0 = tid / chunks16, cr0 = tid - cb0 * chunks16;       // this thread's first staged piece
     const int cdb = nthr / chunks16, cdr = nthr - cdb * chunks16;     // and the step between its pieces
     const int64_t src0 = gsplit >= 0 ? int64_t(g) * K * int64_t(sizeof(P) / 16) : 0;
@@ -665,12 +693,18 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
             const float fdist = dh < 0.f ? -dh : (dh > span32 ? dh - span32 : 0.f);
             const double dist = MIXED ? double(fdist)
                                       : (wl0 < wl_ref ? wl_ref - wl0 : (wl0 > wl_last ? wl0 - wl_last : 0.0));
-            const uint32_t am = a.amask[i];
             uint32_t cls = 0;
             const int g_lo = gsplit >= 0 ? gsplit : 0, g_hi = gsplit >= 0 ? gsplit + 1 : G;
             for (int gg = g_lo; gg < g_hi; gg++) {
                 const float xf = a.xfar[i * G + gg];
-                if (MIXED ? fdist > xf : dist > double(xf)) cls |= (((am >> gg) & 1u) ? 1u : 2u) << (2 * gg);
+                uint32_t c = 0u;
+                if (MIXED) {
+                    if (wcoef && fdist > a.xcub[i * G + gg]) c = 1u;
+                    else if (fdist > xf) c = 2u;
+                } else if (dist > double(xf)) {
+                    c = 2u;
+                }
+                cls |= c << (2 * gg);
             }
             st.wl = wl0;
             st.dhi = dh;
@@ -679,7 +713,7 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
             st.ub = ubi;
             st.cls = cls;
             st.li = int32_t(i);
-            st.cref = wcoef ? reinterpret_cast<const float4*>(a.params)[i * Lp].x : 0.f;  // 2 sigma^2, layer 0
+            st.cref = MIXED ? reinterpret_cast<const float4*>(a.params)[i * Lp].x : 0.f;  // 2 sigma^2, layer 0
             s_ln[s_warp[warp] + __popc(m & ((1u << lane) - 1))] = st;
         }
         const int cnt = s_count;
@@ -697,8 +731,10 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
                 for (int e = tid; e < nb * chunks16; e += nthr) {
                     const LineStage& sl = s_ln[b0 + b];
                     const int64_t li = sl.li;
-                    const void* src = (wcoef && ((sl.cls >> (2 * g)) & 3u) != 0u) ? static_cast<const void*>(a.params_w)
-                                                                                  : a.params;
+                    // mixed: one float4 per layer, so piece r is layer r of the staged line
+                    const int gp = gsplit >= 0 ? gsplit : r / K;
+                    const void* src = (wcoef && ((sl.cls >> (2 * gp)) & 3u) == 1u) ? static_cast<const void*>(a.params_w)
+                                                                                   : a.params;
                     cp_async16(buf + (size_t(b) * chunks16 + r) * 16,
                                reinterpret_cast<const unsigned char*>(src) +
                                    (li * Lp * int64_t(sizeof(P) / 16) + src0 + r) * 16);
@@ -732,32 +768,13 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
                         const float t = __fdividef(1.f, x2);
                         const float4* pr = reinterpret_cast<const float4*>(s_par) + b * SL + goff;
                         const uint32_t cls = (st.cls >> (2 * g)) & 3u;
-                        if (cls == 1u && wcoef) {
-                            // every layer in the asymptotic wing, staged as A1 t' + A2 t'^2 + A3 t'^3
+                        if (cls == 1u) {
+                            // every layer in its cubic regime, staged as A1 t' + A2 t'^2 + A3 t'^3
                             const float tp = t * st.cref;
 #pragma unroll
                             for (int k = 0; k < K; k++) {
                                 const float4 p = pr[k];
                                 part[k] = fmaf(tp, fmaf(tp, fmaf(tp, p.z, p.y), p.x), part[k]);
-                            }
-                        } else if (cls == 1u) {
-                            // every layer in the asymptotic wing: w/v^2 (1 + 1.5/v^2 + 3.75/v^4), 1/v^2 = c t
-#pragma unroll
-                            for (int k = 0; k < K; k++) {
-                                const float4 p = pr[k];
-                                const float iv = t * p.x;
-                                part[k] = fmaf(p.z * iv, fmaf(fmaf(3.75f, iv, 1.5f), iv, 1.f), part[k]);
-                            }
-                        } else if (cls == 2u && wcoef) {
-                            // every layer in a wing branch: the asymptotic cubic (.w < 0) or far Lorentz
-                            const float tp = t * st.cref;
-#pragma unroll
-                            for (int k = 0; k < K; k++) {
-                                const float4 p = pr[k];
-                                if (p.w < 0.f)
-                                    part[k] = fmaf(tp, fmaf(tp, fmaf(tp, p.z, p.y), p.x), part[k]);
-                                else
-                                    part[k] = far_lorentz32w(p, x2, part[k]);
                             }
                         } else if (cls == 2u) {
                             // every layer in a wing branch, chosen per layer (uniform across the warp)

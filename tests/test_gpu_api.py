@@ -94,8 +94,8 @@ def test_precision_must_be_fp64_or_mixed(ctx):
                                           _lib._p(keep.f64(inp.wls.all_wls)), nwl, C.byref(l1), C.byref(s.layers),
                                           C.byref(s.cntm), 3e-4, prec, None)
         assert rc == 1
-    t = (C.c_int32 * 4)()
-    assert ctx.lib.korg_get_tile_config(ctx.h, 56, 2, t, C.byref(t, 4), None, None) == 1
+    tw, stage = C.c_int32(), C.c_int32()
+    assert ctx.lib.korg_get_tile_config(ctx.h, 56, 2, C.byref(tw), C.byref(stage), None, None) == 1
 
 
 def test_full_optical_fp64_against_oracle(ctx, oracle_lib):
