@@ -343,7 +343,8 @@ KORG_API int korg_set_batch_options(korg_ctx *ctx, int use_graph, int autotune,
 /* The tile shape the context uses for (L, precision): wavelengths per CTA, lines per shared
  * memory batch, whether each CTA takes a single layer group (split), and whether it came from
  * the autotuner (split and tuned may be NULL).  korg_set_tile_config fixes the shape instead
- * (counts as tuned).  No counterpart in the reference. */
+ * (counts as tuned); KORG_MIXED shapes always take one layer group per CTA (split = 0 is
+ * KORG_EINVAL).  No counterpart in the reference. */
 KORG_API int korg_get_tile_config(korg_ctx *ctx, int32_t L, int precision, int32_t *tw,
                                   int32_t *stage, int32_t *split, int32_t *tuned);
 KORG_API int korg_set_tile_config(korg_ctx *ctx, int32_t L, int precision, int32_t tw,

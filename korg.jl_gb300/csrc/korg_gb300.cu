@@ -299,12 +299,16 @@ struct TileGeom {
     size_t smem;
 };
 
+// One wavelength per thread; the mixed form always takes one layer group per CTA, the FP64 form
+// one or all layer groups.
 bool tile_geom(bool mixed, int Lp, int G, TileCfg c, TileGeom* g) {
     const size_t psz = mixed ? sizeof(float4) : sizeof(P64);
-    const int B = c.stage > 0 ? c.stage : (mixed ? STAGE_LINES : STAGE_LINES / 2);
+    const int B = c.stage > 0 ? c.stage : (mixed ? 2 * STAGE_LINES : STAGE_LINES / 2);
+    if (mixed && !c.split) return false;
     const int Gc = c.split ? 1 : G;  // layer groups per CTA
     const int SL = c.split ? Lp / G : Lp;
-    if (c.tw < 32 || c.tw % 32 != 0 || c.tw * Gc > 512 || B < 1) return false;
+    const int maxt = mixed ? 256 : 512;
+    if (c.tw < 32 || c.tw % 32 != 0 || c.tw * Gc > maxt || B < 1) return false;
     size_t region = size_t(B) * SL * psz;
     region = std::max(region, (size_t(c.tw) * (SL + 1) * sizeof(double) + 1) / 2);
     region = (region + 15) & ~size_t(15);
@@ -314,9 +318,12 @@ bool tile_geom(bool mixed, int Lp, int G, TileCfg c, TileGeom* g) {
     g->region = int(region);
     g->split = c.split ? 1 : 0;
     g->G = G;
-    g->smem = 2 * region + size_t(g->threads) * sizeof(LineStage);
+    g->smem = 2 * region + size_t(g->threads) * (mixed ? sizeof(LineStage32) : sizeof(LineStage));
     return g->smem <= 227 * 1024;
 }
+
+// Default tile shape: 128 wavelengths x one layer group (mixed: 64-line batches, FP64: 16).
+TileCfg default_tile(bool) { return TileCfg{TILE_TW, 0, 1}; }
 
 template <bool MIXED, int KMAX, int MAXT, int MINB>
 int launch_tile(korg_ctx* ctx, TileArgs ta, const TileGeom& g, const TileQueue* q, cudaStream_t s) {
@@ -343,10 +350,16 @@ int launch_tile(korg_ctx* ctx, TileArgs ta, const TileGeom& g, const TileQueue* 
 template <bool MIXED>
 int dispatch_tile(korg_ctx* ctx, const TileArgs& ta, int kmax, const TileGeom& g, const TileQueue* q,
                   cudaStream_t s) {
-    if (kmax == 14 && g.threads <= 256) return launch_tile<MIXED, 14, 256, MIXED ? 3 : 2>(ctx, ta, g, q, s);
-    if (kmax == 14) return launch_tile<MIXED, 14, 512, 1>(ctx, ta, g, q, s);
-    if (kmax == 16) return launch_tile<MIXED, 16, 512, 1>(ctx, ta, g, q, s);
-    return launch_tile<MIXED, 32, 512, 1>(ctx, ta, g, q, s);
+    if constexpr (MIXED) {  // at most 256 threads (one layer group per CTA)
+        if (kmax == 14) return launch_tile<true, 14, 256, 3>(ctx, ta, g, q, s);
+        if (kmax == 16) return launch_tile<true, 16, 256, 2>(ctx, ta, g, q, s);
+        return launch_tile<true, 32, 256, 2>(ctx, ta, g, q, s);
+    } else {
+        if (kmax == 14 && g.threads <= 256) return launch_tile<false, 14, 256, 2>(ctx, ta, g, q, s);
+        if (kmax == 14) return launch_tile<false, 14, 512, 1>(ctx, ta, g, q, s);
+        if (kmax == 16) return launch_tile<false, 16, 512, 1>(ctx, ta, g, q, s);
+        return launch_tile<false, 32, 512, 1>(ctx, ta, g, q, s);
+    }
 }
 
 int run_tiles(korg_ctx* ctx, const TileArgs& ta, int kmax, const TileGeom& g, const TileQueue* q, bool mixed,
@@ -357,12 +370,13 @@ int run_tiles(korg_ctx* ctx, const TileArgs& ta, int kmax, const TileGeom& g, co
 // The tile shape for (L, precision): the autotuned one when there is one, else the default.
 TileCfg tile_cfg(const korg_ctx* ctx, int L, bool mixed) {
     auto it = ctx->tuned.find(std::make_pair(L, int(mixed)));
-    return it != ctx->tuned.end() ? it->second : TileCfg{TILE_TW, 0, 1};  // one layer group per CTA
+    return it != ctx->tuned.end() ? it->second : default_tile(mixed);
 }
 
-// Autotuner: times every candidate shape (TW in {32, 64, 128} x stage in {B/2, B}) on the real
-// candidate lists of one spectrum, writing into a scratch alpha, and keeps the fastest for
-// (L, precision).  Runs once per (L, precision) per context, outside any stream capture.
+// Autotuner: times every candidate shape (FP64: TW in {32, 64, 128} x stage in {8, 16} x split
+// or not; mixed: TW in {64, 128, 256} x stage in {32, 64}, split) on the real candidate lists of
+// one spectrum, writing into a scratch alpha, and keeps the fastest for (L, precision).  Runs
+// once per (L, precision) per context, outside any stream capture.
 int autotune_tiles(korg_ctx* ctx, const TileArgs& ta0, int kmax, bool mixed, cudaStream_t s) {
     const int L = ta0.L, Lp = ta0.Lp, G = ta0.G;
     const auto key = std::make_pair(L, int(mixed));
@@ -371,12 +385,13 @@ int autotune_tiles(korg_ctx* ctx, const TileArgs& ta0, int kmax, bool mixed, cud
     KCUDA(cudaMemsetAsync(ctx->tune_alpha.p, 0, sizeof(double) * size_t(L) * ta0.nwl, s));
     TileArgs ta = ta0;
     ta.alpha = static_cast<double*>(ctx->tune_alpha.p);
-    const int B0 = mixed ? STAGE_LINES : STAGE_LINES / 2;
-    TileCfg best{TILE_TW, 0, 0};
+    const int B0 = mixed ? 2 * STAGE_LINES : STAGE_LINES / 2;
+    TileCfg best = default_tile(mixed);
     float best_ms = 1e30f;
     for (int split : {0, 1})
-    for (int tw : {64, 32, 128})
+    for (int tw : {64, 32, 128, 256, 512})
         for (int B : {B0, B0 / 2}) {
+            if (mixed ? (tw < 64 || !split) : tw > 128) continue;
             TileGeom g;
             if (!tile_geom(mixed, Lp, G, TileCfg{tw, B, split}, &g)) continue;
             float t = 1e30f;
@@ -1927,7 +1942,7 @@ KORG_API int korg_get_tile_config(korg_ctx* ctx, int32_t L, int precision, int32
     const bool mixed = precision == KORG_MIXED;
     const TileCfg c = tile_cfg(ctx, L, mixed);
     *tw = c.tw;
-    *stage = c.stage > 0 ? c.stage : (mixed ? STAGE_LINES : STAGE_LINES / 2);
+    *stage = c.stage > 0 ? c.stage : (mixed ? 2 * STAGE_LINES : STAGE_LINES / 2);
     if (split) *split = c.split;
     if (tuned) *tuned = ctx->tuned.count(std::make_pair(int(L), int(mixed))) ? 1 : 0;
     return KORG_OK;
@@ -2192,29 +2207,31 @@ int noalloc_setup(unsigned char** out) {
     return KORG_OK;
 }
 
-// The context's default tile shape (TILE_TW wavelengths, one layer group per CTA), so results
-// equal korg_line_absorption_dev's.
-template <bool MIXED, int KMAX, int MAXT, int MINB>
-int noalloc_launch_tile(TileArgs ta, int G, cudaStream_t s) {
+// The context's default tile shape and the same kernel instances as korg_line_absorption_dev,
+// so results are bitwise equal.  (No context: the tile kernel is launched directly.)
+int noalloc_tiles(const TileArgs& ta, int G, int kmax, bool mixed, cudaStream_t s) {
     TileGeom g;
-    if (!tile_geom(MIXED, ta.Lp, G, TileCfg{TILE_TW, 0, 1}, &g)) return KORG_EINVAL;
-    ta.stage = g.stage;
-    ta.region = g.region;
-    ta.split = g.split;
-    ta.G = G;
-    auto kern = line_tile_kernel<MIXED, KMAX, MAXT, MINB>;
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g.smem)) != cudaSuccess)
-        return KORG_ECUDA;
-    kern<<<dim3(unsigned((ta.nwl + g.tw - 1) / g.tw), unsigned(G)), g.threads, g.smem, s>>>(ta);
-    return cudaGetLastError() == cudaSuccess ? KORG_OK : KORG_ECUDA;
-}
-
-template <bool MIXED>
-int noalloc_dispatch_tile(const TileArgs& ta, int G, int kmax, cudaStream_t s) {
-    // one layer group per CTA: TILE_TW threads, the variant run_tiles picks for that count
-    if (kmax == 14) return noalloc_launch_tile<MIXED, 14, 256, MIXED ? 3 : 2>(ta, G, s);
-    if (kmax == 16) return noalloc_launch_tile<MIXED, 16, 512, 1>(ta, G, s);
-    return noalloc_launch_tile<MIXED, 32, 512, 1>(ta, G, s);
+    if (!tile_geom(mixed, ta.Lp, G, default_tile(mixed), &g)) return KORG_EINVAL;
+    TileArgs t = ta;
+    t.stage = g.stage;
+    t.region = g.region;
+    t.split = g.split;
+    t.G = G;
+    const dim3 grid(unsigned((ta.nwl + g.tw - 1) / g.tw), unsigned(G));
+    auto go = [&](auto kern) {
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g.smem)) != cudaSuccess)
+            return KORG_ECUDA;
+        kern<<<grid, g.threads, g.smem, s>>>(t);
+        return cudaGetLastError() == cudaSuccess ? KORG_OK : KORG_ECUDA;
+    };
+    if (mixed) {
+        if (kmax == 14) return go(line_tile_kernel<true, 14, 256, 3>);
+        if (kmax == 16) return go(line_tile_kernel<true, 16, 256, 2>);
+        return go(line_tile_kernel<true, 32, 256, 2>);
+    }
+    if (kmax == 14) return go(line_tile_kernel<false, 14, 256, 2>);  // TILE_TW threads, one group
+    if (kmax == 16) return go(line_tile_kernel<false, 16, 512, 1>);
+    return go(line_tile_kernel<false, 32, 512, 1>);
 }
 
 }  // namespace
@@ -2300,5 +2317,5 @@ extern "C" KORG_API int korg_line_absorption_noalloc(double* alpha, const double
     ta.tier_ci = tl.ci;
     ta.tier_start = tl.start;
     ta.unsorted = tl.unsorted;
-    return mixed ? noalloc_dispatch_tile<true>(ta, G, kmax, s) : noalloc_dispatch_tile<false>(ta, G, kmax, s);
+    return noalloc_tiles(ta, G, kmax, mixed, s);
 }

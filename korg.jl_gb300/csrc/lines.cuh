@@ -1,18 +1,19 @@
-// lines.cuh -- line opacity: per-(line, layer) prologue, window scans and the wavelength-tile
-// accumulation kernel.  Restates line_absorption! (src/line_absorption.jl:33-129).
+// lines.cuh -- line opacity: per-(line, layer) prologue, width-tier candidate lists and the
+// wavelength-tile accumulation kernels.  Restates line_absorption! (src/line_absorption.jl:33-129).
 //
 // Work decomposition
-//   prep:  one warp per line, lanes over layers.  Computes sigma, gamma, amplitude, the
-//          continuum-cutoff window (line_absorption.jl:86-119), the packed profile constants and,
-//          per group of K layers, the distance from the line centre beyond which every layer of
-//          the group is in a closed-form wing branch of the Hjerting approximation.
-//   scan:  running max of ub (prefix) and running min of lb (suffix) over the sorted lines, so
-//          a wavelength tile finds its candidate lines with two binary searches.
-//   tile:  one CTA per tile of TW wavelengths x all layers.  Thread (j, g) owns wavelength j and
-//          the K consecutive layers of group g; alpha accumulates in registers (FP64, or FP32 with
-//          Kahan compensation).  Lines are visited in list order (deterministic, no atomics on
-//          alpha); each chunk of candidates is compacted with warp ballots, and the constants of
-//          32-line batches are copied to shared memory with cp.async, double buffered.
+//   prep:  per-(line, layer) constants, the continuum-cutoff window (line_absorption.jl:86-119)
+//          and, per group of K layers, the distances from the line centre beyond which every
+//          layer of the group is in a closed-form wing branch of the Hjerting approximation and
+//          (mixed) in its cubic regime, where the branch is a cubic in t' = cref / dl^2.
+//   tiers: line indices partitioned by window half-width, each tier ordered by centre, so a
+//          wavelength tile finds its candidate lines with two binary searches per tier.
+//   tile:  one CTA per tile of wavelengths x one layer group (or, FP64, all groups).  Each thread
+//          owns one (FP64) or two (mixed) wavelengths and the K consecutive layers of its group;
+//          alpha accumulates in registers (FP64, or FP32 batch sums with Kahan compensation).
+//          Lines are visited in list order (deterministic, no atomics on alpha); each chunk of
+//          candidates is compacted with warp ballots, and the constants of each batch of lines
+//          are copied to shared memory with cp.async, double buffered.
 #pragma once
 #include "physics.cuh"
 
@@ -529,11 +530,6 @@ __global__ void __launch_bounds__(PART_THREADS) tier_scatter_kernel(const int32_
     }
 }
 
-template <bool MIXED>
-struct ParamT { using type = P64; };
-template <>
-struct ParamT<true> { using type = float4; };
-
 struct TileArgs {
     double* alpha;        // [nwl][L]
     const double* wls;
@@ -569,15 +565,12 @@ __device__ __forceinline__ int64_t upper_bound_i32(const int32_t* a, int64_t lo,
     return lo;
 }
 
-// A candidate line of the current chunk, as the tile sees it.
+// A candidate line of the current chunk, as an FP64 tile sees it.
 struct LineStage {
-    double wl;        // centre (FP64 path)
-    float dhi, dlo;   // centre - first wavelength of the tile, as an FP32 pair (mixed path)
-    int32_t lb, ub;
-    uint32_t cls;     // 2 bits per layer group: 1 = every layer given by its wing cubic (mixed),
-                      // 2 = every layer in a closed-form wing branch, 0 = general
+    double wl;        // centre
+    int32_t lb, ub;   // window (grid indices)
+    uint32_t cls;     // 2 bits per layer group: 2 = every layer in a closed-form wing branch, 0 = general
     int32_t li;       // line index
-    float cref;       // scale of the wing cubics' variable t' = cref / dl^2 (mixed)
 };
 
 __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
@@ -601,15 +594,12 @@ __device__ __forceinline__ double far_lorentz64(const P64& p, double x2) {
     return 0.7978845608028654 * au * (1 + (3 * r2 - 1 + ((r2 - 2) * 15 * r2 + 2) * au2) * au2) * p.scale;
 }
 
-// One tile of TW = blockDim.x / G wavelengths x all layers, computed by one CTA.  Thread (j, g)
-// owns wavelength j and the K consecutive (padded) layers g*K .. g*K+K-1.  `smem` is the
-// dynamic shared memory of the launch (two line-constant buffers, then the LineStage array).
-// In the mixed form a line whose layers of the group are all in their cubic regime over the
-// tile (asymptotic branch, or far-Lorentz branch far enough out) is staged as its wing cubics:
-// three FMAs per evaluation.
-template <bool MIXED, int K>
-__device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, int gsplit, unsigned char* smem) {
-    using P = typename ParamT<MIXED>::type;
+// FP64 tile: TW = blockDim.x / G wavelengths x all layers (or, with gsplit >= 0, x the layers of
+// group gsplit), computed by one CTA.  Thread (j, g) owns wavelength j and the K consecutive
+// (padded) layers g*K .. g*K+K-1, accumulated in FP64 registers.  `smem` is the dynamic shared
+// memory of the launch (two line-constant buffers, then the LineStage array).
+template <int K>
+__device__ __forceinline__ void line_tile_body64(const TileArgs& a, int64_t tile, int gsplit, unsigned char* smem) {
     const int L = a.L, Lp = a.Lp, G = a.G, B = a.stage;
     double* s_alpha = reinterpret_cast<double*>(smem);                          // [TW][SL+1], at the end
     LineStage* s_ln = reinterpret_cast<LineStage*>(smem + 2 * size_t(a.region));  // [blockDim]
@@ -629,11 +619,6 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
     const bool live = jg < a.nwl;
     const double wl_j = live ? a.wls[jg] : 0.0;
     const double wl_ref = a.wls[j0], wl_last = a.wls[jlast];
-    const float span32 = float(wl_last - wl_ref);
-    // mixed precision: offsets from the tile's first wavelength formed in FP64 and kept as
-    // FP32 hi + lo pairs, so |wl_j - wl0| is recovered in FP32 to about one rounding
-    const float xj_hi = float(wl_j - wl_ref);
-    const float xj_lo = float((wl_j - wl_ref) - double(xj_hi));
 
     // candidate runs of the width tiers (threads 0..NTIER-1 search one tier each)
     __shared__ int64_t s_tier[NTIER][2];
@@ -652,17 +637,15 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
     }
     __syncthreads();
 
-    using Acc = typename std::conditional<MIXED, float, double>::type;
-    Acc acc[K], comp[K];
+    double acc[K];
 #pragma unroll
-    for (int k = 0; k < K; k++) { acc[k] = Acc(0); comp[k] = Acc(0); }
+    for (int k = 0; k < K; k++) acc[k] = 0.0;
 
     const int warp = tid >> 5, lane = tid & 31, nwarps = nthr >> 5;
-    const int chunks16 = SL * int(sizeof(P) / 16);  // 16-byte pieces of one line's staged constants
-    const bool wcoef = MIXED && a.params_w != nullptr && a.xcub != nullptr;
+    const int chunks16 = SL * int(sizeof(P64) / 16);  // 16-byte pieces of one line's staged constants
     const int cb0 = tid / chunks16, cr0 = tid - cb0 * chunks16;       // this thread's first staged piece
     const int cdb = nthr / chunks16, cdr = nthr - cdb * chunks16;     // and the step between its pieces
-    const int64_t src0 = gsplit >= 0 ? int64_t(g) * K * int64_t(sizeof(P) / 16) : 0;
+    const int64_t src0 = gsplit >= 0 ? int64_t(g) * K * int64_t(sizeof(P64) / 16) : 0;
     for (int tier = 0; tier < NTIER; tier++)
     for (int64_t base = s_tier[tier][0]; base < s_tier[tier][1]; base += nthr) {
         const int64_t pidx = base + tid;
@@ -686,34 +669,17 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
         __syncthreads();
         if (take) {  // the thread that found the line describes it for the whole CTA
             LineStage st;
-            const double wl0 = a.wl[i], d = wl0 - wl_ref;
-            const float dh = float(d);
-            // distance of the centre from the tile; in FP32 for the mixed form (xfar carries a
-            // 1e-4 relative margin, far above the rounding), so only the offset itself is FP64
-            const float fdist = dh < 0.f ? -dh : (dh > span32 ? dh - span32 : 0.f);
-            const double dist = MIXED ? double(fdist)
-                                      : (wl0 < wl_ref ? wl_ref - wl0 : (wl0 > wl_last ? wl0 - wl_last : 0.0));
+            const double wl0 = a.wl[i];
+            const double dist = wl0 < wl_ref ? wl_ref - wl0 : (wl0 > wl_last ? wl0 - wl_last : 0.0);
             uint32_t cls = 0;
             const int g_lo = gsplit >= 0 ? gsplit : 0, g_hi = gsplit >= 0 ? gsplit + 1 : G;
-            for (int gg = g_lo; gg < g_hi; gg++) {
-                const float xf = a.xfar[i * G + gg];
-                uint32_t c = 0u;
-                if (MIXED) {
-                    if (wcoef && fdist > a.xcub[i * G + gg]) c = 1u;
-                    else if (fdist > xf) c = 2u;
-                } else if (dist > double(xf)) {
-                    c = 2u;
-                }
-                cls |= c << (2 * gg);
-            }
+            for (int gg = g_lo; gg < g_hi; gg++)
+                if (dist > double(a.xfar[i * G + gg])) cls |= 2u << (2 * gg);
             st.wl = wl0;
-            st.dhi = dh;
-            st.dlo = float(d - double(dh));
             st.lb = lbi;
             st.ub = ubi;
             st.cls = cls;
             st.li = int32_t(i);
-            st.cref = MIXED ? reinterpret_cast<const float4*>(a.params)[i * Lp].x : 0.f;  // 2 sigma^2, layer 0
             s_ln[s_warp[warp] + __popc(m & ((1u << lane) - 1))] = st;
         }
         const int cnt = s_count;
@@ -729,15 +695,10 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
                 // stepped without a division
                 int b = cb0, r = cr0;
                 for (int e = tid; e < nb * chunks16; e += nthr) {
-                    const LineStage& sl = s_ln[b0 + b];
-                    const int64_t li = sl.li;
-                    // mixed: one float4 per layer, so piece r is layer r of the staged line
-                    const int gp = gsplit >= 0 ? gsplit : r / K;
-                    const void* src = (wcoef && ((sl.cls >> (2 * gp)) & 3u) == 1u) ? static_cast<const void*>(a.params_w)
-                                                                                   : a.params;
+                    const int64_t li = s_ln[b0 + b].li;
                     cp_async16(buf + (size_t(b) * chunks16 + r) * 16,
-                               reinterpret_cast<const unsigned char*>(src) +
-                                   (li * Lp * int64_t(sizeof(P) / 16) + src0 + r) * 16);
+                               reinterpret_cast<const unsigned char*>(a.params) +
+                                   (li * Lp * int64_t(sizeof(P64) / 16) + src0 + r) * 16);
                     b += cdb;
                     r += cdr;
                     if (r >= chunks16) {
@@ -754,75 +715,27 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
             cp_async_wait_1();  // batch q has landed (this thread's copies) ...
             __syncthreads();    // ... and everybody else's
             const int b0 = q * B, nb = min(B, cnt - b0);
-            const P* s_par = reinterpret_cast<const P*>(smem + size_t(q & 1) * a.region);
+            const P64* s_par = reinterpret_cast<const P64*>(smem + size_t(q & 1) * a.region);
             if (live) {
-                if (MIXED) {
-                    float part[K];
+                for (int b = 0; b < nb; b++) {
+                    const LineStage& st = s_ln[b0 + b];
+                    if (jg < st.lb || jg > st.ub) continue;
+                    const double x = fabs(wl_j - st.wl);
+                    const P64* pr = s_par + b * SL + goff;
+                    if ((st.cls >> (2 * g)) & 3u) {
+                        const double x2 = x * x, t = 1 / x2;
 #pragma unroll
-                    for (int k = 0; k < K; k++) part[k] = 0.f;
-                    for (int b = 0; b < nb; b++) {
-                        const LineStage& st = s_ln[b0 + b];
-                        if (jg < st.lb || jg > st.ub) continue;
-                        const float x = fabsf((xj_hi - st.dhi) + (xj_lo - st.dlo));
-                        const float x2 = x * x;
-                        const float t = __fdividef(1.f, x2);
-                        const float4* pr = reinterpret_cast<const float4*>(s_par) + b * SL + goff;
-                        const uint32_t cls = (st.cls >> (2 * g)) & 3u;
-                        if (cls == 1u) {
-                            // every layer in its cubic regime, staged as A1 t' + A2 t'^2 + A3 t'^3
-                            const float tp = t * st.cref;
-#pragma unroll
-                            for (int k = 0; k < K; k++) {
-                                const float4 p = pr[k];
-                                part[k] = fmaf(tp, fmaf(tp, fmaf(tp, p.z, p.y), p.x), part[k]);
+                        for (int k = 0; k < K; k++) {
+                            if (pr[k].a <= 0.2) {
+                                const double iv = t * pr[k].c;
+                                acc[k] += (pr[k].w * iv) * (1 + iv * (1.5 + 3.75 * iv));
+                            } else {
+                                acc[k] += far_lorentz64(pr[k], x2);
                             }
-                        } else if (cls == 2u) {
-                            // every layer in a wing branch, chosen per layer (uniform across the warp)
-#pragma unroll
-                            for (int k = 0; k < K; k++) {
-                                const float4 p = pr[k];
-                                if (p.y <= 0.2f) {
-                                    const float iv = t * p.x;
-                                    part[k] = fmaf(p.z * iv, fmaf(fmaf(3.75f, iv, 1.5f), iv, 1.f), part[k]);
-                                } else {
-                                    part[k] += far_lorentz32(p, x2);
-                                }
-                            }
-                        } else {
-#pragma unroll
-                            for (int k = 0; k < K; k++) part[k] += profile32x(pr[k], x, t);
                         }
-                    }
-                    // batch partial sums enter the accumulators with Kahan compensation
+                    } else {
 #pragma unroll
-                    for (int k = 0; k < K; k++) {
-                        const float y = part[k] - float(comp[k]);
-                        const float tt = float(acc[k]) + y;
-                        comp[k] = Acc((tt - float(acc[k])) - y);
-                        acc[k] = Acc(tt);
-                    }
-                } else {
-                    for (int b = 0; b < nb; b++) {
-                        const LineStage& st = s_ln[b0 + b];
-                        if (jg < st.lb || jg > st.ub) continue;
-                        const double x = fabs(wl_j - st.wl);
-                        const P64* pr = reinterpret_cast<const P64*>(s_par) + b * SL + goff;
-                        const uint32_t cls = (st.cls >> (2 * g)) & 3u;
-                        if (cls != 0u) {
-                            const double x2 = x * x, t = 1 / x2;
-#pragma unroll
-                            for (int k = 0; k < K; k++) {
-                                if (pr[k].a <= 0.2) {
-                                    const double iv = t * pr[k].c;
-                                    acc[k] += Acc((pr[k].w * iv) * (1 + iv * (1.5 + 3.75 * iv)));
-                                } else {
-                                    acc[k] += Acc(far_lorentz64(pr[k], x2));
-                                }
-                            }
-                        } else {
-#pragma unroll
-                            for (int k = 0; k < K; k++) acc[k] += Acc(voigt64(pr[k].a, x * pr[k].inv_s) * pr[k].scale);
-                        }
+                        for (int k = 0; k < K; k++) acc[k] += voigt64(pr[k].a, x * pr[k].inv_s) * pr[k].scale;
                     }
                 }
             }
@@ -832,8 +745,7 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
     // alpha += accumulated lines, staged through shared memory for coalesced updates
     const int stride = SL + 1;
 #pragma unroll
-    for (int k = 0; k < K; k++)
-        s_alpha[jl * stride + goff + k] = MIXED ? double(acc[k]) - double(comp[k]) : double(acc[k]);
+    for (int k = 0; k < K; k++) s_alpha[jl * stride + goff + k] = acc[k];
     __syncthreads();
     const int64_t nj = jlast - j0 + 1;
     double* dst = a.alpha + j0 * L;
@@ -851,11 +763,212 @@ __device__ __forceinline__ void line_tile_body(const TileArgs& a, int64_t tile, 
     }
 }
 
-// One CTA per tile of one spectrum.
+// A candidate line of the current chunk, as a mixed tile sees it (one layer group per CTA).
+struct LineStage32 {
+    float dhi, dlo;   // centre - first wavelength of the tile, as an FP32 pair
+    int32_t lb, ub;   // window (grid indices)
+    float cref;       // 2 sigma^2 of layer 0: the wing cubics' variable is t' = cref / dl^2
+    float xfar;       // |dl| beyond which every layer of the group is in a closed-form wing branch
+    uint32_t cubic;   // 1: every layer of the group is in its cubic regime over the whole tile
+    int32_t li;       // line index
+};
+static_assert(sizeof(LineStage32) == 32, "LineStage32 is two 16-byte loads");
+
+// Mixed-precision tile: TW = blockDim.x wavelengths x the K layers of group g.  Thread t owns
+// wavelength j0 + t and all K layers.  Per staged line:
+//   * lines whose layers are all in their cubic regime over the tile (most evaluations: far
+//     wings) were staged as wing cubics: t' = cref / dl^2 per wavelength (zero outside the
+//     window), then three FMAs per layer;
+//   * other lines were staged as packed constants; each warp then checks whether its in-window
+//     wavelengths are all beyond the wing boundary (one vote per line and warp) and evaluates
+//     the closed-form wing branches, else the full profile.
+// Accumulation: FP32 partial sums per batch of B lines, added to the accumulators with Kahan
+// compensation.  Lines are visited in list order: results do not depend on the launch shape
+// beyond the batch boundaries and the tile origins.  (Two wavelengths per thread, sharing each
+// shared-memory load of a layer's constants, measured slower: the third accumulator set costs
+// registers and occupancy than the saved loads gain.)
+template <int K>
+__device__ __forceinline__ void line_tile_body_mixed(const TileArgs& a, int64_t tile, int g, unsigned char* smem) {
+    const int Lp = a.Lp, G = a.G, B = a.stage;
+    double* s_alpha = reinterpret_cast<double*>(smem);                              // [TW][K+1], at the end
+    LineStage32* s_ln = reinterpret_cast<LineStage32*>(smem + 2 * size_t(a.region));  // [blockDim]
+    __shared__ int32_t s_warp[32];
+    __shared__ int32_t s_count;
+    __shared__ int64_t s_tier[NTIER][2];
+    const int tid = threadIdx.x, nthr = blockDim.x, TW = nthr;
+    const int warp = tid >> 5, lane = tid & 31, nwarps = nthr >> 5;
+    const int64_t j0 = tile * TW;
+    const int64_t jlast = min(j0 + TW, a.nwl) - 1;
+    const double wl_ref = a.wls[j0], wl_last = a.wls[jlast];
+    const float span32 = float(wl_last - wl_ref);
+    // this thread's wavelength, and its offset from the tile's first one as an FP32 hi + lo pair
+    // (formed in FP64), so |wl_j - wl0| is recovered in FP32 to about one rounding; a wavelength
+    // past the grid end lies in no window
+    const int32_t jm = int32_t(j0 + tid);
+    const double dj = (j0 + tid < a.nwl ? a.wls[j0 + tid] : wl_ref) - wl_ref;
+    const float xh = float(dj), xl = float(dj - double(xh));
+    if (tid < NTIER) {  // candidate runs of the width tiers
+        const int64_t t0 = a.tier_start[tid], t1 = a.tier_start[tid + 1];
+        if (*a.unsorted) {
+            s_tier[tid][0] = t0;
+            s_tier[tid][1] = t1;
+        } else {
+            const int32_t w = c_tier_w[tid] + 1;
+            const int32_t lo = int32_t(max(int64_t(j0) - w, int64_t(INT32_MIN / 2)));
+            const int32_t hi = int32_t(min(int64_t(jlast) + w, int64_t(INT32_MAX / 2)));
+            s_tier[tid][0] = lower_bound_i32(a.tier_ci, t0, t1, lo);
+            s_tier[tid][1] = upper_bound_i32(a.tier_ci, t0, t1, hi);
+        }
+    }
+    __syncthreads();
+
+    float acc[K], comp[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) { acc[k] = 0.f; comp[k] = 0.f; }
+
+    const int64_t src0 = int64_t(g) * K;  // the group's first float4 within a line's Lp constants
+    const int cb0 = tid / K, cr0 = tid - cb0 * K;      // this thread's first staged (line, layer)
+    const int cdb = nthr / K, cdr = nthr - cdb * K;    // and the step between its pieces
+    for (int tier = 0; tier < NTIER; tier++)
+    for (int64_t base = s_tier[tier][0]; base < s_tier[tier][1]; base += nthr) {
+        const int64_t pidx = base + tid;
+        int64_t i = 0;
+        bool take = false;
+        int32_t lbi = 0, ubi = -1;
+        if (pidx < s_tier[tier][1]) {
+            i = a.tier_idx[pidx];
+            lbi = a.lb[i];
+            ubi = a.ub[i];
+            take = lbi <= jlast && ubi >= j0;
+        }
+        const unsigned msk = __ballot_sync(0xffffffffu, take);
+        if (lane == 0) s_warp[warp] = __popc(msk);
+        __syncthreads();
+        if (tid == 0) {
+            int run = 0;
+            for (int w = 0; w < nwarps; w++) { int c = s_warp[w]; s_warp[w] = run; run += c; }
+            s_count = run;
+        }
+        __syncthreads();
+        if (take) {  // the thread that found the line describes it for the whole CTA
+            LineStage32 st;
+            const double d = a.wl[i] - wl_ref;
+            const float dh = float(d);
+            // distance of the centre from the tile in FP32 (the boundaries carry a 1e-4
+            // relative margin, far above the rounding)
+            const float fdist = dh < 0.f ? -dh : (dh > span32 ? dh - span32 : 0.f);
+            st.dhi = dh;
+            st.dlo = float(d - double(dh));
+            st.lb = lbi;
+            st.ub = ubi;
+            st.cref = reinterpret_cast<const float4*>(a.params)[i * Lp].x;  // 2 sigma^2, layer 0
+            st.xfar = a.xfar[i * G + g];
+            st.cubic = fdist > a.xcub[i * G + g] ? 1u : 0u;
+            st.li = int32_t(i);
+            s_ln[s_warp[warp] + __popc(msk & ((1u << lane) - 1))] = st;
+        }
+        const int cnt = s_count;
+        __syncthreads();
+
+        // batches of B lines: the group's constants copied with cp.async into two alternating
+        // buffers (wing cubics for cubic-regime lines, packed constants otherwise)
+        const int nq = (cnt + B - 1) / B;
+        auto issue = [&](int q) {
+            if (q < nq) {
+                const int b0 = q * B, nb = min(B, cnt - b0);
+                unsigned char* buf = smem + size_t(q & 1) * a.region;
+                int b = cb0, r = cr0;  // piece e = tid + k nthr is (line b, layer r), stepped without a division
+                for (int e = tid; e < nb * K; e += nthr) {
+                    const LineStage32& sl = s_ln[b0 + b];
+                    const float4* src = sl.cubic ? a.params_w : reinterpret_cast<const float4*>(a.params);
+                    cp_async16(buf + (size_t(b) * K + r) * 16, src + (int64_t(sl.li) * Lp + src0 + r));
+                    b += cdb;
+                    r += cdr;
+                    if (r >= K) {
+                        r -= K;
+                        b++;
+                    }
+                }
+            }
+            cp_async_commit();
+        };
+        issue(0);
+        for (int q = 0; q < nq; q++) {
+            issue(q + 1);
+            cp_async_wait_1();  // batch q has landed (this thread's copies) ...
+            __syncthreads();    // ... and everybody else's
+            const int b0 = q * B, nb = min(B, cnt - b0);
+            const float4* s_par = reinterpret_cast<const float4*>(smem + size_t(q & 1) * a.region);
+            float part[K];
+#pragma unroll
+            for (int k = 0; k < K; k++) part[k] = 0.f;
+            for (int b = 0; b < nb; b++) {
+                const LineStage32 st = s_ln[b0 + b];
+                const float4* pr = s_par + b * K;
+                const bool in = jm >= st.lb && jm <= st.ub;
+                const float x = fabsf((xh - st.dhi) + (xl - st.dlo));
+                if (st.cubic) {
+                    const float tp = in ? __fdividef(st.cref, x * x) : 0.f;
+#pragma unroll
+                    for (int k = 0; k < K; k++) {
+                        const float4 p = pr[k];
+                        part[k] = fmaf(tp, fmaf(tp, fmaf(tp, p.z, p.y), p.x), part[k]);
+                    }
+                } else if (__all_sync(0xffffffffu, !in || x > st.xfar)) {
+                    // every in-window wavelength of the warp in a closed-form wing branch, chosen
+                    // per layer (uniform across the warp)
+                    if (in) {
+                        const float x2 = x * x, t = __fdividef(1.f, x2);
+#pragma unroll
+                        for (int k = 0; k < K; k++) {
+                            const float4 p = pr[k];
+                            if (p.y <= 0.2f) {
+                                const float iv = t * p.x;
+                                part[k] = fmaf(p.z * iv, fmaf(fmaf(3.75f, iv, 1.5f), iv, 1.f), part[k]);
+                            } else {
+                                part[k] += far_lorentz32(p, x2);
+                            }
+                        }
+                    }
+                } else if (in) {
+                    const float t = __fdividef(1.f, x * x);
+#pragma unroll
+                    for (int k = 0; k < K; k++) part[k] += profile32x(pr[k], x, t);
+                }
+            }
+            // batch partial sums enter the accumulators with Kahan compensation
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                const float y = part[k] - comp[k];
+                const float tt = acc[k] + y;
+                comp[k] = (tt - acc[k]) - y;
+                acc[k] = tt;
+            }
+            __syncthreads();  // buffer (q & 1) is refilled by issue(q + 2)
+        }
+    }
+    // alpha += accumulated lines, staged through shared memory for coalesced updates
+    const int stride = K + 1;
+#pragma unroll
+    for (int k = 0; k < K; k++) s_alpha[tid * stride + k] = double(acc[k]) - double(comp[k]);
+    __syncthreads();
+    const int64_t nj = jlast - j0 + 1;
+    double* dst = a.alpha + j0 * a.L;
+    const int l0 = g * K, nk = min(K, a.L - l0);
+    for (int64_t e = tid; e < nj * nk; e += nthr) {
+        const int j = int(e / nk), k = int(e - int64_t(j) * nk);
+        dst[int64_t(j) * a.L + l0 + k] += s_alpha[j * stride + k];
+    }
+}
+
+// One CTA per tile of one spectrum (per tile and layer group in the mixed form).
 template <bool MIXED, int K, int MAXT, int MINB>
 __global__ void __launch_bounds__(MAXT, MINB) line_tile_kernel(TileArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
-    line_tile_body<MIXED, K>(a, blockIdx.x, a.split ? int(blockIdx.y) : -1, smem);
+    if constexpr (MIXED)
+        line_tile_body_mixed<K>(a, blockIdx.x, int(blockIdx.y), smem);
+    else
+        line_tile_body64<K>(a, blockIdx.x, a.split ? int(blockIdx.y) : -1, smem);
 }
 
 // Work queue of (spectrum, tile) items for a batch of spectra on one wavelength grid.  Item k
@@ -886,7 +999,10 @@ __global__ void __launch_bounds__(MAXT, MINB) line_tile_queue_kernel(TileQueue q
         const long long it = s_item;
         if (it >= q.nitems) break;
         const long long r = it / q.nspec;
-        line_tile_body<MIXED, K>(s_a, r / q.groups, q.groups > 1 ? int(r % q.groups) : -1, smem);
+        if constexpr (MIXED)
+            line_tile_body_mixed<K>(s_a, r / q.groups, int(r % q.groups), smem);
+        else
+            line_tile_body64<K>(s_a, r / q.groups, q.groups > 1 ? int(r % q.groups) : -1, smem);
         __syncthreads();  // s_a and s_item are rewritten for the next item
     }
 }

@@ -78,7 +78,8 @@ def test_batch_autotuner_picks_a_shape_and_keeps_results(gpu_lib):
         tuned.run()
     f1, c1 = tuned.results()
     cfg = tuned.tile_config()
-    assert cfg["tuned"] and cfg["tw"] in (32, 64, 128) and cfg["stage"] in (16, 32)
+    # mixed shapes: 64-256 wavelengths x one layer group, 32- or 64-line batches
+    assert cfg["tuned"] and cfg["tw"] in (64, 128, 256) and cfg["stage"] in (32, 64) and cfg["split"]
     # another tile shape changes the FP32 rounding of the offsets and the Kahan batches only
     np.testing.assert_allclose(f1, f0, rtol=2e-6, atol=0)
     np.testing.assert_allclose(c1, c0, rtol=2e-6, atol=0)
@@ -86,27 +87,34 @@ def test_batch_autotuner_picks_a_shape_and_keeps_results(gpu_lib):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_tile_shapes_give_identical_opacity(gpu_lib, precision):
-    """Splitting the layer groups over CTAs keeps every thread's accumulation order: the FP64
-    opacity is bitwise unchanged (mixed: to FP32 rounding, the compiler may contract the split
-    path differently).  Other tile widths move the tile origins (mixed offsets) and the batch
-    boundaries only."""
+    """FP64: splitting the layer groups over CTAs keeps every thread's accumulation order, so the
+    opacity is bitwise unchanged; other tile widths move only the batch boundaries.  Mixed (always
+    one layer group per CTA; a shape with all groups per CTA is KORG_EINVAL): other widths and
+    batch sizes move the tile origins (the FP32 offsets, and which lines take the wing cubics) and
+    the Kahan batch boundaries only."""
     import ctypes as C
     from korg_gb300 import synthetic
     from korg_gb300.api import synthesize_prepared
     inp = synthetic.prepare(synthetic.config0(n_lines=3000))
     prec = gpu_lib.KORG_MIXED if precision == "mixed" else gpu_lib.KORG_FP64
     L = len(inp.T)
+    shapes = ((64, 0, 0), (64, 0, 1), (32, 16, 1), (128, 0, 0)) if precision == "fp64" else \
+        ((128, 0, 1), (64, 32, 1), (256, 64, 1), (32, 16, 1))
     out = {}
-    for cfg in ((64, 0, 0), (64, 0, 1), (32, 16, 1), (128, 0, 0)):
+    for cfg in shapes:
         ctx = gpu_lib.Context(0)
         ctx.check(ctx.lib.korg_set_tile_config(ctx.h, L, prec, *cfg))
         r = synthesize_prepared(inp, precision=precision, return_alpha=True, ctx=ctx)
         out[cfg] = r
         ctx.close()
-    base = out[(64, 0, 0)]
+    base = out[shapes[0]]
     if precision == "fp64":
         assert np.array_equal(out[(64, 0, 1)].alpha, base.alpha)
+        for cfg in ((32, 16, 1), (128, 0, 0)):
+            np.testing.assert_allclose(out[cfg].alpha, base.alpha, rtol=1e-13)
     else:
-        np.testing.assert_allclose(out[(64, 0, 1)].alpha, base.alpha, rtol=1e-6)
-    for cfg in ((32, 16, 1), (128, 0, 0)):
-        np.testing.assert_allclose(out[cfg].alpha, base.alpha, rtol=1e-5 if precision == "mixed" else 1e-13)
+        for cfg in shapes[1:]:
+            np.testing.assert_allclose(out[cfg].alpha, base.alpha, rtol=1e-5)
+        ctx = gpu_lib.Context(0)
+        assert ctx.lib.korg_set_tile_config(ctx.h, L, prec, 64, 0, 0) == 1  # all groups per CTA: mixed has none
+        ctx.close()
