@@ -169,9 +169,9 @@ void record(korg_ctx* ctx, int i, cudaStream_t s) {
 // G*K.  56-layer (MARCS) atmospheres split exactly into 4 x 14.
 // Tables of the table-driven FP64 exp / log (physics.cuh), in extended precision on the host.
 void fill_math_tables(MathTables& t) {
-    for (int j = 0; j < 64; j++) {
-        t.exp2j[j] = double(exp2l((long double)j / 64.0L));
-        const long double c = 1.0L + ((long double)j + 0.5L) / 64.0L;
+    for (int j = 0; j < MATH_TABLE_N; j++) {
+        t.exp2j[j] = double(exp2l((long double)j / (long double)MATH_TABLE_N));
+        const long double c = 1.0L + ((long double)j + 0.5L) / (long double)MATH_TABLE_N;
         const double ic = double(1.0L / c);
         t.inv_c[j] = ic;
         t.log_c[j] = double(-logl((long double)ic));

@@ -27,53 +27,52 @@ constexpr double SQRT_2PI = 2.5066282746310002;  // sqrt(2*pi)
 
 // ---------------------------------------------------------------- table-driven FP64 exp / log
 // Tang's table-driven method (P. T. P. Tang, ACM TOMS 15 (1989) 144 and 16 (1990) 378),
-// implemented from the mathematics: exp(x) = 2^m 2^(j/64) e^r with |r| <= ln2/128 and a
-// degree-6 Taylor polynomial; log(x) = e ln2 + log(c_j) + log(1 + r), c_j = 1 + (j + 1/2)/64,
-// r = m/c_j - 1 (|r| <= 1/129) and a degree-8 series.  About half the FP64 operations of the
-// general-purpose functions, which matters on GB300 where the FP64 pipe is 1/64 of FP32.
+// implemented from the mathematics with 256-entry tables: exp(x) = 2^m 2^(j/256) e^r with
+// |r| <= ln2/512 and a degree-4 Taylor polynomial (truncation r^5/120 < 4e-17 relative);
+// log(x) = e ln2 + log(c_j) + log(1 + r), c_j = 1 + (j + 1/2)/256, r = m/c_j - 1
+// (|r| <= 1/513) and a degree-5 series (truncation r^6/6 < 1e-17).  About a third of the FP64
+// operations of the general-purpose functions, which matters on GB300 where the FP64 pipe is
+// 1/64 of FP32; the range checks are integer compares on the bit patterns.
 // Tables (computed on the host in extended precision at context creation):
-//   exp2j[j] = 2^(j/64), inv_c[j] = 1/c_j rounded to double, log_c[j] = -log(inv_c[j]).
-// Accuracy: exp within 1 ulp for |x| <= 700 (outside that range the CUDA function is used);
+//   exp2j[j] = 2^(j/256), inv_c[j] = 1/c_j rounded to double, log_c[j] = -log(inv_c[j]).
+// Accuracy: exp within 1 ulp for |x| < 700 (outside that range the CUDA function is used);
 // log within 2e-15 absolute (0.5 ulp for |log x| >~ 4) for normal x.
+constexpr int MATH_TABLE_BITS = 8;
+constexpr int MATH_TABLE_N = 1 << MATH_TABLE_BITS;
 struct MathTables {
-    double exp2j[64];
-    double inv_c[64];
-    double log_c[64];
+    double exp2j[MATH_TABLE_N];
+    double inv_c[MATH_TABLE_N];
+    double log_c[MATH_TABLE_N];
 };
 
 __device__ __forceinline__ double fexp64(double x, const MathTables& t) {
-    if (!(fabs(x) <= 700.0)) return exp(x);
-    const double INV_L = 92.33248261689366;            // 64 / ln 2
-    const double L_HI = 0.010830424696905538;          // ln2 / 64 to 33 bits (k * L_HI exact)
-    const double L_LO = -6.563929801064195e-13;        // ln2 / 64 - L_HI
+    if ((__double2hiint(x) & 0x7fffffff) >= 0x4085E000) return exp(x);  // |x| >= 700, inf, NaN
+    const double INV_L = 369.3299304675746;            // 256 / ln 2
+    const double L_HI = 0.0027076061742263846;         // ln2 / 256 to 33 bits (k * L_HI exact)
+    const double L_LO = -1.6409824502660487e-13;       // ln2 / 256 - L_HI
     const double MAGIC = 6755399441055744.0;           // 1.5 * 2^52: round to integer
     double kd = fma(x, INV_L, MAGIC);
     const int k = __double2loint(kd);
     kd -= MAGIC;
     double r = fma(-kd, L_HI, x);
     r = fma(-kd, L_LO, r);
-    double p = fma(r, 1.0 / 720.0, 1.0 / 120.0);
-    p = fma(p, r, 1.0 / 24.0);
-    p = fma(p, r, 1.0 / 6.0);
+    double p = fma(r, 1.0 / 24.0, 1.0 / 6.0);
     p = fma(p, r, 0.5);
     p = fma(p, r, 1.0);
     p *= r;
-    const double tj = t.exp2j[k & 63];
+    const double tj = t.exp2j[k & (MATH_TABLE_N - 1)];
     const double res = fma(tj, p, tj);
-    return __longlong_as_double(__double_as_longlong(res) + ((long long)(k >> 6) << 52));
+    return __longlong_as_double(__double_as_longlong(res) + ((long long)(k >> MATH_TABLE_BITS) << 52));
 }
 
 __device__ __forceinline__ double flog64(double x, const MathTables& t) {
-    if (!(x >= 2.2250738585072014e-308 && x <= 1.7976931348623157e308)) return log(x);
     const long long b = __double_as_longlong(x);
+    if (b < 0x0010000000000000LL || b >= 0x7FF0000000000000LL) return log(x);  // not normal and positive
     const int e = int((b >> 52) & 0x7ff) - 1023;
     const double m = __longlong_as_double((b & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
-    const int j = int((b >> 46) & 63);
+    const int j = int((b >> (52 - MATH_TABLE_BITS)) & (MATH_TABLE_N - 1));
     const double r = fma(m, t.inv_c[j], -1.0);
-    double p = fma(-0.125, r, 1.0 / 7.0);
-    p = fma(p, r, -1.0 / 6.0);
-    p = fma(p, r, 0.2);
-    p = fma(p, r, -0.25);
+    double p = fma(0.2, r, -0.25);
     p = fma(p, r, 1.0 / 3.0);
     p = fma(p, r, -0.5);
     p = fma(p, r, 1.0);
@@ -86,7 +85,7 @@ __device__ __forceinline__ double flog64(double x, const MathTables& t) {
 __device__ __forceinline__ void load_math_tables(MathTables& dst, const MathTables* src) {
     const double* s = reinterpret_cast<const double*>(src);
     double* d = reinterpret_cast<double*>(&dst);
-    for (int i = threadIdx.x; i < 192; i += blockDim.x) d[i] = s[i];
+    for (int i = threadIdx.x; i < 3 * MATH_TABLE_N; i += blockDim.x) d[i] = s[i];
 }
 
 // ---------------------------------------------------------------- FP64 Voigt-Hjerting
@@ -241,6 +240,19 @@ __device__ __forceinline__ double knot_eval(const double* v, int64_t n, KnotPos 
 }
 
 // ---------------------------------------------------------------- transfer
+// 1/d by Newton-Raphson iteration from an FP32 seed: r0 = 1/float(d) (relative error about
+// 2^-21), then one cubically convergent step r1 = r0 + r0 (e + e^2) with e = 1 - d r0, whose
+// truncation error e^3 ~ 2^-63 is below FP64 rounding: within about one ulp of 1/d, in three
+// FP64 fused multiply-adds instead of a full FP64 division.  Outside the FP32 normal range of
+// the seed the FP64 division is used.
+__device__ __forceinline__ double recip64(double d) {
+    const float f = __double2float_rn(d);
+    if (!(fabsf(f) > 1e-30f && fabsf(f) < 1e30f)) return 1.0 / d;
+    double r = double(__fdividef(1.f, f));
+    const double e = fma(-d, r, 1.0);
+    return fma(r, fma(e, e, e), r);
+}
+
 // RadiativeTransfer.jl:408-497
 __device__ __forceinline__ double expint2_64(double x) {
     if (x == 0) return 1.0;
@@ -292,7 +304,7 @@ __device__ __forceinline__ double expint2_64(double x) {
 // and the table-driven log for the small-argument series (:432-439)
 __device__ __forceinline__ double expint2_ex(double x, double ex, const MathTables& t) {
     if (x >= 9) {
-        const double invx = 1 / x;
+        const double invx = recip64(x);
         return ex * (1 + (-2 + (6 + (-24 + 120 * invx) * invx) * invx) * invx) * invx;
     }
     if (x < 1.1 && x != 0) {
@@ -304,7 +316,10 @@ __device__ __forceinline__ double expint2_ex(double x, double ex, const MathTabl
 }
 
 // RadiativeTransfer.jl:398-400 with E2(tau) and exp(-tau) supplied by the caller (they are
-// per-layer quantities shared by the two segments that meet at a layer).
+// per-layer quantities shared by the two segments that meet at a layer).  Expanded,
+//   core = [3b (tau E2 - e^-tau) + 2m (tau^2 E2 - e^-tau (tau + 1))] / 6 = b G / 2 + m H / 3
+// with G = tau E2 - e^-tau and H = tau G - e^-tau, which depend on the layer only: the planar
+// kernel carries G and H per layer instead of evaluating the core twice per segment.
 __device__ __forceinline__ double expint_core(double tau, double e2, double ex, double m, double b) {
     return 1.0 / 6.0 * (tau * e2 * (3 * b + 2 * m * tau) - ex * (3 * b + 2 * m * (tau + 1)));
 }

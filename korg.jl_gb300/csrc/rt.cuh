@@ -34,36 +34,45 @@ struct RtArgs {
 __device__ __forceinline__ double planck(double pre, double hc_over_wl, double T) {
     return pre * 1 / expm1(hc_over_wl / KBOLTZ_CGS / T);
 }
-// The same with 1/(kT) per layer precomputed and exp(x) - 1 from the table-driven exp: for
-// x = hc/(lambda k T) >= 0.07 (lambda <= 2 um, T <= 1e5 K) the subtraction loses under two
-// bits, so the result stays within a few ulps of expm1's while the FP64 work per
-// (layer, wavelength) drops by about a third.
+// The same with 1/(kT) per layer precomputed, exp(x) - 1 from the table-driven exp and the
+// Newton reciprocal: for x = hc/(lambda k T) >= 0.07 (lambda <= 2 um, T <= 1e5 K) the
+// subtraction loses under two bits, so the result stays within a few ulps of expm1's while the
+// FP64 work per (layer, wavelength) drops by about half.
 __device__ __forceinline__ double planck_t(double pre, double hc_over_wl, double inv_kT, const MathTables& mt) {
     const double x = hc_over_wl * inv_kT;
-    return x < 0.05 ? pre / expm1(x) : pre / (fexp64(x, mt) - 1.0);
+    return x < 0.05 ? pre / expm1(x) : pre * recip64(fexp64(x, mt) - 1.0);
 }
 
-// Once tau at a layer exceeds TAU_STOP, every deeper segment of that column contributes less
-// than S_max * exp(-TAU_STOP) (~1e-44 relative): the recursion stops there.
-constexpr double TAU_STOP = 100.0;
+// Once tau at a layer exceeds TAU_STOP, every deeper segment of that column contributes at most
+// S_max E2(TAU_STOP) < S_max exp(-TAU_STOP) / TAU_STOP ~ 1e-19 S_max; S_max / F stays below
+// ~1e3 for stellar atmospheres (Planck contrast between the top and the bottom), so the
+// neglected part is below 1e-16 of the flux: the recursion stops there.
+constexpr double TAU_STOP = 40.0;
 
-// One pass of the column recursion; the continuum-only and full passes share the loop.
+// One pass of the column recursion; the continuum-only and full passes share the loop.  The
+// segment [l-1, l] adds core(tau_l) - core(tau_{l-1}) with the slope m and intercept b of the
+// linear source function in tau (RadiativeTransfer.jl:382-385); with core = b G / 2 + m H / 3
+// (expint_core) and b = S_{l-1} - m tau_{l-1}:
+//   I += S_{l-1} dG / 2 + m (dH / 3 - tau_{l-1} dG / 2),  m = (S_l - S_{l-1}) / dtau.
 struct RtPass {
-    double ib_prev, tau_prev, e2_prev, ex_prev, I;
+    double ib_prev, tau_prev, G_prev, H_prev, I;
     bool live;
-    __device__ __forceinline__ void step(double alpha, double fac, double dlt, double S, double S_prev,
+    __device__ __forceinline__ void step(double alpha, double fac, double hdlt, double dS, double half_Sp,
                                          const MathTables& mt) {
         const double ib = alpha * fac;
-        const double tau = tau_prev + 0.5 * (ib + ib_prev) * dlt;  // RadiativeTransfer.jl:250-251
-        const double m = (S - S_prev) / (tau - tau_prev);          // :382
-        const double b = S_prev - m * tau_prev;                    // :383
+        const double dtau = (ib + ib_prev) * hdlt;                 // RadiativeTransfer.jl:250-251
+        const double tau = tau_prev + dtau;
+        const double m = dS * recip64(dtau);                        // :382
         const double ex = fexp64(-tau, mt);
         const double e2 = expint2_ex(tau, ex, mt);
-        I += (expint_core(tau, e2, ex, m, b) - expint_core(tau_prev, e2_prev, ex_prev, m, b));  // :384-385
+        const double G = fma(tau, e2, -ex), H = fma(tau, G, -ex);
+        const double dG = G - G_prev, dH = H - H_prev;
+        I = fma(half_Sp, dG, I);                                    // :383-385
+        I = fma(m, fma(-0.5 * tau_prev, dG, dH * (1.0 / 3.0)), I);
         ib_prev = ib;
         tau_prev = tau;
-        e2_prev = e2;
-        ex_prev = ex;
+        G_prev = G;
+        H_prev = H;
         live = tau <= TAU_STOP;
     }
 };
@@ -73,12 +82,12 @@ __global__ void __launch_bounds__(128) rt_kernel(RtArgs a) {
     __shared__ MathTables s_math;
     load_math_tables(s_math, a.math);
     const int L = a.L;
-    double* s_fac = s_rt;          // tau_ref/alpha_ref * ds/dz (= 1)
-    double* s_ltr = s_rt + L;      // log(tau_ref)
-    double* s_ikT = s_rt + 2 * L;  // 1/(k T)
+    double* s_fac = s_rt;           // tau_ref/alpha_ref * ds/dz (= 1)
+    double* s_hdl = s_rt + L;       // (log tau_ref[l] - log tau_ref[l-1]) / 2
+    double* s_ikT = s_rt + 2 * L;   // 1/(k T)
     for (int l = threadIdx.x; l < L; l += blockDim.x) {
         s_fac[l] = a.tau_ref[l] / a.alpha_ref[l] * 1.0;  // RadiativeTransfer.jl:160
-        s_ltr[l] = log(a.tau_ref[l]);                     // :114
+        s_hdl[l] = l > 0 ? 0.5 * (log(a.tau_ref[l]) - log(a.tau_ref[l - 1])) : 0.0;  // :114, :250-251
         s_ikT[l] = a.T ? 1.0 / (KBOLTZ_CGS * a.T[l]) : 0.0;
     }
     __syncthreads();
@@ -96,16 +105,16 @@ __global__ void __launch_bounds__(128) rt_kernel(RtArgs a) {
     const double* al = a.alpha + j * L;
     const double* Sc = a.S ? a.S + j * L : nullptr;
 
-    // layer 0: tau = 0, E2(0) = 1, exp(0) = 1
+    // layer 0: tau = 0, E2(0) = 1, exp(0) = 1, so G = -1 and H = -1
     double S_prev = Sc ? Sc[0] : planck_t(pre, hcw, s_ikT[0], s_math);
-    RtPass full{al[0] * s_fac[0], 0.0, 1.0, 1.0, 0.0, true};
-    RtPass cont{two ? knot_eval(a.cn.vals, a.cn.nk, kp) * s_fac[0] : 0.0, 0.0, 1.0, 1.0, 0.0, two};
+    RtPass full{al[0] * s_fac[0], 0.0, -1.0, -1.0, 0.0, true};
+    RtPass cont{two ? knot_eval(a.cn.vals, a.cn.nk, kp) * s_fac[0] : 0.0, 0.0, -1.0, -1.0, 0.0, two};
     for (int l = 1; l < L && (full.live || cont.live); l++) {
         const double S = Sc ? Sc[l] : planck_t(pre, hcw, s_ikT[l], s_math);
-        const double dlt = s_ltr[l] - s_ltr[l - 1];
-        if (full.live) full.step(al[l], s_fac[l], dlt, S, S_prev, s_math);
+        const double hdl = s_hdl[l], dS = S - S_prev, half_Sp = 0.5 * S_prev;
+        if (full.live) full.step(al[l], s_fac[l], hdl, dS, half_Sp, s_math);
         if (cont.live)
-            cont.step(knot_eval(a.cn.vals + int64_t(l) * a.cn.nk, a.cn.nk, kp), s_fac[l], dlt, S, S_prev, s_math);
+            cont.step(knot_eval(a.cn.vals + int64_t(l) * a.cn.nk, a.cn.nk, kp), s_fac[l], hdl, dS, half_Sp, s_math);
         S_prev = S;
     }
     a.flux[j] = 2 * PI * (full.I * 1.0) * a.unit;  // :136
