@@ -634,6 +634,17 @@ struct __align__(4 * sizeof(R)) AdjW {
 // A stage whose nearest wavelength is already in the layer's wing takes a branch-free loop, and
 // so does a stage entirely in the far-Lorentz branch.  Elsewhere central_derivs differentiates
 // the far-Lorentz branch in closed form and the Harris branches with dual numbers.
+// Mixed form: |dl| beyond which a far-Lorentz layer (a > 0.2) is given by the cubic series of
+// its branch to FP32 rounding (far_lorentz_cubic_rmin), as in the forward tiles: the wing
+// moments then serve it too.  In u = 1/v^2 both wing forms are
+//   H = (c1 u + c2 u^2 + c3 u^3) / sqrt(pi),
+// asymptotic branch (a <= 0.2): c = (a, 1.5 a, 3.75 a); far-Lorentz series (w = 1/r^2 = a^2 u):
+// c = (a, 1.5 a - a^3, 3.75 a - 5 a^3 + a^5).
+__device__ __forceinline__ float adj_fl_cubic_x(float a, float s) {
+    const float xfl = a <= 1.4f ? (3.2f - a) / s : 0.f;
+    return fmaxf(xfl, far_lorentz_cubic_rmin(a) * a / s) * 1.0001f;
+}
+
 template <bool MIXED>
 __global__ void __launch_bounds__(512, MIXED ? 2 : 1) line_adj_kernel(LineAdjArgs a) {
     using R = typename std::conditional<MIXED, float, double>::type;
@@ -644,6 +655,7 @@ __global__ void __launch_bounds__(512, MIXED ? 2 : 1) line_adj_kernel(LineAdjArg
     constexpr int PER = ADJ_SUB / 32;        // table entries per producer lane
     __shared__ long long s_item;
     __shared__ int64_t s_i, s_j0, s_j1;
+    __shared__ float s_dmin;                 // mixed: |dl| from the line centre to the item's nearest wavelength
     __shared__ __align__(8) uint64_t s_full[ADJ_STAGES], s_empty[ADJ_STAGES];
     __shared__ W s_w[ADJ_STAGES][ADJ_SUB];
     __shared__ R s_xmin[ADJ_STAGES];
@@ -696,7 +708,11 @@ __global__ void __launch_bounds__(512, MIXED ? 2 : 1) line_adj_kernel(LineAdjArg
                 s_i = i;
                 s_j0 = max(int64_t(a.lb[i]), k0);
                 s_j1 = min(int64_t(a.ub[i]), k0 + ADJ_CHUNK - 1);
-                if (s_j0 <= s_j1) break;
+                if (s_j0 <= s_j1) {
+                    const double c = a.wl[i], lo = a.wls[s_j0], hi = a.wls[s_j1];
+                    s_dmin = float(c < lo ? lo - c : (c > hi ? c - hi : 0.0));
+                    break;
+                }
             }
         }
         __syncthreads();
@@ -712,13 +728,19 @@ __global__ void __launch_bounds__(512, MIXED ? 2 : 1) line_adj_kernel(LineAdjArg
             break;
         }
         const int64_t i = s_i, j0 = s_j0, j1 = s_j1;
-        // classify the layers: a > 0.2 ("slow") or not, counted per warp of layer indices
+        // classify the layers: a > 0.2 ("slow") or not, counted per warp of layer indices; in
+        // the mixed form a far-Lorentz layer whose cubic regime covers the whole item costs what
+        // a wing layer does and counts as one
         bool slow_l = false;
         unsigned ball = 0;
         if (warp * 32 < L) {
             if (threadIdx.x < L) {
-                slow_l = MIXED ? reinterpret_cast<const float4*>(a.params)[i * Lp + threadIdx.x].y > 0.2f
-                               : reinterpret_cast<const P64*>(a.params)[i * Lp + threadIdx.x].a > 0.2;
+                if (MIXED) {
+                    const float4 p = reinterpret_cast<const float4*>(a.params)[i * Lp + threadIdx.x];
+                    slow_l = p.y > 0.2f && adj_fl_cubic_x(p.y, rsqrtf(p.x)) > s_dmin;
+                } else {
+                    slow_l = reinterpret_cast<const P64*>(a.params)[i * Lp + threadIdx.x].a > 0.2;
+                }
             }
             ball = __ballot_sync(0xffffffffu, slow_l);
             if (lane == 0) s_wslow[warp] = __popc(ball);
@@ -862,6 +884,7 @@ __global__ void __launch_bounds__(512, MIXED ? 2 : 1) line_adj_kernel(LineAdjArg
                 }
                 rho = c2 / cref;
                 if (av <= R(0.2)) xw = R(5) / s;  // the wing starts at v = 5
+                else if (MIXED) xw = R(adj_fl_cubic_x(float(av), float(s)));  // far-Lorentz cubic regime
             }
             const R ia = recip(av), k1 = s * ia;  // far Lorentz: r = v / a = x s / a
             for (int sq = 0; sq < nsub; sq++) {
@@ -874,7 +897,7 @@ __global__ void __launch_bounds__(512, MIXED ? 2 : 1) line_adj_kernel(LineAdjArg
                 if (active) {
                     const R xmin = s_xmin[b];
                     R pm[3] = {0, 0, 0};
-                    if (xmin >= xw) {  // every staged wavelength in the asymptotic wing
+                    if (xmin >= xw) {  // every staged wavelength in the layer's cubic regime
 #pragma unroll 4
                         for (int jj = jr; jj < nw; jj += NJ) {
                             const R g = R(gb[jj * Ls]);
@@ -924,11 +947,20 @@ __global__ void __launch_bounds__(512, MIXED ? 2 : 1) line_adj_kernel(LineAdjArg
             // window sums of this thread: central + wing (from the moments)
             double v3[3] = {0.0, 0.0, 0.0};
             if (active) {
-                const double k = 0.5641895835477563 * double(av);  // a / sqrt(pi)
+                // moments M_k = sum G u^k = rho^k S_k; with H = (c1 u + c2 u^2 + c3 u^3)/sqrt(pi)
+                // (adj_fl_cubic_x) and v d/dv u^k = -2k u^k:
+                //   sum G H = sum_k c_k M_k / sqrt(pi),  sum G H_a = sum_k c_k' M_k / sqrt(pi),
+                //   sum G (a H_a + v H_v) = sum_k (a c_k' - 2k c_k) M_k / sqrt(pi)
+                const double A = double(av), A2 = A * A;
+                const bool fl = MIXED && A > 0.2;
+                const double c1 = A, c2 = fl ? A * (1.5 - A2) : 1.5 * A,
+                             c3 = fl ? A * (3.75 + A2 * (A2 - 5.0)) : 3.75 * A;
+                const double d1 = 1.0, d2 = fl ? 1.5 - 3.0 * A2 : 1.5, d3 = fl ? 3.75 + A2 * (5.0 * A2 - 15.0) : 3.75;
                 const double M1 = rho * mom.get(0), M2 = rho * rho * mom.get(1), M3 = rho * rho * rho * mom.get(2);
-                const double wA = 0.5641895835477563 * (M1 + 1.5 * M2 + 3.75 * M3);
-                const double wH = k * (M1 + 1.5 * M2 + 3.75 * M3);
-                const double wX = wH - 2 * k * (M1 + 3 * M2 + 11.25 * M3);
+                const double isp = 0.5641895835477563;  // 1/sqrt(pi)
+                const double wH = isp * (c1 * M1 + c2 * M2 + c3 * M3);
+                const double wA = isp * (d1 * M1 + d2 * M2 + d3 * M3);
+                const double wX = isp * ((A * d1 - 2 * c1) * M1 + (A * d2 - 4 * c2) * M2 + (A * d3 - 6 * c3) * M3);
                 v3[0] = cen.get(0) + wH;
                 v3[1] = cen.get(1) + wX;
                 v3[2] = cen.get(2) + wA;
