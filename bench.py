@@ -481,6 +481,34 @@ def cpu_sample_batch(inp, threads):
                                "spectra/s = fraction / seconds")
 
 
+def batch_gradient(b, stream, t_forward_ms, steps=1):
+    """Forward + rectified-flux loss + gradient of every spectrum of a batch, reusing the batched
+    forward's opacity (korg_synthesize_batch_vjp_dev), against the batched forward alone."""
+    import numpy as np
+    import torch
+    f, c = b.run(stream)
+    torch.cuda.synchronize()
+    noise = torch.as_tensor(np.random.default_rng(5).normal(0, 0.01, (b.n, b.nwl)), device=b.dev)
+    obs = (f / c) * (1 + noise)
+    times = []
+    for _ in range(steps + 1):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        f, c = b.run(stream)
+        rr = f / c - obs
+        dF, dC = 2 * rr / c, -2 * rr * f / c ** 2
+        b.vjp(dF, dC, reuse_forward=True, stream=stream)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    t = statistics.mean(times[1:])
+    return {"forward_and_gradient_ms": t, "forward_ms": t_forward_ms,
+            "gradient_over_forward": (t - t_forward_ms) / t_forward_ms,
+            "note": "batched forward (graph replay), loss, then korg_synthesize_batch_vjp_dev reusing the forward's "
+                    "opacity for every spectrum; gradient w.r.t. T, ne, n_eff_vdW, xi, n/U, log gf, continuum, "
+                    "H-line inputs (hydrogen by forward differences)"}
+
+
 def _progress(msg, t0=time.perf_counter()):
     print(f"[bench {time.perf_counter() - t0:8.1f} s] {msg}", file=sys.stderr, flush=True)
 
@@ -571,6 +599,11 @@ def run_batch(args):
             "mixed_max_rectified_err": float(np.max(np.abs(fm / cm - f64 / c64))),
             "mixed_rectified_rms": float(np.sqrt(np.mean((fm / cm - f64 / c64) ** 2)))}
     _progress("FP64 comparison done")
+    grad = None
+    if not args.no_adjoint:
+        b.ctx.check(b.ctx.lib.korg_set_batch_options(b.ctx.h, 1, 1, 160 << 30))
+        grad = batch_gradient(b, stream, ms)
+        _progress(f"batch gradient done: {grad['forward_and_gradient_ms']:.0f} ms")
     cpu = None
     if not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -593,6 +626,7 @@ def run_batch(args):
         "evals_per_step": evals, "evals_per_s": evals / (ms * 1e-3),
         "stages_ms": {"total_eager": st.ms_total, "line_tile_queue": st.ms_line_tile, "rt_all": st.ms_rt},
         "fp64": fp64,
+        "gradient": grad,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
                      "frac": achieved / peak.value, "traffic": None,
                      "kernel": "line_tile_queue_kernel<mixed> (one persistent launch over the batch)",
@@ -745,6 +779,8 @@ def run_variants(args):
     e1.synchronize()
     t64 = e0.elapsed_time(e1)
     f64, c64 = one.results()
+    one.ctx.close()
+    grad = None if args.no_adjoint else batch_gradient(b, stream, ms)
     out = {"metric": METRIC, "value": 16 * 1000.0 / ms, "unit": "spectra/s", "n_gpus": 1, "steps": args.steps,
            "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32 profiles + f64 tau/flux (mixed)",
@@ -757,7 +793,7 @@ def run_variants(args):
            "fp64": {"spectra_per_s": 1000.0 / t64, "mixed_speedup": (t64 / 1.0) / (ms / 16),
                     "mixed_max_rel_flux_err": float(np.max(np.abs(fm[0] / f64[0] - 1))),
                     "mixed_rectified_rms": float(np.sqrt(np.mean((fm[0] / cm[0] - f64[0] / c64[0]) ** 2)))},
-           "clocks": clocks}
+           "gradient": grad, "clocks": clocks}
     print(json.dumps(out), flush=True)
 
 

@@ -332,6 +332,23 @@ typedef struct {
 } korg_batch_item;
 KORG_API int korg_synthesize_batch_dev(korg_ctx *ctx, int32_t nspec, const korg_batch_item *items,
                                        const double *wls, int64_t nwl, int precision, void *stream);
+/* Reverse mode of a batch: korg_synthesize_vjp_dev for every spectrum of a batch, as the Fit
+ * module's gradient over many atmospheres or abundance sets needs (src/Fit/fit_via_synthesis.jl:
+ * 345-355 takes that Jacobian with ForwardDiff through synthesize).  cot[i] holds spectrum i's
+ * cotangents (device arrays of nwl; either may be NULL) and its gradient outputs (device
+ * pointers, as in korg_synthesize_vjp).  With KORG_VJP_REUSE_FORWARD the previous batch call on
+ * the context was korg_synthesize_batch_dev of the same items and ran in one chunk (the default
+ * budget holds 256 spectra of 56 x 400,001): every spectrum's opacity, alpha_ref and line
+ * prologue are taken from it instead of recomputed, else KORG_EINVAL.  KORG_VJP_HYDROGEN as in
+ * korg_synthesize_vjp.  Gradients equal korg_synthesize_vjp_dev's for each spectrum (up to the
+ * order of the FP64 atomic additions of the line adjoint). */
+typedef struct {
+    const double *dflux, *dcntm;
+    korg_synth_grads grads;
+} korg_batch_vjp_item;
+KORG_API int korg_synthesize_batch_vjp_dev(korg_ctx *ctx, int32_t nspec, const korg_batch_item *items,
+                                           const korg_batch_vjp_item *cot, const double *wls, int64_t nwl,
+                                           int precision, int flags, void *stream);
 /* Batch options (no counterpart in the reference).  use_graph: a batch submitted twice in a row
  * with identical items (same pointers and sizes; the contents may change) is captured into a
  * CUDA graph on the second submission and replayed from then on.  autotune: the first large

@@ -69,6 +69,13 @@ struct korg_ctx {
     size_t b_host_cap = 0;
     cudaEvent_t b_host_ev = nullptr;  // after the last copy out of b_host
     int64_t batch_budget = int64_t(32) << 30;
+    // the last batch: its key, whether it ran in one chunk (then every spectrum's alpha, line
+    // prologue and alpha_ref stay in b_alpha / b_lines / b_meta until the next batch), and where
+    // the per-spectrum pieces lie -- for a batched reverse mode that reuses the forward's opacity
+    std::vector<unsigned char> b_last_key;
+    bool b_last_resident = false;
+    std::vector<size_t> b_last_line_off;
+    size_t b_last_o_aref = 0, b_last_o_refwl = 0;
     // CUDA graph of the last batch: replayed while the same batch is submitted again
     bool use_graph = false, capturing = false;
     cudaGraphExec_t gexec = nullptr;
@@ -751,9 +758,16 @@ __global__ void hfd_perturb_kernel(HLayers src, int which, double rel, double si
     }
 }
 
+// Opacity of a spectrum of the last batch forward, still in the batch buffers.
+struct VjpOpacity {
+    double* alpha;
+    double* aref;
+    unsigned char* lines;  // the spectrum's line scratch (prologue constants, windows, tiers)
+};
+
 int run_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& ln, const LinesDev& ln5, const double* wls,
             int64_t nwl, bool mixed, const double* dflux, const double* dcntm, const korg_synth_grads& gr, int flags,
-            const double* ref_wl_dev, cudaStream_t s) {
+            const double* ref_wl_dev, cudaStream_t s, const VjpOpacity* op = nullptr) {
     const LayersDev lay = layers_dev(&in->layers);
     const int L = lay.L, S = lay.S;
     if (L > RTA_LMAX) return set_err(ctx, KORG_EINVAL, "the adjoint supports at most %d layers", RTA_LMAX);
@@ -802,11 +816,11 @@ int run_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& ln, cons
     //    states that the previous call on this context was korg_synthesize[_dev] of the same
     //    inputs, whose alpha, alpha_ref and metal-line prologue are still in the scratch
     record(ctx, 8, s);
-    double* alpha = static_cast<double*>(ctx->alpha.p);
-    double* aref = static_cast<double*>(ctx->aref.p);
+    double* alpha = op ? op->alpha : static_cast<double*>(ctx->alpha.p);
+    double* aref = op ? op->aref : static_cast<double*>(ctx->aref.p);
     const CntmDev cref{1, nullptr, in->alpha_ref_cntm};
     const HLayers hl{L, lay.T, lay.ne, in->nH_I, in->nHe_I, in->UH_I, lay.xi};
-    if (!(flags & KORG_VJP_REUSE_FORWARD)) {
+    if (!(flags & KORG_VJP_REUSE_FORWARD) && !op) {
         alpha_init_kernel<<<unsigned((nwl + 63) / 64), 256, 0, s>>>(alpha, wls, nwl, L, cn);
         KCUDA(cudaGetLastError());
         KCUDA(cudaMemcpyAsync(aref, in->alpha_ref_cntm, sizeof(double) * L, cudaMemcpyDeviceToDevice, s));
@@ -815,6 +829,9 @@ int run_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& ln, cons
             KCHECK(run_hydrogen(ctx, alpha, wls, nwl, hl, in->hydrogen_window, in->use_MHD, mixed, s));
         KCHECK(run_line_absorption(ctx, alpha, wls, nwl, ln, lay, cn, in->cutoff_threshold, mixed, s));
     }
+    // the metal-line prologue: the batch's for this spectrum, else the context's line scratch (read
+    // after step 1, which may have grown it)
+    unsigned char* line_base = op ? op->lines : static_cast<unsigned char*>(ctx->lines_scratch.p);
     record(ctx, 9, s);
 
     // 2. transfer adjoint: opacity cotangent G, dL/dT through the source function, dL/dalpha_ref
@@ -892,8 +909,8 @@ int run_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& ln, cons
 
     // 4. metal and molecular lines: window sums per (line, layer), then the prologue chain rule
     const LineAdjOut lo{dT, gr.ne, gr.n_eff_vdW, gr.xi, gr.n_div_U, gr.log_gf};
-    auto line_adjoint = [&](const LinesDev& lns, const void* Gp, int g32_in, const double* w, int64_t nw,
-                            const LineAdjOut& out) -> int {
+    auto line_adjoint = [&](const LinesDev& lns, unsigned char* scratch, const void* Gp, int g32_in, const double* w,
+                            int64_t nw, const LineAdjOut& out) -> int {
         if (lns.n == 0) return KORG_OK;
         if (mixed && !g32_in) {  // the mixed kernel stages float G: convert (a few values)
             float* g32buf = reinterpret_cast<float*>(sm + o_g32);
@@ -904,7 +921,7 @@ int run_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& ln, cons
             g32_in = 1;
         }
         LineScratch sc;
-        line_scratch(static_cast<unsigned char*>(ctx->lines_scratch.p), lns.n, L, Lp, G, mixed, &sc);
+        line_scratch(scratch, lns.n, L, Lp, G, mixed, &sc);
         double* dpar = static_cast<double*>(ctx->vjp_dpar.p);
         KCUDA(cudaMemsetAsync(dpar, 0, sizeof(double) * 3 * size_t(lns.n) * Lp, s));
         KCUDA(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), s));
@@ -943,7 +960,7 @@ int run_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& ln, cons
         return KORG_OK;
     };
     // the metal-line prologue of step 1 is still in the line scratch
-    KCHECK(line_adjoint(ln, ctx->vjp_g.p, int(mixed), wls, nwl, lo));
+    KCHECK(line_adjoint(ln, line_base, ctx->vjp_g.p, int(mixed), wls, nwl, lo));
     // 5. reference-wavelength lines: alpha_ref = continuum + lines at ref_wl, cotangent daref
     if (ln5.n > 0) {
         LineScratch sc;
@@ -951,7 +968,7 @@ int run_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& ln, cons
         line_scratch(static_cast<unsigned char*>(ctx->lines_scratch.p), ln5.n, L, Lp, G, mixed, &sc);
         KCHECK(prep_lines(ctx, sc, ref_wl_dev, 1, ln5, lay, cref, in->cutoff_threshold, mixed, kmax, G, s));
         const LineAdjOut lo5{dT, gr.ne, gr.n_eff_vdW, gr.xi, gr.n_div_U, nullptr};
-        KCHECK(line_adjoint(ln5, daref, 0, ref_wl_dev, 1, lo5));
+        KCHECK(line_adjoint(ln5, static_cast<unsigned char*>(ctx->lines_scratch.p), daref, 0, ref_wl_dev, 1, lo5));
     }
     if (gr.alpha_ref_cntm)
         KCUDA(cudaMemcpyAsync(gr.alpha_ref_cntm, daref, sizeof(double) * L, cudaMemcpyDeviceToDevice, s));
@@ -1925,6 +1942,59 @@ KORG_API int korg_interpolate_molecular_cross_section_dev(korg_ctx* ctx, double*
     return KORG_OK;
 }
 
+KORG_API int korg_synthesize_batch_vjp_dev(korg_ctx* ctx, int32_t nspec, const korg_batch_item* items,
+                                           const korg_batch_vjp_item* cot, const double* wls, int64_t nwl,
+                                           int precision, int flags, void* stream) {
+    if (!ctx) return KORG_EINVAL;
+    KPREC(precision);
+    if (nspec < 1 || !items || !cot || !wls || nwl < 1 || nwl > INT32_MAX - 1)
+        return set_err(ctx, KORG_EINVAL, "bad batch arguments");
+    const int L = items[0].in.layers.L;
+    int64_t nmax = 1;
+    for (int i = 0; i < nspec; i++) {
+        const korg_batch_item& b = items[i];
+        if (b.in.layers.L != L || b.in.cntm.nk < 2 || (!cot[i].dflux && !cot[i].dcntm))
+            return set_err(ctx, KORG_EINVAL, "bad batch item %d", i);
+        if (b.in.hydrogen_lines && !ctx->have_stark)
+            return set_err(ctx, KORG_ENOTABLES, "korg_set_stark_tables() has not been called");
+        nmax = std::max<int64_t>(nmax, std::max<int64_t>(b.lines.n, b.lines5.n));
+    }
+    KCUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const bool mixed = precision == KORG_MIXED;
+    const bool reuse = flags & KORG_VJP_REUSE_FORWARD;
+    if (reuse && (!ctx->b_last_resident || ctx->b_last_key != batch_key(ctx, nspec, items, wls, nwl, precision)))
+        return set_err(ctx, KORG_EINVAL,
+                       "KORG_VJP_REUSE_FORWARD needs the previous batch call to be korg_synthesize_batch_dev of the "
+                       "same items, run in one chunk (raise max_scratch_bytes)");
+    // scratch sized once for the largest spectrum, so no spectrum grows it (a growth synchronises)
+    int kmax = 0;
+    const int G = layer_groups(L, &kmax);
+    if (G < 0) return set_err(ctx, KORG_EINVAL, "at most 256 layers are supported (got %d)", L);
+    KCHECK(ensure(ctx, ctx->vjp_dpar, sizeof(double) * 3 * size_t(nmax) * size_t(G * kmax)));
+    KCHECK(ensure(ctx, ctx->aref, sizeof(double) * (L + 1)));
+    unsigned char* meta = static_cast<unsigned char*>(ctx->b_meta.p);
+    for (int i = 0; i < nspec; i++) {
+        const korg_batch_item& b = items[i];
+        const double* ref_wl_dev;
+        VjpOpacity op{};
+        if (reuse) {
+            op.alpha = static_cast<double*>(ctx->b_alpha.p) + size_t(i) * (a256(8 * size_t(L) * nwl) / 8);
+            op.aref = reinterpret_cast<double*>(meta + ctx->b_last_o_aref) + size_t(i) * L;
+            op.lines = static_cast<unsigned char*>(ctx->b_lines.p) + ctx->b_last_line_off[i];
+            ref_wl_dev = reinterpret_cast<const double*>(meta + ctx->b_last_o_refwl) + i;
+        } else {
+            double* aref = static_cast<double*>(ctx->aref.p);
+            KCUDA(cudaMemcpyAsync(aref + L, &b.in.ref_wl, sizeof(double), cudaMemcpyHostToDevice, s));
+            ref_wl_dev = aref + L;
+        }
+        KCHECK(run_vjp(ctx, &b.in, lines_dev(&b.lines), lines_dev(&b.lines5), wls, nwl, mixed, cot[i].dflux,
+                       cot[i].dcntm, cot[i].grads, flags & ~KORG_VJP_REUSE_FORWARD, ref_wl_dev, s,
+                       reuse ? &op : nullptr));
+    }
+    return KORG_OK;
+}
+
 KORG_API int korg_set_batch_options(korg_ctx* ctx, int use_graph, int autotune, int64_t max_scratch_bytes) {
     if (!ctx) return KORG_EINVAL;
     if (max_scratch_bytes < 0) return set_err(ctx, KORG_EINVAL, "negative scratch budget");
@@ -1978,8 +2048,9 @@ KORG_API int korg_synthesize_batch_dev(korg_ctx* ctx, int32_t nspec, const korg_
         KCUDA(cudaGraphLaunch(ctx->gexec, us));
         KCUDA(cudaEventRecord(ctx->b_host_ev, us));
         ctx->stats_pending = true;
-        return KORG_OK;
+        return KORG_OK;  // the plan of the captured batch (b_last_*) still holds
     }
+    ctx->b_last_key.clear();
     BatchPlan p;
     KCHECK(plan_batch(ctx, nspec, items, nwl, mixed, &p));
     if (ctx->autotune && !ctx->tuned.count(std::make_pair(p.L, int(mixed)))) {
@@ -2045,6 +2116,11 @@ KORG_API int korg_synthesize_batch_dev(korg_ctx* ctx, int32_t nspec, const korg_
         if (ctx->use_graph) ctx->pending_key = key;
     }
     KCUDA(cudaEventRecord(ctx->b_host_ev, us));
+    ctx->b_last_key = key;
+    ctx->b_last_resident = p.chunk_first.size() == 2;
+    ctx->b_last_line_off = p.line_off;
+    ctx->b_last_o_aref = p.o_aref;
+    ctx->b_last_o_refwl = p.o_refwl;
     return KORG_OK;
 }
 

@@ -70,6 +70,11 @@ class BatchItem(C.Structure):
     _fields_ = [("inp", SynthInputs), ("lines", Lines), ("lines5", Lines), ("flux", _dp), ("cntm", _dp)]
 
 
+class BatchVjpItem(C.Structure):
+    """korg_batch_vjp_item: one spectrum's cotangents and gradient outputs (device pointers)."""
+    _fields_ = [("dflux", _dp), ("dcntm", _dp), ("grads", SynthGrads)]
+
+
 class Stats(C.Structure):
     _fields_ = [("line_evals", C.c_int64), ("lines_in_window", C.c_int64), ("ms_ref_lines", C.c_float),
                 ("ms_hydrogen", C.c_float), ("ms_line_prep", C.c_float), ("ms_line_tile", C.c_float),
@@ -128,6 +133,8 @@ def lib():
             L.korg_synthesize_vjp_dev.argtypes = [vp, C.POINTER(SynthInputs), C.POINTER(Lines), C.POINTER(Lines), vp,
                                                   C.c_int64, C.c_int, vp, vp, C.POINTER(SynthGrads), C.c_int, vp]
             L.korg_synthesize_batch_dev.argtypes = [vp, C.c_int32, C.POINTER(BatchItem), vp, C.c_int64, C.c_int, vp]
+            L.korg_synthesize_batch_vjp_dev.argtypes = [vp, C.c_int32, C.POINTER(BatchItem), C.POINTER(BatchVjpItem),
+                                                        vp, C.c_int64, C.c_int, C.c_int, vp]
             L.korg_set_batch_options.argtypes = [vp, C.c_int, C.c_int, C.c_int64]
             L.korg_get_tile_config.argtypes = [vp, C.c_int32, C.c_int, _ip, _ip, _ip, _ip]
             L.korg_set_tile_config.argtypes = [vp, C.c_int32, C.c_int, C.c_int32, C.c_int32, C.c_int32]
@@ -152,7 +159,7 @@ def exported_symbols():
             "korg_hydrogen_line_absorption", "korg_hydrogen_lines_dev", "korg_radiative_transfer",
             "korg_radiative_transfer_dev", "korg_synthesize", "korg_synthesize_dev", "korg_probe_flops",
             "korg_math_selftest", "korg_line_absorption_noalloc", "korg_synthesize_batch_dev",
-            "korg_set_batch_options", "korg_get_tile_config", "korg_set_tile_config", "korg_synthesize_vjp", "korg_synthesize_vjp_dev",
+            "korg_synthesize_batch_vjp_dev", "korg_set_batch_options", "korg_get_tile_config", "korg_set_tile_config", "korg_synthesize_vjp", "korg_synthesize_vjp_dev",
             "korg_radiative_transfer_general", "korg_molecular_cross_section_dev",
             "korg_interpolate_molecular_cross_section_dev", "korg_device_status",
             "korg_selftest_wait_timeout", "korg_apply_lsf_dev", "korg_apply_lsf_vjp_dev", "korg_lsf_windows_dev",

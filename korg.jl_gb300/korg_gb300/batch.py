@@ -131,6 +131,33 @@ class BatchSynthesis:
                                                               self.prec, stream.cuda_stream))
         return self.flux, self.cntm
 
+    def vjp(self, dflux, dcntm=None, hydrogen=True, reuse_forward=True, stream=None):
+        """Reverse mode of the batch (korg_synthesize_batch_vjp_dev): for every spectrum k the
+        gradient of sum(dflux[k] * flux[k] + dcntm[k] * cntm[k]) with respect to its hot-path
+        inputs, as a list of dicts of device tensors keyed like api.GRAD_FIELDS (T, ne, n_eff_vdW,
+        xi, nH_I, nHe_I, UH_I [L]; n_div_U [S, L]; log_gf [lines]; cntm_vals [L, nk];
+        alpha_ref_cntm [L]).  dflux, dcntm: device tensors (n, nwl) or None.  reuse_forward: the
+        last call was run() of this batch (in one chunk), whose opacity is reused."""
+        from .api import GRAD_FIELDS
+        torch = self.torch
+        stream = stream or torch.cuda.current_stream(self.dev)
+        L = len(self.inputs[0].T)
+        out, cot = [], (_lib.BatchVjpItem * self.n)()
+        keep = [dflux, dcntm]
+        for k, inp in enumerate(self.inputs):
+            shapes = {"n_div_U": inp.n_div_U.shape, "log_gf": (len(inp.linelist),), "cntm_vals": inp.cntm_vals.shape}
+            g = {f: torch.zeros(shapes.get(f, (L,)), dtype=torch.float64, device=self.dev) for f in GRAD_FIELDS}
+            out.append(g)
+            ptr = lambda t: C.cast(t.data_ptr(), _lib._dp)
+            cot[k] = _lib.BatchVjpItem(None if dflux is None else C.cast(dflux[k].data_ptr(), _lib._dp),
+                                       None if dcntm is None else C.cast(dcntm[k].data_ptr(), _lib._dp),
+                                       _lib.SynthGrads(*[ptr(g[f]) for f in GRAD_FIELDS]))
+        flags = (_lib.KORG_VJP_HYDROGEN if hydrogen else 0) | (_lib.KORG_VJP_REUSE_FORWARD if reuse_forward else 0)
+        self.ctx.check(self.ctx.lib.korg_synthesize_batch_vjp_dev(self.ctx.h, self.n, self.items, cot, self.wls_ptr,
+                                                                  self.nwl, self.prec, flags, stream.cuda_stream))
+        self._vjp_keep = (keep, cot)
+        return out
+
     def results(self):
         self.torch.cuda.synchronize(self.dev)
         return self.flux.cpu().numpy(), self.cntm.cpu().numpy()

@@ -118,3 +118,35 @@ def test_tile_shapes_give_identical_opacity(gpu_lib, precision):
         ctx = gpu_lib.Context(0)
         assert ctx.lib.korg_set_tile_config(ctx.h, L, prec, 64, 0, 0) == 1  # all groups per CTA: mixed has none
         ctx.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_vjp_equals_per_spectrum_vjp(gpu_lib, precision):
+    """korg_synthesize_batch_vjp_dev, reusing the batched forward's opacity and recomputing it,
+    gives every spectrum the gradients of korg_synthesize_vjp (the same kernels: equal up to the
+    order of the line adjoint's FP64 atomic additions)."""
+    from korg_gb300.api import GRAD_FIELDS, synthesize_vjp
+    from korg_gb300.batch import BatchSynthesis
+    inps = _inputs([(5000.0, 4.4, 800, 7), (4200.0, 2.0, 500, 8), (6500.0, 4.0, 300, 9)])
+    b = BatchSynthesis(inps, precision=precision, use_graph=False)
+    torch = b.torch
+    rng = np.random.default_rng(3)
+    dF = torch.as_tensor(rng.normal(size=(len(inps), b.nwl)), device=b.dev)
+    dC = torch.as_tensor(rng.normal(size=(len(inps), b.nwl)), device=b.dev)
+    b.run()
+    g_reuse = b.vjp(dF, dC, reuse_forward=True)
+    g_recomp = b.vjp(dF, dC, reuse_forward=False)
+    torch.cuda.synchronize()
+    tol = 1e-12 if precision == "fp64" else 1e-9
+    for k, inp in enumerate(inps):
+        ref = synthesize_vjp(inp, dF[k].cpu().numpy(), dC[k].cpu().numpy(), precision=precision, ctx=b.ctx)
+        for f in GRAD_FIELDS:
+            scale = max(float(np.max(np.abs(ref[f]))), 1e-300)
+            for name, g in (("reuse", g_reuse), ("recompute", g_recomp)):
+                got = g[k][f].cpu().numpy().reshape(ref[f].shape)
+                assert np.max(np.abs(got - ref[f])) <= tol * scale, (k, f, name)
+    # reuse needs the batch forward of the same items just before
+    other = BatchSynthesis(inps[:2], precision=precision, use_graph=False, ctx=b.ctx)
+    other.run()
+    with pytest.raises(gpu_lib.KorgError):
+        b.vjp(dF, dC, reuse_forward=True)
