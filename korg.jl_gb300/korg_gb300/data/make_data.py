@@ -111,7 +111,9 @@ def alpha5000(root):
 
 
 if __name__ == "__main__":
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("KORG_REFERENCE")
+    if not root:
+        sys.exit("usage: make_data.py /path/to/Korg.jl  (or set KORG_REFERENCE)")
     stark(root)
     partition(root)
     alpha5000(root)

@@ -19,7 +19,9 @@ from korg_gb300 import hdf5lite  # noqa: E402
 from korg_gb300.data import default_partition_funcs  # noqa: E402
 from korg_gb300.species import parse_species  # noqa: E402
 
-root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("KORG_REFERENCE")
+if not root:
+    sys.exit("usage: make_golden.py /path/to/Korg.jl  (or set KORG_REFERENCE)")
 f = hdf5lite.File(os.path.join(root, "test", "data", "lyman_absorption.h5"))
 a = f["profile"].attrs
 U = default_partition_funcs()[parse_species("H I")](np.log(9000.0))

@@ -40,9 +40,11 @@ def test_cubic_spline_natural():
 
 def test_hdf5_reader_golden_attributes():
     from korg_gb300 import hdf5lite
-    path = "/root/reference/test/data/lyman_absorption.h5"
+    # the reference checkout, if present: KORG_REFERENCE, else a sibling of this repository
+    root = os.environ.get("KORG_REFERENCE", os.path.join(os.path.dirname(ROOT), "reference"))
+    path = os.path.join(root, "test", "data", "lyman_absorption.h5")
     if not os.path.exists(path):
-        pytest.skip("reference data not present")
+        pytest.skip("reference data not present (set KORG_REFERENCE to a Korg.jl checkout)")
     f = hdf5lite.File(path)
     g = np.load(os.path.join(ROOT, "tests", "golden", "lyman_absorption.npz"))
     np.testing.assert_array_equal(f.read("profile"), g["profile"])
