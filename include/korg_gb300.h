@@ -133,6 +133,54 @@ KORG_API int korg_set_timing(korg_ctx *ctx, int enabled);
 /* Uploads the Stehle & Hutcheon tables once (src/hydrogen_line_absorption.jl:38-39). */
 KORG_API int korg_set_stark_tables(korg_ctx *ctx, const korg_stark_tables *host_tables);
 
+/* Continuum absorption, total_continuum_absorption(nus, T, ne, number_densities, partition_funcs)
+ * (src/ContinuumAbsorption/ContinuumAbsorption.jl:39-74) as synthesize evaluates it per layer on
+ * the continuum grid (src/synthesize.jl:211-237): H I bound-free (with MHD level dissolution),
+ * H- bound-free and free-free, H2+ bound-free and free-free, He- free-free, free-free of every
+ * positive ion (hydrogenic with van Hoof Gaunt factors, Peach departure coefficients for He II,
+ * C II, Si II and Mg II), Thomson and Rayleigh scattering.  Metal bound-free absorption
+ * (absorption_metals_bf.jl) is not included: its cross-section tables are not distributed with
+ * the reference.  FP64.
+ *
+ * korg_set_continuum_tables uploads the reference's tables once (sizes, host arrays, row-major):
+ * H I bf cross-sections of levels 1..6 on energy grids [6][h_n] (eV, megabarn); H- bf [hm_n]
+ * (Hz, cm^2); H- ff and He- ff K [nl][nt] in 1e-26 cm^4/dyn over wavelength (A) and theta =
+ * 5040/T; H2+ K(T) [nT] and cross-sections [n][nT] (bf 1e-18 cm^2, ff 1e-39 cm^5) over
+ * wavelength (A); free-free Gaunt factors [nu][ng] over log10 u and log10 gamma^2; Peach
+ * departure coefficients D [nT][ns] over T and sigma, for He II, C II, Si II, Mg II in order. */
+typedef struct {
+    int32_t h_n;
+    const double *h_E, *h_sigma;
+    int64_t hm_n;
+    const double *hm_nu, *hm_sigma;
+    int32_t hff_nl, hff_nt;
+    const double *hff_lambda, *hff_theta, *hff_K;
+    int32_t heff_nl, heff_nt;
+    const double *heff_lambda, *heff_theta, *heff_K;
+    int32_t h2_nT, h2_nbf, h2_nff;
+    const double *h2_T, *h2_K, *h2_bf_lambda, *h2_bf_sigma, *h2_ff_lambda, *h2_ff_sigma;
+    int32_t g_nu, g_ng;
+    const double *g_log_u, *g_log_g2, *g_ff;
+    int32_t p_nT[4], p_ns;
+    const double *p_T[4], *p_sigma, *p_D[4];
+} korg_continuum_tables;
+/* Per-layer inputs [L] (the host's chemical equilibrium): n(H I), n(H II), n(He I), n(H2),
+ * n(H-), 1/U(H I, T) and 1/U(He I, T), n_Z1 / n_Z2 = summed densities of the other singly /
+ * doubly charged species (H II included), n_peach = n(He II), n(C II), n(Si II), n(Mg II). */
+typedef struct {
+    int32_t L;
+    const double *T, *ne, *nH_I, *nH_II, *nHe_I, *nH2, *nH_minus, *invU_H_I, *invU_He_I, *n_Z1, *n_Z2;
+    const double *n_peach[4];
+} korg_continuum_layers;
+KORG_API int korg_set_continuum_tables(korg_ctx *ctx, const korg_continuum_tables *host_tables);
+/* vals[l * nwl + j] = continuum absorption (cm^-1) of layer l at wls[j] (cm), the layout of
+ * korg_cntm.vals.  _dev: device pointers (wls, layer arrays, vals), stream-ordered. */
+KORG_API int korg_continuum_absorption(korg_ctx *ctx, const double *wls, int64_t nwl,
+                                       const korg_continuum_layers *layers, double *vals);
+KORG_API int korg_continuum_absorption_dev(korg_ctx *ctx, const double *wls, int64_t nwl,
+                                           const korg_continuum_layers *layers, double *vals,
+                                           void *stream);
+
 /* line_absorption!(alpha, linelist, wls, temps, ne, n_densities, partition_fns, xi, alpha_cntm;
  * cutoff_threshold) -- src/line_absorption.jl:33-129.  alpha (host, L x nwl) is accumulated in
  * place; an empty line list leaves it untouched (line_absorption.jl:35-37).  n_evals may be

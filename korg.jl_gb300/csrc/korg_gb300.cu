@@ -18,6 +18,7 @@
 
 #include "../../include/korg_gb300.h"
 #include "adjoint.cuh"
+#include "continuum.cuh"
 #include "hydrogen.cuh"
 #include "lines.cuh"
 #include "postprocess.cuh"
@@ -84,6 +85,10 @@ struct korg_ctx {
     bool autotune = false;
     std::map<std::pair<int, int>, TileCfg> tuned;
     std::vector<TuneRecord> tune_log;
+    // continuum-absorption tables (one device buffer)
+    bool have_cntm = false;
+    CntmTables cntm_tab{};
+    void* cntm_buf = nullptr;
     // Stehle tables
     bool have_stark = false;
     StarkDev stark{};
@@ -1236,6 +1241,7 @@ KORG_API void korg_destroy(korg_ctx* ctx) {
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
     for (void* p : ctx->stark_allocs) cudaFree(p);
+    if (ctx->cntm_buf) cudaFree(ctx->cntm_buf);
     if (ctx->stage_host) cudaFreeHost(ctx->stage_host);
     if (ctx->b_host) cudaFreeHost(ctx->b_host);
     if (ctx->dev_err_host) cudaFreeHost(ctx->dev_err_host);
@@ -1342,6 +1348,133 @@ KORG_API int korg_set_stark_tables(korg_ctx* ctx, const korg_stark_tables* t) {
     ctx->stark = d;
     ctx->n_max = n_max;
     ctx->have_stark = true;
+    return KORG_OK;
+}
+
+// ------------------------------------------------------------------ continuum absorption
+KORG_API int korg_set_continuum_tables(korg_ctx* ctx, const korg_continuum_tables* t) {
+    if (!ctx) return KORG_EINVAL;
+    if (!t || t->h_n < 2 || t->hm_n < 2 || t->hff_nl < 2 || t->hff_nt < 2 || t->heff_nl < 2 || t->heff_nt < 2 ||
+        t->h2_nT < 2 || t->h2_nbf < 2 || t->h2_nff < 2 || t->g_nu < 2 || t->g_ng < 2 || t->p_ns < 2)
+        return set_err(ctx, KORG_EINVAL, "bad continuum tables");
+    for (int k = 0; k < CNT_PEACH; k++)
+        if (t->p_nT[k] < 2 || !t->p_T[k] || !t->p_D[k]) return set_err(ctx, KORG_EINVAL, "bad Peach table %d", k);
+    KCUDA(cudaSetDevice(ctx->device));
+    struct Piece { const double* src; size_t n; const double** dst; };
+    CntmTables d{};
+    d.h_n = t->h_n; d.hm_n = t->hm_n; d.hff_nl = t->hff_nl; d.hff_nt = t->hff_nt; d.heff_nl = t->heff_nl;
+    d.heff_nt = t->heff_nt; d.h2_nT = t->h2_nT; d.h2_nbf = t->h2_nbf; d.h2_nff = t->h2_nff; d.g_nu = t->g_nu;
+    d.g_ng = t->g_ng; d.p_ns = t->p_ns;
+    std::vector<Piece> pcs = {
+        {t->h_E, size_t(6) * t->h_n, &d.h_E}, {t->h_sigma, size_t(6) * t->h_n, &d.h_sigma},
+        {t->hm_nu, size_t(t->hm_n), &d.hm_nu}, {t->hm_sigma, size_t(t->hm_n), &d.hm_sigma},
+        {t->hff_lambda, size_t(t->hff_nl), &d.hff_lambda}, {t->hff_theta, size_t(t->hff_nt), &d.hff_theta},
+        {t->hff_K, size_t(t->hff_nl) * t->hff_nt, &d.hff_K},
+        {t->heff_lambda, size_t(t->heff_nl), &d.heff_lambda}, {t->heff_theta, size_t(t->heff_nt), &d.heff_theta},
+        {t->heff_K, size_t(t->heff_nl) * t->heff_nt, &d.heff_K},
+        {t->h2_T, size_t(t->h2_nT), &d.h2_T}, {t->h2_K, size_t(t->h2_nT), &d.h2_K},
+        {t->h2_bf_lambda, size_t(t->h2_nbf), &d.h2_bf_lambda},
+        {t->h2_bf_sigma, size_t(t->h2_nbf) * t->h2_nT, &d.h2_bf_sigma},
+        {t->h2_ff_lambda, size_t(t->h2_nff), &d.h2_ff_lambda},
+        {t->h2_ff_sigma, size_t(t->h2_nff) * t->h2_nT, &d.h2_ff_sigma},
+        {t->g_log_u, size_t(t->g_nu), &d.g_log_u}, {t->g_log_g2, size_t(t->g_ng), &d.g_log_g2},
+        {t->g_ff, size_t(t->g_nu) * t->g_ng, &d.g_ff}, {t->p_sigma, size_t(t->p_ns), &d.p_sigma}};
+    for (int k = 0; k < CNT_PEACH; k++) {
+        d.p_nT[k] = t->p_nT[k];
+        pcs.push_back({t->p_T[k], size_t(t->p_nT[k]), &d.p_T[k]});
+        pcs.push_back({t->p_D[k], size_t(t->p_nT[k]) * t->p_ns, &d.p_D[k]});
+    }
+    size_t total = 0;
+    for (const Piece& q : pcs) {
+        if (!q.src) return set_err(ctx, KORG_EINVAL, "null continuum table");
+        total += a256(8 * q.n);
+    }
+    std::vector<unsigned char> host(total);
+    size_t off = 0;
+    for (const Piece& q : pcs) {
+        memcpy(host.data() + off, q.src, 8 * q.n);
+        off += a256(8 * q.n);
+    }
+    void* buf = nullptr;
+    cudaError_t e = cudaMalloc(&buf, total);
+    if (e != cudaSuccess) return set_err(ctx, KORG_ENOMEM, "cudaMalloc(%zu): %s", total, cudaGetErrorString(e));
+    e = cudaMemcpy(buf, host.data(), total, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(buf);
+        return set_err(ctx, KORG_ECUDA, "continuum tables: %s", cudaGetErrorString(e));
+    }
+    off = 0;
+    for (const Piece& q : pcs) {
+        *q.dst = reinterpret_cast<const double*>(static_cast<unsigned char*>(buf) + off);
+        off += a256(8 * q.n);
+    }
+    if (ctx->cntm_buf) {
+        KCUDA(cudaDeviceSynchronize());
+        cudaFree(ctx->cntm_buf);
+    }
+    ctx->cntm_buf = buf;
+    ctx->cntm_tab = d;
+    ctx->have_cntm = true;
+    return KORG_OK;
+}
+
+namespace {
+CntmLayers cntm_layers(const korg_continuum_layers* y) {
+    CntmLayers c{y->L, y->T, y->ne, y->nH_I, y->nH_II, y->nHe_I, y->nH2, y->nH_minus, y->invU_H_I, y->invU_He_I,
+                 y->n_Z1, y->n_Z2, {}};
+    for (int k = 0; k < CNT_PEACH; k++) c.n_peach[k] = y->n_peach[k];
+    return c;
+}
+bool cntm_layers_ok(const korg_continuum_layers* y) {
+    if (!y || y->L < 1) return false;
+    const double* p[] = {y->T, y->ne, y->nH_I, y->nH_II, y->nHe_I, y->nH2, y->nH_minus, y->invU_H_I, y->invU_He_I,
+                         y->n_Z1, y->n_Z2, y->n_peach[0], y->n_peach[1], y->n_peach[2], y->n_peach[3]};
+    for (const double* q : p)
+        if (!q) return false;
+    return true;
+}
+}  // namespace
+
+KORG_API int korg_continuum_absorption_dev(korg_ctx* ctx, const double* wls, int64_t nwl,
+                                           const korg_continuum_layers* layers, double* vals, void* stream) {
+    if (!ctx) return KORG_EINVAL;
+    if (!wls || nwl < 1 || !vals || !cntm_layers_ok(layers)) return set_err(ctx, KORG_EINVAL, "bad arguments");
+    if (!ctx->have_cntm) return set_err(ctx, KORG_ENOTABLES, "korg_set_continuum_tables() has not been called");
+    KCUDA(cudaSetDevice(ctx->device));
+    const int64_t n = nwl * layers->L;
+    continuum_kernel<<<unsigned((n + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        ctx->cntm_tab, cntm_layers(layers), wls, nwl, vals);
+    KCUDA(cudaGetLastError());
+    return KORG_OK;
+}
+
+KORG_API int korg_continuum_absorption(korg_ctx* ctx, const double* wls, int64_t nwl,
+                                       const korg_continuum_layers* layers, double* vals) {
+    if (!ctx) return KORG_EINVAL;
+    KCHECK(check_wls(ctx, wls, nwl));
+    if (!vals || !cntm_layers_ok(layers)) return set_err(ctx, KORG_EINVAL, "bad arguments");
+    if (!ctx->have_cntm) return set_err(ctx, KORG_ENOTABLES, "korg_set_continuum_tables() has not been called");
+    KCUDA(cudaSetDevice(ctx->device));
+    const int L = layers->L;
+    Stager st;
+    const size_t o_w = st.add(wls, 8 * size_t(nwl));
+    const double* arrs[] = {layers->T, layers->ne, layers->nH_I, layers->nH_II, layers->nHe_I, layers->nH2,
+                            layers->nH_minus, layers->invU_H_I, layers->invU_He_I, layers->n_Z1, layers->n_Z2,
+                            layers->n_peach[0], layers->n_peach[1], layers->n_peach[2], layers->n_peach[3]};
+    size_t o_a[15];
+    for (int k = 0; k < 15; k++) o_a[k] = st.add(arrs[k], 8 * size_t(L));
+    const size_t o_v = st.add(nullptr, 8 * size_t(L) * nwl);
+    char* b = nullptr;
+    KCHECK(upload(ctx, st, &b));
+    korg_continuum_layers d{};
+    d.L = L;
+    const double** dst[] = {&d.T, &d.ne, &d.nH_I, &d.nH_II, &d.nHe_I, &d.nH2, &d.nH_minus, &d.invU_H_I,
+                            &d.invU_He_I, &d.n_Z1, &d.n_Z2, &d.n_peach[0], &d.n_peach[1], &d.n_peach[2],
+                            &d.n_peach[3]};
+    for (int k = 0; k < 15; k++) *dst[k] = (const double*)(b + o_a[k]);
+    KCHECK(korg_continuum_absorption_dev(ctx, (const double*)(b + o_w), nwl, &d, (double*)(b + o_v), ctx->stream));
+    KCUDA(cudaMemcpyAsync(vals, b + o_v, 8 * size_t(L) * nwl, cudaMemcpyDeviceToHost, ctx->stream));
+    KCUDA(cudaStreamSynchronize(ctx->stream));
     return KORG_OK;
 }
 

@@ -70,6 +70,25 @@ class BatchItem(C.Structure):
     _fields_ = [("inp", SynthInputs), ("lines", Lines), ("lines5", Lines), ("flux", _dp), ("cntm", _dp)]
 
 
+class ContinuumTables(C.Structure):
+    """korg_continuum_tables (host arrays)."""
+    _fields_ = [("h_n", C.c_int32), ("h_E", _dp), ("h_sigma", _dp), ("hm_n", C.c_int64), ("hm_nu", _dp),
+                ("hm_sigma", _dp), ("hff_nl", C.c_int32), ("hff_nt", C.c_int32), ("hff_lambda", _dp),
+                ("hff_theta", _dp), ("hff_K", _dp), ("heff_nl", C.c_int32), ("heff_nt", C.c_int32),
+                ("heff_lambda", _dp), ("heff_theta", _dp), ("heff_K", _dp), ("h2_nT", C.c_int32),
+                ("h2_nbf", C.c_int32), ("h2_nff", C.c_int32), ("h2_T", _dp), ("h2_K", _dp), ("h2_bf_lambda", _dp),
+                ("h2_bf_sigma", _dp), ("h2_ff_lambda", _dp), ("h2_ff_sigma", _dp), ("g_nu", C.c_int32),
+                ("g_ng", C.c_int32), ("g_log_u", _dp), ("g_log_g2", _dp), ("g_ff", _dp), ("p_nT", C.c_int32 * 4),
+                ("p_ns", C.c_int32), ("p_T", _dp * 4), ("p_sigma", _dp), ("p_D", _dp * 4)]
+
+
+class ContinuumLayers(C.Structure):
+    """korg_continuum_layers."""
+    _fields_ = [("L", C.c_int32)] + [(k, _dp) for k in ("T", "ne", "nH_I", "nH_II", "nHe_I", "nH2", "nH_minus",
+                                                          "invU_H_I", "invU_He_I", "n_Z1", "n_Z2")] + \
+               [("n_peach", _dp * 4)]
+
+
 class BatchVjpItem(C.Structure):
     """korg_batch_vjp_item: one spectrum's cotangents and gradient outputs (device pointers)."""
     _fields_ = [("dflux", _dp), ("dcntm", _dp), ("grads", SynthGrads)]
@@ -136,6 +155,9 @@ def lib():
             L.korg_synthesize_batch_vjp_dev.argtypes = [vp, C.c_int32, C.POINTER(BatchItem), C.POINTER(BatchVjpItem),
                                                         vp, C.c_int64, C.c_int, C.c_int, vp]
             L.korg_set_batch_options.argtypes = [vp, C.c_int, C.c_int, C.c_int64]
+            L.korg_set_continuum_tables.argtypes = [vp, C.POINTER(ContinuumTables)]
+            L.korg_continuum_absorption.argtypes = [vp, _dp, C.c_int64, C.POINTER(ContinuumLayers), _dp]
+            L.korg_continuum_absorption_dev.argtypes = [vp, vp, C.c_int64, C.POINTER(ContinuumLayers), vp, vp]
             L.korg_get_tile_config.argtypes = [vp, C.c_int32, C.c_int, _ip, _ip, _ip, _ip]
             L.korg_set_tile_config.argtypes = [vp, C.c_int32, C.c_int, C.c_int32, C.c_int32, C.c_int32]
             L.korg_device_status.argtypes = [vp]
@@ -163,7 +185,8 @@ def exported_symbols():
             "korg_radiative_transfer_general", "korg_molecular_cross_section_dev",
             "korg_interpolate_molecular_cross_section_dev", "korg_device_status",
             "korg_selftest_wait_timeout", "korg_apply_lsf_dev", "korg_apply_lsf_vjp_dev", "korg_lsf_windows_dev",
-            "korg_lsf_matrix_values_dev", "korg_apply_rotation_dev", "korg_apply_rotation_vjp_dev"]
+            "korg_lsf_matrix_values_dev", "korg_apply_rotation_dev", "korg_apply_rotation_vjp_dev",
+            "korg_set_continuum_tables", "korg_continuum_absorption", "korg_continuum_absorption_dev"]
 
 
 def _p(a, kind=_dp):
@@ -232,6 +255,28 @@ class Context:
             st = stark_struct(stark_profiles(), keep)
             self.check(self.lib.korg_set_stark_tables(self.h, C.byref(st)))
             self.have_stark = True
+
+    def ensure_continuum(self):
+        """Upload the continuum-absorption tables once (korg_set_continuum_tables)."""
+        if not getattr(self, "have_continuum", False):
+            from .data import continuum_tables
+            t, keep = continuum_tables(), Keep()
+            f = lambda k: _p(keep.f64(t[k]))
+            peach = ("HeII", "CII", "SiII", "MgII")
+            ct = ContinuumTables(t["H_bf_E"].shape[1], f("H_bf_E"), f("H_bf_sigma"), len(t["Hminus_bf_nu"]),
+                                 f("Hminus_bf_nu"), f("Hminus_bf_sigma"), len(t["Hminus_ff_lambda"]),
+                                 len(t["Hminus_ff_theta"]), f("Hminus_ff_lambda"), f("Hminus_ff_theta"),
+                                 f("Hminus_ff_K"), len(t["Heminus_ff_lambda"]), len(t["Heminus_ff_theta"]),
+                                 f("Heminus_ff_lambda"), f("Heminus_ff_theta"), f("Heminus_ff_K"), len(t["H2plus_T"]),
+                                 len(t["H2plus_bf_lambda"]), len(t["H2plus_ff_lambda"]), f("H2plus_T"), f("H2plus_K"),
+                                 f("H2plus_bf_lambda"), f("H2plus_bf_sigma"), f("H2plus_ff_lambda"),
+                                 f("H2plus_ff_sigma"), len(t["gaunt_log_u"]), len(t["gaunt_log_g2"]),
+                                 f("gaunt_log_u"), f("gaunt_log_g2"), f("gaunt_ff"),
+                                 (C.c_int32 * 4)(*[len(t[f"peach_{p}_T"]) for p in peach]),
+                                 len(t["peach_HeII_sigma"]), (_dp * 4)(*[f(f"peach_{p}_T") for p in peach]),
+                                 f("peach_HeII_sigma"), (_dp * 4)(*[f(f"peach_{p}_D") for p in peach]))
+            self.check(self.lib.korg_set_continuum_tables(self.h, C.byref(ct)))
+            self.have_continuum = True
 
     def stats(self):
         s = Stats()

@@ -274,11 +274,13 @@ def _merge_windows(wins):
 def prepare_synthesis(atm, linelist: LineList, A_X, wavelengths, vmic=1.0, line_buffer=10.0, cntm_step=1.0,
                       hydrogen_lines=True, use_MHD_for_hydrogen_lines=None, hydrogen_line_window_size=150,
                       line_cutoff_threshold=3e-4, use_internal_reference_linelist=True,
-                      chemical_equilibrium=None, continuum_opacity=None):
-    """The host part of synthesize (src/synthesize.jl:159-262).  Chemical equilibrium and the
-    continuum come from ``chemical_equilibrium(T, n_tot, A_X) -> (ne, {Species: n})`` and
-    ``continuum_opacity(wls_cm, T, ne, n_HI, n_HII) -> alpha``; by default the stand-ins of
-    :mod:`korg_gb300.standin`."""
+                      chemical_equilibrium=None, continuum_opacity=None, continuum="standin", ctx=None):
+    """The host part of synthesize (src/synthesize.jl:159-262).  Chemical equilibrium comes from
+    ``chemical_equilibrium(T, n_tot, A_X) -> (ne, {Species: n})`` (default: the stand-in of
+    :mod:`korg_gb300.standin`).  The continuum: ``continuum="gpu"`` evaluates Korg's continuum
+    absorption (every term but metal bound-free) on the device (:mod:`korg_gb300.continuum`);
+    ``"standin"`` (the default, CPU only) the compact stand-in of :mod:`korg_gb300.standin`; a
+    ``continuum_opacity(wls_cm, T, ne, n_HI, n_HII) -> alpha`` callable overrides both."""
     from . import standin
     chem = chemical_equilibrium or standin.chemical_equilibrium
     cont = continuum_opacity or standin.continuum_opacity
@@ -316,11 +318,18 @@ def prepare_synthesis(atm, linelist: LineList, A_X, wavelengths, vmic=1.0, line_
     for s in species:  # species the stand-in does not form get zero density
         nd.setdefault(s, np.zeros(L))
     H1, H2, He1 = parse_species("H I"), parse_species("H II"), parse_species("He I")
-    vals = np.empty((L, len(cntm_wls)))
-    aref = np.empty(L)
-    for l in range(L):
-        vals[l] = cont(cntm_wls.all_wls, T[l], ne[l], nd[H1][l], nd[H2][l])
-        aref[l] = cont(np.array([atm.reference_wavelength]), T[l], ne[l], nd[H1][l], nd[H2][l])[0]
+    if continuum_opacity is None and continuum == "gpu":  # src/synthesize.jl:225-235 on the device
+        from .continuum import continuum_absorption
+        vals = continuum_absorption(cntm_wls.all_wls, T, ne, nd, pf, ctx=ctx)
+        aref = continuum_absorption(np.array([atm.reference_wavelength]), T, ne, nd, pf, ctx=ctx)[:, 0].copy()
+    elif continuum_opacity is None and continuum != "standin":
+        raise ValueError(f'continuum must be "gpu" or "standin", got {continuum!r}')
+    else:
+        vals = np.empty((L, len(cntm_wls)))
+        aref = np.empty(L)
+        for l in range(L):
+            vals[l] = cont(cntm_wls.all_wls, T[l], ne[l], nd[H1][l], nd[H2][l])
+            aref[l] = cont(np.array([atm.reference_wavelength]), T[l], ne[l], nd[H1][l], nd[H2][l])[0]
     xi = np.broadcast_to(np.asarray(vmic, np.float64) * 1e5, (L,)).copy()
     return SynthesisInputs(
         wls=wls, linelist=ll, linelist5=ll5, T=T, ne=np.asarray(ne, np.float64),
@@ -353,9 +362,11 @@ def synthesize_prepared(inp: SynthesisInputs, precision="mixed", return_alpha=Fa
                            line_evals=ctx.stats().line_evals)
 
 
-def synthesize(atm, linelist, A_X, wavelengths, precision="mixed", return_alpha=False, ctx=None, **kwargs):
-    """``synthesize(atm, linelist, A_X, wavelengths; kwargs...)`` (src/synthesize.jl:138-324)."""
-    inp = prepare_synthesis(atm, linelist, A_X, wavelengths, **kwargs)
+def synthesize(atm, linelist, A_X, wavelengths, precision="mixed", return_alpha=False, ctx=None, continuum="gpu",
+               **kwargs):
+    """``synthesize(atm, linelist, A_X, wavelengths; kwargs...)`` (src/synthesize.jl:138-324), with
+    the continuum absorption evaluated on the device by default (see :func:`prepare_synthesis`)."""
+    inp = prepare_synthesis(atm, linelist, A_X, wavelengths, continuum=continuum, ctx=ctx, **kwargs)
     return synthesize_prepared(inp, precision=precision, return_alpha=return_alpha, ctx=ctx)
 
 

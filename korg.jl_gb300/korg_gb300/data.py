@@ -75,3 +75,10 @@ def stark_profiles():
                 nT=nT, nNe=nNe, nD=nD, t_off=t_off, ne_off=ne_off, d_off=d_off, p_off=p_off,
                 l_off=l_off, log_gf=d["log_gf"].astype(np.float64), temps=d["temps"], nes=d["nes"],
                 logdnu=logdnu, logP=logP, lambda0=d["lambda0"] * 1e-8, names=d["names"])
+
+
+@functools.lru_cache(maxsize=None)
+def continuum_tables():
+    """The continuum-absorption tables of src/ContinuumAbsorption/ (see make_data.continuum):
+    arrays keyed as in continuum_tables.npz, all float64."""
+    return {k: np.ascontiguousarray(v, dtype=np.float64) for k, v in _npz("continuum_tables.npz").items()}

@@ -10,6 +10,12 @@ It reads (with the package's own HDF5 reader, no h5py needed):
     data/barklem_collet_2016/BarklemCollet2016-molecular_partition.dat -> partition_funcs.npz
   * data/barklem_collet_2016/BarklemCollet2016-ionization_energies.dat -> in partition_funcs.npz
   * data/linelists/alpha_5000/alpha_5000_lines.csv -> alpha_5000_lines.npz
+  * the continuum-absorption tables -> continuum_tables.npz: the H I bound-free cross-sections
+    (data/bf_cross-sections/individual_H_cross-sections.h5, levels 1-6), the H- bound-free
+    cross-sections (data/McLaughlin2017Hminusbf.h5), the free-free Gaunt factors
+    (data/vanHoof2014-nr-gauntff.dat, cut to the reference's T / wavelength / Z range), and the
+    tables written as array literals in src/ContinuumAbsorption/*.jl (H- ff of Bell & Berrington
+    1987, He- ff of John 1994, H2+ of Stancil 1994, departure coefficients of Peach 1970)
 The outputs are the same numbers in a different container; nothing is refitted.
 """
 import csv
@@ -110,6 +116,88 @@ def alpha5000(root):
         vdW=np.array(vdW))
 
 
+def _julia_array(src, name, start=0):
+    """The numbers of the Julia array literal assigned to `name` (first one at or after `start`),
+    as a float array: a matrix literal (rows separated by newlines or ';') gives a 2-D array.  A
+    scalar factor written before it (`10.0 .* [...]`) is applied."""
+    import re
+    m = re.compile(r"\b" + re.escape(name) + r"\s*=\s*([-+0-9.eE]+\s*\.\*\s*)?\[").search(src, start)
+    if not m:
+        raise KeyError(name)
+    i, depth = m.end(), 1
+    j = i
+    while depth:
+        depth += {"[": 1, "]": -1}.get(src[j], 0)
+        j += 1
+    body = "\n".join(line.split("#")[0] for line in src[i:j - 1].split("\n"))
+    rows = [r for r in re.split(r"[;\n]", body) if r.strip()]
+    vals = [[float(x) for x in re.split(r"[,\s]+", r.strip()) if x] for r in rows]
+    arr = np.array(vals) if len(vals) > 1 and len({len(v) for v in vals}) == 1 and len(vals[0]) > 1 else \
+        np.array([x for v in vals for x in v])
+    if m.group(1):
+        arr = arr * float(m.group(1).split(".*")[0])
+    return arr
+
+
+def continuum(root):
+    src_dir = os.path.join(root, "src", "ContinuumAbsorption")
+    read = lambda fn: open(os.path.join(src_dir, fn)).read()
+    out = {}
+    # H I bound-free (Nahar 2021), levels n = 1..6 (absorption_H.jl:9-19, :62 uses [1:n_max_MHD])
+    f = hdf5lite.File(os.path.join(root, "data", "bf_cross-sections", "individual_H_cross-sections.h5"))
+    n = f.read("n")
+    assert list(n[:6]) == [1, 2, 3, 4, 5, 6]
+    out["H_bf_E"], out["H_bf_sigma"] = f.read("E")[:6], f.read("sigma")[:6]  # eV, megabarn
+    # H- bound-free (McLaughlin 2017, absorption_H.jl:170-175)
+    f = hdf5lite.File(os.path.join(root, "data", "McLaughlin2017Hminusbf.h5"))
+    out["Hminus_bf_nu"], out["Hminus_bf_sigma"] = f.read("nu"), f.read("sigma")
+    # H- free-free (Bell & Berrington 1987, absorption_H.jl:232-259): K in 1e-26 cm^4/dyn
+    s = read("absorption_H.jl")
+    out["Hminus_ff_theta"] = _julia_array(s, "theta_ff_absorption_interp")
+    out["Hminus_ff_lambda"] = _julia_array(s, "lambda_ff_absorption_interp")
+    out["Hminus_ff_K"] = _julia_array(s, "ff_absorption")
+    # He- free-free (John 1994, absorption_He.jl:31-53)
+    s = read("absorption_He.jl")
+    out["Heminus_ff_theta"] = _julia_array(s, "theta_ff_absorption_interp")
+    out["Heminus_ff_lambda"] = _julia_array(s, "lambda_ff_absorption_interp")
+    out["Heminus_ff_K"] = _julia_array(s, "ff_absorption")
+    # H2+ (Stancil 1994): K(T) n(H I) n(H II) / n(H2+), cross sections in 1e-18 cm^2 (bf) and
+    # 1e-39 cm^5 (ff) on wavelengths in A (Stancil1994.jl)
+    s = read("Stancil1994.jl")
+    for k in ("Ts_H2plus", "K_H2plus_vals", "λs_H2plus_ff", "λs_bf", "σ_H2plus_bf_table", "σ_H2plus_ff_table"):
+        key = {"λs_H2plus_ff": "H2plus_ff_lambda", "λs_bf": "H2plus_bf_lambda", "σ_H2plus_bf_table": "H2plus_bf_sigma",
+               "σ_H2plus_ff_table": "H2plus_ff_sigma", "Ts_H2plus": "H2plus_T", "K_H2plus_vals": "H2plus_K"}[k]
+        out[key] = _julia_array(s, k)
+    # Peach 1970 ff departure coefficients, per ion taking part (Peach1970.jl)
+    s = read("Peach1970.jl")
+    for sp in ("He II", "C II", "Si II", "Mg II"):
+        at = s.index(f'coeffs[species"{sp}"] = let')
+        tag = sp.replace(" ", "")
+        out[f"peach_{tag}_sigma"] = _julia_array(s, "σ_vals", at)
+        out[f"peach_{tag}_T"] = _julia_array(s, "T_vals", at)
+        out[f"peach_{tag}_D"] = _julia_array(s, "table_vals", at)
+    # van Hoof et al. (2014) non-relativistic thermally averaged ff Gaunt factors
+    # (hydrogenic_bf_ff.jl:16-80): the header gives the grid, rows are log10(u), columns log10(gamma^2)
+    lines = [l for l in open(os.path.join(root, "data", "vanHoof2014-nr-gauntff.dat"))]
+    body = [l for l in lines if not l.startswith("#")]
+    hdr = lambda l: l.split("#")[0].split()
+    assert int(hdr(body[0])[0]) == 20140210
+    n_g2, n_u = (int(x) for x in hdr(body[1]))
+    g2_start, u_start, step = float(hdr(body[2])[0]), float(hdr(body[3])[0]), float(hdr(body[4])[0])
+    tab = np.array([[float(x) for x in body[5 + i].split()] for i in range(n_u)])
+    log_g2 = g2_start + step * np.arange(n_g2)
+    log_u = u_start + step * np.arange(n_u)
+    Ry, kB, h, c = 13.605693122994, 8.617333262145e-5, 6.62607015e-27, 2.99792458e10
+    kB_cgs = 1.380649e-16
+    g2 = [np.log10(Ry * Z * Z / (kB * T)) for Z in (1, 2) for T in (100.0, 1e6)]
+    uu = [np.log10(h * c / (lam * kB_cgs * T)) for lam in (1e-6, 1e-2) for T in (100.0, 1e6)]
+    g_lb, g_ub = np.searchsorted(log_g2, min(g2), "right") - 1, np.searchsorted(log_g2, max(g2), "left")
+    u_lb, u_ub = np.searchsorted(log_u, min(uu), "right") - 1, np.searchsorted(log_u, max(uu), "left")
+    out["gaunt_log_u"], out["gaunt_log_g2"] = log_u[u_lb:u_ub + 1], log_g2[g_lb:g_ub + 1]
+    out["gaunt_ff"] = tab[u_lb:u_ub + 1, g_lb:g_ub + 1]
+    np.savez_compressed(os.path.join(HERE, "continuum_tables.npz"), **out)
+
+
 if __name__ == "__main__":
     root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("KORG_REFERENCE")
     if not root:
@@ -117,4 +205,5 @@ if __name__ == "__main__":
     stark(root)
     partition(root)
     alpha5000(root)
+    continuum(root)
     print("wrote", sorted(x for x in os.listdir(HERE) if x.endswith(".npz")))

@@ -139,7 +139,8 @@ def abundance_variants(inp, n_variants=16, seed=0, spread=0.3):
 
 
 def prepare(work: Workload, **kwargs):
-    """Synthetic atmosphere + host precompute for a workload."""
+    """Synthetic atmosphere + host precompute for a workload (keyword arguments go to
+    prepare_synthesis, e.g. continuum="gpu")."""
     from .api import prepare_synthesis
     atm, A_X = standin.synthetic_atmosphere(work.Teff, work.logg, work.m_H, work.L)
     return prepare_synthesis(atm, work.linelist, A_X, work.wavelengths, vmic=work.vmic,

@@ -35,7 +35,7 @@ def test_synthesize_reference_signature(ctx, oracle_lib):
     w = synthetic.config0()
     atm, A_X = standin.synthetic_atmosphere(w.Teff, w.logg, w.m_H, w.L)
     res = korg_gb300.synthesize(atm, w.linelist, A_X, (5000, 5100), precision="fp64", ctx=ctx)
-    inp = korg_gb300.prepare_synthesis(atm, w.linelist, A_X, (5000, 5100))
+    inp = korg_gb300.prepare_synthesis(atm, w.linelist, A_X, (5000, 5100), continuum="gpu", ctx=ctx)
     flux, cntm, _, _, ev = oracle_lib.synthesize(inp, inp.linelist, inp.linelist5, stark_profiles(),
                                                  inp.wls.all_wls, nthreads=NT)
     assert len(res.flux) == 10001 and np.array_equal(res.wavelengths, inp.wls.all_wls_angstrom)
