@@ -105,15 +105,34 @@ def oracle_flux(inp, threads):
     return flux, cntm, ev, time.perf_counter() - t0
 
 
-def cpu_sample(n_lines, threads, _cache={}):
+def cpu_continuum(inp):
+    """Replace the continuum of prepared inputs by the FP64 CPU restatement of Korg's continuum
+    absorption (the values the device computes for continuum="gpu", to rounding), so that a
+    CPU-only process prepares the GPU arm's workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import continuum_oracle
+    from korg_gb300.continuum import layer_inputs
+    d = layer_inputs(inp.T, inp.ne, inp.number_densities)
+    nu = 2.99792458e10 / inp.cntm_knots
+    nu_ref = 2.99792458e10 / np.array([inp.ref_wl])
+    for l in range(len(inp.T)):
+        dl = {k: v[l] for k, v in d.items()}
+        inp.cntm_vals[l] = continuum_oracle.total_continuum_absorption(nu, inp.T[l], dl["ne"], dl)
+        inp.alpha_ref_cntm[l] = continuum_oracle.total_continuum_absorption(nu_ref, inp.T[l], dl["ne"], dl)[0]
+    return inp
+
+
+def cpu_sample(inp_or_lines, threads, _cache={}):
     """Time the oracle on the CPU sample; returns (spectra/s, seconds, evals, info, flux, cntm).
 
     The sample is the full workload (all lines, the same continuum and atmosphere) on the same
-    3000-10000 A range at 0.05 A: every 5th point of the 0.01 A grid, 20% of the points."""
+    3000-10000 A range at 0.05 A: every 5th point of the 0.01 A grid, 20% of the points.  Given a
+    line count, the workload is prepared here on the CPU (continuum from the CPU restatement)."""
     from korg_gb300 import synthetic
-    key = n_lines
+    key = inp_or_lines if isinstance(inp_or_lines, int) else id(inp_or_lines)
     if key not in _cache:
-        inp = synthetic.prepare(workload(n_lines))
+        inp = cpu_continuum(synthetic.prepare(workload(inp_or_lines))) if isinstance(inp_or_lines, int) else inp_or_lines
         _cache[key] = (strided(inp, CPU_SAMPLE_STEP)[0], len(inp.wls))
     inp, full_points = _cache[key]
     frac = len(inp.wls) / full_points
@@ -275,12 +294,11 @@ def run_korg(args):
     dev = torch.device("cuda", local)
     korg_build.build()
 
+    ctx = _lib.Context(local)
     t0 = time.perf_counter()
     work = workload(args.lines, args.wl)
-    inp = synthetic.prepare(work)
+    inp = synthetic.prepare(work, continuum="gpu", ctx=ctx)
     host_prep_s = time.perf_counter() - t0
-
-    ctx = _lib.Context(local)
     ctx.ensure_stark()
     ctx.check(ctx.lib.korg_set_timing(ctx.h, 1))
     if args.tile:
@@ -379,7 +397,7 @@ def run_korg(args):
     cpu, parity = None, {}
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        v, dt, ev_cpu, info, oflux, ocntm = cpu_sample(args.lines, threads)
+        v, dt, ev_cpu, info, oflux, ocntm = cpu_sample(inp, threads)
         cpu = {"value": v, "unit": "spectra/s", "cores": threads, "kind": "port", "sample": info,
                "evals_per_s": ev_cpu / dt, "seconds": dt}
         # the headline's flux against the FP64 oracle at the sample's points (every 5th point)
@@ -415,6 +433,8 @@ def run_korg(args):
                                f"{args.lines} atomic lines + hydrogen lines, {args.wl[0]:.0f}-{args.wl[1]:.0f} A "
                                f"@ 0.01 A ({nwl} points)",
                    "precision": "mixed",
+                   "continuum": "device (korg_continuum_absorption: Korg's continuum terms except metal bound-free) "
+                                "from the stand-in chemical equilibrium",
                    "l2": f"flushed (256 MiB write) between steps; alpha {8 * L * nwl / 1e6:.0f} MB",
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU", "tile": args.tile or "default",
                    "host_prep_s": host_prep_s},
@@ -744,7 +764,7 @@ def run_variants(args):
     torch.cuda.set_device(dev)
     t0 = time.perf_counter()
     _progress("preparing the 1M-line cool giant")
-    base = synthetic.prepare(synthetic.config4())
+    base = synthetic.prepare(synthetic.config4(), continuum="gpu")
     inps = synthetic.abundance_variants(base, 16)
     host_prep_s = time.perf_counter() - t0
     nwl, L = len(base.wls), len(base.T)
@@ -809,7 +829,8 @@ class AdjointCase:
         from korg_gb300 import _lib, synthetic
         from korg_gb300.api import synthesize_prepared
         self.torch, self.ctx, self.lib = torch, ctx, _lib
-        inp = synthetic.prepare(synthetic.config2(n_atomic=int(50_000 * scale), n_mol=int(20_000 * scale)))
+        inp = synthetic.prepare(synthetic.config2(n_atomic=int(50_000 * scale), n_mol=int(20_000 * scale)),
+                                continuum="gpu", ctx=ctx)
         self.inp = inp
         self.nwl, L = len(inp.wls), len(inp.T)
         ctx.ensure_stark()
@@ -899,10 +920,11 @@ def configs_vs_oracle(ctx, threads):
     0.005 A infrared grids, every 50th of the 0.01 A optical one)."""
     from korg_gb300 import synthetic
     from korg_gb300.api import synthesize_prepared
-    cases = [("cfg2_adjoint_forward", lambda: synthetic.prepare(synthetic.config2()), 0.1),
+    gpu = dict(continuum="gpu", ctx=ctx)
+    cases = [("cfg2_adjoint_forward", lambda: synthetic.prepare(synthetic.config2(), **gpu), 0.1),
              ("cfg3_batch_spectrum0", lambda: synthetic.prepare(synthetic.config3(n_spectra=1)[0]), 0.1),
              ("cfg4_cool_star_variant0",
-              lambda: synthetic.abundance_variants(synthetic.prepare(synthetic.config4()), 1)[0], 0.5)]
+              lambda: synthetic.abundance_variants(synthetic.prepare(synthetic.config4(), **gpu), 1)[0], 0.5)]
     out = {}
     ctx.ensure_stark()
     for name, make, step in cases:
