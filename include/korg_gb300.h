@@ -41,7 +41,8 @@ typedef enum {
     KORG_ENOMEM = 3,   /* device allocation failed */
     KORG_ENOTABLES = 4, /* hydrogen lines requested before korg_set_stark_tables() */
     KORG_ETOOBIG = 5,   /* the problem needs more scratch than KORG_NOALLOC_SCRATCH_BYTES */
-    KORG_ETIMEOUT = 6   /* a device-side wait for staged data ran past its limit (results invalid) */
+    KORG_ETIMEOUT = 6,  /* a device-side wait for staged data ran past its limit (results invalid) */
+    KORG_ECHEM = 7      /* chemical equilibrium failed in at least one layer (see its status) */
 } korg_status;
 
 /* Every call taking a `precision` returns KORG_EINVAL for any other value. */
@@ -180,6 +181,68 @@ KORG_API int korg_continuum_absorption(korg_ctx *ctx, const double *wls, int64_t
 KORG_API int korg_continuum_absorption_dev(korg_ctx *ctx, const double *wls, int64_t nwl,
                                            const korg_continuum_layers *layers, double *vals,
                                            void *stream);
+
+/* Chemical equilibrium, chemical_equilibrium(T, n_tot, ne, absolute_abundances,
+ * ionization_energies, partition_fns, log_equilibrium_constants) (src/statmech.jl:148-206),
+ * solved for every layer of one or many atmospheres at once (synthesize calls it per layer,
+ * src/synthesize.jl:210-219).  The unknowns are log10 of the 92 neutral-atom densities and of
+ * n_e; the solver is the reference's (src/statmech.jl:215-305, src/newton.jl): Newton steps
+ * clipped to 1 dex, tolerance 1e-8 on the scaled residuals, and a continuation on the molecule
+ * and H- scale log xi when the plain solve fails.  FP64 throughout.
+ *
+ * korg_set_equilibrium_tables uploads the data once.  Every spline is Korg's natural cubic
+ * spline over ln T (src/CubicSplines.jl) given by knots t, values u and second derivatives z:
+ *   atomic partition functions on shared knots lnT[n_knots], U_u / U_z [92*3][n_knots] with
+ *     species (Z, q) at row 3(Z-1)+q (the H III row is never read); T must lie in the knot range;
+ *   chi [92*3]: ionization energies (eV) chi1, chi2, chi3 of each element;
+ *   molecules m < n_mol (at most KORG_CHEM_MAX_MOL): atoms [n_mol][6] ascending atomic numbers,
+ *     0-padded; charge 0 or 1 (a charged molecule is a diatomic whose first atom is the ion);
+ *     kind 0: log10 K (partial-pressure form) is the spline at spl[off[m] .. off[m+1]);
+ *     kind 1: a polyatomic, log10 K from its atomization energy D00 (eV), the log10 ratio lmr of
+ *     its atoms' masses product to its mass, and its partition function, the spline at
+ *     spl[off[m] .. off[m+1]) (src/read_statmech_quantities.jl:66-89).
+ * Molecule splines extrapolate flat; the atomic ones do not. */
+#define KORG_CHEM_MAX_MOL 384
+typedef struct {
+    int32_t n_knots;
+    const double *lnT, *U_u, *U_z, *chi;
+    int32_t n_mol;
+    const int32_t *atoms, *charge, *kind;
+    const int64_t *off;
+    const double *spl_t, *spl_u, *spl_z, *D00, *lmr;
+} korg_equilibrium_tables;
+/* Layers: T (K), n_tot and the model atmosphere's n_e (cm^-3, the starting guess) per layer;
+ * abundances [n_atm][92] = N_X / N_total of each atmosphere (positive, normalised by the
+ * caller as src/synthesize.jl:208-209 does); atm [L] the atmosphere of each layer (NULL: all 0). */
+typedef struct {
+    int32_t L;
+    const double *T, *n_tot, *ne_model, *abundances;
+    const int32_t *atm;
+} korg_chem_layers;
+/* densities [L][KORG_CHEM_MOL0 + n_mol]: n_e, n(Z, q) for q = 0, 1, 2 (H III is 0), n(H-), then
+ * each molecule in table order.  status [L]: KORG_CHEM_OK, or why the layer failed; info
+ * [L][4] (may be NULL): Newton iterations, solves, the log xi reached (or where the
+ * continuation stopped), the last residual inf-norm.  The host entry point returns KORG_ECHEM
+ * when any layer failed (densities of the other layers are valid); _dev takes device pointers
+ * and is stream-ordered (read status after the stream). */
+#define KORG_CHEM_NE 0
+#define KORG_CHEM_ATOM(Z, q) (1 + 3 * ((Z) - 1) + (q))
+#define KORG_CHEM_HMINUS 277
+#define KORG_CHEM_MOL0 278
+enum {
+    KORG_CHEM_OK = 0,
+    KORG_CHEM_ANCHOR = 1,     /* no anchor log xi in (-5, -20, -50) converged */
+    KORG_CHEM_ANNEAL = 2,     /* the continuation step fell below 1/16 without converging */
+    KORG_CHEM_NONFINITE = 3,  /* the solution contains non-finite values */
+    KORG_CHEM_BUDGET = 4      /* more than KORG_CHEM_MAX_ITER Newton iterations in total */
+};
+#define KORG_CHEM_MAX_ITER 20000
+KORG_API int korg_set_equilibrium_tables(korg_ctx *ctx, const korg_equilibrium_tables *host_tables);
+KORG_API int korg_chemical_equilibrium(korg_ctx *ctx, const korg_chem_layers *layers, int32_t n_atm,
+                                       double *densities, int32_t *status, double *info);
+KORG_API int korg_chemical_equilibrium_dev(korg_ctx *ctx, const korg_chem_layers *layers,
+                                           int32_t n_atm, double *densities, int32_t *status,
+                                           double *info, void *stream);
 
 /* line_absorption!(alpha, linelist, wls, temps, ne, n_densities, partition_fns, xi, alpha_cntm;
  * cutoff_threshold) -- src/line_absorption.jl:33-129.  alpha (host, L x nwl) is accumulated in

@@ -24,6 +24,7 @@
 #include "postprocess.cuh"
 #include "physics.cuh"
 #include "rt.cuh"
+#include "statmech.cuh"
 
 using namespace korg;
 
@@ -89,6 +90,11 @@ struct korg_ctx {
     bool have_cntm = false;
     CntmTables cntm_tab{};
     void* cntm_buf = nullptr;
+    // chemical-equilibrium tables (one device buffer)
+    bool have_chem = false;
+    ChemTables chem_tab{};
+    void* chem_buf = nullptr;
+    double chem_lnT0 = 0, chem_lnT1 = 0;  // knot range of the atomic partition functions
     // Stehle tables
     bool have_stark = false;
     StarkDev stark{};
@@ -1242,6 +1248,7 @@ KORG_API void korg_destroy(korg_ctx* ctx) {
         if (b->p) cudaFree(b->p);
     for (void* p : ctx->stark_allocs) cudaFree(p);
     if (ctx->cntm_buf) cudaFree(ctx->cntm_buf);
+    if (ctx->chem_buf) cudaFree(ctx->chem_buf);
     if (ctx->stage_host) cudaFreeHost(ctx->stage_host);
     if (ctx->b_host) cudaFreeHost(ctx->b_host);
     if (ctx->dev_err_host) cudaFreeHost(ctx->dev_err_host);
@@ -1489,6 +1496,195 @@ KORG_API int korg_line_absorption_dev(korg_ctx* ctx, double* alpha, const double
     return run_line_absorption(ctx, alpha, wls, nwl, lines_dev(lines), layers_dev(layers),
                                CntmDev{cntm->nk, cntm->knots, cntm->vals}, cutoff, precision == KORG_MIXED,
                                static_cast<cudaStream_t>(stream));
+}
+
+// ------------------------------------------------------------------ chemical equilibrium
+KORG_API int korg_set_equilibrium_tables(korg_ctx* ctx, const korg_equilibrium_tables* t) {
+    if (!ctx) return KORG_EINVAL;
+    if (!t || t->n_knots < 2 || !t->lnT || !t->U_u || !t->U_z || !t->chi || t->n_mol < 0 ||
+        t->n_mol > KORG_CHEM_MAX_MOL || (t->n_mol > 0 && (!t->atoms || !t->charge || !t->kind || !t->off ||
+                                                           !t->spl_t || !t->spl_u || !t->spl_z)))
+        return set_err(ctx, KORG_EINVAL, "bad equilibrium tables");
+    for (int k = 1; k < t->n_knots; k++)
+        if (!(t->lnT[k] > t->lnT[k - 1])) return set_err(ctx, KORG_EINVAL, "partition-function knots not increasing");
+    const int M = t->n_mol;
+    // derived per-molecule data: atom count, distinct atoms with counts, element incidence lists
+    std::vector<int32_t> nat(M), ndist(M), dist_Z(size_t(M) * CE_MAXATOMS, 0), dist_cnt(size_t(M) * CE_MAXATOMS, 0);
+    std::vector<std::vector<std::pair<int32_t, int32_t>>> inc(CE_NZ);
+    bool polyatomic = false;
+    for (int m = 0; m < M; m++) {
+        const int32_t* at = t->atoms + size_t(m) * CE_MAXATOMS;
+        int n = 0;
+        while (n < CE_MAXATOMS && at[n]) n++;
+        for (int j = n; j < CE_MAXATOMS; j++)
+            if (at[j]) return set_err(ctx, KORG_EINVAL, "molecule %d: atoms not 0-padded", m);
+        if (n < 2) return set_err(ctx, KORG_EINVAL, "molecule %d has %d atoms", m, n);
+        for (int j = 0; j < n; j++)
+            if (at[j] < 1 || at[j] > CE_NZ || (j && at[j] < at[j - 1]))
+                return set_err(ctx, KORG_EINVAL, "molecule %d: atomic numbers not ascending in 1..92", m);
+        if (t->charge[m] != 0 && !(t->charge[m] == 1 && n == 2))
+            return set_err(ctx, KORG_EINVAL, "molecule %d: only neutral or singly ionized diatomics", m);
+        if (t->kind[m] != 0 && t->kind[m] != 1) return set_err(ctx, KORG_EINVAL, "molecule %d: kind", m);
+        polyatomic |= t->kind[m] == 1;
+        if (t->off[m + 1] - t->off[m] < 2 || t->off[m] < 0)
+            return set_err(ctx, KORG_EINVAL, "molecule %d: spline needs two knots", m);
+        nat[m] = n;
+        int d = 0;
+        for (int j = 0; j < n; j++) {
+            if (j && at[j] == at[j - 1]) {
+                dist_cnt[size_t(m) * CE_MAXATOMS + d - 1]++;
+            } else {
+                dist_Z[size_t(m) * CE_MAXATOMS + d] = at[j];
+                dist_cnt[size_t(m) * CE_MAXATOMS + d] = 1;
+                d++;
+            }
+        }
+        ndist[m] = d;
+        for (int j = 0; j < d; j++)
+            inc[dist_Z[size_t(m) * CE_MAXATOMS + j] - 1].push_back({m, dist_cnt[size_t(m) * CE_MAXATOMS + j]});
+    }
+    if (polyatomic && (!t->D00 || !t->lmr)) return set_err(ctx, KORG_EINVAL, "polyatomic molecules need D00 and lmr");
+    std::vector<int32_t> inc_ptr(CE_NZ + 1, 0), inc_mol, inc_cnt;
+    for (int Z = 0; Z < CE_NZ; Z++) {
+        for (const auto& e : inc[Z]) {
+            inc_mol.push_back(e.first);
+            inc_cnt.push_back(e.second);
+        }
+        inc_ptr[Z + 1] = int32_t(inc_mol.size());
+    }
+    const int64_t nspl = M ? t->off[M] : 0;
+    std::vector<double> zeros(std::max<int64_t>(M, 1), 0.0);
+    std::vector<int32_t> izeros(1, 0);
+    KCUDA(cudaSetDevice(ctx->device));
+    struct Piece { const void* src; size_t bytes; const void** dst; };
+    ChemTables d{};
+    d.nk = t->n_knots;
+    d.n_mol = M;
+    const size_t nk = size_t(t->n_knots);
+    auto ip = [&](const std::vector<int32_t>& v) { return v.empty() ? (const void*)izeros.data() : (const void*)v.data(); };
+    std::vector<Piece> pcs = {
+        {t->lnT, 8 * nk, (const void**)&d.lnT}, {t->U_u, 8 * nk * 3 * CE_NZ, (const void**)&d.U_u},
+        {t->U_z, 8 * nk * 3 * CE_NZ, (const void**)&d.U_z}, {t->chi, 8 * 3 * size_t(CE_NZ), (const void**)&d.chi},
+        {M ? (const void*)t->atoms : izeros.data(), 4 * std::max<size_t>(size_t(M) * CE_MAXATOMS, 1), (const void**)&d.atoms},
+        {M ? (const void*)t->charge : izeros.data(), 4 * std::max<size_t>(M, 1), (const void**)&d.charge},
+        {M ? (const void*)t->kind : izeros.data(), 4 * std::max<size_t>(M, 1), (const void**)&d.kind},
+        {M ? (const void*)t->off : zeros.data(), 8 * size_t(M + 1 > 1 ? M + 1 : 1), (const void**)&d.off},
+        {M ? (const void*)t->spl_t : zeros.data(), 8 * std::max<size_t>(nspl, 1), (const void**)&d.t},
+        {M ? (const void*)t->spl_u : zeros.data(), 8 * std::max<size_t>(nspl, 1), (const void**)&d.u},
+        {M ? (const void*)t->spl_z : zeros.data(), 8 * std::max<size_t>(nspl, 1), (const void**)&d.z},
+        {polyatomic ? (const void*)t->D00 : zeros.data(), 8 * (polyatomic ? size_t(M) : 1), (const void**)&d.D00},
+        {polyatomic ? (const void*)t->lmr : zeros.data(), 8 * (polyatomic ? size_t(M) : 1), (const void**)&d.lmr},
+        {ip(nat), 4 * std::max<size_t>(M, 1), (const void**)&d.nat},
+        {ip(ndist), 4 * std::max<size_t>(M, 1), (const void**)&d.ndist},
+        {ip(dist_Z), 4 * std::max<size_t>(dist_Z.size(), 1), (const void**)&d.dist_Z},
+        {ip(dist_cnt), 4 * std::max<size_t>(dist_cnt.size(), 1), (const void**)&d.dist_cnt},
+        {inc_ptr.data(), 4 * inc_ptr.size(), (const void**)&d.inc_ptr},
+        {ip(inc_mol), 4 * std::max<size_t>(inc_mol.size(), 1), (const void**)&d.inc_mol},
+        {ip(inc_cnt), 4 * std::max<size_t>(inc_cnt.size(), 1), (const void**)&d.inc_cnt}};
+    size_t total = 0;
+    for (const Piece& q : pcs) {
+        if (!q.src) return set_err(ctx, KORG_EINVAL, "null equilibrium table");
+        total += a256(q.bytes);
+    }
+    std::vector<unsigned char> host(total);
+    size_t off = 0;
+    for (const Piece& q : pcs) {
+        memcpy(host.data() + off, q.src, q.bytes);
+        off += a256(q.bytes);
+    }
+    void* buf = nullptr;
+    cudaError_t e = cudaMalloc(&buf, total);
+    if (e != cudaSuccess) return set_err(ctx, KORG_ENOMEM, "cudaMalloc(%zu): %s", total, cudaGetErrorString(e));
+    e = cudaMemcpy(buf, host.data(), total, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(buf);
+        return set_err(ctx, KORG_ECUDA, "equilibrium tables: %s", cudaGetErrorString(e));
+    }
+    off = 0;
+    for (const Piece& q : pcs) {
+        *q.dst = static_cast<unsigned char*>(buf) + off;
+        off += a256(q.bytes);
+    }
+    if (ctx->chem_buf) {
+        KCUDA(cudaDeviceSynchronize());
+        cudaFree(ctx->chem_buf);
+    }
+    ctx->chem_buf = buf;
+    ctx->chem_tab = d;
+    ctx->chem_lnT0 = t->lnT[0];
+    ctx->chem_lnT1 = t->lnT[t->n_knots - 1];
+    ctx->have_chem = true;
+    return KORG_OK;
+}
+
+KORG_API int korg_chemical_equilibrium_dev(korg_ctx* ctx, const korg_chem_layers* y, int32_t n_atm, double* dens,
+                                           int32_t* status, double* info, void* stream) {
+    if (!ctx) return KORG_EINVAL;
+    if (!y || y->L < 1 || !y->T || !y->n_tot || !y->ne_model || !y->abundances || n_atm < 1 || !dens || !status)
+        return set_err(ctx, KORG_EINVAL, "bad arguments");
+    if (!ctx->have_chem) return set_err(ctx, KORG_ENOTABLES, "korg_set_equilibrium_tables() has not been called");
+    KCUDA(cudaSetDevice(ctx->device));
+    const int smem = int(sizeof(CeShared));
+    KCUDA(cudaFuncSetAttribute(chem_eq_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    const ChemLayersDev ly{y->L, y->T, y->n_tot, y->ne_model, y->abundances, y->atm};
+    chem_eq_kernel<<<unsigned(y->L), CE_THREADS, smem, static_cast<cudaStream_t>(stream)>>>(ctx->chem_tab, ly, dens,
+                                                                                            status, info);
+    KCUDA(cudaGetLastError());
+    return KORG_OK;
+}
+
+KORG_API int korg_chemical_equilibrium(korg_ctx* ctx, const korg_chem_layers* y, int32_t n_atm, double* dens,
+                                       int32_t* status, double* info) {
+    if (!ctx) return KORG_EINVAL;
+    if (!y || y->L < 1 || !y->T || !y->n_tot || !y->ne_model || !y->abundances || n_atm < 1 || !dens || !status)
+        return set_err(ctx, KORG_EINVAL, "bad arguments");
+    if (!ctx->have_chem) return set_err(ctx, KORG_ENOTABLES, "korg_set_equilibrium_tables() has not been called");
+    const int L = y->L;
+    for (int l = 0; l < L; l++) {
+        const double T = y->T[l], nt = y->n_tot[l], ne = y->ne_model[l];
+        if (!(std::isfinite(T) && T > 0 && std::log(T) >= ctx->chem_lnT0 && std::log(T) <= ctx->chem_lnT1))
+            return set_err(ctx, KORG_EINVAL, "layer %d: T = %g outside the partition functions' range", l, T);
+        if (!(std::isfinite(nt) && std::isfinite(ne) && ne > 0 && nt > ne))
+            return set_err(ctx, KORG_EINVAL, "layer %d: need 0 < n_e < n_tot (n_e = %g, n_tot = %g)", l, ne, nt);
+        if (y->atm && (y->atm[l] < 0 || y->atm[l] >= n_atm))
+            return set_err(ctx, KORG_EINVAL, "layer %d: atmosphere index %d", l, y->atm[l]);
+    }
+    for (int64_t k = 0; k < int64_t(n_atm) * CE_NZ; k++)
+        if (!(std::isfinite(y->abundances[k]) && y->abundances[k] > 0))
+            return set_err(ctx, KORG_EINVAL, "abundance %lld is not positive", (long long)k);
+    KCUDA(cudaSetDevice(ctx->device));
+    const size_t nspec = size_t(KORG_CHEM_MOL0 + ctx->chem_tab.n_mol);
+    Stager st;
+    const size_t o_T = st.add(y->T, 8 * size_t(L)), o_n = st.add(y->n_tot, 8 * size_t(L));
+    const size_t o_e = st.add(y->ne_model, 8 * size_t(L));
+    const size_t o_a = st.add(y->abundances, 8 * size_t(n_atm) * CE_NZ);
+    const size_t o_m = y->atm ? st.add(y->atm, 4 * size_t(L)) : 0;
+    const size_t o_d = st.add(nullptr, 8 * size_t(L) * nspec);
+    const size_t o_s = st.add(nullptr, 4 * size_t(L));
+    const size_t o_i = st.add(nullptr, 8 * size_t(L) * CE_NINFO);
+    char* b = nullptr;
+    KCHECK(upload(ctx, st, &b));
+    const korg_chem_layers d{L, (const double*)(b + o_T), (const double*)(b + o_n), (const double*)(b + o_e),
+                             (const double*)(b + o_a), y->atm ? (const int32_t*)(b + o_m) : nullptr};
+    KCHECK(korg_chemical_equilibrium_dev(ctx, &d, n_atm, (double*)(b + o_d), (int32_t*)(b + o_s), (double*)(b + o_i),
+                                         ctx->stream));
+    KCUDA(cudaMemcpyAsync(dens, b + o_d, 8 * size_t(L) * nspec, cudaMemcpyDeviceToHost, ctx->stream));
+    KCUDA(cudaMemcpyAsync(status, b + o_s, 4 * size_t(L), cudaMemcpyDeviceToHost, ctx->stream));
+    std::vector<double> inf(size_t(L) * CE_NINFO);
+    KCUDA(cudaMemcpyAsync(inf.data(), b + o_i, 8 * inf.size(), cudaMemcpyDeviceToHost, ctx->stream));
+    KCUDA(cudaStreamSynchronize(ctx->stream));
+    if (info) memcpy(info, inf.data(), 8 * inf.size());
+    int nbad = 0, first = -1;
+    for (int l = 0; l < L; l++)
+        if (status[l] != KORG_CHEM_OK) {
+            nbad++;
+            if (first < 0) first = l;
+        }
+    if (nbad)
+        return set_err(ctx, KORG_ECHEM, "chemical equilibrium failed in %d layer(s); first: layer %d, status %d "
+                       "(log xi %g, inf-norm %g)", nbad, first, status[first], inf[size_t(first) * CE_NINFO + 2],
+                       inf[size_t(first) * CE_NINFO + 3]);
+    return KORG_OK;
 }
 
 KORG_API int korg_line_absorption(korg_ctx* ctx, double* alpha, const double* wls, int64_t nwl,

@@ -20,9 +20,15 @@ _API = ("line_absorption_", "hydrogen_line_absorption_", "radiative_transfer", "
         "loss_and_gradient", "physical_gradient")
 
 
+_STATMECH = ("chemical_equilibrium", "saha_ion_weights", "translational_U", "get_log_nK", "Hminus_nK",
+             "ChemicalEquilibriumError")
+
+
 def __getattr__(name):
-    # the API module (which loads the CUDA library binding on first call) is imported on first use
+    # the API modules (which load the CUDA library binding on first call) are imported on first use
+    import importlib
     if name in _API:
-        import importlib
         return getattr(importlib.import_module(".api", __name__), name)
+    if name in _STATMECH:
+        return getattr(importlib.import_module(".statmech", __name__), name)
     raise AttributeError(name)

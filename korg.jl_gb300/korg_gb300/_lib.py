@@ -89,6 +89,23 @@ class ContinuumLayers(C.Structure):
                [("n_peach", _dp * 4)]
 
 
+class EquilibriumTables(C.Structure):
+    """korg_equilibrium_tables (host arrays)."""
+    _fields_ = [("n_knots", C.c_int32), ("lnT", _dp), ("U_u", _dp), ("U_z", _dp), ("chi", _dp), ("n_mol", C.c_int32),
+                ("atoms", _ip), ("charge", _ip), ("kind", _ip), ("off", C.POINTER(C.c_int64)), ("spl_t", _dp),
+                ("spl_u", _dp), ("spl_z", _dp), ("D00", _dp), ("lmr", _dp)]
+
+
+class ChemLayers(C.Structure):
+    """korg_chem_layers."""
+    _fields_ = [("L", C.c_int32), ("T", _dp), ("n_tot", _dp), ("ne_model", _dp), ("abundances", _dp), ("atm", _ip)]
+
+
+KORG_ECHEM = 7
+KORG_CHEM_MOL0 = 278
+KORG_CHEM_MAX_MOL = 384
+
+
 class BatchVjpItem(C.Structure):
     """korg_batch_vjp_item: one spectrum's cotangents and gradient outputs (device pointers)."""
     _fields_ = [("dflux", _dp), ("dcntm", _dp), ("grads", SynthGrads)]
@@ -158,6 +175,9 @@ def lib():
             L.korg_set_continuum_tables.argtypes = [vp, C.POINTER(ContinuumTables)]
             L.korg_continuum_absorption.argtypes = [vp, _dp, C.c_int64, C.POINTER(ContinuumLayers), _dp]
             L.korg_continuum_absorption_dev.argtypes = [vp, vp, C.c_int64, C.POINTER(ContinuumLayers), vp, vp]
+            L.korg_set_equilibrium_tables.argtypes = [vp, C.POINTER(EquilibriumTables)]
+            L.korg_chemical_equilibrium.argtypes = [vp, C.POINTER(ChemLayers), C.c_int32, _dp, _ip, _dp]
+            L.korg_chemical_equilibrium_dev.argtypes = [vp, C.POINTER(ChemLayers), C.c_int32, vp, vp, vp, vp]
             L.korg_get_tile_config.argtypes = [vp, C.c_int32, C.c_int, _ip, _ip, _ip, _ip]
             L.korg_set_tile_config.argtypes = [vp, C.c_int32, C.c_int, C.c_int32, C.c_int32, C.c_int32]
             L.korg_device_status.argtypes = [vp]
@@ -186,7 +206,8 @@ def exported_symbols():
             "korg_interpolate_molecular_cross_section_dev", "korg_device_status",
             "korg_selftest_wait_timeout", "korg_apply_lsf_dev", "korg_apply_lsf_vjp_dev", "korg_lsf_windows_dev",
             "korg_lsf_matrix_values_dev", "korg_apply_rotation_dev", "korg_apply_rotation_vjp_dev",
-            "korg_set_continuum_tables", "korg_continuum_absorption", "korg_continuum_absorption_dev"]
+            "korg_set_continuum_tables", "korg_continuum_absorption", "korg_continuum_absorption_dev",
+            "korg_set_equilibrium_tables", "korg_chemical_equilibrium", "korg_chemical_equilibrium_dev"]
 
 
 def _p(a, kind=_dp):
@@ -277,6 +298,24 @@ class Context:
                                  f("peach_HeII_sigma"), (_dp * 4)(*[f(f"peach_{p}_D") for p in peach]))
             self.check(self.lib.korg_set_continuum_tables(self.h, C.byref(ct)))
             self.have_continuum = True
+
+    def ensure_equilibrium(self, tables=None):
+        """Upload chemical-equilibrium tables (korg_set_equilibrium_tables): the default ones once,
+        or ``tables`` (a statmech.EquilibriumTables) when they are not the ones already loaded.
+        Returns the tables in use."""
+        from .statmech import EquilibriumTables as HostTables, default_equilibrium_tables
+        t = tables if tables is not None else default_equilibrium_tables()
+        if getattr(self, "equilibrium_tables", None) is not t:
+            keep = Keep()
+            f = lambda a: _p(keep.f64(a))
+            i = lambda a: _p(keep.i32(a), _ip)
+            et = EquilibriumTables(len(t.lnT), f(t.lnT), f(t.U_u), f(t.U_z), f(t.chi), len(t.molecules), i(t.atoms),
+                                   i(t.charge), i(t.kind), _p(keep.i64(t.off), C.POINTER(C.c_int64)), f(t.spl_t),
+                                   f(t.spl_u), f(t.spl_z), f(t.D00), f(t.lmr))
+            self.check(self.lib.korg_set_equilibrium_tables(self.h, C.byref(et)))
+            self.equilibrium_tables = t
+        assert isinstance(t, HostTables)
+        return t
 
     def stats(self):
         s = Stats()

@@ -274,15 +274,29 @@ def _merge_windows(wins):
 def prepare_synthesis(atm, linelist: LineList, A_X, wavelengths, vmic=1.0, line_buffer=10.0, cntm_step=1.0,
                       hydrogen_lines=True, use_MHD_for_hydrogen_lines=None, hydrogen_line_window_size=150,
                       line_cutoff_threshold=3e-4, use_internal_reference_linelist=True,
-                      chemical_equilibrium=None, continuum_opacity=None, continuum="standin", ctx=None):
-    """The host part of synthesize (src/synthesize.jl:159-262).  Chemical equilibrium comes from
-    ``chemical_equilibrium(T, n_tot, A_X) -> (ne, {Species: n})`` (default: the stand-in of
-    :mod:`korg_gb300.standin`).  The continuum: ``continuum="gpu"`` evaluates Korg's continuum
-    absorption (every term but metal bound-free) on the device (:mod:`korg_gb300.continuum`);
-    ``"standin"`` (the default, CPU only) the compact stand-in of :mod:`korg_gb300.standin`; a
-    ``continuum_opacity(wls_cm, T, ne, n_HI, n_HII) -> alpha`` callable overrides both."""
+                      chemical_equilibrium=None, continuum_opacity=None, continuum="standin", chemistry="standin",
+                      ctx=None):
+    """The host part of synthesize (src/synthesize.jl:159-262).  Chemical equilibrium:
+    ``chemistry="gpu"`` solves Korg's chemical equilibrium for every layer on the device
+    (:mod:`korg_gb300.statmech`, src/synthesize.jl:207-219), starting from the atmosphere's n_e;
+    ``"standin"`` (the default, CPU only) uses the compact stand-in of :mod:`korg_gb300.standin`;
+    a ``chemical_equilibrium(T, n_tot, A_X) -> (ne, {Species: n})`` callable overrides both.  The
+    continuum: ``continuum="gpu"`` evaluates Korg's continuum absorption (every term but metal
+    bound-free) on the device (:mod:`korg_gb300.continuum`); ``"standin"`` (the default, CPU only)
+    the compact stand-in; a ``continuum_opacity(wls_cm, T, ne, n_HI, n_HII) -> alpha`` callable
+    overrides both."""
     from . import standin
-    chem = chemical_equilibrium or standin.chemical_equilibrium
+    if chemical_equilibrium is not None:
+        chem = chemical_equilibrium
+    elif chemistry == "gpu":
+        def chem(T, n_tot, A_X):
+            from .statmech import chemical_equilibrium as solve
+            ab = 10.0 ** (np.asarray(A_X, np.float64) - 12)  # :204-209
+            return solve(T, n_tot, atm.ne, ab / ab.sum(), ctx=ctx)
+    elif chemistry == "standin":
+        chem = standin.chemical_equilibrium
+    else:
+        raise ValueError(f'chemistry must be "gpu" or "standin", got {chemistry!r}')
     cont = continuum_opacity or standin.continuum_opacity
     wls = wavelengths if isinstance(wavelengths, Wavelengths) else Wavelengths(wavelengths)
     use_MHD = (wls.all_wls[-1] < 13_000e-8) if use_MHD_for_hydrogen_lines is None else use_MHD_for_hydrogen_lines
@@ -363,10 +377,12 @@ def synthesize_prepared(inp: SynthesisInputs, precision="mixed", return_alpha=Fa
 
 
 def synthesize(atm, linelist, A_X, wavelengths, precision="mixed", return_alpha=False, ctx=None, continuum="gpu",
-               **kwargs):
+               chemistry="gpu", **kwargs):
     """``synthesize(atm, linelist, A_X, wavelengths; kwargs...)`` (src/synthesize.jl:138-324), with
-    the continuum absorption evaluated on the device by default (see :func:`prepare_synthesis`)."""
-    inp = prepare_synthesis(atm, linelist, A_X, wavelengths, continuum=continuum, ctx=ctx, **kwargs)
+    chemical equilibrium and continuum absorption evaluated on the device by default (see
+    :func:`prepare_synthesis`)."""
+    inp = prepare_synthesis(atm, linelist, A_X, wavelengths, continuum=continuum, chemistry=chemistry, ctx=ctx,
+                            **kwargs)
     return synthesize_prepared(inp, precision=precision, return_alpha=return_alpha, ctx=ctx)
 
 

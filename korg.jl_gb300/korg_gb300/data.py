@@ -39,6 +39,78 @@ def default_partition_funcs():
         except (KeyError, ValueError):
             continue
         out[spec] = CubicSpline(lnT, U, extrapolate=True)
+    e = _npz("equilibrium_constants.npz")  # ExoMol polyatomics, astrophysical convention (:203-226)
+    for k, name in enumerate(e["poly_names"]):
+        a, b = e["poly_off"][k], e["poly_off"][k + 1]
+        with np.errstate(divide="ignore", invalid="ignore"):  # H3+'s table starts at T = 0 (a NaN spline)
+            out[parse_species(str(name))] = CubicSpline(np.log(e["poly_T"][a:b]), e["poly_U"][a:b] / e["poly_g_ns"][k],
+                                                        extrapolate=True)
+    return out
+
+
+class PolyatomicLogK:
+    """log10 of the partial-pressure equilibrium constant of a polyatomic molecule from its
+    atomization energy D00 (kJ/mol) and partition functions (src/read_statmech_quantities.jl:66-89)."""
+
+    def __init__(self, spec, D00_kJmol, partition_funcs):
+        from .constants import hplanck_cgs, kboltz_cgs
+        from .species import Species, atomic_masses
+        self.spec, self.D00 = spec, D00_kJmol * 0.01036  # kJ/mol -> eV
+        self.Zs = spec.atoms
+        self.U_atoms = [partition_funcs[Species([Z], 0)] for Z in self.Zs]
+        self.U_mol = partition_funcs[spec]
+        self.log_masses_ratio = sum(np.log10(atomic_masses[Z - 1]) for Z in self.Zs) - np.log10(spec.mass())
+        self._h, self._k = hplanck_cgs, kboltz_cgs
+
+    def log_nK(self, logT):
+        """log10 of the number-density equilibrium constant n(A)n(B).../n(mol)."""
+        from .constants import kboltz_eV
+        n = len(self.Zs)
+        prod = 1.0
+        for U in self.U_atoms:
+            prod = prod * U(logT)
+        log_Us_ratio = np.log10(prod / self.U_mol(logT))
+        T = np.exp(logT)
+        log_tU = 1.5 * np.log10(2 * np.pi * self._k * T / self._h ** 2)
+        return ((n - 1) * log_tU + 1.5 * self.log_masses_ratio + log_Us_ratio
+                - self.D00 / (kboltz_eV * T * np.log(10)))
+
+    def __call__(self, logT):
+        return self.log_nK(logT) + (len(self.Zs) - 1) * np.log10(self._k * np.exp(logT))
+
+
+C2_CORRECTION_EV = 6.24 - 6.371  # Visser+ 2019 minus Barklem & Collet D0 of C2 (eV)
+
+
+@functools.lru_cache(maxsize=None)
+def barklem_collet_log_K_tables():
+    """[(Species, ln T knots, log10 K)] of the Barklem & Collet molecules with the C2 dissociation
+    energy corrected to Visser+ 2019 (src/read_statmech_quantities.jl:101-130): the non-finite
+    knots of each molecule are dropped."""
+    from .constants import kboltz_eV
+    e = _npz("equilibrium_constants.npz")
+    out = []
+    for name, lnT, logK in zip(e["bc_mols"], e["bc_lnTs"], e["bc_logKs"]):
+        spec = parse_species(str(name))
+        logK = logK.copy()
+        if spec == parse_species("C2"):
+            logK += np.log10(np.e) / (kboltz_eV * np.exp(lnT)) * C2_CORRECTION_EV
+        mask = np.isfinite(lnT)
+        out.append((spec, lnT[mask], logK[mask]))
+    return out
+
+
+@functools.lru_cache(maxsize=None)
+def default_log_equilibrium_constants():
+    """Species -> log10 K(ln T) in partial-pressure form, as Korg's
+    default_log_equilibrium_constants (src/read_statmech_quantities.jl:53-98): flat-extrapolated
+    cubic splines for the Barklem & Collet diatomics, PolyatomicLogK for the polyatomics."""
+    out = {spec: CubicSpline(lnT, logK, extrapolate=True) for spec, lnT, logK in barklem_collet_log_K_tables()}
+    e = _npz("equilibrium_constants.npz")
+    pf = default_partition_funcs()
+    for name, D00 in zip(e["atomization_names"], e["atomization_kJmol"]):
+        spec = parse_species(str(name))
+        out[spec] = PolyatomicLogK(spec, float(D00), pf)
     return out
 
 

@@ -198,6 +198,57 @@ def continuum(root):
     np.savez_compressed(os.path.join(HERE, "continuum_tables.npz"), **out)
 
 
+def _julia_nested_dict(src, name):
+    """``name = Dict(Z => Dict(A => v, ...), ...)`` as {Z: {A: v}} (src/isotopic_data.jl)."""
+    import re
+    start = src.index(name)
+    i = src.index("Dict(", start) + 5
+    depth, j = 1, i
+    while depth:
+        depth += {"(": 1, ")": -1}.get(src[j], 0)
+        j += 1
+    body = "\n".join(line.split("#")[0] for line in src[i:j - 1].split("\n"))
+    out = {}
+    for z, inner in re.findall(r"(\d+)\s*=>\s*Dict\(([^)]*)\)", body):
+        out[int(z)] = {int(a): float(v) for a, v in re.findall(r"(\d+)\s*=>\s*([-+0-9.eE]+)", inner)}
+    return out
+
+
+def equilibrium(root):
+    """Molecular equilibrium constants (src/read_statmech_quantities.jl:53-130, 203-226):
+    Barklem & Collet log10 K tables (molecule names, ln T knots, log10 K, as stored), the ExoMol
+    polyatomic partition functions (T, U as stored) with the nuclear-spin degeneracy of each
+    molecule's most abundant isotopologue, and the polyatomic atomization energies (kJ/mol)."""
+    f = hdf5lite.File(os.path.join(root, "data", "barklem_collet_2016", "barklem_collet_ks.h5"))
+    mols = [str(m) for m in f.read("mols")]
+    lnTs, logKs = f.read("lnTs").T.copy(), f.read("logKs").T.copy()  # file order is (T, molecule)
+    g = hdf5lite.File(os.path.join(root, "data", "polyatomic_partition_funcs", "polyatomic_partition_funcs.h5"))
+    poly, T, U, off = sorted(g.keys()), [], [], [0]
+    for name in poly:
+        T.append(g.read(name + "/temp"))
+        U.append(g.read(name + "/partition_function"))
+        off.append(off[-1] + len(T[-1]))
+    iso = open(os.path.join(root, "src", "isotopic_data.jl")).read()
+    abund = _julia_nested_dict(iso, "isotopic_abundances")
+    spin = _julia_nested_dict(iso, "isotopic_nuclear_spin_degeneracies")
+    g_ns = []
+    for name in poly:  # product over atoms of the most abundant isotope's degeneracy (:211-219)
+        prod = 1.0
+        for Z in parse_species(name).atoms:
+            A = max(abund[Z], key=abund[Z].get)
+            prod *= spin[Z][A]
+        g_ns.append(prod)
+    rows = list(csv.DictReader(open(os.path.join(root, "data", "polyatomic_partition_funcs",
+                                                 "atomization_energies.csv"))))
+    np.savez_compressed(
+        os.path.join(HERE, "equilibrium_constants.npz"),
+        bc_mols=np.array(mols), bc_lnTs=lnTs, bc_logKs=logKs,
+        poly_names=np.array(poly), poly_T=np.concatenate(T), poly_U=np.concatenate(U),
+        poly_off=np.array(off, np.int64), poly_g_ns=np.array(g_ns),
+        atomization_names=np.array([r["spec"] for r in rows]),
+        atomization_kJmol=np.array([float(r["energy"]) for r in rows]))
+
+
 if __name__ == "__main__":
     root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("KORG_REFERENCE")
     if not root:
@@ -206,4 +257,5 @@ if __name__ == "__main__":
     partition(root)
     alpha5000(root)
     continuum(root)
+    equilibrium(root)
     print("wrote", sorted(x for x in os.listdir(HERE) if x.endswith(".npz")))

@@ -343,7 +343,7 @@ class File:
         if node.kind != "dataset":
             raise ValueError(f"{path} is a group")
         dt, shape, layout = node._dtype, node._shape, node._layout
-        if dt is None or dt.dtype is None:
+        if dt is None or (dt.dtype is None and dt.cls not in (3, 9)):
             raise NotImplementedError(f"{path}: unsupported datatype")
         n = int(np.prod(shape)) if shape else 1
         if layout[0] == "contiguous":
@@ -354,8 +354,31 @@ class File:
                 raw = self.buf[addr:addr + n * dt.size]
         else:
             raw = layout[1][:n * dt.size]
-        arr = np.frombuffer(raw, dtype=dt.dtype).astype(dt.dtype.newbyteorder("="))
-        return arr.reshape(shape) if shape else arr[0].item()
+        if dt.cls == 3:  # fixed-length strings, NUL padded
+            vals = [raw[i * dt.size:(i + 1) * dt.size].split(b"\x00")[0].decode() for i in range(n)]
+        elif dt.cls == 9:  # variable-length strings: (length, global heap address, object index)
+            vals = [self._global_heap_object(*struct.unpack_from("<IQI", raw, 16 * i)) for i in range(n)]
+        else:
+            arr = np.frombuffer(raw, dtype=dt.dtype).astype(dt.dtype.newbyteorder("="))
+            return arr.reshape(shape) if shape else arr[0].item()
+        return np.array(vals, dtype=object).reshape(shape) if shape else vals[0]
+
+    def _global_heap_object(self, length, collection, index):
+        """The bytes of object ``index`` of a global heap collection ("GCOL"), decoded as text."""
+        b = self.buf
+        if b[collection:collection + 4] != b"GCOL":
+            raise ValueError("bad global heap collection")
+        end = collection + self._u64(collection + 8)
+        p = collection + 16
+        while p + 16 <= end:
+            idx = struct.unpack_from("<H", b, p)[0]
+            size = self._u64(p + 8)
+            if idx == 0:  # free space ends the collection
+                break
+            if idx == index:
+                return b[p + 16:p + 16 + min(size, length)].decode()
+            p += 16 + (size + 7) // 8 * 8
+        raise ValueError(f"global heap object {index} not found")
 
     def __getitem__(self, path):
         return self.root[path]

@@ -61,6 +61,8 @@ class Species(tuple):
         if self.ismolecule():
             out = "".join(atomic_symbols[z - 1] for z in self.atoms)
             return out + ("+" if self.charge == 1 else "")
+        if self.charge < 0:
+            return atomic_symbols[self.atoms[0] - 1] + "-" * -self.charge
         return f"{atomic_symbols[self.atoms[0] - 1]} {_roman[self.charge]}"
 
     __repr__ = __str__
@@ -79,6 +81,8 @@ def parse_species(code: str) -> Species:
             charge = int(ion) - 1 if ion.isdigit() else 0
     elif s.endswith("+"):
         s, charge = s[:-1], 1
+    elif s.endswith("-"):
+        s, charge = s[:-1], -1
     atoms = []
     for sym, count in re.findall(r"([A-Z][a-z]?)(\d*)", s):
         atoms += [atomic_numbers[sym]] * (int(count) if count else 1)
