@@ -221,8 +221,9 @@ typedef struct {
 } korg_chem_layers;
 /* densities [L][KORG_CHEM_MOL0 + n_mol]: n_e, n(Z, q) for q = 0, 1, 2 (H III is 0), n(H-), then
  * each molecule in table order.  status [L]: KORG_CHEM_OK, or why the layer failed; info
- * [L][4] (may be NULL): Newton iterations, solves, the log xi reached (or where the
- * continuation stopped), the last residual inf-norm.  The host entry point returns KORG_ECHEM
+ * [L][5] (may be NULL): Newton iterations, solves, the log xi reached (or where the
+ * continuation stopped), the last residual inf-norm, and the Newton steps whose linear solve
+ * fell back from FP32 factors with FP64 refinement to FP64 elimination.  The host entry point returns KORG_ECHEM
  * when any layer failed (densities of the other layers are valid); _dev takes device pointers
  * and is stream-ordered (read status after the stream). */
 #define KORG_CHEM_NE 0

@@ -1509,8 +1509,9 @@ KORG_API int korg_set_equilibrium_tables(korg_ctx* ctx, const korg_equilibrium_t
         if (!(t->lnT[k] > t->lnT[k - 1])) return set_err(ctx, KORG_EINVAL, "partition-function knots not increasing");
     const int M = t->n_mol;
     // derived per-molecule data: atom count, distinct atoms with counts, element incidence lists
-    std::vector<int32_t> nat(M), ndist(M), dist_Z(size_t(M) * CE_MAXATOMS, 0), dist_cnt(size_t(M) * CE_MAXATOMS, 0);
+    std::vector<int32_t> nat(M);
     std::vector<std::vector<std::pair<int32_t, int32_t>>> inc(CE_NZ);
+    std::map<std::pair<int32_t, int32_t>, std::vector<std::pair<int32_t, int32_t>>> pairs;  // (Z, W) -> (m, cnt_Z cnt_W)
     bool polyatomic = false;
     for (int m = 0; m < M; m++) {
         const int32_t* at = t->atoms + size_t(m) * CE_MAXATOMS;
@@ -1529,19 +1530,15 @@ KORG_API int korg_set_equilibrium_tables(korg_ctx* ctx, const korg_equilibrium_t
         if (t->off[m + 1] - t->off[m] < 2 || t->off[m] < 0)
             return set_err(ctx, KORG_EINVAL, "molecule %d: spline needs two knots", m);
         nat[m] = n;
-        int d = 0;
+        std::vector<std::pair<int32_t, int32_t>> dist;  // distinct atoms and their counts
         for (int j = 0; j < n; j++) {
-            if (j && at[j] == at[j - 1]) {
-                dist_cnt[size_t(m) * CE_MAXATOMS + d - 1]++;
-            } else {
-                dist_Z[size_t(m) * CE_MAXATOMS + d] = at[j];
-                dist_cnt[size_t(m) * CE_MAXATOMS + d] = 1;
-                d++;
-            }
+            if (j && at[j] == at[j - 1]) dist.back().second++;
+            else dist.push_back({at[j], 1});
         }
-        ndist[m] = d;
-        for (int j = 0; j < d; j++)
-            inc[dist_Z[size_t(m) * CE_MAXATOMS + j] - 1].push_back({m, dist_cnt[size_t(m) * CE_MAXATOMS + j]});
+        for (const auto& a : dist) {
+            inc[a.first - 1].push_back({m, a.second});
+            for (const auto& b : dist) pairs[{a.first - 1, b.first - 1}].push_back({m, a.second * b.second});
+        }
     }
     if (polyatomic && (!t->D00 || !t->lmr)) return set_err(ctx, KORG_EINVAL, "polyatomic molecules need D00 and lmr");
     std::vector<int32_t> inc_ptr(CE_NZ + 1, 0), inc_mol, inc_cnt;
@@ -1552,6 +1549,21 @@ KORG_API int korg_set_equilibrium_tables(korg_ctx* ctx, const korg_equilibrium_t
         }
         inc_ptr[Z + 1] = int32_t(inc_mol.size());
     }
+    if (inc_mol.size() > size_t(CE_MAXINC) || pairs.size() > size_t(CE_MAXPAIR))
+        return set_err(ctx, KORG_EINVAL, "molecule set too large: %zu incidences (max %d), %zu element pairs (max %d)",
+                       inc_mol.size(), CE_MAXINC, pairs.size(), CE_MAXPAIR);
+    std::vector<int32_t> pair_row, pair_col, pair_ptr(1, 0), pair_mol, pair_coef;
+    for (const auto& pr : pairs) {
+        pair_row.push_back(pr.first.first);
+        pair_col.push_back(pr.first.second);
+        for (const auto& e : pr.second) {
+            pair_mol.push_back(e.first);
+            pair_coef.push_back(e.second);
+        }
+        pair_ptr.push_back(int32_t(pair_mol.size()));
+    }
+    if (pair_mol.size() > size_t(CE_MAXPENT))
+        return set_err(ctx, KORG_EINVAL, "molecule set too large: %zu pair entries (max %d)", pair_mol.size(), CE_MAXPENT);
     const int64_t nspl = M ? t->off[M] : 0;
     std::vector<double> zeros(std::max<int64_t>(M, 1), 0.0);
     std::vector<int32_t> izeros(1, 0);
@@ -1560,6 +1572,7 @@ KORG_API int korg_set_equilibrium_tables(korg_ctx* ctx, const korg_equilibrium_t
     ChemTables d{};
     d.nk = t->n_knots;
     d.n_mol = M;
+    d.n_pairs = int32_t(pair_row.size());
     const size_t nk = size_t(t->n_knots);
     auto ip = [&](const std::vector<int32_t>& v) { return v.empty() ? (const void*)izeros.data() : (const void*)v.data(); };
     std::vector<Piece> pcs = {
@@ -1575,12 +1588,14 @@ KORG_API int korg_set_equilibrium_tables(korg_ctx* ctx, const korg_equilibrium_t
         {polyatomic ? (const void*)t->D00 : zeros.data(), 8 * (polyatomic ? size_t(M) : 1), (const void**)&d.D00},
         {polyatomic ? (const void*)t->lmr : zeros.data(), 8 * (polyatomic ? size_t(M) : 1), (const void**)&d.lmr},
         {ip(nat), 4 * std::max<size_t>(M, 1), (const void**)&d.nat},
-        {ip(ndist), 4 * std::max<size_t>(M, 1), (const void**)&d.ndist},
-        {ip(dist_Z), 4 * std::max<size_t>(dist_Z.size(), 1), (const void**)&d.dist_Z},
-        {ip(dist_cnt), 4 * std::max<size_t>(dist_cnt.size(), 1), (const void**)&d.dist_cnt},
         {inc_ptr.data(), 4 * inc_ptr.size(), (const void**)&d.inc_ptr},
         {ip(inc_mol), 4 * std::max<size_t>(inc_mol.size(), 1), (const void**)&d.inc_mol},
-        {ip(inc_cnt), 4 * std::max<size_t>(inc_cnt.size(), 1), (const void**)&d.inc_cnt}};
+        {ip(inc_cnt), 4 * std::max<size_t>(inc_cnt.size(), 1), (const void**)&d.inc_cnt},
+        {ip(pair_row), 4 * std::max<size_t>(pair_row.size(), 1), (const void**)&d.pair_row},
+        {ip(pair_col), 4 * std::max<size_t>(pair_col.size(), 1), (const void**)&d.pair_col},
+        {pair_ptr.data(), 4 * pair_ptr.size(), (const void**)&d.pair_ptr},
+        {ip(pair_mol), 4 * std::max<size_t>(pair_mol.size(), 1), (const void**)&d.pair_mol},
+        {ip(pair_coef), 4 * std::max<size_t>(pair_coef.size(), 1), (const void**)&d.pair_coef}};
     size_t total = 0;
     for (const Piece& q : pcs) {
         if (!q.src) return set_err(ctx, KORG_EINVAL, "null equilibrium table");
@@ -1670,7 +1685,7 @@ KORG_API int korg_chemical_equilibrium(korg_ctx* ctx, const korg_chem_layers* y,
                                          ctx->stream));
     KCUDA(cudaMemcpyAsync(dens, b + o_d, 8 * size_t(L) * nspec, cudaMemcpyDeviceToHost, ctx->stream));
     KCUDA(cudaMemcpyAsync(status, b + o_s, 4 * size_t(L), cudaMemcpyDeviceToHost, ctx->stream));
-    std::vector<double> inf(size_t(L) * CE_NINFO);
+    std::vector<double> inf(size_t(L) * CE_NINFO);  // iterations, solves, log xi, inf-norm, FP64 steps
     KCUDA(cudaMemcpyAsync(inf.data(), b + o_i, 8 * inf.size(), cudaMemcpyDeviceToHost, ctx->stream));
     KCUDA(cudaStreamSynchronize(ctx->stream));
     if (info) memcpy(info, inf.data(), 8 * inf.size());

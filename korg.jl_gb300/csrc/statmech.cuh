@@ -1,5 +1,5 @@
 // statmech.cuh -- chemical equilibrium on the device: chemical_equilibrium (src/statmech.jl:148-206)
-// for every layer of one or many atmospheres, one thread block per layer, FP64.
+// for every layer of one or many atmospheres, one thread block per layer.
 //
 // Unknowns x = (log10 n(X I) for the 92 elements, log10 n_e).  The residuals
 // (setup_chemical_equilibrium_residuals, src/statmech.jl:360-439) are nuclei conservation of each
@@ -8,21 +8,32 @@
 // plain solve fails, a continuation on log xi, the log10 scale of every molecule and H- density
 // (_solve_chemical_equilibrium, src/statmech.jl:215-305).
 //
-// The reference differentiates the residuals with ForwardDiff; here the Jacobian is assembled
-// analytically.  With n_mol = 10^(sum of its constituents' x - log nK + log xi) every density is
-// an exponential of a linear form in x, so
+// Jacobian.  The reference differentiates the residuals with ForwardDiff; here the Jacobian is
+// assembled analytically.  With n_mol = 10^(sum of its constituents' x - log nK + log xi) every
+// density is an exponential of a linear form in x, so
 //   d F_Z / d x_W = ln10 [ sum_mol cnt_Z(mol) cnt_W(mol) n_mol + delta_ZW (n_I + n_II + n_III)_Z
 //                          - ab_Z d n_nuclei / d x_W ] / (ab_Z n_tot)
-// and similarly for the n_e column and the charge row.  The molecule sums run over a per-element
-// incidence list (element -> molecules containing it, with multiplicity) in a fixed order, so a
-// layer's result does not depend on thread timing.
+// and similarly for the n_e column and the charge row.  The molecule sums run over fixed lists
+// (element -> molecules containing it; (row, column) pair -> molecules containing both), one
+// thread per list, so a layer's result does not depend on thread timing.
 //
-// Layout: the augmented system [J | F] sits column-major in shared memory (column c at
-// A[c * CE_LD + r]).  Gaussian elimination with partial pivoting (largest |entry| in the pivot
-// column, lowest row on ties, as LAPACK's getrf) keeps rows in place and a logical-to-physical
-// row permutation; the trailing update is spread over all threads; back substitution runs in one
-// warp.  The work per Newton step is ~93^3/3 FP64 FMAs; GB300's FP64 pipe makes that the cost
-// that bounds the kernel.
+// Newton step J s = F.  The system is assembled in FP64 (column-major in shared memory) and
+// equilibrated with exact powers of two (rows, then columns, scaled to a largest entry in [1, 2)):
+// the condition number of the equilibrated Jacobian at stellar solutions is ~10^2, against up to
+// 10^12 unscaled.  The equilibrated matrix is factorised in FP32 (GB300 runs FP32 FMAs at 64x the
+// FP64 rate) with partial pivoting, and the FP64 solution is recovered by iterative refinement
+// as LAPACK's dsgesv does it: residuals F - J s in FP64, corrections from the FP32 factors, until
+// the equilibrated residual is at the level of a backward-stable FP64 solve.  The refined step
+// is then as accurate as an FP64 elimination (equal to it up to the conditioning of the system).
+// When the refinement stops contracting (an ill-conditioned start of a continuation) or the FP32
+// factorisation meets a zero pivot, the same elimination runs in FP64 on the FP64 matrix, as
+// LAPACK's getrf + getrs would.
+//
+// Elimination: partial pivoting (largest |entry| of the pivot column, lowest row on ties) with
+// rows left in place and a double-buffered logical-to-physical row permutation; one barrier per
+// column (warps over columns, lanes over rows; multipliers written back one column late); warp
+// 0, which updates the next pivot column, also picks the next pivot.  Triangular solves run in
+// one warp with the vector in registers.
 //
 // Every loop is bounded: at most KORG_CHEM_MAX_ITER Newton iterations per layer in total (the
 // reference's own loops are finite but its worst case is ~5e5 iterations); a layer that runs out
@@ -34,13 +45,18 @@ namespace korg {
 
 constexpr int CE_NZ = 92;        // elements H..U
 constexpr int CE_N = 93;         // unknowns
-constexpr int CE_NCOL = 94;      // columns of the augmented matrix (J and the residuals)
+constexpr int CE_NCOL = 94;      // columns of the FP64 system (J and the residuals)
 constexpr int CE_LD = 96;        // column stride (rows padded)
 constexpr int CE_MAXMOL = 384;
-constexpr int CE_THREADS = 128;
+constexpr int CE_THREADS = 256;
+constexpr int CE_WARPS = CE_THREADS / 32;
 constexpr int CE_MAXATOMS = 6;
 constexpr int CE_MAX_ITER = 20000;
-constexpr int CE_NINFO = 4;
+constexpr int CE_NINFO = 5;
+constexpr int CE_REFINE_MAX = 8;
+constexpr int CE_MAXINC = 1024;    // element -> molecule incidences
+constexpr int CE_MAXPAIR = 1024;   // (Z, W) pairs sharing a molecule
+constexpr int CE_MAXPENT = 2048;   // molecule entries of the pair lists
 
 // Device tables (one buffer carved by the host).  The incidence lists are derived on the host.
 struct ChemTables {
@@ -53,8 +69,9 @@ struct ChemTables {
     const double *t, *u, *z;             // concatenated molecule splines
     const double *D00, *lmr;             // polyatomics
     const int32_t *nat;                  // atoms per molecule, with multiplicity
-    const int32_t *ndist, *dist_Z, *dist_cnt;  // distinct atoms [n_mol], [n_mol][6] x2
     const int32_t *inc_ptr, *inc_mol, *inc_cnt;  // element Z-1 -> (molecule, count) at [inc_ptr[Z-1], inc_ptr[Z])
+    int32_t n_pairs;                     // (Z, W) with a molecule containing both
+    const int32_t *pair_row, *pair_col, *pair_ptr, *pair_mol, *pair_coef;  // coef = cnt_Z * cnt_W
 };
 
 struct ChemLayersDev {
@@ -94,12 +111,28 @@ __device__ inline double translational_U(double m, double T) {  // src/statmech.
 }
 
 // warp arg-max of (value, index): larger value wins, the lower index on ties; index < 0 = none
-__device__ inline void warp_argmax(double& v, int& i) {
+template <typename T>
+__device__ inline void warp_argmax(T& v, int& i) {
     for (int o = 16; o; o >>= 1) {
-        const double v2 = __shfl_xor_sync(0xffffffffu, v, o);
+        const T v2 = __shfl_xor_sync(0xffffffffu, v, o);
         const int i2 = __shfl_xor_sync(0xffffffffu, i, o);
         if (i2 >= 0 && (i < 0 || v2 > v || (v2 == v && i2 < i))) {
             v = v2;
+            i = i2;
+        }
+    }
+}
+
+// the same, carrying the signed value of the winning entry
+template <typename T>
+__device__ inline void warp_argmax_signed(T& v, T& sv, int& i) {
+    for (int o = 16; o; o >>= 1) {
+        const T v2 = __shfl_xor_sync(0xffffffffu, v, o);
+        const T s2 = __shfl_xor_sync(0xffffffffu, sv, o);
+        const int i2 = __shfl_xor_sync(0xffffffffu, i, o);
+        if (i2 >= 0 && (i < 0 || v2 > v || (v2 == v && i2 < i))) {
+            v = v2;
+            sv = s2;
             i = i2;
         }
     }
@@ -110,31 +143,366 @@ __device__ inline double warp_sum(double v) {
     return v;
 }
 
+__device__ inline long long warp_max_ll(long long v) {
+    for (int o = 16; o; o >>= 1) v = max(v, (long long)__shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// |v| as its IEEE bit pattern: for finite doubles the order of the patterns is the order of |v|
+__device__ inline long long abits(double v) { return __double_as_longlong(v) & 0x7fffffffffffffffLL; }
+
+// v * 2^-e rounded to FP32 with integer operations (v finite; results below FP32's normal range
+// flush to zero, above it saturate to the largest float)
+__device__ inline float scaled_to_float(double v, int e) {
+    const long long b = __double_as_longlong(v);
+    const long long a = b & 0x7fffffffffffffffLL;
+    if (a == 0) return 0.0f;
+    const int ex = int(a >> 52) - 1023 - e;  // unbiased exponent of the scaled value
+    if (ex < -126) return 0.0f;
+    const unsigned sign = unsigned((unsigned long long)b >> 32) & 0x80000000u;
+    if (ex > 127) return __uint_as_float(sign | 0x7f7fffffu);
+    const unsigned long long mant = (unsigned long long)(a & 0xfffffffffffffULL);
+    unsigned fb = (unsigned(ex + 127) << 23) + unsigned((mant + (1ULL << 28)) >> 29);  // carry rounds up the exponent
+    return __uint_as_float(sign | fb);
+}
+
 }  // namespace ce
 
 struct CeShared {
-    double A[CE_NCOL * CE_LD];
-    double x[CE_N], xs[CE_N], x0[CE_N], y[CE_N], rinv[CE_N], sol[CE_N];
+    double A[CE_NCOL * CE_LD];  // FP64 [J | F], column-major
+    float B[CE_N * CE_LD];      // FP32 equilibrated J, then its LU factors
+    double x[CE_N], xs[CE_N], x0[CE_N], sol[CE_N], res[CE_N];
     double lwII[CE_NZ], lwIII[CE_NZ], rat1[CE_NZ], rat2[CE_NZ], e1[CE_NZ], e2[CE_NZ];
     double ab[CE_NZ], inv_scale[CE_NZ];
     double nI[CE_NZ], nII[CE_NZ], nIII[CE_NZ];
-    double fm[CE_NZ], Sq[CE_NZ], dN[CE_N], F[CE_N];
+    double fm[CE_NZ], Sq[CE_NZ], dNn[CE_N];
     double lognK[CE_MAXMOL], nmol[CE_MAXMOL];
-    double candv[4];
-    double red[4];
-    double ne, nHm, nn_mol, qn, dNe_mol, ion1, ion2, pinv, lognK_Hm, transU, lnT;
-    int candi[4];
-    int perm[CE_N];
-    int prow, flag;
+    double uinv64[CE_N];
+    float uinv32[CE_N], vec32[CE_N];
+    double red[CE_WARPS], red2[CE_WARPS];
+    long long redl[4][CE_WARPS];
+    double ne, nHm, nn_mol, qn, dNe_mol, ion1, ion2, lognK_Hm, transU, lnT;
+    double piv64[2];
+    float piv32[2];
+    int perm[2][CE_LD];
+    // the molecule tables, copied from global memory once per layer
+    unsigned char m_atoms[CE_MAXMOL * CE_MAXATOMS], m_charge[CE_MAXMOL], m_nat[CE_MAXMOL];
+    short inc_ptr[CE_NZ + 1], inc_mol[CE_MAXINC];
+    unsigned char inc_cnt[CE_MAXINC];
+    unsigned char pair_row[CE_MAXPAIR], pair_col[CE_MAXPAIR], pair_coef[CE_MAXPENT];
+    short pair_ptr[CE_MAXPAIR + 1], pair_mol[CE_MAXPENT];
+    int rexp[CE_N], cexp[CE_N];
+    int pivi[2];
 };
+
+// block-wide max of a non-negative value (every thread gets it); two barriers
+__device__ inline double ce_block_max(CeShared& s, double v) {
+    for (int o = 16; o; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0) s.red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double m = s.red[0];
+    for (int w = 1; w < CE_WARPS; ++w) m = fmax(m, s.red[w]);
+    __syncthreads();
+    return m;
+}
+
+// LU factorisation with partial pivoting of the n x n column-major matrix M (stride CE_LD, rows
+// left in place): multipliers below the diagonal, U on and above it in logical row order; the
+// final logical-to-physical permutation in s.perm[(CE_N - 1) & 1]; uinv = reciprocals of U's
+// diagonal.  Returns false on a zero (or non-finite) pivot.  T = float or double.
+//
+// One barrier per column: every warp derives the multipliers of its rows from the pivot column
+// (read-only during the step) and updates its columns of the trailing matrix; warp 0, whose first
+// column is the next pivot column, also picks the next pivot, and writes this step's multipliers
+// into the pivot column during the next step, when nothing reads it any more.
+template <typename T>
+__device__ bool ce_lu(CeShared& s, T* M, T* uinv) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // pivot slots, double-buffered by step parity (read at a step's start, the next one written
+    // by warp 0 during the step)
+    T* piv = reinterpret_cast<T*>(sizeof(T) == 4 ? (void*)s.piv32 : (void*)s.piv64);
+    if (tid < CE_N) s.perm[0][tid] = tid;
+    if (warp == 0) {  // first pivot: column 0
+        T v = T(-1), sv = 0;
+        int bi = -1;
+        for (int i = lane; i < CE_N; i += 32)
+            if (bi < 0 || fabs(M[i]) > v) {
+                v = fabs(M[i]);
+                sv = M[i];
+                bi = i;
+            }
+        ce::warp_argmax_signed(v, sv, bi);
+        if (lane == 0) {
+            s.pivi[0] = bi;
+            piv[0] = sv;
+        }
+    }
+    __syncthreads();
+    bool ok = true;
+    int pr0 = -1, pr1 = -1, pr2 = -1;  // rows and multipliers of the previous step (warp 0 writes them)
+    T pl0 = 0, pl1 = 0, pl2 = 0;
+    for (int k = 0; k < CE_N; ++k) {
+        const int* PR = s.perm[k & 1];
+        int* PW = s.perm[(k + 1) & 1];
+        const int p = s.pivi[k & 1];
+        const T pv = piv[k & 1];
+        if (p < 0 || !(fabs(pv) > T(0)) || !isfinite(pv)) {
+            ok = false;
+            break;
+        }
+        const int pr = PR[p];
+        const T pinv = T(1) / pv;
+        if (tid == 0) uinv[k] = pinv;
+        if (warp == 0 && k > 0) {  // the previous step's multipliers into its pivot column
+            T* colp = M + (k - 1) * CE_LD;
+            if (pr0 >= 0) colp[pr0] = pl0;
+            if (pr1 >= 0) colp[pr1] = pl1;
+            if (pr2 >= 0) colp[pr2] = pl2;
+        }
+        if (k == CE_N - 1) break;
+        if (tid < CE_N) {  // permutation of the next step: logical rows k and p exchange
+            const int i = tid;
+            PW[i] = i == k ? pr : (i == p ? PR[k] : PR[i]);
+        }
+        // this lane's rows (logical k+1+lane, +32, +64) and their multipliers
+        const int i0 = k + 1 + lane, i1 = i0 + 32, i2 = i0 + 64;
+        const T* colk = M + k * CE_LD;
+        int r0 = -1, r1 = -1, r2 = -1;
+        T l0 = 0, l1 = 0, l2 = 0;
+        if (i0 < CE_N) { r0 = i0 == p ? PR[k] : PR[i0]; l0 = colk[r0] * pinv; }
+        if (i1 < CE_N) { r1 = i1 == p ? PR[k] : PR[i1]; l1 = colk[r1] * pinv; }
+        if (i2 < CE_N) { r2 = i2 == p ? PR[k] : PR[i2]; l2 = colk[r2] * pinv; }
+        // trailing update, two columns at a time (loads first, then stores, for overlap)
+        int c = k + 1 + warp;
+        if (c == k + 1) {  // warp 0: the next pivot column first
+            T* col = M + c * CE_LD;
+            const T u = col[pr];
+            T a0 = 0, a1 = 0, a2 = 0;
+            if (r0 >= 0) a0 = fma(-l0, u, col[r0]);
+            if (r1 >= 0) a1 = fma(-l1, u, col[r1]);
+            if (r2 >= 0) a2 = fma(-l2, u, col[r2]);
+            if (r0 >= 0) col[r0] = a0;
+            if (r1 >= 0) col[r1] = a1;
+            if (r2 >= 0) col[r2] = a2;
+            T v = T(-1), sv = 0;
+            int bi = -1;
+            if (r0 >= 0) { v = fabs(a0); sv = a0; bi = i0; }
+            if (r1 >= 0 && fabs(a1) > v) { v = fabs(a1); sv = a1; bi = i1; }
+            if (r2 >= 0 && fabs(a2) > v) { v = fabs(a2); sv = a2; bi = i2; }
+            ce::warp_argmax_signed(v, sv, bi);
+            if (lane == 0) {
+                s.pivi[(k + 1) & 1] = bi;
+                piv[(k + 1) & 1] = sv;
+            }
+            c += CE_WARPS;
+        }
+        for (; c + CE_WARPS < CE_N; c += 2 * CE_WARPS) {
+            T* ca = M + c * CE_LD;
+            T* cb = ca + CE_WARPS * CE_LD;
+            const T ua = ca[pr], ub = cb[pr];
+            T a0 = 0, a1 = 0, a2 = 0, b0 = 0, b1 = 0, b2 = 0;
+            if (r0 >= 0) { a0 = ca[r0]; b0 = cb[r0]; }
+            if (r1 >= 0) { a1 = ca[r1]; b1 = cb[r1]; }
+            if (r2 >= 0) { a2 = ca[r2]; b2 = cb[r2]; }
+            if (r0 >= 0) { ca[r0] = fma(-l0, ua, a0); cb[r0] = fma(-l0, ub, b0); }
+            if (r1 >= 0) { ca[r1] = fma(-l1, ua, a1); cb[r1] = fma(-l1, ub, b1); }
+            if (r2 >= 0) { ca[r2] = fma(-l2, ua, a2); cb[r2] = fma(-l2, ub, b2); }
+        }
+        if (c < CE_N) {
+            T* col = M + c * CE_LD;
+            const T u = col[pr];
+            T a0 = 0, a1 = 0, a2 = 0;
+            if (r0 >= 0) a0 = col[r0];
+            if (r1 >= 0) a1 = col[r1];
+            if (r2 >= 0) a2 = col[r2];
+            if (r0 >= 0) col[r0] = fma(-l0, u, a0);
+            if (r1 >= 0) col[r1] = fma(-l1, u, a1);
+            if (r2 >= 0) col[r2] = fma(-l2, u, a2);
+        }
+        pr0 = r0; pr1 = r1; pr2 = r2;
+        pl0 = l0; pl1 = l1; pl2 = l2;
+        __syncthreads();
+    }
+    __syncthreads();
+    return ok;
+}
+
+// Solve L U x = P b in one warp (warp 0): b in physical row order, x in column order; M, perm
+// and uinv from ce_lu.  Other warps return at once.
+template <typename T>
+__device__ void ce_trisolve(const CeShared& s, const T* M, const T* uinv, const T* b, T* x) {
+    const int tid = threadIdx.x, lane = tid & 31;
+    if (tid >= 32) return;
+    const int* P = s.perm[(CE_N - 1) & 1];
+    const int i0 = lane, i1 = lane + 32, i2 = lane + 64;
+    const bool v2 = i2 < CE_N;
+    const int r0 = P[i0], r1 = P[i1], r2 = v2 ? P[i2] : 0;
+    T y0 = b[r0], y1 = b[r1], y2 = v2 ? b[r2] : T(0);
+    for (int j = 0; j < CE_N - 1; ++j) {  // forward: unit lower L
+        const T yj = __shfl_sync(0xffffffffu, j < 32 ? y0 : (j < 64 ? y1 : y2), j & 31);
+        const T* col = M + j * CE_LD;
+        if (i0 > j) y0 = fma(-col[r0], yj, y0);
+        if (i1 > j) y1 = fma(-col[r1], yj, y1);
+        if (v2 && i2 > j) y2 = fma(-col[r2], yj, y2);
+    }
+    for (int j = CE_N - 1; j >= 0; --j) {  // backward: U
+        const T yj = __shfl_sync(0xffffffffu, j < 32 ? y0 : (j < 64 ? y1 : y2), j & 31);
+        const T xj = yj * uinv[j];
+        if (lane == (j & 31)) {
+            if (j < 32) y0 = xj; else if (j < 64) y1 = xj; else y2 = xj;
+        }
+        const T* col = M + j * CE_LD;
+        if (i0 < j) y0 = fma(-col[r0], xj, y0);
+        if (i1 < j) y1 = fma(-col[r1], xj, y1);
+        if (v2 && i2 < j) y2 = fma(-col[r2], xj, y2);
+    }
+    x[i0] = y0;
+    x[i1] = y1;
+    if (v2) x[i2] = y2;
+}
+
+// The Newton step: s.sol = J^-1 F from the FP64 system in s.A.  Mixed-precision refinement on
+// the equilibrated FP32 copy first, the FP64 elimination when that does not converge.  Returns
+// false when J is singular or the step is not finite; *refined tells which path gave the step.
+__device__ bool ce_solve(CeShared& s, bool& refined) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // equilibration: row exponents, then column exponents of the row-scaled matrix
+    bool bad = false;
+    if (tid < CE_N) {
+        long long m = 0;
+        for (int c = 0; c < CE_N; ++c) {
+            const long long a = ce::abits(s.A[c * CE_LD + tid]);
+            bad |= a >= 0x7ff0000000000000LL;
+            m = max(m, a);
+        }
+        s.rexp[tid] = m ? int(m >> 52) - 1023 : 0;
+    }
+    if (__syncthreads_or(bad)) return false;
+    if (tid < CE_N) {
+        long long m = 0;
+        const double* col = s.A + tid * CE_LD;
+        for (int r = 0; r < CE_N; ++r) {
+            const long long a = ce::abits(col[r]);
+            if (a) m = max(m, a - ((long long)s.rexp[r] << 52));
+        }
+        s.cexp[tid] = m > 0 ? int(m >> 52) - 1023 : 0;
+    }
+    __syncthreads();
+    for (int idx = tid; idx < CE_N * CE_N; idx += CE_THREADS) {
+        const int c = idx / CE_N, r = idx - c * CE_N;
+        s.B[c * CE_LD + r] = ce::scaled_to_float(s.A[c * CE_LD + r], s.rexp[r] + s.cexp[c]);
+    }
+    if (tid < CE_N) {
+        s.sol[tid] = 0.0;
+        s.res[tid] = s.A[CE_N * CE_LD + tid];
+    }
+    __syncthreads();
+    // infinity norm of the equilibrated matrix (for the stopping rule)
+    const double anorm = ce_block_max(s, [&] {
+        double a = 0;
+        if (tid < CE_N)
+            for (int c = 0; c < CE_N; ++c) a += fabs(double(s.B[c * CE_LD + tid]));
+        return a;
+    }());
+    refined = ce_lu<float>(s, s.B, s.uinv32);
+    if (refined) {
+        // iterative refinement (as LAPACK's dsgesv): stop when the equilibrated residual is at
+        // the level of an FP64 backward-stable solve, |R r| <= |C^-1 s| |J^| eps sqrt(n)
+        const double cte = anorm * 0x1p-53 * sqrt(double(CE_N));
+        double prev = INFINITY;
+        bool conv = false;
+        for (int it = 0; it < CE_REFINE_MAX; ++it) {
+            // right-hand side: row-scaled residual, normalised by a power of two
+            long long m = 0;
+            if (tid < CE_N) {
+                const long long a = ce::abits(s.res[tid]);
+                if (a) m = a - ((long long)s.rexp[tid] << 52);
+            }
+            m = ce::warp_max_ll(m);
+            if (lane == 0) s.redl[0][warp] = m;
+            __syncthreads();
+            long long g = s.redl[0][0];
+            for (int w = 1; w < CE_WARPS; ++w) g = max(g, s.redl[0][w]);
+            if (g <= 0) {  // zero residual: the step is exact
+                conv = true;
+                break;
+            }
+            const int G = int(g >> 52) - 1023;
+            if (tid < CE_N) s.vec32[tid] = ce::scaled_to_float(s.res[tid], s.rexp[tid] + G);
+            __syncthreads();
+            ce_trisolve<float>(s, s.B, s.uinv32, s.vec32, s.vec32);
+            __syncthreads();
+            bool fin = true;
+            long long dl = 0;
+            if (tid < CE_N) {
+                const double d = ldexp(double(s.vec32[tid]), G - s.cexp[tid]);
+                fin = isfinite(d);
+                s.sol[tid] += d;
+                if (d != 0) dl = ce::abits(d) + ((long long)s.cexp[tid] << 52);
+            }
+            if (__syncthreads_or(!fin)) {
+                refined = false;
+                break;
+            }
+            // residual F - J s in FP64, its equilibrated norm and that of the step
+            long long rl = 0, xl = 0;
+            if (tid < CE_N) {
+                double r = s.A[CE_N * CE_LD + tid];
+                for (int c = 0; c < CE_N; ++c) r = fma(-s.A[c * CE_LD + tid], s.sol[c], r);
+                s.res[tid] = r;
+                const long long a = ce::abits(r);
+                if (a) rl = max(0LL, a - ((long long)s.rexp[tid] << 52));
+                if (s.sol[tid] != 0) xl = ce::abits(s.sol[tid]) + ((long long)s.cexp[tid] << 52);
+            }
+            dl = ce::warp_max_ll(dl);
+            rl = ce::warp_max_ll(rl);
+            xl = ce::warp_max_ll(xl);
+            if (lane == 0) {
+                s.redl[1][warp] = dl;
+                s.redl[2][warp] = rl;
+                s.redl[3][warp] = xl;
+            }
+            __syncthreads();
+            long long D = 0, R = 0, X = 0;
+            for (int w = 0; w < CE_WARPS; ++w) {
+                D = max(D, s.redl[1][w]);
+                R = max(R, s.redl[2][w]);
+                X = max(X, s.redl[3][w]);
+            }
+            const double dmax = __longlong_as_double(D), rn = __longlong_as_double(R), xn = __longlong_as_double(X);
+            if (rn <= xn * cte) {
+                conv = true;
+                break;
+            }
+            if (it > 0 && !(dmax <= 0.5 * prev)) break;  // not contracting: FP64 elimination
+            prev = dmax;
+        }
+        __syncthreads();
+        refined = refined && conv;
+    }
+    if (!refined) {
+        // FP64 elimination in place (J is rebuilt by the next iteration); F from column CE_N
+        if (tid < CE_N) s.res[tid] = s.A[CE_N * CE_LD + tid];
+        __syncthreads();
+        if (!ce_lu<double>(s, s.A, s.uinv64)) return false;
+        ce_trisolve<double>(s, s.A, s.uinv64, s.res, s.sol);
+        __syncthreads();
+    }
+    bool badS = false;
+    if (tid < CE_N) badS = !isfinite(s.sol[tid]);
+    return !__syncthreads_or(badS);
+}
 
 // One Newton solve at log xi from s.x (clipped_newton, src/newton.jl:2-35).  Every thread calls
 // it; control flow is uniform.  Returns whether |F|_inf < tol was reached; budget counts the
-// iterations left for the layer (exhausted: *out_of_budget is set).
+// iterations left for the layer (exhausted: out_of_budget is set); fallbacks counts the steps
+// that needed the FP64 elimination.
 __device__ bool ce_newton(const ChemTables& tb, CeShared& s, double nt, double logxi, int max_iter, int& budget,
-                          bool& out_of_budget, double& last_inf) {
+                          bool& out_of_budget, double& last_inf, int& fallbacks) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int M = tb.n_mol;
+    const double ln10 = ce::LN10;
+    const double inv_nt = 1.0 / nt;
     last_inf = INFINITY;
     for (int it = 0; it < max_iter; ++it) {
         if (budget <= 0) {
@@ -145,9 +513,9 @@ __device__ bool ce_newton(const ChemTables& tb, CeShared& s, double nt, double l
         // densities of every species at x (src/statmech.jl:385-430)
         const double xe = s.x[CE_NZ];
         for (int m = tid; m < M; m += CE_THREADS) {
-            const int* at = tb.atoms + m * CE_MAXATOMS;
+            const unsigned char* at = s.m_atoms + m * CE_MAXATOMS;
             double lg = -s.lognK[m] + logxi;
-            if (tb.charge[m] == 0) {
+            if (s.m_charge[m] == 0) {
                 for (int j = 0; j < CE_MAXATOMS && at[j]; ++j) lg += s.x[at[j] - 1];
             } else {
                 const int Z1 = at[0] - 1, Z2 = at[1] - 1;
@@ -169,24 +537,24 @@ __device__ bool ce_newton(const ChemTables& tb, CeShared& s, double nt, double l
         // per-element molecule sums (fixed order) and the block-wide sums (warp 3)
         if (tid < CE_NZ) {
             double fm = 0, dn = 0, sq = 0;
-            for (int k = tb.inc_ptr[tid]; k < tb.inc_ptr[tid + 1]; ++k) {
-                const int m = tb.inc_mol[k];
-                const double cn = double(tb.inc_cnt[k]) * s.nmol[m];
+            for (int k = s.inc_ptr[tid]; k < s.inc_ptr[tid + 1]; ++k) {
+                const int m = s.inc_mol[k];
+                const double cn = double(s.inc_cnt[k]) * s.nmol[m];
                 fm += cn;
-                dn += double(tb.nat[m] - 1) * cn;
-                if (tb.charge[m]) sq += cn;
+                dn += double(s.m_nat[m] - 1) * cn;
+                if (s.m_charge[m]) sq += cn;
             }
             s.fm[tid] = fm;
-            s.dN[tid] = ce::LN10 * dn;
+            s.dNn[tid] = -(ln10 * dn) * inv_nt;
             s.Sq[tid] = sq;
         } else if (warp == 3) {
             double nn = 0, qn = 0, dq = 0, i1 = 0, i2 = 0;
             for (int m = lane; m < M; m += 32) {
                 const double n = s.nmol[m];
-                nn += double(tb.nat[m] - 1) * n;
-                if (tb.charge[m]) {
+                nn += double(s.m_nat[m] - 1) * n;
+                if (s.m_charge[m]) {
                     qn += n;
-                    dq += double(tb.nat[m] - 1) * n;
+                    dq += double(s.m_nat[m] - 1) * n;
                 }
             }
             for (int Z = lane; Z < CE_NZ; Z += 32) {
@@ -204,11 +572,12 @@ __device__ bool ce_newton(const ChemTables& tb, CeShared& s, double nt, double l
                 s.dNe_mol = dq;
                 s.ion1 = i1;
                 s.ion2 = i2;
+                s.dNn[CE_NZ] = -(-ln10 * s.ne - ln10 * dq) * inv_nt;
             }
         }
         __syncthreads();
-        // scaled residuals and their inf-norm (src/statmech.jl:418-438, newton.jl:8-14)
-        double fabs_max = 0;
+        // scaled residuals (src/statmech.jl:418-438) into column CE_N; inf-norm (newton.jl:8-14)
+        double fa = 0;
         bool bad = false;
         if (tid < CE_N) {
             double F;
@@ -221,33 +590,30 @@ __device__ bool ce_newton(const ChemTables& tb, CeShared& s, double nt, double l
             } else {
                 F = (((s.qn - s.nHm) + s.ion1) - s.ne) / nt;
             }
-            s.F[tid] = F;
+            s.A[CE_N * CE_LD + tid] = F;
             bad = !isfinite(F);
-            fabs_max = fabs(F);
+            fa = fabs(F);
         }
-        for (int o = 16; o; o >>= 1) fabs_max = fmax(fabs_max, __shfl_xor_sync(0xffffffffu, fabs_max, o));
-        if (lane == 0) s.red[warp] = fabs_max;
         if (__syncthreads_or(bad)) return false;
-        const double inf = fmax(fmax(s.red[0], s.red[1]), fmax(s.red[2], s.red[3]));
+        const double inf = ce_block_max(s, fa);
         last_inf = inf;
         if (inf < 1e-8) return true;
-        // Jacobian, dense part: n_nuclei coupling, the atoms' own densities, the n_e column, the
-        // charge row; residuals in column CE_N
-        const double ln10 = ce::LN10;
-        const double dNe = -ln10 * s.ne - ln10 * s.dNe_mol;
-        const double inv_nt = 1.0 / nt;
-        bool badJ = false;
-        for (int idx = tid; idx < CE_N * CE_NCOL; idx += CE_THREADS) {
-            const int r = idx % CE_N, c = idx / CE_N;
+        // Jacobian, dense part: the n_nuclei coupling (-d n_nuclei/dx_c / n_tot in every atom
+        // row), the atoms' own densities, the n_e column, the charge row
+        for (int idx = tid; idx < CE_N * CE_N; idx += CE_THREADS) {
+            const int c = idx / CE_N, r = idx - c * CE_N;
             double v;
-            if (c == CE_N) {
-                v = s.F[r];
-            } else if (r < CE_NZ) {
-                v = -s.ab[r] * (c < CE_NZ ? s.dN[c] : dNe);
-                if (c == r) v += ln10 * ((s.nI[r] + s.nII[r]) + s.nIII[r]);
-                if (c == CE_NZ) v += -ln10 * s.Sq[r] - ln10 * (s.nII[r] + 2 * s.nIII[r]);
-                if (r == 0 && (c == 0 || c == CE_NZ)) v += ln10 * s.nHm;
-                v *= s.inv_scale[r];
+            if (r < CE_NZ) {
+                v = s.dNn[c];
+                if (c == r) {
+                    double w = ln10 * ((s.nI[r] + s.nII[r]) + s.nIII[r]);
+                    if (r == 0) w += ln10 * s.nHm;
+                    v += w * s.inv_scale[r];
+                } else if (c == CE_NZ) {
+                    double w = -ln10 * s.Sq[r] - ln10 * (s.nII[r] + 2 * s.nIII[r]);
+                    if (r == 0) w += ln10 * s.nHm;
+                    v += w * s.inv_scale[r];
+                }
             } else if (c < CE_NZ) {
                 v = ln10 * s.Sq[c] + ln10 * (s.nII[c] + 2 * s.nIII[c]);
                 if (c == 0) v -= ln10 * s.nHm;
@@ -258,123 +624,19 @@ __device__ bool ce_newton(const ChemTables& tb, CeShared& s, double nt, double l
             s.A[c * CE_LD + r] = v;
         }
         __syncthreads();
-        // Jacobian, molecule coupling: row Z gains ln10 cnt_Z cnt_W n_mol / (ab_Z n_tot) at W
-        if (tid < CE_NZ) {
-            const double sc = ln10 * s.inv_scale[tid];
-            for (int k = tb.inc_ptr[tid]; k < tb.inc_ptr[tid + 1]; ++k) {
-                const int m = tb.inc_mol[k];
-                const double w = sc * double(tb.inc_cnt[k]) * s.nmol[m];
-                for (int d = 0; d < tb.ndist[m]; ++d) {
-                    const int W = tb.dist_Z[m * CE_MAXATOMS + d] - 1;
-                    s.A[W * CE_LD + tid] += w * double(tb.dist_cnt[m * CE_MAXATOMS + d]);
-                }
-            }
-            for (int c = 0; c < CE_N; ++c) badJ |= !isfinite(s.A[c * CE_LD + tid]);
-        } else if (tid == CE_NZ) {
-            for (int c = 0; c < CE_N; ++c) badJ |= !isfinite(s.A[c * CE_LD + tid]);
-        }
-        if (tid < CE_N) s.perm[tid] = tid;
-        if (__syncthreads_or(badJ)) return false;
-        // LU with partial pivoting of the augmented system (J \ F, as LAPACK getrf + getrs)
-        {
-            double v = -1;
-            int i = -1;
-            if (tid < CE_N) {
-                v = fabs(s.A[tid]);
-                i = tid;
-            }
-            ce::warp_argmax(v, i);
-            if (lane == 0) {
-                s.candv[warp] = v;
-                s.candi[warp] = i;
-            }
+        // Jacobian, molecule coupling: entry (Z, W) gains ln10 sum cnt_Z cnt_W n_mol / (ab_Z n_tot)
+        for (int p = tid; p < tb.n_pairs; p += CE_THREADS) {
+            const int Z = s.pair_row[p], W = s.pair_col[p];
+            double sum = 0;
+            for (int k = s.pair_ptr[p]; k < s.pair_ptr[p + 1]; ++k) sum += double(s.pair_coef[k]) * s.nmol[s.pair_mol[k]];
+            s.A[W * CE_LD + Z] += ln10 * sum * s.inv_scale[Z];
         }
         __syncthreads();
-        bool singular = false;
-        for (int k = 0; k < CE_N; ++k) {
-            if (tid == 0) {
-                double bv = -1;
-                int bi = -1;
-                for (int w = 0; w < 4; ++w) {
-                    const int i2 = s.candi[w];
-                    const double v2 = s.candv[w];
-                    if (i2 >= 0 && (bi < 0 || v2 > bv || (v2 == bv && i2 < bi))) {
-                        bv = v2;
-                        bi = i2;
-                    }
-                }
-                int fl = 0;
-                if (bi < 0 || !(bv > 0)) {
-                    fl = 1;
-                } else {
-                    const int pr = s.perm[bi];
-                    s.perm[bi] = s.perm[k];
-                    s.perm[k] = pr;
-                    s.prow = pr;
-                    s.pinv = 1.0 / s.A[k * CE_LD + pr];
-                }
-                s.flag = fl;
-            }
-            __syncthreads();
-            if (s.flag) {
-                singular = true;
-                break;
-            }
-            if (k == CE_N - 1) break;
-            const int prow = s.prow;
-            const double pinv = s.pinv;
-            for (int i = k + 1 + tid; i < CE_N; i += CE_THREADS) s.A[k * CE_LD + s.perm[i]] *= pinv;
-            __syncthreads();
-            const int nrow = CE_N - 1 - k, ncol = CE_NCOL - 1 - k;
-            double cv = -1;
-            int ci = -1;
-            for (int idx = tid; idx < nrow * ncol; idx += CE_THREADS) {
-                const int ii = idx % nrow, cc = idx / nrow;
-                const int i = k + 1 + ii, c = k + 1 + cc;
-                const int r = s.perm[i];
-                const double v = fma(-s.A[k * CE_LD + r], s.A[c * CE_LD + prow], s.A[c * CE_LD + r]);
-                s.A[c * CE_LD + r] = v;
-                if (cc == 0) {
-                    cv = fabs(v);
-                    ci = i;
-                }
-            }
-            ce::warp_argmax(cv, ci);
-            if (lane == 0) {
-                s.candv[warp] = cv;
-                s.candi[warp] = ci;
-            }
-            __syncthreads();
-        }
-        if (singular) return false;
-        // back substitution in one warp: x_j = y_j / U_jj, y_i -= U_ij x_j
-        if (warp == 0) {
-            for (int i = lane; i < CE_N; i += 32) {
-                const int r = s.perm[i];
-                s.y[i] = s.A[CE_N * CE_LD + r];
-                s.rinv[i] = 1.0 / s.A[i * CE_LD + r];
-            }
-            __syncwarp();
-            for (int j = CE_N - 1; j >= 0; --j) {
-                const double xj = s.y[j] * s.rinv[j];
-                if (lane == 0) s.sol[j] = xj;
-                for (int i = lane; i < j; i += 32) s.y[i] = fma(-s.A[j * CE_LD + s.perm[i]], xj, s.y[i]);
-                __syncwarp();
-            }
-        }
-        __syncthreads();
+        bool refined = false;
+        if (!ce_solve(s, refined)) return false;
+        if (!refined) ++fallbacks;
         // step = -(J \ F), clipped so that no unknown moves more than 1 dex
-        double smax = 0;
-        bool badS = false;
-        if (tid < CE_N) {
-            const double st = -s.sol[tid];
-            badS = !isfinite(st);
-            smax = fabs(st);
-        }
-        for (int o = 16; o; o >>= 1) smax = fmax(smax, __shfl_xor_sync(0xffffffffu, smax, o));
-        if (lane == 0) s.red[warp] = smax;
-        if (__syncthreads_or(badS)) return false;
-        const double sm = fmax(fmax(s.red[0], s.red[1]), fmax(s.red[2], s.red[3]));
+        const double sm = ce_block_max(s, tid < CE_N ? fabs(s.sol[tid]) : 0.0);
         const double alpha = sm > 1.0 ? 1.0 / sm : 1.0;
         if (tid < CE_N) s.x[tid] = s.x[tid] + alpha * (-s.sol[tid]);
         __syncthreads();
@@ -395,6 +657,27 @@ __global__ void __launch_bounds__(CE_THREADS) chem_eq_kernel(ChemTables tb, Chem
     const int a = ly.atm ? ly.atm[l] : 0;
     const double lnT = log(T);
     const double transU = ce::translational_U(ce::ME_CGS, T);
+    for (int i = tid; i < M * CE_MAXATOMS; i += CE_THREADS) s.m_atoms[i] = (unsigned char)tb.atoms[i];
+    for (int m = tid; m < M; m += CE_THREADS) {
+        s.m_charge[m] = (unsigned char)tb.charge[m];
+        s.m_nat[m] = (unsigned char)tb.nat[m];
+    }
+    for (int i = tid; i <= CE_NZ; i += CE_THREADS) s.inc_ptr[i] = (short)tb.inc_ptr[i];
+    for (int i = tid; i < tb.inc_ptr[CE_NZ]; i += CE_THREADS) {
+        s.inc_mol[i] = (short)tb.inc_mol[i];
+        s.inc_cnt[i] = (unsigned char)tb.inc_cnt[i];
+    }
+    for (int p = tid; p <= tb.n_pairs; p += CE_THREADS) {
+        s.pair_ptr[p] = (short)tb.pair_ptr[p];
+        if (p < tb.n_pairs) {
+            s.pair_row[p] = (unsigned char)tb.pair_row[p];
+            s.pair_col[p] = (unsigned char)tb.pair_col[p];
+        }
+    }
+    for (int k = tid; k < tb.pair_ptr[tb.n_pairs]; k += CE_THREADS) {
+        s.pair_mol[k] = (short)tb.pair_mol[k];
+        s.pair_coef[k] = (unsigned char)tb.pair_coef[k];
+    }
     // per-layer constants: Saha factors (saha_ion_weights with n_e = 1, src/statmech.jl:19-35,
     // 362-372), the starting guess (atoms only, n_e from the model atmosphere, :151-155, 235-237),
     // molecular log nK (get_log_nK, :60-62; polyatomics read_statmech_quantities.jl:66-89)
@@ -459,12 +742,12 @@ __global__ void __launch_bounds__(CE_THREADS) chem_eq_kernel(ChemTables tb, Chem
     int budget = CE_MAX_ITER;
     bool oob = false;
     double last_inf = INFINITY;
-    int solves = 0, st = KORG_CHEM_OK;
+    int solves = 0, st = KORG_CHEM_OK, fallbacks = 0;
     double logxi = 0.0;
     if (tid < CE_N) s.x[tid] = s.x0[tid];
     __syncthreads();
     ++solves;
-    bool conv = ce_newton(tb, s, nt, 0.0, 50, budget, oob, last_inf);
+    bool conv = ce_newton(tb, s, nt, 0.0, 50, budget, oob, last_inf, fallbacks);
     if (!conv && !oob) {
         const double anchors[3] = {-5.0, -20.0, -50.0};
         bool anchored = false;
@@ -472,7 +755,7 @@ __global__ void __launch_bounds__(CE_THREADS) chem_eq_kernel(ChemTables tb, Chem
             if (tid < CE_N) s.x[tid] = s.x0[tid];
             __syncthreads();
             ++solves;
-            anchored = ce_newton(tb, s, nt, anchors[q], 100, budget, oob, last_inf);
+            anchored = ce_newton(tb, s, nt, anchors[q], 100, budget, oob, last_inf, fallbacks);
             if (anchored) logxi = anchors[q];
         }
         if (!anchored) {
@@ -487,14 +770,14 @@ __global__ void __launch_bounds__(CE_THREADS) chem_eq_kernel(ChemTables tb, Chem
                 if (tid < CE_N) s.x[tid] = s.xs[tid];
                 __syncthreads();
                 ++solves;
-                bool c2 = ce_newton(tb, s, nt, logxi + step, 100, budget, oob, last_inf);
+                bool c2 = ce_newton(tb, s, nt, logxi + step, 100, budget, oob, last_inf, fallbacks);
                 if (!c2) {
                     step /= 2;
                     while (!c2 && step >= 0.0625 && !oob) {
                         if (tid < CE_N) s.x[tid] = s.xs[tid];
                         __syncthreads();
                         ++solves;
-                        c2 = ce_newton(tb, s, nt, logxi + step, 100, budget, oob, last_inf);
+                        c2 = ce_newton(tb, s, nt, logxi + step, 100, budget, oob, last_inf, fallbacks);
                         if (!c2) step /= 2;
                     }
                     if (!c2) {
@@ -555,6 +838,7 @@ __global__ void __launch_bounds__(CE_THREADS) chem_eq_kernel(ChemTables tb, Chem
             info[CE_NINFO * l + 1] = double(solves);
             info[CE_NINFO * l + 2] = logxi;
             info[CE_NINFO * l + 3] = last_inf;
+            info[CE_NINFO * l + 4] = double(fallbacks);
         }
     }
 }

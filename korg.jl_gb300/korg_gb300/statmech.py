@@ -156,7 +156,8 @@ def solve_layers(T, n_tot, ne_model, abundances, atm=None, tables=None, ctx=None
 
     ``abundances`` is [n_atm, 92] (N_X / N_total, normalised) or [92]; ``atm`` maps each layer to
     its atmosphere.  Returns (densities [L, 278 + n_mol] in the order of ``tables.species`` -- n_e
-    first --, status [L], info [L, 4]: Newton iterations, solves, log xi reached, last inf-norm)."""
+    first --, status [L], info [L, 5]: Newton iterations, solves, log xi reached, last inf-norm,
+    steps solved by the FP64 fallback)."""
     ctx = ctx or _lib.default_context()
     t = ctx.ensure_equilibrium(tables)
     keep = _lib.Keep()
@@ -172,7 +173,7 @@ def solve_layers(T, n_tot, ne_model, abundances, atm=None, tables=None, ctx=None
         raise ValueError("atm must have one entry per layer")
     dens = np.empty((L, _lib.KORG_CHEM_MOL0 + len(t.molecules)))
     status = np.empty(L, np.int32)
-    info = np.empty((L, 4))
+    info = np.empty((L, 5))
     y = _lib.ChemLayers(L, _lib._p(T), _lib._p(nt), _lib._p(ne), _lib._p(ab), _lib._p(at, _lib._ip))
     rc = ctx.lib.korg_chemical_equilibrium(ctx.h, C.byref(y), ab.shape[0], _lib._p(dens),
                                            _lib._p(status, _lib._ip), _lib._p(info))
