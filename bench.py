@@ -42,6 +42,7 @@ import subprocess
 import sys
 import tempfile
 import time
+import warnings
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "korg.jl_gb300"))
@@ -67,6 +68,7 @@ def parse():
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the oracle comparison of the adjoint, batch and cool-star configurations")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the reverse-mode measurement")
+    ap.add_argument("--no-chemistry", action="store_true", help="skip the chemical-equilibrium measurement")
     ap.add_argument("--workload", default="synth", choices=["synth", "batch", "adjoint", "variants", "postprocess"])
     ap.add_argument("--tile", default=None, help="force the line tile shape: tw,stage,split (e.g. 64,32,1)")
     ap.add_argument("--spectra", type=int, default=256, help="batch workload: number of spectra")
@@ -123,6 +125,128 @@ def cpu_continuum(inp):
     return inp
 
 
+def _oracle_chem_layer(a):
+    """One layer of the FP64 chemical-equilibrium restatement (spawn-pool worker)."""
+    T, nt, ne, ab = a
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "korg.jl_gb300"))
+    import numpy as np
+    import statmech_oracle
+    from korg_gb300 import data
+    from korg_gb300.statmech import default_equilibrium_tables
+    out_ne, nd = statmech_oracle.chemical_equilibrium(T, nt, ne, ab, data.ionization_energies(),
+                                                      data.default_partition_funcs(),
+                                                      data.default_log_equilibrium_constants(),
+                                                      electron_number_density_warn_threshold=np.inf)
+    return out_ne, np.array([out_ne] + [nd[s] for s in default_equilibrium_tables().species[1:]])
+
+
+def oracle_chemistry(T, n_tot, ne_model, ab, threads=None):
+    """Chemical equilibrium of every layer with the FP64 CPU restatement, in a spawn pool: the
+    same (T, n_tot, ne, abundances) -> (ne, {Species: n}) interface as the device solve."""
+    import multiprocessing as mp
+    import numpy as np
+    from korg_gb300.statmech import default_equilibrium_tables
+    T = np.atleast_1d(T)
+    args = [(float(T[l]), float(np.broadcast_to(n_tot, T.shape)[l]), float(np.broadcast_to(ne_model, T.shape)[l]),
+             np.asarray(ab)) for l in range(len(T))]
+    with mp.get_context("spawn").Pool(min(len(args), threads or os.cpu_count() or 1)) as pool:
+        res = pool.map(_oracle_chem_layer, args, chunksize=1)
+    dens = np.stack([r[1] for r in res])
+    species = default_equilibrium_tables().species
+    return dens[:, 0].copy(), {sp: dens[:, k].copy() for k, sp in enumerate(species) if sp is not None}
+
+
+CHEM_STARS = [(3500.0, 1.0, -2.5), (3500.0, 4.5, 0.0), (3800.0, 2.0, -1.0), (4000.0, 4.8, 0.5),
+              (4200.0, 1.5, 0.0), (4500.0, 2.5, -0.5), (4800.0, 4.5, -2.0), (5000.0, 3.0, 0.3),
+              (5300.0, 4.0, -1.5), (5600.0, 4.4, 0.0), (5777.0, 4.44, 0.0), (6000.0, 4.2, -0.7),
+              (6300.0, 3.5, 0.2), (6600.0, 4.0, -2.5), (6800.0, 2.5, 0.0), (7000.0, 4.3, 0.5)]
+
+
+def chemistry_measure(ctx, torch, dev, threads):
+    """Chemical equilibrium (korg_chemical_equilibrium_dev) of every layer of 16 56-layer stars in
+    one batched call, device-timed, against the FP64 CPU restatement on every 8th layer."""
+    import warnings
+    import numpy as np
+    from korg_gb300 import _lib, standin
+    from korg_gb300.statmech import solve_layers
+    atms = []
+    for Teff, logg, m_H in CHEM_STARS:
+        atm, A_X = standin.synthetic_atmosphere(Teff, logg, m_H)
+        ab = 10.0 ** (A_X - 12)
+        atms.append((atm, ab / ab.sum()))
+    T = np.concatenate([a.T for a, _ in atms])
+    nt = np.concatenate([a.n_tot for a, _ in atms])
+    ne = np.concatenate([a.ne for a, _ in atms])
+    abund = np.stack([ab for _, ab in atms])
+    atm_idx = np.concatenate([np.full(len(a.T), k, np.int32) for k, (a, _) in enumerate(atms)])
+    L = len(T)
+    tab = ctx.ensure_equilibrium()
+    nspec = _lib.KORG_CHEM_MOL0 + len(tab.molecules)
+    d = lambda a, dt=torch.float64: torch.as_tensor(np.ascontiguousarray(a)).to(dt).to(dev)
+    tT, tnt, tne, tab_, tatm = d(T), d(nt), d(ne), d(abund), d(atm_idx, torch.int32)
+    dens = torch.empty((L, nspec), dtype=torch.float64, device=dev)
+    status = torch.empty(L, dtype=torch.int32, device=dev)
+    info = torch.empty((L, 5), dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    dp = lambda t: C.cast(t.data_ptr(), _lib._dp)
+
+    def run(lo, hi, atm_ptr):
+        y = _lib.ChemLayers(hi - lo, dp(tT[lo:hi]), dp(tnt[lo:hi]), dp(tne[lo:hi]), dp(tab_),
+                            C.cast(atm_ptr, _lib._ip) if atm_ptr else None)
+        ctx.check(ctx.lib.korg_chemical_equilibrium_dev(ctx.h, C.byref(y), len(atms), dens[lo:hi].data_ptr(),
+                                                        status[lo:hi].data_ptr(), info[lo:hi].data_ptr(),
+                                                        stream.cuda_stream))
+
+    def timed(fn, reps=3):
+        fn()
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return statistics.mean(ts)
+
+    ms_all = timed(lambda: run(0, L, tatm.data_ptr()))
+    st, inf, got = status.cpu().numpy(), info.cpu().numpy(), dens.cpu().numpy()
+    k10 = 10 * 56  # the 5777 K star, the headline's atmosphere: what one synthesize pays
+    ms_one = timed(lambda: run(k10, k10 + 56, 0), reps=5)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        t1 = time.perf_counter()
+        solve_layers(T, nt, ne, abund, atm=atm_idx, ctx=ctx)
+        e2e_s = time.perf_counter() - t1
+    # FP64 CPU restatement on every 8th layer (spawn pool, all host cores)
+    sample = np.arange(0, L, 8)
+    t1 = time.perf_counter()
+    import multiprocessing as mp
+    with mp.get_context("spawn").Pool(min(len(sample), threads)) as pool:
+        res = pool.map(_oracle_chem_layer, [(float(T[l]), float(nt[l]), float(ne[l]), abund[atm_idx[l]])
+                                            for l in sample], chunksize=1)
+    cpu_s = time.perf_counter() - t1
+    worst = 0.0
+    for (o_ne, o_vec), l in zip(res, sample):
+        keep = o_vec > 1e-30 * nt[l]
+        worst = max(worst, float(np.max(np.abs(got[l][keep] / o_vec[keep] - 1))))
+    iters = float(inf[:, 0].sum())
+    return {"workload": f"{len(atms)} stars x 56 layers (Teff 3500-7000 K, logg 1-5, [M/H] -2.5..0.5; grey "
+                        f"atmospheres), {len(tab.molecules)} molecules, one batched call",
+            "layers": L, "ms": ms_all, "layers_per_s": L / (ms_all * 1e-3),
+            "one_atmosphere_ms": ms_one, "one_atmosphere": "the 5777 K, log g 4.44 star (56 layers)",
+            "e2e_layers_per_s": L / e2e_s, "e2e": "host-pointer korg_chemical_equilibrium (H2D, solve, D2H)",
+            "status_ok": int((st == 0).sum()), "newton_iterations": iters,
+            "us_per_newton_iteration_per_layer": ms_all * 1e3 / iters * min(L, 152),
+            "fp64_fallback_steps": float(inf[:, 4].sum()), "max_solves_per_layer": float(inf[:, 1].max()),
+            "max_rel_density_err_vs_oracle": worst,
+            "oracle_compare": f"every 8th layer ({len(sample)}), species above 1e-30 n_tot",
+            "cpu_baseline": {"value": len(sample) / cpu_s, "unit": "layers/s", "cores": threads, "kind": "port",
+                             "sample": f"{len(sample)} layers (every 8th) with the FP64 numpy restatement of "
+                                       "statmech.jl, one layer per process"}}
+
+
 def cpu_sample(inp_or_lines, threads, _cache={}):
     """Time the oracle on the CPU sample; returns (spectra/s, seconds, evals, info, flux, cntm).
 
@@ -132,7 +256,8 @@ def cpu_sample(inp_or_lines, threads, _cache={}):
     from korg_gb300 import synthetic
     key = inp_or_lines if isinstance(inp_or_lines, int) else id(inp_or_lines)
     if key not in _cache:
-        inp = cpu_continuum(synthetic.prepare(workload(inp_or_lines))) if isinstance(inp_or_lines, int) else inp_or_lines
+        inp = (cpu_continuum(synthetic.prepare(workload(inp_or_lines), chemistry=oracle_chemistry))
+               if isinstance(inp_or_lines, int) else inp_or_lines)
         _cache[key] = (strided(inp, CPU_SAMPLE_STEP)[0], len(inp.wls))
     inp, full_points = _cache[key]
     frac = len(inp.wls) / full_points
@@ -297,7 +422,9 @@ def run_korg(args):
     ctx = _lib.Context(local)
     t0 = time.perf_counter()
     work = workload(args.lines, args.wl)
-    inp = synthetic.prepare(work, continuum="gpu", ctx=ctx)
+    with warnings.catch_warnings():  # the grey atmosphere's n_e is not Korg's: the n_e warning is expected
+        warnings.simplefilter("ignore")
+        inp = synthetic.prepare(work, continuum="gpu", chemistry="gpu", ctx=ctx)
     host_prep_s = time.perf_counter() - t0
     ctx.ensure_stark()
     ctx.check(ctx.lib.korg_set_timing(ctx.h, 1))
@@ -413,6 +540,8 @@ def run_korg(args):
         if not args.no_configs:
             parity.update(configs_vs_oracle(ctx, threads))
     adj = adjoint_measure(ctx, torch, dev, steps=5) if rank == 0 and not args.no_adjoint else None
+    chem = (chemistry_measure(ctx, torch, dev, os.cpu_count() or 1)
+            if rank == 0 and not args.no_chemistry else None)
 
     # alpha init, reference-wavelength lines (5), hydrogen (3), metal lines (5), transfer
     launches_per_step = 1 + 5 + (3 if inp.hydrogen_lines else 0) + 5 + 1
@@ -433,8 +562,8 @@ def run_korg(args):
                                f"{args.lines} atomic lines + hydrogen lines, {args.wl[0]:.0f}-{args.wl[1]:.0f} A "
                                f"@ 0.01 A ({nwl} points)",
                    "precision": "mixed",
-                   "continuum": "device (korg_continuum_absorption: Korg's continuum terms except metal bound-free) "
-                                "from the stand-in chemical equilibrium",
+                   "chemistry": "device (korg_chemical_equilibrium: Korg's chemical equilibrium, 306 molecules)",
+                   "continuum": "device (korg_continuum_absorption: Korg's continuum terms except metal bound-free)",
                    "l2": f"flushed (256 MiB write) between steps; alpha {8 * L * nwl / 1e6:.0f} MB",
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU", "tile": args.tile or "default",
                    "host_prep_s": host_prep_s},
@@ -455,6 +584,7 @@ def run_korg(args):
         "cpu_baseline": cpu,
         "parity_vs_oracle": parity,
         "adjoint": adj,
+        "chemical_equilibrium": chem,
         "e2e": {"value": world / e2e_s, "unit": "spectra/s", "h2d_bytes_per_step": host_bytes(inp),
                 "d2h_bytes_per_step": 16 * nwl},
         "gpu_launches": launches_per_step * args.steps,
@@ -467,19 +597,58 @@ def run_korg(args):
         tdist.destroy_process_group()
 
 
-def _prep_batch_one(w):
+def _batch_atmosphere(w):
     sys.path.insert(0, os.path.join(ROOT, "korg.jl_gb300"))
-    from korg_gb300 import synthetic
-    return synthetic.prepare(w)
+    from korg_gb300 import standin
+    return standin.synthetic_atmosphere(w.Teff, w.logg, w.m_H, w.L)
+
+
+def _fixed_chemistry(ne, nd, T, n_tot, A_X):
+    return ne, nd
+
+
+def _prep_batch_one(a):
+    sys.path.insert(0, os.path.join(ROOT, "korg.jl_gb300"))
+    import functools
+    from korg_gb300.api import prepare_synthesis
+    w, (atm, A_X), ne, nd = a
+    return prepare_synthesis(atm, w.linelist, A_X, w.wavelengths, vmic=w.vmic, hydrogen_lines=w.hydrogen_lines,
+                             chemical_equilibrium=functools.partial(_fixed_chemistry, ne, nd))
 
 
 def batch_inputs(n_spectra):
-    """Host precompute of the batch workload in a spawn pool (before any CUDA call)."""
+    """Host precompute of the batch workload: the atmospheres in a spawn pool, the chemical
+    equilibrium of every layer of every atmosphere in one batched device call
+    (korg_chemical_equilibrium), then the rest of each spectrum's precompute in the pool."""
     import multiprocessing as mp
-    from korg_gb300 import synthetic
+    import numpy as np
+    from korg_gb300 import _lib, synthetic
+    from korg_gb300.statmech import default_equilibrium_tables, solve_layers
     works = synthetic.config3(n_spectra=n_spectra)
+    t0 = time.perf_counter()
     with mp.get_context("spawn").Pool(min(len(works), os.cpu_count() or 1)) as pool:
-        return pool.map(_prep_batch_one, works, chunksize=1)
+        atms = pool.map(_batch_atmosphere, works, chunksize=1)
+    t1 = time.perf_counter()
+    ctx = _lib.Context(0)
+    abund = np.stack([10.0 ** (A_X - 12) / np.sum(10.0 ** (A_X - 12)) for _, A_X in atms])
+    idx = np.concatenate([np.full(len(a.T), k, np.int32) for k, (a, _) in enumerate(atms)])
+    ctx.ensure_equilibrium()
+    t2 = time.perf_counter()
+    dens, status, info = solve_layers(np.concatenate([a.T for a, _ in atms]), np.concatenate([a.n_tot for a, _ in atms]),
+                                      np.concatenate([a.ne for a, _ in atms]), abund, atm=idx, ctx=ctx)
+    t3 = time.perf_counter()
+    ctx.close()
+    species = default_equilibrium_tables().species
+    chem = []
+    for k in range(len(atms)):
+        rows = dens[idx == k]
+        chem.append((rows[:, 0].copy(), {sp: rows[:, j].copy() for j, sp in enumerate(species) if sp is not None}))
+    with mp.get_context("spawn").Pool(min(len(works), os.cpu_count() or 1)) as pool:
+        inps = pool.map(_prep_batch_one, [(w, a, c[0], c[1]) for w, a, c in zip(works, atms, chem)], chunksize=1)
+    t4 = time.perf_counter()
+    return inps, {"atmospheres_s": t1 - t0, "chemistry_s": t3 - t2, "chemistry_layers": len(idx),
+                  "chemistry_newton_iterations": float(info[:, 0].sum()), "rest_s": t4 - t3,
+                  "chemistry": "korg_chemical_equilibrium, every layer of every atmosphere in one call (host pointers)"}
 
 
 def cpu_sample_batch(inp, threads):
@@ -537,7 +706,7 @@ def run_batch(args):
     import numpy as np
     t0 = time.perf_counter()
     _progress(f"host precompute of {args.spectra} spectra")
-    inps = batch_inputs(args.spectra)
+    inps, prep_parts = batch_inputs(args.spectra)
     host_prep_s = time.perf_counter() - t0
     _progress(f"host precompute done ({host_prep_s:.1f} s, {sum(len(i.linelist) for i in inps)} lines)")
     import torch
@@ -642,7 +811,9 @@ def run_batch(args):
                                f"15000-17000 A @ 0.005 A ({nwl} points); one step = the whole batch",
                    "precision": "mixed", "lines_per_spectrum": [len(i.linelist) for i in inps][:8] + ["..."],
                    "l2": f"batch alpha {8 * L * nwl * n / 1e9:.1f} GB >> L2", "graph": True, "tile": cfg,
-                   "host_prep_s": host_prep_s},
+                   "host_prep_s": host_prep_s, "host_prep_parts": prep_parts,
+                   "chemistry": "device (korg_chemical_equilibrium, all atmospheres in one call)",
+                   "continuum": "CPU stand-in"},
         "evals_per_step": evals, "evals_per_s": evals / (ms * 1e-3),
         "stages_ms": {"total_eager": st.ms_total, "line_tile_queue": st.ms_line_tile, "rt_all": st.ms_rt},
         "fp64": fp64,
@@ -764,7 +935,9 @@ def run_variants(args):
     torch.cuda.set_device(dev)
     t0 = time.perf_counter()
     _progress("preparing the 1M-line cool giant")
-    base = synthetic.prepare(synthetic.config4(), continuum="gpu")
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        base = synthetic.prepare(synthetic.config4(), continuum="gpu", chemistry="gpu")
     inps = synthetic.abundance_variants(base, 16)
     host_prep_s = time.perf_counter() - t0
     nwl, L = len(base.wls), len(base.T)
@@ -829,8 +1002,10 @@ class AdjointCase:
         from korg_gb300 import _lib, synthetic
         from korg_gb300.api import synthesize_prepared
         self.torch, self.ctx, self.lib = torch, ctx, _lib
-        inp = synthetic.prepare(synthetic.config2(n_atomic=int(50_000 * scale), n_mol=int(20_000 * scale)),
-                                continuum="gpu", ctx=ctx)
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            inp = synthetic.prepare(synthetic.config2(n_atomic=int(50_000 * scale), n_mol=int(20_000 * scale)),
+                                    continuum="gpu", chemistry="gpu", ctx=ctx)
         self.inp = inp
         self.nwl, L = len(inp.wls), len(inp.T)
         ctx.ensure_stark()
@@ -920,9 +1095,10 @@ def configs_vs_oracle(ctx, threads):
     0.005 A infrared grids, every 50th of the 0.01 A optical one)."""
     from korg_gb300 import synthetic
     from korg_gb300.api import synthesize_prepared
-    gpu = dict(continuum="gpu", ctx=ctx)
+    gpu = dict(continuum="gpu", chemistry="gpu", ctx=ctx)
+    warnings.simplefilter("ignore")  # the grey atmospheres' n_e differ from Korg's: expected
     cases = [("cfg2_adjoint_forward", lambda: synthetic.prepare(synthetic.config2(), **gpu), 0.1),
-             ("cfg3_batch_spectrum0", lambda: synthetic.prepare(synthetic.config3(n_spectra=1)[0]), 0.1),
+             ("cfg3_batch_spectrum0", lambda: synthetic.prepare(synthetic.config3(n_spectra=1)[0], **gpu), 0.1),
              ("cfg4_cool_star_variant0",
               lambda: synthetic.abundance_variants(synthetic.prepare(synthetic.config4(), **gpu), 1)[0], 0.5)]
     out = {}

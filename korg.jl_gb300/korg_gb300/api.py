@@ -14,6 +14,7 @@ array of shape (L, nwl) in Fortran order (equivalently (nwl, L) in C order).  ``
 from __future__ import annotations
 
 import ctypes as C
+import functools
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -278,25 +279,31 @@ def prepare_synthesis(atm, linelist: LineList, A_X, wavelengths, vmic=1.0, line_
                       ctx=None):
     """The host part of synthesize (src/synthesize.jl:159-262).  Chemical equilibrium:
     ``chemistry="gpu"`` solves Korg's chemical equilibrium for every layer on the device
-    (:mod:`korg_gb300.statmech`, src/synthesize.jl:207-219), starting from the atmosphere's n_e;
-    ``"standin"`` (the default, CPU only) uses the compact stand-in of :mod:`korg_gb300.standin`;
-    a ``chemical_equilibrium(T, n_tot, A_X) -> (ne, {Species: n})`` callable overrides both.  The
-    continuum: ``continuum="gpu"`` evaluates Korg's continuum absorption (every term but metal
-    bound-free) on the device (:mod:`korg_gb300.continuum`); ``"standin"`` (the default, CPU only)
-    the compact stand-in; a ``continuum_opacity(wls_cm, T, ne, n_HI, n_HII) -> alpha`` callable
-    overrides both."""
+    (:func:`korg_gb300.statmech.chemical_equilibrium`, src/synthesize.jl:207-219), starting from
+    the atmosphere's n_e; a callable ``chemistry(T, n_tot, ne_model, absolute_abundances) ->
+    (ne, {Species: n})`` over the layers (the reference's argument order) does the same with
+    another solver; ``"standin"`` (the default, CPU only) uses the compact stand-in of
+    :mod:`korg_gb300.standin`; a ``chemical_equilibrium(T, n_tot, A_X) -> (ne, {Species: n})``
+    callable overrides all of them.  The continuum: ``continuum="gpu"`` evaluates Korg's
+    continuum absorption (every term but metal bound-free) on the device
+    (:mod:`korg_gb300.continuum`); ``"standin"`` (the default, CPU only) the compact stand-in; a
+    ``continuum_opacity(wls_cm, T, ne, n_HI, n_HII) -> alpha`` callable overrides both."""
     from . import standin
     if chemical_equilibrium is not None:
         chem = chemical_equilibrium
-    elif chemistry == "gpu":
-        def chem(T, n_tot, A_X):
-            from .statmech import chemical_equilibrium as solve
-            ab = 10.0 ** (np.asarray(A_X, np.float64) - 12)  # :204-209
-            return solve(T, n_tot, atm.ne, ab / ab.sum(), ctx=ctx)
     elif chemistry == "standin":
         chem = standin.chemical_equilibrium
+    elif chemistry == "gpu" or callable(chemistry):
+        def chem(T, n_tot, A_X):
+            if chemistry == "gpu":
+                from .statmech import chemical_equilibrium
+                solve = functools.partial(chemical_equilibrium, ctx=ctx)
+            else:
+                solve = chemistry
+            ab = 10.0 ** (np.asarray(A_X, np.float64) - 12)  # :204-209
+            return solve(T, n_tot, np.asarray(atm.ne, np.float64), ab / ab.sum())
     else:
-        raise ValueError(f'chemistry must be "gpu" or "standin", got {chemistry!r}')
+        raise ValueError(f'chemistry must be "gpu", "standin" or a callable, got {chemistry!r}')
     cont = continuum_opacity or standin.continuum_opacity
     wls = wavelengths if isinstance(wavelengths, Wavelengths) else Wavelengths(wavelengths)
     use_MHD = (wls.all_wls[-1] < 13_000e-8) if use_MHD_for_hydrogen_lines is None else use_MHD_for_hydrogen_lines
