@@ -21,7 +21,8 @@
  * Precision: KORG_FP64 evaluates everything in FP64 (the plain form).  KORG_MIXED evaluates
  * line profiles in FP32 with Kahan-compensated accumulation, and keeps FP64 for the
  * wavelength offsets from line centres (rounded to FP32 afterwards), the per-layer line
- * strengths (Boltzmann factors, n/U), the optical-depth integration and the formal solution.
+ * strengths (Boltzmann factors, n/U), the reference-wavelength line opacity (one wavelength,
+ * which anchors the optical depths), the optical-depth integration and the formal solution.
  */
 #ifndef KORG_GB300_H
 #define KORG_GB300_H

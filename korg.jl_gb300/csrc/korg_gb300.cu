@@ -542,11 +542,13 @@ int run_synthesize(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& l
     // src/synthesize.jl:249-252 alpha from the continuum interpolants
     alpha_init_kernel<<<unsigned((nwl + 63) / 64), 256, 0, s>>>(alpha, wls, nwl, L, cn);
     KCUDA(cudaGetLastError());
-    // :265-283 reference-wavelength line opacity on a copy of the continuum alpha_ref
+    // :265-283 reference-wavelength line opacity on a copy of the continuum alpha_ref, in FP64 in
+    // both precisions (one wavelength): the anchored optical depths, and so the continuum flux,
+    // carry no FP32 rounding
     KCUDA(cudaMemcpyAsync(aref, in->alpha_ref_cntm, sizeof(double) * L, cudaMemcpyDeviceToDevice, s));
     const CntmDev cref{1, nullptr, in->alpha_ref_cntm};
     record(ctx, 1, s);
-    KCHECK(run_line_absorption(ctx, aref, ref_wl_dev, 1, ln5, lay, cref, in->cutoff_threshold, mixed, s));
+    KCHECK(run_line_absorption(ctx, aref, ref_wl_dev, 1, ln5, lay, cref, in->cutoff_threshold, false, s));
     // :293-303 hydrogen lines
     record(ctx, 3, s);
     if (in->hydrogen_lines) {
@@ -657,7 +659,7 @@ int enqueue_batch(korg_ctx* ctx, const BatchPlan& p, int nspec, const korg_batch
             KCUDA(cudaMemcpyAsync(aref, in.alpha_ref_cntm, sizeof(double) * L, cudaMemcpyDeviceToDevice, s));
             const CntmDev cref{1, nullptr, in.alpha_ref_cntm};
             KCHECK(run_line_absorption(ctx, aref, d_refwl + i, 1, lines_dev(&it[i].lines5), lay, cref,
-                                       in.cutoff_threshold, mixed, s));
+                                       in.cutoff_threshold, false, s));
             if (in.hydrogen_lines) {
                 const HLayers hl{L, lay.T, lay.ne, in.nH_I, in.nHe_I, in.UH_I, lay.xi};
                 KCHECK(run_hydrogen(ctx, alpha, wls, nwl, hl, in.hydrogen_window, in.use_MHD, mixed, s));
@@ -835,7 +837,7 @@ int run_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& ln, cons
         alpha_init_kernel<<<unsigned((nwl + 63) / 64), 256, 0, s>>>(alpha, wls, nwl, L, cn);
         KCUDA(cudaGetLastError());
         KCUDA(cudaMemcpyAsync(aref, in->alpha_ref_cntm, sizeof(double) * L, cudaMemcpyDeviceToDevice, s));
-        KCHECK(run_line_absorption(ctx, aref, ref_wl_dev, 1, ln5, lay, cref, in->cutoff_threshold, mixed, s));
+        KCHECK(run_line_absorption(ctx, aref, ref_wl_dev, 1, ln5, lay, cref, in->cutoff_threshold, false, s));
         if (in->hydrogen_lines)
             KCHECK(run_hydrogen(ctx, alpha, wls, nwl, hl, in->hydrogen_window, in->use_MHD, mixed, s));
         KCHECK(run_line_absorption(ctx, alpha, wls, nwl, ln, lay, cn, in->cutoff_threshold, mixed, s));

@@ -63,9 +63,11 @@ def _perturbed(inp, field, idx, delta):
     return c
 
 
-def _fd(inp, obs, ctx, field, idx, rel=1e-6, loss=None, noise=False):
+def _fd(inp, obs, ctx, field, idx, rel=1e-5, loss=None, noise=False):
     """Central difference; with noise=True also returns the rounding floor of the estimate
-    (a few ulps of the loss over the step)."""
+    (a few ulps of the loss over the step).  The relative step 1e-5 balances truncation (below
+    3e-5 of the derivative for T, the most curved parameter) against the loss's round-off, which
+    at a step of 1e-6 already reaches ~1e-4 of the n_e derivatives."""
     loss = loss or (lambda x: _loss(x, obs, ctx))
     v = (inp.linelist.log_gf if field == "log_gf" else getattr(inp, field))[idx]
     h = rel * max(abs(v), 1e-300) if field != "log_gf" else 1e-6

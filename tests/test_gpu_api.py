@@ -13,6 +13,8 @@ FP64 oracle (needs a GB300).
 """
 import os
 
+import warnings
+
 import numpy as np
 import pytest
 
@@ -35,7 +37,10 @@ def test_synthesize_reference_signature(ctx, oracle_lib):
     w = synthetic.config0()
     atm, A_X = standin.synthetic_atmosphere(w.Teff, w.logg, w.m_H, w.L)
     res = korg_gb300.synthesize(atm, w.linelist, A_X, (5000, 5100), precision="fp64", ctx=ctx)
-    inp = korg_gb300.prepare_synthesis(atm, w.linelist, A_X, (5000, 5100), continuum="gpu", ctx=ctx)
+    with warnings.catch_warnings():  # synthesize's default: Korg's chemical equilibrium on the device
+        warnings.simplefilter("ignore")
+        inp = korg_gb300.prepare_synthesis(atm, w.linelist, A_X, (5000, 5100), continuum="gpu", chemistry="gpu",
+                                           ctx=ctx)
     flux, cntm, _, _, ev = oracle_lib.synthesize(inp, inp.linelist, inp.linelist5, stark_profiles(),
                                                  inp.wls.all_wls, nthreads=NT)
     assert len(res.flux) == 10001 and np.array_equal(res.wavelengths, inp.wls.all_wls_angstrom)
