@@ -28,6 +28,11 @@ each with its own random 20k-200k-line subset of a 500k-line atomic + molecular 
 400,001-point 15000-17000 A grid; one step = the whole batch through korg_synthesize_batch_dev
 (CUDA-graph replay, autotuned tile shape).
 
+    python bench.py --workload chemistry [--spectra 16]
+
+times Korg's chemical equilibrium of every layer of up to 16 stars (Teff 3500-7000 K) in one
+batched device call (--spectra 1: the 5777 K star alone).
+
     python bench.py --workload postprocess
 
 times the post-processing of 64 synthesised spectra on that grid: rotational broadening
@@ -69,7 +74,8 @@ def parse():
                     help="skip the oracle comparison of the adjoint, batch and cool-star configurations")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the reverse-mode measurement")
     ap.add_argument("--no-chemistry", action="store_true", help="skip the chemical-equilibrium measurement")
-    ap.add_argument("--workload", default="synth", choices=["synth", "batch", "adjoint", "variants", "postprocess"])
+    ap.add_argument("--workload", default="synth",
+                    choices=["synth", "batch", "adjoint", "variants", "postprocess", "chemistry"])
     ap.add_argument("--tile", default=None, help="force the line tile shape: tw,stage,split (e.g. 64,32,1)")
     ap.add_argument("--spectra", type=int, default=256, help="batch workload: number of spectra")
     ap.add_argument("--adj-scale", type=float, default=1.0, help="adjoint workload: fraction of its 70k lines")
@@ -163,15 +169,16 @@ CHEM_STARS = [(3500.0, 1.0, -2.5), (3500.0, 4.5, 0.0), (3800.0, 2.0, -1.0), (400
               (6300.0, 3.5, 0.2), (6600.0, 4.0, -2.5), (6800.0, 2.5, 0.0), (7000.0, 4.3, 0.5)]
 
 
-def chemistry_measure(ctx, torch, dev, threads):
-    """Chemical equilibrium (korg_chemical_equilibrium_dev) of every layer of 16 56-layer stars in
-    one batched call, device-timed, against the FP64 CPU restatement on every 8th layer."""
+def chemistry_measure(ctx, torch, dev, threads, n_stars=16, steps=3, warmup=1, cpu=True):
+    """Chemical equilibrium (korg_chemical_equilibrium_dev) of every layer of n_stars 56-layer
+    stars (the first n of CHEM_STARS, the 5777 K star alone for n_stars=1) in one batched call,
+    device-timed, against the FP64 CPU restatement on every 8th layer."""
     import warnings
     import numpy as np
     from korg_gb300 import _lib, standin
     from korg_gb300.statmech import solve_layers
     atms = []
-    for Teff, logg, m_H in CHEM_STARS:
+    for Teff, logg, m_H in ([CHEM_STARS[10]] if n_stars == 1 else CHEM_STARS[:n_stars]):
         atm, A_X = standin.synthetic_atmosphere(Teff, logg, m_H)
         ab = 10.0 ** (A_X - 12)
         atms.append((atm, ab / ab.sum()))
@@ -198,8 +205,9 @@ def chemistry_measure(ctx, torch, dev, threads):
                                                         status[lo:hi].data_ptr(), info[lo:hi].data_ptr(),
                                                         stream.cuda_stream))
 
-    def timed(fn, reps=3):
-        fn()
+    def timed(fn, reps=steps):
+        for _ in range(warmup):
+            fn()
         ts = []
         for _ in range(reps):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -212,6 +220,9 @@ def chemistry_measure(ctx, torch, dev, threads):
 
     ms_all = timed(lambda: run(0, L, tatm.data_ptr()))
     st, inf, got = status.cpu().numpy(), info.cpu().numpy(), dens.cpu().numpy()
+    if n_stars == 1:
+        return {"layers": L, "ms": ms_all, "layers_per_s": L / (ms_all * 1e-3), "status_ok": int((st == 0).sum()),
+                "newton_iterations": float(inf[:, 0].sum())}
     k10 = 10 * 56  # the 5777 K star, the headline's atmosphere: what one synthesize pays
     ms_one = timed(lambda: run(k10, k10 + 56, 0), reps=5)
     with warnings.catch_warnings():
@@ -219,6 +230,10 @@ def chemistry_measure(ctx, torch, dev, threads):
         t1 = time.perf_counter()
         solve_layers(T, nt, ne, abund, atm=atm_idx, ctx=ctx)
         e2e_s = time.perf_counter() - t1
+    if not cpu:
+        return {"layers": L, "ms": ms_all, "layers_per_s": L / (ms_all * 1e-3), "one_atmosphere_ms": ms_one,
+                "e2e_layers_per_s": L / e2e_s, "status_ok": int((st == 0).sum()), "newton_iterations": float(inf[:, 0].sum()),
+                "fp64_fallback_steps": float(inf[:, 4].sum())}
     # FP64 CPU restatement on every 8th layer (spawn pool, all host cores)
     sample = np.arange(0, L, 8)
     t1 = time.perf_counter()
@@ -1178,12 +1193,38 @@ def run_adjoint(args):
     ctx.close()
 
 
+def run_chemistry(args):
+    """Chemical equilibrium of every layer of a set of stars (--spectra stars, up to 16; 1: the
+    5777 K star alone), one batched korg_chemical_equilibrium_dev call per step."""
+    import torch
+    import build as korg_build
+    from korg_gb300 import _lib
+    korg_build.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    ctx = _lib.Context(0)
+    n = max(1, min(args.spectra, len(CHEM_STARS)))
+    clk = Clocks(0)
+    r = chemistry_measure(ctx, torch, dev, os.cpu_count() or 1, n_stars=n, steps=args.steps,
+                          warmup=max(args.warmup, 1), cpu=not args.no_cpu and n > 1)
+    clocks = clk.stop()
+    out = {"metric": "chemical-equilibrium layers/s", "value": r["layers_per_s"], "unit": "layers/s", "n_gpus": 1,
+           "steps": args.steps, "warmup": max(args.warmup, 1), "ms_per_step": r["ms"], "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64 (FP32 factors + FP64 refinement)", "data": "synthetic",
+           "config": {"workload": f"{n} star(s) x 56 layers, 306 molecules, one batched call per step"},
+           "chemical_equilibrium": r, "gpu_launches": args.steps, "clocks": clocks}
+    print(json.dumps(out), flush=True)
+    ctx.close()
+
+
 if __name__ == "__main__":
     a = parse()
     if a.steps is None:
         a.steps = 3 if a.workload == "batch" else 20
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload == "chemistry":
+        run_chemistry(a)
     elif a.workload == "batch":
         run_batch(a)
     elif a.workload == "postprocess":

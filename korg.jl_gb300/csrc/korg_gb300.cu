@@ -1539,7 +1539,8 @@ KORG_API int korg_set_equilibrium_tables(korg_ctx* ctx, const korg_equilibrium_t
         }
         for (const auto& a : dist) {
             inc[a.first - 1].push_back({m, a.second});
-            for (const auto& b : dist) pairs[{a.first - 1, b.first - 1}].push_back({m, a.second * b.second});
+            for (const auto& b : dist)
+                if (b.first != a.first) pairs[{a.first - 1, b.first - 1}].push_back({m, a.second * b.second});
         }
     }
     if (polyatomic && (!t->D00 || !t->lmr)) return set_err(ctx, KORG_EINVAL, "polyatomic molecules need D00 and lmr");
@@ -1551,6 +1552,18 @@ KORG_API int korg_set_equilibrium_tables(korg_ctx* ctx, const korg_equilibrium_t
         }
         inc_ptr[Z + 1] = int32_t(inc_mol.size());
     }
+    // work items of the element sums: runs of <= CE_CHUNK consecutive incidences of one element
+    std::vector<int32_t> item_elem, item_begin, elem_item_ptr(CE_NZ + 1, 0);
+    for (int Z = 0; Z < CE_NZ; Z++) {
+        for (int k = inc_ptr[Z]; k < inc_ptr[Z + 1]; k += CE_CHUNK) {
+            item_elem.push_back(Z);
+            item_begin.push_back(k);
+        }
+        elem_item_ptr[Z + 1] = int32_t(item_elem.size());
+    }
+    item_begin.push_back(inc_ptr[CE_NZ]);
+    if (item_elem.size() > size_t(CE_MAXITEM))
+        return set_err(ctx, KORG_EINVAL, "molecule set too large: %zu work items (max %d)", item_elem.size(), CE_MAXITEM);
     if (inc_mol.size() > size_t(CE_MAXINC) || pairs.size() > size_t(CE_MAXPAIR))
         return set_err(ctx, KORG_EINVAL, "molecule set too large: %zu incidences (max %d), %zu element pairs (max %d)",
                        inc_mol.size(), CE_MAXINC, pairs.size(), CE_MAXPAIR);
@@ -1575,6 +1588,7 @@ KORG_API int korg_set_equilibrium_tables(korg_ctx* ctx, const korg_equilibrium_t
     d.nk = t->n_knots;
     d.n_mol = M;
     d.n_pairs = int32_t(pair_row.size());
+    d.n_items = int32_t(item_elem.size());
     const size_t nk = size_t(t->n_knots);
     auto ip = [&](const std::vector<int32_t>& v) { return v.empty() ? (const void*)izeros.data() : (const void*)v.data(); };
     std::vector<Piece> pcs = {
@@ -1593,6 +1607,9 @@ KORG_API int korg_set_equilibrium_tables(korg_ctx* ctx, const korg_equilibrium_t
         {inc_ptr.data(), 4 * inc_ptr.size(), (const void**)&d.inc_ptr},
         {ip(inc_mol), 4 * std::max<size_t>(inc_mol.size(), 1), (const void**)&d.inc_mol},
         {ip(inc_cnt), 4 * std::max<size_t>(inc_cnt.size(), 1), (const void**)&d.inc_cnt},
+        {ip(item_elem), 4 * std::max<size_t>(item_elem.size(), 1), (const void**)&d.item_elem},
+        {item_begin.data(), 4 * item_begin.size(), (const void**)&d.item_begin},
+        {elem_item_ptr.data(), 4 * elem_item_ptr.size(), (const void**)&d.elem_item_ptr},
         {ip(pair_row), 4 * std::max<size_t>(pair_row.size(), 1), (const void**)&d.pair_row},
         {ip(pair_col), 4 * std::max<size_t>(pair_col.size(), 1), (const void**)&d.pair_col},
         {pair_ptr.data(), 4 * pair_ptr.size(), (const void**)&d.pair_ptr},

@@ -55,8 +55,10 @@ constexpr int CE_MAX_ITER = 20000;
 constexpr int CE_NINFO = 5;
 constexpr int CE_REFINE_MAX = 8;
 constexpr int CE_MAXINC = 1024;    // element -> molecule incidences
-constexpr int CE_MAXPAIR = 1024;   // (Z, W) pairs sharing a molecule
-constexpr int CE_MAXPENT = 2048;   // molecule entries of the pair lists
+constexpr int CE_MAXPAIR = 1024;   // (Z, W), Z != W, pairs sharing a molecule
+constexpr int CE_MAXPENT = 1024;   // molecule entries of the pair lists
+constexpr int CE_CHUNK = 8;        // incidences per work item of the element sums
+constexpr int CE_MAXITEM = 224;    // work items (threads of warps 0-6)
 
 // Device tables (one buffer carved by the host).  The incidence lists are derived on the host.
 struct ChemTables {
@@ -70,7 +72,9 @@ struct ChemTables {
     const double *D00, *lmr;             // polyatomics
     const int32_t *nat;                  // atoms per molecule, with multiplicity
     const int32_t *inc_ptr, *inc_mol, *inc_cnt;  // element Z-1 -> (molecule, count) at [inc_ptr[Z-1], inc_ptr[Z])
-    int32_t n_pairs;                     // (Z, W) with a molecule containing both
+    int32_t n_items;                     // element sums split in items of <= CE_CHUNK incidences
+    const int32_t *item_elem, *item_begin, *elem_item_ptr;  // item i covers [item_begin[i], item_begin[i + 1])
+    int32_t n_pairs;                     // (Z, W), Z != W, with a molecule containing both
     const int32_t *pair_row, *pair_col, *pair_ptr, *pair_mol, *pair_coef;  // coef = cnt_Z * cnt_W
 };
 
@@ -175,7 +179,8 @@ struct CeShared {
     double lwII[CE_NZ], lwIII[CE_NZ], rat1[CE_NZ], rat2[CE_NZ], e1[CE_NZ], e2[CE_NZ];
     double ab[CE_NZ], inv_scale[CE_NZ];
     double nI[CE_NZ], nII[CE_NZ], nIII[CE_NZ];
-    double fm[CE_NZ], Sq[CE_NZ], dNn[CE_N];
+    double fm[CE_NZ], Sq[CE_NZ], dd[CE_NZ], dNn[CE_N];
+    double part[CE_MAXITEM][4];  // per-item partial sums: cnt n, cnt (nat-1) n, cnt q n, cnt^2 n
     double lognK[CE_MAXMOL], nmol[CE_MAXMOL];
     double uinv64[CE_N];
     float uinv32[CE_N], vec32[CE_N];
@@ -187,9 +192,10 @@ struct CeShared {
     int perm[2][CE_LD];
     // the molecule tables, copied from global memory once per layer
     unsigned char m_atoms[CE_MAXMOL * CE_MAXATOMS], m_charge[CE_MAXMOL], m_nat[CE_MAXMOL];
+    double inc_cntd[CE_MAXINC], natm1[CE_MAXMOL], chg[CE_MAXMOL], pair_coefd[CE_MAXPENT];
     short inc_ptr[CE_NZ + 1], inc_mol[CE_MAXINC];
-    unsigned char inc_cnt[CE_MAXINC];
-    unsigned char pair_row[CE_MAXPAIR], pair_col[CE_MAXPAIR], pair_coef[CE_MAXPENT];
+    short item_begin[CE_MAXITEM + 1], elem_item_ptr[CE_NZ + 1];
+    unsigned char pair_row[CE_MAXPAIR], pair_col[CE_MAXPAIR];
     short pair_ptr[CE_MAXPAIR + 1], pair_mol[CE_MAXPENT];
     int rexp[CE_N], cexp[CE_N];
     int pivi[2];
@@ -327,13 +333,13 @@ __device__ bool ce_lu(CeShared& s, T* M, T* uinv) {
     return ok;
 }
 
-// Solve L U x = P b in one warp (warp 0): b in physical row order, x in column order; M, perm
-// and uinv from ce_lu.  Other warps return at once.
+// Solve L U x = P b in one warp (warp 0): b in physical row order, x in column order; M, the
+// permutation P (logical -> physical row) and uinv from the factorisation.  Other warps return
+// at once.
 template <typename T>
-__device__ void ce_trisolve(const CeShared& s, const T* M, const T* uinv, const T* b, T* x) {
+__device__ void ce_trisolve(const int* P, const T* M, const T* uinv, const T* b, T* x) {
     const int tid = threadIdx.x, lane = tid & 31;
     if (tid >= 32) return;
-    const int* P = s.perm[(CE_N - 1) & 1];
     const int i0 = lane, i1 = lane + 32, i2 = lane + 64;
     const bool v2 = i2 < CE_N;
     const int r0 = P[i0], r1 = P[i1], r2 = v2 ? P[i2] : 0;
@@ -399,10 +405,10 @@ __device__ bool ce_solve(CeShared& s, bool& refined) {
     __syncthreads();
     // infinity norm of the equilibrated matrix (for the stopping rule)
     const double anorm = ce_block_max(s, [&] {
-        double a = 0;
+        float a = 0;
         if (tid < CE_N)
-            for (int c = 0; c < CE_N; ++c) a += fabs(double(s.B[c * CE_LD + tid]));
-        return a;
+            for (int c = 0; c < CE_N; ++c) a += fabsf(s.B[c * CE_LD + tid]);
+        return double(a);
     }());
     refined = ce_lu<float>(s, s.B, s.uinv32);
     if (refined) {
@@ -430,7 +436,7 @@ __device__ bool ce_solve(CeShared& s, bool& refined) {
             const int G = int(g >> 52) - 1023;
             if (tid < CE_N) s.vec32[tid] = ce::scaled_to_float(s.res[tid], s.rexp[tid] + G);
             __syncthreads();
-            ce_trisolve<float>(s, s.B, s.uinv32, s.vec32, s.vec32);
+            ce_trisolve<float>(s.perm[(CE_N - 1) & 1], s.B, s.uinv32, s.vec32, s.vec32);
             __syncthreads();
             bool fin = true;
             long long dl = 0;
@@ -485,7 +491,7 @@ __device__ bool ce_solve(CeShared& s, bool& refined) {
         if (tid < CE_N) s.res[tid] = s.A[CE_N * CE_LD + tid];
         __syncthreads();
         if (!ce_lu<double>(s, s.A, s.uinv64)) return false;
-        ce_trisolve<double>(s, s.A, s.uinv64, s.res, s.sol);
+        ce_trisolve<double>(s.perm[(CE_N - 1) & 1], s.A, s.uinv64, s.res, s.sol);
         __syncthreads();
     }
     bool badS = false;
@@ -534,28 +540,29 @@ __device__ bool ce_newton(const ChemTables& tb, CeShared& s, double nt, double l
             s.nHm = exp10(((s.lognK_Hm + s.x[0]) + xe) + logxi);
         }
         __syncthreads();
-        // per-element molecule sums (fixed order) and the block-wide sums (warp 3)
-        if (tid < CE_NZ) {
-            double fm = 0, dn = 0, sq = 0;
-            for (int k = s.inc_ptr[tid]; k < s.inc_ptr[tid + 1]; ++k) {
+        // element sums in work items of <= CE_CHUNK incidences (warps 0-6), the block-wide sums
+        // over molecules and ions (warp 7)
+        if (tid < tb.n_items) {
+            double fm = 0, dn = 0, sq = 0, dd = 0;
+            for (int k = s.item_begin[tid]; k < s.item_begin[tid + 1]; ++k) {
                 const int m = s.inc_mol[k];
-                const double cn = double(s.inc_cnt[k]) * s.nmol[m];
+                const double cn = s.inc_cntd[k] * s.nmol[m];
                 fm += cn;
-                dn += double(s.m_nat[m] - 1) * cn;
-                if (s.m_charge[m]) sq += cn;
+                dn = fma(s.natm1[m], cn, dn);
+                sq = fma(s.chg[m], cn, sq);
+                dd = fma(s.inc_cntd[k], cn, dd);
             }
-            s.fm[tid] = fm;
-            s.dNn[tid] = -(ln10 * dn) * inv_nt;
-            s.Sq[tid] = sq;
-        } else if (warp == 3) {
+            s.part[tid][0] = fm;
+            s.part[tid][1] = dn;
+            s.part[tid][2] = sq;
+            s.part[tid][3] = dd;
+        } else if (warp == CE_WARPS - 1) {
             double nn = 0, qn = 0, dq = 0, i1 = 0, i2 = 0;
             for (int m = lane; m < M; m += 32) {
                 const double n = s.nmol[m];
-                nn += double(s.m_nat[m] - 1) * n;
-                if (s.m_charge[m]) {
-                    qn += n;
-                    dq += double(s.m_nat[m] - 1) * n;
-                }
+                nn = fma(s.natm1[m], n, nn);
+                qn = fma(s.chg[m], n, qn);
+                dq = fma(s.chg[m] * s.natm1[m], n, dq);
             }
             for (int Z = lane; Z < CE_NZ; Z += 32) {
                 i1 += s.nII[Z] + 2 * s.nIII[Z];
@@ -576,14 +583,25 @@ __device__ bool ce_newton(const ChemTables& tb, CeShared& s, double nt, double l
             }
         }
         __syncthreads();
-        // scaled residuals (src/statmech.jl:418-438) into column CE_N; inf-norm (newton.jl:8-14)
+        // each element's sums from its items (fixed order); scaled residuals (src/statmech.jl:418-438)
+        // into column CE_N; inf-norm (newton.jl:8-14)
         double fa = 0;
         bool bad = false;
         if (tid < CE_N) {
             double F;
             if (tid < CE_NZ) {
+                double fm = 0, dn = 0, sq = 0, dd = 0;
+                for (int i = s.elem_item_ptr[tid]; i < s.elem_item_ptr[tid + 1]; ++i) {
+                    fm += s.part[i][0];
+                    dn += s.part[i][1];
+                    sq += s.part[i][2];
+                    dd += s.part[i][3];
+                }
+                s.dNn[tid] = -(ln10 * dn) * inv_nt;
+                s.Sq[tid] = sq;
+                s.dd[tid] = dd;
                 const double n_nuclei = (nt - s.ne) + s.nn_mol;
-                double f = s.fm[tid];
+                double f = fm;
                 if (tid == 0) f += s.nHm;
                 f += ((s.nI[tid] + s.nII[tid]) + s.nIII[tid]) - s.ab[tid] * n_nuclei;
                 F = f / (s.ab[tid] * nt);
@@ -600,35 +618,35 @@ __device__ bool ce_newton(const ChemTables& tb, CeShared& s, double nt, double l
         if (inf < 1e-8) return true;
         // Jacobian, dense part: the n_nuclei coupling (-d n_nuclei/dx_c / n_tot in every atom
         // row), the atoms' own densities, the n_e column, the charge row
-        for (int idx = tid; idx < CE_N * CE_N; idx += CE_THREADS) {
-            const int c = idx / CE_N, r = idx - c * CE_N;
-            double v;
-            if (r < CE_NZ) {
-                v = s.dNn[c];
-                if (c == r) {
-                    double w = ln10 * ((s.nI[r] + s.nII[r]) + s.nIII[r]);
-                    if (r == 0) w += ln10 * s.nHm;
-                    v += w * s.inv_scale[r];
-                } else if (c == CE_NZ) {
-                    double w = -ln10 * s.Sq[r] - ln10 * (s.nII[r] + 2 * s.nIII[r]);
-                    if (r == 0) w += ln10 * s.nHm;
-                    v += w * s.inv_scale[r];
-                }
-            } else if (c < CE_NZ) {
-                v = ln10 * s.Sq[c] + ln10 * (s.nII[c] + 2 * s.nIII[c]);
-                if (c == 0) v -= ln10 * s.nHm;
-                v *= inv_nt;
+        for (int idx = tid; idx < CE_NZ * CE_NZ; idx += CE_THREADS) {  // atom rows, atom columns
+            const int c = idx / CE_NZ, r = idx - c * CE_NZ;
+            if (c != r) s.A[c * CE_LD + r] = s.dNn[c];
+        }
+        for (int q = tid; q < 3 * CE_NZ + 1; q += CE_THREADS) {  // diagonal, n_e column, charge row
+            const int r = q % CE_NZ, part = q / CE_NZ;
+            if (part == 0) {
+                double w = ln10 * (((s.nI[r] + s.nII[r]) + s.nIII[r]) + s.dd[r]);
+                if (r == 0) w += ln10 * s.nHm;
+                s.A[r * CE_LD + r] = s.dNn[r] + w * s.inv_scale[r];
+            } else if (part == 1) {
+                double w = -ln10 * s.Sq[r] - ln10 * (s.nII[r] + 2 * s.nIII[r]);
+                if (r == 0) w += ln10 * s.nHm;
+                s.A[CE_NZ * CE_LD + r] = s.dNn[CE_NZ] + w * s.inv_scale[r];
+            } else if (part == 2) {
+                double v = ln10 * s.Sq[r] + ln10 * (s.nII[r] + 2 * s.nIII[r]);
+                if (r == 0) v -= ln10 * s.nHm;
+                s.A[r * CE_LD + CE_NZ] = v * inv_nt;
             } else {
-                v = (((-ln10 * s.qn) - ln10 * s.nHm) - ln10 * s.ion2 - ln10 * s.ne) * inv_nt;
+                s.A[CE_NZ * CE_LD + CE_NZ] = (((-ln10 * s.qn) - ln10 * s.nHm) - ln10 * s.ion2 - ln10 * s.ne) * inv_nt;
             }
-            s.A[c * CE_LD + r] = v;
         }
         __syncthreads();
-        // Jacobian, molecule coupling: entry (Z, W) gains ln10 sum cnt_Z cnt_W n_mol / (ab_Z n_tot)
+        // Jacobian, molecule coupling off the diagonal (the diagonal's came with the element sums):
+        // entry (Z, W) gains ln10 sum cnt_Z cnt_W n_mol / (ab_Z n_tot)
         for (int p = tid; p < tb.n_pairs; p += CE_THREADS) {
             const int Z = s.pair_row[p], W = s.pair_col[p];
             double sum = 0;
-            for (int k = s.pair_ptr[p]; k < s.pair_ptr[p + 1]; ++k) sum += double(s.pair_coef[k]) * s.nmol[s.pair_mol[k]];
+            for (int k = s.pair_ptr[p]; k < s.pair_ptr[p + 1]; ++k) sum = fma(s.pair_coefd[k], s.nmol[s.pair_mol[k]], sum);
             s.A[W * CE_LD + Z] += ln10 * sum * s.inv_scale[Z];
         }
         __syncthreads();
@@ -661,12 +679,18 @@ __global__ void __launch_bounds__(CE_THREADS) chem_eq_kernel(ChemTables tb, Chem
     for (int m = tid; m < M; m += CE_THREADS) {
         s.m_charge[m] = (unsigned char)tb.charge[m];
         s.m_nat[m] = (unsigned char)tb.nat[m];
+        s.natm1[m] = double(tb.nat[m] - 1);
+        s.chg[m] = double(tb.charge[m]);
     }
-    for (int i = tid; i <= CE_NZ; i += CE_THREADS) s.inc_ptr[i] = (short)tb.inc_ptr[i];
+    for (int i = tid; i <= CE_NZ; i += CE_THREADS) {
+        s.inc_ptr[i] = (short)tb.inc_ptr[i];
+        s.elem_item_ptr[i] = (short)tb.elem_item_ptr[i];
+    }
     for (int i = tid; i < tb.inc_ptr[CE_NZ]; i += CE_THREADS) {
         s.inc_mol[i] = (short)tb.inc_mol[i];
-        s.inc_cnt[i] = (unsigned char)tb.inc_cnt[i];
+        s.inc_cntd[i] = double(tb.inc_cnt[i]);
     }
+    for (int i = tid; i <= tb.n_items; i += CE_THREADS) s.item_begin[i] = (short)tb.item_begin[i];
     for (int p = tid; p <= tb.n_pairs; p += CE_THREADS) {
         s.pair_ptr[p] = (short)tb.pair_ptr[p];
         if (p < tb.n_pairs) {
@@ -676,7 +700,7 @@ __global__ void __launch_bounds__(CE_THREADS) chem_eq_kernel(ChemTables tb, Chem
     }
     for (int k = tid; k < tb.pair_ptr[tb.n_pairs]; k += CE_THREADS) {
         s.pair_mol[k] = (short)tb.pair_mol[k];
-        s.pair_coef[k] = (unsigned char)tb.pair_coef[k];
+        s.pair_coefd[k] = double(tb.pair_coef[k]);
     }
     // per-layer constants: Saha factors (saha_ion_weights with n_e = 1, src/statmech.jl:19-35,
     // 362-372), the starting guess (atoms only, n_e from the model atmosphere, :151-155, 235-237),
