@@ -175,6 +175,133 @@ function radiative_transfer(atm::Korg.PlanarAtmosphere, α::Matrix{Float64}, S::
     F, reshape(F ./ 2π, 1, nwl), [1.0], [1.0]
 end
 
+# ---------------------------------------------------------------------------- chemical equilibrium
+# korg_equilibrium_tables / korg_chem_layers of include/korg_gb300.h
+struct CEqTables
+    n_knots::Int32
+    lnT::Ptr{Float64}
+    U_u::Ptr{Float64}
+    U_z::Ptr{Float64}
+    chi::Ptr{Float64}
+    n_mol::Int32
+    atoms::Ptr{Int32}
+    charge::Ptr{Int32}
+    kind::Ptr{Int32}
+    off::Ptr{Int64}
+    spl_t::Ptr{Float64}
+    spl_u::Ptr{Float64}
+    spl_z::Ptr{Float64}
+    D00::Ptr{Float64}
+    lmr::Ptr{Float64}
+end
+
+struct CChemLayers
+    L::Int32
+    T::Ptr{Float64}
+    n_tot::Ptr{Float64}
+    ne_model::Ptr{Float64}
+    abundances::Ptr{Float64}
+    atm::Ptr{Int32}
+end
+
+const KORG_ECHEM = 7
+
+"""
+    set_equilibrium_tables!(ctx; ionization_energies, partition_funcs, log_equilibrium_constants)
+
+Uploads Korg's statmech data (src/read_statmech_quantities.jl) for `chemical_equilibrium`:
+atomic partition-function splines, ionisation energies, the Barklem & Collet log K splines and,
+for the polyatomics (whose log K Korg builds as closures, :63-90), their atomization energies,
+mass ratios and partition-function splines.  Returns the molecules in table order.
+"""
+function set_equilibrium_tables!(ctx::Context=default_context();
+                                 ionization_energies=Korg.ionization_energies,
+                                 partition_funcs=Korg.default_partition_funcs,
+                                 log_equilibrium_constants=Korg.default_log_equilibrium_constants)
+    ref = partition_funcs[Korg.species"H I"]
+    nk = length(ref.t)
+    U_u, U_z = zeros(nk, 276), zeros(nk, 276)        # column 3(Z-1)+q: row-major [276][nk] in C
+    for Z in 1:92, q in 0:2
+        (Z == 1 && q == 2) && continue
+        spl = partition_funcs[Korg.Species(Korg.Formula(Z), q)]
+        U_u[:, 3(Z - 1) + q + 1] .= spl.u
+        U_z[:, 3(Z - 1) + q + 1] .= spl.z
+    end
+    chi = zeros(3, 92)
+    for Z in 1:92
+        chi[:, Z] .= ionization_energies[Z][1:3]
+    end
+    D00s = Dict{Korg.Species,Float64}()
+    csv = joinpath(pkgdir(Korg), "data", "polyatomic_partition_funcs", "atomization_energies.csv")
+    for line in readlines(csv)[2:end]
+        name, e = split(line, ",")
+        D00s[Korg.Species(name)] = parse(Float64, e) * 0.01036
+    end
+    mols = collect(keys(log_equilibrium_constants))
+    n = length(mols)
+    atoms, charge, kind = zeros(Int32, 6, n), zeros(Int32, n), zeros(Int32, n)
+    D00, lmr, off = zeros(n), zeros(n), Int64[0]
+    t, u, z = Float64[], Float64[], Float64[]
+    for (m, mol) in enumerate(mols)
+        Zs = Korg.get_atoms(mol.formula)
+        atoms[1:length(Zs), m] .= Zs
+        charge[m] = mol.charge
+        if haskey(D00s, mol)
+            kind[m] = 1
+            D00[m] = D00s[mol]
+            lmr[m] = sum(log10(Korg.atomic_masses[Z]) for Z in Zs) - log10(Korg.get_mass(mol))
+            spl = partition_funcs[mol]
+        else
+            spl = log_equilibrium_constants[mol]
+        end
+        append!(t, spl.t)
+        append!(u, spl.u)
+        append!(z, spl.z)
+        push!(off, length(t))
+    end
+    GC.@preserve U_u U_z chi atoms charge kind off t u z D00 lmr begin
+        tab = Ref(CEqTables(nk, pointer(collect(Float64, ref.t)), pointer(U_u), pointer(U_z), pointer(chi), n,
+                            pointer(atoms), pointer(charge), pointer(kind), pointer(off), pointer(t),
+                            pointer(u), pointer(z), pointer(D00), pointer(lmr)))
+        check(ctx, ccall((:korg_set_equilibrium_tables, LIB), Cint, (Ptr{Cvoid}, Ref{CEqTables}), ctx.ptr, tab))
+    end
+    mols
+end
+
+"""
+    chemical_equilibrium(temps, nₜs, nₑs, absolute_abundances; ctx, molecules)
+
+GPU drop-in for the per-layer `Korg.chemical_equilibrium` loop of `synthesize`
+(src/statmech.jl:148-206, src/synthesize.jl:210-219): every layer in one call.  Returns the
+electron densities and a Dict species => per-layer number densities, as the loop builds them.
+`molecules` is what `set_equilibrium_tables!` returned for this context.
+"""
+function chemical_equilibrium(temps, nₜs, nₑs, absolute_abundances; molecules, ctx::Context=default_context())
+    L = length(temps)
+    T, nt, ne = collect(Float64, temps), collect(Float64, nₜs), collect(Float64, nₑs)
+    ab = collect(Float64, absolute_abundances)
+    dens = Matrix{Float64}(undef, 278 + length(molecules), L)
+    status = Vector{Int32}(undef, L)
+    rc = GC.@preserve T nt ne ab begin
+        lay = Ref(CChemLayers(L, pointer(T), pointer(nt), pointer(ne), pointer(ab), C_NULL))
+        ccall((:korg_chemical_equilibrium, LIB), Cint,
+              (Ptr{Cvoid}, Ref{CChemLayers}, Int32, Ptr{Float64}, Ptr{Int32}, Ptr{Float64}),
+              ctx.ptr, lay, 1, dens, status, C_NULL)
+    end
+    rc == KORG_ECHEM && throw(Korg.ChemicalEquilibriumError("layer $(findfirst(!=(0), status)): status " *
+                                                            "$(status[findfirst(!=(0), status)])"))
+    check(ctx, rc)
+    nd = Dict{Korg.Species,Vector{Float64}}()
+    for Z in 1:92, q in 0:2
+        nd[Korg.Species(Korg.Formula(Z), q)] = dens[2 + 3(Z - 1) + q, :]
+    end
+    nd[Korg.species"H-"] = dens[278, :]
+    for (m, mol) in enumerate(molecules)
+        nd[mol] = dens[278 + m, :]
+    end
+    dens[1, :], nd
+end
+
 # ---------------------------------------------------------------------------- differentiable path
 # korg_synth_inputs / korg_synth_grads of include/korg_gb300.h
 struct CSynthInputs
