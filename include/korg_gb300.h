@@ -245,6 +245,20 @@ KORG_API int korg_chemical_equilibrium(korg_ctx *ctx, const korg_chem_layers *la
 KORG_API int korg_chemical_equilibrium_dev(korg_ctx *ctx, const korg_chem_layers *layers,
                                            int32_t n_atm, double *densities, int32_t *status,
                                            double *info, void *stream);
+/* Reverse mode of chemical_equilibrium at the solution `densities` returned for `layers` (what
+ * the reference's ForwardDiff method computes, src/statmech.jl:307-355, by the implicit-function
+ * rule): given gbar [L][KORG_CHEM_MOL0 + n_mol], the cotangents of every density in the same
+ * layout, returns per layer dL/dT (dT [L]), dL/dn_tot (dn_tot [L]) and dL/d(abundance of each
+ * element) (dab [L][92], the abundances as passed, i.e. normalised; sum over an atmosphere's
+ * layers for its gradient).  The model n_e does not enter the solution.  KORG_ECHEM if a layer's
+ * system is singular; _dev: device pointers, status [L] on the device, stream-ordered. */
+KORG_API int korg_chemical_equilibrium_vjp(korg_ctx *ctx, const korg_chem_layers *layers, int32_t n_atm,
+                                           const double *densities, const double *gbar, double *dT,
+                                           double *dn_tot, double *dab);
+KORG_API int korg_chemical_equilibrium_vjp_dev(korg_ctx *ctx, const korg_chem_layers *layers,
+                                               int32_t n_atm, const double *densities,
+                                               const double *gbar, double *dT, double *dn_tot,
+                                               double *dab, int32_t *status, void *stream);
 
 /* line_absorption!(alpha, linelist, wls, temps, ne, n_densities, partition_fns, xi, alpha_cntm;
  * cutoff_threshold) -- src/line_absorption.jl:33-129.  alpha (host, L x nwl) is accumulated in

@@ -1721,6 +1721,71 @@ KORG_API int korg_chemical_equilibrium(korg_ctx* ctx, const korg_chem_layers* y,
     return KORG_OK;
 }
 
+KORG_API int korg_chemical_equilibrium_vjp_dev(korg_ctx* ctx, const korg_chem_layers* y, int32_t n_atm,
+                                               const double* dens, const double* gbar, double* dT, double* dn_tot,
+                                               double* dab, int32_t* status, void* stream) {
+    if (!ctx) return KORG_EINVAL;
+    if (!y || y->L < 1 || !y->T || !y->n_tot || !y->ne_model || !y->abundances || n_atm < 1 || !dens || !gbar ||
+        !dT || !dn_tot || !dab || !status)
+        return set_err(ctx, KORG_EINVAL, "bad arguments");
+    if (!ctx->have_chem) return set_err(ctx, KORG_ENOTABLES, "korg_set_equilibrium_tables() has not been called");
+    KCUDA(cudaSetDevice(ctx->device));
+    const int smem = int(sizeof(CeShared));
+    KCUDA(cudaFuncSetAttribute(chem_vjp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    const ChemLayersDev ly{y->L, y->T, y->n_tot, y->ne_model, y->abundances, y->atm};
+    chem_vjp_kernel<<<unsigned(y->L), CE_THREADS, smem, static_cast<cudaStream_t>(stream)>>>(ctx->chem_tab, ly, dens,
+                                                                                             gbar, dT, dn_tot, dab,
+                                                                                             status);
+    KCUDA(cudaGetLastError());
+    return KORG_OK;
+}
+
+KORG_API int korg_chemical_equilibrium_vjp(korg_ctx* ctx, const korg_chem_layers* y, int32_t n_atm,
+                                           const double* dens, const double* gbar, double* dT, double* dn_tot,
+                                           double* dab) {
+    if (!ctx) return KORG_EINVAL;
+    if (!y || y->L < 1 || !y->T || !y->n_tot || !y->ne_model || !y->abundances || n_atm < 1 || !dens || !gbar ||
+        !dT || !dn_tot || !dab)
+        return set_err(ctx, KORG_EINVAL, "bad arguments");
+    if (!ctx->have_chem) return set_err(ctx, KORG_ENOTABLES, "korg_set_equilibrium_tables() has not been called");
+    const int L = y->L;
+    for (int l = 0; l < L; l++) {
+        const double T = y->T[l];
+        if (!(std::isfinite(T) && T > 0 && std::log(T) >= ctx->chem_lnT0 && std::log(T) <= ctx->chem_lnT1))
+            return set_err(ctx, KORG_EINVAL, "layer %d: T = %g outside the partition functions' range", l, T);
+        if (y->atm && (y->atm[l] < 0 || y->atm[l] >= n_atm))
+            return set_err(ctx, KORG_EINVAL, "layer %d: atmosphere index %d", l, y->atm[l]);
+    }
+    KCUDA(cudaSetDevice(ctx->device));
+    const size_t nspec = size_t(KORG_CHEM_MOL0 + ctx->chem_tab.n_mol);
+    Stager st;
+    const size_t o_T = st.add(y->T, 8 * size_t(L)), o_n = st.add(y->n_tot, 8 * size_t(L));
+    const size_t o_e = st.add(y->ne_model, 8 * size_t(L));
+    const size_t o_a = st.add(y->abundances, 8 * size_t(n_atm) * CE_NZ);
+    const size_t o_m = y->atm ? st.add(y->atm, 4 * size_t(L)) : 0;
+    const size_t o_d = st.add(dens, 8 * size_t(L) * nspec), o_g = st.add(gbar, 8 * size_t(L) * nspec);
+    const size_t o_dT = st.add(nullptr, 8 * size_t(L)), o_dn = st.add(nullptr, 8 * size_t(L));
+    const size_t o_da = st.add(nullptr, 8 * size_t(L) * CE_NZ), o_s = st.add(nullptr, 4 * size_t(L));
+    char* b = nullptr;
+    KCHECK(upload(ctx, st, &b));
+    const korg_chem_layers d{L, (const double*)(b + o_T), (const double*)(b + o_n), (const double*)(b + o_e),
+                             (const double*)(b + o_a), y->atm ? (const int32_t*)(b + o_m) : nullptr};
+    KCHECK(korg_chemical_equilibrium_vjp_dev(ctx, &d, n_atm, (const double*)(b + o_d), (const double*)(b + o_g),
+                                             (double*)(b + o_dT), (double*)(b + o_dn), (double*)(b + o_da),
+                                             (int32_t*)(b + o_s), ctx->stream));
+    std::vector<int32_t> status(L);
+    KCUDA(cudaMemcpyAsync(dT, b + o_dT, 8 * size_t(L), cudaMemcpyDeviceToHost, ctx->stream));
+    KCUDA(cudaMemcpyAsync(dn_tot, b + o_dn, 8 * size_t(L), cudaMemcpyDeviceToHost, ctx->stream));
+    KCUDA(cudaMemcpyAsync(dab, b + o_da, 8 * size_t(L) * CE_NZ, cudaMemcpyDeviceToHost, ctx->stream));
+    KCUDA(cudaMemcpyAsync(status.data(), b + o_s, 4 * size_t(L), cudaMemcpyDeviceToHost, ctx->stream));
+    KCUDA(cudaStreamSynchronize(ctx->stream));
+    for (int l = 0; l < L; l++)
+        if (status[l] != KORG_CHEM_OK)
+            return set_err(ctx, KORG_ECHEM, "chemical-equilibrium reverse mode: singular or non-finite system in layer %d",
+                           l);
+    return KORG_OK;
+}
+
 KORG_API int korg_line_absorption(korg_ctx* ctx, double* alpha, const double* wls, int64_t nwl,
                                   const korg_lines* lines, const korg_layers* layers, const korg_cntm* cntm,
                                   double cutoff, int precision, int64_t* n_evals) {

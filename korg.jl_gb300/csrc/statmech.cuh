@@ -110,6 +110,21 @@ __device__ inline double spline(const double* t, const double* u, const double* 
     return I + C + D;
 }
 
+// d/dx of the same spline (zero outside the knots, where it is flat)
+__device__ inline double spline_deriv(const double* t, const double* u, const double* z, int n, double x) {
+    if (!(t[0] <= x && x <= t[n - 1])) return 0.0;
+    int lo = 0, hi = n;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (t[mid] <= x) lo = mid; else hi = mid;
+    }
+    const int i = lo < n - 2 ? lo : n - 2;
+    const double h = t[i + 1] - t[i];
+    const double a = t[i + 1] - x, b = x - t[i];
+    return -z[i] * (a * a) / (2 * h) + z[i + 1] * (b * b) / (2 * h) + (u[i + 1] / h - z[i + 1] * h / 6) -
+           (u[i] / h - z[i] * h / 6);
+}
+
 __device__ inline double translational_U(double m, double T) {  // src/statmech.jl:47-51
     return pow(TWO_PI * m * KB_CGS * T / (H_CGS * H_CGS), 1.5);
 }
@@ -182,11 +197,13 @@ struct CeShared {
     double fm[CE_NZ], Sq[CE_NZ], dd[CE_NZ], dNn[CE_N];
     double part[CE_MAXITEM][4];  // per-item partial sums: cnt n, cnt (nat-1) n, cnt q n, cnt^2 n
     double lognK[CE_MAXMOL], nmol[CE_MAXMOL];
+    double dlognK[CE_MAXMOL], wmol[CE_MAXMOL], dlwII[CE_NZ], dlwIII[CE_NZ];  // reverse mode
     double uinv64[CE_N];
     float uinv32[CE_N], vec32[CE_N];
     double red[CE_WARPS], red2[CE_WARPS];
     long long redl[4][CE_WARPS];
-    double ne, nHm, nn_mol, qn, dNe_mol, ion1, ion2, lognK_Hm, transU, lnT;
+    double ne, nHm, nn_mol, qn, dNe_mol, ion1, ion2, lognK_Hm, transU, lnT, dlognK_Hm;
+    double vsum[3];
     double piv64[2];
     float piv32[2];
     int perm[2][CE_LD];
@@ -499,182 +516,165 @@ __device__ bool ce_solve(CeShared& s, bool& refined) {
     return !__syncthreads_or(badS);
 }
 
-// One Newton solve at log xi from s.x (clipped_newton, src/newton.jl:2-35).  Every thread calls
-// it; control flow is uniform.  Returns whether |F|_inf < tol was reached; budget counts the
-// iterations left for the layer (exhausted: out_of_budget is set); fallbacks counts the steps
-// that needed the FP64 elimination.
-__device__ bool ce_newton(const ChemTables& tb, CeShared& s, double nt, double logxi, int max_iter, int& budget,
-                          bool& out_of_budget, double& last_inf, int& fallbacks) {
+// Densities of every species, the scaled residuals F (column CE_N of s.A) and their inf-norm at
+// s.x for log xi; then, unless |F|_inf < 1e-8 (or always_jacobian), the Jacobian in s.A.
+// Returns 1 when converged, 0 with the system assembled, -1 when F is not finite.  Every thread
+// calls it; control flow is uniform.
+__device__ int ce_assemble(const ChemTables& tb, CeShared& s, double nt, double logxi, bool always_jacobian,
+                           double& inf_out) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int M = tb.n_mol;
     const double ln10 = ce::LN10;
     const double inv_nt = 1.0 / nt;
-    last_inf = INFINITY;
-    for (int it = 0; it < max_iter; ++it) {
-        if (budget <= 0) {
-            out_of_budget = true;
-            return false;
+    // densities of every species at x (src/statmech.jl:385-430)
+    const double xe = s.x[CE_NZ];
+    for (int m = tid; m < M; m += CE_THREADS) {
+        const unsigned char* at = s.m_atoms + m * CE_MAXATOMS;
+        double lg = -s.lognK[m] + logxi;
+        if (s.m_charge[m] == 0) {
+            for (int j = 0; j < CE_MAXATOMS && at[j]; ++j) lg += s.x[at[j] - 1];
+        } else {
+            const int Z1 = at[0] - 1, Z2 = at[1] - 1;
+            lg += ((s.x[Z1] + s.lwII[Z1]) - xe) + s.x[Z2];
         }
-        --budget;
-        // densities of every species at x (src/statmech.jl:385-430)
-        const double xe = s.x[CE_NZ];
-        for (int m = tid; m < M; m += CE_THREADS) {
-            const unsigned char* at = s.m_atoms + m * CE_MAXATOMS;
-            double lg = -s.lognK[m] + logxi;
-            if (s.m_charge[m] == 0) {
-                for (int j = 0; j < CE_MAXATOMS && at[j]; ++j) lg += s.x[at[j] - 1];
-            } else {
-                const int Z1 = at[0] - 1, Z2 = at[1] - 1;
-                lg += ((s.x[Z1] + s.lwII[Z1]) - xe) + s.x[Z2];
-            }
-            s.nmol[m] = exp10(lg);
-        }
-        for (int Z = tid; Z < CE_NZ; Z += CE_THREADS) {
-            const double xz = s.x[Z];
-            s.nI[Z] = exp10(xz);
-            s.nII[Z] = exp10((xz + s.lwII[Z]) - xe);
-            s.nIII[Z] = exp10((xz + s.lwIII[Z]) - 2 * xe);
-        }
-        if (tid == 0) {
-            s.ne = exp10(xe);
-            s.nHm = exp10(((s.lognK_Hm + s.x[0]) + xe) + logxi);
-        }
-        __syncthreads();
-        // element sums in work items of <= CE_CHUNK incidences (warps 0-6), the block-wide sums
-        // over molecules and ions (warp 7)
-        if (tid < tb.n_items) {
-            double fm = 0, dn = 0, sq = 0, dd = 0;
-            for (int k = s.item_begin[tid]; k < s.item_begin[tid + 1]; ++k) {
-                const int m = s.inc_mol[k];
-                const double cn = s.inc_cntd[k] * s.nmol[m];
-                fm += cn;
-                dn = fma(s.natm1[m], cn, dn);
-                sq = fma(s.chg[m], cn, sq);
-                dd = fma(s.inc_cntd[k], cn, dd);
-            }
-            s.part[tid][0] = fm;
-            s.part[tid][1] = dn;
-            s.part[tid][2] = sq;
-            s.part[tid][3] = dd;
-        } else if (warp == CE_WARPS - 1) {
-            double nn = 0, qn = 0, dq = 0, i1 = 0, i2 = 0;
-            for (int m = lane; m < M; m += 32) {
-                const double n = s.nmol[m];
-                nn = fma(s.natm1[m], n, nn);
-                qn = fma(s.chg[m], n, qn);
-                dq = fma(s.chg[m] * s.natm1[m], n, dq);
-            }
-            for (int Z = lane; Z < CE_NZ; Z += 32) {
-                i1 += s.nII[Z] + 2 * s.nIII[Z];
-                i2 += s.nII[Z] + 4 * s.nIII[Z];
-            }
-            nn = ce::warp_sum(nn);
-            qn = ce::warp_sum(qn);
-            dq = ce::warp_sum(dq);
-            i1 = ce::warp_sum(i1);
-            i2 = ce::warp_sum(i2);
-            if (lane == 0) {
-                s.nn_mol = nn;
-                s.qn = qn;
-                s.dNe_mol = dq;
-                s.ion1 = i1;
-                s.ion2 = i2;
-                s.dNn[CE_NZ] = -(-ln10 * s.ne - ln10 * dq) * inv_nt;
-            }
-        }
-        __syncthreads();
-        // each element's sums from its items (fixed order); scaled residuals (src/statmech.jl:418-438)
-        // into column CE_N; inf-norm (newton.jl:8-14)
-        double fa = 0;
-        bool bad = false;
-        if (tid < CE_N) {
-            double F;
-            if (tid < CE_NZ) {
-                double fm = 0, dn = 0, sq = 0, dd = 0;
-                for (int i = s.elem_item_ptr[tid]; i < s.elem_item_ptr[tid + 1]; ++i) {
-                    fm += s.part[i][0];
-                    dn += s.part[i][1];
-                    sq += s.part[i][2];
-                    dd += s.part[i][3];
-                }
-                s.dNn[tid] = -(ln10 * dn) * inv_nt;
-                s.Sq[tid] = sq;
-                s.dd[tid] = dd;
-                const double n_nuclei = (nt - s.ne) + s.nn_mol;
-                double f = fm;
-                if (tid == 0) f += s.nHm;
-                f += ((s.nI[tid] + s.nII[tid]) + s.nIII[tid]) - s.ab[tid] * n_nuclei;
-                F = f / (s.ab[tid] * nt);
-            } else {
-                F = (((s.qn - s.nHm) + s.ion1) - s.ne) / nt;
-            }
-            s.A[CE_N * CE_LD + tid] = F;
-            bad = !isfinite(F);
-            fa = fabs(F);
-        }
-        if (__syncthreads_or(bad)) return false;
-        const double inf = ce_block_max(s, fa);
-        last_inf = inf;
-        if (inf < 1e-8) return true;
-        // Jacobian, dense part: the n_nuclei coupling (-d n_nuclei/dx_c / n_tot in every atom
-        // row), the atoms' own densities, the n_e column, the charge row
-        for (int idx = tid; idx < CE_NZ * CE_NZ; idx += CE_THREADS) {  // atom rows, atom columns
-            const int c = idx / CE_NZ, r = idx - c * CE_NZ;
-            if (c != r) s.A[c * CE_LD + r] = s.dNn[c];
-        }
-        for (int q = tid; q < 3 * CE_NZ + 1; q += CE_THREADS) {  // diagonal, n_e column, charge row
-            const int r = q % CE_NZ, part = q / CE_NZ;
-            if (part == 0) {
-                double w = ln10 * (((s.nI[r] + s.nII[r]) + s.nIII[r]) + s.dd[r]);
-                if (r == 0) w += ln10 * s.nHm;
-                s.A[r * CE_LD + r] = s.dNn[r] + w * s.inv_scale[r];
-            } else if (part == 1) {
-                double w = -ln10 * s.Sq[r] - ln10 * (s.nII[r] + 2 * s.nIII[r]);
-                if (r == 0) w += ln10 * s.nHm;
-                s.A[CE_NZ * CE_LD + r] = s.dNn[CE_NZ] + w * s.inv_scale[r];
-            } else if (part == 2) {
-                double v = ln10 * s.Sq[r] + ln10 * (s.nII[r] + 2 * s.nIII[r]);
-                if (r == 0) v -= ln10 * s.nHm;
-                s.A[r * CE_LD + CE_NZ] = v * inv_nt;
-            } else {
-                s.A[CE_NZ * CE_LD + CE_NZ] = (((-ln10 * s.qn) - ln10 * s.nHm) - ln10 * s.ion2 - ln10 * s.ne) * inv_nt;
-            }
-        }
-        __syncthreads();
-        // Jacobian, molecule coupling off the diagonal (the diagonal's came with the element sums):
-        // entry (Z, W) gains ln10 sum cnt_Z cnt_W n_mol / (ab_Z n_tot)
-        for (int p = tid; p < tb.n_pairs; p += CE_THREADS) {
-            const int Z = s.pair_row[p], W = s.pair_col[p];
-            double sum = 0;
-            for (int k = s.pair_ptr[p]; k < s.pair_ptr[p + 1]; ++k) sum = fma(s.pair_coefd[k], s.nmol[s.pair_mol[k]], sum);
-            s.A[W * CE_LD + Z] += ln10 * sum * s.inv_scale[Z];
-        }
-        __syncthreads();
-        bool refined = false;
-        if (!ce_solve(s, refined)) return false;
-        if (!refined) ++fallbacks;
-        // step = -(J \ F), clipped so that no unknown moves more than 1 dex
-        const double sm = ce_block_max(s, tid < CE_N ? fabs(s.sol[tid]) : 0.0);
-        const double alpha = sm > 1.0 ? 1.0 / sm : 1.0;
-        if (tid < CE_N) s.x[tid] = s.x[tid] + alpha * (-s.sol[tid]);
-        __syncthreads();
+        s.nmol[m] = exp10(lg);
     }
-    return false;
+    for (int Z = tid; Z < CE_NZ; Z += CE_THREADS) {
+        const double xz = s.x[Z];
+        s.nI[Z] = exp10(xz);
+        s.nII[Z] = exp10((xz + s.lwII[Z]) - xe);
+        s.nIII[Z] = exp10((xz + s.lwIII[Z]) - 2 * xe);
+    }
+    if (tid == 0) {
+        s.ne = exp10(xe);
+        s.nHm = exp10(((s.lognK_Hm + s.x[0]) + xe) + logxi);
+    }
+    __syncthreads();
+    // element sums in work items of <= CE_CHUNK incidences (warps 0-6), the block-wide sums
+    // over molecules and ions (warp 7)
+    if (tid < tb.n_items) {
+        double fm = 0, dn = 0, sq = 0, dd = 0;
+        for (int k = s.item_begin[tid]; k < s.item_begin[tid + 1]; ++k) {
+            const int m = s.inc_mol[k];
+            const double cn = s.inc_cntd[k] * s.nmol[m];
+            fm += cn;
+            dn = fma(s.natm1[m], cn, dn);
+            sq = fma(s.chg[m], cn, sq);
+            dd = fma(s.inc_cntd[k], cn, dd);
+        }
+        s.part[tid][0] = fm;
+        s.part[tid][1] = dn;
+        s.part[tid][2] = sq;
+        s.part[tid][3] = dd;
+    } else if (warp == CE_WARPS - 1) {
+        double nn = 0, qn = 0, dq = 0, i1 = 0, i2 = 0;
+        for (int m = lane; m < M; m += 32) {
+            const double n = s.nmol[m];
+            nn = fma(s.natm1[m], n, nn);
+            qn = fma(s.chg[m], n, qn);
+            dq = fma(s.chg[m] * s.natm1[m], n, dq);
+        }
+        for (int Z = lane; Z < CE_NZ; Z += 32) {
+            i1 += s.nII[Z] + 2 * s.nIII[Z];
+            i2 += s.nII[Z] + 4 * s.nIII[Z];
+        }
+        nn = ce::warp_sum(nn);
+        qn = ce::warp_sum(qn);
+        dq = ce::warp_sum(dq);
+        i1 = ce::warp_sum(i1);
+        i2 = ce::warp_sum(i2);
+        if (lane == 0) {
+            s.nn_mol = nn;
+            s.qn = qn;
+            s.dNe_mol = dq;
+            s.ion1 = i1;
+            s.ion2 = i2;
+            s.dNn[CE_NZ] = -(-ln10 * s.ne - ln10 * dq) * inv_nt;
+        }
+    }
+    __syncthreads();
+    // each element's sums from its items (fixed order); scaled residuals (src/statmech.jl:418-438)
+    // into column CE_N; inf-norm (newton.jl:8-14)
+    double fa = 0;
+    bool bad = false;
+    if (tid < CE_N) {
+        double F;
+        if (tid < CE_NZ) {
+            double fm = 0, dn = 0, sq = 0, dd = 0;
+            for (int i = s.elem_item_ptr[tid]; i < s.elem_item_ptr[tid + 1]; ++i) {
+                fm += s.part[i][0];
+                dn += s.part[i][1];
+                sq += s.part[i][2];
+                dd += s.part[i][3];
+            }
+            s.dNn[tid] = -(ln10 * dn) * inv_nt;
+            s.Sq[tid] = sq;
+            s.dd[tid] = dd;
+            const double n_nuclei = (nt - s.ne) + s.nn_mol;
+            double f = fm;
+            if (tid == 0) f += s.nHm;
+            f += ((s.nI[tid] + s.nII[tid]) + s.nIII[tid]) - s.ab[tid] * n_nuclei;
+            F = f / (s.ab[tid] * nt);
+        } else {
+            F = (((s.qn - s.nHm) + s.ion1) - s.ne) / nt;
+        }
+        s.A[CE_N * CE_LD + tid] = F;
+        bad = !isfinite(F);
+        fa = fabs(F);
+    }
+    if (__syncthreads_or(bad)) return -1;
+    inf_out = ce_block_max(s, fa);
+    if (inf_out < 1e-8 && !always_jacobian) return 1;
+    // Jacobian, dense part: the n_nuclei coupling (-d n_nuclei/dx_c / n_tot in every atom
+    // row), the atoms' own densities, the n_e column, the charge row
+    for (int idx = tid; idx < CE_NZ * CE_NZ; idx += CE_THREADS) {  // atom rows, atom columns
+        const int c = idx / CE_NZ, r = idx - c * CE_NZ;
+        if (c != r) s.A[c * CE_LD + r] = s.dNn[c];
+    }
+    for (int q = tid; q < 3 * CE_NZ + 1; q += CE_THREADS) {  // diagonal, n_e column, charge row
+        const int r = q % CE_NZ, part = q / CE_NZ;
+        if (part == 0) {
+            double w = ln10 * (((s.nI[r] + s.nII[r]) + s.nIII[r]) + s.dd[r]);
+            if (r == 0) w += ln10 * s.nHm;
+            s.A[r * CE_LD + r] = s.dNn[r] + w * s.inv_scale[r];
+        } else if (part == 1) {
+            double w = -ln10 * s.Sq[r] - ln10 * (s.nII[r] + 2 * s.nIII[r]);
+            if (r == 0) w += ln10 * s.nHm;
+            s.A[CE_NZ * CE_LD + r] = s.dNn[CE_NZ] + w * s.inv_scale[r];
+        } else if (part == 2) {
+            double v = ln10 * s.Sq[r] + ln10 * (s.nII[r] + 2 * s.nIII[r]);
+            if (r == 0) v -= ln10 * s.nHm;
+            s.A[r * CE_LD + CE_NZ] = v * inv_nt;
+        } else {
+            s.A[CE_NZ * CE_LD + CE_NZ] = (((-ln10 * s.qn) - ln10 * s.nHm) - ln10 * s.ion2 - ln10 * s.ne) * inv_nt;
+        }
+    }
+    __syncthreads();
+    // Jacobian, molecule coupling off the diagonal (the diagonal's came with the element sums):
+    // entry (Z, W) gains ln10 sum cnt_Z cnt_W n_mol / (ab_Z n_tot)
+    for (int p = tid; p < tb.n_pairs; p += CE_THREADS) {
+        const int Z = s.pair_row[p], W = s.pair_col[p];
+        double sum = 0;
+        for (int k = s.pair_ptr[p]; k < s.pair_ptr[p + 1]; ++k) sum = fma(s.pair_coefd[k], s.nmol[s.pair_mol[k]], sum);
+        s.A[W * CE_LD + Z] += ln10 * sum * s.inv_scale[Z];
+    }
+    __syncthreads();
+    return 0;
 }
 
-__global__ void __launch_bounds__(CE_THREADS) chem_eq_kernel(ChemTables tb, ChemLayersDev ly, double* __restrict__ dens,
-                                                             int32_t* __restrict__ status, double* __restrict__ info) {
-    extern __shared__ __align__(16) unsigned char ce_smem[];
-    CeShared& s = *reinterpret_cast<CeShared*>(ce_smem);
-    const int l = blockIdx.x;
-    if (l >= ly.L) return;
+// Per-layer set-up shared by the solve and its reverse mode: the molecule tables in shared
+// memory, Saha factors (saha_ion_weights with n_e = 1, src/statmech.jl:19-35, 362-372), the
+// starting guess (atoms only, n_e from the model atmosphere, :151-155, 235-237), molecular log nK
+// (get_log_nK, :60-62; polyatomics read_statmech_quantities.jl:66-89); with derivs, also the
+// derivatives of log10 wII, log10 wIII, log10 nK (molecules and H-) with respect to T.
+__device__ void ce_prologue(const ChemTables& tb, const ChemLayersDev& ly, int l, CeShared& s, bool derivs) {
     const int tid = threadIdx.x;
     const int M = tb.n_mol;
-    const int nspec = 278 + M;
     const double T = ly.T[l], nt = ly.n_tot[l], ne_g = ly.ne_model[l];
     const int a = ly.atm ? ly.atm[l] : 0;
     const double lnT = log(T);
     const double transU = ce::translational_U(ce::ME_CGS, T);
+    const double iTl = 1.0 / (T * ce::LN10);  // d log10(f) / dT = (d ln f / d ln T) / (T ln10)
     for (int i = tid; i < M * CE_MAXATOMS; i += CE_THREADS) s.m_atoms[i] = (unsigned char)tb.atoms[i];
     for (int m = tid; m < M; m += CE_THREADS) {
         s.m_charge[m] = (unsigned char)tb.charge[m];
@@ -723,6 +723,19 @@ __global__ void __launch_bounds__(CE_THREADS) chem_eq_kernel(ChemTables tb, Chem
             wIII1 = wII1 * 2.0 * r2 * transU * e2;
             wIIIg = wIIg * 2.0 / ne_g * r2 * transU * e2;
         }
+        if (derivs) {  // d ln(U) / d ln T from the splines; d/dT of T^1.5 exp(-chi/kT)
+            const double dI = ce::spline_deriv(tb.lnT, U, Uz, tb.nk, lnT) / UI;
+            const double dII = ce::spline_deriv(tb.lnT, U + tb.nk, Uz + tb.nk, tb.nk, lnT) / UII;
+            const double dw2 = (dII - dI + 1.5 + chiI / (ce::KB_EV * T)) * iTl;
+            s.dlwII[Z] = dw2;
+            if (Z > 0) {
+                const double UIII = ce::spline(tb.lnT, U + 2 * tb.nk, Uz + 2 * tb.nk, tb.nk, lnT);
+                const double dIII = ce::spline_deriv(tb.lnT, U + 2 * tb.nk, Uz + 2 * tb.nk, tb.nk, lnT) / UIII;
+                s.dlwIII[Z] = dw2 + (dIII - dII + 1.5 + chiII / (ce::KB_EV * T)) * iTl;
+            } else {
+                s.dlwIII[Z] = 0.0;
+            }
+        }
         s.rat1[Z] = r1;
         s.rat2[Z] = r2;
         s.e1[Z] = e1;
@@ -738,30 +751,86 @@ __global__ void __launch_bounds__(CE_THREADS) chem_eq_kernel(ChemTables tb, Chem
         const int64_t o = tb.off[m];
         const int n = int(tb.off[m + 1] - o);
         const int na = tb.nat[m];
-        double logK;
+        double logK, dlog = 0;  // dlog: d log10 nK / dT
         if (tb.kind[m] == 0) {
             logK = ce::spline(tb.t + o, tb.u + o, tb.z + o, n, lnT);
+            if (derivs) dlog = ce::spline_deriv(tb.t + o, tb.u + o, tb.z + o, n, lnT) / T - double(na - 1) * iTl;
         } else {
             const double Tp = exp(lnT);
-            double prodU = 1.0;
+            double prodU = 1.0, dlnU = 0;
             for (int j = 0; j < CE_MAXATOMS && tb.atoms[m * CE_MAXATOMS + j]; ++j) {
                 const int Z = tb.atoms[m * CE_MAXATOMS + j] - 1;
-                prodU *= ce::spline(tb.lnT, tb.U_u + size_t(3 * Z) * tb.nk, tb.U_z + size_t(3 * Z) * tb.nk, tb.nk, lnT);
+                const double* Ua = tb.U_u + size_t(3 * Z) * tb.nk;
+                const double* Uza = tb.U_z + size_t(3 * Z) * tb.nk;
+                const double Uv = ce::spline(tb.lnT, Ua, Uza, tb.nk, lnT);
+                prodU *= Uv;
+                if (derivs) dlnU += ce::spline_deriv(tb.lnT, Ua, Uza, tb.nk, lnT) / Uv;
             }
-            const double log_Us = log10(prodU / ce::spline(tb.t + o, tb.u + o, tb.z + o, n, lnT));
+            const double Umol = ce::spline(tb.t + o, tb.u + o, tb.z + o, n, lnT);
+            const double log_Us = log10(prodU / Umol);
+            if (derivs) {
+                dlnU -= ce::spline_deriv(tb.t + o, tb.u + o, tb.z + o, n, lnT) / Umol;
+                dlog = (double(na - 1) * 1.5 + dlnU + tb.D00[m] / (ce::KB_EV * T)) * iTl;
+            }
             const double ltU = 1.5 * log10(ce::TWO_PI * ce::KB_CGS * Tp / (ce::H_CGS * ce::H_CGS));
             const double lnK = double(na - 1) * ltU + 1.5 * tb.lmr[m] + log_Us - tb.D00[m] / (ce::KB_EV * Tp * log(10.0));
             logK = lnK + double(na - 1) * log10(ce::KB_CGS * Tp);
         }
         s.lognK[m] = logK - double(na - 1) * log10(ce::KB_CGS * T);
+        if (derivs) s.dlognK[m] = dlog;
     }
     if (tid == 0) {
         s.x0[CE_NZ] = log10(ne_g);
         s.lognK_Hm = log10(exp(ce::HMINUS_EA_EV / (ce::KB_EV * T)) / (4 * transU));
+        s.dlognK_Hm = (-ce::HMINUS_EA_EV / (ce::KB_EV * T) - 1.5) * iTl;
         s.transU = transU;
         s.lnT = lnT;
     }
     __syncthreads();
+}
+
+// One Newton solve at log xi from s.x (clipped_newton, src/newton.jl:2-35).  Every thread calls
+// it; control flow is uniform.  Returns whether |F|_inf < tol was reached; budget counts the
+// iterations left for the layer (exhausted: out_of_budget is set); fallbacks counts the steps
+// that needed the FP64 elimination.
+__device__ bool ce_newton(const ChemTables& tb, CeShared& s, double nt, double logxi, int max_iter, int& budget,
+                          bool& out_of_budget, double& last_inf, int& fallbacks) {
+    const int tid = threadIdx.x;
+    last_inf = INFINITY;
+    for (int it = 0; it < max_iter; ++it) {
+        if (budget <= 0) {
+            out_of_budget = true;
+            return false;
+        }
+        --budget;
+        double inf = last_inf;
+        const int st = ce_assemble(tb, s, nt, logxi, false, inf);
+        if (st < 0) return false;
+        last_inf = inf;
+        if (st > 0) return true;
+        bool refined = false;
+        if (!ce_solve(s, refined)) return false;
+        if (!refined) ++fallbacks;
+        // step = -(J \ F), clipped so that no unknown moves more than 1 dex
+        const double sm = ce_block_max(s, tid < CE_N ? fabs(s.sol[tid]) : 0.0);
+        const double alpha = sm > 1.0 ? 1.0 / sm : 1.0;
+        if (tid < CE_N) s.x[tid] = s.x[tid] + alpha * (-s.sol[tid]);
+        __syncthreads();
+    }
+    return false;
+}
+
+__global__ void __launch_bounds__(CE_THREADS) chem_eq_kernel(ChemTables tb, ChemLayersDev ly, double* __restrict__ dens,
+                                                             int32_t* __restrict__ status, double* __restrict__ info) {
+    extern __shared__ __align__(16) unsigned char ce_smem[];
+    CeShared& s = *reinterpret_cast<CeShared*>(ce_smem);
+    const int l = blockIdx.x;
+    if (l >= ly.L) return;
+    const int tid = threadIdx.x;
+    const int M = tb.n_mol;
+    const int nspec = 278 + M;
+    ce_prologue(tb, ly, l, s, false);
+    const double T = ly.T[l], nt = ly.n_tot[l];
     // the solve (src/statmech.jl:240-305)
     int budget = CE_MAX_ITER;
     bool oob = false;
@@ -864,6 +933,150 @@ __global__ void __launch_bounds__(CE_THREADS) chem_eq_kernel(ChemTables tb, Chem
             info[CE_NINFO * l + 3] = last_inf;
             info[CE_NINFO * l + 4] = double(fallbacks);
         }
+    }
+}
+
+// block-wide sum of one value per thread, in a fixed order (every thread gets it); two barriers
+__device__ inline double ce_block_sum(CeShared& s, double v) {
+    v = ce::warp_sum(v);
+    if ((threadIdx.x & 31) == 0) s.red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double m = 0;
+    for (int w = 0; w < CE_WARPS; ++w) m += s.red[w];
+    __syncthreads();
+    return m;
+}
+
+// s.part[i][slot] = sum over work item i's incidences of cnt * s.wmol[m] (threads < n_items)
+__device__ inline void ce_item_sums(const ChemTables& tb, CeShared& s, int slot) {
+    const int tid = threadIdx.x;
+    if (tid < tb.n_items) {
+        double acc = 0;
+        for (int k = s.item_begin[tid]; k < s.item_begin[tid + 1]; ++k) acc = fma(s.inc_cntd[k], s.wmol[s.inc_mol[k]], acc);
+        s.part[tid][slot] = acc;
+    }
+}
+
+__device__ inline double ce_elem_total(const CeShared& s, int Z, int slot) {
+    double acc = 0;
+    for (int i = s.elem_item_ptr[Z]; i < s.elem_item_ptr[Z + 1]; ++i) acc += s.part[i][slot];
+    return acc;
+}
+
+// Reverse mode of chemical_equilibrium at a solution, the implicit-function rule of the
+// reference's ForwardDiff method (src/statmech.jl:307-355): with J dx/dp = -dF/dp at F = 0, the
+// cotangents g of every output density (the layout of korg_chemical_equilibrium's densities)
+// give, per layer, dL/dp = g (dn/dp)|x - lambda (dF/dp) with J^T lambda = (dn/dx)^T g, for p =
+// T, n_tot and the (normalised) abundances.  J is the Newton step's system, solved the same way
+// (equilibrated FP32 factors, FP64 refinement), transposed.
+__global__ void __launch_bounds__(CE_THREADS) chem_vjp_kernel(ChemTables tb, ChemLayersDev ly, const double* __restrict__ dens,
+                                                              const double* __restrict__ gbar, double* __restrict__ dT,
+                                                              double* __restrict__ dnt, double* __restrict__ dab,
+                                                              int32_t* __restrict__ status) {
+    extern __shared__ __align__(16) unsigned char ce_smem[];
+    CeShared& s = *reinterpret_cast<CeShared*>(ce_smem);
+    const int l = blockIdx.x;
+    if (l >= ly.L) return;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int M = tb.n_mol;
+    const int nspec = 278 + M;
+    const double ln10 = ce::LN10;
+    ce_prologue(tb, ly, l, s, true);
+    const double nt = ly.n_tot[l];
+    const double* d = dens + size_t(l) * nspec;
+    const double* g = gbar + size_t(l) * nspec;
+    if (tid < CE_NZ) s.x[tid] = log10(d[1 + 3 * tid]);
+    if (tid == CE_NZ) s.x[CE_NZ] = log10(d[0]);
+    __syncthreads();
+    double inf = 0;
+    bool ok = ce_assemble(tb, s, nt, 0.0, true, inf) >= 0;  // densities, F and J at the solution
+    // xbar = (dn/dx)^T g; molecule weights g_m n_m
+    for (int m = tid; m < M; m += CE_THREADS) s.wmol[m] = g[278 + m] * s.nmol[m];
+    if (tid < CE_N) s.x0[tid] = s.A[CE_N * CE_LD + tid];  // keep F (column CE_N becomes xbar)
+    __syncthreads();
+    ce_item_sums(tb, s, 0);
+    if (warp == CE_WARPS - 1) {
+        double wq = 0, gi = 0;
+        for (int m = lane; m < M; m += 32) wq = fma(s.chg[m], s.wmol[m], wq);
+        for (int Z = lane; Z < CE_NZ; Z += 32) gi += g[2 + 3 * Z] * s.nII[Z] + 2 * g[3 + 3 * Z] * s.nIII[Z];
+        wq = ce::warp_sum(wq);
+        gi = ce::warp_sum(gi);
+        if (lane == 0) {
+            s.vsum[0] = wq;
+            s.vsum[1] = gi;
+        }
+    }
+    __syncthreads();
+    if (tid < CE_NZ) {
+        double xb = g[1 + 3 * tid] * s.nI[tid] + g[2 + 3 * tid] * s.nII[tid] + g[3 + 3 * tid] * s.nIII[tid] +
+                    ce_elem_total(s, tid, 0);
+        if (tid == 0) xb += g[277] * s.nHm;
+        s.A[CE_N * CE_LD + tid] = ln10 * xb;
+    } else if (tid == CE_NZ) {
+        s.A[CE_N * CE_LD + CE_NZ] = ln10 * (g[0] * s.ne - s.vsum[1] + g[277] * s.nHm - s.vsum[0]);
+    }
+    // J^T in place
+    for (int idx = tid; idx < CE_N * CE_N; idx += CE_THREADS) {
+        const int c = idx / CE_N, r = idx - c * CE_N;
+        if (r < c) {
+            const double t = s.A[c * CE_LD + r];
+            s.A[c * CE_LD + r] = s.A[r * CE_LD + c];
+            s.A[r * CE_LD + c] = t;
+        }
+    }
+    __syncthreads();
+    bool refined = false;
+    ok = ce_solve(s, refined) && ok;  // s.sol = lambda
+    // temperature sensitivities of the densities at fixed x: d n / d T = n * ln10 * d log10 n / dT
+    for (int m = tid; m < M; m += CE_THREADS) {
+        double dl = -s.dlognK[m];
+        if (s.m_charge[m]) dl += s.dlwII[s.m_atoms[m * CE_MAXATOMS] - 1];
+        s.wmol[m] = s.nmol[m] * ln10 * dl;
+    }
+    __syncthreads();
+    ce_item_sums(tb, s, 1);
+    if (warp == CE_WARPS - 1) {
+        double sn = 0, sq = 0, si = 0;
+        for (int m = lane; m < M; m += 32) {
+            sn = fma(s.natm1[m], s.wmol[m], sn);
+            sq = fma(s.chg[m], s.wmol[m], sq);
+        }
+        for (int Z = lane; Z < CE_NZ; Z += 32)
+            si += ln10 * (s.nII[Z] * s.dlwII[Z] + 2 * s.nIII[Z] * s.dlwIII[Z]);
+        sn = ce::warp_sum(sn);
+        sq = ce::warp_sum(sq);
+        si = ce::warp_sum(si);
+        if (lane == 0) {
+            s.vsum[0] = sn;
+            s.vsum[1] = sq;
+            s.vsum[2] = si;
+        }
+    }
+    __syncthreads();
+    // per-thread contributions to dL/dT and dL/dn_tot; dL/dab per element
+    double cT = 0, cN = 0;
+    const double dHm = s.nHm * ln10 * s.dlognK_Hm;
+    if (tid < CE_NZ) {
+        const double dII = s.nII[tid] * ln10 * s.dlwII[tid], dIII = s.nIII[tid] * ln10 * s.dlwIII[tid];
+        double num = ce_elem_total(s, tid, 1) + dII + dIII - s.ab[tid] * s.vsum[0];
+        if (tid == 0) num += dHm;
+        const double lam = s.sol[tid], F = s.x0[tid];
+        cT = g[2 + 3 * tid] * dII + g[3 + 3 * tid] * dIII - lam * num * s.inv_scale[tid];
+        cN = lam * (1 + F) / nt;
+        const double n_nuclei = (nt - s.ne) + s.nn_mol;
+        dab[size_t(l) * CE_NZ + tid] = lam * (n_nuclei / nt + F) / s.ab[tid];
+    } else if (tid == CE_NZ) {
+        const double lam = s.sol[CE_NZ], F = s.x0[CE_NZ];
+        cT = g[277] * dHm - lam * ((s.vsum[1] - dHm) + s.vsum[2]) / nt;
+        cN = lam * F / nt;
+    }
+    for (int m = tid; m < M; m += CE_THREADS) cT = fma(g[278 + m], s.wmol[m], cT);
+    const double sT = ce_block_sum(s, cT);
+    const double sN = ce_block_sum(s, cN);
+    if (tid == 0) {
+        dT[l] = sT;
+        dnt[l] = sN;
+        status[l] = ok ? KORG_CHEM_OK : KORG_CHEM_NONFINITE;
     }
 }
 

@@ -178,6 +178,10 @@ def lib():
             L.korg_set_equilibrium_tables.argtypes = [vp, C.POINTER(EquilibriumTables)]
             L.korg_chemical_equilibrium.argtypes = [vp, C.POINTER(ChemLayers), C.c_int32, _dp, _ip, _dp]
             L.korg_chemical_equilibrium_dev.argtypes = [vp, C.POINTER(ChemLayers), C.c_int32, vp, vp, vp, vp]
+            L.korg_chemical_equilibrium_vjp.argtypes = [vp, C.POINTER(ChemLayers), C.c_int32, _dp, _dp, _dp, _dp,
+                                                        _dp]
+            L.korg_chemical_equilibrium_vjp_dev.argtypes = [vp, C.POINTER(ChemLayers), C.c_int32, vp, vp, vp, vp, vp,
+                                                            vp, vp]
             L.korg_get_tile_config.argtypes = [vp, C.c_int32, C.c_int, _ip, _ip, _ip, _ip]
             L.korg_set_tile_config.argtypes = [vp, C.c_int32, C.c_int, C.c_int32, C.c_int32, C.c_int32]
             L.korg_device_status.argtypes = [vp]
@@ -207,7 +211,8 @@ def exported_symbols():
             "korg_selftest_wait_timeout", "korg_apply_lsf_dev", "korg_apply_lsf_vjp_dev", "korg_lsf_windows_dev",
             "korg_lsf_matrix_values_dev", "korg_apply_rotation_dev", "korg_apply_rotation_vjp_dev",
             "korg_set_continuum_tables", "korg_continuum_absorption", "korg_continuum_absorption_dev",
-            "korg_set_equilibrium_tables", "korg_chemical_equilibrium", "korg_chemical_equilibrium_dev"]
+            "korg_set_equilibrium_tables", "korg_chemical_equilibrium", "korg_chemical_equilibrium_dev",
+            "korg_chemical_equilibrium_vjp", "korg_chemical_equilibrium_vjp_dev"]
 
 
 def _p(a, kind=_dp):

@@ -187,6 +187,31 @@ def solve_layers(T, n_tot, ne_model, abundances, atm=None, tables=None, ctx=None
     return dens, status, info
 
 
+def chemical_equilibrium_vjp(T, n_tot, ne_model, abundances, densities, gbar, atm=None, tables=None, ctx=None):
+    """Reverse mode of :func:`solve_layers` at its solution ``densities`` (korg_chemical_equilibrium_vjp):
+    given ``gbar`` [L, 278 + n_mol], the cotangents of every density in the same layout, returns
+    (dL/dT [L], dL/dn_tot [L], dL/dabundances [L, 92]) per layer -- the reference differentiates
+    through its solver with ForwardDiff and the implicit-function rule (src/statmech.jl:307-355)."""
+    ctx = ctx or _lib.default_context()
+    t = ctx.ensure_equilibrium(tables)
+    keep = _lib.Keep()
+    T = keep.f64(np.atleast_1d(T))
+    L = len(T)
+    nt = keep.f64(np.broadcast_to(np.asarray(n_tot, np.float64), (L,)))
+    ne = keep.f64(np.broadcast_to(np.asarray(ne_model, np.float64), (L,)))
+    ab = keep.f64(np.atleast_2d(abundances))
+    at = None if atm is None else keep.i32(atm)
+    nspec = _lib.KORG_CHEM_MOL0 + len(t.molecules)
+    d, g = keep.f64(densities), keep.f64(gbar)
+    if d.shape != (L, nspec) or g.shape != (L, nspec):
+        raise ValueError(f"densities and gbar must be [{L}, {nspec}]")
+    dT, dnt, dab = np.empty(L), np.empty(L), np.empty((L, MAX_ATOMIC_NUMBER))
+    y = _lib.ChemLayers(L, _lib._p(T), _lib._p(nt), _lib._p(ne), _lib._p(ab), _lib._p(at, _lib._ip))
+    ctx.check(ctx.lib.korg_chemical_equilibrium_vjp(ctx.h, C.byref(y), ab.shape[0], _lib._p(d), _lib._p(g),
+                                                    _lib._p(dT), _lib._p(dnt), _lib._p(dab)))
+    return dT, dnt, dab
+
+
 def chemical_equilibrium(T, n_tot, model_atm_ne, absolute_abundances, ionization_energies=None,
                          partition_funcs=None, log_equilibrium_constants=None,
                          electron_number_density_warn_threshold=0.1,

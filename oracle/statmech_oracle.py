@@ -225,6 +225,86 @@ def solve_chemical_equilibrium(T, n_tot, absolute_abundances, neutral_fraction_g
     return x
 
 
+_T_FACTORS = {}
+
+
+def _t_factors(T, ionization_energies, partition_funcs, log_equilibrium_constants):
+    """Saha weights at n_e = 1 and log nK of every molecule at T (cached by T)."""
+    key = (float(T), id(partition_funcs), id(log_equilibrium_constants))
+    if key not in _T_FACTORS:
+        w = np.array([saha_ion_weights(T, 1.0, Z, ionization_energies, partition_funcs)
+                      for Z in range(1, MAX_ATOMIC_NUMBER + 1)])
+        lk = np.array([get_log_nK(m, T, log_equilibrium_constants) for m in log_equilibrium_constants])
+        if len(_T_FACTORS) > 64:
+            _T_FACTORS.clear()
+        _T_FACTORS[key] = (w[:, 0], w[:, 1], lk)
+    return _T_FACTORS[key]
+
+
+def densities_from_x(x, T, ionization_energies, partition_funcs, log_equilibrium_constants):
+    """The number densities chemical_equilibrium returns for the solver's unknowns x
+    (statmech.jl:160-205, the Saha weights scaled from n_e = 1): {"ne": n_e, Species: n}."""
+    species = _species_ctor(partition_funcs)
+    w2, w3, lk = _t_factors(T, ionization_energies, partition_funcs, log_equilibrium_constants)
+    ne = 10.0 ** x[-1]
+    nI = 10.0 ** np.asarray(x[:MAX_ATOMIC_NUMBER])
+    nII = w2 / ne * nI
+    nIII = w3 / ne ** 2 * nI
+    nd = {"ne": ne}
+    for Z in range(1, MAX_ATOMIC_NUMBER + 1):
+        nd[species(Z, 0)] = nI[Z - 1]
+        nd[species(Z, 1)] = nII[Z - 1]
+        nd[species(Z, 2)] = nIII[Z - 1]
+    nd[type(next(iter(partition_funcs)))([1], -1)] = Hminus_nK(T) * nI[0] * ne
+    for mol, log_nK in zip(log_equilibrium_constants, lk):
+        if mol.charge == 0:
+            s = sum(np.log10(nI[Z - 1]) for Z in mol.atoms)
+        else:
+            Z1, Z2 = mol.atoms
+            s = np.log10(nII[Z1 - 1]) + np.log10(nI[Z2 - 1])
+        nd[mol] = 10.0 ** (s - log_nK)
+    return nd
+
+
+def chemical_equilibrium_vjp(T, n_tot, absolute_abundances, x, gbar, ionization_energies, partition_funcs,
+                             log_equilibrium_constants, elements=(), rel=1e-6):
+    """Gradient of L = sum_s gbar[s] n_s(x*(p), p) with respect to p = T, n_tot and the abundances
+    of ``elements`` at the solution x* (the implicit-function rule of the reference's ForwardDiff
+    method, statmech.jl:307-355): lambda = J^-T (dn/dx)^T gbar with the restated residuals'
+    Jacobian, then dL/dp = gbar (dn/dp)|x - lambda (dF/dp)|x, the explicit derivatives at fixed x
+    by central differences (smooth functions; no solver in them).  ``gbar``: {"ne" or Species: g}."""
+    ab = np.asarray(absolute_abundances, np.float64)
+    args = (ionization_energies, partition_funcs, log_equilibrium_constants)
+    keys = list(gbar)
+    gv = np.array([gbar[k] for k in keys])
+    def dens(xx, TT):
+        d = densities_from_x(xx, TT, *args)
+        return np.array([d[k] for k in keys])
+    n = len(x)
+    dndx = np.empty((len(keys), n))
+    h = 1e-7
+    for j in range(n):
+        e = np.zeros(n)
+        e[j] = h
+        dndx[:, j] = (dens(x + e, T) - dens(x - e, T)) / (2 * h)
+    F, J = Residuals(T, n_tot, ab, *args, 0.0)(x)
+    lam = np.linalg.solve(J.T, dndx.T @ gv)
+    hT = rel * T
+    dFdT = (Residuals(T + hT, n_tot, ab, *args, 0.0)(x)[0] - Residuals(T - hT, n_tot, ab, *args, 0.0)(x)[0]) / (2 * hT)
+    dndT = (dens(x, T + hT) - dens(x, T - hT)) / (2 * hT)
+    hn = rel * n_tot
+    dFdn = (Residuals(T, n_tot + hn, ab, *args, 0.0)(x)[0] - Residuals(T, n_tot - hn, ab, *args, 0.0)(x)[0]) / (2 * hn)
+    dab = {}
+    for Z in elements:
+        ha = rel * ab[Z - 1]
+        ap, am = ab.copy(), ab.copy()
+        ap[Z - 1] += ha
+        am[Z - 1] -= ha
+        dFda = (Residuals(T, n_tot, ap, *args, 0.0)(x)[0] - Residuals(T, n_tot, am, *args, 0.0)(x)[0]) / (2 * ha)
+        dab[Z] = -lam @ dFda
+    return gv @ dndT - lam @ dFdT, -lam @ dFdn, dab
+
+
 def chemical_equilibrium(T, n_tot, model_atm_ne, absolute_abundances, ionization_energies,
                          partition_funcs, log_equilibrium_constants,
                          electron_number_density_warn_threshold=0.1,

@@ -195,3 +195,61 @@ def test_synthesize_with_device_chemistry(ctx, tabs):
             assert abs(inp.number_densities[sp][l] / o_nd[sp] - 1) <= 1e-9, s
     res = synthesize_prepared(inp, precision="fp64", ctx=ctx)
     assert np.all(np.isfinite(res.flux)) and np.all(res.flux > 0)
+
+
+def _cotangent(dens_row, nt, seed):
+    """Random cotangent r_s / n_s on the species above 1e-30 n_tot (each weighs O(1))."""
+    rng = np.random.default_rng(seed)
+    r = rng.normal(size=dens_row.shape)
+    return np.where(dens_row > 1e-30 * nt, r / np.maximum(dens_row, 1e-300), 0.0)
+
+
+@pytest.mark.parametrize("which,layers", [("sun", (0, 20, 40, 55)), ("M dwarf", (10,)),
+                                          ("cool metal-poor dwarf", (25,))])
+def test_vjp_matches_restatement(ctx, tabs, which, layers):
+    """Reverse mode (korg_chemical_equilibrium_vjp) against the restatement's implicit-function
+    gradient at the device's solution (tests/test_statmech_oracle.py pins that gradient against
+    differences of the whole solve): dL/dT, dL/dn_tot and dL/d(abundance) of H, C, O and Fe."""
+    import statmech_oracle as so
+    from korg_gb300.statmech import chemical_equilibrium_vjp, default_equilibrium_tables, solve_layers
+    chi, pf, K = tabs
+    atms = {a[0]: a for a in cc.marcs_atmospheres() + cc.representative_atmospheres()}
+    _, T, nt, ne, ab = atms[which]
+    dens, status, _ = solve_layers(T, nt, ne, ab, ctx=ctx)
+    g = np.stack([_cotangent(dens[l], nt[l], l) for l in range(len(T))])
+    dT, dnt, dab = chemical_equilibrium_vjp(T, nt, ne, ab, dens, g, ctx=ctx)
+    species = default_equilibrium_tables().species
+    worst = 0.0
+    for l in layers:
+        x = np.log10(np.concatenate([dens[l, 1:277:3], [dens[l, 0]]]))
+        gd = {("ne" if sp is None else sp): g[l, k] for k, sp in enumerate(species)}
+        oT, on, oab = so.chemical_equilibrium_vjp(T[l], nt[l], ab, x, gd, chi, pf, K, elements=(1, 6, 8, 26))
+        pairs = [(dT[l], oT), (dnt[l], on)] + [(dab[l, Z - 1], oab[Z]) for Z in (1, 6, 8, 26)]
+        scale = max(abs(v) for _, v in pairs)
+        for got, want in pairs:
+            err = abs(got - want) / max(abs(want), 1e-6 * scale)
+            worst = max(worst, err)
+            assert err <= 1e-6, (which, l, got, want)
+    print(f"{which}: worst rel err of the reverse mode vs the restatement {worst:.1e}")
+
+
+def test_vjp_matches_device_differences(ctx):
+    """Reverse mode against central differences of the device solve itself (every layer at once:
+    layers are independent), on the solar MARCS atmosphere."""
+    from korg_gb300.statmech import chemical_equilibrium_vjp, solve_layers
+    _, T, nt, ne, ab = cc.marcs_atmospheres()[0]
+    dens, _, _ = solve_layers(T, nt, ne, ab, ctx=ctx)
+    g = np.stack([_cotangent(dens[l], nt[l], 100 + l) for l in range(len(T))])
+    dT, dnt, _ = chemical_equilibrium_vjp(T, nt, ne, ab, dens, g, ctx=ctx)
+    loss = lambda d: np.sum(g * d, axis=1)
+    h = 1e-5
+    fT = (loss(solve_layers(T * (1 + h), nt, ne, ab, ctx=ctx)[0]) -
+          loss(solve_layers(T * (1 - h), nt, ne, ab, ctx=ctx)[0])) / (2 * h * T)
+    fn = (loss(solve_layers(T, nt * (1 + h), ne, ab, ctx=ctx)[0]) -
+          loss(solve_layers(T, nt * (1 - h), ne, ab, ctx=ctx)[0])) / (2 * h * nt)
+    eT = np.abs(dT - fT) / np.abs(fT)
+    en = np.abs(dnt - fn) / np.abs(fn)
+    print(f"device differences: median rel err T {np.median(eT):.1e} (max {eT.max():.1e}), "
+          f"n_tot {np.median(en):.1e} (max {en.max():.1e})")
+    assert np.median(eT) <= 1e-5 and np.median(en) <= 1e-5
+    assert eT.max() <= 1e-3 and en.max() <= 1e-3  # the solve stops at |F| < 1e-8, not at rounding

@@ -169,3 +169,43 @@ def test_CO_ratio_sweep(so, tabs, d):
     ne, nd = _run(so, tabs, 1500.0, 1e17, 1e9, ab)
     assert cc.check_solution(1500.0, ne, nd, 1e17, ab, so.Hminus_nK) == []
     assert cc.co_bound_ok(nd)
+
+
+def _cotangent(nd, nt, seed):
+    """Random cotangent g_s = r_s / n_s on the species above 1e-30 n_tot (every species weighs O(1))."""
+    rng = np.random.default_rng(seed)
+    return {k: (rng.normal() / v if v > 1e-30 * nt else 0.0) for k, v in nd.items()}
+
+
+def test_vjp_matches_solver_differences(so, tabs):
+    """The implicit-function gradient of L = sum g n against central differences of the whole
+    solve (what ForwardDiff through chemical_equilibrium gives in the reference,
+    test/statmech.jl:199-212), at a solar photospheric layer."""
+    chi, pf, K = tabs
+    ab = cc.absolute_abundances(cc.format_A_X())
+    T, nt, ne0 = 5000.0, 1e16, 1e12
+
+    def solve(TT, ntt, abb):  # the solve, then two plain Newton steps: x to rounding level
+        guess = np.array([1 / (1 + sum(so.saha_ion_weights(TT, ne0, Z, chi, pf))) for Z in range(1, 93)])
+        x = so.solve_chemical_equilibrium(TT, ntt, abb, guess, ne0, chi, pf, K)
+        r = so.Residuals(TT, ntt, abb, chi, pf, K, 0.0)
+        for _ in range(2):
+            F, J = r(x)
+            x = x - np.linalg.solve(J, F)
+        return x, so.densities_from_x(x, TT, chi, pf, K)
+
+    x, nd = solve(T, nt, ab)
+    g = _cotangent(nd, nt, 0)
+    loss = lambda d: sum(g[k] * d[k] for k in g)
+    dT, dnt, dab = so.chemical_equilibrium_vjp(T, nt, ab, x, g, chi, pf, K, elements=(6, 26))
+    h = 1e-5  # relative step: the Boltzmann factors' (chi / kT)^2 ~ 900 make h^2 terms ~1e-5 at 1e-4
+    fT = (loss(solve(T * (1 + h), nt, ab)[1]) - loss(solve(T * (1 - h), nt, ab)[1])) / (2 * h * T)
+    fn = (loss(solve(T, nt * (1 + h), ab)[1]) - loss(solve(T, nt * (1 - h), ab)[1])) / (2 * h * nt)
+    assert abs(dT - fT) <= 1e-5 * abs(fT), (dT, fT)
+    assert abs(dnt - fn) <= 1e-5 * abs(fn), (dnt, fn)
+    for Z in (6, 26):
+        ap, am = ab.copy(), ab.copy()
+        ap[Z - 1] *= 1 + h
+        am[Z - 1] *= 1 - h
+        fa = (loss(solve(T, nt, ap)[1]) - loss(solve(T, nt, am)[1])) / (2 * h * ab[Z - 1])
+        assert abs(dab[Z] - fa) <= 1e-5 * abs(fa), (Z, dab[Z], fa)
