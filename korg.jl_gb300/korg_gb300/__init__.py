@@ -17,7 +17,7 @@ __all__ = ["Wavelengths", "LineList", "make_line", "filter_linelist", "alpha_500
 
 _API = ("line_absorption_", "hydrogen_line_absorption_", "radiative_transfer", "synthesize", "prepare_synthesis",
         "synthesize_prepared", "SynthesisInputs", "SynthesisResult", "ContinuumInterpolant", "synthesize_vjp",
-        "loss_and_gradient", "physical_gradient")
+        "loss_and_gradient", "physical_gradient", "atmosphere_gradient")
 
 
 _STATMECH = ("chemical_equilibrium", "saha_ion_weights", "translational_U", "get_log_nK", "Hminus_nK",

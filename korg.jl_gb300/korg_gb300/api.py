@@ -233,6 +233,9 @@ class SynthesisInputs:
     hydrogen_window: float = 150e-8
     cutoff_threshold: float = 3e-4
     number_densities: dict = field(default_factory=dict)
+    # what the chemical equilibrium was solved from (chemistry="gpu"): n_tot, the model n_e and the
+    # normalised abundances, per layer / per element; None otherwise
+    chemistry: tuple | None = None
 
     def struct(self, keep):
         L = len(self.T)
@@ -359,7 +362,10 @@ def prepare_synthesis(atm, linelist: LineList, A_X, wavelengths, vmic=1.0, line_
         UH_I=pf[H1](np.log(T)), alpha_ref_cntm=aref, cntm_knots=cntm_wls.all_wls, cntm_vals=vals,
         ref_wl=atm.reference_wavelength, hydrogen_lines=hydrogen_lines, use_MHD=bool(use_MHD),
         hydrogen_window=hydrogen_line_window_size * 1e-8, cutoff_threshold=line_cutoff_threshold,
-        number_densities=nd)
+        number_densities=nd,
+        chemistry=(np.asarray(atm.n_tot, np.float64), np.asarray(atm.ne, np.float64),
+                   10.0 ** (np.asarray(A_X, np.float64) - 12) / np.sum(10.0 ** (np.asarray(A_X, np.float64) - 12)))
+        if chemical_equilibrium is None and chemistry == "gpu" else None)
 
 
 def synthesize_prepared(inp: SynthesisInputs, precision="mixed", return_alpha=False, ctx=None) -> SynthesisResult:
@@ -441,6 +447,52 @@ def loss_and_gradient(inp: SynthesisInputs, obs, precision="fp64", hydrogen=True
     loss, dF, dC = rectified_loss(res.flux, res.cntm, obs)
     return loss, synthesize_vjp(inp, dF, dC, precision=precision, hydrogen=hydrogen, reuse_forward=reuse_forward,
                                 ctx=ctx)
+
+
+def atmosphere_gradient(inp: SynthesisInputs, g, ctx=None):
+    """Gradient of a synthesis loss with respect to the model atmosphere's layer temperatures and
+    total number densities and the abundances A(X), through Korg's continuum absorption and chemical
+    equilibrium as prepare_synthesis(chemistry="gpu", continuum="gpu") evaluated them: what
+    ForwardDiff through synthesize gives for those inputs (src/Fit/fit_via_synthesis.jl:345-355).
+    ``g`` is the hot-path gradient (:func:`synthesize_vjp`).  The chain: the hot path's own
+    dependences (:func:`physical_gradient`), the continuum's (central differences of the device
+    kernel, :func:`korg_gb300.continuum.absorption_vjp`), then the chemical equilibrium's
+    (implicit-function rule on the device, korg_chemical_equilibrium_vjp); A(X) enters through the
+    normalised abundances 10^(A(X) - 12) / sum.  Returns {"T", "n_tot", "A_X", "vmic", "log_gf"}."""
+    from .continuum import absorption_vjp, layer_inputs, layer_inputs_vjp
+    from .statmech import chemical_equilibrium_vjp, default_equilibrium_tables
+    if inp.chemistry is None:
+        raise ValueError('needs inputs prepared with chemistry="gpu"')
+    n_tot, ne_model, ab = inp.chemistry
+    pf = default_partition_funcs()
+    T = inp.T
+    L = len(T)
+    phys = physical_gradient(inp, g)
+    dT, dne, dn = phys["T"].copy(), np.array(phys["ne"], np.float64), dict(phys["n"])
+    d = layer_inputs(T, inp.ne, inp.number_densities, pf)
+    gk = absorption_vjp(inp.cntm_knots, d, g["cntm_vals"], ctx)
+    gr = absorption_vjp(np.array([inp.ref_wl]), d, np.asarray(g["alpha_ref_cntm"])[:, None], ctx)
+    cT, cne, cn = layer_inputs_vjp({k: gk[k] + gr[k] for k in gk}, T, inp.number_densities, pf)
+    dT += cT
+    dne += cne
+    for s, v in cn.items():
+        dn[s] = dn.get(s, 0.0) + v
+    species = default_equilibrium_tables().species
+    col = {s: k for k, s in enumerate(species) if s is not None}
+    dens = np.empty((L, len(species)))
+    dens[:, 0] = inp.ne
+    for s, k in col.items():
+        dens[:, k] = np.broadcast_to(np.asarray(inp.number_densities[s], np.float64), (L,))
+    gbar = np.zeros_like(dens)
+    gbar[:, 0] = dne
+    for s, v in dn.items():
+        if s in col:  # species outside the chemical equilibrium have no density to differentiate
+            gbar[:, col[s]] += v
+    chT, dnt, dab = chemical_equilibrium_vjp(T, n_tot, ne_model, ab, dens, gbar, ctx=ctx)
+    dT += chT
+    tot = dab.sum(axis=0)
+    dA = np.log(10.0) * ab * (tot - np.dot(ab, tot))
+    return {"T": dT, "n_tot": dnt, "A_X": dA, "vmic": phys["vmic"], "log_gf": phys["log_gf"]}
 
 
 def physical_gradient(inp: SynthesisInputs, g, vmic_scalar=True):

@@ -73,17 +73,78 @@ def _layers_struct(d, keep):
                                 (_lib._dp * 4)(*[f("n_" + s.replace(" ", "")) for s in _PEACH]))
 
 
-def continuum_absorption(wls_cm, T, ne, number_densities, partition_funcs=None, ctx=None):
-    """Continuum absorption (cm^-1) of every layer at every wavelength (cm): array (L, nwl)."""
+def absorption_from_inputs(wls_cm, d, ctx=None):
+    """korg_continuum_absorption for the per-layer inputs of :func:`layer_inputs`: array (L, nwl)."""
     ctx = ctx or _lib.default_context()
     ctx.ensure_continuum()
     keep = _lib.Keep()
-    d = layer_inputs(T, ne, number_densities, partition_funcs)
     w = keep.f64(np.atleast_1d(wls_cm))
     out = np.empty((len(d["T"]), len(w)))
     ctx.check(ctx.lib.korg_continuum_absorption(ctx.h, _lib._p(w), len(w), C.byref(_layers_struct(d, keep)),
                                                 _lib._p(out)))
     return out
+
+
+def continuum_absorption(wls_cm, T, ne, number_densities, partition_funcs=None, ctx=None):
+    """Continuum absorption (cm^-1) of every layer at every wavelength (cm): array (L, nwl)."""
+    return absorption_from_inputs(wls_cm, layer_inputs(T, ne, number_densities, partition_funcs), ctx)
+
+
+INPUTS = ("T", "ne", "nH_I", "nH_II", "nHe_I", "nH2", "nH_minus", "invU_H_I", "invU_He_I", "n_Z1", "n_Z2",
+          "n_HeII", "n_CII", "n_SiII", "n_MgII")
+
+
+def absorption_vjp(wls_cm, d, gbar, ctx=None, rel=1e-6):
+    """Reverse mode of :func:`absorption_from_inputs`: {input: dL/dinput [L]} for L = sum gbar *
+    alpha, by central differences of the FP64 device kernel, every layer's input perturbed at once
+    (the layers are independent).  The terms are linear in the densities (the step is exact there)
+    and piecewise-smooth in T (table interpolation), so a relative step of 1e-6 leaves ~1e-10 of
+    truncation and rounding; an input that is zero takes an absolute step of 1."""
+    gbar = np.asarray(gbar, np.float64)
+    out = {}
+    for k in INPUTS:
+        v = d[k]
+        h = np.where(v != 0, rel * np.abs(v), 1.0)
+        dp, dm = dict(d), dict(d)
+        dp[k], dm[k] = v + h, v - h
+        diff = absorption_from_inputs(wls_cm, dp, ctx) - absorption_from_inputs(wls_cm, dm, ctx)
+        out[k] = np.sum(gbar * diff, axis=1) / (2 * h)
+    return out
+
+
+def layer_inputs_vjp(grads, T, number_densities, partition_funcs=None):
+    """Chain the continuum inputs' gradients (:func:`absorption_vjp`) back to the layer
+    temperatures, n_e and the number density of each species (the map of :func:`layer_inputs`):
+    returns (dT [L], dne [L], {Species: dn [L]})."""
+    from .data import default_partition_funcs
+    pf = partition_funcs or default_partition_funcs()
+    T = np.atleast_1d(np.asarray(T, np.float64))
+    lnT = np.log(T)
+    dn = {}
+    add = lambda s, v: dn.__setitem__(s, dn.get(s, 0.0) + v)
+    add(parse_species("H I"), grads["nH_I"])
+    add(parse_species("H II"), grads["nH_II"])
+    add(parse_species("He I"), grads["nHe_I"])
+    add(parse_species("H2"), grads["nH2"])
+    Hminus = Species([1], -1)
+    if Hminus not in number_densities:  # Korg's chemical equilibrium always provides it
+        raise NotImplementedError("the continuum reverse mode needs n(H-) among the number densities")
+    add(Hminus, grads["nH_minus"])
+    dT = grads["T"].copy()
+    for k, s in (("invU_H_I", "H I"), ("invU_He_I", "He I")):
+        U = pf[parse_species(s)](lnT)
+        dT += grads[k] * (-pf[parse_species(s)].derivative(lnT) / T) / U ** 2
+    peach = {parse_species(s): "n_" + s.replace(" ", "") for s in _PEACH}
+    for spec in number_densities:
+        if spec.charge <= 0:
+            continue
+        if spec in peach:
+            add(spec, grads[peach[spec]])
+        elif spec.charge == 1:
+            add(spec, grads["n_Z1"])
+        elif spec.charge == 2:
+            add(spec, grads["n_Z2"])
+    return dT, grads["ne"].copy(), dn
 
 
 def total_continuum_absorption(nus, T, ne, number_densities, partition_funcs=None, ctx=None):

@@ -253,3 +253,101 @@ def test_vjp_matches_device_differences(ctx):
           f"n_tot {np.median(en):.1e} (max {en.max():.1e})")
     assert np.median(eT) <= 1e-5 and np.median(en) <= 1e-5
     assert eT.max() <= 1e-3 and en.max() <= 1e-3  # the solve stops at |F| < 1e-8, not at rounding
+
+
+def test_atmosphere_gradient_matches_differences(ctx):
+    """The loss gradient with respect to A(X), layer T and n_tot through the hot path, the device
+    continuum and the device chemical equilibrium (atmosphere_gradient) against central
+    differences of the whole pipeline: prepare_synthesis(chemistry="gpu", continuum="gpu"), the
+    FP64 synthesis and the rectified-flux loss."""
+    import copy
+    from korg_gb300 import standin, synthetic
+    from korg_gb300.api import atmosphere_gradient, prepare_synthesis, synthesize_prepared, synthesize_vjp
+    ctx.ensure_stark()
+    atm, A_X = standin.synthetic_atmosphere(5000.0, 4.0, 0.0)
+    ll = synthetic.synthetic_linelist(400, 5001.0, 5029.0, seed=11)
+
+    import statmech_oracle as so
+    from korg_gb300 import data
+    from korg_gb300.statmech import chemical_equilibrium as device_chemistry
+    tabs = data.ionization_energies(), data.default_partition_funcs(), data.default_log_equilibrium_constants()
+
+    def polished(T, n_tot, ne_model, ab):
+        """The device solve, then two Newton steps of the restatement per layer: the differences of
+        the pipeline then see the root to rounding, not the solver's 1e-8 residual tolerance."""
+        ne, nd = device_chemistry(T, n_tot, ne_model, ab, ctx=ctx)
+        keys = [k for k in nd if k.charge == 0 and len(k.atoms) == 1]
+        out = {k: np.empty(len(T)) for k in nd}
+        out_ne = np.empty(len(T))
+        for l in range(len(T)):
+            x = np.log10(np.array([nd[so._species_ctor(tabs[1])(Z, 0)][l] for Z in range(1, 93)] + [ne[l]]))
+            r = so.Residuals(T[l], n_tot[l], ab, *tabs, 0.0)
+            for _ in range(2):
+                F, J = r(x)
+                x = x - np.linalg.solve(J, F)
+            d = so.densities_from_x(x, T[l], *tabs)
+            out_ne[l] = d["ne"]
+            for k in out:
+                out[k][l] = d[k]
+        assert keys
+        return out_ne, out
+
+    def prep(a, A, chemistry="gpu"):
+        # cutoff 1e-12 and 1000 A hydrogen windows: every line window spans the grid, so no window
+        # edge (a step in the loss, not part of its derivative) moves under the perturbations;
+        # the hydrogen lines' centres shift with n_e, and H beta's 150 A window ends at 5011 A
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            return prepare_synthesis(a, ll, A, (5000, 5030), chemistry=chemistry, continuum="gpu",
+                                     line_cutoff_threshold=1e-12, hydrogen_line_window_size=1000, ctx=ctx)
+
+    inp = prep(atm, A_X)
+    base = synthesize_prepared(inp, precision="fp64", ctx=ctx)
+    obs = base.flux / base.cntm * (1 + np.random.default_rng(3).normal(0, 0.01, len(base.flux)))
+
+    def terms_at(a, A):
+        """The loss's per-wavelength terms (flux/cntm - obs)^2."""
+        r = synthesize_prepared(prep(a, A, polished), precision="fp64", ctx=ctx)
+        return (r.flux / r.cntm - obs) ** 2
+
+    def differences(at):
+        """Per-wavelength central differences of the loss terms at steps h and h/2 (``at(s)`` gives
+        the terms at s steps of h)."""
+        tp, tm, hp, hm = at(1.0), at(-1.0), at(0.5), at(-0.5)
+        return (tp - tm) / 2, hp - hm
+
+    perturbations = []
+    for Z in (1, 2, 6, 26):  # H, He, C, Fe
+        def at(s, Z=Z, h=1e-4):
+            A = A_X.copy()
+            A[Z - 1] += s * h
+            return terms_at(atm, A)
+        perturbations.append((f"A({Z})", ("A_X", Z - 1), 1e-4, differences(at)))
+    for field, l in (("T", 15), ("T", 35), ("n_tot", 30)):
+        h = 1e-5 * getattr(atm, field)[l]
+        def at(s, field=field, l=l, h=h):
+            a = copy.deepcopy(atm)
+            getattr(a, field)[l] += s * h
+            return terms_at(a, A_X)
+        perturbations.append((f"{field}[{l}]", (field, l), h, differences(at)))
+
+    # Korg's E2(x) (RadiativeTransfer.jl:408-497) is piecewise and jumps at its segment ends (by 1%
+    # at x = 1.1), so the flux steps where a layer's optical depth crosses one: a step inside the
+    # difference interval shows as disagreement between the h and h/2 differences of that
+    # wavelength's term (a smooth term's differ by O(h^2)).  Those wavelengths get weight 0 in the
+    # loss and in its gradient.
+    keep = np.ones(len(obs), bool)
+    for _, _, _, (d1, d2) in perturbations:
+        keep &= np.abs(d1 - d2) <= 1e-3 * np.abs(d2) + 1e-9 * np.max(np.abs(d2))
+    print(f"{np.count_nonzero(~keep)} of {len(keep)} wavelengths step within a difference interval")
+    assert np.count_nonzero(keep) >= 0.95 * len(keep)
+    w = keep * 2 * (base.flux / base.cntm - obs)
+    dF, dC = w / base.cntm, -w * base.flux / base.cntm ** 2
+    ag = atmosphere_gradient(inp, synthesize_vjp(inp, dF, dC, precision="fp64", ctx=ctx), ctx=ctx)
+
+    checks = [(name, ag[key][i], np.sum(keep * d1) / h) for name, (key, i), h, (d1, _) in perturbations]
+    scale = max(abs(fd) for _, _, fd in checks)
+    for name, ad, fd in checks:
+        print(f"{name}: adjoint {ad:.6e}, differences {fd:.6e}")
+    for name, ad, fd in checks:
+        assert abs(ad - fd) <= 1e-4 * abs(fd) + 1e-7 * scale, (name, ad, fd)
