@@ -220,9 +220,21 @@ def chemistry_measure(ctx, torch, dev, threads, n_stars=16, steps=3, warmup=1, c
 
     ms_all = timed(lambda: run(0, L, tatm.data_ptr()))
     st, inf, got = status.cpu().numpy(), info.cpu().numpy(), dens.cpu().numpy()
+    # reverse mode at the solution: every density carries a cotangent
+    gbar = torch.randn((L, nspec), dtype=torch.float64, device=dev, generator=torch.Generator(dev).manual_seed(5))
+    dT, dnt = torch.empty(L, dtype=torch.float64, device=dev), torch.empty(L, dtype=torch.float64, device=dev)
+    dab = torch.empty((L, 92), dtype=torch.float64, device=dev)
+    vstatus = torch.empty(L, dtype=torch.int32, device=dev)
+    yv = _lib.ChemLayers(L, dp(tT), dp(tnt), dp(tne), dp(tab_), C.cast(tatm.data_ptr(), _lib._ip))
+
+    def vjp():
+        ctx.check(ctx.lib.korg_chemical_equilibrium_vjp_dev(ctx.h, C.byref(yv), len(atms), dp(dens), dp(gbar), dp(dT),
+                                                            dp(dnt), dp(dab), vstatus.data_ptr(), stream.cuda_stream))
+    ms_vjp = timed(vjp)
+    vjp_ok = int((vstatus == 0).sum().item())
     if n_stars == 1:
         return {"layers": L, "ms": ms_all, "layers_per_s": L / (ms_all * 1e-3), "status_ok": int((st == 0).sum()),
-                "newton_iterations": float(inf[:, 0].sum())}
+                "newton_iterations": float(inf[:, 0].sum()), "vjp_ms": ms_vjp, "vjp_status_ok": vjp_ok}
     k10 = 10 * 56  # the 5777 K star, the headline's atmosphere: what one synthesize pays
     ms_one = timed(lambda: run(k10, k10 + 56, 0), reps=5)
     with warnings.catch_warnings():
@@ -233,7 +245,7 @@ def chemistry_measure(ctx, torch, dev, threads, n_stars=16, steps=3, warmup=1, c
     if not cpu:
         return {"layers": L, "ms": ms_all, "layers_per_s": L / (ms_all * 1e-3), "one_atmosphere_ms": ms_one,
                 "e2e_layers_per_s": L / e2e_s, "status_ok": int((st == 0).sum()), "newton_iterations": float(inf[:, 0].sum()),
-                "fp64_fallback_steps": float(inf[:, 4].sum())}
+                "fp64_fallback_steps": float(inf[:, 4].sum()), "vjp_ms": ms_vjp, "vjp_status_ok": vjp_ok}
     # FP64 CPU restatement on every 8th layer (spawn pool, all host cores)
     sample = np.arange(0, L, 8)
     t1 = time.perf_counter()
@@ -252,6 +264,7 @@ def chemistry_measure(ctx, torch, dev, threads, n_stars=16, steps=3, warmup=1, c
             "layers": L, "ms": ms_all, "layers_per_s": L / (ms_all * 1e-3),
             "one_atmosphere_ms": ms_one, "one_atmosphere": "the 5777 K, log g 4.44 star (56 layers)",
             "e2e_layers_per_s": L / e2e_s, "e2e": "host-pointer korg_chemical_equilibrium (H2D, solve, D2H)",
+            "vjp_ms": ms_vjp, "vjp_layers_per_s": L / (ms_vjp * 1e-3), "vjp_status_ok": vjp_ok,
             "status_ok": int((st == 0).sum()), "newton_iterations": iters,
             "us_per_newton_iteration_per_layer": ms_all * 1e3 / iters * min(L, 152),
             "fp64_fallback_steps": float(inf[:, 4].sum()), "max_solves_per_layer": float(inf[:, 1].max()),

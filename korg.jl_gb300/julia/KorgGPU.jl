@@ -302,6 +302,52 @@ function chemical_equilibrium(temps, nₜs, nₑs, absolute_abundances; molecule
     dens[1, :], nd
 end
 
+# (nₑ, Dict species => per-layer values) <-> the [278 + n_mol, L] layout of the C ABI's densities
+function _pack_densities(ne, nd, molecules, L)
+    out = zeros(Float64, 278 + length(molecules), L)
+    out[1, :] .= ne
+    for Z in 1:92, q in 0:2
+        v = get(nd, Korg.Species(Korg.Formula(Z), q), nothing)
+        v === nothing || (out[2 + 3(Z - 1) + q, :] .= v)
+    end
+    v = get(nd, Korg.species"H-", nothing)
+    v === nothing || (out[278, :] .= v)
+    for (m, mol) in enumerate(molecules)
+        v = get(nd, mol, nothing)
+        v === nothing || (out[278 + m, :] .= v)
+    end
+    out
+end
+
+"""
+    chemical_equilibrium_vjp(temps, nₜs, nₑs, absolute_abundances, (nₑ, nd), (n̄ₑ, n̄d); ctx, molecules)
+
+Reverse mode of [`chemical_equilibrium`](@ref) at its solution `(nₑ, nd)`: given cotangents of
+the electron density and of each species' densities (a Dict; absent species count as zero),
+returns `(T̄, n̄ₜ, āb)`: per-layer dL/dT, dL/dnₜ, and dL/d(absolute abundance) as a 92 × L
+matrix.  This is what ForwardDiff computes through the implicit-function method of
+`solve_chemical_equilibrium` (src/statmech.jl:307-355).
+"""
+function chemical_equilibrium_vjp(temps, nₜs, nₑs, absolute_abundances, solution, cotangents;
+                                  molecules, ctx::Context=default_context())
+    L = length(temps)
+    T, nt, ne = collect(Float64, temps), collect(Float64, nₜs), collect(Float64, nₑs)
+    ab = collect(Float64, absolute_abundances)
+    dens = _pack_densities(solution[1], solution[2], molecules, L)
+    gbar = _pack_densities(cotangents[1], cotangents[2], molecules, L)
+    dT, dnt, dab = Vector{Float64}(undef, L), Vector{Float64}(undef, L), Matrix{Float64}(undef, 92, L)
+    rc = GC.@preserve T nt ne ab begin
+        lay = Ref(CChemLayers(L, pointer(T), pointer(nt), pointer(ne), pointer(ab), C_NULL))
+        ccall((:korg_chemical_equilibrium_vjp, LIB), Cint,
+              (Ptr{Cvoid}, Ref{CChemLayers}, Int32, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+               Ptr{Float64}),
+              ctx.ptr, lay, 1, dens, gbar, dT, dnt, dab)
+    end
+    rc == KORG_ECHEM && throw(Korg.ChemicalEquilibriumError("singular system in the reverse mode"))
+    check(ctx, rc)
+    dT, dnt, dab
+end
+
 # ---------------------------------------------------------------------------- differentiable path
 # korg_synth_inputs / korg_synth_grads of include/korg_gb300.h
 struct CSynthInputs

@@ -103,6 +103,17 @@ def test_header_symbols_exported():
     ctypes.CDLL(_lib.LIB_PATH)  # loads without a GPU
 
 
+def test_julia_binding_symbols_declared():
+    """Every entry point the Julia binding ccalls is declared in include/korg_gb300.h (Julia is
+    not in this image, so the binding is checked by its text)."""
+    hdr = open(os.path.join(ROOT, "include", "korg_gb300.h")).read()
+    declared = set(re.findall(r"KORG_API\s+[\w\s\*]+?\b(korg_\w+)\s*\(", hdr))
+    jl = open(os.path.join(ROOT, "korg.jl_gb300", "julia", "KorgGPU.jl")).read()
+    called = set(re.findall(r"ccall\(\(:(korg_\w+)\s*,", jl))
+    assert {"korg_chemical_equilibrium", "korg_chemical_equilibrium_vjp", "korg_synthesize_vjp"} <= called
+    assert called <= declared, called - declared
+
+
 def test_no_oracle_in_product():
     """The product package never imports or links the oracle."""
     pkg = os.path.join(ROOT, "korg.jl_gb300")
