@@ -1184,7 +1184,7 @@ def run_adjoint(args):
     g32, g64 = res["mixed"][2], res["fp64"][2]
     reuse_same = all(np.allclose(g_reuse[k], g32[k], rtol=1e-6, atol=0) for k in g32)
     agree = {k: float(np.max(np.abs(g32[k] - g64[k])) / max(np.max(np.abs(g64[k])), 1e-300))
-             for k in ("T", "ne", "n_eff_vdW", "xi", "n_div_U", "log_gf")}
+             for k in ("T", "ne", "n_eff_vdW", "xi", "n_div_U", "log_gf", "nH_I", "UH_I")}
     t_fwd, t_step = res["mixed"][0], res["mixed"][1]
     out = {"metric": METRIC, "value": 1000.0 / t_step, "unit": "gradient steps/s (forward + loss + VJP)",
            "n_gpus": 1, "steps": args.steps, "warmup": 1, "ms_per_step": t_step, "higher_is_better": True,

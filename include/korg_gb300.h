@@ -342,9 +342,9 @@ KORG_API int korg_synthesize_dev(korg_ctx *ctx, const korg_synth_inputs *in,
  * equilibrium, partition functions and continuum (T -> n, U, alpha_cntm) is the caller's.
  * alpha is recomputed (not stored by the forward call); the line windows carry no derivative,
  * as under ForwardDiff.  With KORG_VJP_HYDROGEN the hydrogen-line opacity contributes too,
- * through forward differences of the FP64 hydrogen kernel (its Jacobian is layer diagonal;
- * the U(H I) and, without MHD, n(H I) derivatives are exact);
- * without it, hydrogen lines are held fixed. */
+ * with the exact derivatives of its approximation (layer diagonal; forward-mode dual numbers
+ * through the line records, the Stehle table interpolation, the ABO Voigt profiles and the
+ * Brackett profiles); without it, hydrogen lines are held fixed. */
 typedef struct {
     double *T, *ne, *n_eff_vdW, *xi;
     double *n_div_U;
@@ -354,8 +354,8 @@ typedef struct {
     double *alpha_ref_cntm;
 } korg_synth_grads;
 /* KORG_VJP_REUSE_FORWARD: the previous call on this context was korg_synthesize[_dev] with the
- * same inputs; its alpha (kept in the context when alpha_out was NULL), alpha_ref and line
- * prologue are reused instead of recomputed. */
+ * same inputs; its alpha (kept in the context when alpha_out was NULL), alpha_ref, line prologue
+ * and hydrogen-line records are reused instead of recomputed. */
 enum { KORG_VJP_HYDROGEN = 1, KORG_VJP_REUSE_FORWARD = 2 };
 KORG_API int korg_synthesize_vjp(korg_ctx *ctx, const korg_synth_inputs *in, const korg_lines *lines,
                                  const korg_lines *lines5, const double *wls, int64_t nwl,

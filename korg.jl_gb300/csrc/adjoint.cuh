@@ -1096,26 +1096,4 @@ __global__ void __launch_bounds__(256) line_adj_prologue_kernel(LinesDev ln, Lay
     }
 }
 
-// Hydrogen-line opacity is layer-local (each layer's row depends on that layer's T, n_e,
-// n(H I), n(He I), U(H I), xi only), so its Jacobian is block diagonal: per layer and input,
-// d alpha_H[l, :]/dp_l is a central difference of two FP64 evaluations with every layer
-// perturbed at once, and the cotangent is its contraction with G.
-__global__ void hydro_fd_contract_kernel(const void* G, int32_t g32, const double* ap, const double* am,
-                                         const double* h, int64_t nwl, int32_t L, double* out) {
-    __shared__ double s_acc[RTA_LMAX];
-    for (int l = threadIdx.x; l < L; l += blockDim.x) s_acc[l] = 0.0;
-    __syncthreads();
-    const int64_t n = nwl * L;
-    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < n; e += int64_t(gridDim.x) * blockDim.x) {
-        const double d = ap[e] - am[e];
-        if (d == 0.0) continue;
-        const int l = int(e % L);
-        const double g = g32 ? double(static_cast<const float*>(G)[e]) : static_cast<const double*>(G)[e];
-        atomicAdd(s_acc + l, g * d);
-    }
-    __syncthreads();
-    for (int l = threadIdx.x; l < L; l += blockDim.x)
-        if (s_acc[l] != 0.0) atomicAdd(out + l, s_acc[l] / (2 * h[l]));
-}
-
 }  // namespace korg

@@ -20,6 +20,7 @@
 #include "adjoint.cuh"
 #include "continuum.cuh"
 #include "hydrogen.cuh"
+#include "hydrogen_adj.cuh"
 #include "lines.cuh"
 #include "postprocess.cuh"
 #include "physics.cuh"
@@ -58,7 +59,7 @@ struct korg_ctx {
     DevBuf lines_scratch, counters, tune_alpha;
     DevBuf hrec, hQ, hQ32, hulb, huub;
     DevBuf stage_dev, aref, alpha, flux, cntm, math;
-    DevBuf vjp_g, vjp_dpar, vjp_small, vjp_hfd;  // reverse mode
+    DevBuf vjp_g, vjp_dpar, vjp_small, vjp_hder, vjp_hdq;  // reverse mode
     DevBuf mx_layers;                            // molecular cross-section layer inputs
     void* stage_host = nullptr;
     size_t stage_host_cap = 0;
@@ -100,6 +101,8 @@ struct korg_ctx {
     StarkDev stark{};
     int n_max = 0;
     std::vector<void*> stark_allocs;
+    // the hydrogen prep records and tables now in hrec / hQ: -1 none, 0 FP64, 1 mixed (FP64 and FP32)
+    int hyd_prep = -1;
     // statistics
     bool timing = false;
     cudaEvent_t ev[NEV] = {};
@@ -456,14 +459,11 @@ int run_line_absorption(korg_ctx* ctx, double* alpha, const double* wls, int64_t
 }
 
 // ------------------------------------------------------------------ hydrogen lines
-int run_hydrogen(korg_ctx* ctx, double* alpha, const double* wls, int64_t nwl, const HLayers& hl, double window,
-                 int use_MHD, bool mixed, cudaStream_t s) {
+// The per-(transition, layer) records and profile tables of the hydrogen lines (the prep kernels).
+int run_hydrogen_prep(korg_ctx* ctx, const double* wls, int64_t nwl, const HLayers& hl, double window, int use_MHD,
+                      bool mixed, cudaStream_t s, HOut* out) {
     if (!ctx->have_stark) return set_err(ctx, KORG_ENOTABLES, "korg_set_stark_tables() has not been called");
     const int L = hl.L;
-    // the hydrogen tile kernel interleaves layers: thread group g owns layers g, g+G, ...
-    int kmax = 16, G = (L + 15) / 16;
-    if (G > 8) { kmax = 32; G = (L + 31) / 32; }
-    if (G > 8) return set_err(ctx, KORG_EINVAL, "at most 256 layers are supported (got %d)", L);
     const int ntrans = ctx->stark.ntrans;
     const int nbr = std::max(0, ctx->n_max - 4);
     const int ntot = ntrans + nbr;
@@ -490,6 +490,22 @@ int run_hydrogen(korg_ctx* ctx, double* alpha, const double* wls, int64_t nwl, c
             brackett_prep_kernel<false><<<dim3(nbr, L), 256, 0, s>>>(hl, ntrans, ctx->n_max, wls, nwl, use_MHD, ho, brQ);
         KCUDA(cudaGetLastError());
     }
+    ctx->hyd_prep = mixed ? 1 : 0;
+    *out = ho;
+    return KORG_OK;
+}
+
+int run_hydrogen(korg_ctx* ctx, double* alpha, const double* wls, int64_t nwl, const HLayers& hl, double window,
+                 int use_MHD, bool mixed, cudaStream_t s) {
+    const int L = hl.L;
+    // the hydrogen tile kernel interleaves layers: thread group g owns layers g, g+G, ...
+    int kmax = 16, G = (L + 15) / 16;
+    if (G > 8) { kmax = 32; G = (L + 31) / 32; }
+    if (G > 8) return set_err(ctx, KORG_EINVAL, "at most 256 layers are supported (got %d)", L);
+    HOut ho;
+    KCHECK(run_hydrogen_prep(ctx, wls, nwl, hl, window, use_MHD, mixed, s, &ho));
+    const int ntrans = ctx->stark.ntrans;
+    const int ntot = ntrans + std::max(0, ctx->n_max - 4);
     HTileArgs ha{};
     ha.alpha = alpha;
     ha.wls = wls;
@@ -747,30 +763,6 @@ __global__ void to_float_kernel(const double* x, int64_t n, float* y) {
     if (i < n) y[i] = float(x[i]);
 }
 
-// h[l] = sign * x[l] / 2 (hydro_fd_contract_kernel then divides by 2 h = sign * x)
-__global__ void hfd_half_kernel(const double* x, int L, double sign, double* h) {
-    const int l = blockIdx.x * blockDim.x + threadIdx.x;
-    if (l < L) h[l] = sign * 0.5 * x[l];
-}
-
-// Perturbed copies of the per-layer hydrogen-line inputs: field `which` of {T, ne, nH_I, nHe_I,
-// UH_I, xi} scaled by (1 + sign * rel) in every layer; h[l] = rel * |value|.
-__global__ void hfd_perturb_kernel(HLayers src, int which, double rel, double sign, double* dst, double* h) {
-    const int l = blockIdx.x * blockDim.x + threadIdx.x;
-    const int L = src.L;
-    if (l >= L) return;
-    const double* f[6] = {src.T, src.ne, src.nH, src.nHe, src.UH, src.xi};
-    for (int k = 0; k < 6; k++) {
-        double v = f[k][l];
-        if (k == which) {
-            const double d = rel * fabs(v);
-            if (sign > 0) h[l] = d;
-            v += sign * d;
-        }
-        dst[k * L + l] = v;
-    }
-}
-
 // Opacity of a spectrum of the last batch forward, still in the batch buffers.
 struct VjpOpacity {
     double* alpha;
@@ -795,9 +787,8 @@ int run_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& ln, cons
     KCHECK(ensure(ctx, ctx->aref, sizeof(double) * (L + 1)));
     KCHECK(ensure(ctx, ctx->vjp_g, (mixed ? sizeof(float) : sizeof(double)) * nLw));
     KCHECK(ensure(ctx, ctx->vjp_dpar, sizeof(double) * 3 * size_t(nmax) * Lp));
-    // small pieces: daref [L], a scratch dT [L], hydrogen FD inputs [2][6][L], steps [L], counter
-    const size_t o_dar = 0, o_dT = a256(8 * L), o_hin = o_dT + a256(8 * L), o_h = o_hin + a256(8 * 12 * L),
-                 o_ctr = o_h + a256(8 * L), o_g32 = o_ctr + 256;
+    // small pieces: daref [L], a scratch dT [L], counter
+    const size_t o_dar = 0, o_dT = a256(8 * L), o_ctr = o_dT + a256(8 * L), o_g32 = o_ctr + 256;
     // line-adjoint items ((chunk, tier) pairs) and the wavelengths as FP32 pairs
     const int np_max = int((nwl + ADJ_CHUNK - 1) / ADJ_CHUNK) * NTIER;
     const size_t o_ilo = o_g32 + a256(4 * L), o_ipre = o_ilo + a256(4 * size_t(np_max)),
@@ -859,64 +850,71 @@ int run_vjp(korg_ctx* ctx, const korg_synth_inputs* in, const LinesDev& ln, cons
     }
     record(ctx, 10, s);
 
-    // 3. hydrogen lines: layer-diagonal Jacobian.  alpha_H is proportional to nH_I / UH_I
-    //    (hydrogen_line_absorption.jl:110-111, 152-154); n(H I) also enters the ABO widths of
-    //    H alpha/beta/gamma (:130) and, with n(He I), the MHD occupation probabilities (:89).
-    //    So d/dUH_I = -alpha_H / UH_I always, d/dnH_I = alpha_H / nH_I when MHD is off and no ABO
-    //    line reaches the grid, d/dnHe_I = 0 when MHD is off; the rest (T, n_e, xi, and nH_I /
-    //    nHe_I otherwise) by forward differences (relative step 1e-7: truncation ~1e-7, rounding
-    //    ~1e-9 of the derivative) of the FP64 kernel against the unperturbed evaluation, all
-    //    layers perturbed at once.
+    // 3. hydrogen lines: alpha_H[l, :] depends only on layer l's inputs.  The forward prep's
+    //    records and tables, their derivatives (hline_adj_prep_kernel, brackett_adj_prep_kernel:
+    //    dual numbers in T, n_e, xi, n(H I), n(He I)), then one pass over the opacity cotangent
+    //    that forms d alpha_H / d input per (wavelength, layer) and contracts it
+    //    (hline_adj_kernel); U(H I) from alpha_H itself (alpha_H is proportional to 1 / U(H I)).
     if (in->hydrogen_lines && (flags & KORG_VJP_HYDROGEN)) {
-        KCHECK(ensure(ctx, ctx->vjp_hfd, sizeof(double) * 2 * nLw));
-        double* a0 = static_cast<double*>(ctx->vjp_hfd.p);
-        double* a1 = a0 + nLw;
-        double* hin = reinterpret_cast<double*>(sm + o_hin);
-        double* h = reinterpret_cast<double*>(sm + o_h);
-        double* outs[6] = {dT, gr.ne, gr.nH_I, gr.nHe_I, gr.UH_I, gr.xi};
-        bool abo_near = false;  // H alpha, beta, gamma (6564.6, 4862.7, 4341.7 A in vacuum)
-        {
-            double wmin = 0, wmax = 0;
-            KCUDA(cudaMemcpyAsync(&wmin, wls, sizeof(double), cudaMemcpyDeviceToHost, s));
-            KCUDA(cudaMemcpyAsync(&wmax, wls + nwl - 1, sizeof(double), cudaMemcpyDeviceToHost, s));
-            KCUDA(cudaStreamSynchronize(s));
-            for (double w0 : {6564.6e-8, 4862.7e-8, 4341.7e-8})
-                abo_near |= (w0 + 2 * in->hydrogen_window >= wmin) && (w0 - 2 * in->hydrogen_window <= wmax);
-        }
-        const bool linear_nH = !in->use_MHD && !abo_near;
-        // the unperturbed FP64 evaluation (hydro_fd_contract_kernel computes sum G (x - y) / (2 h))
-        KCUDA(cudaMemsetAsync(a0, 0, sizeof(double) * nLw, s));
-        KCHECK(run_hydrogen(ctx, a0, wls, nwl, hl, in->hydrogen_window, in->use_MHD, false, s));
-        if (outs[4] || (linear_nH && outs[2])) {
-            // x = alpha_H, y = 0, h = -UH_I / 2 or nH_I / 2: sum G alpha_H / (-UH_I) or / nH_I
-            KCUDA(cudaMemsetAsync(a1, 0, sizeof(double) * nLw, s));
-            if (outs[4]) {
-                hfd_half_kernel<<<(L + 127) / 128, 128, 0, s>>>(in->UH_I, L, -1.0, h);
-                hydro_fd_contract_kernel<<<ctx->sms * 4, 256, 0, s>>>(ctx->vjp_g.p, int32_t(mixed), a0, a1, h, nwl, L,
-                                                                     outs[4]);
-            }
-            if (linear_nH && outs[2]) {
-                hfd_half_kernel<<<(L + 127) / 128, 128, 0, s>>>(in->nH_I, L, 1.0, h);
-                hydro_fd_contract_kernel<<<ctx->sms * 4, 256, 0, s>>>(ctx->vjp_g.p, int32_t(mixed), a0, a1, h, nwl, L,
-                                                                     outs[2]);
-            }
+        const int ntrans = ctx->stark.ntrans, nbr = std::max(0, ctx->n_max - 4), ntot = ntrans + nbr;
+        if (ntot > HADJ_MAXT)
+            return set_err(ctx, KORG_EINVAL, "the hydrogen reverse mode supports %d transitions (got %d)", HADJ_MAXT,
+                           ntot);
+        // the forward's records and tables when the caller reuses its opacity (unless a batch
+        // forward, which overwrote them spectrum by spectrum, ran), else the prep again
+        HOut ho{static_cast<HRec*>(ctx->hrec.p), static_cast<double*>(ctx->hQ.p), static_cast<float*>(ctx->hQ32.p),
+                static_cast<int32_t*>(ctx->hulb.p), static_cast<int32_t*>(ctx->huub.p)};
+        const bool have_prep = (flags & KORG_VJP_REUSE_FORWARD) && !op && ctx->hyd_prep >= int(mixed);
+        if (!have_prep) KCHECK(run_hydrogen_prep(ctx, wls, nwl, hl, in->hydrogen_window, in->use_MHD, mixed, s, &ho));
+        const size_t n_dq = size_t(ntrans) * L * 2 * HND_MAX + size_t(nbr) * L * 3 * BR_NP;
+        // mixed: the Stehle table derivatives, then the Brackett profiles with theirs, in FP32
+        const size_t n_dq32 = mixed ? size_t(ntrans) * L * 2 * HND_MAX + size_t(nbr) * L * 4 * BR_NP : 0;
+        const size_t o_der32 = a256(sizeof(HDer) * size_t(ntot) * L);
+        KCHECK(ensure(ctx, ctx->vjp_hder, o_der32 + (mixed ? sizeof(HDer32) * size_t(ntot) * L : 0)));
+        KCHECK(ensure(ctx, ctx->vjp_hdq, sizeof(double) * n_dq + sizeof(float) * n_dq32));
+        HDer* hder = static_cast<HDer*>(ctx->vjp_hder.p);
+        HDer32* hder32 = mixed ? reinterpret_cast<HDer32*>(static_cast<unsigned char*>(ctx->vjp_hder.p) + o_der32)
+                               : nullptr;
+        double* hdq = static_cast<double*>(ctx->vjp_hdq.p);
+        float* hdq32 = mixed ? reinterpret_cast<float*>(hdq + n_dq) : nullptr;
+        hline_adj_prep_kernel<<<(ntrans * L + 127) / 128, 128, 0, s>>>(ctx->stark, hl, in->use_MHD, ho.rec, hder, hdq,
+                                                                      hder32, hdq32);
+        KCUDA(cudaGetLastError());
+        if (nbr > 0) {
+            brackett_adj_prep_kernel<<<dim3(nbr, L), 256, 0, s>>>(
+                hl, ntrans, wls, nwl, in->use_MHD, ho.rec, hder, hdq + size_t(ntrans) * L * 2 * HND_MAX, hder32,
+                mixed ? hdq32 + size_t(ntrans) * L * 2 * HND_MAX : nullptr);
             KCUDA(cudaGetLastError());
         }
-        for (int k = 0; k < 6; k++) {
-            if (!outs[k] || k == 4) continue;
-            if (k == 2 && linear_nH) continue;
-            if (k == 3 && !in->use_MHD) continue;  // n(He I) only enters the MHD probabilities
-            // x = alpha_H(p + dp), y = alpha_H(p), h = dp / 2
-            hfd_perturb_kernel<<<(L + 127) / 128, 128, 0, s>>>(hl, k, 1e-7, +1.0, hin, h);
-            hfd_half_kernel<<<(L + 127) / 128, 128, 0, s>>>(h, L, 1.0, h);
-            KCUDA(cudaGetLastError());
-            KCUDA(cudaMemsetAsync(a1, 0, sizeof(double) * nLw, s));
-            const HLayers hp{L, hin, hin + L, hin + 2 * L, hin + 3 * L, hin + 4 * L, hin + 5 * L};
-            KCHECK(run_hydrogen(ctx, a1, wls, nwl, hp, in->hydrogen_window, in->use_MHD, false, s));
-            hydro_fd_contract_kernel<<<ctx->sms * 4, 256, 0, s>>>(ctx->vjp_g.p, int32_t(mixed), a1, a0, h, nwl, L,
-                                                                 outs[k]);
-            KCUDA(cudaGetLastError());
-        }
+        HAdjArgs ha{};
+        ha.G = ctx->vjp_g.p;
+        ha.g32 = int32_t(mixed);
+        ha.wls = wls;
+        ha.nwl = nwl;
+        ha.L = L;
+        ha.ntrans = ntrans;
+        ha.ntot = ntot;
+        ha.rec = ho.rec;
+        ha.der = hder;
+        ha.der32 = hder32;
+        ha.Q = ho.Q;
+        ha.Q32 = ho.Q32;
+        ha.dQ = hdq;
+        ha.dQ32 = hdq32;
+        ha.bq32 = mixed ? hdq32 + size_t(ntrans) * L * 2 * HND_MAX : nullptr;
+        ha.ulb = ho.ulb;
+        ha.uub = ho.uub;
+        ha.d_off = ctx->stark.d_off;
+        ha.logdnu = ctx->stark.logdnu;
+        ha.logdnu32 = ctx->stark.logdnu32;
+        ha.UH = in->UH_I;
+        double* outs[6] = {dT, gr.ne, gr.xi, gr.nH_I, gr.nHe_I, gr.UH_I};
+        for (int k = 0; k < 6; k++) ha.out[k] = outs[k];
+        const int64_t tiles = (nwl + 31) / 32;
+        const int64_t blocks = std::min<int64_t>((tiles + HADJ_WARPS - 1) / HADJ_WARPS, int64_t(ctx->sms) * 4);
+        if (mixed) hline_adj_kernel<true><<<unsigned(blocks), 32 * HADJ_WARPS, 0, s>>>(ha);
+        else hline_adj_kernel<false><<<unsigned(blocks), 32 * HADJ_WARPS, 0, s>>>(ha);
+        KCUDA(cudaGetLastError());
     }
     record(ctx, 11, s);
 
@@ -1245,7 +1243,7 @@ KORG_API void korg_destroy(korg_ctx* ctx) {
     DevBuf* bufs[] = {&ctx->lines_scratch, &ctx->counters, &ctx->tune_alpha, &ctx->hrec, &ctx->hQ, &ctx->hQ32,
                       &ctx->hulb, &ctx->huub, &ctx->stage_dev, &ctx->aref, &ctx->alpha, &ctx->flux, &ctx->cntm,
                       &ctx->math, &ctx->b_alpha, &ctx->b_lines, &ctx->b_meta, &ctx->vjp_g, &ctx->vjp_dpar,
-                      &ctx->vjp_small, &ctx->vjp_hfd, &ctx->mx_layers};
+                      &ctx->vjp_small, &ctx->vjp_hder, &ctx->vjp_hdq, &ctx->mx_layers};
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
     for (void* p : ctx->stark_allocs) cudaFree(p);

@@ -104,10 +104,69 @@ def test_vjp_mixed_close_to_fp64(ctx):
     obs = _obs(inp, ctx)
     _, g64 = loss_and_gradient(inp, obs, precision="fp64", ctx=ctx)
     _, g32 = loss_and_gradient(inp, obs, precision="mixed", ctx=ctx)
-    for k in ("T", "ne", "n_eff_vdW", "xi", "n_div_U", "log_gf", "cntm_vals", "alpha_ref_cntm"):
+    for k in ("T", "ne", "n_eff_vdW", "xi", "n_div_U", "log_gf", "cntm_vals", "alpha_ref_cntm", "nH_I", "nHe_I",
+              "UH_I"):
         a, b = g32[k], g64[k]
         err = np.max(np.abs(a - b)) / np.max(np.abs(b))
         assert err <= 2e-3, (k, err)
+
+
+# (wavelength range, MHD, checks (input, layer, relative step)): the inputs and layers whose loss
+# derivative stands well above the FP64 synthesis's rounding.  Deep layers, n(He I) (it only
+# enters the MHD occupation probabilities) and, in the H band, n(H I) and U(H I) change the loss
+# by less than its rounding lets a difference resolve at 1e-6.  n(H I) and U(H I) enter alpha_H
+# linearly or as 1/U, so they take larger steps.
+_HCHECKS = [("T", 8, 1e-4), ("T", 30, 1e-4), ("ne", 30, 1e-4), ("xi", 8, 1e-4), ("xi", 30, 1e-4),
+            ("nH_I", 30, 1e-3), ("UH_I", 30, 1e-3)]
+HYDROGEN_CASES = {"Balmer with MHD": ((4840.0, 4885.0), True, _HCHECKS),
+                  "Balmer": ((4840.0, 4885.0), False, _HCHECKS),
+                  "Brackett": ((16790.0, 16830.0), False, _HCHECKS[1:5])}
+
+
+@pytest.mark.parametrize("case", list(HYDROGEN_CASES))
+def test_hydrogen_gradient_exact(ctx, case):
+    """The hydrogen-line reverse mode is exact: the gradient with respect to the hydrogen-line
+    inputs of single layers (H beta with its ABO profile and the Stehle Balmer lines, with and
+    without the MHD occupation probabilities; Griem Brackett lines in the H band) against
+    Richardson-extrapolated central differences of the FP64 forward, to 1e-6.  Each difference
+    also states its own uncertainty, the change of the extrapolation from steps (h, h/2) to
+    (2h, h), which must itself be below 1e-6.  A wavelength whose loss term steps inside a
+    difference interval has weight 0 in that check's loss and gradient: Korg's E2 is piecewise
+    with jumps at its segment ends, and the hydrogen windows' edges follow the interpolated line
+    centre."""
+    from korg_gb300.api import synthesize_prepared, synthesize_vjp
+    wl, mhd, checks = HYDROGEN_CASES[case]
+    inp = _case(n_lines=30, wl=wl, seed=3)
+    inp.use_MHD = mhd
+    obs = _obs(inp, ctx)
+    base = synthesize_prepared(inp, precision="fp64", ctx=ctx)
+    r0 = base.flux / base.cntm - obs
+
+    def terms(x):
+        r = synthesize_prepared(x, precision="fp64", ctx=ctx)
+        return (r.flux / r.cntm - obs) ** 2
+
+    rows = []
+    for field, l, rel in checks:
+        h = rel * abs(getattr(inp, field)[l])
+        t = {s: terms(_perturbed(inp, field, l, s * h)) for s in (2.0, 1.0, 0.5, -0.5, -1.0, -2.0)}
+        d = {s: (t[s] - t[-s]) / (2 * s * h) for s in (2.0, 1.0, 0.5)}
+        S = np.sum(np.abs(d[0.5]))
+        # a smooth term's differences at h and h/2 differ by O(h^2) of itself; a step by far more
+        keep = ((np.abs(d[1.0] - d[0.5]) <= 1e-3 * np.abs(d[0.5]) + 1e-7 * S) &
+                (np.abs(d[2.0] - d[1.0]) <= 4e-3 * np.abs(d[1.0]) + 4e-7 * S))
+        assert np.count_nonzero(keep) >= 0.95 * len(keep), (field, l)
+        fd = np.sum(keep * (4 * d[0.5] - d[1.0]) / 3)  # Richardson: truncation O(h^4)
+        unc = abs(fd - np.sum(keep * (4 * d[1.0] - d[2.0]) / 3))
+        w = keep * 2 * r0
+        g = synthesize_vjp(inp, w / base.cntm, -w * base.flux / base.cntm ** 2, precision="fp64", hydrogen=True,
+                           ctx=ctx)
+        rows.append((field, l, g[field][l], fd, unc, np.count_nonzero(~keep)))
+        print(f"{case} {field}[{l}]: adjoint {g[field][l]:.10e}, differences {fd:.10e} +- {unc:.1e} "
+              f"({np.count_nonzero(~keep)} wavelengths stepped)")
+    for field, l, ad, fd, unc, _ in rows:
+        assert np.isfinite(ad) and unc <= 1e-6 * abs(fd), (field, l, ad, fd, unc)
+        assert abs(ad - fd) <= 1e-6 * abs(fd) + unc, (field, l, ad, fd, unc)
 
 
 def test_vjp_without_hydrogen_holds_hydrogen_fixed(ctx):
