@@ -723,7 +723,7 @@ def batch_gradient(b, stream, t_forward_ms, steps=1):
             "gradient_over_forward": (t - t_forward_ms) / t_forward_ms,
             "note": "batched forward (graph replay), loss, then korg_synthesize_batch_vjp_dev reusing the forward's "
                     "opacity for every spectrum; gradient w.r.t. T, ne, n_eff_vdW, xi, n/U, log gf, continuum, "
-                    "H-line inputs (hydrogen by forward differences)"}
+                    "H-line inputs (hydrogen lines with their exact derivatives)"}
 
 
 def _progress(msg, t0=time.perf_counter()):
