@@ -138,3 +138,50 @@ def test_reference_signature_entry_points_are_functions():
     params = list(inspect.signature(korg_gb300.line_absorption_).parameters)
     assert params[:9] == ["alpha", "linelist", "wls", "temps", "ne", "n_densities", "partition_fns", "xi",
                           "alpha_cntm"]
+
+
+def test_continuum_layer_inputs_vjp_is_the_chain_rule():
+    """continuum.layer_inputs_vjp (the host chain rule behind the continuum's reverse mode) against
+    central differences of sum(gbar * layer_inputs(T, ne, densities)): the temperatures through
+    1/U(H I), 1/U(He I) and T itself, n_e, and each species' density, including the Peach ions,
+    the other ions' charge sums and a neutral species that does not enter."""
+    from korg_gb300 import continuum
+    from korg_gb300.data import default_partition_funcs
+    from korg_gb300.species import Species, parse_species
+    rng = np.random.default_rng(2)
+    L = 4
+    T, ne = rng.uniform(4000, 7000, L), 10 ** rng.uniform(12, 14, L)
+    names = ["H I", "H II", "He I", "H2", "He II", "C II", "Si II", "Mg II", "Fe II", "Fe III", "Ca II", "O I"]
+    nd = {parse_species(n): 10 ** rng.uniform(8, 16, L) for n in names}
+    nd[Species([1], -1)] = 10 ** rng.uniform(6, 9, L)
+    pf = default_partition_funcs()
+    gbar = {k: rng.normal(size=L) for k in continuum.INPUTS}
+
+    def diff(Tp, Tm, nep, nem, ndp, ndm):
+        dp, dm = continuum.layer_inputs(Tp, nep, ndp, pf), continuum.layer_inputs(Tm, nem, ndm, pf)
+        return sum(float(np.sum(gbar[k] * (dp[k] - dm[k]))) for k in continuum.INPUTS)
+
+    dT, dne, dn = continuum.layer_inputs_vjp(gbar, T, nd, pf)
+    for l in range(L):
+        h = 1e-5 * T[l]
+        Tp, Tm = T.copy(), T.copy()
+        Tp[l] += h
+        Tm[l] -= h
+        fd = diff(Tp, Tm, ne, ne, nd, nd) / (2 * h)
+        assert abs(dT[l] - fd) <= 1e-6 * abs(fd), (l, dT[l], fd)
+        h = 1e-6 * ne[l]
+        nep, nem = ne.copy(), ne.copy()
+        nep[l] += h
+        nem[l] -= h
+        fd = diff(T, T, nep, nem, nd, nd) / (2 * h)
+        assert abs(dne[l] - fd) <= 1e-6 * abs(fd), (l, dne[l], fd)
+        for s in nd:
+            h = 0.5 * nd[s][l]  # the inputs are linear in the densities: any step is exact
+            ndp, ndm = dict(nd), dict(nd)
+            ndp[s], ndm[s] = nd[s].copy(), nd[s].copy()
+            ndp[s][l] += h
+            ndm[s][l] -= h
+            fd = diff(T, T, ne, ne, ndp, ndm) / (2 * h)
+            ad = np.asarray(dn.get(s, np.zeros(L)))[l]
+            assert abs(ad - fd) <= 1e-6 * abs(fd) + 1e-12 * abs(gbar["n_Z1"][l]), (str(s), l, ad, fd)
+    assert np.all(np.asarray(dn.get(parse_species("O I"), np.zeros(L))) == 0)
