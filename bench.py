@@ -74,6 +74,7 @@ def parse():
                     help="skip the oracle comparison of the adjoint, batch and cool-star configurations")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the reverse-mode measurement")
     ap.add_argument("--no-chemistry", action="store_true", help="skip the chemical-equilibrium measurement")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 16-spectrum batched-engine measurement")
     ap.add_argument("--workload", default="synth",
                     choices=["synth", "batch", "adjoint", "variants", "postprocess", "chemistry"])
     ap.add_argument("--tile", default=None, help="force the line tile shape: tw,stage,split (e.g. 64,32,1)")
@@ -593,6 +594,7 @@ def run_korg(args):
     adj = adjoint_measure(ctx, torch, dev, steps=5) if rank == 0 and not args.no_adjoint else None
     chem = (chemistry_measure(ctx, torch, dev, os.cpu_count() or 1)
             if rank == 0 and not args.no_chemistry else None)
+    batch = batch_measure(torch, dev) if rank == 0 and not args.no_batch else None
 
     # alpha init, reference-wavelength lines (5), hydrogen (3), metal lines (5), transfer
     launches_per_step = 1 + 5 + (3 if inp.hydrogen_lines else 0) + 5 + 1
@@ -636,6 +638,7 @@ def run_korg(args):
         "parity_vs_oracle": parity,
         "adjoint": adj,
         "chemical_equilibrium": chem,
+        "batch": batch,
         "e2e": {"value": world / e2e_s, "unit": "spectra/s", "h2d_bytes_per_step": host_bytes(inp),
                 "d2h_bytes_per_step": 16 * nwl},
         "gpu_launches": launches_per_step * args.steps,
@@ -658,22 +661,31 @@ def _fixed_chemistry(ne, nd, T, n_tot, A_X):
     return ne, nd
 
 
+def _no_continuum(wls_cm, T, ne, n_HI, n_HII):
+    """Placeholder continuum for the pool workers: the batch's continuum is evaluated afterwards on
+    the device for every atmosphere (korg_continuum_absorption)."""
+    import numpy as np
+    return np.zeros(len(wls_cm))
+
+
 def _prep_batch_one(a):
     sys.path.insert(0, os.path.join(ROOT, "korg.jl_gb300"))
     import functools
     from korg_gb300.api import prepare_synthesis
     w, (atm, A_X), ne, nd = a
     return prepare_synthesis(atm, w.linelist, A_X, w.wavelengths, vmic=w.vmic, hydrogen_lines=w.hydrogen_lines,
-                             chemical_equilibrium=functools.partial(_fixed_chemistry, ne, nd))
+                             chemical_equilibrium=functools.partial(_fixed_chemistry, ne, nd),
+                             continuum_opacity=_no_continuum)
 
 
 def batch_inputs(n_spectra):
     """Host precompute of the batch workload: the atmospheres in a spawn pool, the chemical
     equilibrium of every layer of every atmosphere in one batched device call
-    (korg_chemical_equilibrium), then the rest of each spectrum's precompute in the pool."""
+    (korg_chemical_equilibrium), the rest of each spectrum's precompute in the pool, then Korg's
+    continuum absorption of every atmosphere on the device (korg_continuum_absorption)."""
     import multiprocessing as mp
     import numpy as np
-    from korg_gb300 import _lib, synthetic
+    from korg_gb300 import _lib, continuum, synthetic
     from korg_gb300.statmech import default_equilibrium_tables, solve_layers
     works = synthetic.config3(n_spectra=n_spectra)
     t0 = time.perf_counter()
@@ -688,7 +700,6 @@ def batch_inputs(n_spectra):
     dens, status, info = solve_layers(np.concatenate([a.T for a, _ in atms]), np.concatenate([a.n_tot for a, _ in atms]),
                                       np.concatenate([a.ne for a, _ in atms]), abund, atm=idx, ctx=ctx)
     t3 = time.perf_counter()
-    ctx.close()
     species = default_equilibrium_tables().species
     chem = []
     for k in range(len(atms)):
@@ -697,9 +708,18 @@ def batch_inputs(n_spectra):
     with mp.get_context("spawn").Pool(min(len(works), os.cpu_count() or 1)) as pool:
         inps = pool.map(_prep_batch_one, [(w, a, c[0], c[1]) for w, a, c in zip(works, atms, chem)], chunksize=1)
     t4 = time.perf_counter()
+    ctx.ensure_continuum()
+    for inp in inps:
+        d = continuum.layer_inputs(inp.T, inp.ne, inp.number_densities)
+        inp.cntm_vals = continuum.absorption_from_inputs(inp.cntm_knots, d, ctx)
+        inp.alpha_ref_cntm = continuum.absorption_from_inputs(np.array([inp.ref_wl]), d, ctx)[:, 0].copy()
+    t5 = time.perf_counter()
+    ctx.close()
     return inps, {"atmospheres_s": t1 - t0, "chemistry_s": t3 - t2, "chemistry_layers": len(idx),
                   "chemistry_newton_iterations": float(info[:, 0].sum()), "rest_s": t4 - t3,
-                  "chemistry": "korg_chemical_equilibrium, every layer of every atmosphere in one call (host pointers)"}
+                  "continuum_s": t5 - t4,
+                  "chemistry": "korg_chemical_equilibrium, every layer of every atmosphere in one call (host pointers)",
+                  "continuum": "korg_continuum_absorption per atmosphere (host pointers)"}
 
 
 def cpu_sample_batch(inp, threads):
@@ -747,6 +767,56 @@ def batch_gradient(b, stream, t_forward_ms, steps=1):
             "note": "batched forward (graph replay), loss, then korg_synthesize_batch_vjp_dev reusing the forward's "
                     "opacity for every spectrum; gradient w.r.t. T, ne, n_eff_vdW, xi, n/U, log gf, continuum, "
                     "H-line inputs (hydrogen lines with their exact derivatives)"}
+
+
+def batch_measure(torch, dev, n=16, steps=3):
+    """The batched engine on n spectra of the batch workload (its distributions: Teff 3500-7000 K,
+    20k-200k-line subsets, 15000-17000 A at 0.005 A): forward throughput (graph replay), the
+    speed-up over the plain FP64 form and the mixed form's error on 2 of them, and forward + loss +
+    gradient of the whole batch (korg_synthesize_batch_vjp_dev)."""
+    import numpy as np
+    from korg_gb300.batch import BatchSynthesis
+    t0 = time.perf_counter()
+    inps, _ = batch_inputs(n)
+    host_s = time.perf_counter() - t0
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(bs, reps):
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            bs.run(stream)
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return statistics.mean(ts)
+
+    b = BatchSynthesis(inps, precision="mixed", use_graph=True, autotune=False, max_scratch_bytes=160 << 30)
+    for _ in range(3):
+        b.run(stream)
+        torch.cuda.synchronize()
+    ms = timed(b, steps)
+    fm, cm = b.results()
+    sub = inps[:2]
+    b64 = BatchSynthesis(sub, precision="fp64", use_graph=False, autotune=False, max_scratch_bytes=160 << 30)
+    b64.run(stream)
+    torch.cuda.synchronize()
+    ms64 = timed(b64, 1)
+    f64, c64 = b64.results()
+    b64.ctx.close()
+    grad = batch_gradient(b, stream, ms)
+    b.ctx.close()
+    mixed, plain = 1000.0 * n / ms, 1000.0 * len(sub) / ms64
+    return {"workload": f"{n} spectra of the batch workload (56 layers, Teff 3500-7000 K, logg 1-5, [M/H] "
+                        f"-2.5..0.5, {sum(len(i.linelist) for i in inps)} lines in all, 15000-17000 A @ 0.005 A), "
+                        "device chemistry and continuum",
+            "spectra_per_s": mixed, "ms_per_batch": ms, "plain_fp64_spectra_per_s": plain,
+            "plain_fp64": f"the same engine in plain FP64 on {len(sub)} of the spectra",
+            "batched_speedup_vs_plain_fp64": mixed / plain,
+            "mixed_max_rel_flux_err_vs_fp64": float(np.max(np.abs(fm[:len(sub)] / f64 - 1))),
+            "mixed_rectified_rms_vs_fp64": float(np.sqrt(np.mean((fm[:len(sub)] / cm[:len(sub)] - f64 / c64) ** 2))),
+            "gradient": {k: v for k, v in grad.items() if k != "note"}, "host_prep_s": host_s}
 
 
 def _progress(msg, t0=time.perf_counter()):
@@ -864,7 +934,7 @@ def run_batch(args):
                    "l2": f"batch alpha {8 * L * nwl * n / 1e9:.1f} GB >> L2", "graph": True, "tile": cfg,
                    "host_prep_s": host_prep_s, "host_prep_parts": prep_parts,
                    "chemistry": "device (korg_chemical_equilibrium, all atmospheres in one call)",
-                   "continuum": "CPU stand-in"},
+                   "continuum": "device (korg_continuum_absorption: Korg's terms but metal bound-free)"},
         "evals_per_step": evals, "evals_per_s": evals / (ms * 1e-3),
         "stages_ms": {"total_eager": st.ms_total, "line_tile_queue": st.ms_line_tile, "rt_all": st.ms_rt},
         "fp64": fp64,
