@@ -1285,7 +1285,8 @@ def run_adjoint(args):
            "scaling": "weak", "vs_baseline": None, "dtype": "f32 profiles + f64 tau/flux (mixed)",
            "data": "synthetic (seeded line list and stand-in atmosphere)",
            "config": {"workload": f"adjoint: 72 layers, Teff 4500 logg 2.5 [M/H] -0.5, {len(inp.linelist)} lines "
-                                  f"(50k atomic + 20k CO/OH/CN), 15000-17000 A @ 0.005 A ({nwl} points); loss = "
+                                  f"({round(50 * args.adj_scale, 1):g}k atomic + {round(20 * args.adj_scale, 1):g}k "
+                                  f"CO/OH/CN), 15000-17000 A @ 0.005 A ({nwl} points); loss = "
                                   "sum of squared rectified-flux residuals; gradient w.r.t. T, ne, n_eff_vdW, xi, "
                                   "n/U, log gf, continuum, H-line inputs"},
            "forward_ms": t_fwd, "gradient_over_forward": (t_step - t_fwd) / t_fwd, "vjp_stages_ms": vjp_stages,
