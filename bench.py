@@ -724,14 +724,14 @@ def batch_inputs(n_spectra):
 
 def cpu_sample_batch(inps, threads):
     """Oracle on the first spectra of the batch (their line counts spread over the batch's
-    20k-200k), each over 20 windows of 20 A spread evenly over the grid (20% of it)."""
+    20k-200k), each over 10 windows of 20 A spread evenly over the grid (10% of it)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import copy
     import oracle
     from korg_gb300.data import stark_profiles
     from korg_gb300.wavelengths import Wavelengths
     oracle.build()
-    win = Wavelengths([(15040.0 + 100.0 * k, 15060.0 + 100.0 * k, 0.005) for k in range(20)])
+    win = Wavelengths([(15090.0 + 200.0 * k, 15110.0 + 200.0 * k, 0.005) for k in range(10)])
     frac = len(win) / len(inps[0].wls)
     dt, ev = 0.0, 0
     for inp in inps:
@@ -741,7 +741,7 @@ def cpu_sample_batch(inps, threads):
         ev += oracle.synthesize(s, s.linelist, s.linelist5, stark_profiles(), s.wls.all_wls, nthreads=threads)[4]
         dt += time.perf_counter() - t0
     return len(inps) * frac / dt, dt, ev, (f"spectra 0-{len(inps) - 1} of the batch "
-                                           f"({', '.join(str(len(i.linelist)) for i in inps)} lines) on 20 windows "
+                                           f"({', '.join(str(len(i.linelist)) for i in inps)} lines) on 10 windows "
                                            f"of 20 A ({len(win)} of {len(inps[0].wls)} points, fraction {frac:.4f}); "
                                            "spectra/s = spectra x fraction / seconds")
 
@@ -922,7 +922,7 @@ def run_batch(args):
     cpu = None
     if not args.no_cpu:
         threads = os.cpu_count() or 1
-        v, dt, ev_cpu, info = cpu_sample_batch(inps[:8], threads)
+        v, dt, ev_cpu, info = cpu_sample_batch(inps[:4], threads)
         _progress("CPU sample done")
         cpu = {"value": v, "unit": "spectra/s", "cores": threads, "kind": "port", "sample": info,
                "evals_per_s": ev_cpu / dt, "seconds": dt}

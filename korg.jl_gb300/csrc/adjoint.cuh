@@ -185,7 +185,7 @@ __device__ __forceinline__ double expint2_deriv(double x, double e2, double ex, 
         return a[1] + y * (2 * a[2] + y * (3 * a[3] + y * (4 * a[4] + y * 5 * a[5])));
     }
     // E2 = e^-x u R(u), u = 1/x
-    const double u = 1 / x;
+    const double u = recip64(x);
     const double R = 1 + (-2 + (6 + (-24 + 120 * u) * u) * u) * u;
     const double dR = -2 + (12 + (-72 + 480 * u) * u) * u;
     return -e2 - ex * u * u * (R + u * dR);
@@ -193,9 +193,10 @@ __device__ __forceinline__ double expint2_deriv(double x, double e2, double ex, 
 
 // One transfer pass over the column `al` (global or shared) with cotangent w of 2 pi I unit:
 // writes dL/dalpha of the pass into gout[l], adds dL/dS into c.Sbar and dL/dalpha_ref into
-// s_daref (shared, atomically).
+// s_daref (shared, atomically).  s_iaref = 1 / alpha_ref.  No FP64 division: one Newton
+// reciprocal of each segment's dtau (recip64) serves its three quotients.
 __device__ __forceinline__ void rt_adj_pass(const RtaCol& c, const double* al, double w, const double* s_fac,
-                                            const double* s_dlt, const double* s_aref, int L, const MathTables& mt,
+                                            const double* s_dlt, const double* s_iaref, int L, const MathTables& mt,
                                             double* gout, double* s_daref, int lane) {
     // optical depth (RadiativeTransfer.jl:244-253): ib, trapezoid increments, warp scans
     for (int l = lane; l < L; l += 32) c.ib[l] = al[l] * s_fac[l];
@@ -247,7 +248,8 @@ __device__ __forceinline__ void rt_adj_pass(const RtaCol& c, const double* al, d
         const double ta_ = c.tau[l - 1], tb_ = c.tau[l];
         const double Sa = c.S[l - 1], Sb = c.S[l];
         const double D = tb_ - ta_;
-        const double m = (Sb - Sa) / D;
+        const double iD = recip64(D);
+        const double m = (Sb - Sa) * iD;
         const double bb = Sa - m * ta_;
         const double Pb = 0.5 * ((tb_ * c.e2[l] - c.ex[l]) - (ta_ * c.e2[l - 1] - c.ex[l - 1]));
         const double Pm = (1.0 / 3.0) * ((tb_ * tb_ * c.e2[l] - c.ex[l] * (tb_ + 1)) -
@@ -255,10 +257,11 @@ __device__ __forceinline__ void rt_adj_pass(const RtaCol& c, const double* al, d
         const double Q = Pm - ta_ * Pb;  // total derivative through m (b depends on m)
         const double Ctb = dC(tb_, c.e2[l], c.d2[l], c.ex[l], m, bb);
         const double Cta = l == 1 ? 0.0 : dC(ta_, c.e2[l - 1], c.d2[l - 1], c.ex[l - 1], m, bb);
-        c.tb[l] = w * (Ctb - Q * m / D);
-        c.ta[l - 1] = w * (-Cta - Pb * m + Q * m / D);
-        c.sb[l] = w * (Q / D);
-        c.sa[l - 1] = w * (Pb - Q / D);
+        const double QD = Q * iD, QmD = QD * m;
+        c.tb[l] = w * (Ctb - QmD);
+        c.ta[l - 1] = w * (-Cta - Pb * m + QmD);
+        c.sb[l] = w * QD;
+        c.sa[l - 1] = w * (Pb - QD);
     }
     __syncwarp();
     // tau_bar[l] = sum over k >= l of the direct cotangents (tau_k = tau_{k-1} + increment):
@@ -282,7 +285,7 @@ __device__ __forceinline__ void rt_adj_pass(const RtaCol& c, const double* al, d
         if (l >= 1) ibar += 0.5 * s_dlt[l] * c.tau[l];
         if (l + 1 < L) ibar += 0.5 * s_dlt[l + 1] * c.tau[l + 1];
         gout[l] = ibar * s_fac[l];
-        if (ibar != 0.0) atomicAdd(s_daref + l, -ibar * c.ib[l] / s_aref[l]);  // fac = tau_ref/alpha_ref
+        if (ibar != 0.0) atomicAdd(s_daref + l, -ibar * c.ib[l] * s_iaref[l]);  // fac = tau_ref/alpha_ref
         c.Sbar[l] += c.sb[l] + c.sa[l];
     }
     __syncwarp();
@@ -290,7 +293,7 @@ __device__ __forceinline__ void rt_adj_pass(const RtaCol& c, const double* al, d
 
 __global__ void __launch_bounds__(32 * RTA_WARPS) rt_adjoint_kernel(RtAdjArgs a) {
     __shared__ MathTables s_math;
-    __shared__ double s_fac[RTA_LMAX], s_dlt[RTA_LMAX], s_aref[RTA_LMAX], s_T[RTA_LMAX];
+    __shared__ double s_fac[RTA_LMAX], s_dlt[RTA_LMAX], s_iaref[RTA_LMAX], s_iT[RTA_LMAX], s_ikT[RTA_LMAX];
     __shared__ double s_dT[RTA_LMAX], s_dar[RTA_LMAX];
     extern __shared__ double s_cols[];  // [warps][RTA_ARRAYS][L + 1]
     load_math_tables(s_math, a.math);
@@ -298,8 +301,9 @@ __global__ void __launch_bounds__(32 * RTA_WARPS) rt_adjoint_kernel(RtAdjArgs a)
     for (int l = threadIdx.x; l < L; l += blockDim.x) {
         s_fac[l] = a.tau_ref[l] / a.alpha_ref[l];
         s_dlt[l] = l == 0 ? 0.0 : log(a.tau_ref[l]) - log(a.tau_ref[l - 1]);
-        s_aref[l] = a.alpha_ref[l];
-        s_T[l] = a.T[l];
+        s_iaref[l] = 1.0 / a.alpha_ref[l];
+        s_iT[l] = 1.0 / a.T[l];
+        s_ikT[l] = 1.0 / (KBOLTZ_CGS * a.T[l]);  // as the forward transfer forms it
         s_dT[l] = 0.0;
         s_dar[l] = 0.0;
     }
@@ -318,18 +322,19 @@ __global__ void __launch_bounds__(32 * RTA_WARPS) rt_adjoint_kernel(RtAdjArgs a)
         const double wc = (two && a.dcntm) ? a.dcntm[j] * 2 * PI * a.unit : 0.0;
         const double pre = 2 * HPLANCK_CGS * (C_CGS * C_CGS) / (wl * wl * wl * wl * wl);
         const double hcw = HPLANCK_CGS * C_CGS / wl;
+        const double ipre = recip64(pre);
         for (int l = lane; l < L; l += 32) {
-            c.S[l] = planck(pre, hcw, s_T[l]);
+            c.S[l] = planck_t(pre, hcw, s_ikT[l], s_math);  // the forward transfer's source function
             c.Sbar[l] = 0.0;
         }
         __syncwarp();
-        rt_adj_pass(c, a.alpha + j * L, wf, s_fac, s_dlt, s_aref, L, s_math, c.g, s_dar, lane);
+        rt_adj_pass(c, a.alpha + j * L, wf, s_fac, s_dlt, s_iaref, L, s_math, c.g, s_dar, lane);
         if (two) {
             // continuum-only column (src/synthesize.jl:287-291), as the forward interpolates it
             const KnotPos kp = knot_pos(a.cn.knots, a.cn.nk, wl);
             for (int l = lane; l < L; l += 32) c.col[l] = knot_eval(a.cn.vals + int64_t(l) * a.cn.nk, a.cn.nk, kp);
             __syncwarp();
-            rt_adj_pass(c, c.col, wc, s_fac, s_dlt, s_aref, L, s_math, c.gc, s_dar, lane);
+            rt_adj_pass(c, c.col, wc, s_fac, s_dlt, s_iaref, L, s_math, c.gc, s_dar, lane);
             // the knots feed both passes' opacity (alpha = continuum + hydrogen + lines)
             if (a.dvals) {
                 for (int l = lane; l < L; l += 32) {
@@ -348,8 +353,8 @@ __global__ void __launch_bounds__(32 * RTA_WARPS) rt_adjoint_kernel(RtAdjArgs a)
         // Planck source function (src/synthesize.jl:412-418): dB/dT = B x/T (1 + B/pre)
         for (int l = lane; l < L; l += 32) {
             const double B = c.S[l];
-            const double x = hcw / KBOLTZ_CGS / s_T[l];
-            const double d = c.Sbar[l] * B * (x / s_T[l]) * (1.0 + B / pre);
+            const double x = hcw * s_ikT[l];
+            const double d = c.Sbar[l] * B * (x * s_iT[l]) * (1.0 + B * ipre);
             if (d != 0.0) atomicAdd(s_dT + l, d);
             if (a.g32)
                 static_cast<float*>(a.G)[j * L + l] = float(c.g[l]);

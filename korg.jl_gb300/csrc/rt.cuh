@@ -30,14 +30,10 @@ struct RtArgs {
     double unit;             // multiplies 2*pi*I (1e-8 in synthesize, src/synthesize.jl:315-318)
 };
 
-// src/synthesize.jl:412-418 with the column factors hoisted
-__device__ __forceinline__ double planck(double pre, double hc_over_wl, double T) {
-    return pre * 1 / expm1(hc_over_wl / KBOLTZ_CGS / T);
-}
-// The same with 1/(kT) per layer precomputed, exp(x) - 1 from the table-driven exp and the
-// Newton reciprocal: for x = hc/(lambda k T) >= 0.07 (lambda <= 2 um, T <= 1e5 K) the
-// subtraction loses under two bits, so the result stays within a few ulps of expm1's while the
-// FP64 work per (layer, wavelength) drops by about half.
+// src/synthesize.jl:412-418 with the column factors hoisted and 1/(kT) per layer precomputed,
+// exp(x) - 1 from the table-driven exp and the Newton reciprocal: for x = hc/(lambda k T) >= 0.07
+// (lambda <= 2 um, T <= 1e5 K) the subtraction loses under two bits, so the result stays within a
+// few ulps of pre / expm1(x), at about half the FP64 work per (layer, wavelength).
 __device__ __forceinline__ double planck_t(double pre, double hc_over_wl, double inv_kT, const MathTables& mt) {
     const double x = hc_over_wl * inv_kT;
     return x < 0.05 ? pre / expm1(x) : pre * recip64(fexp64(x, mt) - 1.0);
