@@ -411,7 +411,9 @@ def synthesize_vjp(inp: SynthesisInputs, dflux, dcntm=None, precision="fp64", hy
     gradient of sum(dflux * flux + dcntm * cntm) with respect to the hot-path inputs, as a dict
     keyed by GRAD_FIELDS (shapes: [L], n_div_U [S, L], log_gf [n lines], cntm_vals [L, nk]).
     reuse_forward: the previous call on ``ctx`` was synthesize_prepared of the same inputs and
-    precision; its opacity is reused instead of recomputed."""
+    precision; its opacity is reused instead of recomputed.  hydrogen: differentiate the
+    hydrogen lines too (the exact derivatives of their approximation with respect to T, ne, xi,
+    nH_I, nHe_I, UH_I); False holds them fixed."""
     ctx = ctx or _lib.default_context()
     if inp.hydrogen_lines:
         ctx.ensure_stark()
