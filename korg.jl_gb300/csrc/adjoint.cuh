@@ -191,6 +191,23 @@ __device__ __forceinline__ double expint2_deriv(double x, double e2, double ex, 
     return -e2 - ex * u * u * (R + u * dR);
 }
 
+// E2(x) as expint2_ex evaluates it, with d/dx of the same branch (expint2_deriv) from one
+// logarithm: for x < 1.1 both need ln x.
+__device__ __forceinline__ double expint2_and_deriv(double x, double ex, const MathTables& t, double& d2) {
+    if (x < 1.1 && x != 0) {  // E2 = 1 + x (ln x + EM - 1) + x Q(x)
+        const double EM = 0.57721566490153286060651209008240243104215933593992;
+        const double c2 = 0.08333333333333333, c3 = -0.013888888888888888, c4 = 0.0020833333333333333;
+        const double lg = flog64(x, t);
+        const double Q = (-0.5 + (c2 + (c3 + c4 * x) * x) * x) * x;
+        const double dQ = -0.5 + (2 * c2 + (3 * c3 + 4 * c4 * x) * x) * x;
+        d2 = lg + EM + Q + x * dQ;
+        return 1 + ((lg + EM - 1) + Q) * x;
+    }
+    const double e2 = expint2_ex(x, ex, t);
+    d2 = expint2_deriv(x, e2, ex, t);
+    return e2;
+}
+
 // One transfer pass over the column `al` (global or shared) with cotangent w of 2 pi I unit:
 // writes dL/dalpha of the pass into gout[l], adds dL/dS into c.Sbar and dL/dalpha_ref into
 // s_daref (shared, atomically).  s_iaref = 1 / alpha_ref.  No FP64 division: one Newton
@@ -225,10 +242,11 @@ __device__ __forceinline__ void rt_adj_pass(const RtaCol& c, const double* al, d
         if (l < L) {
             const double t = c.tau[l];
             const double ex = l == 0 ? 1.0 : fexp64(-t, mt);
-            const double e2 = l == 0 ? 1.0 : expint2_ex(t, ex, mt);
+            double d2 = 0.0;  // tau_0 = 0 is not a variable
+            const double e2 = l == 0 ? 1.0 : expint2_and_deriv(t, ex, mt, d2);
             c.ex[l] = ex;
             c.e2[l] = e2;
-            c.d2[l] = l == 0 ? 0.0 : expint2_deriv(t, e2, ex, mt);  // tau_0 = 0 is not a variable
+            c.d2[l] = d2;
             c.tb[l] = 0.0;
             c.sb[l] = 0.0;
         }
