@@ -1309,6 +1309,7 @@ KORG_API int korg_set_stark_tables(korg_ctx* ctx, const korg_stark_tables* t) {
     for (void* p : ctx->stark_allocs) cudaFree(p);
     ctx->stark_allocs.clear();
     ctx->have_stark = false;
+    ctx->hyd_prep = -1;  // records made with the previous tables are not reused
     const int n = t->ntrans;
     int64_t sz_t = 0, sz_ne = 0, sz_d = 0, sz_p = 0, sz_l = 0;
     int n_max = 0, nd_max = 0;
