@@ -449,4 +449,36 @@ function ChainRulesCore.rrule(::typeof(hotpath_flux), hp::HotPath, T, ne, n_eff,
     y, hotpath_pullback
 end
 
+# Cotangent of one per-layer output of chemical_equilibrium as a Float64 vector (zeros if absent).
+_cotangent_vector(x, L) = (x = unthunk(x); x isa AbstractZero ? zeros(L) : collect(Float64, x))
+
+"""
+ChainRules rule for [`chemical_equilibrium`](@ref): the pullback takes the cotangents of the
+electron densities and of the species densities (a Dict species => per-layer values; absent
+species count as zero) to the temperatures, the total number densities and the absolute
+abundances through `korg_chemical_equilibrium_vjp`, the implicit-function rule the reference's
+ForwardDiff method applies (src/statmech.jl:307-355).  The model nₑ is the solver's starting
+guess and gets no tangent.
+"""
+function ChainRulesCore.rrule(::typeof(chemical_equilibrium), temps, nₜs, nₑs, absolute_abundances;
+                              molecules, ctx::Context=default_context())
+    y = chemical_equilibrium(temps, nₜs, nₑs, absolute_abundances; molecules=molecules, ctx=ctx)
+    function chemical_equilibrium_pullback(ȳ)
+        ȳ = unthunk(ȳ)
+        L = length(temps)
+        n̄e = _cotangent_vector(ȳ[1], L)
+        n̄d_in = unthunk(ȳ[2])
+        n̄d = Dict{Korg.Species,Vector{Float64}}()
+        if !(n̄d_in isa AbstractZero)
+            for (s, v) in pairs(n̄d_in)
+                n̄d[s] = _cotangent_vector(v, L)
+            end
+        end
+        T̄, n̄t, āb = chemical_equilibrium_vjp(temps, nₜs, nₑs, absolute_abundances, y, (n̄e, n̄d);
+                                             molecules=molecules, ctx=ctx)
+        (NoTangent(), T̄, n̄t, NoTangent(), vec(sum(āb; dims=2)))
+    end
+    y, chemical_equilibrium_pullback
+end
+
 end # module
