@@ -111,6 +111,20 @@ def test_vjp_mixed_close_to_fp64(ctx):
         assert err <= 2e-3, (k, err)
 
 
+def test_vjp_mixed_close_to_fp64_brackett(ctx):
+    """The mixed form's hydrogen-line reverse mode in the H band, where the Griem Brackett lines
+    take its FP32 branch (FP32 profiles and profile derivatives on the 201-point grid)."""
+    from korg_gb300.api import loss_and_gradient
+    inp = _case(n_lines=200, wl=(16790.0, 16830.0), seed=5)
+    obs = _obs(inp, ctx)
+    _, g64 = loss_and_gradient(inp, obs, precision="fp64", ctx=ctx)
+    _, g32 = loss_and_gradient(inp, obs, precision="mixed", ctx=ctx)
+    for k in ("T", "ne", "xi", "nH_I", "UH_I"):
+        err = np.max(np.abs(g32[k] - g64[k])) / np.max(np.abs(g64[k]))
+        assert err <= 2e-3, (k, err)
+    assert np.max(np.abs(g64["nH_I"])) > 0  # the Brackett lines are in reach
+
+
 # (wavelength range, MHD, checks (input, layer, relative step)): the inputs and layers whose loss
 # derivative stands well above the FP64 synthesis's rounding.  Deep layers, n(He I) (it only
 # enters the MHD occupation probabilities) and, in the H band, n(H I) and U(H I) change the loss
