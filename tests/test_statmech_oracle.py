@@ -209,3 +209,41 @@ def test_vjp_matches_solver_differences(so, tabs):
         am[Z - 1] *= 1 - h
         fa = (loss(solve(T, nt, ap)[1]) - loss(solve(T, nt, am)[1])) / (2 * h * ab[Z - 1])
         assert abs(dab[Z] - fa) <= 1e-5 * abs(fa), (Z, dab[Z], fa)
+
+
+def test_product_host_helpers_match_the_restatement(so, tabs):
+    """The package's host helpers mirroring src/statmech.jl:19-79 (saha_ion_weights,
+    translational_U, get_log_nK, Hminus_nK) equal the restatement's over temperatures, electron
+    densities, elements and molecules."""
+    from korg_gb300 import statmech as sm
+    from korg_gb300.constants import electron_mass_cgs
+    chi, pf, K = tabs
+    Ts = np.array([2500.0, 3500.0, 5777.0, 9000.0, 15000.0])
+    for T in Ts:
+        assert sm.translational_U(electron_mass_cgs, T) == pytest.approx(so.translational_U(electron_mass_cgs, T),
+                                                                         rel=1e-15)
+        assert sm.Hminus_nK(T) == pytest.approx(so.Hminus_nK(T), rel=1e-15)
+        for ne in (1e8, 1e12, 1e15):
+            for Z in (1, 2, 6, 8, 12, 14, 20, 26, 56, 92):
+                a, b = sm.saha_ion_weights(T, ne, Z, chi, pf), so.saha_ion_weights(T, ne, Z, chi, pf)
+                np.testing.assert_allclose(a, b, rtol=1e-15, atol=0)
+        for mol in list(K)[::17]:
+            assert sm.get_log_nK(mol, T, K) == pytest.approx(so.get_log_nK(mol, T, K), rel=1e-14, abs=1e-12)
+
+
+def test_equilibrium_tables_layout():
+    """The host table builder (korg_set_equilibrium_tables' input) on the package's data: 306
+    molecules, the densities layout n_e, (Z, charge 0..2) for Z = 1..92, H-, then the molecules."""
+    from korg_gb300 import _lib
+    from korg_gb300.species import Species, parse_species
+    from korg_gb300.statmech import default_equilibrium_tables
+    t = default_equilibrium_tables()
+    assert len(t.molecules) == 306
+    sp = t.species
+    assert len(sp) == _lib.KORG_CHEM_MOL0 + 306 and _lib.KORG_CHEM_MOL0 == 278
+    assert sp[0] is None
+    assert sp[1] == parse_species("H I") and sp[2] == parse_species("H II")
+    assert sp[1 + 3 * 25] == parse_species("Fe I") and sp[3 + 3 * 25] == parse_species("Fe III")
+    assert sp[277] == Species([1], -1)
+    assert list(sp[278:]) == list(t.molecules)
+    assert parse_species("CO") in t.molecules and parse_species("H2O") in t.molecules
