@@ -492,9 +492,16 @@ def atmosphere_gradient(inp: SynthesisInputs, g, ctx=None):
             gbar[:, col[s]] += v
     chT, dnt, dab = chemical_equilibrium_vjp(T, n_tot, ne_model, ab, dens, gbar, ctx=ctx)
     dT += chT
-    tot = dab.sum(axis=0)
-    dA = np.log(10.0) * ab * (tot - np.dot(ab, tot))
-    return {"T": dT, "n_tot": dnt, "A_X": dA, "vmic": phys["vmic"], "log_gf": phys["log_gf"]}
+    return {"T": dT, "n_tot": dnt, "A_X": abundance_vjp(ab, dab.sum(axis=0)), "vmic": phys["vmic"],
+            "log_gf": phys["log_gf"]}
+
+
+def abundance_vjp(ab, gbar_ab):
+    """Reverse mode of the normalisation ab = 10^(A(X) - 12) / sum (src/synthesize.jl:204-209):
+    the cotangent of the normalised abundances ``ab`` to dL/dA(X),
+    ln 10 ab_Z (gbar_Z - sum_Y ab_Y gbar_Y)."""
+    ab, gbar_ab = np.asarray(ab, np.float64), np.asarray(gbar_ab, np.float64)
+    return np.log(10.0) * ab * (gbar_ab - np.dot(ab, gbar_ab))
 
 
 def physical_gradient(inp: SynthesisInputs, g, vmic_scalar=True):

@@ -185,3 +185,25 @@ def test_continuum_layer_inputs_vjp_is_the_chain_rule():
             ad = np.asarray(dn.get(s, np.zeros(L)))[l]
             assert abs(ad - fd) <= 1e-6 * abs(fd) + 1e-12 * abs(gbar["n_Z1"][l]), (str(s), l, ad, fd)
     assert np.all(np.asarray(dn.get(parse_species("O I"), np.zeros(L))) == 0)
+
+
+def test_abundance_vjp_is_the_chain_rule():
+    """api.abundance_vjp, the last link of atmosphere_gradient: d/dA(X) of
+    sum(gbar * 10^(A - 12) / sum(10^(A - 12))) against central differences."""
+    from korg_gb300.api import abundance_vjp
+    rng = np.random.default_rng(4)
+    A = 12 + rng.uniform(-9, 0, 92)
+    A[0] = 12.0
+    gbar = rng.normal(size=92)
+    f = lambda A: float(np.dot(gbar, 10.0 ** (A - 12) / np.sum(10.0 ** (A - 12))))
+    ab = 10.0 ** (A - 12) / np.sum(10.0 ** (A - 12))
+    dA = abundance_vjp(ab, gbar)
+    def central(Z, h):
+        Ap, Am = A.copy(), A.copy()
+        Ap[Z - 1] += h
+        Am[Z - 1] -= h
+        return (f(Ap) - f(Am)) / (2 * h)
+
+    for Z in (1, 2, 6, 26, 92):
+        fd = (4 * central(Z, 5e-4) - central(Z, 1e-3)) / 3  # Richardson: truncation O(h^4)
+        assert abs(dA[Z - 1] - fd) <= 1e-6 * abs(fd) + 1e-13, (Z, dA[Z - 1], fd)
